@@ -1,0 +1,56 @@
+/*
+ * jn_gen.h — synthetic NCSM problem generator (Anicre-format stand-in).
+ *
+ * Writes a complete JupiterNCSM input directory (comb.txt, index lists,
+ * matrix-element blocks, evaluation order, Anicre basis files, bacchus.conf)
+ * for an harmonic-oscillator M-scheme basis with a seeded random M-scheme
+ * interaction.  All entry points return 0 on success or a JN_GEN_E* code;
+ * jn_gen_last_error() describes the last failure.
+ */
+#ifndef JN_GEN_H
+#define JN_GEN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { JN_GEN_OK = 0, JN_GEN_EINVAL = 1, JN_GEN_EIO = 2, JN_GEN_ENOMEM = 3 };
+
+typedef struct {
+	int Z, N;               /* protons, neutrons */
+	int Nmax;               /* excitation truncation in HO quanta */
+	int M2;                 /* total 2*M */
+	int parity;             /* 0 positive, 1 negative */
+	int nbody;              /* 2: two-body, 3: two- plus three-body */
+	uint64_t seed;
+	double hbar_omega;      /* MeV; 0 disables the oscillator term */
+	double sigma2, sigma3;  /* widths of the two- and three-body deviates (MeV) */
+	int me_only;            /* write only matrix-element blocks into me_subdir */
+	const char *me_subdir;  /* default "matrix_elements" */
+	int write_basis_files;  /* Anicre basis_energy_<E> files under anicr/ */
+	int lanczos_iterations; /* written into bacchus.conf */
+} jn_gen_config;
+
+typedef struct {
+	size_t dimension;
+	int num_basis_blocks;
+	size_t num_lists, list_entries;
+	size_t num_me_blocks, me_elements;
+	size_t num_calc_blocks;
+	unsigned long long multiplications;
+	int num_orbitals, num_proton_sds, num_neutron_sds;
+} jn_gen_summary;
+
+void jn_gen_default_config(jn_gen_config *cfg);
+int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *summary);
+const char *jn_gen_last_error(void);
+/* the seeded N(0,1) deviate attached to the unordered pair {ka, kb} */
+double jn_gen_pair_normal(uint64_t seed, uint64_t tag, uint64_t ka, uint64_t kb);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
