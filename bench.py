@@ -1,0 +1,297 @@
+"""Benchmark: index-list matvec GB/s on one GB300 (and N independent replicas).
+
+A step is one Hamiltonian product y = H x of the JupiterNCSM hot path on the
+workload below, with x, y, the index lists and the matrix elements already
+resident in HBM.  `value` is the algorithmic traffic of one product (index
+lists in the reference's 12-byte format, the matrix elements they reference,
+x read and y written) times the steps of all ranks, divided by the CUDA-event
+time of the slowest rank.  L2 is flushed (256 MiB write) between timed steps.
+
+`e2e` is the same metric through the public C ABI call jn_matvec with host
+buffers in pinned memory: host->device copy of x and y and device->host copy
+of y inside the timed region of every step.
+
+`--impl reference` times the reference's CPU algorithm (OpenMP task farm over
+the evaluation order with per-thread output replicas) on the host cores: the
+compiled reference where it was built on this machine, else the oracle's
+plain-C restatement of it.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # the A=4 configuration the matvec metric is quoted on: Nmax=6, two- plus three-body forces
+    "he4_nmax6_2nf3nf": dict(Z=2, N=2, nmax=6, nbody=3, M2=0,
+                             label="4He (Z=2,N=2) HO M-scheme Nmax=6, 2M=0, +parity, seeded 2NF N(0,1) + 3NF N(0,0.1) MeV, hw=20 MeV"),
+    "he4_nmax4_2nf": dict(Z=2, N=2, nmax=4, nbody=2, M2=0,
+                          label="4He (Z=2,N=2) HO M-scheme Nmax=4, 2M=0, +parity, seeded 2NF N(0,1) MeV, hw=20 MeV"),
+    "li6_nmax6_2nf": dict(Z=3, N=3, nmax=6, nbody=2, M2=2,
+                          label="6Li (Z=3,N=3) HO M-scheme Nmax=6, 2M=2, +parity, seeded 2NF N(0,1) MeV, hw=20 MeV"),
+}
+METRIC = "index-list matvec GB/s vs HBM peak"
+FLUSH_BYTES = 256 << 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def profile_traffic(workload):
+    """dram bytes per launch of the gather kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"matvec_units_kernel_{workload}.md")
+    try:
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=fd, stderr=subprocess.DEVNULL)
+            os.close(fd)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            w = [x.strip() for x in line.split(",")]
+            if len(w) >= 9:
+                rows.append(w)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def prepare(workload, workdir):
+    import jupiterncsm_gb300 as jn
+    w = WORKLOADS[workload]
+    d = os.path.join(workdir, workload)
+    stamp = os.path.join(d, ".complete")
+    if not os.path.exists(stamp):
+        t = time.time()
+        jn.generate(d, Z=w["Z"], N=w["N"], nmax=w["nmax"], nbody=w["nbody"], M2=w["M2"], basis_files=False)
+        open(stamp, "w").write("ok\n")
+        log(f"generated {workload} in {time.time() - t:.1f} s")
+    return d
+
+
+def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
+    """The reference's CPU algorithm on all host threads over a time-bounded sample."""
+    import numpy as np
+    import oracle
+    threads = os.cpu_count() or 1
+    kind = "port"
+    impl = None
+    if oracle.reference_available():
+        try:
+            impl = oracle.Reference(d, w["Z"], w["N"], threads=threads)
+            kind = "reference"
+        except OSError:
+            impl = None
+    if impl is None:
+        impl = oracle.Port(d)
+    D = impl.dimension
+    x = np.random.default_rng(1).standard_normal(D)
+    y = np.zeros(D)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while len(times) < min_steps or time.perf_counter() < t_end:
+        if kind == "reference":
+            impl.matvec(x, y)
+            times.append(impl.seconds)
+        else:
+            times.append(impl.matvec_omp(x, y, threads))
+    impl.close()
+    per = sum(times) / len(times)
+    return {"value": bytes_per_step / per / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
+            "sample": f"{len(times)} full products of the workload ({sum(times):.1f} s of CPU work), "
+                      f"OpenMP task farm with per-thread replicas, {threads} threads",
+            "ms_per_step": per * 1e3}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="he4_nmax6_2nf3nf", choices=sorted(WORKLOADS))
+    ap.add_argument("--workdir", default=os.environ.get("JNCSM_BENCH_DIR", os.path.join(tempfile.gettempdir(), "jncsm_bench")))
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import jupiterncsm_gb300 as jn
+        d = prepare(args.workload, args.workdir)
+        stats = algorithmic_stats(d, w)
+        cb = cpu_baseline(d, w, stats["bytes"], seconds=args.cpu_seconds)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": w["label"], "dimension": stats["dimension"], "threads": cb["cores"]},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import numpy as np
+    import jupiterncsm_gb300 as jn
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    wd = os.path.join(args.workdir, f"rank{rank}") if world > 1 else args.workdir
+    d = prepare(args.workload, wd)
+    H = jn.Hamiltonian.from_dir(d, w["Z"], w["N"])
+    st = H.stats()
+    D = H.dimension
+    bytes_step = st["algorithmic_bytes"]
+    dev = torch.device("cuda", local)
+    x = torch.randn(D, dtype=torch.float64, device=dev)
+    y = torch.zeros(D, dtype=torch.float64, device=dev)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        flush.zero_()
+        torch.cuda.synchronize()
+        return H.matvec_profile(x.data_ptr(), y.data_ptr(), accumulate=False)
+
+    for _ in range(args.warmup):
+        step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    units_ms, total_ms = 0.0, 0.0
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        a, b = step()
+        units_ms += a
+        total_ms += a + b
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    t_max = total_ms
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = bytes_step * args.steps * world / (t_max / 1e3) / 1e9
+
+    # end to end through the public host-pointer call, pinned host buffers
+    hx = torch.randn(D, dtype=torch.float64).pin_memory().numpy()
+    hy = torch.zeros(D, dtype=torch.float64).pin_memory().numpy()
+    for _ in range(args.warmup):
+        H.matvec(hx, hy)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        H.matvec(hx, hy)
+        e2e_s += time.perf_counter() - t0
+    e2e_value = bytes_step * args.steps * world / e2e_s / 1e9
+
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = bytes_step / (units_ms / args.steps / 1e3) / 1e9
+    traffic = profile_traffic(args.workload)
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["label"], "dimension": D, "instructions": st["num_instructions"],
+                       "list_entries": st["list_entries"], "me_elements": st["me_elements"],
+                       "me_elements_referenced": st["me_referenced"],
+                       "multiply_adds": st["multiply_adds"], "bytes_per_step": bytes_step,
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
+                       "wall_s": wall},
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * D, "d2h_bytes_per_step": 8 * D},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
+                         "kernel": "jn_units_kernel"},
+            "clocks": clocks}
+    if rank == 0:
+        try:
+            line["cpu_baseline"] = cpu_baseline(d, w, bytes_step, seconds=args.cpu_seconds)
+        except Exception as e:  # the baseline must never hide the GPU line
+            line["cpu_baseline"] = {"error": str(e)}
+        print(json.dumps(line), flush=True)
+    H.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def algorithmic_stats(d, w):
+    """Bytes per product from the plan statistics, computed on the host (no GPU needed)."""
+    import jupiterncsm_gb300 as jn
+    st = jn.inspect(d, w["Z"], w["N"])
+    return {"bytes": st["algorithmic_bytes"], "dimension": st["dimension"]}
+
+
+if __name__ == "__main__":
+    main()

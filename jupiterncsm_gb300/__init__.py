@@ -1,0 +1,222 @@
+"""jupiterncsm_gb300 — GB300-native hot path of JupiterNCSM.
+
+The product is the C ABI in ``include/jncsm.h`` implemented by
+``lib/libjncsm_gpu.so`` (sm_103a CUDA kernels).  This module is a thin ctypes
+binding used by the tests and the benchmark; it adds no computation of its
+own and fails loudly when the native library is missing.
+
+Reference interfaces mirrored (paths relative to the reference src/ tree):
+``run_matrix_vector_multiplication`` (Minerva/scheduler/scheduler.c:80-145),
+``new_combination_table`` (Utilities/combination_table/combination_table.c:83-137),
+``read_evaluation_order`` (Minerva/evaluation_order/evaluation_order.c:43-112).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIBDIR = os.path.join(HERE, "lib")
+GPU_LIB = os.path.join(LIBDIR, "libjncsm_gpu.so")
+GEN_LIB = os.path.join(LIBDIR, "libjncsm_gen.so")
+GEN_CLI = os.path.join(LIBDIR, "jn_gen")
+
+JN_OK = 0
+STATUS_NAMES = {0: "JN_OK", 1: "JN_ERR_INVALID", 2: "JN_ERR_IO", 3: "JN_ERR_FORMAT", 4: "JN_ERR_CUDA",
+                5: "JN_ERR_NOMEM", 6: "JN_ERR_NOT_CONVERGED", 7: "JN_ERR_TIMEOUT"}
+
+
+class JnError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def build(jobs=8):
+    """Compile the native libraries in-tree (nvcc for sm_103a, gcc for host C)."""
+    subprocess.run(["make", "-s", f"-j{jobs}", "-C", os.path.join(HERE, "csrc")], check=True)
+
+
+class PlanStats(ctypes.Structure):
+    _fields_ = [("dimension", ctypes.c_size_t), ("num_blocks", ctypes.c_int), ("num_instructions", ctypes.c_int),
+                ("list_entries", ctypes.c_size_t), ("me_elements", ctypes.c_size_t),
+                ("me_referenced", ctypes.c_size_t), ("multiply_adds", ctypes.c_double), ("algorithmic_bytes", ctypes.c_double),
+                ("num_work_units", ctypes.c_int), ("num_tiles", ctypes.c_int)]
+
+
+_gpu = None
+
+
+def gpu_lib():
+    """Load libjncsm_gpu.so with the prototypes of include/jncsm.h."""
+    global _gpu
+    if _gpu is not None:
+        return _gpu
+    if not os.path.exists(GPU_LIB):
+        raise JnError(4, f"native library {GPU_LIB} is missing: run jupiterncsm_gb300.build()")
+    L = ctypes.CDLL(GPU_LIB)
+    vp, cp, ci, csz = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_size_t
+    L.jn_last_error.restype = cp
+    L.jn_version.restype = cp
+    L.jn_open.argtypes = [cp, ctypes.POINTER(vp)]
+    L.jn_open_files.argtypes = [cp, cp, cp, cp, ci, ci, ctypes.POINTER(vp)]
+    L.jn_close.argtypes = [vp]
+    L.jn_close.restype = None
+    L.jn_dimension.argtypes = [vp]
+    L.jn_dimension.restype = csz
+    L.jn_num_blocks.argtypes = [vp]
+    L.jn_block_info.argtypes = [vp, ci, ctypes.POINTER(ci), ctypes.POINTER(csz), ctypes.POINTER(csz)]
+    L.jn_matvec.argtypes = [vp, vp, vp]
+    L.jn_matvec_device.argtypes = [vp, vp, vp, ci, vp]
+    L.jn_matvec_files.argtypes = [vp, cp, cp]
+    L.jn_synchronize.argtypes = [vp]
+    L.jn_matvec_profile.argtypes = [vp, vp, vp, ci, ctypes.POINTER(ctypes.c_float)]
+    L.jn_get_plan_stats.argtypes = [vp, ctypes.POINTER(PlanStats)]
+    L.jn_inspect_files.argtypes = [cp, cp, cp, cp, ci, ci, ctypes.POINTER(PlanStats)]
+    for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
+                 "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files"):
+        getattr(L, name).restype = ci
+    _gpu = L
+    return L
+
+
+def _check(status):
+    if status != JN_OK:
+        raise JnError(status, gpu_lib().jn_last_error().decode(errors="replace"))
+
+
+class Hamiltonian:
+    """An opened Hamiltonian: index lists and matrix elements resident in HBM."""
+
+    def __init__(self, conf=None, *, comb=None, order=None, lists=None, mes=None, Z=None, N=None):
+        L = gpu_lib()
+        h = ctypes.c_void_p()
+        if conf is not None:
+            _check(L.jn_open(conf.encode(), ctypes.byref(h)))
+        else:
+            _check(L.jn_open_files(comb.encode(), order.encode(), lists.encode(), mes.encode(), int(Z), int(N),
+                                   ctypes.byref(h)))
+        self._h = h
+        self.dimension = L.jn_dimension(h)
+
+    @classmethod
+    def from_dir(cls, d, Z, N):
+        return cls(comb=f"{d}/comb.txt", order=f"{d}/evaluation_order.txt", lists=f"{d}/index_lists",
+                   mes=f"{d}/matrix_elements", Z=Z, N=N)
+
+    def close(self):
+        if self._h:
+            gpu_lib().jn_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def matvec(self, x, y=None):
+        """y += H x on host arrays (y = H x when y is None)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (self.dimension,):
+            raise ValueError("x has the wrong dimension")
+        y = np.zeros(self.dimension) if y is None else y
+        if y.dtype != np.float64 or not y.flags.c_contiguous or y.shape != x.shape:
+            raise ValueError("y must be a contiguous float64 vector of the same dimension")
+        _check(gpu_lib().jn_matvec(self._h, x.ctypes.data, y.ctypes.data))
+        return y
+
+    def matvec_device(self, d_x, d_y, accumulate=False, stream=0):
+        _check(gpu_lib().jn_matvec_device(self._h, ctypes.c_void_p(d_x), ctypes.c_void_p(d_y), int(accumulate),
+                                          ctypes.c_void_p(stream)))
+
+    def matvec_profile(self, d_x, d_y, accumulate=False):
+        """Device product on the context stream; returns (ms gather kernel, ms reduction kernel)."""
+        ms = (ctypes.c_float * 2)()
+        _check(gpu_lib().jn_matvec_profile(self._h, ctypes.c_void_p(d_x), ctypes.c_void_p(d_y), int(accumulate), ms))
+        return ms[0], ms[1]
+
+    def matvec_files(self, out_dir, in_dir):
+        _check(gpu_lib().jn_matvec_files(self._h, out_dir.encode(), in_dir.encode()))
+
+    def synchronize(self):
+        _check(gpu_lib().jn_synchronize(self._h))
+
+    def stats(self):
+        s = PlanStats()
+        _check(gpu_lib().jn_get_plan_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in PlanStats._fields_}
+
+    def blocks(self):
+        L = gpu_lib()
+        out = []
+        for b in range(L.jn_num_blocks(self._h)):
+            i, o, n = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
+            _check(L.jn_block_info(self._h, b, ctypes.byref(i), ctypes.byref(o), ctypes.byref(n)))
+            out.append((i.value, o.value, n.value))
+        return out
+
+
+def inspect(d, Z, N):
+    """Plan statistics of a problem directory, computed on the host (no GPU)."""
+    s = PlanStats()
+    e = lambda t: t.encode()
+    _check(gpu_lib().jn_inspect_files(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                                      e(f"{d}/matrix_elements"), int(Z), int(N), ctypes.byref(s)))
+    return {k: getattr(s, k) for k, _ in PlanStats._fields_}
+
+
+# ---------------------------------------------------------------- generator
+class GenConfig(ctypes.Structure):
+    _fields_ = [("Z", ctypes.c_int), ("N", ctypes.c_int), ("Nmax", ctypes.c_int), ("M2", ctypes.c_int),
+                ("parity", ctypes.c_int), ("nbody", ctypes.c_int), ("seed", ctypes.c_uint64),
+                ("hbar_omega", ctypes.c_double), ("sigma2", ctypes.c_double), ("sigma3", ctypes.c_double),
+                ("me_only", ctypes.c_int), ("me_subdir", ctypes.c_char_p), ("write_basis_files", ctypes.c_int),
+                ("lanczos_iterations", ctypes.c_int)]
+
+
+class GenSummary(ctypes.Structure):
+    _fields_ = [("dimension", ctypes.c_size_t), ("num_basis_blocks", ctypes.c_int), ("num_lists", ctypes.c_size_t),
+                ("list_entries", ctypes.c_size_t), ("num_me_blocks", ctypes.c_size_t),
+                ("me_elements", ctypes.c_size_t), ("num_calc_blocks", ctypes.c_size_t),
+                ("multiplications", ctypes.c_ulonglong), ("num_orbitals", ctypes.c_int),
+                ("num_proton_sds", ctypes.c_int), ("num_neutron_sds", ctypes.c_int)]
+
+
+_gen = None
+
+
+def gen_lib():
+    global _gen
+    if _gen is None:
+        if not os.path.exists(GEN_LIB):
+            raise JnError(2, f"{GEN_LIB} is missing: run jupiterncsm_gb300.build()")
+        _gen = ctypes.CDLL(GEN_LIB)
+        _gen.jn_generate.argtypes = [ctypes.POINTER(GenConfig), ctypes.c_char_p, ctypes.POINTER(GenSummary)]
+        _gen.jn_gen_last_error.restype = ctypes.c_char_p
+        _gen.jn_gen_default_config.argtypes = [ctypes.POINTER(GenConfig)]
+        _gen.jn_gen_pair_normal.restype = ctypes.c_double
+        _gen.jn_gen_pair_normal.argtypes = [ctypes.c_uint64] * 4
+    return _gen
+
+
+def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, hbar_omega=20.0, sigma2=1.0,
+             sigma3=0.1, me_only_subdir=None, basis_files=True, lanczos_iterations=200):
+    """Write a synthetic problem in the reference formats; returns the generator summary."""
+    G = gen_lib()
+    c = GenConfig()
+    G.jn_gen_default_config(ctypes.byref(c))
+    c.Z, c.N, c.Nmax, c.M2, c.parity, c.nbody = Z, N, nmax, M2, parity, nbody
+    c.seed, c.hbar_omega, c.sigma2, c.sigma3 = seed, hbar_omega, sigma2, sigma3
+    c.write_basis_files = int(basis_files)
+    c.lanczos_iterations = lanczos_iterations
+    if me_only_subdir:
+        c.me_only = 1
+        c.me_subdir = me_only_subdir.encode()
+    s = GenSummary()
+    rc = G.jn_generate(ctypes.byref(c), outdir.encode(), ctypes.byref(s))
+    if rc != 0:
+        raise JnError(rc, G.jn_gen_last_error().decode())
+    return {k: getattr(s, k) for k, _ in GenSummary._fields_}

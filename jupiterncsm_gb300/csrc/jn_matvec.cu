@@ -1,0 +1,427 @@
+/*
+ * jn_matvec.cu — sm_103a kernels for the index-list block matrix-vector
+ * product and the C ABI around them (include/jncsm.h).
+ *
+ * Semantics are the reference Minerva kernels'
+ * (src/Minerva/matrix_vector_multiplication/matrix_vector_multiplication.c):
+ *   neutron list  y[n_o + Nn p] += s M[k] x[n_i + Nn p]       (:20-77)
+ *   proton list   y[Nn p_o + n] += s M[k] x[Nn p_i + n]       (:79-132)
+ *   n x p lists   y[n_o + Nn_o p_o] += s_n s_p M[k_n + Nd k_p] x[n_i + Nn_i p_i]   (:134-210)
+ *   off-diagonal instructions also apply the transpose into the input block
+ *   (:212-462); single-species terms skip |M| < 1e-12 (:52-53, 107-108).
+ *
+ * GB300 organisation (see jn_problem.h): the host plan turns every
+ * instruction into terms owned by their destination block; destination
+ * blocks are cut into tiles of at most 512 elements; the terms of a tile are
+ * cut into chunks of similar work.  One CTA computes one (tile, chunk):
+ * every output element is owned by one thread (or a fixed group of threads
+ * reduced in fixed order through shared memory), which walks the CSR rows
+ * of the lists in list order.  Partial sums land in a scratch array and the
+ * reduction pass adds them in chunk order, so no atomics are used and the
+ * result is bit-identical from run to run.
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include "../../include/jncsm.h"
+#include "jn_problem.h"
+
+#define JN_VERSION "jncsm-gb300 0.1"
+
+static thread_local char g_last_error[1024];
+
+static jn_status fail(jn_status s, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
+	va_end(ap);
+	return s;
+}
+
+#define CUDA_TRY(call)                                                                       \
+	do {                                                                                 \
+		cudaError_t e_ = (call);                                                     \
+		if (e_ != cudaSuccess)                                                       \
+			return fail(JN_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+	} while (0)
+
+extern "C" const char *jn_last_error(void) { return g_last_error; }
+extern "C" const char *jn_version(void) { return JN_VERSION; }
+
+struct jn_ctx {
+	jn_plan_t plan;
+	int device;
+	cudaStream_t stream;
+	uint32_t *d_rowptr;
+	uint2 *d_ent;
+	double *d_me;
+	jn_term_t *d_terms;
+	jn_tile_t *d_tiles;
+	jn_unit_t *d_units;
+	int32_t *d_unit_terms;
+	double *d_partial;
+	double *d_x, *d_y;      /* staging for the host-pointer entry points */
+	double *h_pinned;       /* pinned staging for host copies */
+};
+
+/* ------------------------------------------------------------------ */
+/* kernels                                                             */
+/* ------------------------------------------------------------------ */
+#define THREADS 256
+#define MASK31 0x7fffffffu
+
+struct DevPlan {
+	const uint32_t *__restrict__ rowptr;
+	const uint2 *__restrict__ ent;
+	const double *__restrict__ me;
+	const jn_term_t *__restrict__ terms;
+	const jn_tile_t *__restrict__ tiles;
+	const jn_unit_t *__restrict__ units;
+	const int32_t *__restrict__ unit_terms;
+};
+
+__device__ __forceinline__ double signed_me(const double *__restrict__ me, uint32_t mi)
+{
+	double m = __ldg(me + (mi & MASK31));
+	return (mi & 0x80000000u) ? -m : m;
+}
+
+/* contribution of one term to element (p, n) of its destination block */
+__device__ __forceinline__ double term_element(const DevPlan &P, const jn_term_t &t, const double *__restrict__ x,
+					       int p, int n)
+{
+	const double *__restrict__ xs = x + t.src_off;
+	const double *__restrict__ me = P.me + t.me_off;
+	double acc = 0.0;
+	if (t.kind == JN_KIND_P) {
+		uint32_t j0 = __ldg(P.rowptr + t.p_ptr + p), j1 = __ldg(P.rowptr + t.p_ptr + p + 1);
+		for (uint32_t j = j0; j < j1; j++) {
+			uint2 e = __ldg(P.ent + j);
+			double m = __ldg(me + (e.y & MASK31));
+			if (fabs(m) < 1e-12) continue;
+			if (e.y & 0x80000000u) m = -m;
+			acc = fma(m, __ldg(xs + (size_t)e.x * t.Nn_src + n), acc);
+		}
+	} else if (t.kind == JN_KIND_N) {
+		uint32_t j0 = __ldg(P.rowptr + t.n_ptr + n), j1 = __ldg(P.rowptr + t.n_ptr + n + 1);
+		const double *__restrict__ xrow = xs + (size_t)p * t.Nn_src;
+		for (uint32_t j = j0; j < j1; j++) {
+			uint2 e = __ldg(P.ent + j);
+			double m = __ldg(me + (e.y & MASK31));
+			if (fabs(m) < 1e-12) continue;
+			if (e.y & 0x80000000u) m = -m;
+			acc = fma(m, __ldg(xrow + e.x), acc);
+		}
+	} else {
+		uint32_t i0 = __ldg(P.rowptr + t.p_ptr + p), i1 = __ldg(P.rowptr + t.p_ptr + p + 1);
+		uint32_t j0 = __ldg(P.rowptr + t.n_ptr + n), j1 = __ldg(P.rowptr + t.n_ptr + n + 1);
+		if (j0 == j1) return 0.0;
+		for (uint32_t i = i0; i < i1; i++) {
+			uint2 ep = __ldg(P.ent + i);
+			const double *__restrict__ mrow = me + (size_t)t.nd * (ep.y & MASK31);
+			const double *__restrict__ xrow = xs + (size_t)ep.x * t.Nn_src;
+			double inner = 0.0;
+			for (uint32_t j = j0; j < j1; j++) {
+				uint2 en = __ldg(P.ent + j);
+				double m = __ldg(mrow + (en.y & MASK31));
+				if (en.y & 0x80000000u) m = -m;
+				inner = fma(m, __ldg(xrow + en.x), inner);
+			}
+			acc += (ep.y & 0x80000000u) ? -inner : inner;
+		}
+	}
+	return acc;
+}
+
+__global__ void __launch_bounds__(THREADS) jn_units_kernel(DevPlan P, const double *__restrict__ x,
+							   double *__restrict__ partial)
+{
+	__shared__ double red[THREADS];
+	const jn_unit_t u = P.units[blockIdx.x];
+	const jn_tile_t tile = P.tiles[u.tile];
+	const int E = tile.nrows * tile.ncols;
+	int EP = 1;
+	while (EP < E) EP <<= 1;
+	const int tid = threadIdx.x;
+	double *out = partial + tile.partial + (int64_t)u.chunk * E;
+	if (EP <= THREADS) {
+		/* G groups of threads share each element; group g takes terms g, g+G, ... */
+		const int G = THREADS / EP;
+		const int g = tid / EP, e = tid % EP;
+		double acc = 0.0;
+		if (e < E) {
+			const int p = tile.row0 + e / tile.ncols, n = tile.col0 + e % tile.ncols;
+			for (int64_t q = u.t0 + g; q < u.t1; q += G) {
+				const jn_term_t t = P.terms[P.unit_terms[q]];
+				acc += term_element(P, t, x, p, n);
+			}
+		}
+		red[tid] = acc;
+		__syncthreads();
+		if (g == 0 && e < E) {
+			double s = red[e];
+			for (int h = 1; h < G; h++) s += red[h * EP + e];
+			out[e] = s;
+		}
+	} else {
+		for (int e = tid; e < E; e += THREADS) {
+			const int p = tile.row0 + e / tile.ncols, n = tile.col0 + e % tile.ncols;
+			double acc = 0.0;
+			for (int64_t q = u.t0; q < u.t1; q++) {
+				const jn_term_t t = P.terms[P.unit_terms[q]];
+				acc += term_element(P, t, x, p, n);
+			}
+			out[e] = acc;
+		}
+	}
+}
+
+__global__ void __launch_bounds__(THREADS) jn_reduce_kernel(const jn_tile_t *__restrict__ tiles,
+							    const double *__restrict__ partial,
+							    double *__restrict__ y, int accumulate)
+{
+	const jn_tile_t t = tiles[blockIdx.x];
+	const int E = t.nrows * t.ncols;
+	for (int e = threadIdx.x; e < E; e += blockDim.x) {
+		double s = 0.0;
+		for (int c = 0; c < t.nchunks; c++) s += partial[t.partial + (int64_t)c * E + e];
+		const int64_t at = t.dst_off + (int64_t)(t.row0 + e / t.ncols) * t.Nn + t.col0 + e % t.ncols;
+		y[at] = accumulate ? y[at] + s : s;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* host side                                                           */
+/* ------------------------------------------------------------------ */
+template <typename T>
+static jn_status upload(T **dst, const void *src, size_t n)
+{
+	size_t bytes = (n ? n : 1) * sizeof(T);
+	cudaError_t e = cudaMalloc((void **)dst, bytes);
+	if (e != cudaSuccess) return fail(JN_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+	if (n && src) {
+		e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+		if (e != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemcpy failed: %s", cudaGetErrorString(e));
+	}
+	return JN_OK;
+}
+
+extern "C" void jn_close(jn_ctx *c)
+{
+	if (!c) return;
+	cudaFree(c->d_rowptr); cudaFree(c->d_ent); cudaFree(c->d_me); cudaFree(c->d_terms);
+	cudaFree(c->d_tiles); cudaFree(c->d_units); cudaFree(c->d_unit_terms); cudaFree(c->d_partial);
+	cudaFree(c->d_x); cudaFree(c->d_y);
+	if (c->h_pinned) cudaFreeHost(c->h_pinned);
+	if (c->stream) cudaStreamDestroy(c->stream);
+	jn_plan_free(&c->plan);
+	free(c);
+}
+
+extern "C" jn_status jn_open_files(const char *comb, const char *order, const char *lists_dir, const char *me_dir,
+				   int Z, int N, jn_ctx **out)
+{
+	if (!comb || !order || !lists_dir || !me_dir || !out) return fail(JN_ERR_INVALID, "null argument");
+	*out = NULL;
+	int ndev = 0;
+	cudaError_t ce = cudaGetDeviceCount(&ndev);
+	if (ce != cudaSuccess || ndev == 0)
+		return fail(JN_ERR_CUDA, "no usable CUDA device (%s)", ce == cudaSuccess ? "0 devices" : cudaGetErrorString(ce));
+	jn_ctx *c = (jn_ctx *)calloc(1, sizeof *c);
+	char err[1024] = { 0 };
+	int sms = 0;
+	CUDA_TRY(cudaGetDevice(&c->device));
+	CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+	if (jn_plan_build(&c->plan, comb, order, lists_dir, me_dir, Z, N, sms * 8, err, sizeof err)) {
+		free(c);
+		int io = strstr(err, "open") != NULL;
+		return fail(io ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
+	}
+	jn_plan_t *p = &c->plan;
+	jn_status s;
+	if ((s = upload(&c->d_rowptr, p->rowptr, p->n_rowptr)) ||
+	    (s = upload(&c->d_ent, p->ent, p->n_ent)) ||
+	    (s = upload(&c->d_me, p->me, p->n_me)) ||
+	    (s = upload(&c->d_terms, p->terms, p->nterms)) ||
+	    (s = upload(&c->d_tiles, p->tiles, p->ntiles)) ||
+	    (s = upload(&c->d_units, p->units, p->nunits)) ||
+	    (s = upload(&c->d_unit_terms, p->unit_terms, p->n_unit_terms)) ||
+	    (s = upload(&c->d_partial, (const void *)NULL, p->n_partial)) ||
+	    (s = upload(&c->d_x, (const void *)NULL, p->dim)) ||
+	    (s = upload(&c->d_y, (const void *)NULL, p->dim))) {
+		jn_close(c);
+		return s;
+	}
+	/* host copies of the lists are no longer needed on the product path */
+	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+	if (e != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+	e = cudaMallocHost((void **)&c->h_pinned, (p->dim ? p->dim : 1) * sizeof(double));
+	if (e != cudaSuccess) { jn_close(c); return fail(JN_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)); }
+	*out = c;
+	return JN_OK;
+}
+
+extern "C" jn_status jn_open(const char *conf, jn_ctx **out)
+{
+	jn_runfile_t rf;
+	char err[1024] = { 0 };
+	if (!conf || !out) return fail(JN_ERR_INVALID, "null argument");
+	if (jn_read_runfile(conf, &rf, err, sizeof err)) return fail(JN_ERR_FORMAT, "%s", err);
+	return jn_open_files(rf.comb, rf.order, rf.lists, rf.mes, rf.Z, rf.N, out);
+}
+
+extern "C" size_t jn_dimension(const jn_ctx *c) { return c ? (size_t)c->plan.dim : 0; }
+extern "C" int jn_num_blocks(const jn_ctx *c) { return c ? c->plan.nblocks : 0; }
+
+extern "C" jn_status jn_block_info(const jn_ctx *c, int b, int *id, size_t *offset, size_t *length)
+{
+	if (!c || b < 0 || b >= c->plan.nblocks) return fail(JN_ERR_INVALID, "block index out of range");
+	const jn_block_t *B = &c->plan.blocks[b];
+	if (id) *id = B->id;
+	if (offset) *offset = (size_t)B->offset;
+	if (length) *length = (size_t)(B->Np * B->Nn);
+	return JN_OK;
+}
+
+static jn_status launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st)
+{
+	const jn_plan_t *p = &c->plan;
+	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
+	if (p->nunits > 0) jn_units_kernel<<<p->nunits, THREADS, 0, st>>>(P, d_x, c->d_partial);
+	if (p->ntiles > 0) jn_reduce_kernel<<<p->ntiles, THREADS, 0, st>>>(c->d_tiles, c->d_partial, d_y, accumulate);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+extern "C" jn_status jn_matvec_device(jn_ctx *c, const double *d_x, double *d_y, int accumulate, void *stream)
+{
+	if (!c || !d_x || !d_y) return fail(JN_ERR_INVALID, "null argument");
+	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
+	return launch_matvec(c, d_x, d_y, accumulate, stream ? (cudaStream_t)stream : c->stream);
+}
+
+extern "C" jn_status jn_matvec_profile(jn_ctx *c, const double *d_x, double *d_y, int accumulate, float ms[2])
+{
+	if (!c || !d_x || !d_y || !ms) return fail(JN_ERR_INVALID, "null argument");
+	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
+	const jn_plan_t *p = &c->plan;
+	cudaEvent_t ev[3];
+	for (int i = 0; i < 3; i++) CUDA_TRY(cudaEventCreate(&ev[i]));
+	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
+	CUDA_TRY(cudaEventRecord(ev[0], c->stream));
+	if (p->nunits > 0) jn_units_kernel<<<p->nunits, THREADS, 0, c->stream>>>(P, d_x, c->d_partial);
+	CUDA_TRY(cudaEventRecord(ev[1], c->stream));
+	if (p->ntiles > 0) jn_reduce_kernel<<<p->ntiles, THREADS, 0, c->stream>>>(c->d_tiles, c->d_partial, d_y, accumulate);
+	CUDA_TRY(cudaEventRecord(ev[2], c->stream));
+	CUDA_TRY(cudaGetLastError());
+	CUDA_TRY(cudaEventSynchronize(ev[2]));
+	CUDA_TRY(cudaEventElapsedTime(&ms[0], ev[0], ev[1]));
+	CUDA_TRY(cudaEventElapsedTime(&ms[1], ev[1], ev[2]));
+	for (int i = 0; i < 3; i++) cudaEventDestroy(ev[i]);
+	return JN_OK;
+}
+
+extern "C" jn_status jn_matvec(jn_ctx *c, const double *x, double *y)
+{
+	if (!c || !x || !y) return fail(JN_ERR_INVALID, "null argument");
+	const size_t bytes = (size_t)c->plan.dim * sizeof(double);
+	CUDA_TRY(cudaMemcpyAsync(c->d_x, x, bytes, cudaMemcpyHostToDevice, c->stream));
+	CUDA_TRY(cudaMemcpyAsync(c->d_y, y, bytes, cudaMemcpyHostToDevice, c->stream));
+	jn_status s = launch_matvec(c, c->d_x, c->d_y, 1, c->stream);
+	if (s) return s;
+	CUDA_TRY(cudaMemcpyAsync(y, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
+	CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return JN_OK;
+}
+
+extern "C" jn_status jn_synchronize(jn_ctx *c)
+{
+	if (!c) return fail(JN_ERR_INVALID, "null argument");
+	CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return JN_OK;
+}
+
+static jn_status read_vec_file(const char *dir, int id, double *dst, size_t n)
+{
+	char path[8192];
+	snprintf(path, sizeof path, "%s/vec_%d", dir, id);
+	FILE *f = fopen(path, "rb");
+	if (!f) return fail(JN_ERR_IO, "Could not open vector block file %s", path);
+	size_t got = fread(dst, sizeof(double), n, f);
+	fclose(f);
+	if (got != n) return fail(JN_ERR_IO, "Could not read elements of block %d in %s", id, dir);
+	return JN_OK;
+}
+
+extern "C" jn_status jn_matvec_files(jn_ctx *c, const char *out_dir, const char *in_dir)
+{
+	if (!c || !out_dir || !in_dir) return fail(JN_ERR_INVALID, "null argument");
+	const jn_plan_t *p = &c->plan;
+	double *x = (double *)malloc((p->dim ? p->dim : 1) * sizeof(double));
+	double *y = (double *)malloc((p->dim ? p->dim : 1) * sizeof(double));
+	jn_status s = JN_OK;
+	if (!x || !y) { s = fail(JN_ERR_NOMEM, "out of host memory"); goto done; }
+	for (int b = 0; b < p->nblocks && !s; b++) {
+		const jn_block_t *B = &p->blocks[b];
+		size_t n = (size_t)(B->Np * B->Nn);
+		s = read_vec_file(in_dir, B->id, x + B->offset, n);
+		if (!s) s = read_vec_file(out_dir, B->id, y + B->offset, n);
+	}
+	if (!s) s = jn_matvec(c, x, y);
+	for (int b = 0; b < p->nblocks && !s; b++) {
+		const jn_block_t *B = &p->blocks[b];
+		size_t n = (size_t)(B->Np * B->Nn);
+		char path[8192];
+		snprintf(path, sizeof path, "%s/vec_%d", out_dir, B->id);
+		FILE *f = fopen(path, "wb");
+		if (!f) { s = fail(JN_ERR_IO, "Could not open vector block file %s", path); break; }
+		if (fwrite(y + B->offset, sizeof(double), n, f) != n) s = fail(JN_ERR_IO, "Could not write elements to block %d in %s", B->id, out_dir);
+		fclose(f);
+	}
+done:
+	free(x); free(y);
+	return s;
+}
+
+static void fill_stats(const jn_plan_t *p, jn_plan_stats *st)
+{
+	memset(st, 0, sizeof *st);
+	st->dimension = (size_t)p->dim;
+	st->num_blocks = p->nblocks;
+	st->num_instructions = p->ninstr;
+	st->list_entries = (size_t)p->list_entries;
+	st->me_elements = (size_t)p->me_elements;
+	st->me_referenced = (size_t)p->me_referenced;
+	st->multiply_adds = p->visits;
+	st->algorithmic_bytes = 12.0 * (double)p->list_entries + 8.0 * (double)p->me_referenced + 16.0 * (double)p->dim;
+	st->num_work_units = p->nunits;
+	st->num_tiles = p->ntiles;
+}
+
+extern "C" jn_status jn_get_plan_stats(const jn_ctx *c, jn_plan_stats *st)
+{
+	if (!c || !st) return fail(JN_ERR_INVALID, "null argument");
+	fill_stats(&c->plan, st);
+	return JN_OK;
+}
+
+extern "C" jn_status jn_inspect_files(const char *comb, const char *order, const char *lists_dir, const char *me_dir,
+				      int Z, int N, jn_plan_stats *st)
+{
+	if (!comb || !order || !lists_dir || !me_dir || !st) return fail(JN_ERR_INVALID, "null argument");
+	jn_plan_t plan;
+	char err[1024] = { 0 };
+	if (jn_plan_build(&plan, comb, order, lists_dir, me_dir, Z, N, 152 * 8, err, sizeof err))
+		return fail(strstr(err, "open") ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
+	fill_stats(&plan, st);
+	jn_plan_free(&plan);
+	return JN_OK;
+}

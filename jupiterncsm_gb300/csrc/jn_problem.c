@@ -1,0 +1,707 @@
+/*
+ * jn_problem.c — reads the reference's run file, combination table,
+ * evaluation order, index lists and matrix-element blocks, validates them,
+ * and builds the output-owned device plan described in jn_problem.h.
+ *
+ * Parsing follows the reference consumers:
+ *   bacchus.conf   src/Bacchus/settings/settings.c:79-211 (libconfig keys)
+ *   comb.txt       src/Utilities/combination_table/combination_table.c:419-640
+ *                  (titles :679-703, id strings "12=" :705-713)
+ *   BLOCK rows     src/Minerva/evaluation_order/evaluation_order.c:175-243
+ *   index lists    src/Minerva/index_list/index_list.c:69-97
+ *   ME blocks      src/Minerva/matrix_block/matrix_block.c:22-62
+ * Where the reference calls error() and exits, these functions return a
+ * non-zero status and a message.
+ */
+#define _GNU_SOURCE
+#include "jn_problem.h"
+
+#include <ctype.h>
+#include <errno.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ERR(...) do { if (err) snprintf(err, errlen, __VA_ARGS__); goto fail; } while (0)
+
+static int split_words(char *s, char **w, int maxw)
+{
+	int n = 0;
+	while (*s && n < maxw) {
+		while (*s && isspace((unsigned char)*s)) s++;
+		if (!*s) break;
+		w[n++] = s;
+		while (*s && !isspace((unsigned char)*s)) s++;
+		if (*s) *s++ = 0;
+	}
+	return n;
+}
+
+/* "12=" -> 12, digits up to '=' (combination_table.c:705-713) */
+static long id_string(const char *s)
+{
+	long v = 0;
+	while (*s && *s != '=') {
+		if (*s < '0' || *s > '9') return -1;
+		v = 10 * v + (*s++ - '0');
+	}
+	return v;
+}
+
+/* ------------------------------------------------------------------ */
+/* run file: the libconfig subset Bacchus uses                          */
+/* ------------------------------------------------------------------ */
+static char *slurp(const char *path, size_t *len)
+{
+	FILE *f = fopen(path, "rb");
+	if (!f) return NULL;
+	fseek(f, 0, SEEK_END);
+	long n = ftell(f);
+	fseek(f, 0, SEEK_SET);
+	char *b = malloc((size_t)n + 1);
+	if (!b) { fclose(f); return NULL; }
+	size_t got = fread(b, 1, (size_t)n, f);
+	fclose(f);
+	b[got] = 0;
+	if (len) *len = got;
+	return b;
+}
+
+/* find `key = value;` inside group `group:{ ... }`; returns pointer to value text */
+static int rf_lookup(const char *text, const char *group, const char *key, char *out, size_t outlen)
+{
+	const char *g = text;
+	size_t gl = strlen(group), kl = strlen(key);
+	while ((g = strstr(g, group)) != NULL) {
+		const char *after = g + gl;
+		int boundary = (g == text || !(isalnum((unsigned char)g[-1]) || g[-1] == '_'));
+		while (*after == ' ' || *after == '\t' || *after == '\n' || *after == '\r') after++;
+		if (boundary && (*after == ':' || *after == '=')) {
+			const char *open = strchr(after, '{');
+			if (!open) return 0;
+			int depth = 1;
+			const char *p = open + 1;
+			const char *end = p;
+			while (*end && depth) { if (*end == '{') depth++; else if (*end == '}') depth--; end++; }
+			while (p < end) {
+				/* skip comments */
+				if (*p == '#' || (p[0] == '/' && p[1] == '/')) { while (p < end && *p != '\n') p++; continue; }
+				if (!strncmp(p, key, kl) && (p == open + 1 || !(isalnum((unsigned char)p[-1]) || p[-1] == '_')) &&
+				    !(isalnum((unsigned char)p[kl]) || p[kl] == '_')) {
+					const char *v = p + kl;
+					while (*v == ' ' || *v == '\t') v++;
+					if (*v != '=' && *v != ':') { p++; continue; }
+					v++;
+					while (*v == ' ' || *v == '\t') v++;
+					size_t i = 0;
+					if (*v == '"') {
+						v++;
+						while (*v && *v != '"' && i + 1 < outlen) out[i++] = *v++;
+					} else {
+						while (*v && *v != ';' && *v != '\n' && *v != ',' && i + 1 < outlen) out[i++] = *v++;
+						while (i && isspace((unsigned char)out[i - 1])) i--;
+					}
+					out[i] = 0;
+					return 1;
+				}
+				p++;
+			}
+			return 0;
+		}
+		g += gl;
+	}
+	return 0;
+}
+
+int jn_read_runfile(const char *path, jn_runfile_t *rf, char *err, size_t errlen)
+{
+	char v[4096];
+	char *text = slurp(path, NULL);
+	memset(rf, 0, sizeof *rf);
+	if (!text) ERR("could not read run file %s: %s", path, strerror(errno));
+#define REQ_STR(grp, key, dst) do { if (!rf_lookup(text, grp, key, v, sizeof v)) ERR("No %s.%s found in \"%s\"", grp, key, path); snprintf(dst, sizeof dst, "%s", v); } while (0)
+#define REQ_NUM(grp, key) (rf_lookup(text, grp, key, v, sizeof v) ? 1 : 0)
+	REQ_STR("interaction", "combination_table_file", rf->comb);
+	REQ_STR("interaction", "evaluation_order_file", rf->order);
+	REQ_STR("interaction", "index_lists_base_directory", rf->lists);
+	REQ_STR("interaction", "matrix_file_base_directory", rf->mes);
+	if (!REQ_NUM("interaction", "num_neutrons")) ERR("No interaction.num_neutrons found in \"%s\"", path);
+	rf->N = atoi(v);
+	if (!REQ_NUM("interaction", "num_protons")) ERR("No interaction.num_protons found in \"%s\"", path);
+	rf->Z = atoi(v);
+	REQ_STR("lanczos", "krylow_vector_directory", rf->krylov);
+	if (!REQ_NUM("lanczos", "max_num_lanczos_iterations")) ERR("No lanczos.max_num_lanczos_iterations found in \"%s\"", path);
+	rf->max_iterations = atol(v);
+	if (!REQ_NUM("lanczos", "convergence_tolerance")) ERR("No lanczos.convergence_tolerance found in \"%s\"", path);
+	rf->tolerance = atof(v);
+	if (!REQ_NUM("lanczos", "target_eigenvector")) ERR("No lanczos.target_eigenvector found in \"%s\"", path);
+	rf->target_eigenvector = atol(v);
+	rf->converge_eigenvectors = 0;
+	if (REQ_NUM("lanczos", "converge_eigenvectors")) rf->converge_eigenvectors = (!strcmp(v, "true") || !strcmp(v, "TRUE"));
+	REQ_STR("lanczos", "eigenvector_directory", rf->eigvec);
+	/* additive GPU group, ignored by the reference */
+	rf->num_eigenvalues = 10;
+	rf->precision = 64;
+	rf->reorthogonalize = 1;
+	if (REQ_NUM("gpu", "num_eigenvalues")) rf->num_eigenvalues = atoi(v);
+	if (REQ_NUM("gpu", "precision")) rf->precision = (strstr(v, "32") ? 32 : 64);
+	if (REQ_NUM("gpu", "reorthogonalize")) rf->reorthogonalize = !(strstr(v, "partial") || !strcmp(v, "false"));
+	free(text);
+	return 0;
+fail:
+	free(text);
+	return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* combination table                                                   */
+/* ------------------------------------------------------------------ */
+typedef struct { long id; char type; long length; } listset_t;
+typedef struct { long id; long len_comb; } meset_t;
+
+static int is_title(const char *row) { return strstr(row, "***") != NULL; }
+
+typedef struct {
+	jn_block_t *b; int nb, cb;
+	listset_t *l; int nl, cl;
+	meset_t *m; int nm, cm;
+} comb_t;
+
+static int read_comb(const char *path, comb_t *c, char *err, size_t errlen)
+{
+	FILE *f = fopen(path, "r");
+	char *line = NULL;
+	size_t cap = 0;
+	memset(c, 0, sizeof *c);
+	if (!f) ERR("Could not open \"%s\". %s", path, strerror(errno));
+	int section = 0; /* 1 mp-states, 2 conn lists, 3 cross, 4 same */
+	while (getline(&line, &cap, f) >= 0) {
+		if (is_title(line)) {
+			section = strstr(line, "mp-states") ? 1 : strstr(line, "Conn lists") ? 2 :
+				  strstr(line, "Matrix-elements V (cross p-n)") ? 3 :
+				  strstr(line, "Matrix-elements V (same p/n)") ? 4 : 0;
+			continue;
+		}
+		char *w[40];
+		if (section == 1 && strstr(line, "ARRAYMP:")) {
+			int n = split_words(line, w, 40);
+			if (n < 10) ERR("malformed mp-states row in %s", path);
+			if (c->nb == c->cb) { c->cb = c->cb ? 2 * c->cb : 64; c->b = realloc(c->b, c->cb * sizeof *c->b); }
+			jn_block_t *b = &c->b[c->nb++];
+			memset(b, 0, sizeof *b);
+			b->Ep = atoi(w[0]); b->Mp = atoi(w[1]); b->En = atoi(w[2]); b->Mn = atoi(w[3]);
+			b->Np = atoll(w[4]); b->Nn = atoll(w[5]);
+			b->id = (int)id_string(w[9]);
+			if (b->id <= 0 || b->Np < 0 || b->Nn < 0) ERR("malformed mp-states row in %s", path);
+		} else if (section == 2 && strstr(line, "ARRAY:")) {
+			int n = split_words(line, w, 40);
+			if (n < 10) ERR("malformed Conn lists row in %s", path);
+			if (w[0][0] != 'n' && w[0][0] != 'p') ERR("Not a particle type %s", w[0]);
+			if (c->nl == c->cl) { c->cl = c->cl ? 2 * c->cl : 256; c->l = realloc(c->l, c->cl * sizeof *c->l); }
+			listset_t *l = &c->l[c->nl++];
+			l->type = w[0][0]; l->length = atol(w[6]); l->id = id_string(w[9]);
+			if (l->id <= 0) ERR("malformed Conn lists row in %s", path);
+		} else if ((section == 3 || section == 4) && strstr(line, "ARRAY:")) {
+			int n = split_words(line, w, 40);
+			int need = section == 3 ? 14 : 9;
+			if (n < need) ERR("malformed matrix-element row in %s", path);
+			if (c->nm == c->cm) { c->cm = c->cm ? 2 * c->cm : 256; c->m = realloc(c->m, c->cm * sizeof *c->m); }
+			meset_t *m = &c->m[c->nm++];
+			m->id = id_string(w[section == 3 ? 13 : 8]);
+			m->len_comb = section == 3 ? atol(w[8]) * atol(w[9]) : atol(w[4]);
+			if (m->id <= 0) ERR("malformed matrix-element row in %s", path);
+		}
+	}
+	free(line);
+	fclose(f);
+	if (!c->nb) { if (err) snprintf(err, errlen, "no basis blocks in %s", path); return 1; }
+	return 0;
+fail:
+	free(line);
+	if (f) fclose(f);
+	return 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* plan                                                                */
+/* ------------------------------------------------------------------ */
+typedef struct { long *v; long n, cap; } ivec_t;
+
+static int32_t *read_list_file(const char *dir, long id, int64_t *len, char *err, size_t errlen)
+{
+	char path[8192];
+	snprintf(path, sizeof path, "%s/index_list_%ld", dir, id);
+	FILE *f = fopen(path, "rb");
+	int32_t *d = NULL;
+	if (!f) ERR("Could not open file %s. %s", path, strerror(errno));
+	fseek(f, 0, SEEK_END);
+	long nb = ftell(f);
+	fseek(f, 0, SEEK_SET);
+	if (nb < 0 || nb % 12) ERR("%s does not hold whole index triples (%ld bytes)", path, nb);
+	*len = nb / 12;
+	d = malloc(nb ? (size_t)nb : 12);
+	if (!d) ERR("out of host memory reading %s", path);
+	if ((long)fread(d, 12, (size_t)*len, f) != *len) ERR("Could not read the index_list elements from %s", path);
+	fclose(f);
+	return d;
+fail:
+	if (f) fclose(f);
+	free(d);
+	return NULL;
+}
+
+static double *read_me_file(const char *dir, long id, uint64_t *nd_n, uint64_t *nd_p, int64_t *len, char *err,
+			    size_t errlen)
+{
+	char path[8192];
+	snprintf(path, sizeof path, "%s/%ld_matrix_elements", dir, id);
+	FILE *f = fopen(path, "rb");
+	double *d = NULL;
+	uint64_t hdr[2];
+	if (!f) ERR("Could not open block file %s. %s", path, strerror(errno));
+	if (fread(hdr, sizeof(uint64_t), 2, f) != 2) ERR("Could not read dimensions from matrix file %ld", id);
+	*nd_n = hdr[0]; *nd_p = hdr[1];
+	uint64_t n = hdr[0] == 0 ? hdr[1] : hdr[1] == 0 ? hdr[0] : hdr[0] * hdr[1];
+	if (hdr[0] && hdr[1] && n / hdr[0] != hdr[1]) ERR("matrix file %ld: dimension overflow", id);
+	fseek(f, 0, SEEK_END);
+	long fsz = ftell(f);
+	if ((uint64_t)fsz < 16 + 8 * n) ERR("Could not read matrix elements form matrix file %ld", id);
+	fseek(f, 16, SEEK_SET);
+	*len = (int64_t)n;
+	d = malloc(n ? n * sizeof(double) : 8);
+	if (!d) ERR("out of host memory reading %s", path);
+	if (fread(d, sizeof(double), n, f) != n) ERR("Could not read matrix elements form matrix file %ld", id);
+	fclose(f);
+	return d;
+fail:
+	if (f) fclose(f);
+	free(d);
+	return NULL;
+}
+
+static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
+{
+	/* stable counting sort on the destination index; entries (source, matrix_index) */
+	memset(rowptr, 0, (size_t)(nrows + 1) * sizeof(uint32_t));
+	for (int64_t e = 0; e < len; e++) rowptr[(by_out ? tri[3 * e + 1] : tri[3 * e]) + 1]++;
+	for (int32_t r = 0; r < nrows; r++) rowptr[r + 1] += rowptr[r];
+	uint32_t *fill = malloc((size_t)(nrows + 1) * sizeof(uint32_t));
+	memcpy(fill, rowptr, (size_t)(nrows + 1) * sizeof(uint32_t));
+	for (int64_t e = 0; e < len; e++) {
+		int32_t dst = by_out ? tri[3 * e + 1] : tri[3 * e];
+		int32_t src = by_out ? tri[3 * e] : tri[3 * e + 1];
+		uint32_t at = fill[dst]++;
+		ent[2 * at] = (uint32_t)src;
+		ent[2 * at + 1] = (uint32_t)tri[3 * e + 2];
+	}
+	free(fill);
+}
+
+void jn_plan_free(jn_plan_t *p)
+{
+	if (!p) return;
+	free(p->blocks);
+	free(p->instr);
+	for (int i = 0; i < p->nlists; i++) free(p->lists[i].triples);
+	free(p->lists);
+	free(p->mes);
+	free(p->rowptr); free(p->ent); free(p->me);
+	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
+	memset(p, 0, sizeof *p);
+}
+
+#define TILE_ELEMENTS 512
+
+/* work estimate of term t restricted to tile rows [r0,r1) x cols [c0,c1) */
+static double term_cost(const jn_plan_t *p, const jn_term_t *t, int r0, int r1, int c0, int c1)
+{
+	const uint32_t *rp = p->rowptr;
+	double np = 0, nn = 0;
+	if (t->kind != JN_KIND_N) {
+		for (int r = r0; r < r1; r++) np += rp[t->p_ptr + r + 1] - rp[t->p_ptr + r];
+		if (np == 0) return 0;
+	}
+	if (t->kind != JN_KIND_P) {
+		for (int c = c0; c < c1; c++) nn += rp[t->n_ptr + c + 1] - rp[t->n_ptr + c];
+		if (nn == 0) return 0;
+	}
+	if (t->kind == JN_KIND_P) return np * (c1 - c0);
+	if (t->kind == JN_KIND_N) return nn * (r1 - r0);
+	return np * nn;
+}
+
+int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, const char *lists_dir,
+		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen)
+{
+	comb_t c;
+	FILE *f = NULL;
+	char *line = NULL;
+	size_t cap = 0;
+	long maxid = 0;
+	int *slot_of_id = NULL;     /* id -> block / list / me slot */
+	char *kind_of_id = NULL;    /* 'b' 'l' 'm' */
+	int rc;
+	memset(p, 0, sizeof *p);
+	p->Z = Z; p->N = N;
+	if ((rc = read_comb(comb_path, &c, err, errlen))) return rc;
+	for (int i = 0; i < c.nb; i++) if (c.b[i].id > maxid) maxid = c.b[i].id;
+	for (int i = 0; i < c.nl; i++) if (c.l[i].id > maxid) maxid = c.l[i].id;
+	for (int i = 0; i < c.nm; i++) if (c.m[i].id > maxid) maxid = c.m[i].id;
+	slot_of_id = malloc((maxid + 1) * sizeof(int));
+	kind_of_id = calloc(maxid + 1, 1);
+	for (long i = 0; i <= maxid; i++) slot_of_id[i] = -1;
+	p->nblocks = c.nb;
+	p->blocks = c.b; c.b = NULL;
+	int64_t off = 0;
+	for (int i = 0; i < p->nblocks; i++) {
+		jn_block_t *b = &p->blocks[i];
+		if (kind_of_id[b->id]) ERR("array id %d used twice in %s", b->id, comb_path);
+		kind_of_id[b->id] = 'b'; slot_of_id[b->id] = i;
+		b->offset = off;
+		off += b->Np * b->Nn;
+	}
+	p->dim = off;
+	for (int i = 0; i < c.nl; i++) {
+		if (kind_of_id[c.l[i].id]) ERR("array id %ld used twice in %s", c.l[i].id, comb_path);
+		kind_of_id[c.l[i].id] = 'l'; slot_of_id[c.l[i].id] = -2 - i; /* resolved lazily */
+	}
+	for (int i = 0; i < c.nm; i++) {
+		if (kind_of_id[c.m[i].id]) ERR("array id %ld used twice in %s", c.m[i].id, comb_path);
+		kind_of_id[c.m[i].id] = 'm'; slot_of_id[c.m[i].id] = -2 - i;
+	}
+
+	/* evaluation order */
+	f = fopen(order_path, "r");
+	if (!f) ERR("Could not open evaluation order file %s. %s", order_path, strerror(errno));
+	int icap = 0;
+	while (getline(&line, &cap, f) >= 0) {
+		char *b = strstr(line, "BLOCK:");
+		if (!b || strstr(line, "UNLOAD_")) continue;
+		char *w[16];
+		int n = split_words(b, w, 16);
+		if (n != 5 && n != 6) ERR("malformed evaluation-order row \"%s\"", b);
+		long v[5];
+		for (int q = 1; q < n; q++) {
+			char *end;
+			v[q - 1] = strtol(w[q], &end, 10);
+			if (*end || v[q - 1] <= 0 || v[q - 1] > maxid) ERR("unknown array id \"%s\" in evaluation order", w[q]);
+		}
+		jn_instr_t in = { 0, -1, -1, -1, -1, -1 };
+		if (kind_of_id[v[0]] != 'b' || kind_of_id[v[1]] != 'b') ERR("BLOCK row names a non-vector array");
+		in.bin = slot_of_id[v[0]]; in.bout = slot_of_id[v[1]];
+		long lids[2] = { v[2], n == 6 ? v[3] : 0 };
+		long meid = n == 6 ? v[4] : v[3];
+		if (kind_of_id[meid] != 'm') ERR("BLOCK row names %ld as matrix elements but it is not one", meid);
+		int nl = n == 6 ? 2 : 1;
+		int lslot[2] = { -1, -1 };
+		char ltype[2] = { 0, 0 };
+		for (int q = 0; q < nl; q++) {
+			if (kind_of_id[lids[q]] != 'l') ERR("BLOCK row names %ld as an index list but it is not one", lids[q]);
+			int s = slot_of_id[lids[q]];
+			if (s < 0) {
+				int ci = -2 - s;
+				if (p->nlists % 256 == 0) p->lists = realloc(p->lists, (p->nlists + 256) * sizeof(jn_list_t));
+				jn_list_t *L = &p->lists[p->nlists];
+				memset(L, 0, sizeof *L);
+				L->id = (int)lids[q]; L->type = c.l[ci].type; L->nin = L->nout = -1;
+				L->triples = read_list_file(lists_dir, lids[q], &L->len, err, errlen);
+				if (!L->triples) goto fail;
+				s = slot_of_id[lids[q]] = p->nlists++;
+			}
+			lslot[q] = s;
+			ltype[q] = p->lists[s].type;
+		}
+		if (nl == 2) {
+			in.kind = JN_KIND_NP;
+			if (ltype[0] == 'n') { in.ln = lslot[0]; in.lp = lslot[1]; } else { in.ln = lslot[1]; in.lp = lslot[0]; }
+			if (p->lists[in.ln].type != 'n' || p->lists[in.lp].type != 'p')
+				ERR("neutron-proton BLOCK row needs one neutron and one proton list");
+		} else if (ltype[0] == 'n') { in.kind = JN_KIND_N; in.ln = lslot[0]; }
+		else { in.kind = JN_KIND_P; in.lp = lslot[0]; }
+		int ms = slot_of_id[meid];
+		if (ms < 0) {
+			if (p->nmes % 256 == 0) p->mes = realloc(p->mes, (p->nmes + 256) * sizeof(jn_me_t));
+			jn_me_t *M = &p->mes[p->nmes];
+			memset(M, 0, sizeof *M);
+			M->id = (int)meid;
+			ms = slot_of_id[meid] = p->nmes++;
+		}
+		in.me = ms;
+		if (p->ninstr == icap) { icap = icap ? 2 * icap : 1024; p->instr = realloc(p->instr, icap * sizeof(jn_instr_t)); }
+		p->instr[p->ninstr++] = in;
+	}
+	fclose(f); f = NULL;
+	if (!p->ninstr) ERR("evaluation order %s holds no BLOCK rows", order_path);
+
+	/* matrix elements */
+	int64_t me_total = 0;
+	double **me_data = calloc(p->nmes, sizeof(double *));
+	for (int i = 0; i < p->nmes; i++) {
+		jn_me_t *M = &p->mes[i];
+		me_data[i] = read_me_file(me_dir, M->id, &M->nd_n, &M->nd_p, &M->len, err, errlen);
+		if (!me_data[i]) { for (int q = 0; q < i; q++) free(me_data[q]); free(me_data); goto fail; }
+		M->offset = me_total;
+		me_total += M->len;
+	}
+	p->n_me = me_total;
+	p->me = malloc((me_total ? me_total : 1) * sizeof(double));
+	if (!p->me) ERR("out of host memory for matrix elements");
+	for (int i = 0; i < p->nmes; i++) {
+		memcpy(p->me + p->mes[i].offset, me_data[i], (size_t)p->mes[i].len * sizeof(double));
+		free(me_data[i]);
+	}
+	free(me_data);
+	p->me_elements = me_total;
+
+	/* validation and list dimensions */
+	for (int i = 0; i < p->ninstr; i++) {
+		jn_instr_t *x = &p->instr[i];
+		jn_block_t *bi = &p->blocks[x->bin], *bo = &p->blocks[x->bout];
+		jn_me_t *M = &p->mes[x->me];
+		if (x->kind == JN_KIND_N && bi->Np != bo->Np) ERR("instruction %d: neutron term between blocks of different proton dimension", i);
+		if (x->kind == JN_KIND_P && bi->Nn != bo->Nn) ERR("instruction %d: proton term between blocks of different neutron dimension", i);
+		if (x->kind == JN_KIND_NP && M->nd_n == 0) ERR("instruction %d: matrix block %d has no neutron dimension", i, M->id);
+		int slots[2] = { x->ln, x->lp };
+		for (int q = 0; q < 2; q++) {
+			if (slots[q] < 0) continue;
+			jn_list_t *L = &p->lists[slots[q]];
+			int32_t nin = (int32_t)(L->type == 'n' ? bi->Nn : bi->Np);
+			int32_t nout = (int32_t)(L->type == 'n' ? bo->Nn : bo->Np);
+			if (L->nin < 0) { L->nin = nin; L->nout = nout; }
+			else if (L->nin != nin || L->nout != nout)
+				ERR("index list %d is used between sub-bases of different sizes", L->id);
+		}
+	}
+	for (int l = 0; l < p->nlists; l++) {
+		jn_list_t *L = &p->lists[l];
+		for (int64_t e = 0; e < L->len; e++) {
+			int32_t a = L->triples[3 * e], b = L->triples[3 * e + 1];
+			if (a < 0 || a >= L->nin || b < 0 || b >= L->nout)
+				ERR("index list %d entry %lld: in %d / out %d outside the %d x %d sub-bases", L->id, (long long)e, a, b,
+				    L->nin, L->nout);
+		}
+	}
+	for (int i = 0; i < p->ninstr; i++) {
+		jn_instr_t *x = &p->instr[i];
+		jn_me_t *M = &p->mes[x->me];
+		if (x->kind == JN_KIND_NP) {
+			uint64_t kmax_n = 0, kmax_p = 0;
+			jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+			for (int64_t e = 0; e < Ln->len; e++) { uint64_t k = (uint32_t)Ln->triples[3 * e + 2] & 0x7fffffffu; if (k > kmax_n) kmax_n = k; }
+			for (int64_t e = 0; e < Lp->len; e++) { uint64_t k = (uint32_t)Lp->triples[3 * e + 2] & 0x7fffffffu; if (k > kmax_p) kmax_p = k; }
+			if (Ln->len && Lp->len && (kmax_n >= M->nd_n || kmax_n + M->nd_n * kmax_p >= (uint64_t)M->len))
+				ERR("instruction %d: matrix index outside matrix block %d", i, M->id);
+		} else {
+			jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
+			for (int64_t e = 0; e < L->len; e++)
+				if ((int64_t)((uint32_t)L->triples[3 * e + 2] & 0x7fffffffu) >= M->len)
+					ERR("index list %d entry %lld: matrix index outside matrix block %d", L->id, (long long)e, M->id);
+		}
+	}
+
+	/* matrix elements some product actually reads: the compulsory traffic */
+	{
+		uint8_t *mark = calloc(p->n_me ? p->n_me : 1, 1);
+		int64_t *kn = NULL, *kp = NULL;
+		size_t capn = 0, capp = 0;
+		if (!mark) ERR("out of host memory");
+		for (int i = 0; i < p->ninstr; i++) {
+			jn_instr_t *x = &p->instr[i];
+			jn_me_t *M = &p->mes[x->me];
+			uint8_t *mk = mark + M->offset;
+			if (x->kind != JN_KIND_NP) {
+				jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
+				for (int64_t e = 0; e < L->len; e++) mk[(uint32_t)L->triples[3 * e + 2] & 0x7fffffffu] = 1;
+				continue;
+			}
+			/* every (k_n, k_p) pair of the two lists is visited: mark the product of the distinct sets */
+			jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+			size_t nn = 0, np_ = 0;
+			if ((size_t)Ln->len > capn) { capn = Ln->len; kn = realloc(kn, capn * sizeof(int64_t)); }
+			if ((size_t)Lp->len > capp) { capp = Lp->len; kp = realloc(kp, capp * sizeof(int64_t)); }
+			uint8_t *seen_n = calloc(M->nd_n + 1, 1), *seen_p = calloc(M->nd_p + 1, 1);
+			for (int64_t e = 0; e < Ln->len; e++) {
+				uint32_t k = (uint32_t)Ln->triples[3 * e + 2] & 0x7fffffffu;
+				if (!seen_n[k]) { seen_n[k] = 1; kn[nn++] = k; }
+			}
+			for (int64_t e = 0; e < Lp->len; e++) {
+				uint32_t k = (uint32_t)Lp->triples[3 * e + 2] & 0x7fffffffu;
+				if (!seen_p[k]) { seen_p[k] = 1; kp[np_++] = k; }
+			}
+			for (size_t a = 0; a < np_; a++)
+				for (size_t b = 0; b < nn; b++) mk[kn[b] + (int64_t)M->nd_n * kp[a]] = 1;
+			free(seen_n); free(seen_p);
+		}
+		for (int64_t e = 0; e < p->n_me; e++) p->me_referenced += mark[e];
+		free(mark); free(kn); free(kp);
+	}
+
+	/* CSR views */
+	int64_t nrp = 0, nent = 0;
+	for (int l = 0; l < p->nlists; l++) {
+		jn_list_t *L = &p->lists[l];
+		L->csr_out_ptr = nrp; nrp += L->nout + 1;
+		L->csr_in_ptr = nrp; nrp += L->nin + 1;
+		L->ent_out = nent; nent += L->len;
+		L->ent_in = nent; nent += L->len;
+		p->list_entries += L->len;
+	}
+	if (nent > 0xffffffffll) ERR("index lists too long for 32-bit offsets");
+	p->n_rowptr = nrp; p->n_ent = nent;
+	p->rowptr = malloc((nrp ? nrp : 1) * sizeof(uint32_t));
+	p->ent = malloc((nent ? nent : 1) * 2 * sizeof(uint32_t));
+	if (!p->rowptr || !p->ent) ERR("out of host memory for list views");
+	for (int l = 0; l < p->nlists; l++) {
+		jn_list_t *L = &p->lists[l];
+		build_csr(L->triples, L->len, L->nout, 1, p->rowptr + L->csr_out_ptr, p->ent + 2 * L->ent_out);
+		build_csr(L->triples, L->len, L->nin, 0, p->rowptr + L->csr_in_ptr, p->ent + 2 * L->ent_in);
+		/* the CSR row pointers are list-local: make them absolute entry indices */
+		for (int32_t r = 0; r <= L->nout; r++) p->rowptr[L->csr_out_ptr + r] += (uint32_t)L->ent_out;
+		for (int32_t r = 0; r <= L->nin; r++) p->rowptr[L->csr_in_ptr + r] += (uint32_t)L->ent_in;
+	}
+
+	/* terms: forward on the output block, transpose on the input block */
+	p->terms = malloc(2 * (size_t)p->ninstr * sizeof(jn_term_t));
+	int *term_dst = malloc(2 * (size_t)p->ninstr * sizeof(int));
+	for (int i = 0; i < p->ninstr; i++) {
+		jn_instr_t *x = &p->instr[i];
+		for (int dir = 0; dir < 2; dir++) {
+			if (dir == 1 && x->bin == x->bout) break;
+			jn_term_t t;
+			memset(&t, 0, sizeof t);
+			int src = dir ? x->bout : x->bin, dst = dir ? x->bin : x->bout;
+			t.kind = x->kind;
+			t.nd = (int32_t)p->mes[x->me].nd_n;
+			t.src_off = p->blocks[src].offset;
+			t.Nn_src = (int32_t)p->blocks[src].Nn;
+			t.Nn_dst = (int32_t)p->blocks[dst].Nn;
+			if (x->lp >= 0) {
+				jn_list_t *L = &p->lists[x->lp];
+				t.p_ptr = dir ? L->csr_in_ptr : L->csr_out_ptr;
+				t.p_ent = 0;
+			}
+			if (x->ln >= 0) {
+				jn_list_t *L = &p->lists[x->ln];
+				t.n_ptr = dir ? L->csr_in_ptr : L->csr_out_ptr;
+				t.n_ent = 0;
+			}
+			t.me_off = p->mes[x->me].offset;
+			t.instr = i;
+			t.transpose = dir;
+			term_dst[p->nterms] = dst;
+			p->terms[p->nterms++] = t;
+		}
+	}
+	/* visits for accounting */
+	for (int i = 0; i < p->ninstr; i++) {
+		jn_instr_t *x = &p->instr[i];
+		double v;
+		if (x->kind == JN_KIND_NP) v = (double)p->lists[x->ln].len * (double)p->lists[x->lp].len;
+		else if (x->kind == JN_KIND_P) v = (double)p->lists[x->lp].len * (double)p->blocks[x->bin].Nn;
+		else v = (double)p->lists[x->ln].len * (double)p->blocks[x->bin].Np;
+		p->visits += (x->bin == x->bout) ? v : 2 * v;
+	}
+
+	/* tiles and units */
+	{
+		/* terms grouped per destination block, in evaluation order */
+		int *count = calloc(p->nblocks + 1, sizeof(int));
+		for (int t = 0; t < p->nterms; t++) count[term_dst[t] + 1]++;
+		for (int b = 0; b < p->nblocks; b++) count[b + 1] += count[b];
+		int *byblk = malloc((p->nterms ? p->nterms : 1) * sizeof(int));
+		int *fillp = malloc((p->nblocks + 1) * sizeof(int));
+		memcpy(fillp, count, (p->nblocks + 1) * sizeof(int));
+		for (int t = 0; t < p->nterms; t++) byblk[fillp[term_dst[t]]++] = t;
+		free(fillp);
+		/* pass 1: tiles and their costs */
+		int tcap = 1024;
+		p->tiles = malloc(tcap * sizeof(jn_tile_t));
+		double *tile_cost = malloc(tcap * sizeof(double));
+		double total_cost = 0;
+		for (int b = 0; b < p->nblocks; b++) {
+			jn_block_t *B = &p->blocks[b];
+			if (B->Np == 0 || B->Nn == 0) continue;
+			int64_t cw = B->Nn < TILE_ELEMENTS ? B->Nn : TILE_ELEMENTS;
+			int64_t R = B->Nn >= TILE_ELEMENTS ? 1 : TILE_ELEMENTS / B->Nn;
+			for (int64_t r0 = 0; r0 < B->Np; r0 += R)
+				for (int64_t c0 = 0; c0 < B->Nn; c0 += cw) {
+					if (p->ntiles == tcap) {
+						tcap *= 2;
+						p->tiles = realloc(p->tiles, tcap * sizeof(jn_tile_t));
+						tile_cost = realloc(tile_cost, tcap * sizeof(double));
+					}
+					jn_tile_t *T = &p->tiles[p->ntiles];
+					memset(T, 0, sizeof *T);
+					T->dst_off = B->offset;
+					T->Nn = (int32_t)B->Nn;
+					T->row0 = (int32_t)r0; T->nrows = (int32_t)((r0 + R <= B->Np) ? R : B->Np - r0);
+					T->col0 = (int32_t)c0; T->ncols = (int32_t)((c0 + cw <= B->Nn) ? cw : B->Nn - c0);
+					T->pad = b;     /* destination block while planning */
+					double cost = 0;
+					for (int q = count[b]; q < count[b + 1]; q++)
+						cost += term_cost(p, &p->terms[byblk[q]], T->row0, T->row0 + T->nrows, T->col0, T->col0 + T->ncols);
+					tile_cost[p->ntiles++] = cost;
+					total_cost += cost;
+				}
+		}
+		if (target_units <= 0) target_units = 152 * 8;
+		double target = total_cost / target_units;
+		if (target < 4096) target = 4096;
+		/* pass 2: chunks */
+		int64_t ucap = 4096, tcap2 = 1 << 16;
+		p->units = malloc(ucap * sizeof(jn_unit_t));
+		p->unit_terms = malloc(tcap2 * sizeof(int32_t));
+		int64_t partial = 0;
+		for (int ti = 0; ti < p->ntiles; ti++) {
+			jn_tile_t *T = &p->tiles[ti];
+			int b = T->pad;
+			T->pad = 0;
+			T->unit0 = p->nunits;
+			int nchunk = (int)ceil(tile_cost[ti] / target);
+			if (nchunk < 1) nchunk = 1;
+			double per = tile_cost[ti] / nchunk, acc = 0;
+			int nb_terms = count[b + 1] - count[b];
+			double *cst = malloc((nb_terms ? nb_terms : 1) * sizeof(double));
+			int lastnz = -1;
+			for (int q = 0; q < nb_terms; q++) {
+				cst[q] = term_cost(p, &p->terms[byblk[count[b] + q]], T->row0, T->row0 + T->nrows, T->col0,
+						   T->col0 + T->ncols);
+				if (cst[q] > 0) lastnz = q;
+			}
+			int64_t begin = p->n_unit_terms;
+			int chunks = 0;
+			for (int q = 0; q <= lastnz; q++) {
+				if (cst[q] == 0) continue;
+				if (p->n_unit_terms == tcap2) { tcap2 *= 2; p->unit_terms = realloc(p->unit_terms, tcap2 * sizeof(int32_t)); }
+				p->unit_terms[p->n_unit_terms++] = byblk[count[b] + q];
+				acc += cst[q];
+				if (acc >= per * (chunks + 1) || q == lastnz) {
+					if (p->nunits == ucap) { ucap *= 2; p->units = realloc(p->units, ucap * sizeof(jn_unit_t)); }
+					jn_unit_t *U = &p->units[p->nunits++];
+					U->tile = ti; U->chunk = chunks++;
+					U->t0 = begin; U->t1 = p->n_unit_terms;
+					begin = p->n_unit_terms;
+				}
+			}
+			free(cst);
+			T->nchunks = chunks;
+			T->partial = partial;
+			partial += (int64_t)chunks * T->nrows * T->ncols;
+		}
+		p->n_partial = partial;
+		free(tile_cost); free(byblk); free(count);
+	}
+	free(term_dst);
+	free(slot_of_id); free(kind_of_id);
+	free(c.l); free(c.m); free(line);
+	return 0;
+fail:
+	if (f) fclose(f);
+	free(line);
+	free(c.b); free(c.l); free(c.m);
+	free(slot_of_id); free(kind_of_id);
+	jn_plan_free(p);
+	return 1;
+}

@@ -1,0 +1,147 @@
+/*
+ * jn_problem.h — host-side model of one JupiterNCSM Hamiltonian and the
+ * device execution plan built from it.
+ *
+ * The files read are the reference's (src/Utilities/combination_table/
+ * combination_table.c:419-640, src/Minerva/evaluation_order/evaluation_order.c:43-243,
+ * src/Minerva/index_list/index_list.c:69-97, src/Minerva/matrix_block/matrix_block.c:22-62).
+ * Everything is validated on the host so that no device access can leave
+ * its buffer: every in/out index against the basis-block dimensions and every
+ * connection index against its matrix-element block.
+ *
+ * The plan turns the evaluation order into output-owned work: each
+ * instruction contributes a forward term to its output block and, when
+ * off-diagonal, a transposed term to its input block
+ * (src/Minerva/matrix_vector_multiplication/matrix_vector_multiplication.c:212-462).
+ * Output blocks are cut into element tiles; the terms touching a tile are
+ * cut into chunks of similar work.  A chunk is one CTA's work unit; its
+ * partial sums are added in chunk order by the reduction pass, so the
+ * summation order of every output element is fixed by the files alone.
+ */
+#ifndef JN_PROBLEM_H
+#define JN_PROBLEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { JN_KIND_N = 1, JN_KIND_P = 2, JN_KIND_NP = 3 };
+
+typedef struct {
+	int Ep, Mp, En, Mn;
+	int64_t Np, Nn;
+	int64_t offset;         /* first element in the full vector */
+	int id;
+} jn_block_t;
+
+typedef struct {
+	int kind;               /* JN_KIND_* */
+	int bin, bout;          /* basis block indices (0-based) */
+	int ln, lp;             /* list slots or -1 */
+	int me;                 /* matrix-element slot */
+} jn_instr_t;
+
+/* one index list: file contents plus both CSR views */
+typedef struct {
+	int id;
+	char type;              /* 'n' or 'p' */
+	int64_t len;
+	int32_t *triples;       /* len*3 as on disk: in, out, matrix_index */
+	int32_t nin, nout;      /* sub-basis sizes it maps between */
+	int64_t csr_out_ptr;    /* offsets into jn_plan_t.rowptr (nout+1 entries) */
+	int64_t csr_in_ptr;     /* (nin+1 entries) */
+	int64_t ent_out;        /* offsets into jn_plan_t.ent (len entries) */
+	int64_t ent_in;
+} jn_list_t;
+
+typedef struct {
+	int id;
+	uint64_t nd_n, nd_p;    /* header dimensions */
+	int64_t len;
+	int64_t offset;         /* into jn_plan_t.me */
+} jn_me_t;
+
+/* device term descriptor: one direction of one instruction, seen from its
+ * destination block.  Entry arrays hold (source index, matrix_index). */
+typedef struct {
+	int32_t kind;
+	int32_t nd;             /* neutron matrix dimension (NP) */
+	int64_t src_off;        /* source block offset in x */
+	int32_t Nn_src, Nn_dst;
+	int64_t p_ptr, p_ent;   /* CSR (by destination row) of the proton list */
+	int64_t n_ptr, n_ent;   /* CSR (by destination column) of the neutron list */
+	int64_t me_off;
+	int32_t instr;          /* evaluation-order index */
+	int32_t transpose;
+} jn_term_t;
+
+typedef struct {
+	int64_t dst_off;        /* block offset in y */
+	int32_t Nn;             /* destination block columns */
+	int32_t row0, nrows, col0, ncols;
+	int32_t nchunks;
+	int64_t partial;        /* first partial slot: chunk c, element e at partial + c*E + e */
+	int32_t unit0;          /* first unit of this tile */
+	int32_t pad;
+} jn_tile_t;
+
+typedef struct {
+	int32_t tile;
+	int32_t chunk;
+	int64_t t0, t1;         /* range into jn_plan_t.unit_terms */
+} jn_unit_t;
+
+typedef struct {
+	/* problem */
+	int Z, N;
+	int nblocks;
+	jn_block_t *blocks;
+	int64_t dim;
+	int ninstr;
+	jn_instr_t *instr;
+	int nlists;
+	jn_list_t *lists;
+	int nmes;
+	jn_me_t *mes;
+	/* flattened device arrays */
+	int64_t n_rowptr;  uint32_t *rowptr;
+	int64_t n_ent;     uint32_t *ent;      /* pairs: src, matrix_index */
+	int64_t n_me;      double *me;
+	int nterms;        jn_term_t *terms;
+	int ntiles;        jn_tile_t *tiles;
+	int nunits;        jn_unit_t *units;
+	int64_t n_unit_terms; int32_t *unit_terms;
+	int64_t n_partial;
+	/* accounting */
+	int64_t list_entries;           /* sum of distinct list lengths */
+	int64_t me_elements;            /* sum of distinct ME block lengths */
+	int64_t me_referenced;          /* elements some list pair actually indexes */
+	double visits;                  /* multiply-adds per product (both directions) */
+} jn_plan_t;
+
+typedef struct {
+	char comb[4096], order[4096], lists[4096], mes[4096];
+	char krylov[4096], eigvec[4096];
+	int Z, N;
+	long max_iterations;
+	double tolerance;
+	long target_eigenvector;
+	int converge_eigenvectors;
+	/* optional GPU group */
+	int num_eigenvalues;
+	int precision;          /* 64 or 32 */
+	int reorthogonalize;    /* 1 full, 0 reference-style partial */
+} jn_runfile_t;
+
+int jn_read_runfile(const char *path, jn_runfile_t *rf, char *err, size_t errlen);
+int jn_plan_build(jn_plan_t *plan, const char *comb, const char *order, const char *lists_dir,
+		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen);
+void jn_plan_free(jn_plan_t *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,157 @@
+"""The oracle — TEST INFRASTRUCTURE ONLY.
+
+CPU restatements of the reference's hot path and a driver for the compiled
+reference itself.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg use this package, always as the checker, never as the path
+being measured or shipped.
+
+* ``Port``       plain-C restatement of the Minerva kernels (minerva_port.c)
+* ``Reference``  the reference's own Minerva code, compiled unchanged into
+                 _ref/libref_minerva.so when the reference tree is present
+* ``dense_h``    independent second-quantisation dense Hamiltonian
+* ``index_lists`` Python restatement of index-list construction
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "libminerva_port.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_minerva.so")
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+def reference_available():
+    return os.path.exists(REF_LIB)
+
+
+class Port:
+    """Single-threaded (or OpenMP task-farm) restatement of run_matrix_vector_multiplication."""
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            L = ctypes.CDLL(PORT_LIB)
+            L.port_open.restype = ctypes.c_void_p
+            L.port_open.argtypes = [ctypes.c_char_p] * 4
+            L.port_matvec.argtypes = [ctypes.c_void_p] * 3
+            L.port_matvec_omp.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int]
+            L.port_matvec_omp.restype = ctypes.c_double
+            L.port_dimension.restype = ctypes.c_size_t
+            L.port_dimension.argtypes = [ctypes.c_void_p]
+            L.port_close.argtypes = [ctypes.c_void_p]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, d):
+        e = lambda s: s.encode()
+        self.h = self.lib().port_open(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                                      e(f"{d}/matrix_elements"))
+        if not self.h:
+            raise RuntimeError(f"oracle port could not open {d}")
+        self.dimension = self.lib().port_dimension(self.h)
+
+    def matvec(self, x, y=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.dimension) if y is None else y
+        self.lib().port_matvec(self.h, x.ctypes.data, y.ctypes.data)
+        return y
+
+    def matvec_omp(self, x, y, threads=0):
+        """y += H x with the reference's OpenMP task farm; returns seconds of the kernel region."""
+        return self.lib().port_matvec_omp(self.h, x.ctypes.data, y.ctypes.data, int(threads))
+
+    def close(self):
+        if self.h:
+            self.lib().port_close(self.h)
+            self.h = None
+
+
+class Reference:
+    """The compiled reference Minerva (in-memory kernels and the file-level scheduler)."""
+    _lib = None
+
+    @classmethod
+    def lib(cls):
+        if cls._lib is None:
+            L = ctypes.CDLL(REF_LIB)
+            L.ref_mem_open.restype = ctypes.c_void_p
+            L.ref_mem_open.argtypes = [ctypes.c_char_p] * 5 + [ctypes.c_int] * 3
+            L.ref_mem_matvec.restype = ctypes.c_double
+            L.ref_mem_matvec.argtypes = [ctypes.c_void_p] * 3
+            L.ref_mem_dimension.restype = ctypes.c_size_t
+            L.ref_mem_dimension.argtypes = [ctypes.c_void_p]
+            L.ref_mem_threads.argtypes = [ctypes.c_void_p]
+            L.ref_mem_close.argtypes = [ctypes.c_void_p]
+            L.ref_matvec_files.argtypes = [ctypes.c_char_p] * 6 + [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                                   ctypes.c_int]
+            cls._lib = L
+        return cls._lib
+
+    def __init__(self, d, Z, N, threads=0):
+        self.d, self.Z, self.N = d, Z, N
+        zero = write_zero_vectors(d)
+        e = lambda s: s.encode()
+        self.h = self.lib().ref_mem_open(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                                         e(f"{d}/matrix_elements"), e(zero), Z, N, int(threads))
+        self.dimension = self.lib().ref_mem_dimension(self.h)
+        self.threads = self.lib().ref_mem_threads(self.h)
+
+    def matvec(self, x, y=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.dimension) if y is None else y
+        self.seconds = self.lib().ref_mem_matvec(self.h, x.ctypes.data, y.ctypes.data)
+        return y
+
+    def matvec_files(self, out_dir, in_dir, threads=0, max_memory=64e9):
+        e = lambda s: s.encode()
+        d = self.d
+        self.lib().ref_matvec_files(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                                    e(f"{d}/matrix_elements"), e(in_dir), e(out_dir), self.Z, self.N, max_memory,
+                                    int(threads))
+
+    def close(self):
+        if self.h:
+            self.lib().ref_mem_close(self.h)
+            self.h = None
+
+
+def read_blocks(d):
+    """[(id, Np, Nn)] of the basis blocks in comb.txt order."""
+    out, sec = [], None
+    with open(f"{d}/comb.txt") as f:
+        for row in f:
+            if "***" in row:
+                sec = "mp" if "mp-states" in row else None
+                continue
+            if sec == "mp" and "ARRAYMP:" in row:
+                w = row.split()
+                out.append((int(w[9].rstrip("=")), int(w[4]), int(w[5])))
+    return out
+
+
+def write_vector_dir(d, blocks, v):
+    os.makedirs(d, exist_ok=True)
+    off = 0
+    for (bid, np_, nn_) in blocks:
+        n = np_ * nn_
+        np.asarray(v[off:off + n], dtype=np.float64).tofile(f"{d}/vec_{bid}")
+        off += n
+
+
+def read_vector_dir(d, blocks):
+    return np.concatenate([np.fromfile(f"{d}/vec_{bid}", dtype=np.float64) for (bid, _, _) in blocks])
+
+
+def write_zero_vectors(d):
+    z = f"{d}/zero_vectors"
+    blocks = read_blocks(d)
+    if not os.path.isdir(z):
+        write_vector_dir(z, blocks, np.zeros(sum(a * b for _, a, b in blocks)))
+    return z

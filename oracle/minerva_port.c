@@ -18,7 +18,9 @@
  *   diagonal vs off-diagonal dispatch    Minerva/scheduler/scheduler.c:194-246
  */
 #include <math.h>
+#include <omp.h>
 #include <stdint.h>
+#include <time.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -169,12 +171,57 @@ long port_num_instructions(void *h) { return ((port_t *)h)->nins; }
 static inline int sgn(int32_t mi) { return (mi & (int32_t)0x80000000) ? -1 : 1; }
 static inline size_t idx(int32_t mi) { return (size_t)(mi & 0x7FFFFFFF); }
 
+static void apply_instr(const port_t *p, const instr_t *I, const double *x, double *y);
+
 /* y += H x, instructions applied in evaluation-order sequence */
 void port_matvec(void *h, const double *x, double *y)
 {
 	port_t *p = h;
-	for (long i = 0; i < p->nins; i++) {
-		const instr_t *I = &p->ins[i];
+	for (long i = 0; i < p->nins; i++) apply_instr(p, &p->ins[i], x, y);
+}
+
+/*
+ * y += H x with the reference's parallel scheme: an OpenMP task farm over
+ * the instructions (Minerva/scheduler/scheduler.c:97-137, lock-guarded
+ * fetch evaluation_order.c:138-161) writing into one output replica per
+ * thread, reduced at the end (Minerva/vector_block/vector_block.c:49-66,
+ * 145-155).  Returns the wall time of the parallel region in seconds.
+ */
+double port_matvec_omp(void *h, const double *x, double *y, int nthreads)
+{
+	port_t *p = h;
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+	int T = omp_get_max_threads();
+	double *rep = calloc((size_t)T * p->dim + 1, sizeof(double));
+	struct timespec t0, t1;
+	clock_gettime(CLOCK_MONOTONIC, &t0);
+	long next = 0;
+#pragma omp parallel
+	{
+		double *mine = rep + (size_t)omp_get_thread_num() * p->dim;
+		for (;;) {
+			long i;
+#pragma omp atomic capture
+			i = next++;
+			if (i >= p->nins) break;
+			apply_instr(p, &p->ins[i], x, mine);
+		}
+#pragma omp barrier
+#pragma omp for schedule(static)
+		for (long e = 0; e < (long)p->dim; e++) {
+			double s = 0.0;
+			for (int t = 0; t < omp_get_num_threads(); t++) s += rep[(size_t)t * p->dim + e];
+			y[e] += s;
+		}
+	}
+	clock_gettime(CLOCK_MONOTONIC, &t1);
+	free(rep);
+	return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+static void apply_instr(const port_t *p, const instr_t *I, const double *x, double *y)
+{
+	{
 		const int diag = I->bin == I->bout;
 		const long Np_i = p->np[I->bin], Nn_i = p->nn[I->bin], Nn_o = p->nn[I->bout];
 		const double *xi = x + p->offset[I->bin], *xo = x + p->offset[I->bout];

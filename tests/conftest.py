@@ -1,0 +1,70 @@
+import os
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "slow: takes more than a few seconds")
+
+
+def _ensure_built():
+    import jupiterncsm_gb300 as jn
+    import oracle
+    if not (os.path.exists(jn.GPU_LIB) and os.path.exists(jn.GEN_LIB)):
+        jn.build()
+    if not os.path.exists(oracle.PORT_LIB):
+        subprocess.run(["make", "-s", "-C", oracle.HERE, "port"], check=True)
+    if os.path.isdir("/root/reference/src") and not os.path.exists(oracle.REF_LIB):
+        subprocess.run(["make", "-s", "-C", oracle.HERE, "ref"], check=True)
+    emu = os.path.join(ROOT, "tests", "_build", "libplan_emu.so")
+    if not os.path.exists(emu):
+        os.makedirs(os.path.dirname(emu), exist_ok=True)
+        subprocess.run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-o", emu,
+                        os.path.join(ROOT, "tests", "native", "plan_emulator.c"),
+                        os.path.join(ROOT, "jupiterncsm_gb300", "csrc", "jn_problem.c"), "-lm"], check=True)
+
+
+_ensure_built()
+
+# name -> (Z, N, Nmax, nbody, 2M)
+PROBLEMS = {
+    "he4_n2_2b": (2, 2, 2, 2, 0),
+    "he4_n2_3b": (2, 2, 2, 3, 0),
+    "he4_n4_2b": (2, 2, 4, 2, 0),
+    "li6_n2_3b": (3, 3, 2, 3, 2),
+    "he4_n6_3b": (2, 2, 6, 3, 0),
+}
+
+
+@pytest.fixture(scope="session")
+def problem_root(tmp_path_factory):
+    return tmp_path_factory.mktemp("problems")
+
+
+_cache = {}
+
+
+@pytest.fixture(scope="session")
+def problem(problem_root):
+    """problem(name) -> (directory, Z, N, Nmax, nbody)."""
+    import jupiterncsm_gb300 as jn
+
+    def get(name):
+        if name not in _cache:
+            Z, N, nmax, nbody, M2 = PROBLEMS[name]
+            d = str(problem_root / name)
+            jn.generate(d, Z=Z, N=N, nmax=nmax, nbody=nbody, M2=M2, basis_files=False)
+            _cache[name] = (d, Z, N, nmax, nbody)
+        return _cache[name]
+    return get
+
+
+def reference_tree_present():
+    return os.path.isdir("/root/reference/src")

@@ -1,0 +1,93 @@
+"""GPU matrix-vector product through the C ABI against the oracle."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import jupiterncsm_gb300 as jn
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TOL = 1e-12   # relative to max|y|: FP64 path, only the summation order differs
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "li6_n2_3b"])
+def test_golden_reference_products(tmp_path, name):
+    meta = json.load(open(os.path.join(GOLDEN, f"{name}.json")))
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    d = str(tmp_path / name)
+    jn.generate(d, basis_files=False, **meta["config"])
+    H = jn.Hamiltonian.from_dir(d, meta["config"]["Z"], meta["config"]["N"])
+    y = H.matvec(g["x"])
+    assert np.abs(y - g["y"]).max() <= TOL * np.abs(g["y"]).max()
+    H.close()
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
+def test_matches_port_and_accumulates(problem, name):
+    d, Z, N, *_ = problem(name)
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    p = oracle.Port(d)
+    rng = np.random.default_rng(11)
+    x, y0 = rng.standard_normal(H.dimension), rng.standard_normal(H.dimension)
+    want = p.matvec(x, y0.copy())
+    got = H.matvec(x, y0.copy())
+    assert np.abs(got - want).max() <= TOL * np.abs(want).max()
+    H.close()
+    p.close()
+
+
+def test_bit_identical_repeats(problem):
+    d, Z, N, *_ = problem("he4_n6_3b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    x = np.random.default_rng(3).standard_normal(H.dimension)
+    a = H.matvec(x)
+    b = H.matvec(x)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    H.close()
+
+
+def test_unit_vector_products_rebuild_dense_h(problem):
+    from oracle import dense_h
+    d, Z, N, nmax, nbody = problem("he4_n2_3b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    D = H.dimension
+    M = np.column_stack([H.matvec(np.eye(D)[j]) for j in range(D)])
+    Hd = dense_h.build_dense_h(d, Z, N, nmax, nbody=nbody)
+    assert np.abs(M - Hd).max() <= TOL * np.abs(Hd).max()
+    H.close()
+
+
+def test_file_level_drop_in(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n4_2b")
+    blocks = oracle.read_blocks(d)
+    D = sum(a * b for _, a, b in blocks)
+    rng = np.random.default_rng(4)
+    x, y0 = rng.standard_normal(D), rng.standard_normal(D)
+    oracle.write_vector_dir(str(tmp_path / "in"), blocks, x)
+    oracle.write_vector_dir(str(tmp_path / "out"), blocks, y0)
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.matvec_files(str(tmp_path / "out"), str(tmp_path / "in"))
+    got = oracle.read_vector_dir(str(tmp_path / "out"), blocks)
+    want = oracle.Port(d).matvec(x, y0.copy())
+    assert np.abs(got - want).max() <= TOL * np.abs(want).max()
+    H.close()
+
+
+def test_open_errors_are_status_codes(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    with pytest.raises(jn.JnError) as e:
+        jn.Hamiltonian(comb=f"{d}/nope.txt", order=f"{d}/evaluation_order.txt", lists=f"{d}/index_lists",
+                       mes=f"{d}/matrix_elements", Z=Z, N=N)
+    assert e.value.status == 2
+
+
+def test_runfile_open(problem):
+    d, Z, N, *_ = problem("he4_n2_3b")
+    H = jn.Hamiltonian(f"{d}/bacchus.conf")
+    x = np.random.default_rng(2).standard_normal(H.dimension)
+    want = oracle.Port(d).matvec(x)
+    assert np.abs(H.matvec(x) - want).max() <= TOL * np.abs(want).max()
+    H.close()

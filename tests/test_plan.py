@@ -1,0 +1,114 @@
+"""The device plan (CSR views, terms, tiles, chunks) executed on the CPU by a
+statement-for-statement model of the kernels, against the oracle; and the
+host-side validation that keeps every device access in bounds."""
+import ctypes
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import oracle
+
+EMU = os.path.join(os.path.dirname(__file__), "_build", "libplan_emu.so")
+
+
+def emu_lib():
+    L = ctypes.CDLL(EMU)
+    L.emu_open.restype = ctypes.c_void_p
+    L.emu_open.argtypes = [ctypes.c_char_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_char_p, ctypes.c_int]
+    L.emu_matvec.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int]
+    L.emu_dimension.restype = ctypes.c_long
+    L.emu_dimension.argtypes = [ctypes.c_void_p]
+    L.emu_units.argtypes = [ctypes.c_void_p]
+    L.emu_close.argtypes = [ctypes.c_void_p]
+    return L
+
+
+def open_plan(d, Z, N, units=1216):
+    L = emu_lib()
+    err = ctypes.create_string_buffer(2048)
+    e = lambda s: s.encode()
+    h = L.emu_open(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                   e(f"{d}/matrix_elements"), Z, N, units, err, 2048)
+    return L, h, err.value.decode()
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b"])
+@pytest.mark.parametrize("units", [1, 64, 1216])
+def test_plan_matches_port(problem, name, units):
+    d, Z, N, *_ = problem(name)
+    L, h, err = open_plan(d, Z, N, units)
+    assert h, err
+    D = L.emu_dimension(h)
+    p = oracle.Port(d)
+    rng = np.random.default_rng(units)
+    x, y0 = rng.standard_normal(D), rng.standard_normal(D)
+    a = y0.copy()
+    L.emu_matvec(h, x.ctypes.data, a.ctypes.data, 1)
+    b = p.matvec(x, y0.copy())
+    assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    c = np.full(D, np.nan)
+    L.emu_matvec(h, x.ctypes.data, c.ctypes.data, 0)
+    assert np.abs(c - (b - y0)).max() <= 1e-12 * np.abs(b).max()
+    L.emu_close(h)
+    p.close()
+
+
+def corrupt_copy(src, dst):
+    shutil.copytree(src, dst)
+    return dst
+
+
+def first_list(d):
+    return sorted(os.listdir(f"{d}/index_lists"), key=lambda s: int(s.split("_")[-1]))[0]
+
+
+def test_rejects_out_of_range_index(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    f = f"{c}/index_lists/{first_list(c)}"
+    a = np.fromfile(f, dtype=np.int32)
+    a[1] = 1 << 20
+    a.tofile(f)
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "outside" in err
+
+
+def test_rejects_out_of_range_matrix_index(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    f = f"{c}/index_lists/{first_list(c)}"
+    a = np.fromfile(f, dtype=np.uint32)
+    a[2] = 0x80000000 | 0x7ffffff0
+    a.tofile(f)
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "matrix index" in err
+
+
+def test_rejects_truncated_list(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    f = f"{c}/index_lists/{first_list(c)}"
+    open(f, "ab").write(b"\x01\x02")
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "whole index triples" in err
+
+
+def test_rejects_short_matrix_file(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    name = sorted(os.listdir(f"{c}/matrix_elements"))[0]
+    f = f"{c}/matrix_elements/{name}"
+    raw = open(f, "rb").read()
+    open(f, "wb").write(raw[:-8])
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "matrix" in err
+
+
+def test_missing_file_reports_path(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    os.remove(f"{c}/index_lists/{first_list(c)}")
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "Could not open" in err
