@@ -166,6 +166,7 @@ def main():
     ap.add_argument("--workload", default="he4_nmax6_2nf3nf", choices=sorted(WORKLOADS))
     ap.add_argument("--workdir", default=os.environ.get("JNCSM_BENCH_DIR", os.path.join(tempfile.gettempdir(), "jncsm_bench")))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -205,43 +206,60 @@ def main():
     H = jn.Hamiltonian.from_dir(d, w["Z"], w["N"])
     st = H.stats()
     D = H.dimension
-    bytes_step = st["algorithmic_bytes"]
     dev = torch.device("cuda", local)
-    x = torch.randn(D, dtype=torch.float64, device=dev)
+    x = torch.randn(D, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
     y = torch.zeros(D, dtype=torch.float64, device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    # bytes of one product: lists (12 B/entry), referenced matrix elements (8 or 4 B), x and y (FP64)
+    me_bytes = {64: 8, 32: 4}
 
-    def step():
-        flush.zero_()
+    def bytes_for(prec):
+        return 12.0 * st["list_entries"] + me_bytes[prec] * st["me_referenced"] + 16.0 * D
+
+    def timed(prec):
+        H.set_precision(prec)
+
+        def step():
+            flush.zero_()
+            torch.cuda.synchronize()
+            return H.matvec_profile(x.data_ptr(), y.data_ptr(), accumulate=False)
+
+        for _ in range(args.warmup):
+            step()
+        sampler = ClockSampler(local)
+        sampler.start()
+        if dist:
+            dist.barrier()
         torch.cuda.synchronize()
-        return H.matvec_profile(x.data_ptr(), y.data_ptr(), accumulate=False)
+        kern_ms, total_ms = 0.0, 0.0
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            a, b = step()
+            kern_ms += a
+            total_ms += a + b
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        wall = time.perf_counter() - wall0
+        clocks = sampler.stop()
+        t_max = total_ms
+        if dist:
+            t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_max = float(t.item())
+        return {"ms_per_step": t_max / args.steps, "kernel_ms": kern_ms / args.steps, "wall_s": wall,
+                "clocks": clocks, "y": y.clone()}
 
-    for _ in range(args.warmup):
-        step()
-    sampler = ClockSampler(local)
-    sampler.start()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    units_ms, total_ms = 0.0, 0.0
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        a, b = step()
-        units_ms += a
-        total_ms += a + b
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    wall = time.perf_counter() - wall0
-    clocks = sampler.stop()
-    t_max = total_ms
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = bytes_step * args.steps * world / (t_max / 1e3) / 1e9
+    r64 = timed(64)
+    r32 = timed(32)
+    rel32 = float((r32["y"] - r64["y"]).abs().max() / r64["y"].abs().max())
+    prec = args.precision
+    main_r = r64 if prec == 64 else r32
+    bytes_step = bytes_for(prec)
+    value = bytes_step * world / (main_r["ms_per_step"] / 1e3) / 1e9
 
     # end to end through the public host-pointer call, pinned host buffers
+    H.set_precision(prec)
     hx = torch.randn(D, dtype=torch.float64).pin_memory().numpy()
     hy = torch.zeros(D, dtype=torch.float64).pin_memory().numpy()
     for _ in range(args.warmup):
@@ -257,27 +275,40 @@ def main():
 
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    achieved = bytes_step / (units_ms / args.steps / 1e3) / 1e9
+    achieved = bytes_step / (main_r["kernel_ms"] / 1e3) / 1e9
     traffic = profile_traffic(args.workload)
+
+    def path_summary(r, p):
+        b = bytes_for(p)
+        return {"ms_per_step": r["ms_per_step"], "GB_per_s": b / (r["ms_per_step"] / 1e3) / 1e9,
+                "bytes_per_step": b, "gather_kernel_ms": r["kernel_ms"],
+                "hbm_frac": b / (r["kernel_ms"] / 1e3) / 1e9 / peak,
+                "fp64_multiply_adds_per_s" if p == 64 else "multiply_adds_per_s":
+                    st["multiply_adds"] / (r["kernel_ms"] / 1e3)}
+
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "warmup": args.warmup, "ms_per_step": main_r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == 64 else "f32 (matrix elements and x; compensated sums; f64 in/out)",
+            "data": "synthetic",
             "config": {"workload": w["label"], "dimension": D, "instructions": st["num_instructions"],
                        "list_entries": st["list_entries"], "me_elements": st["me_elements"],
                        "me_elements_referenced": st["me_referenced"],
                        "multiply_adds": st["multiply_adds"], "bytes_per_step": bytes_step,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
-                       "wall_s": wall},
+                       "precision": prec, "work_units": st["num_work_units"], "pieces": st["num_tiles"]},
+            "paths": {"fp64": path_summary(r64, 64), "fp32": path_summary(r32, 32),
+                      "fp32_max_rel_diff_vs_fp64": rel32},
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * D, "d2h_bytes_per_step": 8 * D},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": (2 if prec == 64 else 3) * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
-                         "kernel": "jn_units_kernel"},
-            "clocks": clocks}
+                         "kernel": "jn_pieces_kernel"},
+            "clocks": main_r["clocks"]}
     if rank == 0:
         try:
-            line["cpu_baseline"] = cpu_baseline(d, w, bytes_step, seconds=args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline(d, w, bytes_for(64), seconds=args.cpu_seconds)
         except Exception as e:  # the baseline must never hide the GPU line
             line["cpu_baseline"] = {"error": str(e)}
         print(json.dumps(line), flush=True)

@@ -52,6 +52,28 @@ const char *jn_version(void);
  */
 jn_status jn_open(const char *bacchus_conf, jn_ctx **ctx);
 
+/* The Bacchus run file (libconfig syntax) as the reference reads it
+ * (Bacchus/settings/settings.c:79-211), plus an optional `gpu` group that the
+ * reference ignores: gpu.num_eigenvalues, gpu.precision ("fp64"/"fp32"),
+ * gpu.reorthogonalize ("full"/"partial"). */
+typedef struct {
+	char combination_table_file[4096];
+	char evaluation_order_file[4096];
+	char index_lists_base_directory[4096];
+	char matrix_file_base_directory[4096];
+	int num_protons, num_neutrons;
+	char krylow_vector_directory[4096];
+	int max_num_lanczos_iterations;
+	double convergence_tolerance;
+	int target_eigenvector;
+	int converge_eigenvectors;
+	char eigenvector_directory[4096];
+	int gpu_num_eigenvalues;
+	int gpu_precision;              /* 64 or 32 */
+	int gpu_full_reorthogonalization;
+} jn_run_settings;
+jn_status jn_read_settings(const char *bacchus_conf, jn_run_settings *settings);
+
 /* The same from explicit paths (Z protons, N neutrons). */
 jn_status jn_open_files(const char *combination_table_file, const char *evaluation_order_file,
 			const char *index_lists_base_directory, const char *matrix_file_base_directory,
@@ -94,6 +116,14 @@ jn_status jn_matvec_files(jn_ctx *ctx, const char *output_vector_directory, cons
  * ms[1] the ordered reduction).  Used for roofline accounting. */
 jn_status jn_matvec_profile(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, float ms[2]);
 
+/* Arithmetic of the products of this context: 64 (default) computes every
+ * multiply-add in FP64; 32 uses FP32 copies of the matrix elements and of x,
+ * sums each term in FP32 and combines the terms with error-free (TwoSum)
+ * compensation; x and y stay FP64 at the interface.  Matrix elements of
+ * single-species blocks below 1e-12 in magnitude are stored as zero in the
+ * FP32 copy, which is the reference's skip (matrix_vector_multiplication.c:52-53). */
+jn_status jn_set_precision(jn_ctx *ctx, int precision);
+
 /* Synchronise the context's stream. */
 jn_status jn_synchronize(jn_ctx *ctx);
 
@@ -121,6 +151,63 @@ jn_status jn_get_plan_stats(const jn_ctx *ctx, jn_plan_stats *stats);
 jn_status jn_inspect_files(const char *combination_table_file, const char *evaluation_order_file,
 			   const char *index_lists_base_directory, const char *matrix_file_base_directory,
 			   int num_protons, int num_neutrons, jn_plan_stats *stats);
+
+/* ------------------------------------------------------------------ */
+/* Lanczos (Bacchus/lanczos/lanczos.c)                                 */
+/* ------------------------------------------------------------------ */
+#define JN_MAX_REPORTED 64
+
+typedef enum {
+	/* full reorthogonalisation; converged when min(r, r^2/gap) < tolerance
+	 * for each of the num_eigenvalues lowest Ritz values */
+	JN_LANCZOS_FULL = 0,
+	/* the reference's algorithm: start e_0, reorthogonalise v_{k+1} against
+	 * v_0..v_{k-3} only, converged when the lowest Ritz value moves by less
+	 * than tolerance (lanczos.c:60-253) */
+	JN_LANCZOS_REFERENCE = 1
+} jn_lanczos_mode;
+
+typedef struct {
+	int max_iterations;            /* lanczos.max_num_lanczos_iterations */
+	int num_eigenvalues;           /* lowest eigenpairs wanted (<= JN_MAX_REPORTED) */
+	double tolerance;              /* lanczos.convergence_tolerance (MeV) */
+	int mode;                      /* jn_lanczos_mode */
+	int check_every;               /* convergence test interval (1 = every step) */
+	const double *start_vector;    /* host, length D; NULL = e_0 as the reference */
+	int verbose;                   /* per-iteration lines on stdout */
+} jn_lanczos_options;
+
+typedef struct {
+	int iterations;                /* Krylov dimension reached */
+	int converged;
+	int num_ritz_values;           /* = iterations */
+	int num_eigenvalues;           /* entries filled below */
+	double eigenvalues[JN_MAX_REPORTED];    /* Rayleigh quotients of the Ritz vectors (FP64 products) */
+	double ritz_values[JN_MAX_REPORTED];    /* eigenvalues of the tridiagonal matrix */
+	double residual_norms[JN_MAX_REPORTED]; /* |H x - rq x| / |x| */
+} jn_lanczos_result;
+
+/* Run Lanczos on the context's Hamiltonian.  Replaces new_lanczos_environment
+ * + diagonalize (Bacchus/lanczos/lanczos.c:37-253).  The Krylov basis stays
+ * on the device.  Returns JN_ERR_NOT_CONVERGED (results still filled) when
+ * JN_LANCZOS_FULL stops at max_iterations. */
+jn_status jn_lanczos(jn_ctx *ctx, const jn_lanczos_options *options, jn_lanczos_result *result);
+
+/* All Ritz values of the last solve in ascending order, as get_eigensystem +
+ * print_eigensystem report them (lanczos.c:255-265, eigensystem.c:99-113). */
+jn_status jn_lanczos_ritz_values(jn_ctx *ctx, double *out, int capacity, int *count);
+
+/* Ritz vector i (0 = lowest) of the last solve, full length D, host memory
+ * (get_eigenvector, Bacchus/eigensystem/eigensystem.c:86-97). */
+jn_status jn_lanczos_eigenvector(jn_ctx *ctx, int i, double *host_out);
+
+/* Write Ritz vectors 0..count-1 as <directory>/eigenvector_<i+1>/vec_<b>
+ * (Bacchus/programs/bacchus.c:68-87). */
+jn_status jn_lanczos_save_eigenvectors(jn_ctx *ctx, const char *directory, int count);
+
+/* Print the eigensystem block exactly as print_eigensystem does
+ * (Bacchus/eigensystem/eigensystem.c:99-113) for the given values. */
+void jn_print_eigensystem(const double *eigenvalues, int count);
 
 #ifdef __cplusplus
 }

@@ -22,6 +22,7 @@ LIBDIR = os.path.join(HERE, "lib")
 GPU_LIB = os.path.join(LIBDIR, "libjncsm_gpu.so")
 GEN_LIB = os.path.join(LIBDIR, "libjncsm_gen.so")
 GEN_CLI = os.path.join(LIBDIR, "jn_gen")
+BACCHUS_CLI = os.path.join(LIBDIR, "jn_bacchus")
 
 JN_OK = 0
 STATUS_NAMES = {0: "JN_OK", 1: "JN_ERR_INVALID", 2: "JN_ERR_IO", 3: "JN_ERR_FORMAT", 4: "JN_ERR_CUDA",
@@ -44,6 +45,22 @@ class PlanStats(ctypes.Structure):
                 ("list_entries", ctypes.c_size_t), ("me_elements", ctypes.c_size_t),
                 ("me_referenced", ctypes.c_size_t), ("multiply_adds", ctypes.c_double), ("algorithmic_bytes", ctypes.c_double),
                 ("num_work_units", ctypes.c_int), ("num_tiles", ctypes.c_int)]
+
+
+MAX_REPORTED = 64
+LANCZOS_FULL, LANCZOS_REFERENCE = 0, 1
+
+
+class LanczosOptions(ctypes.Structure):
+    _fields_ = [("max_iterations", ctypes.c_int), ("num_eigenvalues", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("mode", ctypes.c_int), ("check_every", ctypes.c_int), ("start_vector", ctypes.c_void_p),
+                ("verbose", ctypes.c_int)]
+
+
+class LanczosResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("num_ritz_values", ctypes.c_int),
+                ("num_eigenvalues", ctypes.c_int), ("eigenvalues", ctypes.c_double * MAX_REPORTED),
+                ("ritz_values", ctypes.c_double * MAX_REPORTED), ("residual_norms", ctypes.c_double * MAX_REPORTED)]
 
 
 _gpu = None
@@ -75,8 +92,16 @@ def gpu_lib():
     L.jn_matvec_profile.argtypes = [vp, vp, vp, ci, ctypes.POINTER(ctypes.c_float)]
     L.jn_get_plan_stats.argtypes = [vp, ctypes.POINTER(PlanStats)]
     L.jn_inspect_files.argtypes = [cp, cp, cp, cp, ci, ci, ctypes.POINTER(PlanStats)]
+    L.jn_set_precision.argtypes = [vp, ci]
+    L.jn_lanczos.argtypes = [vp, ctypes.POINTER(LanczosOptions), ctypes.POINTER(LanczosResult)]
+    L.jn_lanczos_ritz_values.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ci, ctypes.POINTER(ci)]
+    L.jn_lanczos_eigenvector.argtypes = [vp, ci, vp]
+    L.jn_lanczos_save_eigenvectors.argtypes = [vp, cp, ci]
+    L.jn_print_eigensystem.argtypes = [ctypes.POINTER(ctypes.c_double), ci]
+    L.jn_print_eigensystem.restype = None
     for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
-                 "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files"):
+                 "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_lanczos",
+                 "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors"):
         getattr(L, name).restype = ci
     _gpu = L
     return L
@@ -137,6 +162,42 @@ class Hamiltonian:
         ms = (ctypes.c_float * 2)()
         _check(gpu_lib().jn_matvec_profile(self._h, ctypes.c_void_p(d_x), ctypes.c_void_p(d_y), int(accumulate), ms))
         return ms[0], ms[1]
+
+    def set_precision(self, bits):
+        """64: FP64 products (default); 32: FP32 matrix elements and x with compensated sums."""
+        _check(gpu_lib().jn_set_precision(self._h, int(bits)))
+
+    def lanczos(self, max_iterations=200, num_eigenvalues=10, tolerance=1e-6, mode=LANCZOS_FULL, check_every=1,
+                start_vector=None, verbose=False, allow_unconverged=False):
+        """Run Lanczos on the GPU; returns a dict with eigenvalues (refined), Ritz values, residuals."""
+        o = LanczosOptions(max_iterations, num_eigenvalues, tolerance, mode, check_every, None, int(verbose))
+        sv = None
+        if start_vector is not None:
+            sv = np.ascontiguousarray(start_vector, dtype=np.float64)
+            o.start_vector = sv.ctypes.data
+        r = LanczosResult()
+        st = gpu_lib().jn_lanczos(self._h, ctypes.byref(o), ctypes.byref(r))
+        if st != JN_OK and not (allow_unconverged and st == 6):
+            _check(st)
+        n = r.num_eigenvalues
+        return {"iterations": r.iterations, "converged": bool(r.converged), "num_ritz_values": r.num_ritz_values,
+                "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
+                "residual_norms": np.array(r.residual_norms[:n]), "status": st}
+
+    def ritz_values(self):
+        cap = 4096
+        out = (ctypes.c_double * cap)()
+        cnt = ctypes.c_int()
+        _check(gpu_lib().jn_lanczos_ritz_values(self._h, out, cap, ctypes.byref(cnt)))
+        return np.array(out[:min(cnt.value, cap)])
+
+    def eigenvector(self, i):
+        v = np.zeros(self.dimension)
+        _check(gpu_lib().jn_lanczos_eigenvector(self._h, int(i), v.ctypes.data))
+        return v
+
+    def save_eigenvectors(self, directory, count):
+        _check(gpu_lib().jn_lanczos_save_eigenvectors(self._h, directory.encode(), int(count)))
 
     def matvec_files(self, out_dir, in_dir):
         _check(gpu_lib().jn_matvec_files(self._h, out_dir.encode(), in_dir.encode()))

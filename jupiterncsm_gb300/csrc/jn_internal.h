@@ -1,0 +1,52 @@
+/*
+ * jn_internal.h — state shared by the CUDA translation units of
+ * libjncsm_gpu.so (not part of the public ABI).
+ */
+#ifndef JN_INTERNAL_H
+#define JN_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include "../../include/jncsm.h"
+#include "jn_problem.h"
+
+/* records the message of a failure for jn_last_error() and returns s */
+jn_status jn_fail(jn_status s, const char *fmt, ...);
+
+#define CUDA_TRY(call)                                                                          \
+	do {                                                                                    \
+		cudaError_t e_ = (call);                                                        \
+		if (e_ != cudaSuccess)                                                          \
+			return jn_fail(JN_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+	} while (0)
+
+struct jn_lanczos_state;
+
+struct jn_ctx {
+	jn_plan_t plan;
+	int device;
+	int num_sms;
+	cudaStream_t stream;
+	uint32_t *d_rowptr;
+	uint2 *d_ent;
+	double *d_me;
+	jn_term_t *d_terms;
+	jn_tile_t *d_tiles;
+	jn_unit_t *d_units;
+	int32_t *d_unit_terms;
+	double *d_partial;
+	double *d_x, *d_y;      /* staging for the host-pointer entry points */
+	double *h_pinned;       /* pinned staging for host copies */
+	int precision;          /* 64: FP64 products; 32: FP32 matrix elements and x, compensated sums */
+	float *d_me32;          /* FP32 copy of the matrix elements (built on first FP32 use) */
+	float *d_x32;
+	struct jn_lanczos_state *lz;
+};
+
+/* enqueue y (+)= H x on stream st */
+jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st);
+
+/* release the Lanczos state of a context */
+void jn_lanczos_release(jn_ctx *c);
+
+#endif

@@ -1,0 +1,591 @@
+/*
+ * jn_lanczos.cu — the Lanczos eigensolver of Bacchus on the GPU, in FP64.
+ *
+ * Reference: src/Bacchus/lanczos/lanczos.c.  One iteration
+ * (lanczos_iteration, :74-153) is
+ *     w = H v_k;  alpha_k = <v_k|w>;  w -= alpha_k v_k + beta_{k-1} v_{k-1};
+ *     beta_k = |w|;  v_{k+1} = w / beta_k
+ * followed by reorthogonalisation (orthogonalize_krylow_basis, :155-169) and
+ * the eigen-decomposition of the tridiagonal matrix (diagonalize, :171-253;
+ * dsteqr in src/Bacchus/diagonalization/diagonalization.c:16-68).
+ *
+ * Two modes:
+ *   JN_LANCZOS_REFERENCE  the reference's choices: start vector e_0
+ *                         (lanczos.c:60-72), reorthogonalisation of
+ *                         v_{k+1} against v_0..v_{k-3} only, without
+ *                         renormalising (lanczos.c:155-169,
+ *                         vector.c:461-476), convergence when the target
+ *                         (ground-state) Ritz value moves by less than the
+ *                         tolerance (lanczos.c:199-235).
+ *   JN_LANCZOS_FULL       full reorthogonalisation (classical Gram-Schmidt,
+ *                         applied twice) and convergence when the error
+ *                         bound min(r, r^2/gap) of each of the lowest `nev`
+ *                         Ritz values is below the tolerance, r being the
+ *                         residual norm beta_k |s_{k,i}|.
+ *
+ * The Krylov basis stays in HBM.  Every reduction is a two-pass fixed-order
+ * reduction, so two runs give bit-identical alpha/beta.  The tridiagonal
+ * eigenvalues are computed on the GPU by Sturm-sequence bisection (one
+ * thread per eigenvalue) and the eigenvectors by inverse iteration on the
+ * tridiagonal matrix; the final Ritz vectors are refined by FP64 products
+ * (Rayleigh quotient and residual norm).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+#include <sys/types.h>
+
+#include "jn_internal.h"
+
+#define RED_BLOCKS 304      /* 2 x 152 SMs */
+#define RED_THREADS 256
+
+struct jn_lanczos_state {
+	int64_t D;
+	int mmax;               /* allocated Krylov dimension (vectors mmax+1) */
+	int k;                  /* Lanczos steps done */
+	int nev;
+	double *d_V;            /* (mmax+1) x D */
+	double *d_w;
+	double *d_alpha, *d_beta;
+	double *d_part;         /* RED_BLOCKS x (mmax+2) partials */
+	double *d_h;            /* mmax+2 coefficients */
+	double *d_scalar;       /* 4 scalars */
+	double *d_theta;        /* Ritz values (ascending), mmax */
+	double *d_Z;            /* nev_cap x mmax tridiagonal eigenvectors */
+	double *d_ritz;         /* nev x D Ritz vectors */
+	double *h_alpha, *h_beta;
+	double *h_theta;
+	double *h_zlast;        /* bottom components */
+	int nev_cap;
+	int have_ritz;
+	double *h_rq, *h_res;   /* refined Rayleigh quotients and residual norms */
+};
+
+void jn_lanczos_release(jn_ctx *c)
+{
+	struct jn_lanczos_state *s = c->lz;
+	if (!s) return;
+	cudaFree(s->d_V); cudaFree(s->d_w); cudaFree(s->d_alpha); cudaFree(s->d_beta); cudaFree(s->d_part);
+	cudaFree(s->d_h); cudaFree(s->d_scalar); cudaFree(s->d_theta); cudaFree(s->d_Z); cudaFree(s->d_ritz);
+	free(s->h_alpha); free(s->h_beta); free(s->h_theta); free(s->h_zlast); free(s->h_rq); free(s->h_res);
+	free(s);
+	c->lz = NULL;
+}
+
+/* ------------------------------------------------------------------ */
+/* BLAS-1/2 kernels with fixed reduction order                         */
+/* ------------------------------------------------------------------ */
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+	const int t = threadIdx.x;
+	sh[t] = v;
+	__syncthreads();
+	for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+		if (t < s) sh[t] += sh[t + s];
+		__syncthreads();
+	}
+	double r = sh[0];
+	__syncthreads();
+	return r;
+}
+
+/* part[b*ncol + j] = sum over this block's slice of V[j] . w, j < nvec */
+__global__ void __launch_bounds__(RED_THREADS) k_gemv_t(const double *__restrict__ V, int64_t D, int nvec,
+							 const double *__restrict__ w, double *__restrict__ part, int ncol)
+{
+	__shared__ double sh[RED_THREADS];
+	const int64_t chunk = (D + gridDim.x - 1) / gridDim.x;
+	const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(D, i0 + chunk);
+	for (int j = 0; j < nvec; j++) {
+		const double *v = V + (int64_t)j * D;
+		double s = 0.0;
+		for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
+		s = block_sum(s, sh);
+		if (threadIdx.x == 0) part[(int64_t)blockIdx.x * ncol + j] = s;
+	}
+}
+
+/* out[j] = sum_b part[b*ncol + j] in block order; optional scale */
+__global__ void k_finish(const double *__restrict__ part, int nblk, int ncol, int nvec, double *__restrict__ out)
+{
+	int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j >= nvec) return;
+	double s = 0.0;
+	for (int b = 0; b < nblk; b++) s += part[(int64_t)b * ncol + j];
+	out[j] = s;
+}
+
+/* w -= sum_j V[j] h[j] (j < nvec) */
+__global__ void k_gemv_n_sub(const double *__restrict__ V, int64_t D, int nvec, const double *__restrict__ h,
+			     double *__restrict__ w)
+{
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int j = 0; j < nvec; j++) s = fma(V[(int64_t)j * D + i], h[j], s);
+		w[i] -= s;
+	}
+}
+
+/* out = sum_j V[j] z[j] */
+__global__ void k_gemv_n(const double *__restrict__ V, int64_t D, int nvec, const double *__restrict__ z,
+			 double *__restrict__ out)
+{
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int j = 0; j < nvec; j++) s = fma(V[(int64_t)j * D + i], z[j], s);
+		out[i] = s;
+	}
+}
+
+/* w -= a*v + b*u (reads a = *pa, b = *pb on the device; u may be NULL) */
+__global__ void k_three_term(double *__restrict__ w, const double *__restrict__ v, const double *__restrict__ u,
+			     const double *pa, const double *pb, int64_t D)
+{
+	const double a = *pa, b = pb ? *pb : 0.0;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double r = w[i] - a * v[i];
+		if (u) r -= b * u[i];
+		w[i] = r;
+	}
+}
+
+/* dst = src / sqrt(*nrm2) ; beta_out = sqrt(*nrm2) */
+__global__ void k_normalize(double *__restrict__ dst, const double *__restrict__ src, const double *nrm2,
+			    double *beta_out, int64_t D)
+{
+	const double b = sqrt(*nrm2);
+	if (blockIdx.x == 0 && threadIdx.x == 0 && beta_out) *beta_out = b;
+	const double inv = 1.0 / b;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		dst[i] = src[i] * inv;
+}
+
+__global__ void k_scale_copy(double *__restrict__ dst, const double *__restrict__ src, double s, int64_t D)
+{
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		dst[i] = src[i] * s;
+}
+
+__global__ void k_axpy_neg(double *__restrict__ y, const double *__restrict__ x, const double *pa, int64_t D)
+{
+	const double a = *pa;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		y[i] -= a * x[i];
+}
+
+/* ------------------------------------------------------------------ */
+/* tridiagonal eigenproblem                                            */
+/* ------------------------------------------------------------------ */
+/* number of eigenvalues of T (diag a, offdiag b, order n) below x */
+__device__ int sturm_count(const double *a, const double *b, int n, double x)
+{
+	int c = 0;
+	double q = a[0] - x;
+	if (q < 0) c++;
+	for (int i = 1; i < n; i++) {
+		double qq = q == 0.0 ? 1e-300 : q;
+		q = a[i] - x - b[i - 1] * b[i - 1] / qq;
+		if (q < 0) c++;
+	}
+	return c;
+}
+
+/* theta[i] for i < want: the i-th smallest eigenvalue, by bisection */
+__global__ void k_tri_bisect(const double *__restrict__ a, const double *__restrict__ b, int n, int want,
+			     double *__restrict__ theta)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= want) return;
+	double lo = a[0], hi = a[0];
+	for (int j = 0; j < n; j++) {
+		double r = (j > 0 ? fabs(b[j - 1]) : 0.0) + (j < n - 1 ? fabs(b[j]) : 0.0);
+		lo = fmin(lo, a[j] - r);
+		hi = fmax(hi, a[j] + r);
+	}
+	double span = fmax(fabs(lo), fabs(hi));
+	lo -= 1e-12 * span + 1e-300;
+	hi += 1e-12 * span + 1e-300;
+	for (int it = 0; it < 200; it++) {
+		double mid = 0.5 * (lo + hi);
+		if (mid <= lo || mid >= hi) break;
+		if (sturm_count(a, b, n, mid) > i) hi = mid; else lo = mid;
+	}
+	theta[i] = 0.5 * (lo + hi);
+}
+
+/* eigenvector of T for theta[i] by inverse iteration (LU with partial
+ * pivoting of T - theta I), normalised, component 0 made non-negative as
+ * diagonalization.c:55-58 does.  Z row i holds the n components. */
+__global__ void k_tri_vectors(const double *__restrict__ a, const double *__restrict__ b, int n, int want,
+			      const double *__restrict__ theta, double *__restrict__ Z, int ldz, double *__restrict__ work,
+			      int ldw)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= want) return;
+	double *z = Z + (int64_t)i * ldz;
+	/* work: d (diag of U), u1, u2 (super diagonals of U), l (multipliers), piv flags */
+	double *d = work + (int64_t)i * ldw, *u1 = d + n, *u2 = u1 + n, *l = u2 + n, *pv = l + n;
+	double span = 0.0;
+	for (int j = 0; j < n; j++) span = fmax(span, fabs(a[j]) + (j < n - 1 ? fabs(b[j]) : 0.0));
+	const double eps = 2.2e-16 * fmax(span, 1e-300);
+	const double sh = theta[i];
+	/* factorisation of T - sh I with row interchanges */
+	double dd = a[0] - sh, e = n > 1 ? b[0] : 0.0, f = 0.0;
+	for (int j = 0; j < n - 1; j++) {
+		double sub = b[j];
+		double nd = a[j + 1] - sh, ne = (j + 1 < n - 1) ? b[j + 1] : 0.0;
+		if (fabs(dd) >= fabs(sub)) {
+			pv[j] = 0.0;
+			if (dd == 0.0) dd = eps;
+			double m = sub / dd;
+			l[j] = m;
+			d[j] = dd; u1[j] = e; u2[j] = 0.0;
+			dd = nd - m * e;
+			e = ne;
+		} else {
+			pv[j] = 1.0;
+			double m = dd / sub;
+			l[j] = m;
+			d[j] = sub; u1[j] = nd; u2[j] = ne;
+			dd = e - m * nd;
+			e = -m * ne;
+		}
+		(void)f;
+	}
+	if (dd == 0.0) dd = eps;
+	d[n - 1] = dd; u1[n - 1] = 0.0; u2[n - 1] = 0.0;
+	for (int j = 0; j < n; j++) z[j] = 1.0;
+	for (int iter = 0; iter < 3; iter++) {
+		/* forward: apply L^-1 with the interchanges */
+		for (int j = 0; j < n - 1; j++) {
+			if (pv[j] != 0.0) { double t = z[j]; z[j] = z[j + 1]; z[j + 1] = t - l[j] * z[j]; }
+			else z[j + 1] -= l[j] * z[j];
+		}
+		/* back substitution with U */
+		for (int j = n - 1; j >= 0; j--) {
+			double s = z[j];
+			if (j + 1 < n) s -= u1[j] * z[j + 1];
+			if (j + 2 < n) s -= u2[j] * z[j + 2];
+			z[j] = s / (fabs(d[j]) < eps ? (d[j] < 0 ? -eps : eps) : d[j]);
+		}
+		double nrm = 0.0;
+		for (int j = 0; j < n; j++) nrm = fma(z[j], z[j], nrm);
+		nrm = sqrt(nrm);
+		for (int j = 0; j < n; j++) z[j] /= nrm;
+	}
+	if (z[0] < 0)
+		for (int j = 0; j < n; j++) z[j] = -z[j];
+}
+
+/* modified Gram-Schmidt among the `want` tridiagonal eigenvectors (one CTA),
+ * which repairs inverse-iteration vectors of close eigenvalues */
+__global__ void k_tri_mgs(double *__restrict__ Z, int ldz, int n, int want)
+{
+	__shared__ double sh[RED_THREADS];
+	for (int i = 0; i < want; i++) {
+		double *zi = Z + (int64_t)i * ldz;
+		for (int j = 0; j < i; j++) {
+			const double *zj = Z + (int64_t)j * ldz;
+			double s = 0.0;
+			for (int t = threadIdx.x; t < n; t += blockDim.x) s = fma(zi[t], zj[t], s);
+			s = block_sum(s, sh);
+			for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] -= s * zj[t];
+			__syncthreads();
+		}
+		double s = 0.0;
+		for (int t = threadIdx.x; t < n; t += blockDim.x) s = fma(zi[t], zi[t], s);
+		s = block_sum(s, sh);
+		double inv = 1.0 / sqrt(s);
+		for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] *= inv;
+		__syncthreads();
+		if (threadIdx.x == 0 && zi[0] < 0) sh[0] = -1.0; else if (threadIdx.x == 0) sh[0] = 1.0;
+		__syncthreads();
+		double sg = sh[0];
+		__syncthreads();
+		for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] *= sg;
+		__syncthreads();
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* host driver                                                         */
+/* ------------------------------------------------------------------ */
+static int grid_for(int64_t D) { int64_t g = (D + 255) / 256; return (int)(g < 4096 ? (g > 0 ? g : 1) : 4096); }
+
+/* res = <x|y> into device scalar */
+static void dot_dev(jn_ctx *c, const double *x, const double *y, double *res)
+{
+	struct jn_lanczos_state *s = c->lz;
+	k_gemv_t<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(x, s->D, 1, y, s->d_part, 1);
+	k_finish<<<1, 32, 0, c->stream>>>(s->d_part, RED_BLOCKS, 1, 1, res);
+}
+
+/* w -= V[0..nvec) (V[0..nvec)^T w) */
+static void cgs_pass(jn_ctx *c, int nvec)
+{
+	struct jn_lanczos_state *s = c->lz;
+	if (nvec <= 0) return;
+	int ncol = s->mmax + 2;
+	k_gemv_t<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(s->d_V, s->D, nvec, s->d_w, s->d_part, ncol);
+	k_finish<<<(nvec + 127) / 128, 128, 0, c->stream>>>(s->d_part, RED_BLOCKS, ncol, nvec, s->d_h);
+	k_gemv_n_sub<<<grid_for(s->D), 256, 0, c->stream>>>(s->d_V, s->D, nvec, s->d_h, s->d_w);
+}
+
+static jn_status ensure_state(jn_ctx *c, int mmax, int nev)
+{
+	struct jn_lanczos_state *s = c->lz;
+	int64_t D = c->plan.dim;
+	if (s && s->mmax >= mmax && s->nev_cap >= nev) return JN_OK;
+	jn_lanczos_release(c);
+	s = (struct jn_lanczos_state *)calloc(1, sizeof *s);
+	c->lz = s;
+	s->D = D; s->mmax = mmax; s->nev_cap = nev;
+	size_t ncol = (size_t)mmax + 2;
+	cudaError_t e = cudaSuccess;
+#define DALLOC(ptr, n) if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (size_t)(n) * sizeof(double))
+	DALLOC(s->d_V, (size_t)(mmax + 1) * D);
+	DALLOC(s->d_w, D);
+	DALLOC(s->d_alpha, mmax + 1);
+	DALLOC(s->d_beta, mmax + 1);
+	DALLOC(s->d_part, RED_BLOCKS * ncol);
+	DALLOC(s->d_h, ncol);
+	DALLOC(s->d_scalar, 8);
+	DALLOC(s->d_theta, mmax + 1);
+	DALLOC(s->d_Z, (size_t)nev * (mmax + 1) + (size_t)nev * 5 * (mmax + 1));
+	DALLOC(s->d_ritz, (size_t)nev * D);
+#undef DALLOC
+	if (e != cudaSuccess) {
+		jn_lanczos_release(c);
+		return jn_fail(JN_ERR_NOMEM, "Lanczos workspace (%d vectors of %lld): %s", mmax + 1, (long long)D,
+			       cudaGetErrorString(e));
+	}
+	s->h_alpha = (double *)calloc(mmax + 1, sizeof(double));
+	s->h_beta = (double *)calloc(mmax + 1, sizeof(double));
+	s->h_theta = (double *)calloc(mmax + 1, sizeof(double));
+	s->h_zlast = (double *)calloc(nev + 1, sizeof(double));
+	s->h_rq = (double *)calloc(nev + 1, sizeof(double));
+	s->h_res = (double *)calloc(nev + 1, sizeof(double));
+	return JN_OK;
+}
+
+/* Ritz values of T_n (ascending) for the lowest `want`, and the tridiagonal
+ * eigenvectors when vectors != 0; results copied to the host arrays. */
+static jn_status tri_eig(jn_ctx *c, int n, int want, int vectors)
+{
+	struct jn_lanczos_state *s = c->lz;
+	if (want > n) want = n;
+	k_tri_bisect<<<(want + 63) / 64, 64, 0, c->stream>>>(s->d_alpha, s->d_beta, n, want, s->d_theta);
+	if (vectors) {
+		int ldz = s->mmax + 1;
+		double *work = s->d_Z + (size_t)s->nev_cap * ldz;
+		int w2 = want < s->nev_cap ? want : s->nev_cap;
+		k_tri_vectors<<<(w2 + 31) / 32, 32, 0, c->stream>>>(s->d_alpha, s->d_beta, n, w2, s->d_theta, s->d_Z, ldz,
+								    work, 5 * ldz);
+		k_tri_mgs<<<1, RED_THREADS, 0, c->stream>>>(s->d_Z, ldz, n, w2);
+		for (int i = 0; i < w2; i++)
+			CUDA_TRY(cudaMemcpyAsync(s->h_zlast + i, s->d_Z + (size_t)i * ldz + n - 1, sizeof(double),
+						 cudaMemcpyDeviceToHost, c->stream));
+	}
+	CUDA_TRY(cudaMemcpyAsync(s->h_theta, s->d_theta, want * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+	CUDA_TRY(cudaStreamSynchronize(c->stream));
+	CUDA_TRY(cudaGetLastError());
+	return JN_OK;
+}
+
+extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lanczos_result *res)
+{
+	if (!c || !opt || !res) return jn_fail(JN_ERR_INVALID, "null argument");
+	const int64_t D = c->plan.dim;
+	int m = opt->max_iterations > 0 ? opt->max_iterations : 200;
+	if ((int64_t)m > D) m = (int)D;               /* lanczos.c:181-185 */
+	int nev = opt->num_eigenvalues > 0 ? opt->num_eigenvalues : 10;
+	if (nev > JN_MAX_REPORTED) nev = JN_MAX_REPORTED;
+	if (nev > m) nev = m;
+	const int reference_mode = opt->mode == JN_LANCZOS_REFERENCE;
+	const int check_every = opt->check_every > 0 ? opt->check_every : 1;
+	jn_status st = ensure_state(c, m, nev < 1 ? 1 : nev);
+	if (st) return st;
+	struct jn_lanczos_state *s = c->lz;
+	s->nev = nev;
+	s->have_ritz = 0;
+	cudaStream_t q = c->stream;
+	const int g = grid_for(D);
+	double *V = s->d_V;
+
+	/* v_0 */
+	if (opt->start_vector) {
+		CUDA_TRY(cudaMemcpyAsync(s->d_w, opt->start_vector, D * sizeof(double), cudaMemcpyHostToDevice, q));
+		dot_dev(c, s->d_w, s->d_w, s->d_scalar);
+		k_normalize<<<g, 256, 0, q>>>(V, s->d_w, s->d_scalar, NULL, D);
+	} else {
+		CUDA_TRY(cudaMemsetAsync(V, 0, D * sizeof(double), q));
+		double one = 1.0;
+		CUDA_TRY(cudaMemcpyAsync(V, &one, sizeof(double), cudaMemcpyHostToDevice, q));
+		CUDA_TRY(cudaStreamSynchronize(q));
+	}
+
+	double prev = 0.0;
+	int k, converged = 0;
+	res->iterations = 0;
+	for (k = 0; k < m; k++) {
+		double *vk = V + (int64_t)k * D, *vk1 = V + (int64_t)(k + 1) * D;
+		st = jn_launch_matvec(c, vk, s->d_w, 0, q);
+		if (st) return st;
+		dot_dev(c, vk, s->d_w, s->d_alpha + k);
+		k_three_term<<<g, 256, 0, q>>>(s->d_w, vk, k ? V + (int64_t)(k - 1) * D : NULL, s->d_alpha + k,
+					       k ? s->d_beta + k - 1 : NULL, D);
+		if (!reference_mode) {
+			cgs_pass(c, k + 1);
+			cgs_pass(c, k + 1);
+		}
+		dot_dev(c, s->d_w, s->d_w, s->d_scalar);
+		k_normalize<<<g, 256, 0, q>>>(vk1, s->d_w, s->d_scalar, s->d_beta + k, D);
+		if (reference_mode && k > 2) {
+			/* MGS of v_{k+1} against v_0..v_{k-3}, no renormalisation (vector.c:461-476) */
+			for (int j = 0; j + 2 < k; j++) {
+				dot_dev(c, vk1, V + (int64_t)j * D, s->d_scalar + 1);
+				k_axpy_neg<<<g, 256, 0, q>>>(vk1, V + (int64_t)j * D, s->d_scalar + 1, D);
+			}
+		}
+		CUDA_TRY(cudaGetLastError());
+		const int n = k + 1;
+		if ((n % check_every) && n < m) continue;
+		CUDA_TRY(cudaMemcpyAsync(s->h_alpha, s->d_alpha, n * sizeof(double), cudaMemcpyDeviceToHost, q));
+		CUDA_TRY(cudaMemcpyAsync(s->h_beta, s->d_beta, n * sizeof(double), cudaMemcpyDeviceToHost, q));
+		if (reference_mode) {
+			st = tri_eig(c, n, 1, 0);
+			if (st) return st;
+			double diff = fabs(s->h_theta[0] - prev);
+			prev = s->h_theta[0];
+			if (opt->verbose)
+				printf("Lanczos iteration %d: lowest Ritz value %.17lg, difference %lg\n", n, s->h_theta[0], diff);
+			if (diff < opt->tolerance) { converged = 1; k++; break; }
+		} else {
+			int want = nev < n ? nev : n;
+			st = tri_eig(c, n, want + (want < n ? 1 : 0), 1);
+			if (st) return st;
+			int ok = n >= nev;
+			double beta = s->h_beta[n - 1];
+			for (int i = 0; i < want && ok; i++) {
+				double r = fabs(beta * s->h_zlast[i]);
+				double gap = 1e300;
+				if (i > 0) gap = fmin(gap, s->h_theta[i] - s->h_theta[i - 1]);
+				if (i + 1 < want + (want < n ? 1 : 0)) gap = fmin(gap, s->h_theta[i + 1] - s->h_theta[i]);
+				double bound = fmin(r, r * r / fmax(gap, 1e-300));
+				if (!(bound < opt->tolerance)) ok = 0;
+			}
+			if (opt->verbose)
+				printf("Lanczos iteration %d: lowest Ritz value %.17lg, beta %lg\n", n, s->h_theta[0], beta);
+			if (ok || beta == 0.0) { converged = 1; k++; break; }
+		}
+	}
+	s->k = k;
+	res->iterations = k;
+	res->converged = converged;
+	/* final decomposition of T_k: all Ritz values, vectors of the lowest nev */
+	CUDA_TRY(cudaMemcpyAsync(s->h_alpha, s->d_alpha, k * sizeof(double), cudaMemcpyDeviceToHost, q));
+	CUDA_TRY(cudaMemcpyAsync(s->h_beta, s->d_beta, k * sizeof(double), cudaMemcpyDeviceToHost, q));
+	int want = nev < k ? nev : k;
+	st = tri_eig(c, k, k, 0);
+	if (st) return st;
+	res->num_ritz_values = k;
+	st = tri_eig(c, k, want, 1);
+	if (st) return st;
+	/* Ritz vectors x_i = sum_j z_i[j] v_j and their FP64 refinement */
+	int ldz = s->mmax + 1;
+	for (int i = 0; i < want; i++)
+		k_gemv_n<<<g, 256, 0, q>>>(V, D, k, s->d_Z + (size_t)i * ldz, s->d_ritz + (size_t)i * D);
+	s->have_ritz = 1;
+	for (int i = 0; i < want; i++) {
+		double *xi = s->d_ritz + (size_t)i * D;
+		st = jn_launch_matvec(c, xi, s->d_w, 0, q);
+		if (st) return st;
+		dot_dev(c, xi, s->d_w, s->d_scalar + 0);
+		dot_dev(c, xi, xi, s->d_scalar + 1);
+		double h2[2];
+		CUDA_TRY(cudaMemcpyAsync(h2, s->d_scalar, 2 * sizeof(double), cudaMemcpyDeviceToHost, q));
+		CUDA_TRY(cudaStreamSynchronize(q));
+		double rq = h2[0] / h2[1];
+		s->h_rq[i] = rq;
+		/* r = H x - rq x */
+		CUDA_TRY(cudaMemcpyAsync(s->d_scalar + 2, &rq, sizeof(double), cudaMemcpyHostToDevice, q));
+		k_axpy_neg<<<g, 256, 0, q>>>(s->d_w, xi, s->d_scalar + 2, D);
+		dot_dev(c, s->d_w, s->d_w, s->d_scalar + 3);
+		double r2;
+		CUDA_TRY(cudaMemcpyAsync(&r2, s->d_scalar + 3, sizeof(double), cudaMemcpyDeviceToHost, q));
+		CUDA_TRY(cudaStreamSynchronize(q));
+		s->h_res[i] = sqrt(r2 / h2[1]);
+	}
+	CUDA_TRY(cudaGetLastError());
+	res->num_eigenvalues = want;
+	for (int i = 0; i < want && i < JN_MAX_REPORTED; i++) {
+		res->eigenvalues[i] = s->h_rq[i];
+		res->ritz_values[i] = s->h_theta[i];
+		res->residual_norms[i] = s->h_res[i];
+	}
+	return converged ? JN_OK : (opt->mode == JN_LANCZOS_REFERENCE ? JN_OK : jn_fail(JN_ERR_NOT_CONVERGED,
+		"Lanczos did not converge in %d iterations", k));
+}
+
+extern "C" jn_status jn_lanczos_ritz_values(jn_ctx *c, double *out, int capacity, int *count)
+{
+	if (!c || !c->lz || !out) return jn_fail(JN_ERR_INVALID, "no Lanczos solve on this context");
+	struct jn_lanczos_state *s = c->lz;
+	jn_status st = tri_eig(c, s->k, s->k, 0);
+	if (st) return st;
+	int n = s->k < capacity ? s->k : capacity;
+	memcpy(out, s->h_theta, n * sizeof(double));
+	if (count) *count = s->k;
+	return JN_OK;
+}
+
+extern "C" jn_status jn_lanczos_eigenvector(jn_ctx *c, int i, double *host_out)
+{
+	if (!c || !c->lz || !c->lz->have_ritz || !host_out) return jn_fail(JN_ERR_INVALID, "no Ritz vectors on this context");
+	struct jn_lanczos_state *s = c->lz;
+	if (i < 0 || i >= s->nev || i >= s->k) return jn_fail(JN_ERR_INVALID, "eigenvector index out of range");
+	CUDA_TRY(cudaMemcpyAsync(host_out, s->d_ritz + (size_t)i * s->D, s->D * sizeof(double), cudaMemcpyDeviceToHost,
+				 c->stream));
+	CUDA_TRY(cudaStreamSynchronize(c->stream));
+	return JN_OK;
+}
+
+extern "C" jn_status jn_lanczos_save_eigenvectors(jn_ctx *c, const char *directory, int count)
+{
+	if (!c || !directory) return jn_fail(JN_ERR_INVALID, "null argument");
+	const jn_plan_t *p = &c->plan;
+	double *buf = (double *)malloc((p->dim ? p->dim : 1) * sizeof(double));
+	jn_status st = JN_OK;
+	mkdir(directory, 0755);
+	for (int i = 0; i < count && !st; i++) {
+		st = jn_lanczos_eigenvector(c, i, buf);
+		if (st) break;
+		char dir[8192];
+		snprintf(dir, sizeof dir, "%s/eigenvector_%d", directory, i + 1);   /* bacchus.c:68-87 */
+		mkdir(dir, 0755);
+		for (int b = 0; b < p->nblocks && !st; b++) {
+			char path[8300];
+			snprintf(path, sizeof path, "%s/vec_%d", dir, b + 1);            /* vector.c:538-555 */
+			FILE *f = fopen(path, "wb");
+			if (!f) { st = jn_fail(JN_ERR_IO, "Could not open %s", path); break; }
+			size_t n = (size_t)(p->blocks[b].Np * p->blocks[b].Nn);
+			if (fwrite(buf + p->blocks[b].offset, sizeof(double), n, f) != n) st = jn_fail(JN_ERR_IO, "write %s", path);
+			fclose(f);
+		}
+	}
+	free(buf);
+	return st;
+}
+
+extern "C" void jn_print_eigensystem(const double *ev, int n)
+{
+	printf("eigensystem:\n{\n");
+	printf("\tnum_eigenvalues = %d;\n", n);
+	printf("\teigenvalues = ( ");
+	for (int i = 0; i < n; i++) printf("%.17lg%s ", ev[i], i == n - 1 ? "" : ",");
+	printf(");\n}\n");
+	fflush(stdout);
+}

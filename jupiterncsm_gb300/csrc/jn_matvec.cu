@@ -29,14 +29,13 @@
 #include <string.h>
 #include <sys/stat.h>
 
-#include "../../include/jncsm.h"
-#include "jn_problem.h"
+#include "jn_internal.h"
 
 #define JN_VERSION "jncsm-gb300 0.1"
 
 static thread_local char g_last_error[1024];
 
-static jn_status fail(jn_status s, const char *fmt, ...)
+jn_status jn_fail(jn_status s, const char *fmt, ...)
 {
 	va_list ap;
 	va_start(ap, fmt);
@@ -44,37 +43,14 @@ static jn_status fail(jn_status s, const char *fmt, ...)
 	va_end(ap);
 	return s;
 }
-
-#define CUDA_TRY(call)                                                                       \
-	do {                                                                                 \
-		cudaError_t e_ = (call);                                                     \
-		if (e_ != cudaSuccess)                                                       \
-			return fail(JN_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
-	} while (0)
+#define fail jn_fail
 
 extern "C" const char *jn_last_error(void) { return g_last_error; }
 extern "C" const char *jn_version(void) { return JN_VERSION; }
 
-struct jn_ctx {
-	jn_plan_t plan;
-	int device;
-	cudaStream_t stream;
-	uint32_t *d_rowptr;
-	uint2 *d_ent;
-	double *d_me;
-	jn_term_t *d_terms;
-	jn_tile_t *d_tiles;
-	jn_unit_t *d_units;
-	int32_t *d_unit_terms;
-	double *d_partial;
-	double *d_x, *d_y;      /* staging for the host-pointer entry points */
-	double *h_pinned;       /* pinned staging for host copies */
-};
-
 /* ------------------------------------------------------------------ */
 /* kernels                                                             */
 /* ------------------------------------------------------------------ */
-#define THREADS 256
 #define MASK31 0x7fffffffu
 
 struct DevPlan {
@@ -87,114 +63,139 @@ struct DevPlan {
 	const int32_t *__restrict__ unit_terms;
 };
 
-__device__ __forceinline__ double signed_me(const double *__restrict__ me, uint32_t mi)
-{
-	double m = __ldg(me + (mi & MASK31));
-	return (mi & 0x80000000u) ? -m : m;
-}
+#define WARPS 8
+#define TINY_BITS 0x3D719799812DEA11ull   /* bit pattern of 1e-12 */
+#define TINY_BITS32 0x2B8CBCCCu          /* bit pattern of 1e-12f */
 
-/* contribution of one term to element (p, n) of its destination block */
-__device__ __forceinline__ double term_element(const DevPlan &P, const jn_term_t &t, const double *__restrict__ x,
-					       int p, int n)
+__device__ __forceinline__ double flip_sign(double m, uint32_t sbit)
 {
-	const double *__restrict__ xs = x + t.src_off;
-	const double *__restrict__ me = P.me + t.me_off;
-	double acc = 0.0;
+	return __longlong_as_double(__double_as_longlong(m) ^ ((unsigned long long)(sbit & 0x80000000u) << 32));
+}
+__device__ __forceinline__ float flip_sign(float m, uint32_t sbit)
+{
+	return __uint_as_float(__float_as_uint(m) ^ (sbit & 0x80000000u));
+}
+/* |m| < 1e-12, decided on the bit pattern (no floating-point instruction) */
+__device__ __forceinline__ bool tiny(double m)
+{
+	return ((unsigned long long)__double_as_longlong(m) & 0x7fffffffffffffffull) < TINY_BITS;
+}
+__device__ __forceinline__ bool tiny(float m) { return false; /* pre-zeroed on upload */ }
+
+/*
+ * Contribution of term t to element (p, n) of its destination block, summed
+ * into acc in list order.  One floating-point instruction per multiply-add:
+ * signs are applied with integer XORs and the reference's |M| < 1e-12 skip
+ * of single-species terms is a bit-pattern compare.
+ */
+template <typename T>
+__device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, const T *__restrict__ x,
+					  const T *__restrict__ me_all, int p, int n)
+{
+	const T *__restrict__ xs = x + t.src_off;
+	const T *__restrict__ me = me_all + t.me_off;
+	const uint32_t *__restrict__ rp = P.rowptr;
+	T acc = 0;
 	if (t.kind == JN_KIND_P) {
-		uint32_t j0 = __ldg(P.rowptr + t.p_ptr + p), j1 = __ldg(P.rowptr + t.p_ptr + p + 1);
+		const uint32_t j0 = __ldg(rp + t.p_ptr + p), j1 = __ldg(rp + t.p_ptr + p + 1);
 		for (uint32_t j = j0; j < j1; j++) {
-			uint2 e = __ldg(P.ent + j);
-			double m = __ldg(me + (e.y & MASK31));
-			if (fabs(m) < 1e-12) continue;
-			if (e.y & 0x80000000u) m = -m;
-			acc = fma(m, __ldg(xs + (size_t)e.x * t.Nn_src + n), acc);
+			const uint2 e = __ldg(P.ent + j);
+			T m = __ldg(me + (e.y & MASK31));
+			if (tiny(m)) continue;
+			acc = fma(flip_sign(m, e.y), __ldg(xs + (size_t)e.x * t.Nn_src + n), acc);
 		}
 	} else if (t.kind == JN_KIND_N) {
-		uint32_t j0 = __ldg(P.rowptr + t.n_ptr + n), j1 = __ldg(P.rowptr + t.n_ptr + n + 1);
-		const double *__restrict__ xrow = xs + (size_t)p * t.Nn_src;
+		const uint32_t j0 = __ldg(rp + t.n_ptr + n), j1 = __ldg(rp + t.n_ptr + n + 1);
+		const T *__restrict__ xrow = xs + (size_t)p * t.Nn_src;
 		for (uint32_t j = j0; j < j1; j++) {
-			uint2 e = __ldg(P.ent + j);
-			double m = __ldg(me + (e.y & MASK31));
-			if (fabs(m) < 1e-12) continue;
-			if (e.y & 0x80000000u) m = -m;
-			acc = fma(m, __ldg(xrow + e.x), acc);
+			const uint2 e = __ldg(P.ent + j);
+			T m = __ldg(me + (e.y & MASK31));
+			if (tiny(m)) continue;
+			acc = fma(flip_sign(m, e.y), __ldg(xrow + e.x), acc);
 		}
 	} else {
-		uint32_t i0 = __ldg(P.rowptr + t.p_ptr + p), i1 = __ldg(P.rowptr + t.p_ptr + p + 1);
-		uint32_t j0 = __ldg(P.rowptr + t.n_ptr + n), j1 = __ldg(P.rowptr + t.n_ptr + n + 1);
-		if (j0 == j1) return 0.0;
+		const uint32_t j0 = __ldg(rp + t.n_ptr + n), j1 = __ldg(rp + t.n_ptr + n + 1);
+		if (j0 == j1) return acc;
+		const uint32_t i0 = __ldg(rp + t.p_ptr + p), i1 = __ldg(rp + t.p_ptr + p + 1);
 		for (uint32_t i = i0; i < i1; i++) {
-			uint2 ep = __ldg(P.ent + i);
-			const double *__restrict__ mrow = me + (size_t)t.nd * (ep.y & MASK31);
-			const double *__restrict__ xrow = xs + (size_t)ep.x * t.Nn_src;
-			double inner = 0.0;
+			const uint2 ep = __ldg(P.ent + i);
+			const T *__restrict__ mrow = me + (size_t)t.nd * (ep.y & MASK31);
+			const T *__restrict__ xrow = xs + (size_t)ep.x * t.Nn_src;
 			for (uint32_t j = j0; j < j1; j++) {
-				uint2 en = __ldg(P.ent + j);
-				double m = __ldg(mrow + (en.y & MASK31));
-				if (en.y & 0x80000000u) m = -m;
-				inner = fma(m, __ldg(xrow + en.x), inner);
+				const uint2 en = __ldg(P.ent + j);
+				const T m = __ldg(mrow + (en.y & MASK31));
+				acc = fma(flip_sign(m, ep.y ^ en.y), __ldg(xrow + en.x), acc);
 			}
-			acc += (ep.y & 0x80000000u) ? -inner : inner;
 		}
 	}
 	return acc;
 }
 
-__global__ void __launch_bounds__(THREADS) jn_units_kernel(DevPlan P, const double *__restrict__ x,
-							   double *__restrict__ partial)
+/*
+ * One warp per work unit.  A unit is a piece of a destination block (R rows
+ * x W columns, R*W <= 32, one element per lane) and a chunk of the terms that
+ * touch it.  FP64: the lane accumulates every multiply-add in FP64.  FP32:
+ * matrix elements and x in FP32, each term's sum in FP32, terms combined by
+ * error-free TwoSum into an FP32 sum and FP32 compensation.
+ */
+template <bool F32>
+__global__ void __launch_bounds__(WARPS * 32) jn_pieces_kernel(DevPlan P, const void *__restrict__ xv,
+							       const void *__restrict__ mev,
+							       double *__restrict__ partial, int nunits)
 {
-	__shared__ double red[THREADS];
-	const jn_unit_t u = P.units[blockIdx.x];
+	const int lane = threadIdx.x & 31;
+	const int ui = blockIdx.x * WARPS + (threadIdx.x >> 5);
+	if (ui >= nunits) return;
+	const jn_unit_t u = P.units[ui];
 	const jn_tile_t tile = P.tiles[u.tile];
 	const int E = tile.nrows * tile.ncols;
-	int EP = 1;
-	while (EP < E) EP <<= 1;
-	const int tid = threadIdx.x;
-	double *out = partial + tile.partial + (int64_t)u.chunk * E;
-	if (EP <= THREADS) {
-		/* G groups of threads share each element; group g takes terms g, g+G, ... */
-		const int G = THREADS / EP;
-		const int g = tid / EP, e = tid % EP;
+	if (lane >= E) return;
+	const int p = tile.row0 + lane / tile.ncols, n = tile.col0 + lane % tile.ncols;
+	double result;
+	if (!F32) {
+		const double *x = (const double *)xv, *me = (const double *)mev;
 		double acc = 0.0;
-		if (e < E) {
-			const int p = tile.row0 + e / tile.ncols, n = tile.col0 + e % tile.ncols;
-			for (int64_t q = u.t0 + g; q < u.t1; q += G) {
-				const jn_term_t t = P.terms[P.unit_terms[q]];
-				acc += term_element(P, t, x, p, n);
-			}
+		for (int64_t q = u.t0; q < u.t1; q++) {
+			const jn_term_t t = P.terms[__ldg(P.unit_terms + q)];
+			acc += term_element<double>(P, t, x, me, p, n);
 		}
-		red[tid] = acc;
-		__syncthreads();
-		if (g == 0 && e < E) {
-			double s = red[e];
-			for (int h = 1; h < G; h++) s += red[h * EP + e];
-			out[e] = s;
-		}
+		result = acc;
 	} else {
-		for (int e = tid; e < E; e += THREADS) {
-			const int p = tile.row0 + e / tile.ncols, n = tile.col0 + e % tile.ncols;
-			double acc = 0.0;
-			for (int64_t q = u.t0; q < u.t1; q++) {
-				const jn_term_t t = P.terms[P.unit_terms[q]];
-				acc += term_element(P, t, x, p, n);
-			}
-			out[e] = acc;
+		const float *x = (const float *)xv, *me = (const float *)mev;
+		float s = 0.0f, c = 0.0f;
+		for (int64_t q = u.t0; q < u.t1; q++) {
+			const jn_term_t t = P.terms[__ldg(P.unit_terms + q)];
+			const float v = term_element<float>(P, t, x, me, p, n);
+			const float s2 = s + v, bp = s2 - s;
+			c += (s - (s2 - bp)) + (v - bp);
+			s = s2;
 		}
+		result = (double)s + (double)c;
 	}
+	partial[tile.partial + (int64_t)u.chunk * E + lane] = result;
 }
 
-__global__ void __launch_bounds__(THREADS) jn_reduce_kernel(const jn_tile_t *__restrict__ tiles,
-							    const double *__restrict__ partial,
-							    double *__restrict__ y, int accumulate)
+/* y (+)= sum of the unit partials of each piece, in chunk order; one warp per piece */
+__global__ void __launch_bounds__(WARPS * 32) jn_reduce_kernel(const jn_tile_t *__restrict__ tiles, int ntiles,
+							       const double *__restrict__ partial,
+							       double *__restrict__ y, int accumulate)
 {
-	const jn_tile_t t = tiles[blockIdx.x];
+	const int lane = threadIdx.x & 31;
+	const int ti = blockIdx.x * WARPS + (threadIdx.x >> 5);
+	if (ti >= ntiles) return;
+	const jn_tile_t t = tiles[ti];
 	const int E = t.nrows * t.ncols;
-	for (int e = threadIdx.x; e < E; e += blockDim.x) {
-		double s = 0.0;
-		for (int c = 0; c < t.nchunks; c++) s += partial[t.partial + (int64_t)c * E + e];
-		const int64_t at = t.dst_off + (int64_t)(t.row0 + e / t.ncols) * t.Nn + t.col0 + e % t.ncols;
-		y[at] = accumulate ? y[at] + s : s;
-	}
+	if (lane >= E) return;
+	double s = 0.0;
+	for (int c = 0; c < t.nchunks; c++) s += partial[t.partial + (int64_t)c * E + lane];
+	const int64_t at = t.dst_off + (int64_t)(t.row0 + lane / t.ncols) * t.Nn + t.col0 + lane % t.ncols;
+	y[at] = accumulate ? y[at] + s : s;
+}
+
+__global__ void jn_to_f32_kernel(const double *__restrict__ x, float *__restrict__ y, int64_t n)
+{
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		y[i] = (float)x[i];
 }
 
 /* ------------------------------------------------------------------ */
@@ -218,8 +219,9 @@ extern "C" void jn_close(jn_ctx *c)
 	if (!c) return;
 	cudaFree(c->d_rowptr); cudaFree(c->d_ent); cudaFree(c->d_me); cudaFree(c->d_terms);
 	cudaFree(c->d_tiles); cudaFree(c->d_units); cudaFree(c->d_unit_terms); cudaFree(c->d_partial);
-	cudaFree(c->d_x); cudaFree(c->d_y);
+	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
+	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
 	jn_plan_free(&c->plan);
 	free(c);
@@ -239,7 +241,9 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	int sms = 0;
 	CUDA_TRY(cudaGetDevice(&c->device));
 	CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-	if (jn_plan_build(&c->plan, comb, order, lists_dir, me_dir, Z, N, sms * 8, err, sizeof err)) {
+	c->num_sms = sms;
+	c->precision = 64;
+	if (jn_plan_build(&c->plan, comb, order, lists_dir, me_dir, Z, N, sms * 48, err, sizeof err)) {
 		free(c);
 		int io = strstr(err, "open") != NULL;
 		return fail(io ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
@@ -290,14 +294,62 @@ extern "C" jn_status jn_block_info(const jn_ctx *c, int b, int *id, size_t *offs
 	return JN_OK;
 }
 
-static jn_status launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st)
+static jn_status ensure_f32(jn_ctx *c)
+{
+	const jn_plan_t *p = &c->plan;
+	if (c->d_me32) return JN_OK;
+	float *h = (float *)malloc((p->n_me ? p->n_me : 1) * sizeof(float));
+	if (!h) return fail(JN_ERR_NOMEM, "out of host memory");
+	for (int b = 0; b < p->nmes; b++) {
+		const jn_me_t *M = &p->mes[b];
+		for (int64_t e = 0; e < M->len; e++) {
+			double v = p->me[M->offset + e];
+			/* single-species terms skip |M| < 1e-12 (matrix_vector_multiplication.c:52-53) */
+			h[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0f : (float)v;
+		}
+	}
+	jn_status s = upload(&c->d_me32, h, p->n_me);
+	free(h);
+	if (s) return s;
+	return upload(&c->d_x32, (const void *)NULL, p->dim);
+}
+
+/* enqueue the two kernels of one product; `mid` (optional) is recorded between them */
+static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t mid)
 {
 	const jn_plan_t *p = &c->plan;
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
-	if (p->nunits > 0) jn_units_kernel<<<p->nunits, THREADS, 0, st>>>(P, d_x, c->d_partial);
-	if (p->ntiles > 0) jn_reduce_kernel<<<p->ntiles, THREADS, 0, st>>>(c->d_tiles, c->d_partial, d_y, accumulate);
+	const int ug = (p->nunits + WARPS - 1) / WARPS, tg = (p->ntiles + WARPS - 1) / WARPS;
+	if (c->precision == 32) {
+		jn_status s = ensure_f32(c);
+		if (s) return s;
+		int g = (int)((p->dim + 255) / 256);
+		if (g > 4096) g = 4096;
+		if (p->dim) jn_to_f32_kernel<<<g, 256, 0, st>>>(d_x, c->d_x32, p->dim);
+		if (p->nunits) jn_pieces_kernel<true><<<ug, WARPS * 32, 0, st>>>(P, c->d_x32, c->d_me32, c->d_partial, p->nunits);
+	} else if (p->nunits) {
+		jn_pieces_kernel<false><<<ug, WARPS * 32, 0, st>>>(P, d_x, c->d_me, c->d_partial, p->nunits);
+	}
+	if (mid) cudaEventRecord(mid, st);
+	if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st)
+{
+	return enqueue(c, d_x, d_y, accumulate, st, NULL);
+}
+
+extern "C" jn_status jn_set_precision(jn_ctx *c, int precision)
+{
+	if (!c || (precision != 32 && precision != 64)) return fail(JN_ERR_INVALID, "precision must be 32 or 64");
+	if (precision == 32) {
+		jn_status s = ensure_f32(c);
+		if (s) return s;
+	}
+	c->precision = precision;
 	return JN_OK;
 }
 
@@ -305,23 +357,19 @@ extern "C" jn_status jn_matvec_device(jn_ctx *c, const double *d_x, double *d_y,
 {
 	if (!c || !d_x || !d_y) return fail(JN_ERR_INVALID, "null argument");
 	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
-	return launch_matvec(c, d_x, d_y, accumulate, stream ? (cudaStream_t)stream : c->stream);
+	return jn_launch_matvec(c, d_x, d_y, accumulate, stream ? (cudaStream_t)stream : c->stream);
 }
 
 extern "C" jn_status jn_matvec_profile(jn_ctx *c, const double *d_x, double *d_y, int accumulate, float ms[2])
 {
 	if (!c || !d_x || !d_y || !ms) return fail(JN_ERR_INVALID, "null argument");
 	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
-	const jn_plan_t *p = &c->plan;
 	cudaEvent_t ev[3];
 	for (int i = 0; i < 3; i++) CUDA_TRY(cudaEventCreate(&ev[i]));
-	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
 	CUDA_TRY(cudaEventRecord(ev[0], c->stream));
-	if (p->nunits > 0) jn_units_kernel<<<p->nunits, THREADS, 0, c->stream>>>(P, d_x, c->d_partial);
-	CUDA_TRY(cudaEventRecord(ev[1], c->stream));
-	if (p->ntiles > 0) jn_reduce_kernel<<<p->ntiles, THREADS, 0, c->stream>>>(c->d_tiles, c->d_partial, d_y, accumulate);
+	jn_status s = enqueue(c, d_x, d_y, accumulate, c->stream, ev[1]);
+	if (s) return s;
 	CUDA_TRY(cudaEventRecord(ev[2], c->stream));
-	CUDA_TRY(cudaGetLastError());
 	CUDA_TRY(cudaEventSynchronize(ev[2]));
 	CUDA_TRY(cudaEventElapsedTime(&ms[0], ev[0], ev[1]));
 	CUDA_TRY(cudaEventElapsedTime(&ms[1], ev[1], ev[2]));
@@ -335,7 +383,7 @@ extern "C" jn_status jn_matvec(jn_ctx *c, const double *x, double *y)
 	const size_t bytes = (size_t)c->plan.dim * sizeof(double);
 	CUDA_TRY(cudaMemcpyAsync(c->d_x, x, bytes, cudaMemcpyHostToDevice, c->stream));
 	CUDA_TRY(cudaMemcpyAsync(c->d_y, y, bytes, cudaMemcpyHostToDevice, c->stream));
-	jn_status s = launch_matvec(c, c->d_x, c->d_y, 1, c->stream);
+	jn_status s = jn_launch_matvec(c, c->d_x, c->d_y, 1, c->stream);
 	if (s) return s;
 	CUDA_TRY(cudaMemcpyAsync(y, c->d_y, bytes, cudaMemcpyDeviceToHost, c->stream));
 	CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -423,5 +471,30 @@ extern "C" jn_status jn_inspect_files(const char *comb, const char *order, const
 		return fail(strstr(err, "open") ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
 	fill_stats(&plan, st);
 	jn_plan_free(&plan);
+	return JN_OK;
+}
+
+extern "C" jn_status jn_read_settings(const char *conf, jn_run_settings *s)
+{
+	if (!conf || !s) return fail(JN_ERR_INVALID, "null argument");
+	jn_runfile_t rf;
+	char err[1024] = { 0 };
+	if (jn_read_runfile(conf, &rf, err, sizeof err)) return fail(strstr(err, "could not read") ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
+	memset(s, 0, sizeof *s);
+	snprintf(s->combination_table_file, sizeof s->combination_table_file, "%s", rf.comb);
+	snprintf(s->evaluation_order_file, sizeof s->evaluation_order_file, "%s", rf.order);
+	snprintf(s->index_lists_base_directory, sizeof s->index_lists_base_directory, "%s", rf.lists);
+	snprintf(s->matrix_file_base_directory, sizeof s->matrix_file_base_directory, "%s", rf.mes);
+	s->num_protons = rf.Z;
+	s->num_neutrons = rf.N;
+	snprintf(s->krylow_vector_directory, sizeof s->krylow_vector_directory, "%s", rf.krylov);
+	s->max_num_lanczos_iterations = (int)rf.max_iterations;
+	s->convergence_tolerance = rf.tolerance;
+	s->target_eigenvector = (int)rf.target_eigenvector;
+	s->converge_eigenvectors = rf.converge_eigenvectors;
+	snprintf(s->eigenvector_directory, sizeof s->eigenvector_directory, "%s", rf.eigvec);
+	s->gpu_num_eigenvalues = rf.num_eigenvalues;
+	s->gpu_precision = rf.precision;
+	s->gpu_full_reorthogonalization = rf.reorthogonalize;
 	return JN_OK;
 }

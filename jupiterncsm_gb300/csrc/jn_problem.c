@@ -312,24 +312,43 @@ void jn_plan_free(jn_plan_t *p)
 	memset(p, 0, sizeof *p);
 }
 
-#define TILE_ELEMENTS 512
+/* warp pieces: R rows x W columns of one destination block, R*W <= 32 */
+#define PIECE_LANES 32
 
-/* work estimate of term t restricted to tile rows [r0,r1) x cols [c0,c1) */
+/* estimated warp time of term t on the piece rows [r0,r1) x cols [c0,c1):
+ * every lane owns one element, so the warp runs as long as its longest
+ * lane.  Zero when the term contributes nothing to the piece. */
 static double term_cost(const jn_plan_t *p, const jn_term_t *t, int r0, int r1, int c0, int c1)
 {
 	const uint32_t *rp = p->rowptr;
-	double np = 0, nn = 0;
+	double np = 0, nn = 0, npmax = 0, nnmax = 0;
 	if (t->kind != JN_KIND_N) {
-		for (int r = r0; r < r1; r++) np += rp[t->p_ptr + r + 1] - rp[t->p_ptr + r];
+		for (int r = r0; r < r1; r++) {
+			double v = rp[t->p_ptr + r + 1] - rp[t->p_ptr + r];
+			np += v;
+			if (v > npmax) npmax = v;
+		}
 		if (np == 0) return 0;
 	}
 	if (t->kind != JN_KIND_P) {
-		for (int c = c0; c < c1; c++) nn += rp[t->n_ptr + c + 1] - rp[t->n_ptr + c];
+		for (int c = c0; c < c1; c++) {
+			double v = rp[t->n_ptr + c + 1] - rp[t->n_ptr + c];
+			nn += v;
+			if (v > nnmax) nnmax = v;
+		}
 		if (nn == 0) return 0;
 	}
-	if (t->kind == JN_KIND_P) return np * (c1 - c0);
-	if (t->kind == JN_KIND_N) return nn * (r1 - r0);
-	return np * nn;
+	if (t->kind == JN_KIND_P) return 4.0 + npmax;
+	if (t->kind == JN_KIND_N) return 4.0 + nnmax;
+	return 4.0 + npmax * (1.0 + nnmax);
+}
+
+static const double *g_unit_cost;
+static int cmp_unit_cost(const void *a, const void *b)
+{
+	double x = g_unit_cost[*(const int *)a], y = g_unit_cost[*(const int *)b];
+	if (x != y) return x < y ? 1 : -1;
+	return *(const int *)a - *(const int *)b;
 }
 
 int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, const char *lists_dir,
@@ -463,6 +482,7 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 		if (x->kind == JN_KIND_N && bi->Np != bo->Np) ERR("instruction %d: neutron term between blocks of different proton dimension", i);
 		if (x->kind == JN_KIND_P && bi->Nn != bo->Nn) ERR("instruction %d: proton term between blocks of different neutron dimension", i);
 		if (x->kind == JN_KIND_NP && M->nd_n == 0) ERR("instruction %d: matrix block %d has no neutron dimension", i, M->id);
+		if (x->kind != JN_KIND_NP) M->single = 1;
 		int slots[2] = { x->ln, x->lp };
 		for (int q = 0; q < 2; q++) {
 			if (slots[q] < 0) continue;
@@ -623,8 +643,8 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 		for (int b = 0; b < p->nblocks; b++) {
 			jn_block_t *B = &p->blocks[b];
 			if (B->Np == 0 || B->Nn == 0) continue;
-			int64_t cw = B->Nn < TILE_ELEMENTS ? B->Nn : TILE_ELEMENTS;
-			int64_t R = B->Nn >= TILE_ELEMENTS ? 1 : TILE_ELEMENTS / B->Nn;
+			int64_t cw = B->Nn < PIECE_LANES ? B->Nn : PIECE_LANES;
+			int64_t R = B->Nn >= PIECE_LANES ? 1 : PIECE_LANES / B->Nn;
 			for (int64_t r0 = 0; r0 < B->Np; r0 += R)
 				for (int64_t c0 = 0; c0 < B->Nn; c0 += cw) {
 					if (p->ntiles == tcap) {
@@ -646,9 +666,9 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 					total_cost += cost;
 				}
 		}
-		if (target_units <= 0) target_units = 152 * 8;
+		if (target_units <= 0) target_units = 152 * 48;
 		double target = total_cost / target_units;
-		if (target < 4096) target = 4096;
+		if (target < 256) target = 256;
 		/* pass 2: chunks */
 		int64_t ucap = 4096, tcap2 = 1 << 16;
 		p->units = malloc(ucap * sizeof(jn_unit_t));
@@ -691,6 +711,28 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 			partial += (int64_t)chunks * T->nrows * T->ncols;
 		}
 		p->n_partial = partial;
+		/* longest units first: the warps that start first take the heaviest work */
+		{
+			double *uc = malloc((p->nunits ? p->nunits : 1) * sizeof(double));
+			int *ord = malloc((p->nunits ? p->nunits : 1) * sizeof(int));
+			for (int u = 0; u < p->nunits; u++) {
+				const jn_unit_t *U = &p->units[u];
+				const jn_tile_t *T = &p->tiles[U->tile];
+				double cst = 0;
+				for (int64_t q = U->t0; q < U->t1; q++)
+					cst += term_cost(p, &p->terms[p->unit_terms[q]], T->row0, T->row0 + T->nrows, T->col0,
+							 T->col0 + T->ncols);
+				uc[u] = cst;
+				ord[u] = u;
+			}
+			g_unit_cost = uc;
+			qsort(ord, p->nunits, sizeof(int), cmp_unit_cost);
+			jn_unit_t *sorted = malloc((p->nunits ? p->nunits : 1) * sizeof(jn_unit_t));
+			for (int u = 0; u < p->nunits; u++) sorted[u] = p->units[ord[u]];
+			free(p->units);
+			p->units = sorted;
+			free(uc); free(ord);
+		}
 		free(tile_cost); free(byblk); free(count);
 	}
 	free(term_dst);

@@ -62,6 +62,7 @@ typedef struct {
 	uint64_t nd_n, nd_p;    /* header dimensions */
 	int64_t len;
 	int64_t offset;         /* into jn_plan_t.me */
+	int single;             /* used by single-species (n or p) instructions */
 } jn_me_t;
 
 /* device term descriptor: one direction of one instruction, seen from its

@@ -37,14 +37,12 @@ static double term_element(const jn_plan_t *P, const jn_term_t *t, const double 
 			uint32_t ps = ent[2 * i], mip = ent[2 * i + 1];
 			const double *mrow = me + (size_t)t->nd * (mip & 0x7fffffffu);
 			const double *xrow = xs + (size_t)ps * t->Nn_src;
-			double inner = 0.0;
 			for (uint32_t j = j0; j < j1; j++) {
 				uint32_t ns = ent[2 * j], min = ent[2 * j + 1];
 				double m = mrow[min & 0x7fffffffu];
-				if (min & 0x80000000u) m = -m;
-				inner = fma(m, xrow[ns], inner);
+				if ((mip ^ min) & 0x80000000u) m = -m;
+				acc = fma(m, xrow[ns], acc);
 			}
-			acc += (mip & 0x80000000u) ? -inner : inner;
 		}
 	}
 	return acc;
@@ -62,43 +60,21 @@ long emu_dimension(void *h) { return (long)((jn_plan_t *)h)->dim; }
 int emu_units(void *h) { return ((jn_plan_t *)h)->nunits; }
 int emu_tiles(void *h) { return ((jn_plan_t *)h)->ntiles; }
 
-/* y (+)= H x following the kernel's thread mapping and reduction order */
+/* y (+)= H x following the kernel's warp mapping (one lane per piece
+ * element, terms of a unit in order) and the chunk-ordered reduction */
 void emu_matvec(void *h, const double *x, double *y, int accumulate)
 {
 	const jn_plan_t *P = h;
 	double *partial = calloc(P->n_partial ? P->n_partial : 1, sizeof(double));
-	double red[256];
 	for (int b = 0; b < P->nunits; b++) {
 		const jn_unit_t *u = &P->units[b];
 		const jn_tile_t *tile = &P->tiles[u->tile];
 		const int E = tile->nrows * tile->ncols;
-		int EP = 1;
-		while (EP < E) EP <<= 1;
-		double *out = partial + tile->partial + (int64_t)u->chunk * E;
-		if (EP <= 256) {
-			const int G = 256 / EP;
-			for (int tid = 0; tid < 256; tid++) {
-				int g = tid / EP, e = tid % EP;
-				double acc = 0.0;
-				if (e < E) {
-					int p = tile->row0 + e / tile->ncols, n = tile->col0 + e % tile->ncols;
-					for (int64_t q = u->t0 + g; q < u->t1; q += G)
-						acc += term_element(P, &P->terms[P->unit_terms[q]], x, p, n);
-				}
-				red[tid] = acc;
-			}
-			for (int e = 0; e < E; e++) {
-				double s = red[e];
-				for (int hh = 1; hh < G; hh++) s += red[hh * EP + e];
-				out[e] = s;
-			}
-		} else {
-			for (int e = 0; e < E; e++) {
-				int p = tile->row0 + e / tile->ncols, n = tile->col0 + e % tile->ncols;
-				double acc = 0.0;
-				for (int64_t q = u->t0; q < u->t1; q++) acc += term_element(P, &P->terms[P->unit_terms[q]], x, p, n);
-				out[e] = acc;
-			}
+		for (int lane = 0; lane < E; lane++) {
+			int p = tile->row0 + lane / tile->ncols, n = tile->col0 + lane % tile->ncols;
+			double acc = 0.0;
+			for (int64_t q = u->t0; q < u->t1; q++) acc += term_element(P, &P->terms[P->unit_terms[q]], x, p, n);
+			partial[tile->partial + (int64_t)u->chunk * E + lane] = acc;
 		}
 	}
 	for (int ti = 0; ti < P->ntiles; ti++) {
