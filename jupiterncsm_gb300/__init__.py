@@ -93,6 +93,7 @@ def gpu_lib():
     L.jn_get_plan_stats.argtypes = [vp, ctypes.POINTER(PlanStats)]
     L.jn_inspect_files.argtypes = [cp, cp, cp, cp, ci, ci, ctypes.POINTER(PlanStats)]
     L.jn_set_precision.argtypes = [vp, ci]
+    L.jn_set_engine.argtypes = [vp, ci]
     L.jn_lanczos.argtypes = [vp, ctypes.POINTER(LanczosOptions), ctypes.POINTER(LanczosResult)]
     L.jn_lanczos_ritz_values.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ci, ctypes.POINTER(ci)]
     L.jn_lanczos_eigenvector.argtypes = [vp, ci, vp]
@@ -100,7 +101,7 @@ def gpu_lib():
     L.jn_print_eigensystem.argtypes = [ctypes.POINTER(ctypes.c_double), ci]
     L.jn_print_eigensystem.restype = None
     for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
-                 "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_lanczos",
+                 "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_set_engine", "jn_lanczos",
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors"):
         getattr(L, name).restype = ci
     _gpu = L
@@ -198,6 +199,10 @@ class Hamiltonian:
 
     def save_eigenvectors(self, directory, count):
         _check(gpu_lib().jn_lanczos_save_eigenvectors(self._h, directory.encode(), int(count)))
+
+    def set_engine(self, engine):
+        """3: block tiles with exact fixed-point sums (default); 2: warp pieces."""
+        _check(gpu_lib().jn_set_engine(self._h, int(engine)))
 
     def matvec_files(self, out_dir, in_dir):
         _check(gpu_lib().jn_matvec_files(self._h, out_dir.encode(), in_dir.encode()))

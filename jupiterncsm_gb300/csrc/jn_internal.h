@@ -40,6 +40,11 @@ struct jn_ctx {
 	int precision;          /* 64: FP64 products; 32: FP32 matrix elements and x, compensated sums */
 	float *d_me32;          /* FP32 copy of the matrix elements (built on first FP32 use) */
 	float *d_x32;
+	int engine;             /* 3: block tiles with exact fixed-point sums (default); 2: warp pieces */
+	jn_btile_t *d_btiles;
+	jn_piece_t *d_pieces;
+	unsigned long long *d_gacc;     /* 64-bit fixed-point accumulator, zero between products */
+	unsigned int *d_xmax;           /* max|x| of the current product (FP32 bit pattern) */
 	struct jn_lanczos_state *lz;
 };
 

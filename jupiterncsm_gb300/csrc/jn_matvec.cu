@@ -102,7 +102,8 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 			const uint2 e = __ldg(P.ent + j);
 			T m = __ldg(me + (e.y & MASK31));
 			if (tiny(m)) continue;
-			acc = fma(flip_sign(m, e.y), __ldg(xs + (size_t)e.x * t.Nn_src + n), acc);
+			const uint32_t src = t.transpose ? (e.x >> 16) : (e.x & 0xffffu);
+			acc = fma(flip_sign(m, e.y), __ldg(xs + (size_t)src * t.Nn_src + n), acc);
 		}
 	} else if (t.kind == JN_KIND_N) {
 		const uint32_t j0 = __ldg(rp + t.n_ptr + n), j1 = __ldg(rp + t.n_ptr + n + 1);
@@ -111,7 +112,8 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 			const uint2 e = __ldg(P.ent + j);
 			T m = __ldg(me + (e.y & MASK31));
 			if (tiny(m)) continue;
-			acc = fma(flip_sign(m, e.y), __ldg(xrow + e.x), acc);
+			const uint32_t src = t.transpose ? (e.x >> 16) : (e.x & 0xffffu);
+			acc = fma(flip_sign(m, e.y), __ldg(xrow + src), acc);
 		}
 	} else {
 		const uint32_t j0 = __ldg(rp + t.n_ptr + n), j1 = __ldg(rp + t.n_ptr + n + 1);
@@ -120,11 +122,13 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 		for (uint32_t i = i0; i < i1; i++) {
 			const uint2 ep = __ldg(P.ent + i);
 			const T *__restrict__ mrow = me + (size_t)t.nd * (ep.y & MASK31);
-			const T *__restrict__ xrow = xs + (size_t)ep.x * t.Nn_src;
+			const uint32_t psrc = t.transpose ? (ep.x >> 16) : (ep.x & 0xffffu);
+			const T *__restrict__ xrow = xs + (size_t)psrc * t.Nn_src;
 			for (uint32_t j = j0; j < j1; j++) {
 				const uint2 en = __ldg(P.ent + j);
 				const T m = __ldg(mrow + (en.y & MASK31));
-				acc = fma(flip_sign(m, ep.y ^ en.y), __ldg(xrow + en.x), acc);
+				const uint32_t nsrc = t.transpose ? (en.x >> 16) : (en.x & 0xffffu);
+				acc = fma(flip_sign(m, ep.y ^ en.y), __ldg(xrow + nsrc), acc);
 			}
 		}
 	}
@@ -199,6 +203,158 @@ __global__ void jn_to_f32_kernel(const double *__restrict__ x, float *__restrict
 }
 
 /* ------------------------------------------------------------------ */
+/* block-tile kernels: exact 64-bit fixed-point accumulation           */
+/* ------------------------------------------------------------------ */
+#define TILE_THREADS 256
+
+/* exponent S of the fixed-point unit 2^-S: |y| <= abs_bound * max|x| <= 2^(62-S).
+ * Integer arithmetic on the exponent field only, identical in every kernel. */
+__device__ __forceinline__ int fixed_exponent(unsigned int xmax_bits, double abs_bound)
+{
+	const double yb = abs_bound * (double)__uint_as_float(xmax_bits);
+	if (!(yb > 0.0)) return 0;
+	const long long bits = __double_as_longlong(yb);
+	int e = (int)((bits >> 52) & 0x7ff) - 1022;       /* yb < 2^e */
+	int S = 62 - e;
+	return S < -60 ? -60 : (S > 100 ? 100 : S);
+}
+
+/* x (FP64) -> optional FP32 copy, and max|x| into *xmax_bits (zeroed before) */
+__global__ void jn_prep_kernel(const double *__restrict__ x, float *__restrict__ x32, int64_t n,
+			       unsigned int *__restrict__ xmax_bits)
+{
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = x[i];
+		if (x32) x32[i] = (float)v;
+		m = fmaxf(m, (float)fabs(v) * 1.0000002f);  /* round-up margin of the FP32 conversion */
+	}
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(xmax_bits, __float_as_uint(m));
+}
+
+template <typename T> __device__ __forceinline__ long long to_fixed(T v);
+template <> __device__ __forceinline__ long long to_fixed<float>(float v) { return __float2ll_rn(v); }
+template <> __device__ __forceinline__ long long to_fixed<double>(double v) { return __double2ll_rn(v); }
+
+__device__ __forceinline__ int pow2_at_least(int v)
+{
+	int b = 1;
+	while (b < v) b <<= 1;
+	return b;
+}
+
+/*
+ * One CTA per block tile (rows [row0, row0+nrows) of one destination block).
+ * Each warp takes pieces in turn and spreads a piece over its lanes as an
+ * (a x b) grid: b lanes over the neutron entries (or columns), a lanes over
+ * contiguous sub-ranges of the proton entries (or rows).  A lane sums the run
+ * of consecutive proton entries that share a destination row in T
+ * arithmetic, scales by 2^S, rounds to a 64-bit integer and adds it into the
+ * tile's shared-memory accumulator; the tile is then added into the global
+ * 64-bit accumulator.  Integer addition is exact and associative, so the
+ * result does not depend on the order in which warps and CTAs run.
+ */
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles,
+							       const jn_piece_t *__restrict__ pieces,
+							       const T *__restrict__ x, const T *__restrict__ me,
+							       unsigned long long *__restrict__ gacc,
+							       const unsigned int *__restrict__ xmax_bits, double abs_bound)
+{
+	extern __shared__ unsigned long long sacc[];
+	const jn_btile_t tl = tiles[blockIdx.x];
+	const int Nn = tl.Nn;
+	const int E = tl.nrows * Nn;
+	for (int i = threadIdx.x; i < E; i += blockDim.x) sacc[i] = 0ull;
+	const int S = fixed_exponent(*xmax_bits, abs_bound);
+	const T scale = (T)ldexp(1.0, S);
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	for (int64_t pc = tl.pc0 + warp; pc < tl.pc1; pc += TILE_THREADS / 32) {
+		const jn_piece_t pcs = pieces[pc];
+		const jn_term_t t = P.terms[pcs.term];
+		const T *__restrict__ xs = x + t.src_off;
+		const T *__restrict__ mb = me + t.me_off;
+		const bool tr = t.transpose != 0;
+		const int Ns = t.Nn_src;
+		if (t.kind == JN_KIND_NP || t.kind == JN_KIND_P) {
+			const int ncol = t.kind == JN_KIND_NP ? (int)(t.n_e1 - t.n_e0) : t.Nn_dst;
+			const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
+			const int gi = lane / b, gj = lane % b;
+			const uint32_t na = pcs.a1 - pcs.a0, per = (na + a - 1) / a;
+			const uint32_t e0 = pcs.a0 + gi * per, e1 = min(pcs.a1, e0 + per);
+			for (int cj = gj; cj < ncol; cj += b) {
+				int scol, dcol;
+				uint32_t kn = 0, sn = 0;
+				if (t.kind == JN_KIND_NP) {
+					const uint2 qn = __ldg(P.ent + t.n_e0 + cj);
+					const int nin = qn.x & 0xffff, nout = qn.x >> 16;
+					scol = tr ? nout : nin;
+					dcol = tr ? nin : nout;
+					kn = qn.y & MASK31;
+					sn = qn.y;
+				} else {
+					scol = dcol = cj;
+				}
+				T run = 0;
+				int cur = -1;
+				for (uint32_t ep = e0; ep < e1; ep++) {
+					const uint2 qp = __ldg(P.ent + ep);
+					const int pin = qp.x & 0xffff, pout = qp.x >> 16;
+					const int srow = tr ? pout : pin, drow = tr ? pin : pout;
+					if (drow != cur) {
+						if (cur >= 0)
+							atomicAdd(&sacc[(cur - tl.row0) * Nn + dcol],
+								  (unsigned long long)to_fixed<T>(run * scale));
+						run = 0;
+						cur = drow;
+					}
+					const uint32_t kp = qp.y & MASK31;
+					const T m = __ldg(mb + (t.kind == JN_KIND_NP ? (size_t)kn + (size_t)t.nd * kp : (size_t)kp));
+					if (t.kind == JN_KIND_P && tiny(m)) continue;
+					run = fma(flip_sign(m, qp.y ^ sn), __ldg(xs + (size_t)srow * Ns + scol), run);
+				}
+				if (cur >= 0)
+					atomicAdd(&sacc[(cur - tl.row0) * Nn + dcol], (unsigned long long)to_fixed<T>(run * scale));
+			}
+		} else {
+			/* neutron-only term: the proton row is a spectator, rows [a0, a1) */
+			const int ncol = (int)(t.n_e1 - t.n_e0);
+			const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
+			const int gi = lane / b, gj = lane % b;
+			for (int cj = gj; cj < ncol; cj += b) {
+				const uint2 qn = __ldg(P.ent + t.n_e0 + cj);
+				const int nin = qn.x & 0xffff, nout = qn.x >> 16;
+				const int scol = tr ? nout : nin, dcol = tr ? nin : nout;
+				const T m = flip_sign(__ldg(mb + (qn.y & MASK31)), qn.y);
+				if (tiny(m)) continue;
+				for (uint32_t r = pcs.a0 + gi; r < pcs.a1; r += a)
+					atomicAdd(&sacc[(r - tl.row0) * Nn + dcol],
+						  (unsigned long long)to_fixed<T>(m * __ldg(xs + (size_t)r * Ns + scol) * scale));
+			}
+		}
+	}
+	__syncthreads();
+	unsigned long long *g = gacc + tl.dst_off + (int64_t)tl.row0 * Nn;
+	for (int i = threadIdx.x; i < E; i += blockDim.x)
+		if (sacc[i]) atomicAdd(g + i, sacc[i]);
+}
+
+/* y (+)= acc * 2^-S, and the accumulator is cleared for the next product */
+__global__ void jn_finalize_kernel(unsigned long long *__restrict__ gacc, double *__restrict__ y, int64_t n,
+				   const unsigned int *__restrict__ xmax_bits, double abs_bound, int accumulate)
+{
+	const int S = fixed_exponent(*xmax_bits, abs_bound);
+	const double unit = ldexp(1.0, -S);
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = (double)(long long)gacc[i] * unit;
+		y[i] = accumulate ? y[i] + v : v;
+		gacc[i] = 0ull;
+	}
+}
+
+/* ------------------------------------------------------------------ */
 /* host side                                                           */
 /* ------------------------------------------------------------------ */
 template <typename T>
@@ -220,6 +376,7 @@ extern "C" void jn_close(jn_ctx *c)
 	cudaFree(c->d_rowptr); cudaFree(c->d_ent); cudaFree(c->d_me); cudaFree(c->d_terms);
 	cudaFree(c->d_tiles); cudaFree(c->d_units); cudaFree(c->d_unit_terms); cudaFree(c->d_partial);
 	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
+	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
@@ -259,11 +416,24 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	    (s = upload(&c->d_unit_terms, p->unit_terms, p->n_unit_terms)) ||
 	    (s = upload(&c->d_partial, (const void *)NULL, p->n_partial)) ||
 	    (s = upload(&c->d_x, (const void *)NULL, p->dim)) ||
-	    (s = upload(&c->d_y, (const void *)NULL, p->dim))) {
+	    (s = upload(&c->d_y, (const void *)NULL, p->dim)) ||
+	    (s = upload(&c->d_btiles, p->btiles, p->nbtiles)) ||
+	    (s = upload(&c->d_pieces, p->pieces, p->npieces)) ||
+	    (s = upload(&c->d_gacc, (const void *)NULL, p->dim)) ||
+	    (s = upload(&c->d_xmax, (const void *)NULL, 1))) {
 		jn_close(c);
 		return s;
 	}
-	/* host copies of the lists are no longer needed on the product path */
+	{
+		cudaError_t z = cudaMemset(c->d_gacc, 0, (p->dim ? p->dim : 1) * sizeof(unsigned long long));
+		size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * sizeof(unsigned long long);
+		if (z == cudaSuccess)
+			z = cudaFuncSetAttribute(jn_tile_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (z == cudaSuccess)
+			z = cudaFuncSetAttribute(jn_tile_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (z != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "tile kernel set-up: %s", cudaGetErrorString(z)); }
+	}
+	c->engine = 3;
 	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
 	if (e != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
 	e = cudaMallocHost((void **)&c->h_pinned, (p->dim ? p->dim : 1) * sizeof(double));
@@ -319,21 +489,51 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 {
 	const jn_plan_t *p = &c->plan;
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
-	const int ug = (p->nunits + WARPS - 1) / WARPS, tg = (p->ntiles + WARPS - 1) / WARPS;
-	if (c->precision == 32) {
+	const int f32 = c->precision == 32;
+	if (f32) {
 		jn_status s = ensure_f32(c);
 		if (s) return s;
-		int g = (int)((p->dim + 255) / 256);
-		if (g > 4096) g = 4096;
-		if (p->dim) jn_to_f32_kernel<<<g, 256, 0, st>>>(d_x, c->d_x32, p->dim);
-		if (p->nunits) jn_pieces_kernel<true><<<ug, WARPS * 32, 0, st>>>(P, c->d_x32, c->d_me32, c->d_partial, p->nunits);
-	} else if (p->nunits) {
-		jn_pieces_kernel<false><<<ug, WARPS * 32, 0, st>>>(P, d_x, c->d_me, c->d_partial, p->nunits);
 	}
-	if (mid) cudaEventRecord(mid, st);
-	if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (g < 1) g = 1;
+	if (c->engine == 2) {
+		const int ug = (p->nunits + WARPS - 1) / WARPS, tg = (p->ntiles + WARPS - 1) / WARPS;
+		if (f32) {
+			if (p->dim) jn_to_f32_kernel<<<g, 256, 0, st>>>(d_x, c->d_x32, p->dim);
+			if (p->nunits) jn_pieces_kernel<true><<<ug, WARPS * 32, 0, st>>>(P, c->d_x32, c->d_me32, c->d_partial, p->nunits);
+		} else if (p->nunits) {
+			jn_pieces_kernel<false><<<ug, WARPS * 32, 0, st>>>(P, d_x, c->d_me, c->d_partial, p->nunits);
+		}
+		if (mid) cudaEventRecord(mid, st);
+		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
+	} else {
+		const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * sizeof(unsigned long long);
+		cudaError_t e0 = cudaMemsetAsync(c->d_xmax, 0, sizeof(unsigned int), st);
+		if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
+		if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? c->d_x32 : NULL, p->dim, c->d_xmax);
+		if (p->nbtiles) {
+			if (f32)
+				jn_tile_kernel<float><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_x32,
+											   c->d_me32, c->d_gacc, c->d_xmax,
+											   p->abs_bound);
+			else
+				jn_tile_kernel<double><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, d_x,
+												c->d_me, c->d_gacc, c->d_xmax,
+												p->abs_bound);
+		}
+		if (mid) cudaEventRecord(mid, st);
+		if (p->dim) jn_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, c->d_xmax, p->abs_bound, accumulate);
+	}
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
+{
+	if (!c || (engine != 2 && engine != 3)) return fail(JN_ERR_INVALID, "engine must be 2 or 3");
+	c->engine = engine;
 	return JN_OK;
 }
 

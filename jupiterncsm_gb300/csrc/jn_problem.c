@@ -283,7 +283,7 @@ fail:
 
 static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
 {
-	/* stable counting sort on the destination index; entries (source, matrix_index) */
+	/* stable counting sort on the destination index; entries (in | out << 16, matrix_index) */
 	memset(rowptr, 0, (size_t)(nrows + 1) * sizeof(uint32_t));
 	for (int64_t e = 0; e < len; e++) rowptr[(by_out ? tri[3 * e + 1] : tri[3 * e]) + 1]++;
 	for (int32_t r = 0; r < nrows; r++) rowptr[r + 1] += rowptr[r];
@@ -291,9 +291,8 @@ static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out
 	memcpy(fill, rowptr, (size_t)(nrows + 1) * sizeof(uint32_t));
 	for (int64_t e = 0; e < len; e++) {
 		int32_t dst = by_out ? tri[3 * e + 1] : tri[3 * e];
-		int32_t src = by_out ? tri[3 * e] : tri[3 * e + 1];
 		uint32_t at = fill[dst]++;
-		ent[2 * at] = (uint32_t)src;
+		ent[2 * at] = (uint32_t)tri[3 * e] | ((uint32_t)tri[3 * e + 1] << 16);
 		ent[2 * at + 1] = (uint32_t)tri[3 * e + 2];
 	}
 	free(fill);
@@ -309,6 +308,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->mes);
 	free(p->rowptr); free(p->ent); free(p->me);
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
+	free(p->btiles); free(p->pieces);
 	memset(p, 0, sizeof *p);
 }
 
@@ -349,6 +349,127 @@ static int cmp_unit_cost(const void *a, const void *b)
 	double x = g_unit_cost[*(const int *)a], y = g_unit_cost[*(const int *)b];
 	if (x != y) return x < y ? 1 : -1;
 	return *(const int *)a - *(const int *)b;
+}
+
+/* shared-memory accumulator budget of one CTA, in 64-bit elements */
+#define TILE_SMEM_ELEMS 8192
+
+/*
+ * Block tiles: every destination block is cut into row ranges whose
+ * accumulator fits in shared memory; the terms touching a range become
+ * pieces (proton-entry sub-ranges for NP and P terms, row sub-ranges for N
+ * terms) of bounded work, packed into tiles of similar work.  Also computes
+ * abs_bound, the largest sum of |M| over the contributions to one element,
+ * which bounds |y| by abs_bound * max|x| for the fixed-point scale.
+ */
+static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units, char *err, size_t errlen)
+{
+	const uint32_t *rp = p->rowptr;
+	double total = 0;
+	/* per-term work and the largest |M| of its block */
+	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
+	for (int t = 0; t < p->nterms; t++) {
+		const jn_term_t *T = &p->terms[t];
+		const jn_instr_t *x = &p->instr[T->instr];
+		const jn_me_t *M = &p->mes[x->me];
+		double m = 0;
+		for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(p->me[M->offset + e]));
+		tmax[t] = m;
+		double Ln = x->ln >= 0 ? (double)p->lists[x->ln].len : 0, Lp = x->lp >= 0 ? (double)p->lists[x->lp].len : 0;
+		const jn_block_t *B = &p->blocks[term_dst[t]];
+		total += T->kind == JN_KIND_NP ? Lp * Ln : T->kind == JN_KIND_P ? Lp * (double)B->Nn : Ln * (double)B->Np;
+	}
+	if (target_units <= 0) target_units = 152 * 4;
+	double unit_target = total / target_units;
+	if (unit_target < 2048) unit_target = 2048;
+	double piece_target = unit_target / 4;
+	if (piece_target < 512) piece_target = 512;
+	/* terms per destination block, in evaluation order */
+	int *cnt = calloc(p->nblocks + 1, sizeof(int));
+	for (int t = 0; t < p->nterms; t++) cnt[term_dst[t] + 1]++;
+	for (int b = 0; b < p->nblocks; b++) cnt[b + 1] += cnt[b];
+	int *byb = malloc((p->nterms ? p->nterms : 1) * sizeof(int)), *fl = malloc((p->nblocks + 1) * sizeof(int));
+	memcpy(fl, cnt, (p->nblocks + 1) * sizeof(int));
+	for (int t = 0; t < p->nterms; t++) byb[fl[term_dst[t]]++] = t;
+	free(fl);
+	int64_t pcap = 4096, tcap = 1024;
+	p->pieces = malloc(pcap * sizeof(jn_piece_t));
+	p->btiles = malloc(tcap * sizeof(jn_btile_t));
+	p->max_tile_elems = 0;
+	p->abs_bound = 0;
+	double *bound = NULL;
+	size_t bcap = 0;
+	for (int b = 0; b < p->nblocks; b++) {
+		const jn_block_t *B = &p->blocks[b];
+		if (B->Np == 0 || B->Nn == 0) continue;
+		if (B->Nn > TILE_SMEM_ELEMS) {
+			free(tmax); free(cnt); free(byb); free(bound);
+			if (err) snprintf(err, errlen, "basis block %d has %lld neutron states: more than one shared-memory tile row",
+					  B->id, (long long)B->Nn);
+			return 1;
+		}
+		/* |M| bound per element of this block */
+		size_t E = (size_t)(B->Np * B->Nn);
+		if (E > bcap) { bcap = E; bound = realloc(bound, bcap * sizeof(double)); }
+		memset(bound, 0, E * sizeof(double));
+		for (int q = cnt[b]; q < cnt[b + 1]; q++) {
+			const jn_term_t *T = &p->terms[byb[q]];
+			for (int64_t r = 0; r < B->Np; r++) {
+				double np = T->kind == JN_KIND_N ? 1.0 : (double)(rp[T->p_ptr + r + 1] - rp[T->p_ptr + r]);
+				if (np == 0) continue;
+				for (int64_t c = 0; c < B->Nn; c++) {
+					double nn = T->kind == JN_KIND_P ? 1.0 : (double)(rp[T->n_ptr + c + 1] - rp[T->n_ptr + c]);
+					bound[r * B->Nn + c] += np * nn * tmax[byb[q]];
+				}
+			}
+		}
+		for (size_t e = 0; e < E; e++) p->abs_bound = fmax(p->abs_bound, bound[e]);
+		int64_t R = TILE_SMEM_ELEMS / B->Nn;
+		for (int64_t r0 = 0; r0 < B->Np; r0 += R) {
+			int64_t r1 = r0 + R < B->Np ? r0 + R : B->Np;
+			double acc = 0;
+			int64_t tile_start = p->npieces;
+			for (int q = cnt[b]; q <= cnt[b + 1]; q++) {
+				int last = q == cnt[b + 1];
+				if (!last) {
+					const jn_term_t *T = &p->terms[byb[q]];
+					uint32_t a0, a1;
+					double per, Ln = (double)(T->n_e1 - T->n_e0);
+					if (T->kind == JN_KIND_N) { a0 = (uint32_t)r0; a1 = (uint32_t)r1; per = Ln; }
+					else {
+						a0 = rp[T->p_ptr + r0]; a1 = rp[T->p_ptr + r1];
+						per = T->kind == JN_KIND_NP ? Ln : (double)B->Nn;
+					}
+					if (a1 <= a0 || per == 0) continue;
+					uint32_t step = (uint32_t)fmax(1.0, floor(piece_target / per));
+					for (uint32_t s = a0; s < a1; s += step) {
+						if (p->npieces == pcap) { pcap *= 2; p->pieces = realloc(p->pieces, pcap * sizeof(jn_piece_t)); }
+						jn_piece_t *P = &p->pieces[p->npieces++];
+						P->term = byb[q]; P->a0 = s; P->a1 = s + step < a1 ? s + step : a1; P->pad = 0;
+						acc += per * (P->a1 - P->a0);
+						if (acc >= unit_target) {
+							if (p->nbtiles == tcap) { tcap *= 2; p->btiles = realloc(p->btiles, tcap * sizeof(jn_btile_t)); }
+							jn_btile_t *Tl = &p->btiles[p->nbtiles++];
+							Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)r0;
+							Tl->nrows = (int32_t)(r1 - r0); Tl->pad = 0; Tl->pc0 = tile_start; Tl->pc1 = p->npieces;
+							tile_start = p->npieces;
+							acc = 0;
+						}
+					}
+				} else if (p->npieces > tile_start) {
+					if (p->nbtiles == tcap) { tcap *= 2; p->btiles = realloc(p->btiles, tcap * sizeof(jn_btile_t)); }
+					jn_btile_t *Tl = &p->btiles[p->nbtiles++];
+					Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)r0;
+					Tl->nrows = (int32_t)(r1 - r0); Tl->pad = 0; Tl->pc0 = tile_start; Tl->pc1 = p->npieces;
+				}
+			}
+			int64_t el = (r1 - r0) * B->Nn;
+			if (el > p->max_tile_elems) p->max_tile_elems = (int)el;
+		}
+	}
+	free(tmax); free(cnt); free(byb); free(bound);
+	/* heaviest tiles first */
+	return 0;
 }
 
 int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, const char *lists_dir,
@@ -496,6 +617,9 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	}
 	for (int l = 0; l < p->nlists; l++) {
 		jn_list_t *L = &p->lists[l];
+		if (L->nin > 65535 || L->nout > 65535)
+			ERR("index list %d maps sub-bases of %d x %d states: more than the 65535 of the packed device format", L->id,
+			    L->nin, L->nout);
 		for (int64_t e = 0; e < L->len; e++) {
 			int32_t a = L->triples[3 * e], b = L->triples[3 * e + 1];
 			if (a < 0 || a >= L->nin || b < 0 || b >= L->nout)
@@ -608,6 +732,10 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 				t.n_ent = 0;
 			}
 			t.me_off = p->mes[x->me].offset;
+			if (x->ln >= 0) {
+				t.n_e0 = p->rowptr[t.n_ptr];
+				t.n_e1 = p->rowptr[t.n_ptr + t.Nn_dst];
+			}
 			t.instr = i;
 			t.transpose = dir;
 			term_dst[p->nterms] = dst;
@@ -735,6 +863,8 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 		}
 		free(tile_cost); free(byblk); free(count);
 	}
+	/* block tiles for exact fixed-point accumulation */
+	if (build_block_tiles(p, term_dst, target_units, err, errlen)) goto fail;
 	free(term_dst);
 	free(slot_of_id); free(kind_of_id);
 	free(c.l); free(c.m); free(line);

@@ -77,6 +77,7 @@ typedef struct {
 	int64_t me_off;
 	int32_t instr;          /* evaluation-order index */
 	int32_t transpose;
+	uint32_t n_e0, n_e1;    /* absolute range of the neutron entries (N, NP) */
 } jn_term_t;
 
 typedef struct {
@@ -94,6 +95,27 @@ typedef struct {
 	int32_t chunk;
 	int64_t t0, t1;         /* range into jn_plan_t.unit_terms */
 } jn_unit_t;
+
+/* Block-tile plan (exact fixed-point accumulation).  A CTA owns rows
+ * [row0, row0+nrows) of one destination block in shared memory and
+ * processes pieces [pc0, pc1): each piece is one term restricted to a range
+ * of proton entries (NP and P terms, absolute indices into the entry array,
+ * all with their destination row inside the tile) or to a range of rows
+ * (N terms).  Sums are kept as 64-bit integers in units of 2^-S, so their
+ * order does not change the result. */
+typedef struct {
+	int64_t dst_off;
+	int32_t Nn;
+	int32_t row0, nrows;
+	int32_t pad;
+	int64_t pc0, pc1;       /* range into jn_plan_t.pieces */
+} jn_btile_t;
+
+typedef struct {
+	int32_t term;
+	uint32_t a0, a1;        /* proton-entry range (NP, P) or row range (N) */
+	int32_t pad;
+} jn_piece_t;
 
 typedef struct {
 	/* problem */
@@ -116,6 +138,10 @@ typedef struct {
 	int nunits;        jn_unit_t *units;
 	int64_t n_unit_terms; int32_t *unit_terms;
 	int64_t n_partial;
+	int nbtiles;       jn_btile_t *btiles;
+	int64_t npieces;   jn_piece_t *pieces;
+	int max_tile_elems;             /* shared-memory accumulator size needed */
+	double abs_bound;               /* max over y elements of sum |M| over its contributions */
 	/* accounting */
 	int64_t list_entries;           /* sum of distinct list lengths */
 	int64_t me_elements;            /* sum of distinct ME block lengths */

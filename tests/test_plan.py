@@ -112,3 +112,22 @@ def test_missing_file_reports_path(problem, tmp_path):
     os.remove(f"{c}/index_lists/{first_list(c)}")
     L, h, err = open_plan(c, Z, N)
     assert not h and "Could not open" in err
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b"])
+@pytest.mark.parametrize("units", [1, 97, 608])
+def test_block_tile_plan_model_matches_port(problem, name, units):
+    """CPU model of the fixed-point block-tile kernels: every index checked,
+    FP64 within 1e-12 and FP32 within 2e-6 of the oracle."""
+    d, Z, N, *_ = problem(name)
+    L, h, err = open_plan(d, Z, N, units)
+    assert h, err
+    L.emu_matvec3.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(units).standard_normal(D)
+    want = oracle.Port(d).matvec(x)
+    for f32, tol in ((0, 1e-12), (1, 2e-6)):
+        y = np.zeros(D)
+        assert L.emu_matvec3(h, x.ctypes.data, y.ctypes.data, 0, f32) == 0
+        assert np.abs(y - want).max() <= tol * np.abs(want).max()
+    L.emu_close(h)
