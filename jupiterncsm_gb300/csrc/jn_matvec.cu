@@ -255,90 +255,121 @@ __device__ __forceinline__ int pow2_at_least(int v)
  * 64-bit accumulator.  Integer addition is exact and associative, so the
  * result does not depend on the order in which warps and CTAs run.
  */
+/* 64-bit two's-complement add into separate low / high 32-bit shared words
+ * with two native 32-bit atomics: the carry of each addition is taken from
+ * the value its own atomic saw, so (high, low) holds the exact sum modulo
+ * 2^64 once every addition has landed, whatever their interleaving. */
+__device__ __forceinline__ void add_fixed(unsigned int *lo, unsigned int *hi, int i, long long v)
+{
+	if (v == 0) return;
+	const unsigned int l = (unsigned int)(unsigned long long)v;
+	unsigned int h = (unsigned int)((unsigned long long)v >> 32);
+	const unsigned int old = atomicAdd(lo + i, l);
+	h += (unsigned int)(old + l < old);
+	if (h) atomicAdd(hi + i, h);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles,
-							       const jn_piece_t *__restrict__ pieces,
+							       const jn_piece_t *__restrict__ tasks,
 							       const T *__restrict__ x, const T *__restrict__ me,
 							       unsigned long long *__restrict__ gacc,
 							       const unsigned int *__restrict__ xmax_bits, double abs_bound)
 {
-	extern __shared__ unsigned long long sacc[];
+	extern __shared__ unsigned int sacc[];
+	__shared__ int next_task;
 	const jn_btile_t tl = tiles[blockIdx.x];
-	const int Nn = tl.Nn;
-	const int E = tl.nrows * Nn;
-	for (int i = threadIdx.x; i < E; i += blockDim.x) sacc[i] = 0ull;
+	const int Nn = tl.Nn, stride = tl.stride;
+	const int Ep = tl.nrows * stride;
+	unsigned int *lo = sacc, *hi = sacc + Ep;
+	for (int i = threadIdx.x; i < 2 * Ep; i += blockDim.x) sacc[i] = 0u;
+	if (threadIdx.x == 0) next_task = 0;
 	const int S = fixed_exponent(*xmax_bits, abs_bound);
 	const T scale = (T)ldexp(1.0, S);
 	__syncthreads();
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	for (int64_t pc = tl.pc0 + warp; pc < tl.pc1; pc += TILE_THREADS / 32) {
-		const jn_piece_t pcs = pieces[pc];
-		const jn_term_t t = P.terms[pcs.term];
-		const T *__restrict__ xs = x + t.src_off;
-		const T *__restrict__ mb = me + t.me_off;
-		const bool tr = t.transpose != 0;
-		const int Ns = t.Nn_src;
-		if (t.kind == JN_KIND_NP || t.kind == JN_KIND_P) {
-			const int ncol = t.kind == JN_KIND_NP ? (int)(t.n_e1 - t.n_e0) : t.Nn_dst;
-			const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
-			const int gi = lane / b, gj = lane % b;
-			const uint32_t na = pcs.a1 - pcs.a0, per = (na + a - 1) / a;
-			const uint32_t e0 = pcs.a0 + gi * per, e1 = min(pcs.a1, e0 + per);
-			for (int cj = gj; cj < ncol; cj += b) {
-				int scol, dcol;
-				uint32_t kn = 0, sn = 0;
-				if (t.kind == JN_KIND_NP) {
-					const uint2 qn = __ldg(P.ent + t.n_e0 + cj);
-					const int nin = qn.x & 0xffff, nout = qn.x >> 16;
-					scol = tr ? nout : nin;
-					dcol = tr ? nin : nout;
-					kn = qn.y & MASK31;
-					sn = qn.y;
-				} else {
-					scol = dcol = cj;
-				}
-				T run = 0;
-				int cur = -1;
-				for (uint32_t ep = e0; ep < e1; ep++) {
-					const uint2 qp = __ldg(P.ent + ep);
-					const int pin = qp.x & 0xffff, pout = qp.x >> 16;
-					const int srow = tr ? pout : pin, drow = tr ? pin : pout;
-					if (drow != cur) {
-						if (cur >= 0)
-							atomicAdd(&sacc[(cur - tl.row0) * Nn + dcol],
-								  (unsigned long long)to_fixed<T>(run * scale));
-						run = 0;
-						cur = drow;
-					}
-					const uint32_t kp = qp.y & MASK31;
-					const T m = __ldg(mb + (t.kind == JN_KIND_NP ? (size_t)kn + (size_t)t.nd * kp : (size_t)kp));
-					if (t.kind == JN_KIND_P && tiny(m)) continue;
-					run = fma(flip_sign(m, qp.y ^ sn), __ldg(xs + (size_t)srow * Ns + scol), run);
-				}
-				if (cur >= 0)
-					atomicAdd(&sacc[(cur - tl.row0) * Nn + dcol], (unsigned long long)to_fixed<T>(run * scale));
+	const int lane = threadIdx.x & 31;
+	const int ntask = (int)(tl.pc1 - tl.pc0);
+	const uint32_t *__restrict__ rp = P.rowptr;
+	for (;;) {
+		int k = 0;
+		if (lane == 0) k = atomicAdd(&next_task, 1);
+		k = __shfl_sync(0xffffffffu, k, 0);
+		if (k >= ntask) break;
+		const jn_piece_t task = tasks[tl.pc0 + k];
+		if (lane >= task.count) continue;
+		const jn_term_t &tg = P.terms[task.term];
+		const int64_t src_off = tg.src_off, me_off = tg.me_off;
+		const int Ns = tg.Nn_src, nd = tg.nd;
+		const bool tr = tg.transpose != 0;
+		const T *__restrict__ xs = x + src_off;
+		const T *__restrict__ mb = me + me_off;
+		T run = 0;
+		int drow, dcol;
+		if (task.kind == JN_TASK_EN) {
+			const uint2 qn = __ldg(P.ent + task.start + lane);
+			const int nin = qn.x & 0xffff, nout = qn.x >> 16;
+			const int scol = tr ? nout : nin;
+			dcol = tr ? nin : nout;
+			drow = task.fixed;
+			const uint32_t kn = qn.y & MASK31, sn = qn.y;
+			const uint32_t i0 = __ldg(rp + tg.p_ptr + drow), i1 = __ldg(rp + tg.p_ptr + drow + 1);
+			for (uint32_t i = i0; i < i1; i++) {
+				const uint2 qp = __ldg(P.ent + i);
+				const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+				const T m = __ldg(mb + kn + (size_t)nd * (qp.y & MASK31));
+				run = fma(flip_sign(m, qp.y ^ sn), __ldg(xs + srow * Ns + scol), run);
+			}
+		} else if (task.kind == JN_TASK_EP) {
+			const uint2 qp = __ldg(P.ent + task.start + lane);
+			const int pin = qp.x & 0xffff, pout = qp.x >> 16;
+			const int srow = tr ? pout : pin;
+			drow = tr ? pin : pout;
+			dcol = task.fixed;
+			const T *__restrict__ mrow = mb + (size_t)nd * (qp.y & MASK31);
+			const T *__restrict__ xrow = xs + srow * Ns;
+			const uint32_t j0 = __ldg(rp + tg.n_ptr + dcol), j1 = __ldg(rp + tg.n_ptr + dcol + 1);
+			for (uint32_t j = j0; j < j1; j++) {
+				const uint2 qn = __ldg(P.ent + j);
+				const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+				const T m = __ldg(mrow + (qn.y & MASK31));
+				run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xrow + scol), run);
+			}
+		} else if (task.kind == JN_TASK_PC) {
+			const int c = task.start + lane;
+			drow = task.fixed;
+			dcol = c;
+			const uint32_t i0 = __ldg(rp + tg.p_ptr + drow), i1 = __ldg(rp + tg.p_ptr + drow + 1);
+			for (uint32_t i = i0; i < i1; i++) {
+				const uint2 qp = __ldg(P.ent + i);
+				const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+				const T m = __ldg(mb + (qp.y & MASK31));
+				if (tiny(m)) continue;
+				run = fma(flip_sign(m, qp.y), __ldg(xs + srow * Ns + c), run);
 			}
 		} else {
-			/* neutron-only term: the proton row is a spectator, rows [a0, a1) */
-			const int ncol = (int)(t.n_e1 - t.n_e0);
-			const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
-			const int gi = lane / b, gj = lane % b;
-			for (int cj = gj; cj < ncol; cj += b) {
-				const uint2 qn = __ldg(P.ent + t.n_e0 + cj);
-				const int nin = qn.x & 0xffff, nout = qn.x >> 16;
-				const int scol = tr ? nout : nin, dcol = tr ? nin : nout;
-				const T m = flip_sign(__ldg(mb + (qn.y & MASK31)), qn.y);
+			const int r = task.start + lane;
+			drow = r;
+			dcol = task.fixed;
+			const T *__restrict__ xrow = xs + r * Ns;
+			const uint32_t j0 = __ldg(rp + tg.n_ptr + dcol), j1 = __ldg(rp + tg.n_ptr + dcol + 1);
+			for (uint32_t j = j0; j < j1; j++) {
+				const uint2 qn = __ldg(P.ent + j);
+				const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+				const T m = __ldg(mb + (qn.y & MASK31));
 				if (tiny(m)) continue;
-				for (uint32_t r = pcs.a0 + gi; r < pcs.a1; r += a)
-					atomicAdd(&sacc[(r - tl.row0) * Nn + dcol],
-						  (unsigned long long)to_fixed<T>(m * __ldg(xs + (size_t)r * Ns + scol) * scale));
+				run = fma(flip_sign(m, qn.y), __ldg(xrow + scol), run);
 			}
 		}
+		add_fixed(lo, hi, (drow - tl.row0) * stride + dcol, to_fixed<T>(run * scale));
 	}
 	__syncthreads();
 	unsigned long long *g = gacc + tl.dst_off + (int64_t)tl.row0 * Nn;
-	for (int i = threadIdx.x; i < E; i += blockDim.x)
-		if (sacc[i]) atomicAdd(g + i, sacc[i]);
+	const int E = tl.nrows * Nn;
+	for (int i = threadIdx.x; i < E; i += blockDim.x) {
+		const int si = (i / Nn) * stride + i % Nn;
+		const unsigned long long v = (unsigned long long)lo[si] | ((unsigned long long)hi[si] << 32);
+		if (v) atomicAdd(g + i, v);
+	}
 }
 
 /* y (+)= acc * 2^-S, and the accumulator is cleared for the next product */
@@ -426,7 +457,7 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	}
 	{
 		cudaError_t z = cudaMemset(c->d_gacc, 0, (p->dim ? p->dim : 1) * sizeof(unsigned long long));
-		size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * sizeof(unsigned long long);
+		size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
 		if (z == cudaSuccess)
 			z = cudaFuncSetAttribute(jn_tile_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (z == cudaSuccess)
@@ -508,7 +539,7 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		if (mid) cudaEventRecord(mid, st);
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
 	} else {
-		const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * sizeof(unsigned long long);
+		const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
 		cudaError_t e0 = cudaMemsetAsync(c->d_xmax, 0, sizeof(unsigned int), st);
 		if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
 		if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? c->d_x32 : NULL, p->dim, c->d_xmax);

@@ -353,38 +353,43 @@ static int cmp_unit_cost(const void *a, const void *b)
 
 /* shared-memory accumulator budget of one CTA, in 64-bit elements */
 #define TILE_SMEM_ELEMS 8192
+/* fixed per-task cost in the work model, in multiply-add units */
+#define TASK_OVERHEAD 6.0
+
+typedef struct { jn_piece_t t; double cost; } task_cost_t;
+
+static int cmp_task_cost(const void *a, const void *b)
+{
+	const task_cost_t *x = a, *y = b;
+	if (x->cost != y->cost) return x->cost < y->cost ? 1 : -1;
+	if (x->t.term != y->t.term) return x->t.term - y->t.term;
+	if (x->t.fixed != y->t.fixed) return (int)x->t.fixed - (int)y->t.fixed;
+	return x->t.start < y->t.start ? -1 : (x->t.start > y->t.start);
+}
 
 /*
- * Block tiles: every destination block is cut into row ranges whose
- * accumulator fits in shared memory; the terms touching a range become
- * pieces (proton-entry sub-ranges for NP and P terms, row sub-ranges for N
- * terms) of bounded work, packed into tiles of similar work.  Also computes
+ * Block tiles and warp tasks.  Every destination block is cut into row
+ * ranges whose accumulator fits in shared memory.  Each term touching a
+ * range becomes warp tasks in the orientation that keeps more lanes busy:
+ *   NP  lanes over the neutron entries, each walking Pout(row) for one row
+ *       (EN), or lanes over the proton entries, each walking Nout(col) for
+ *       one column (EP);
+ *   P   lanes over columns, walking Pout(row) (PC);
+ *   N   lanes over rows, walking Nout(col) (NR).
+ * Tasks are packed into tiles of similar work, longest first.  Also computes
  * abs_bound, the largest sum of |M| over the contributions to one element,
  * which bounds |y| by abs_bound * max|x| for the fixed-point scale.
  */
 static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units, char *err, size_t errlen)
 {
 	const uint32_t *rp = p->rowptr;
-	double total = 0;
-	/* per-term work and the largest |M| of its block */
 	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
 	for (int t = 0; t < p->nterms; t++) {
-		const jn_term_t *T = &p->terms[t];
-		const jn_instr_t *x = &p->instr[T->instr];
-		const jn_me_t *M = &p->mes[x->me];
+		const jn_me_t *M = &p->mes[p->instr[p->terms[t].instr].me];
 		double m = 0;
 		for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(p->me[M->offset + e]));
 		tmax[t] = m;
-		double Ln = x->ln >= 0 ? (double)p->lists[x->ln].len : 0, Lp = x->lp >= 0 ? (double)p->lists[x->lp].len : 0;
-		const jn_block_t *B = &p->blocks[term_dst[t]];
-		total += T->kind == JN_KIND_NP ? Lp * Ln : T->kind == JN_KIND_P ? Lp * (double)B->Nn : Ln * (double)B->Np;
 	}
-	if (target_units <= 0) target_units = 152 * 4;
-	double unit_target = total / target_units;
-	if (unit_target < 2048) unit_target = 2048;
-	double piece_target = unit_target / 4;
-	if (piece_target < 512) piece_target = 512;
-	/* terms per destination block, in evaluation order */
 	int *cnt = calloc(p->nblocks + 1, sizeof(int));
 	for (int t = 0; t < p->nterms; t++) cnt[term_dst[t] + 1]++;
 	for (int b = 0; b < p->nblocks; b++) cnt[b + 1] += cnt[b];
@@ -392,18 +397,33 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	memcpy(fl, cnt, (p->nblocks + 1) * sizeof(int));
 	for (int t = 0; t < p->nterms; t++) byb[fl[term_dst[t]]++] = t;
 	free(fl);
-	int64_t pcap = 4096, tcap = 1024;
-	p->pieces = malloc(pcap * sizeof(jn_piece_t));
-	p->btiles = malloc(tcap * sizeof(jn_btile_t));
+	/* pass 1: tasks of every (block, row range), with their costs */
+	typedef struct { int b; int64_t r0, r1; int64_t t0, t1; double cost; } range_t;
+	range_t *ranges = NULL;
+	int nranges = 0, rcap = 0;
+	task_cost_t *tasks = NULL;
+	int64_t ntasks = 0, tcap = 0;
+	double total = 0;
 	p->max_tile_elems = 0;
 	p->abs_bound = 0;
 	double *bound = NULL;
 	size_t bcap = 0;
+#define PUSH_TASK(TERM, START, FIXED, COUNT, KIND, COST)                                       \
+	do {                                                                                   \
+		if (ntasks == tcap) { tcap = tcap ? 2 * tcap : 65536; tasks = realloc(tasks, tcap * sizeof *tasks); } \
+		task_cost_t *q_ = &tasks[ntasks++];                                            \
+		memset(q_, 0, sizeof *q_);                                                     \
+		q_->t.term = (TERM); q_->t.start = (uint32_t)(START); q_->t.fixed = (uint16_t)(FIXED); \
+		q_->t.count = (uint8_t)(COUNT); q_->t.kind = (uint8_t)(KIND);                  \
+		q_->cost = TASK_OVERHEAD + (COST);                                             \
+		total += q_->cost;                                                             \
+	} while (0)
 	for (int b = 0; b < p->nblocks; b++) {
 		const jn_block_t *B = &p->blocks[b];
 		if (B->Np == 0 || B->Nn == 0) continue;
-		if (B->Nn > TILE_SMEM_ELEMS) {
-			free(tmax); free(cnt); free(byb); free(bound);
+		int64_t stride = B->Nn | 1;
+		if (stride > TILE_SMEM_ELEMS) {
+			free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
 			if (err) snprintf(err, errlen, "basis block %d has %lld neutron states: more than one shared-memory tile row",
 					  B->id, (long long)B->Nn);
 			return 1;
@@ -424,51 +444,91 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 			}
 		}
 		for (size_t e = 0; e < E; e++) p->abs_bound = fmax(p->abs_bound, bound[e]);
-		int64_t R = TILE_SMEM_ELEMS / B->Nn;
+		int64_t R = TILE_SMEM_ELEMS / stride;
 		for (int64_t r0 = 0; r0 < B->Np; r0 += R) {
 			int64_t r1 = r0 + R < B->Np ? r0 + R : B->Np;
-			double acc = 0;
-			int64_t tile_start = p->npieces;
-			for (int q = cnt[b]; q <= cnt[b + 1]; q++) {
-				int last = q == cnt[b + 1];
-				if (!last) {
-					const jn_term_t *T = &p->terms[byb[q]];
-					uint32_t a0, a1;
-					double per, Ln = (double)(T->n_e1 - T->n_e0);
-					if (T->kind == JN_KIND_N) { a0 = (uint32_t)r0; a1 = (uint32_t)r1; per = Ln; }
-					else {
-						a0 = rp[T->p_ptr + r0]; a1 = rp[T->p_ptr + r1];
-						per = T->kind == JN_KIND_NP ? Ln : (double)B->Nn;
-					}
-					if (a1 <= a0 || per == 0) continue;
-					uint32_t step = (uint32_t)fmax(1.0, floor(piece_target / per));
-					for (uint32_t s = a0; s < a1; s += step) {
-						if (p->npieces == pcap) { pcap *= 2; p->pieces = realloc(p->pieces, pcap * sizeof(jn_piece_t)); }
-						jn_piece_t *P = &p->pieces[p->npieces++];
-						P->term = byb[q]; P->a0 = s; P->a1 = s + step < a1 ? s + step : a1; P->pad = 0;
-						acc += per * (P->a1 - P->a0);
-						if (acc >= unit_target) {
-							if (p->nbtiles == tcap) { tcap *= 2; p->btiles = realloc(p->btiles, tcap * sizeof(jn_btile_t)); }
-							jn_btile_t *Tl = &p->btiles[p->nbtiles++];
-							Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)r0;
-							Tl->nrows = (int32_t)(r1 - r0); Tl->pad = 0; Tl->pc0 = tile_start; Tl->pc1 = p->npieces;
-							tile_start = p->npieces;
-							acc = 0;
+			if (nranges == rcap) { rcap = rcap ? 2 * rcap : 256; ranges = realloc(ranges, rcap * sizeof *ranges); }
+			range_t *rg = &ranges[nranges++];
+			rg->b = b; rg->r0 = r0; rg->r1 = r1; rg->t0 = ntasks;
+			double before = total;
+			for (int q = cnt[b]; q < cnt[b + 1]; q++) {
+				const int ti = byb[q];
+				const jn_term_t *T = &p->terms[ti];
+				const int64_t Ln = (int64_t)T->n_e1 - (int64_t)T->n_e0;
+				if (T->kind == JN_KIND_NP) {
+					const int64_t ep0 = rp[T->p_ptr + r0], ep1 = rp[T->p_ptr + r1], Lp = ep1 - ep0;
+					if (Lp == 0 || Ln == 0) continue;
+					double eff_en = (double)Ln / (32.0 * ceil(Ln / 32.0)), eff_ep = (double)Lp / (32.0 * ceil(Lp / 32.0));
+					if (eff_en >= eff_ep) {
+						for (int64_t r = r0; r < r1; r++) {
+							int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
+							if (!pr) continue;
+							for (int64_t s = 0; s < Ln; s += 32)
+								PUSH_TASK(ti, T->n_e0 + s, r, Ln - s < 32 ? Ln - s : 32, JN_TASK_EN, (double)pr);
+						}
+					} else {
+						for (int64_t c = 0; c < B->Nn; c++) {
+							int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
+							if (!nc) continue;
+							for (int64_t s = ep0; s < ep1; s += 32)
+								PUSH_TASK(ti, s, c, ep1 - s < 32 ? ep1 - s : 32, JN_TASK_EP, (double)nc);
 						}
 					}
-				} else if (p->npieces > tile_start) {
-					if (p->nbtiles == tcap) { tcap *= 2; p->btiles = realloc(p->btiles, tcap * sizeof(jn_btile_t)); }
-					jn_btile_t *Tl = &p->btiles[p->nbtiles++];
-					Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)r0;
-					Tl->nrows = (int32_t)(r1 - r0); Tl->pad = 0; Tl->pc0 = tile_start; Tl->pc1 = p->npieces;
+				} else if (T->kind == JN_KIND_P) {
+					for (int64_t r = r0; r < r1; r++) {
+						int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
+						if (!pr) continue;
+						for (int64_t c = 0; c < B->Nn; c += 32)
+							PUSH_TASK(ti, c, r, B->Nn - c < 32 ? B->Nn - c : 32, JN_TASK_PC, (double)pr);
+					}
+				} else {
+					for (int64_t c = 0; c < B->Nn; c++) {
+						int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
+						if (!nc) continue;
+						for (int64_t r = r0; r < r1; r += 32)
+							PUSH_TASK(ti, r, c, r1 - r < 32 ? r1 - r : 32, JN_TASK_NR, (double)nc);
+					}
 				}
 			}
-			int64_t el = (r1 - r0) * B->Nn;
+			rg->t1 = ntasks;
+			rg->cost = total - before;
+			int64_t el = (r1 - r0) * stride;
 			if (el > p->max_tile_elems) p->max_tile_elems = (int)el;
 		}
 	}
-	free(tmax); free(cnt); free(byb); free(bound);
-	/* heaviest tiles first */
+#undef PUSH_TASK
+	/* pass 2: tiles of similar work, tasks longest first inside a tile */
+	int ntile_target = target_units > 0 ? target_units / 6 : 152 * 8;
+	if (ntile_target < 1) ntile_target = 1;
+	double tile_target = total / ntile_target;
+	if (tile_target < 64 * 32) tile_target = 64 * 32;
+	p->pieces = malloc((ntasks ? ntasks : 1) * sizeof(jn_piece_t));
+	int tmax_tiles = 1024;
+	p->btiles = malloc(tmax_tiles * sizeof(jn_btile_t));
+	for (int ri = 0; ri < nranges; ri++) {
+		const range_t *rg = &ranges[ri];
+		const jn_block_t *B = &p->blocks[rg->b];
+		int nt = (int)ceil(rg->cost / tile_target);
+		if (nt < 1) nt = 1;
+		double per = rg->cost / nt, acc = 0;
+		int64_t begin = rg->t0;
+		for (int64_t k = rg->t0; k < rg->t1; k++) {
+			acc += tasks[k].cost;
+			if (acc >= per || k == rg->t1 - 1) {
+				if (p->nbtiles == tmax_tiles) { tmax_tiles *= 2; p->btiles = realloc(p->btiles, tmax_tiles * sizeof(jn_btile_t)); }
+				jn_btile_t *Tl = &p->btiles[p->nbtiles++];
+				Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)rg->r0;
+				Tl->nrows = (int32_t)(rg->r1 - rg->r0); Tl->stride = (int32_t)(B->Nn | 1);
+				qsort(tasks + begin, k + 1 - begin, sizeof *tasks, cmp_task_cost);
+				Tl->pc0 = p->npieces;
+				for (int64_t q = begin; q <= k; q++) p->pieces[p->npieces++] = tasks[q].t;
+				Tl->pc1 = p->npieces;
+				begin = k + 1;
+				acc = 0;
+			}
+		}
+	}
+	free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
 	return 0;
 }
 

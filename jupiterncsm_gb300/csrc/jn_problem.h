@@ -97,24 +97,35 @@ typedef struct {
 } jn_unit_t;
 
 /* Block-tile plan (exact fixed-point accumulation).  A CTA owns rows
- * [row0, row0+nrows) of one destination block in shared memory and
- * processes pieces [pc0, pc1): each piece is one term restricted to a range
- * of proton entries (NP and P terms, absolute indices into the entry array,
- * all with their destination row inside the tile) or to a range of rows
- * (N terms).  Sums are kept as 64-bit integers in units of 2^-S, so their
- * order does not change the result. */
+ * [row0, row0+nrows) of one destination block in shared memory and runs the
+ * warp tasks [pc0, pc1).  A warp task gives each of its `count` lanes one
+ * run: a list entry (or column / row) that stays fixed while the lane walks
+ * the matching entries of the other list, all landing on one output
+ * element.  Runs are summed in T arithmetic and added to the tile as 64-bit
+ * integers in units of 2^-S, so the order of the runs does not change the
+ * result. */
 typedef struct {
 	int64_t dst_off;
 	int32_t Nn;
 	int32_t row0, nrows;
-	int32_t pad;
+	int32_t stride;         /* shared-memory row stride (odd) */
 	int64_t pc0, pc1;       /* range into jn_plan_t.pieces */
 } jn_btile_t;
 
+enum {
+	JN_TASK_EN = 0,         /* NP: lanes over neutron entries [start, start+count), walk Pout(fixed row) */
+	JN_TASK_EP = 1,         /* NP: lanes over proton entries [start, ...), walk Nout(fixed column) */
+	JN_TASK_PC = 2,         /* P: lanes over columns [start, ...), walk Pout(fixed row) */
+	JN_TASK_NR = 3          /* N: lanes over rows [start, ...), walk Nout(fixed column) */
+};
+
 typedef struct {
 	int32_t term;
-	uint32_t a0, a1;        /* proton-entry range (NP, P) or row range (N) */
-	int32_t pad;
+	uint32_t start;         /* first lane's entry (absolute entry index) / column / row */
+	uint16_t fixed;         /* destination row (EN, PC) or column (EP, NR) */
+	uint8_t count;          /* active lanes, 1..32 */
+	uint8_t kind;           /* JN_TASK_* */
+	uint32_t pad;
 } jn_piece_t;
 
 typedef struct {

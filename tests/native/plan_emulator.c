@@ -113,98 +113,87 @@ static int fixed_exponent(float xmax, double bound)
 	return S < -60 ? -60 : (S > 100 ? 100 : S);
 }
 
-static int pow2_at_least(int v) { int b = 1; while (b < v) b <<= 1; return b; }
 
 static int tiny64(double m) { uint64_t b; memcpy(&b, &m, 8); return (b & 0x7fffffffffffffffull) < 0x3D719799812DEA11ull; }
 
 static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x64, const float *x32, const double *me64,
 		       const float *me32, int f32, int S, int64_t *gacc)
 {
-	const int Nn = tl->Nn, E = tl->nrows * Nn;
+	const int Nn = tl->Nn, stride = tl->stride, E = tl->nrows * Nn;
+	CHECK(stride >= Nn && (stride & 1));
+	CHECK(tl->nrows * stride <= P->max_tile_elems);
 	int64_t *sacc = calloc(E ? E : 1, sizeof(int64_t));
-	const uint32_t *ent = P->ent;
+	const uint32_t *ent = P->ent, *rp = P->rowptr;
 	double scale = ldexp(1.0, S);
 	float scalef = (float)scale;
-	for (int64_t pc = tl->pc0; pc < tl->pc1; pc++) {
-		const jn_piece_t *pcs = &P->pieces[pc];
-		CHECK(pcs->term >= 0 && pcs->term < P->nterms);
-		const jn_term_t *t = &P->terms[pcs->term];
-		const int tr = t->transpose != 0, Ns = t->Nn_src;
-		for (int lane = 0; lane < 32; lane++) {
-			if (t->kind != JN_KIND_N) {
-				const int ncol = t->kind == JN_KIND_NP ? (int)(t->n_e1 - t->n_e0) : t->Nn_dst;
-				const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
-				const int gi = lane / b, gj = lane % b;
-				const uint32_t na = pcs->a1 - pcs->a0, per = (na + a - 1) / a;
-				const uint32_t e0 = pcs->a0 + gi * per, e1 = (pcs->a1 < e0 + per) ? pcs->a1 : e0 + per;
-				for (int cj = gj; cj < ncol; cj += b) {
-					int scol, dcol;
-					uint32_t kn = 0, sn = 0;
-					if (t->kind == JN_KIND_NP) {
-						CHECK(t->n_e0 + cj < (uint64_t)P->n_ent);
-						uint32_t qx = ent[2 * (t->n_e0 + cj)], qy = ent[2 * (t->n_e0 + cj) + 1];
-						int nin = qx & 0xffff, nout = qx >> 16;
-						scol = tr ? nout : nin; dcol = tr ? nin : nout;
-						kn = qy & 0x7fffffffu; sn = qy;
-					} else { scol = dcol = cj; }
-					CHECK(dcol >= 0 && dcol < Nn);
-					double run = 0; float runf = 0; int cur = -1;
-					for (uint32_t ep = e0; ep < e1; ep++) {
-						CHECK(ep < (uint64_t)P->n_ent);
-						uint32_t qx = ent[2 * ep], qy = ent[2 * ep + 1];
-						int pin = qx & 0xffff, pout = qx >> 16;
-						int srow = tr ? pout : pin, drow = tr ? pin : pout;
-						if (drow != cur) {
-							if (cur >= 0) sacc[(cur - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
-							run = 0; runf = 0; cur = drow;
-							CHECK(cur >= tl->row0 && cur < tl->row0 + tl->nrows);
-						}
-						uint32_t kp = qy & 0x7fffffffu;
-						size_t mi = t->kind == JN_KIND_NP ? (size_t)kn + (size_t)t->nd * kp : (size_t)kp;
-						CHECK(t->me_off + (int64_t)mi < P->n_me);
-						size_t xi = (size_t)t->src_off + (size_t)srow * Ns + scol;
-						CHECK((int64_t)xi < P->dim);
-						int neg = ((qy ^ sn) & 0x80000000u) != 0;
-						if (f32) {
-							float m = me32[t->me_off + mi];
-							if (neg) m = -m;
-							runf = fmaf(m, x32[xi], runf);
-						} else {
-							double m = me64[t->me_off + mi];
-							if (t->kind == JN_KIND_P && tiny64(m)) continue;
-							if (neg) m = -m;
-							run = fma(m, x64[xi], run);
-						}
-					}
-					if (cur >= 0) sacc[(cur - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
+	for (int64_t k = tl->pc0; k < tl->pc1; k++) {
+		const jn_piece_t *task = &P->pieces[k];
+		CHECK(task->term >= 0 && task->term < P->nterms && task->count >= 1 && task->count <= 32);
+		const jn_term_t *t = &P->terms[task->term];
+		const int tr = t->transpose != 0, Ns = t->Nn_src, nd = t->nd;
+		for (int lane = 0; lane < task->count; lane++) {
+			double run = 0;
+			float runf = 0;
+			int drow = 0, dcol = 0;
+#define VISIT(MI, XI, NEG, SKIP_TINY)                                                       \
+			do {                                                                        \
+				CHECK(t->me_off + (int64_t)(MI) < P->n_me);                          \
+				CHECK((int64_t)(XI) >= 0 && (int64_t)(XI) < P->dim);                 \
+				if (f32) { float m_ = me32[t->me_off + (MI)]; if (NEG) m_ = -m_; runf = fmaf(m_, x32[XI], runf); } \
+				else { double m_ = me64[t->me_off + (MI)]; if ((SKIP_TINY) && tiny64(m_)) break; if (NEG) m_ = -m_; run = fma(m_, x64[XI], run); } \
+			} while (0)
+			if (task->kind == JN_TASK_EN) {
+				uint64_t en = task->start + lane;
+				CHECK(en >= t->n_e0 && en < t->n_e1);
+				uint32_t qx = ent[2 * en], qy = ent[2 * en + 1];
+				int nin = qx & 0xffff, nout = qx >> 16;
+				int scol = tr ? nout : nin;
+				dcol = tr ? nin : nout;
+				drow = task->fixed;
+				for (uint32_t i = rp[t->p_ptr + drow]; i < rp[t->p_ptr + drow + 1]; i++) {
+					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
+					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+					int prow = tr ? (int)(px & 0xffff) : (int)(px >> 16);
+					CHECK(prow == drow);
+					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
+					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
+				}
+			} else if (task->kind == JN_TASK_EP) {
+				uint64_t ep = task->start + lane;
+				CHECK(ep < (uint64_t)P->n_ent);
+				uint32_t px = ent[2 * ep], py = ent[2 * ep + 1];
+				int pin = px & 0xffff, pout = px >> 16;
+				int srow = tr ? pout : pin;
+				drow = tr ? pin : pout;
+				dcol = task->fixed;
+				for (uint32_t j = rp[t->n_ptr + dcol]; j < rp[t->n_ptr + dcol + 1]; j++) {
+					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
+					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
+					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
+				}
+			} else if (task->kind == JN_TASK_PC) {
+				int c = task->start + lane;
+				drow = task->fixed;
+				dcol = c;
+				for (uint32_t i = rp[t->p_ptr + drow]; i < rp[t->p_ptr + drow + 1]; i++) {
+					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
+					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+					VISIT(py & 0x7fffffffu, t->src_off + srow * Ns + c, (py & 0x80000000u) != 0, 1);
 				}
 			} else {
-				const int ncol = (int)(t->n_e1 - t->n_e0);
-				const int b = ncol >= 32 ? 32 : pow2_at_least(ncol), a = 32 / b;
-				const int gi = lane / b, gj = lane % b;
-				for (int cj = gj; cj < ncol; cj += b) {
-					uint32_t qx = ent[2 * (t->n_e0 + cj)], qy = ent[2 * (t->n_e0 + cj) + 1];
-					int nin = qx & 0xffff, nout = qx >> 16;
-					int scol = tr ? nout : nin, dcol = tr ? nin : nout;
-					CHECK(dcol < Nn);
-					int neg = (qy & 0x80000000u) != 0;
-					for (uint32_t r = pcs->a0 + gi; r < pcs->a1; r += a) {
-						CHECK((int)r >= tl->row0 && (int)r < tl->row0 + tl->nrows);
-						size_t xi = (size_t)t->src_off + (size_t)r * Ns + scol;
-						CHECK((int64_t)xi < P->dim);
-						if (f32) {
-							float m = me32[t->me_off + (qy & 0x7fffffffu)];
-							if (neg) m = -m;
-							sacc[(r - tl->row0) * Nn + dcol] += llrintf(m * x32[xi] * scalef);
-						} else {
-							double m = me64[t->me_off + (qy & 0x7fffffffu)];
-							if (tiny64(m)) continue;
-							if (neg) m = -m;
-							sacc[(r - tl->row0) * Nn + dcol] += llrint(m * x64[xi] * scale);
-						}
-					}
+				int r = task->start + lane;
+				drow = r;
+				dcol = task->fixed;
+				for (uint32_t j = rp[t->n_ptr + dcol]; j < rp[t->n_ptr + dcol + 1]; j++) {
+					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
+					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+					VISIT(qy & 0x7fffffffu, t->src_off + r * Ns + scol, (qy & 0x80000000u) != 0, 1);
 				}
 			}
+#undef VISIT
+			CHECK(drow >= tl->row0 && drow < tl->row0 + tl->nrows && dcol >= 0 && dcol < Nn);
+			sacc[(drow - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
 		}
 	}
 	for (int i = 0; i < E; i++) gacc[tl->dst_off + (int64_t)tl->row0 * Nn + i] += sacc[i];
