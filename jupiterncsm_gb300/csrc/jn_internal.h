@@ -43,6 +43,7 @@ struct jn_ctx {
 	int engine;             /* 3: block tiles with exact fixed-point sums (default); 2: warp pieces */
 	jn_btile_t *d_btiles;
 	jn_piece_t *d_pieces;
+	jn_tterm_t *d_tterms;
 	unsigned long long *d_gacc;     /* 64-bit fixed-point accumulator, zero between products */
 	unsigned int *d_xmax;           /* max|x| of the current product (FP32 bit pattern) */
 	struct jn_lanczos_state *lz;

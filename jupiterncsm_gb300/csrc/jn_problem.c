@@ -308,7 +308,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->mes);
 	free(p->rowptr); free(p->ent); free(p->me);
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
-	free(p->btiles); free(p->pieces);
+	free(p->btiles); free(p->pieces); free(p->tterms);
 	memset(p, 0, sizeof *p);
 }
 
@@ -362,7 +362,7 @@ static int cmp_task_cost(const void *a, const void *b)
 {
 	const task_cost_t *x = a, *y = b;
 	if (x->cost != y->cost) return x->cost < y->cost ? 1 : -1;
-	if (x->t.term != y->t.term) return x->t.term - y->t.term;
+	if (x->t.head != y->t.head) return x->t.head < y->t.head ? -1 : 1;
 	if (x->t.fixed != y->t.fixed) return (int)x->t.fixed - (int)y->t.fixed;
 	return x->t.start < y->t.start ? -1 : (x->t.start > y->t.start);
 }
@@ -408,16 +408,19 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	p->abs_bound = 0;
 	double *bound = NULL;
 	size_t bcap = 0;
-#define PUSH_TASK(TERM, START, FIXED, COUNT, KIND, COST)                                       \
+#define PUSH_TASK(TERM, START, FIXED, COUNT, KIND, W0, WLEN)                                  \
 	do {                                                                                   \
+		if ((WLEN) > 65535) { bad = 1; break; }                                        \
 		if (ntasks == tcap) { tcap = tcap ? 2 * tcap : 65536; tasks = realloc(tasks, tcap * sizeof *tasks); } \
 		task_cost_t *q_ = &tasks[ntasks++];                                            \
-		memset(q_, 0, sizeof *q_);                                                     \
-		q_->t.term = (TERM); q_->t.start = (uint32_t)(START); q_->t.fixed = (uint16_t)(FIXED); \
-		q_->t.count = (uint8_t)(COUNT); q_->t.kind = (uint8_t)(KIND);                  \
-		q_->cost = TASK_OVERHEAD + (COST);                                             \
+		q_->t.head = (uint32_t)(TERM) | ((uint32_t)(KIND) << 24) | ((uint32_t)((COUNT) - 1) << 26); \
+		q_->t.start = (uint32_t)(START); q_->t.w0 = (uint32_t)(W0);                    \
+		q_->t.wlen = (uint16_t)(WLEN); q_->t.fixed = (uint16_t)(FIXED);                \
+		q_->cost = TASK_OVERHEAD + (double)(WLEN);                                     \
 		total += q_->cost;                                                             \
 	} while (0)
+	int bad = 0;
+	if (p->nterms >= (1 << 24)) bad = 2;
 	for (int b = 0; b < p->nblocks; b++) {
 		const jn_block_t *B = &p->blocks[b];
 		if (B->Np == 0 || B->Nn == 0) continue;
@@ -464,14 +467,16 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 							int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
 							if (!pr) continue;
 							for (int64_t s = 0; s < Ln; s += 32)
-								PUSH_TASK(ti, T->n_e0 + s, r, Ln - s < 32 ? Ln - s : 32, JN_TASK_EN, (double)pr);
+								PUSH_TASK(ti, T->n_e0 + s, r, Ln - s < 32 ? Ln - s : 32, JN_TASK_EN,
+									  rp[T->p_ptr + r], pr);
 						}
 					} else {
 						for (int64_t c = 0; c < B->Nn; c++) {
 							int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
 							if (!nc) continue;
 							for (int64_t s = ep0; s < ep1; s += 32)
-								PUSH_TASK(ti, s, c, ep1 - s < 32 ? ep1 - s : 32, JN_TASK_EP, (double)nc);
+								PUSH_TASK(ti, s, c, ep1 - s < 32 ? ep1 - s : 32, JN_TASK_EP,
+									  rp[T->n_ptr + c], nc);
 						}
 					}
 				} else if (T->kind == JN_KIND_P) {
@@ -479,14 +484,16 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 						int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
 						if (!pr) continue;
 						for (int64_t c = 0; c < B->Nn; c += 32)
-							PUSH_TASK(ti, c, r, B->Nn - c < 32 ? B->Nn - c : 32, JN_TASK_PC, (double)pr);
+							PUSH_TASK(ti, c, r, B->Nn - c < 32 ? B->Nn - c : 32, JN_TASK_PC,
+								  rp[T->p_ptr + r], pr);
 					}
 				} else {
 					for (int64_t c = 0; c < B->Nn; c++) {
 						int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
 						if (!nc) continue;
 						for (int64_t r = r0; r < r1; r += 32)
-							PUSH_TASK(ti, r, c, r1 - r < 32 ? r1 - r : 32, JN_TASK_NR, (double)nc);
+							PUSH_TASK(ti, r, c, r1 - r < 32 ? r1 - r : 32, JN_TASK_NR,
+								  rp[T->n_ptr + c], nc);
 					}
 				}
 			}
@@ -497,6 +504,27 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		}
 	}
 #undef PUSH_TASK
+	if (bad) {
+		free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
+		if (err) snprintf(err, errlen, bad == 2 ? "too many terms for the packed task format"
+						       : "a destination row or column has more than 65535 list entries");
+		return 1;
+	}
+	/* compact term descriptions */
+	p->tterms = calloc(p->nterms ? p->nterms : 1, sizeof(jn_tterm_t));
+	for (int t = 0; t < p->nterms; t++) {
+		const jn_term_t *T = &p->terms[t];
+		if (T->src_off > 0x7fffffffll) {
+			free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
+			if (err) snprintf(err, errlen, "vector too long for 32-bit block offsets");
+			return 1;
+		}
+		p->tterms[t].me_off = T->me_off;
+		p->tterms[t].src_off = (int32_t)T->src_off;
+		p->tterms[t].nd = T->nd;
+		p->tterms[t].Nn_src = T->Nn_src;
+		p->tterms[t].transpose = T->transpose;
+	}
 	/* pass 2: tiles of similar work, tasks longest first inside a tile */
 	int ntile_target = target_units > 0 ? target_units / 6 : 152 * 8;
 	if (ntile_target < 1) ntile_target = 1;

@@ -119,14 +119,28 @@ enum {
 	JN_TASK_NR = 3          /* N: lanes over rows [start, ...), walk Nout(fixed column) */
 };
 
+/* 16-byte warp task */
 typedef struct {
-	int32_t term;
+	uint32_t head;          /* term (bits 0-23) | kind (24-25) | count-1 (26-30) */
 	uint32_t start;         /* first lane's entry (absolute entry index) / column / row */
+	uint32_t w0;            /* first entry of the walk (absolute entry index) */
+	uint16_t wlen;          /* entries walked */
 	uint16_t fixed;         /* destination row (EN, PC) or column (EP, NR) */
-	uint8_t count;          /* active lanes, 1..32 */
-	uint8_t kind;           /* JN_TASK_* */
-	uint32_t pad;
 } jn_piece_t;
+
+#define JN_TASK_TERM(h) ((h) & 0xffffffu)
+#define JN_TASK_KIND(h) (((h) >> 24) & 3u)
+#define JN_TASK_COUNT(h) ((((h) >> 26) & 31u) + 1u)
+
+/* compact term description read by the tile kernel (32 bytes) */
+typedef struct {
+	int64_t me_off;
+	int32_t src_off;
+	int32_t nd;
+	int32_t Nn_src;
+	int32_t transpose;
+	int32_t pad0, pad1;
+} jn_tterm_t;
 
 typedef struct {
 	/* problem */
@@ -151,6 +165,7 @@ typedef struct {
 	int64_t n_partial;
 	int nbtiles;       jn_btile_t *btiles;
 	int64_t npieces;   jn_piece_t *pieces;
+	jn_tterm_t *tterms;             /* nterms compact term descriptions */
 	int max_tile_elems;             /* shared-memory accumulator size needed */
 	double abs_bound;               /* max over y elements of sum |M| over its contributions */
 	/* accounting */

@@ -128,10 +128,16 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 	float scalef = (float)scale;
 	for (int64_t k = tl->pc0; k < tl->pc1; k++) {
 		const jn_piece_t *task = &P->pieces[k];
-		CHECK(task->term >= 0 && task->term < P->nterms && task->count >= 1 && task->count <= 32);
-		const jn_term_t *t = &P->terms[task->term];
+		const int term = (int)JN_TASK_TERM(task->head), kind = (int)JN_TASK_KIND(task->head);
+		const int count = (int)JN_TASK_COUNT(task->head);
+		CHECK(term < P->nterms && count >= 1 && count <= 32);
+		const jn_term_t *t = &P->terms[term];
+		const jn_tterm_t *tt = &P->tterms[term];
+		CHECK(tt->me_off == t->me_off && tt->src_off == t->src_off && tt->nd == t->nd && tt->Nn_src == t->Nn_src &&
+		      tt->transpose == t->transpose);
+		const uint32_t w0 = task->w0, w1 = task->w0 + task->wlen;
 		const int tr = t->transpose != 0, Ns = t->Nn_src, nd = t->nd;
-		for (int lane = 0; lane < task->count; lane++) {
+		for (int lane = 0; lane < count; lane++) {
 			double run = 0;
 			float runf = 0;
 			int drow = 0, dcol = 0;
@@ -142,7 +148,7 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				if (f32) { float m_ = me32[t->me_off + (MI)]; if (NEG) m_ = -m_; runf = fmaf(m_, x32[XI], runf); } \
 				else { double m_ = me64[t->me_off + (MI)]; if ((SKIP_TINY) && tiny64(m_)) break; if (NEG) m_ = -m_; run = fma(m_, x64[XI], run); } \
 			} while (0)
-			if (task->kind == JN_TASK_EN) {
+			if (kind == JN_TASK_EN) {
 				uint64_t en = task->start + lane;
 				CHECK(en >= t->n_e0 && en < t->n_e1);
 				uint32_t qx = ent[2 * en], qy = ent[2 * en + 1];
@@ -150,7 +156,8 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				int scol = tr ? nout : nin;
 				dcol = tr ? nin : nout;
 				drow = task->fixed;
-				for (uint32_t i = rp[t->p_ptr + drow]; i < rp[t->p_ptr + drow + 1]; i++) {
+				CHECK(w0 == rp[t->p_ptr + drow] && w1 == rp[t->p_ptr + drow + 1]);
+				for (uint32_t i = w0; i < w1; i++) {
 					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
 					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
 					int prow = tr ? (int)(px & 0xffff) : (int)(px >> 16);
@@ -158,7 +165,7 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
 					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
 				}
-			} else if (task->kind == JN_TASK_EP) {
+			} else if (kind == JN_TASK_EP) {
 				uint64_t ep = task->start + lane;
 				CHECK(ep < (uint64_t)P->n_ent);
 				uint32_t px = ent[2 * ep], py = ent[2 * ep + 1];
@@ -166,17 +173,19 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				int srow = tr ? pout : pin;
 				drow = tr ? pin : pout;
 				dcol = task->fixed;
-				for (uint32_t j = rp[t->n_ptr + dcol]; j < rp[t->n_ptr + dcol + 1]; j++) {
+				CHECK(w0 == rp[t->n_ptr + dcol] && w1 == rp[t->n_ptr + dcol + 1]);
+				for (uint32_t j = w0; j < w1; j++) {
 					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
 					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
 					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
 					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
 				}
-			} else if (task->kind == JN_TASK_PC) {
+			} else if (kind == JN_TASK_PC) {
 				int c = task->start + lane;
 				drow = task->fixed;
 				dcol = c;
-				for (uint32_t i = rp[t->p_ptr + drow]; i < rp[t->p_ptr + drow + 1]; i++) {
+				CHECK(w0 == rp[t->p_ptr + drow] && w1 == rp[t->p_ptr + drow + 1]);
+				for (uint32_t i = w0; i < w1; i++) {
 					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
 					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
 					VISIT(py & 0x7fffffffu, t->src_off + srow * Ns + c, (py & 0x80000000u) != 0, 1);
@@ -185,7 +194,8 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				int r = task->start + lane;
 				drow = r;
 				dcol = task->fixed;
-				for (uint32_t j = rp[t->n_ptr + dcol]; j < rp[t->n_ptr + dcol + 1]; j++) {
+				CHECK(w0 == rp[t->n_ptr + dcol] && w1 == rp[t->n_ptr + dcol + 1]);
+				for (uint32_t j = w0; j < w1; j++) {
 					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
 					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
 					VISIT(qy & 0x7fffffffu, t->src_off + r * Ns + scol, (qy & 0x80000000u) != 0, 1);
