@@ -44,6 +44,7 @@ struct jn_ctx {
 	jn_btile_t *d_btiles;
 	jn_piece_t *d_pieces;
 	jn_tterm_t *d_tterms;
+	uint2 *d_walks;
 	unsigned long long *d_gacc;     /* 64-bit fixed-point accumulator, zero between products */
 	unsigned int *d_xmax;           /* max|x| of the current product (FP32 bit pattern) */
 	struct jn_lanczos_state *lz;

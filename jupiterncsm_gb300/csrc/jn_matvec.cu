@@ -273,6 +273,7 @@ template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles,
 							       const jn_piece_t *__restrict__ tasks,
 							       const jn_tterm_t *__restrict__ tterms,
+							       const uint2 *__restrict__ walks,
 							       const T *__restrict__ x, const T *__restrict__ me,
 							       unsigned long long *__restrict__ gacc,
 							       const unsigned int *__restrict__ xmax_bits, double abs_bound)
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 	const int ntask = (int)(tl.pc1 - tl.pc0);
 	const uint4 *__restrict__ tq4 = (const uint4 *)(tasks + tl.pc0);
 	const uint4 *__restrict__ tt4 = (const uint4 *)tterms;
+	const uint2 *__restrict__ ent = P.ent;
 	for (;;) {
 		int k = 0;
 		if (lane == 0) k = atomicAdd(&next_task, 1);
@@ -299,85 +301,125 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 		if (k >= ntask) break;
 		const uint4 tq = __ldg(tq4 + k);
 		const uint32_t kind = JN_TASK_KIND(tq.x), count = JN_TASK_COUNT(tq.x), term = JN_TASK_TERM(tq.x);
-		const uint32_t w0 = tq.z, w1 = tq.z + (tq.w & 0xffffu);
-		const int fixed = (int)(tq.w >> 16);
+		if ((uint32_t)lane >= count) continue;
 		const uint4 ta = __ldg(tt4 + 2 * term), tb = __ldg(tt4 + 2 * term + 1);
 		const T *__restrict__ mb = me + ((int64_t)ta.x | ((int64_t)ta.y << 32));
 		const T *__restrict__ xs = x + (int)ta.z;
 		const int nd = (int)ta.w, Ns = (int)tb.x;
 		const bool tr = tb.y != 0;
-		const bool active = (uint32_t)lane < count;
-		T run = 0;
-		int drow = 0, dcol = 0;
-		if (active) {
-			if (kind == JN_TASK_EN) {
-				const uint2 qn = __ldg(P.ent + tq.y + lane);
-				const int nin = qn.x & 0xffff, nout = qn.x >> 16;
-				const int scol = tr ? nout : nin;
-				dcol = tr ? nin : nout;
-				drow = fixed;
-				const T *__restrict__ mcol = mb + (qn.y & MASK31);
-				const uint32_t sn = qn.y;
-				for (uint32_t i = w0; i < w1; i++) {
-					const uint2 qp = __ldg(P.ent + i);
-					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
-					const T m = __ldg(mcol + nd * (qp.y & MASK31));
-					run = fma(flip_sign(m, qp.y ^ sn), __ldg(xs + srow * Ns + scol), run);
-				}
-			} else if (kind == JN_TASK_EP) {
-				const uint2 qp = __ldg(P.ent + tq.y + lane);
-				const int pin = qp.x & 0xffff, pout = qp.x >> 16;
-				const int srow = tr ? pout : pin;
-				drow = tr ? pin : pout;
-				dcol = fixed;
-				const T *__restrict__ mrow = mb + nd * (qp.y & MASK31);
-				const T *__restrict__ xrow = xs + srow * Ns;
-				const uint32_t sp = qp.y;
-				for (uint32_t j = w0; j < w1; j++) {
-					const uint2 qn = __ldg(P.ent + j);
+		const uint32_t lb = tq.y + lane, l0 = tq.z, nl = tq.w;
+		const int rbase = -tl.row0 * stride;
+		if (kind == JN_TASK_NP_A) {
+			const uint2 nw = __ldg(walks + lb);
+			const uint32_t n0 = nw.x, n1 = nw.x + (nw.y & 0xffffu);
+			const int dcol = (int)(nw.y >> 16);
+			for (uint32_t q = 0; q < nl; q++) {
+				const uint2 pw = __ldg(walks + l0 + q);
+				const uint32_t p0 = pw.x, p1 = pw.x + (pw.y & 0xffffu);
+				const int drow = (int)(pw.y >> 16);
+				T run = 0;
+				for (uint32_t j = n0; j < n1; j++) {
+					const uint2 qn = __ldg(ent + j);
 					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
-					const T m = __ldg(mrow + (qn.y & MASK31));
-					run = fma(flip_sign(m, qn.y ^ sp), __ldg(xrow + scol), run);
+					const T *__restrict__ mcol = mb + (qn.y & MASK31);
+					for (uint32_t i = p0; i < p1; i++) {
+						const uint2 qp = __ldg(ent + i);
+						const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+						const T m = __ldg(mcol + nd * (qp.y & MASK31));
+						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xs + srow * Ns + scol), run);
+					}
 				}
-			} else if (kind == JN_TASK_PC) {
-				const int c = (int)tq.y + lane;
-				drow = fixed;
-				dcol = c;
-				for (uint32_t i = w0; i < w1; i++) {
-					const uint2 qp = __ldg(P.ent + i);
+				add_fixed(lo, hi, rbase + drow * stride + dcol, to_fixed<T>(run * scale));
+			}
+		} else if (kind == JN_TASK_NP_B) {
+			const uint2 pw = __ldg(walks + lb);
+			const uint32_t p0 = pw.x, p1 = pw.x + (pw.y & 0xffffu);
+			const int drow = (int)(pw.y >> 16);
+			for (uint32_t q = 0; q < nl; q++) {
+				const uint2 nw = __ldg(walks + l0 + q);
+				const uint32_t n0 = nw.x, n1 = nw.x + (nw.y & 0xffffu);
+				const int dcol = (int)(nw.y >> 16);
+				T run = 0;
+				for (uint32_t i = p0; i < p1; i++) {
+					const uint2 qp = __ldg(ent + i);
+					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+					const T *__restrict__ mrow = mb + nd * (qp.y & MASK31);
+					const T *__restrict__ xrow = xs + srow * Ns;
+					for (uint32_t j = n0; j < n1; j++) {
+						const uint2 qn = __ldg(ent + j);
+						const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+						const T m = __ldg(mrow + (qn.y & MASK31));
+						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xrow + scol), run);
+					}
+				}
+				add_fixed(lo, hi, rbase + drow * stride + dcol, to_fixed<T>(run * scale));
+			}
+		} else if (kind == JN_TASK_P_A) {
+			const int c = (int)lb;
+			for (uint32_t q = 0; q < nl; q++) {
+				const uint2 pw = __ldg(walks + l0 + q);
+				const uint32_t p0 = pw.x, p1 = pw.x + (pw.y & 0xffffu);
+				const int drow = (int)(pw.y >> 16);
+				T run = 0;
+				for (uint32_t i = p0; i < p1; i++) {
+					const uint2 qp = __ldg(ent + i);
 					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
 					const T m = __ldg(mb + (qp.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qp.y), __ldg(xs + srow * Ns + c), run);
 				}
-			} else {
-				const int r = (int)tq.y + lane;
-				drow = r;
-				dcol = fixed;
+				add_fixed(lo, hi, rbase + drow * stride + c, to_fixed<T>(run * scale));
+			}
+		} else if (kind == JN_TASK_P_B) {
+			const uint2 pw = __ldg(walks + lb);
+			const uint32_t p0 = pw.x, p1 = pw.x + (pw.y & 0xffffu);
+			const int drow = (int)(pw.y >> 16);
+			for (uint32_t q = 0; q < nl; q++) {
+				const int c = (int)(l0 + q);
+				T run = 0;
+				for (uint32_t i = p0; i < p1; i++) {
+					const uint2 qp = __ldg(ent + i);
+					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+					const T m = __ldg(mb + (qp.y & MASK31));
+					if (tiny(m)) continue;
+					run = fma(flip_sign(m, qp.y), __ldg(xs + srow * Ns + c), run);
+				}
+				add_fixed(lo, hi, rbase + drow * stride + c, to_fixed<T>(run * scale));
+			}
+		} else if (kind == JN_TASK_N_A) {
+			const uint2 nw = __ldg(walks + lb);
+			const uint32_t n0 = nw.x, n1 = nw.x + (nw.y & 0xffffu);
+			const int dcol = (int)(nw.y >> 16);
+			for (uint32_t q = 0; q < nl; q++) {
+				const int r = (int)(l0 + q);
 				const T *__restrict__ xrow = xs + r * Ns;
-				for (uint32_t j = w0; j < w1; j++) {
-					const uint2 qn = __ldg(P.ent + j);
+				T run = 0;
+				for (uint32_t j = n0; j < n1; j++) {
+					const uint2 qn = __ldg(ent + j);
 					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
 					const T m = __ldg(mb + (qn.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qn.y), __ldg(xrow + scol), run);
 				}
+				add_fixed(lo, hi, rbase + r * stride + dcol, to_fixed<T>(run * scale));
 			}
-		}
-		long long v = active ? to_fixed<T>(run * scale) : 0ll;
-		int key = active ? (drow - tl.row0) * stride + dcol : -1 - lane;
-		if (kind == JN_TASK_EN || kind == JN_TASK_EP) {
-			/* lanes of one output are adjacent (entries in destination order):
-			 * exact segmented integer scan, the last lane of a run adds it */
-			for (int off = 1; off < 32; off <<= 1) {
-				const long long ov = __shfl_up_sync(0xffffffffu, v, off);
-				const int ok = __shfl_up_sync(0xffffffffu, key, off);
-				if (lane >= off && ok == key) v += ov;
+		} else {
+			const int r = (int)lb;
+			const T *__restrict__ xrow = xs + r * Ns;
+			for (uint32_t q = 0; q < nl; q++) {
+				const uint2 nw = __ldg(walks + l0 + q);
+				const uint32_t n0 = nw.x, n1 = nw.x + (nw.y & 0xffffu);
+				const int dcol = (int)(nw.y >> 16);
+				T run = 0;
+				for (uint32_t j = n0; j < n1; j++) {
+					const uint2 qn = __ldg(ent + j);
+					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+					const T m = __ldg(mb + (qn.y & MASK31));
+					if (tiny(m)) continue;
+					run = fma(flip_sign(m, qn.y), __ldg(xrow + scol), run);
+				}
+				add_fixed(lo, hi, rbase + r * stride + dcol, to_fixed<T>(run * scale));
 			}
-			const int nk = __shfl_down_sync(0xffffffffu, key, 1);
-			if (active && (lane == 31 || nk != key)) add_fixed(lo, hi, key, v);
-		} else if (active) {
-			add_fixed(lo, hi, key, v);
 		}
 	}
 	__syncthreads();
@@ -425,7 +467,7 @@ extern "C" void jn_close(jn_ctx *c)
 	cudaFree(c->d_rowptr); cudaFree(c->d_ent); cudaFree(c->d_me); cudaFree(c->d_terms);
 	cudaFree(c->d_tiles); cudaFree(c->d_units); cudaFree(c->d_unit_terms); cudaFree(c->d_partial);
 	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
-	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms);
+	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms); cudaFree(c->d_walks);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
@@ -469,6 +511,7 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	    (s = upload(&c->d_btiles, p->btiles, p->nbtiles)) ||
 	    (s = upload(&c->d_pieces, p->pieces, p->npieces)) ||
 	    (s = upload(&c->d_tterms, p->tterms, p->nterms)) ||
+	    (s = upload(&c->d_walks, p->walks, p->nwalks)) ||
 	    (s = upload(&c->d_gacc, (const void *)NULL, p->dim)) ||
 	    (s = upload(&c->d_xmax, (const void *)NULL, 1))) {
 		jn_close(c);
@@ -564,11 +607,11 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? c->d_x32 : NULL, p->dim, c->d_xmax);
 		if (p->nbtiles) {
 			if (f32)
-				jn_tile_kernel<float><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, c->d_x32,
+				jn_tile_kernel<float><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, c->d_walks, c->d_x32,
 											   c->d_me32, c->d_gacc, c->d_xmax,
 											   p->abs_bound);
 			else
-				jn_tile_kernel<double><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, d_x,
+				jn_tile_kernel<double><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, c->d_walks, d_x,
 												c->d_me, c->d_gacc, c->d_xmax,
 												p->abs_bound);
 		}

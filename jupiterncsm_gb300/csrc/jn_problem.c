@@ -308,7 +308,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->mes);
 	free(p->rowptr); free(p->ent); free(p->me);
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
-	free(p->btiles); free(p->pieces); free(p->tterms);
+	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks);
 	memset(p, 0, sizeof *p);
 }
 
@@ -353,6 +353,8 @@ static int cmp_unit_cost(const void *a, const void *b)
 
 /* shared-memory accumulator budget of one CTA, in 64-bit elements */
 #define TILE_SMEM_ELEMS 8192
+/* work of one lane in one task, at most (multiply-adds plus per-output cost) */
+#define LANE_VISITS 96
 /* fixed per-task cost in the work model, in multiply-add units */
 #define TASK_OVERHEAD 6.0
 
@@ -363,8 +365,8 @@ static int cmp_task_cost(const void *a, const void *b)
 	const task_cost_t *x = a, *y = b;
 	if (x->cost != y->cost) return x->cost < y->cost ? 1 : -1;
 	if (x->t.head != y->t.head) return x->t.head < y->t.head ? -1 : 1;
-	if (x->t.fixed != y->t.fixed) return (int)x->t.fixed - (int)y->t.fixed;
-	return x->t.start < y->t.start ? -1 : (x->t.start > y->t.start);
+	if (x->t.lane_base != y->t.lane_base) return x->t.lane_base < y->t.lane_base ? -1 : 1;
+	return x->t.loop_base < y->t.loop_base ? -1 : (x->t.loop_base > y->t.loop_base);
 }
 
 /*
@@ -408,15 +410,14 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	p->abs_bound = 0;
 	double *bound = NULL;
 	size_t bcap = 0;
-#define PUSH_TASK(TERM, START, FIXED, COUNT, KIND, W0, WLEN)                                  \
+#define PUSH_TASK(TERM, KIND, COUNT, LANE_BASE, LOOP_BASE, LOOP_LEN, COST)                     \
 	do {                                                                                   \
-		if ((WLEN) > 65535) { bad = 1; break; }                                        \
 		if (ntasks == tcap) { tcap = tcap ? 2 * tcap : 65536; tasks = realloc(tasks, tcap * sizeof *tasks); } \
 		task_cost_t *q_ = &tasks[ntasks++];                                            \
-		q_->t.head = (uint32_t)(TERM) | ((uint32_t)(KIND) << 24) | ((uint32_t)((COUNT) - 1) << 26); \
-		q_->t.start = (uint32_t)(START); q_->t.w0 = (uint32_t)(W0);                    \
-		q_->t.wlen = (uint16_t)(WLEN); q_->t.fixed = (uint16_t)(FIXED);                \
-		q_->cost = TASK_OVERHEAD + (double)(WLEN);                                     \
+		q_->t.head = (uint32_t)(TERM) | ((uint32_t)(KIND) << 24) | ((uint32_t)((COUNT) - 1) << 27); \
+		q_->t.lane_base = (uint32_t)(LANE_BASE); q_->t.loop_base = (uint32_t)(LOOP_BASE); \
+		q_->t.loop_len = (uint32_t)(LOOP_LEN);                                         \
+		q_->cost = TASK_OVERHEAD + (COST);                                             \
 		total += q_->cost;                                                             \
 	} while (0)
 	int bad = 0;
@@ -457,45 +458,58 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 			for (int q = cnt[b]; q < cnt[b + 1]; q++) {
 				const int ti = byb[q];
 				const jn_term_t *T = &p->terms[ti];
-				const int64_t Ln = (int64_t)T->n_e1 - (int64_t)T->n_e0;
+				const uint32_t *W = p->walks;
+				/* P-walks with destination rows in [r0, r1) */
+				int64_t pa = T->pw0, pb = T->pw0;
+				if (T->kind != JN_KIND_N) {
+					while (pa < T->pw1 && (W[2 * pa + 1] >> 16) < (uint32_t)r0) pa++;
+					pb = pa;
+					while (pb < T->pw1 && (W[2 * pb + 1] >> 16) < (uint32_t)r1) pb++;
+				}
+				const int64_t nR = pb - pa, nC = T->nw1 - T->nw0;
+				int lanes_on_n;
+				int64_t lane0, nlane, loop0, nloop;
+				int kind;
 				if (T->kind == JN_KIND_NP) {
-					const int64_t ep0 = rp[T->p_ptr + r0], ep1 = rp[T->p_ptr + r1], Lp = ep1 - ep0;
-					if (Lp == 0 || Ln == 0) continue;
-					double eff_en = (double)Ln / (32.0 * ceil(Ln / 32.0)), eff_ep = (double)Lp / (32.0 * ceil(Lp / 32.0));
-					if (eff_en >= eff_ep) {
-						for (int64_t r = r0; r < r1; r++) {
-							int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
-							if (!pr) continue;
-							for (int64_t s = 0; s < Ln; s += 32)
-								PUSH_TASK(ti, T->n_e0 + s, r, Ln - s < 32 ? Ln - s : 32, JN_TASK_EN,
-									  rp[T->p_ptr + r], pr);
-						}
-					} else {
-						for (int64_t c = 0; c < B->Nn; c++) {
-							int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
-							if (!nc) continue;
-							for (int64_t s = ep0; s < ep1; s += 32)
-								PUSH_TASK(ti, s, c, ep1 - s < 32 ? ep1 - s : 32, JN_TASK_EP,
-									  rp[T->n_ptr + c], nc);
-						}
-					}
+					if (!nR || !nC) continue;
+					lanes_on_n = nC >= nR;
+					kind = lanes_on_n ? JN_TASK_NP_A : JN_TASK_NP_B;
+					lane0 = lanes_on_n ? T->nw0 : pa; nlane = lanes_on_n ? nC : nR;
+					loop0 = lanes_on_n ? pa : T->nw0; nloop = lanes_on_n ? nR : nC;
 				} else if (T->kind == JN_KIND_P) {
-					for (int64_t r = r0; r < r1; r++) {
-						int64_t pr = rp[T->p_ptr + r + 1] - rp[T->p_ptr + r];
-						if (!pr) continue;
-						for (int64_t c = 0; c < B->Nn; c += 32)
-							PUSH_TASK(ti, c, r, B->Nn - c < 32 ? B->Nn - c : 32, JN_TASK_PC,
-								  rp[T->p_ptr + r], pr);
-					}
+					if (!nR) continue;
+					lanes_on_n = B->Nn >= nR;          /* lanes over columns */
+					kind = lanes_on_n ? JN_TASK_P_A : JN_TASK_P_B;
+					lane0 = lanes_on_n ? 0 : pa; nlane = lanes_on_n ? B->Nn : nR;
+					loop0 = lanes_on_n ? pa : 0; nloop = lanes_on_n ? nR : B->Nn;
 				} else {
-					for (int64_t c = 0; c < B->Nn; c++) {
-						int64_t nc = rp[T->n_ptr + c + 1] - rp[T->n_ptr + c];
-						if (!nc) continue;
-						for (int64_t r = r0; r < r1; r += 32)
-							PUSH_TASK(ti, r, c, r1 - r < 32 ? r1 - r : 32, JN_TASK_NR,
-								  rp[T->n_ptr + c], nc);
+					if (!nC) continue;
+					lanes_on_n = nC >= r1 - r0;         /* lanes over N-walks */
+					kind = lanes_on_n ? JN_TASK_N_A : JN_TASK_N_B;
+					lane0 = lanes_on_n ? T->nw0 : r0; nlane = lanes_on_n ? nC : r1 - r0;
+					loop0 = lanes_on_n ? r0 : T->nw0; nloop = lanes_on_n ? r1 - r0 : nC;
+				}
+				/* walk lengths (1 for a dense column or row) of the two sides */
+#define LANE_LEN(i) ((kind == JN_TASK_P_A || kind == JN_TASK_N_B) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
+#define LOOP_LEN(i) ((kind == JN_TASK_P_B || kind == JN_TASK_N_A) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
+				for (int64_t l0 = 0; l0 < nlane; l0 += 32) {
+					const int64_t cntl = nlane - l0 < 32 ? nlane - l0 : 32;
+					double lane_max = 0;
+					for (int64_t i = 0; i < cntl; i++) lane_max = fmax(lane_max, LANE_LEN(lane0 + l0 + i));
+					/* split the loop so that one task stays short */
+					int64_t s0 = 0;
+					double acc = 0;
+					for (int64_t sI = 0; sI < nloop; sI++) {
+						acc += LOOP_LEN(loop0 + sI) * lane_max + 4.0;
+						if (acc >= LANE_VISITS || sI == nloop - 1) {
+							PUSH_TASK(ti, kind, cntl, lane0 + l0, loop0 + s0, sI + 1 - s0, acc);
+							s0 = sI + 1;
+							acc = 0;
+						}
 					}
 				}
+#undef LANE_LEN
+#undef LOOP_LEN
 			}
 			rg->t1 = ntasks;
 			rg->cost = total - before;
@@ -506,8 +520,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 #undef PUSH_TASK
 	if (bad) {
 		free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
-		if (err) snprintf(err, errlen, bad == 2 ? "too many terms for the packed task format"
-						       : "a destination row or column has more than 65535 list entries");
+		if (err) snprintf(err, errlen, "too many terms for the packed task format");
 		return 1;
 	}
 	/* compact term descriptions */
@@ -793,6 +806,34 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 		for (int32_t r = 0; r <= L->nout; r++) p->rowptr[L->csr_out_ptr + r] += (uint32_t)L->ent_out;
 		for (int32_t r = 0; r <= L->nin; r++) p->rowptr[L->csr_in_ptr + r] += (uint32_t)L->ent_in;
 	}
+	/* walks: the non-empty destination rows of both views of every list */
+	{
+		int64_t nw = 0;
+		for (int l = 0; l < p->nlists; l++) {
+			jn_list_t *L = &p->lists[l];
+			for (int32_t r = 0; r < L->nout; r++) nw += p->rowptr[L->csr_out_ptr + r + 1] > p->rowptr[L->csr_out_ptr + r];
+			for (int32_t r = 0; r < L->nin; r++) nw += p->rowptr[L->csr_in_ptr + r + 1] > p->rowptr[L->csr_in_ptr + r];
+		}
+		p->walks = malloc((nw ? nw : 1) * 2 * sizeof(uint32_t));
+		if (!p->walks) ERR("out of host memory for walks");
+		for (int l = 0; l < p->nlists; l++) {
+			jn_list_t *L = &p->lists[l];
+			for (int view = 0; view < 2; view++) {
+				const int64_t ptr = view ? L->csr_in_ptr : L->csr_out_ptr;
+				const int32_t n = view ? L->nin : L->nout;
+				if (view) L->walk_in = p->nwalks; else L->walk_out = p->nwalks;
+				for (int32_t r = 0; r < n; r++) {
+					uint32_t a = p->rowptr[ptr + r], b = p->rowptr[ptr + r + 1];
+					if (b == a) continue;
+					if (b - a > 65535) ERR("index list %d: %u entries map onto one state, more than 65535", L->id, b - a);
+					p->walks[2 * p->nwalks] = a;
+					p->walks[2 * p->nwalks + 1] = (b - a) | ((uint32_t)r << 16);
+					p->nwalks++;
+				}
+				if (view) L->nwalk_in = p->nwalks - L->walk_in; else L->nwalk_out = p->nwalks - L->walk_out;
+			}
+		}
+	}
 
 	/* terms: forward on the output block, transpose on the input block */
 	p->terms = malloc(2 * (size_t)p->ninstr * sizeof(jn_term_t));
@@ -823,6 +864,14 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 			if (x->ln >= 0) {
 				t.n_e0 = p->rowptr[t.n_ptr];
 				t.n_e1 = p->rowptr[t.n_ptr + t.Nn_dst];
+				const jn_list_t *L = &p->lists[x->ln];
+				t.nw0 = dir ? L->walk_in : L->walk_out;
+				t.nw1 = t.nw0 + (dir ? L->nwalk_in : L->nwalk_out);
+			}
+			if (x->lp >= 0) {
+				const jn_list_t *L = &p->lists[x->lp];
+				t.pw0 = dir ? L->walk_in : L->walk_out;
+				t.pw1 = t.pw0 + (dir ? L->nwalk_in : L->nwalk_out);
 			}
 			t.instr = i;
 			t.transpose = dir;

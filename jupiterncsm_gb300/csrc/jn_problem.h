@@ -55,6 +55,8 @@ typedef struct {
 	int64_t csr_in_ptr;     /* (nin+1 entries) */
 	int64_t ent_out;        /* offsets into jn_plan_t.ent (len entries) */
 	int64_t ent_in;
+	int64_t walk_out, nwalk_out;    /* walks of the by-out view (first index, count) */
+	int64_t walk_in, nwalk_in;      /* walks of the by-in view */
 } jn_list_t;
 
 typedef struct {
@@ -78,6 +80,8 @@ typedef struct {
 	int32_t instr;          /* evaluation-order index */
 	int32_t transpose;
 	uint32_t n_e0, n_e1;    /* absolute range of the neutron entries (N, NP) */
+	int64_t pw0, pw1;       /* walks of the proton list in this direction */
+	int64_t nw0, nw1;       /* walks of the neutron list in this direction */
 } jn_term_t;
 
 typedef struct {
@@ -112,25 +116,32 @@ typedef struct {
 	int64_t pc0, pc1;       /* range into jn_plan_t.pieces */
 } jn_btile_t;
 
+/*
+ * A walk is one non-empty row of a list's destination-ordered view: the
+ * entries [w0, w0+len) that all map onto destination index `idx`, stored as
+ * uint2 {w0, len | idx << 16}.  The product of a term restricted to output
+ * (row, col) is the double walk P-walk(row) x N-walk(col).
+ */
 enum {
-	JN_TASK_EN = 0,         /* NP: lanes over neutron entries [start, start+count), walk Pout(fixed row) */
-	JN_TASK_EP = 1,         /* NP: lanes over proton entries [start, ...), walk Nout(fixed column) */
-	JN_TASK_PC = 2,         /* P: lanes over columns [start, ...), walk Pout(fixed row) */
-	JN_TASK_NR = 3          /* N: lanes over rows [start, ...), walk Nout(fixed column) */
+	JN_TASK_NP_A = 0,       /* lanes over N-walks (columns), loop over P-walks (rows) */
+	JN_TASK_NP_B = 1,       /* lanes over P-walks (rows), loop over N-walks (columns) */
+	JN_TASK_P_A = 2,        /* P: lanes over columns, loop over P-walks */
+	JN_TASK_P_B = 3,        /* P: lanes over P-walks, loop over columns */
+	JN_TASK_N_A = 4,        /* N: lanes over N-walks, loop over rows */
+	JN_TASK_N_B = 5         /* N: lanes over rows, loop over N-walks */
 };
 
 /* 16-byte warp task */
 typedef struct {
-	uint32_t head;          /* term (bits 0-23) | kind (24-25) | count-1 (26-30) */
-	uint32_t start;         /* first lane's entry (absolute entry index) / column / row */
-	uint32_t w0;            /* first entry of the walk (absolute entry index) */
-	uint16_t wlen;          /* entries walked */
-	uint16_t fixed;         /* destination row (EN, PC) or column (EP, NR) */
+	uint32_t head;          /* term (bits 0-23) | kind (24-26) | count-1 (27-31) */
+	uint32_t lane_base;     /* first lane's walk index / column / row */
+	uint32_t loop_base;     /* first looped walk index / column / row */
+	uint32_t loop_len;      /* looped walks / columns / rows */
 } jn_piece_t;
 
 #define JN_TASK_TERM(h) ((h) & 0xffffffu)
-#define JN_TASK_KIND(h) (((h) >> 24) & 3u)
-#define JN_TASK_COUNT(h) ((((h) >> 26) & 31u) + 1u)
+#define JN_TASK_KIND(h) (((h) >> 24) & 7u)
+#define JN_TASK_COUNT(h) ((((h) >> 27) & 31u) + 1u)
 
 /* compact term description read by the tile kernel (32 bytes) */
 typedef struct {
@@ -166,6 +177,7 @@ typedef struct {
 	int nbtiles;       jn_btile_t *btiles;
 	int64_t npieces;   jn_piece_t *pieces;
 	jn_tterm_t *tterms;             /* nterms compact term descriptions */
+	int64_t nwalks;    uint32_t *walks;    /* pairs {w0, len | idx << 16} */
 	int max_tile_elems;             /* shared-memory accumulator size needed */
 	double abs_bound;               /* max over y elements of sum |M| over its contributions */
 	/* accounting */

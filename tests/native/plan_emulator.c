@@ -123,87 +123,87 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 	CHECK(stride >= Nn && (stride & 1));
 	CHECK(tl->nrows * stride <= P->max_tile_elems);
 	int64_t *sacc = calloc(E ? E : 1, sizeof(int64_t));
-	const uint32_t *ent = P->ent, *rp = P->rowptr;
+	const uint32_t *ent = P->ent, *W = P->walks;
 	double scale = ldexp(1.0, S);
 	float scalef = (float)scale;
 	for (int64_t k = tl->pc0; k < tl->pc1; k++) {
 		const jn_piece_t *task = &P->pieces[k];
 		const int term = (int)JN_TASK_TERM(task->head), kind = (int)JN_TASK_KIND(task->head);
 		const int count = (int)JN_TASK_COUNT(task->head);
-		CHECK(term < P->nterms && count >= 1 && count <= 32);
+		CHECK(term < P->nterms && count >= 1 && count <= 32 && kind <= JN_TASK_N_B);
 		const jn_term_t *t = &P->terms[term];
 		const jn_tterm_t *tt = &P->tterms[term];
 		CHECK(tt->me_off == t->me_off && tt->src_off == t->src_off && tt->nd == t->nd && tt->Nn_src == t->Nn_src &&
 		      tt->transpose == t->transpose);
-		const uint32_t w0 = task->w0, w1 = task->w0 + task->wlen;
 		const int tr = t->transpose != 0, Ns = t->Nn_src, nd = t->nd;
 		for (int lane = 0; lane < count; lane++) {
-			double run = 0;
-			float runf = 0;
-			int drow = 0, dcol = 0;
+			const uint32_t lb = task->lane_base + lane;
+			for (uint32_t q = 0; q < task->loop_len; q++) {
+				const uint32_t lq = task->loop_base + q;
+				double run = 0;
+				float runf = 0;
+				int drow, dcol;
+				uint32_t p0 = 0, p1 = 0, n0 = 0, n1 = 0;
+				int ccol = -1, rrow = -1;
+#define WALK(i, a, b, idx) do { CHECK((int64_t)(i) < P->nwalks); a = W[2 * (i)]; b = a + (W[2 * (i) + 1] & 0xffff); idx = (int)(W[2 * (i) + 1] >> 16); } while (0)
+				if (kind == JN_TASK_NP_A) { CHECK(lb >= t->nw0 && lb < t->nw1 && lq >= t->pw0 && lq < t->pw1); WALK(lb, n0, n1, dcol); WALK(lq, p0, p1, drow); }
+				else if (kind == JN_TASK_NP_B) { CHECK(lb >= t->pw0 && lb < t->pw1 && lq >= t->nw0 && lq < t->nw1); WALK(lb, p0, p1, drow); WALK(lq, n0, n1, dcol); }
+				else if (kind == JN_TASK_P_A) { CHECK(lq >= t->pw0 && lq < t->pw1); WALK(lq, p0, p1, drow); ccol = (int)lb; dcol = ccol; }
+				else if (kind == JN_TASK_P_B) { CHECK(lb >= t->pw0 && lb < t->pw1); WALK(lb, p0, p1, drow); ccol = (int)lq; dcol = ccol; }
+				else if (kind == JN_TASK_N_A) { CHECK(lb >= t->nw0 && lb < t->nw1); WALK(lb, n0, n1, dcol); rrow = (int)lq; drow = rrow; }
+				else { CHECK(lq >= t->nw0 && lq < t->nw1); WALK(lq, n0, n1, dcol); rrow = (int)lb; drow = rrow; }
+#undef WALK
+				CHECK(drow >= tl->row0 && drow < tl->row0 + tl->nrows && dcol >= 0 && dcol < Nn);
 #define VISIT(MI, XI, NEG, SKIP_TINY)                                                       \
-			do {                                                                        \
-				CHECK(t->me_off + (int64_t)(MI) < P->n_me);                          \
-				CHECK((int64_t)(XI) >= 0 && (int64_t)(XI) < P->dim);                 \
-				if (f32) { float m_ = me32[t->me_off + (MI)]; if (NEG) m_ = -m_; runf = fmaf(m_, x32[XI], runf); } \
-				else { double m_ = me64[t->me_off + (MI)]; if ((SKIP_TINY) && tiny64(m_)) break; if (NEG) m_ = -m_; run = fma(m_, x64[XI], run); } \
-			} while (0)
-			if (kind == JN_TASK_EN) {
-				uint64_t en = task->start + lane;
-				CHECK(en >= t->n_e0 && en < t->n_e1);
-				uint32_t qx = ent[2 * en], qy = ent[2 * en + 1];
-				int nin = qx & 0xffff, nout = qx >> 16;
-				int scol = tr ? nout : nin;
-				dcol = tr ? nin : nout;
-				drow = task->fixed;
-				CHECK(w0 == rp[t->p_ptr + drow] && w1 == rp[t->p_ptr + drow + 1]);
-				for (uint32_t i = w0; i < w1; i++) {
-					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
-					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
-					int prow = tr ? (int)(px & 0xffff) : (int)(px >> 16);
-					CHECK(prow == drow);
-					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
-					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
+				do {                                                                \
+					CHECK(t->me_off + (int64_t)(MI) < P->n_me);                  \
+					CHECK((int64_t)(XI) >= 0 && (int64_t)(XI) < P->dim);         \
+					if (f32) { float m_ = me32[t->me_off + (MI)]; if (NEG) m_ = -m_; runf = fmaf(m_, x32[XI], runf); } \
+					else { double m_ = me64[t->me_off + (MI)]; if ((SKIP_TINY) && tiny64(m_)) break; if (NEG) m_ = -m_; run = fma(m_, x64[XI], run); } \
+				} while (0)
+				if (kind == JN_TASK_NP_A) {
+					for (uint32_t j = n0; j < n1; j++) {
+						uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
+						int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+						int ndst = tr ? (int)(qx & 0xffff) : (int)(qx >> 16);
+						CHECK(ndst == dcol);
+						for (uint32_t i = p0; i < p1; i++) {
+							uint32_t px = ent[2 * i], py = ent[2 * i + 1];
+							int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+							int pdst = tr ? (int)(px & 0xffff) : (int)(px >> 16);
+							CHECK(pdst == drow);
+							size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
+							VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
+						}
+					}
+				} else if (kind == JN_TASK_NP_B) {
+					for (uint32_t i = p0; i < p1; i++) {
+						uint32_t px = ent[2 * i], py = ent[2 * i + 1];
+						int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+						for (uint32_t j = n0; j < n1; j++) {
+							uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
+							int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+							size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
+							VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
+						}
+					}
+				} else if (kind == JN_TASK_P_A || kind == JN_TASK_P_B) {
+					CHECK(ccol >= 0 && ccol < Nn);
+					for (uint32_t i = p0; i < p1; i++) {
+						uint32_t px = ent[2 * i], py = ent[2 * i + 1];
+						int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+						VISIT(py & 0x7fffffffu, t->src_off + srow * Ns + ccol, (py & 0x80000000u) != 0, 1);
+					}
+				} else {
+					for (uint32_t j = n0; j < n1; j++) {
+						uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
+						int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+						VISIT(qy & 0x7fffffffu, t->src_off + rrow * Ns + scol, (qy & 0x80000000u) != 0, 1);
+					}
 				}
-			} else if (kind == JN_TASK_EP) {
-				uint64_t ep = task->start + lane;
-				CHECK(ep < (uint64_t)P->n_ent);
-				uint32_t px = ent[2 * ep], py = ent[2 * ep + 1];
-				int pin = px & 0xffff, pout = px >> 16;
-				int srow = tr ? pout : pin;
-				drow = tr ? pin : pout;
-				dcol = task->fixed;
-				CHECK(w0 == rp[t->n_ptr + dcol] && w1 == rp[t->n_ptr + dcol + 1]);
-				for (uint32_t j = w0; j < w1; j++) {
-					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
-					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
-					size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
-					VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
-				}
-			} else if (kind == JN_TASK_PC) {
-				int c = task->start + lane;
-				drow = task->fixed;
-				dcol = c;
-				CHECK(w0 == rp[t->p_ptr + drow] && w1 == rp[t->p_ptr + drow + 1]);
-				for (uint32_t i = w0; i < w1; i++) {
-					uint32_t px = ent[2 * i], py = ent[2 * i + 1];
-					int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
-					VISIT(py & 0x7fffffffu, t->src_off + srow * Ns + c, (py & 0x80000000u) != 0, 1);
-				}
-			} else {
-				int r = task->start + lane;
-				drow = r;
-				dcol = task->fixed;
-				CHECK(w0 == rp[t->n_ptr + dcol] && w1 == rp[t->n_ptr + dcol + 1]);
-				for (uint32_t j = w0; j < w1; j++) {
-					uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
-					int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
-					VISIT(qy & 0x7fffffffu, t->src_off + r * Ns + scol, (qy & 0x80000000u) != 0, 1);
-				}
-			}
 #undef VISIT
-			CHECK(drow >= tl->row0 && drow < tl->row0 + tl->nrows && dcol >= 0 && dcol < Nn);
-			sacc[(drow - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
+				sacc[(drow - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
+			}
 		}
 	}
 	for (int i = 0; i < E; i++) gacc[tl->dst_off + (int64_t)tl->row0 * Nn + i] += sacc[i];
@@ -238,4 +238,21 @@ int emu_matvec3(void *h, const double *x, double *y, int accumulate, int f32)
 	for (int64_t i = 0; i < P->dim; i++) y[i] = accumulate ? y[i] + (double)gacc[i] * unit : (double)gacc[i] * unit;
 	free(gacc); free(x32); free(me32);
 	return emu_fail;
+}
+
+/* task statistics of the block-tile plan: tasks, tiles, lane slots, walk steps */
+void emu_task_stats(void *h, double *out)
+{
+	const jn_plan_t *P = h;
+	double lanes = 0, steps = 0, visits = 0, kinds[4] = { 0, 0, 0, 0 };
+	for (int64_t k = 0; k < P->npieces; k++) {
+		const jn_piece_t *t = &P->pieces[k];
+		double c = JN_TASK_COUNT(t->head);
+		lanes += c;
+		steps += t->loop_len;
+		visits += c * t->loop_len;
+		kinds[JN_TASK_KIND(t->head) >> 1] += 1;
+	}
+	out[0] = (double)P->npieces; out[1] = P->nbtiles; out[2] = lanes; out[3] = steps; out[4] = visits;
+	out[5] = kinds[0]; out[6] = kinds[1]; out[7] = kinds[2]; out[8] = kinds[3];
 }
