@@ -45,8 +45,10 @@ struct jn_ctx {
 	jn_piece_t *d_pieces;
 	jn_tterm_t *d_tterms;
 	uint2 *d_walks;
+	unsigned int *d_items;
+	int tile_grid;          /* persistent CTAs of the tile kernel */
 	unsigned long long *d_gacc;     /* 64-bit fixed-point accumulator, zero between products */
-	unsigned int *d_xmax;           /* max|x| of the current product (FP32 bit pattern) */
+	unsigned int *d_xmax;           /* [0] max|x| of the current product (FP32 bits), [1] tile counter */
 	struct jn_lanczos_state *lz;
 };
 

@@ -102,7 +102,7 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 			const uint2 e = __ldg(P.ent + j);
 			T m = __ldg(me + (e.y & MASK31));
 			if (tiny(m)) continue;
-			const uint32_t src = t.transpose ? (e.x >> 16) : (e.x & 0xffffu);
+			const uint32_t src = e.x & 0xffffu;
 			acc = fma(flip_sign(m, e.y), __ldg(xs + (size_t)src * t.Nn_src + n), acc);
 		}
 	} else if (t.kind == JN_KIND_N) {
@@ -112,7 +112,7 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 			const uint2 e = __ldg(P.ent + j);
 			T m = __ldg(me + (e.y & MASK31));
 			if (tiny(m)) continue;
-			const uint32_t src = t.transpose ? (e.x >> 16) : (e.x & 0xffffu);
+			const uint32_t src = e.x & 0xffffu;
 			acc = fma(flip_sign(m, e.y), __ldg(xrow + src), acc);
 		}
 	} else {
@@ -122,12 +122,12 @@ __device__ __forceinline__ T term_element(const DevPlan &P, const jn_term_t &t, 
 		for (uint32_t i = i0; i < i1; i++) {
 			const uint2 ep = __ldg(P.ent + i);
 			const T *__restrict__ mrow = me + (size_t)t.nd * (ep.y & MASK31);
-			const uint32_t psrc = t.transpose ? (ep.x >> 16) : (ep.x & 0xffffu);
+			const uint32_t psrc = ep.x & 0xffffu;
 			const T *__restrict__ xrow = xs + (size_t)psrc * t.Nn_src;
 			for (uint32_t j = j0; j < j1; j++) {
 				const uint2 en = __ldg(P.ent + j);
 				const T m = __ldg(mrow + (en.y & MASK31));
-				const uint32_t nsrc = t.transpose ? (en.x >> 16) : (en.x & 0xffffu);
+				const uint32_t nsrc = en.x & 0xffffu;
 				acc = fma(flip_sign(m, ep.y ^ en.y), __ldg(xrow + nsrc), acc);
 			}
 		}
@@ -270,7 +270,9 @@ __device__ __forceinline__ void add_fixed(unsigned int *lo, unsigned int *hi, in
 }
 
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles,
+__global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles, int ntiles,
+							       unsigned int *__restrict__ tile_counter,
+							       const uint2 *__restrict__ items,
 							       const jn_piece_t *__restrict__ tasks,
 							       const jn_tterm_t *__restrict__ tterms,
 							       const uint2 *__restrict__ walks,
@@ -279,36 +281,47 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 							       const unsigned int *__restrict__ xmax_bits, double abs_bound)
 {
 	extern __shared__ unsigned int sacc[];
-	__shared__ int next_task;
-	const jn_btile_t tl = tiles[blockIdx.x];
-	const int Nn = tl.Nn, stride = tl.stride;
-	const int Ep = tl.nrows * stride;
-	unsigned int *lo = sacc, *hi = sacc + Ep;
-	for (int i = threadIdx.x; i < 2 * Ep; i += blockDim.x) sacc[i] = 0u;
-	if (threadIdx.x == 0) next_task = 0;
+	__shared__ int next_item, cur_tile;
 	const int S = fixed_exponent(*xmax_bits, abs_bound);
 	const T scale = (T)ldexp(1.0, S);
-	__syncthreads();
 	const int lane = threadIdx.x & 31;
-	const int ntask = (int)(tl.pc1 - tl.pc0);
-	const uint4 *__restrict__ tq4 = (const uint4 *)(tasks + tl.pc0);
+	const uint4 *__restrict__ tq4 = (const uint4 *)tasks;
 	const uint4 *__restrict__ tt4 = (const uint4 *)tterms;
 	const uint2 *__restrict__ ent = P.ent;
 	for (;;) {
-		int k = 0;
-		if (lane == 0) k = atomicAdd(&next_task, 1);
-		k = __shfl_sync(0xffffffffu, k, 0);
-		if (k >= ntask) break;
-		const uint4 tq = __ldg(tq4 + k);
-		const uint32_t kind = JN_TASK_KIND(tq.x), count = JN_TASK_COUNT(tq.x), term = JN_TASK_TERM(tq.x);
-		if ((uint32_t)lane >= count) continue;
-		const uint4 ta = __ldg(tt4 + 2 * term), tb = __ldg(tt4 + 2 * term + 1);
-		const T *__restrict__ mb = me + ((int64_t)ta.x | ((int64_t)ta.y << 32));
-		const T *__restrict__ xs = x + (int)ta.z;
-		const int nd = (int)ta.w, Ns = (int)tb.x;
-		const bool tr = tb.y != 0;
-		const uint32_t lb = tq.y + lane, l0 = tq.z, nl = tq.w;
+		/* persistent CTAs take tiles heaviest first */
+		if (threadIdx.x == 0) {
+			cur_tile = (int)atomicAdd(tile_counter, 1u);
+			next_item = 0;
+		}
+		__syncthreads();
+		const int ti = cur_tile;
+		if (ti >= ntiles) break;
+		const jn_btile_t tl = tiles[ti];
+		const int Nn = tl.Nn, stride = tl.stride;
+		const int Ep = tl.nrows * stride;
+		unsigned int *lo = sacc, *hi = sacc + Ep;
+		for (int i = threadIdx.x; i < 2 * Ep; i += blockDim.x) sacc[i] = 0u;
+		__syncthreads();
+		const int nitem = (int)(tl.pc1 - tl.pc0);
 		const int rbase = -tl.row0 * stride;
+		for (;;) {
+			int k = 0;
+			if (lane == 0) k = atomicAdd(&next_item, 1);
+			k = __shfl_sync(0xffffffffu, k, 0);
+			if (k >= nitem) break;
+			const uint2 it = __ldg(items + tl.pc0 + k);
+			const uint32_t w = it.y & 0xffu, nsub = it.y >> 8;
+			const uint32_t sub = (uint32_t)lane / w, sl = (uint32_t)lane & (w - 1u);
+			if (sub >= nsub) continue;
+			const uint4 tq = __ldg(tq4 + it.x + sub);
+			const uint32_t kind = JN_TASK_KIND(tq.x), count = JN_TASK_COUNT(tq.x), term = JN_TASK_TERM(tq.x);
+			if (sl >= count) continue;
+			const uint4 ta = __ldg(tt4 + 2 * term), tb = __ldg(tt4 + 2 * term + 1);
+			const T *__restrict__ mb = me + ((int64_t)ta.x | ((int64_t)ta.y << 32));
+			const T *__restrict__ xs = x + (int)ta.z;
+			const int nd = (int)ta.w, Ns = (int)tb.x;
+			const uint32_t lb = tq.y + sl, l0 = tq.z, nl = tq.w;
 		if (kind == JN_TASK_NP_A) {
 			const uint2 nw = __ldg(walks + lb);
 			const uint32_t n0 = nw.x, n1 = nw.x + (nw.y & 0xffffu);
@@ -320,11 +333,11 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t j = n0; j < n1; j++) {
 					const uint2 qn = __ldg(ent + j);
-					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+					const int scol = (int)(qn.x & 0xffffu);
 					const T *__restrict__ mcol = mb + (qn.y & MASK31);
 					for (uint32_t i = p0; i < p1; i++) {
 						const uint2 qp = __ldg(ent + i);
-						const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+						const int srow = (int)(qp.x & 0xffffu);
 						const T m = __ldg(mcol + nd * (qp.y & MASK31));
 						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xs + srow * Ns + scol), run);
 					}
@@ -342,12 +355,12 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t i = p0; i < p1; i++) {
 					const uint2 qp = __ldg(ent + i);
-					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+					const int srow = (int)(qp.x & 0xffffu);
 					const T *__restrict__ mrow = mb + nd * (qp.y & MASK31);
 					const T *__restrict__ xrow = xs + srow * Ns;
 					for (uint32_t j = n0; j < n1; j++) {
 						const uint2 qn = __ldg(ent + j);
-						const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+						const int scol = (int)(qn.x & 0xffffu);
 						const T m = __ldg(mrow + (qn.y & MASK31));
 						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xrow + scol), run);
 					}
@@ -363,7 +376,7 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t i = p0; i < p1; i++) {
 					const uint2 qp = __ldg(ent + i);
-					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+					const int srow = (int)(qp.x & 0xffffu);
 					const T m = __ldg(mb + (qp.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qp.y), __ldg(xs + srow * Ns + c), run);
@@ -379,7 +392,7 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t i = p0; i < p1; i++) {
 					const uint2 qp = __ldg(ent + i);
-					const int srow = tr ? (int)(qp.x >> 16) : (int)(qp.x & 0xffff);
+					const int srow = (int)(qp.x & 0xffffu);
 					const T m = __ldg(mb + (qp.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qp.y), __ldg(xs + srow * Ns + c), run);
@@ -396,7 +409,7 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t j = n0; j < n1; j++) {
 					const uint2 qn = __ldg(ent + j);
-					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+					const int scol = (int)(qn.x & 0xffffu);
 					const T m = __ldg(mb + (qn.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qn.y), __ldg(xrow + scol), run);
@@ -413,7 +426,7 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				T run = 0;
 				for (uint32_t j = n0; j < n1; j++) {
 					const uint2 qn = __ldg(ent + j);
-					const int scol = tr ? (int)(qn.x >> 16) : (int)(qn.x & 0xffff);
+					const int scol = (int)(qn.x & 0xffffu);
 					const T m = __ldg(mb + (qn.y & MASK31));
 					if (tiny(m)) continue;
 					run = fma(flip_sign(m, qn.y), __ldg(xrow + scol), run);
@@ -421,14 +434,16 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 				add_fixed(lo, hi, rbase + r * stride + dcol, to_fixed<T>(run * scale));
 			}
 		}
-	}
-	__syncthreads();
-	unsigned long long *g = gacc + tl.dst_off + (int64_t)tl.row0 * Nn;
-	const int E = tl.nrows * Nn;
-	for (int i = threadIdx.x; i < E; i += blockDim.x) {
-		const int si = (i / Nn) * stride + i % Nn;
-		const unsigned long long v = (unsigned long long)lo[si] | ((unsigned long long)hi[si] << 32);
-		if (v) atomicAdd(g + i, v);
+		}
+		__syncthreads();
+		unsigned long long *g = gacc + tl.dst_off + (int64_t)tl.row0 * Nn;
+		const int E = tl.nrows * Nn;
+		for (int i = threadIdx.x; i < E; i += blockDim.x) {
+			const int si = (i / Nn) * stride + i % Nn;
+			const unsigned long long v = (unsigned long long)lo[si] | ((unsigned long long)hi[si] << 32);
+			if (v) atomicAdd(g + i, v);
+		}
+		__syncthreads();
 	}
 }
 
@@ -467,7 +482,7 @@ extern "C" void jn_close(jn_ctx *c)
 	cudaFree(c->d_rowptr); cudaFree(c->d_ent); cudaFree(c->d_me); cudaFree(c->d_terms);
 	cudaFree(c->d_tiles); cudaFree(c->d_units); cudaFree(c->d_unit_terms); cudaFree(c->d_partial);
 	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
-	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms); cudaFree(c->d_walks);
+	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms); cudaFree(c->d_walks); cudaFree(c->d_items);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
@@ -513,7 +528,8 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	    (s = upload(&c->d_tterms, p->tterms, p->nterms)) ||
 	    (s = upload(&c->d_walks, p->walks, p->nwalks)) ||
 	    (s = upload(&c->d_gacc, (const void *)NULL, p->dim)) ||
-	    (s = upload(&c->d_xmax, (const void *)NULL, 1))) {
+	    (s = upload(&c->d_items, p->items, 2 * p->nitems)) ||
+	    (s = upload(&c->d_xmax, (const void *)NULL, 2))) {
 		jn_close(c);
 		return s;
 	}
@@ -524,7 +540,16 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 			z = cudaFuncSetAttribute(jn_tile_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 		if (z == cudaSuccess)
 			z = cudaFuncSetAttribute(jn_tile_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		int per_sm_f = 1, per_sm_d = 1;
+		if (z == cudaSuccess)
+			z = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_f, jn_tile_kernel<float>, TILE_THREADS, smem);
+		if (z == cudaSuccess)
+			z = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_d, jn_tile_kernel<double>, TILE_THREADS, smem);
 		if (z != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "tile kernel set-up: %s", cudaGetErrorString(z)); }
+		int per_sm = per_sm_f < per_sm_d ? per_sm_f : per_sm_d;
+		if (per_sm < 1) per_sm = 1;
+		c->tile_grid = c->num_sms * per_sm;
+		if (c->tile_grid > p->nbtiles) c->tile_grid = p->nbtiles > 0 ? p->nbtiles : 1;
 	}
 	c->engine = 3;
 	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -602,16 +627,16 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
 	} else {
 		const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
-		cudaError_t e0 = cudaMemsetAsync(c->d_xmax, 0, sizeof(unsigned int), st);
+		cudaError_t e0 = cudaMemsetAsync(c->d_xmax, 0, 2 * sizeof(unsigned int), st);
 		if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
 		if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? c->d_x32 : NULL, p->dim, c->d_xmax);
 		if (p->nbtiles) {
 			if (f32)
-				jn_tile_kernel<float><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, c->d_walks, c->d_x32,
+				jn_tile_kernel<float><<<c->tile_grid, TILE_THREADS, smem, st>>>(P, c->d_btiles, p->nbtiles, c->d_xmax + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms, c->d_walks, c->d_x32,
 											   c->d_me32, c->d_gacc, c->d_xmax,
 											   p->abs_bound);
 			else
-				jn_tile_kernel<double><<<p->nbtiles, TILE_THREADS, smem, st>>>(P, c->d_btiles, c->d_pieces, c->d_tterms, c->d_walks, d_x,
+				jn_tile_kernel<double><<<c->tile_grid, TILE_THREADS, smem, st>>>(P, c->d_btiles, p->nbtiles, c->d_xmax + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms, c->d_walks, d_x,
 												c->d_me, c->d_gacc, c->d_xmax,
 												p->abs_bound);
 		}

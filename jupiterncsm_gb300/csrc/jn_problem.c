@@ -283,7 +283,7 @@ fail:
 
 static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
 {
-	/* stable counting sort on the destination index; entries (in | out << 16, matrix_index) */
+	/* stable counting sort on the destination index; entries (source | destination << 16, matrix_index) */
 	memset(rowptr, 0, (size_t)(nrows + 1) * sizeof(uint32_t));
 	for (int64_t e = 0; e < len; e++) rowptr[(by_out ? tri[3 * e + 1] : tri[3 * e]) + 1]++;
 	for (int32_t r = 0; r < nrows; r++) rowptr[r + 1] += rowptr[r];
@@ -292,7 +292,9 @@ static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out
 	for (int64_t e = 0; e < len; e++) {
 		int32_t dst = by_out ? tri[3 * e + 1] : tri[3 * e];
 		uint32_t at = fill[dst]++;
-		ent[2 * at] = (uint32_t)tri[3 * e] | ((uint32_t)tri[3 * e + 1] << 16);
+		/* source index in the low half, destination in the high half, in both views */
+		ent[2 * at] = by_out ? ((uint32_t)tri[3 * e] | ((uint32_t)tri[3 * e + 1] << 16))
+				     : ((uint32_t)tri[3 * e + 1] | ((uint32_t)tri[3 * e] << 16));
 		ent[2 * at + 1] = (uint32_t)tri[3 * e + 2];
 	}
 	free(fill);
@@ -308,7 +310,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->mes);
 	free(p->rowptr); free(p->ent); free(p->me);
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
-	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks);
+	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks); free(p->items);
 	memset(p, 0, sizeof *p);
 }
 
@@ -359,6 +361,14 @@ static int cmp_unit_cost(const void *a, const void *b)
 #define TASK_OVERHEAD 6.0
 
 typedef struct { jn_piece_t t; double cost; } task_cost_t;
+
+static const double *g_tile_cost;
+static int cmp_tile_cost(const void *a, const void *b)
+{
+	double x = g_tile_cost[*(const int *)a], y = g_tile_cost[*(const int *)b];
+	if (x != y) return x < y ? 1 : -1;
+	return *(const int *)a - *(const int *)b;
+}
 
 static int cmp_task_cost(const void *a, const void *b)
 {
@@ -538,14 +548,21 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		p->tterms[t].Nn_src = T->Nn_src;
 		p->tterms[t].transpose = T->transpose;
 	}
-	/* pass 2: tiles of similar work, tasks longest first inside a tile */
-	int ntile_target = target_units > 0 ? target_units / 6 : 152 * 8;
+	/* pass 2: tiles of similar work.  Inside a tile, tasks of one kind and
+	 * similar width are packed into warp items (one task per 8, 16 or 32
+	 * lanes), heaviest items first; tiles are ordered heaviest first too. */
+	int ntile_target = target_units > 0 ? target_units / 2 : 152 * 24;
 	if (ntile_target < 1) ntile_target = 1;
 	double tile_target = total / ntile_target;
 	if (tile_target < 64 * 32) tile_target = 64 * 32;
 	p->pieces = malloc((ntasks ? ntasks : 1) * sizeof(jn_piece_t));
+	p->items = malloc((ntasks ? ntasks : 1) * 2 * sizeof(uint32_t));
 	int tmax_tiles = 1024;
-	p->btiles = malloc(tmax_tiles * sizeof(jn_btile_t));
+	jn_btile_t *tiles = malloc(tmax_tiles * sizeof(jn_btile_t));
+	double *tile_cost = malloc(tmax_tiles * sizeof(double));
+	int ntl = 0;
+	typedef struct { uint32_t first, width_n; double cost; } item_t;
+	item_t *items = malloc((ntasks ? ntasks : 1) * sizeof(item_t));
 	for (int ri = 0; ri < nranges; ri++) {
 		const range_t *rg = &ranges[ri];
 		const jn_block_t *B = &p->blocks[rg->b];
@@ -555,20 +572,76 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		int64_t begin = rg->t0;
 		for (int64_t k = rg->t0; k < rg->t1; k++) {
 			acc += tasks[k].cost;
-			if (acc >= per || k == rg->t1 - 1) {
-				if (p->nbtiles == tmax_tiles) { tmax_tiles *= 2; p->btiles = realloc(p->btiles, tmax_tiles * sizeof(jn_btile_t)); }
-				jn_btile_t *Tl = &p->btiles[p->nbtiles++];
-				Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)rg->r0;
-				Tl->nrows = (int32_t)(rg->r1 - rg->r0); Tl->stride = (int32_t)(B->Nn | 1);
-				qsort(tasks + begin, k + 1 - begin, sizeof *tasks, cmp_task_cost);
-				Tl->pc0 = p->npieces;
-				for (int64_t q = begin; q <= k; q++) p->pieces[p->npieces++] = tasks[q].t;
-				Tl->pc1 = p->npieces;
-				begin = k + 1;
-				acc = 0;
+			if (!(acc >= per || k == rg->t1 - 1)) continue;
+			if (ntl == tmax_tiles) {
+				tmax_tiles *= 2;
+				tiles = realloc(tiles, tmax_tiles * sizeof(jn_btile_t));
+				tile_cost = realloc(tile_cost, tmax_tiles * sizeof(double));
 			}
+			jn_btile_t *Tl = &tiles[ntl];
+			Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)rg->r0;
+			Tl->nrows = (int32_t)(rg->r1 - rg->r0); Tl->stride = (int32_t)(B->Nn | 1);
+			/* group by (kind, width), heaviest first inside a group */
+			int64_t n = k + 1 - begin;
+			for (int64_t q = begin; q <= k; q++) {
+				uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
+				uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32;
+				/* sort key: kind, width, then cost */
+				tasks[q].cost += 1e12 * (double)(JN_TASK_KIND(tasks[q].t.head) * 4 + (w >> 3));
+			}
+			qsort(tasks + begin, n, sizeof *tasks, cmp_task_cost);
+			int64_t nitems = 0;
+			double tcost = 0;
+			for (int64_t q = begin; q <= k;) {
+				const uint32_t kind = JN_TASK_KIND(tasks[q].t.head);
+				const uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
+				const uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32, per_item = 32 / w;
+				item_t *it = &items[nitems++];
+				it->first = (uint32_t)p->npieces;
+				it->cost = 0;
+				uint32_t m = 0;
+				while (q <= k && m < per_item && JN_TASK_KIND(tasks[q].t.head) == kind &&
+				       (JN_TASK_COUNT(tasks[q].t.head) <= 8 ? 8u : JN_TASK_COUNT(tasks[q].t.head) <= 16 ? 16u : 32u) == w) {
+					double cst = fmod(tasks[q].cost, 1e12);
+					if (cst > it->cost) it->cost = cst;
+					p->pieces[p->npieces++] = tasks[q].t;
+					q++;
+					m++;
+				}
+				it->width_n = w | (m << 8);
+				tcost += it->cost;
+			}
+			/* heaviest items first for the warps' dynamic fetch */
+			for (int64_t i = 1; i < nitems; i++) {
+				item_t v = items[i];
+				int64_t j = i - 1;
+				while (j >= 0 && items[j].cost < v.cost) { items[j + 1] = items[j]; j--; }
+				items[j + 1] = v;
+			}
+			Tl->pc0 = p->nitems;
+			for (int64_t i = 0; i < nitems; i++) {
+				p->items[2 * p->nitems] = items[i].first;
+				p->items[2 * p->nitems + 1] = items[i].width_n;
+				p->nitems++;
+			}
+			Tl->pc1 = p->nitems;
+			tile_cost[ntl++] = tcost;
+			begin = k + 1;
+			acc = 0;
 		}
 	}
+	/* tiles heaviest first: persistent CTAs fetch them in this order */
+	{
+		int *ord = malloc((ntl ? ntl : 1) * sizeof(int));
+		for (int i = 0; i < ntl; i++) ord[i] = i;
+		g_tile_cost = tile_cost;
+		qsort(ord, ntl, sizeof(int), cmp_tile_cost);
+		p->btiles = malloc((ntl ? ntl : 1) * sizeof(jn_btile_t));
+		for (int i = 0; i < ntl; i++) p->btiles[i] = tiles[ord[i]];
+		p->nbtiles = ntl;
+		free(ord);
+	}
+	free(tiles); free(tile_cost); free(items);
 	free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
 	return 0;
 }

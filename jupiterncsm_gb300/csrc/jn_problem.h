@@ -113,7 +113,7 @@ typedef struct {
 	int32_t Nn;
 	int32_t row0, nrows;
 	int32_t stride;         /* shared-memory row stride (odd) */
-	int64_t pc0, pc1;       /* range into jn_plan_t.pieces */
+	int64_t pc0, pc1;       /* range into jn_plan_t.items */
 } jn_btile_t;
 
 /*
@@ -178,6 +178,7 @@ typedef struct {
 	int64_t npieces;   jn_piece_t *pieces;
 	jn_tterm_t *tterms;             /* nterms compact term descriptions */
 	int64_t nwalks;    uint32_t *walks;    /* pairs {w0, len | idx << 16} */
+	int64_t nitems;    uint32_t *items;    /* warp items {first task, width | ntasks << 8} */
 	int max_tile_elems;             /* shared-memory accumulator size needed */
 	double abs_bound;               /* max over y elements of sum |M| over its contributions */
 	/* accounting */

@@ -16,7 +16,7 @@ static double term_element(const jn_plan_t *P, const jn_term_t *t, const double 
 	double acc = 0.0;
 	if (t->kind == JN_KIND_P) {
 		for (uint32_t j = rp[t->p_ptr + p]; j < rp[t->p_ptr + p + 1]; j++) {
-			uint32_t src = t->transpose ? ent[2 * j] >> 16 : ent[2 * j] & 0xffffu, mi = ent[2 * j + 1];
+			uint32_t src = ent[2 * j] & 0xffffu, mi = ent[2 * j + 1];
 			double m = me[mi & 0x7fffffffu];
 			if (fabs(m) < 1e-12) continue;
 			if (mi & 0x80000000u) m = -m;
@@ -24,7 +24,7 @@ static double term_element(const jn_plan_t *P, const jn_term_t *t, const double 
 		}
 	} else if (t->kind == JN_KIND_N) {
 		for (uint32_t j = rp[t->n_ptr + n]; j < rp[t->n_ptr + n + 1]; j++) {
-			uint32_t src = t->transpose ? ent[2 * j] >> 16 : ent[2 * j] & 0xffffu, mi = ent[2 * j + 1];
+			uint32_t src = ent[2 * j] & 0xffffu, mi = ent[2 * j + 1];
 			double m = me[mi & 0x7fffffffu];
 			if (fabs(m) < 1e-12) continue;
 			if (mi & 0x80000000u) m = -m;
@@ -34,11 +34,11 @@ static double term_element(const jn_plan_t *P, const jn_term_t *t, const double 
 		uint32_t j0 = rp[t->n_ptr + n], j1 = rp[t->n_ptr + n + 1];
 		if (j0 == j1) return 0.0;
 		for (uint32_t i = rp[t->p_ptr + p]; i < rp[t->p_ptr + p + 1]; i++) {
-			uint32_t ps = t->transpose ? ent[2 * i] >> 16 : ent[2 * i] & 0xffffu, mip = ent[2 * i + 1];
+			uint32_t ps = ent[2 * i] & 0xffffu, mip = ent[2 * i + 1];
 			const double *mrow = me + (size_t)t->nd * (mip & 0x7fffffffu);
 			const double *xrow = xs + (size_t)ps * t->Nn_src;
 			for (uint32_t j = j0; j < j1; j++) {
-				uint32_t ns = t->transpose ? ent[2 * j] >> 16 : ent[2 * j] & 0xffffu, min = ent[2 * j + 1];
+				uint32_t ns = ent[2 * j] & 0xffffu, min = ent[2 * j + 1];
 				double m = mrow[min & 0x7fffffffu];
 				if ((mip ^ min) & 0x80000000u) m = -m;
 				acc = fma(m, xrow[ns], acc);
@@ -126,16 +126,21 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 	const uint32_t *ent = P->ent, *W = P->walks;
 	double scale = ldexp(1.0, S);
 	float scalef = (float)scale;
-	for (int64_t k = tl->pc0; k < tl->pc1; k++) {
-		const jn_piece_t *task = &P->pieces[k];
+	for (int64_t it = tl->pc0; it < tl->pc1; it++) {
+	CHECK(it < P->nitems);
+	const uint32_t first = P->items[2 * it], w = P->items[2 * it + 1] & 0xff, nsub = P->items[2 * it + 1] >> 8;
+	CHECK((w == 8 || w == 16 || w == 32) && nsub >= 1 && nsub * w <= 32 && first + nsub <= (uint64_t)P->npieces);
+	for (uint32_t sub = 0; sub < nsub; sub++) {
+		const jn_piece_t *task = &P->pieces[first + sub];
 		const int term = (int)JN_TASK_TERM(task->head), kind = (int)JN_TASK_KIND(task->head);
 		const int count = (int)JN_TASK_COUNT(task->head);
-		CHECK(term < P->nterms && count >= 1 && count <= 32 && kind <= JN_TASK_N_B);
+		CHECK(term < P->nterms && count >= 1 && (uint32_t)count <= w && kind <= JN_TASK_N_B);
+		CHECK(kind == (int)JN_TASK_KIND(P->pieces[first].head));
 		const jn_term_t *t = &P->terms[term];
 		const jn_tterm_t *tt = &P->tterms[term];
 		CHECK(tt->me_off == t->me_off && tt->src_off == t->src_off && tt->nd == t->nd && tt->Nn_src == t->Nn_src &&
 		      tt->transpose == t->transpose);
-		const int tr = t->transpose != 0, Ns = t->Nn_src, nd = t->nd;
+		const int Ns = t->Nn_src, nd = t->nd;
 		for (int lane = 0; lane < count; lane++) {
 			const uint32_t lb = task->lane_base + lane;
 			for (uint32_t q = 0; q < task->loop_len; q++) {
@@ -164,13 +169,13 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				if (kind == JN_TASK_NP_A) {
 					for (uint32_t j = n0; j < n1; j++) {
 						uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
-						int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
-						int ndst = tr ? (int)(qx & 0xffff) : (int)(qx >> 16);
+						int scol = (int)(qx & 0xffff);
+						int ndst = (int)(qx >> 16);
 						CHECK(ndst == dcol);
 						for (uint32_t i = p0; i < p1; i++) {
 							uint32_t px = ent[2 * i], py = ent[2 * i + 1];
-							int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
-							int pdst = tr ? (int)(px & 0xffff) : (int)(px >> 16);
+							int srow = (int)(px & 0xffff);
+							int pdst = (int)(px >> 16);
 							CHECK(pdst == drow);
 							size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
 							VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
@@ -179,10 +184,10 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				} else if (kind == JN_TASK_NP_B) {
 					for (uint32_t i = p0; i < p1; i++) {
 						uint32_t px = ent[2 * i], py = ent[2 * i + 1];
-						int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+						int srow = (int)(px & 0xffff);
 						for (uint32_t j = n0; j < n1; j++) {
 							uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
-							int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+							int scol = (int)(qx & 0xffff);
 							size_t mi = (qy & 0x7fffffffu) + (size_t)nd * (py & 0x7fffffffu);
 							VISIT(mi, t->src_off + srow * Ns + scol, ((py ^ qy) & 0x80000000u) != 0, 0);
 						}
@@ -191,13 +196,13 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 					CHECK(ccol >= 0 && ccol < Nn);
 					for (uint32_t i = p0; i < p1; i++) {
 						uint32_t px = ent[2 * i], py = ent[2 * i + 1];
-						int srow = tr ? (int)(px >> 16) : (int)(px & 0xffff);
+						int srow = (int)(px & 0xffff);
 						VISIT(py & 0x7fffffffu, t->src_off + srow * Ns + ccol, (py & 0x80000000u) != 0, 1);
 					}
 				} else {
 					for (uint32_t j = n0; j < n1; j++) {
 						uint32_t qx = ent[2 * j], qy = ent[2 * j + 1];
-						int scol = tr ? (int)(qx >> 16) : (int)(qx & 0xffff);
+						int scol = (int)(qx & 0xffff);
 						VISIT(qy & 0x7fffffffu, t->src_off + rrow * Ns + scol, (qy & 0x80000000u) != 0, 1);
 					}
 				}
@@ -205,6 +210,7 @@ static void tile_model(const jn_plan_t *P, const jn_btile_t *tl, const double *x
 				sacc[(drow - tl->row0) * Nn + dcol] += f32 ? llrintf(runf * scalef) : llrint(run * scale);
 			}
 		}
+	}
 	}
 	for (int i = 0; i < E; i++) gacc[tl->dst_off + (int64_t)tl->row0 * Nn + i] += sacc[i];
 	free(sacc);
