@@ -335,25 +335,11 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 					const uint2 qn = __ldg(ent + j);
 					const int scol = (int)(qn.x & 0xffffu);
 					const T *__restrict__ mcol = mb + (qn.y & MASK31);
-					const T *__restrict__ xcol = xs + scol;
-					uint32_t i = p0;
-					/* four gathers in flight, then the multiply-adds in list order */
-					for (; i + 4 <= p1; i += 4) {
-						const uint2 q0 = __ldg(ent + i), q1 = __ldg(ent + i + 1);
-						const uint2 q2 = __ldg(ent + i + 2), q3 = __ldg(ent + i + 3);
-						const T m0 = __ldg(mcol + nd * (q0.y & MASK31)), m1 = __ldg(mcol + nd * (q1.y & MASK31));
-						const T m2 = __ldg(mcol + nd * (q2.y & MASK31)), m3 = __ldg(mcol + nd * (q3.y & MASK31));
-						const T x0 = __ldg(xcol + (int)(q0.x & 0xffffu) * Ns), x1 = __ldg(xcol + (int)(q1.x & 0xffffu) * Ns);
-						const T x2 = __ldg(xcol + (int)(q2.x & 0xffffu) * Ns), x3 = __ldg(xcol + (int)(q3.x & 0xffffu) * Ns);
-						run = fma(flip_sign(m0, q0.y ^ qn.y), x0, run);
-						run = fma(flip_sign(m1, q1.y ^ qn.y), x1, run);
-						run = fma(flip_sign(m2, q2.y ^ qn.y), x2, run);
-						run = fma(flip_sign(m3, q3.y ^ qn.y), x3, run);
-					}
-					for (; i < p1; i++) {
+					for (uint32_t i = p0; i < p1; i++) {
 						const uint2 qp = __ldg(ent + i);
+						const int srow = (int)(qp.x & 0xffffu);
 						const T m = __ldg(mcol + nd * (qp.y & MASK31));
-						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xcol + (int)(qp.x & 0xffffu) * Ns), run);
+						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xs + srow * Ns + scol), run);
 					}
 				}
 				add_fixed(lo, hi, rbase + drow * stride + dcol, to_fixed<T>(run * scale));
@@ -372,23 +358,11 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 					const int srow = (int)(qp.x & 0xffffu);
 					const T *__restrict__ mrow = mb + nd * (qp.y & MASK31);
 					const T *__restrict__ xrow = xs + srow * Ns;
-					uint32_t j = n0;
-					for (; j + 4 <= n1; j += 4) {
-						const uint2 q0 = __ldg(ent + j), q1 = __ldg(ent + j + 1);
-						const uint2 q2 = __ldg(ent + j + 2), q3 = __ldg(ent + j + 3);
-						const T m0 = __ldg(mrow + (q0.y & MASK31)), m1 = __ldg(mrow + (q1.y & MASK31));
-						const T m2 = __ldg(mrow + (q2.y & MASK31)), m3 = __ldg(mrow + (q3.y & MASK31));
-						const T x0 = __ldg(xrow + (q0.x & 0xffffu)), x1 = __ldg(xrow + (q1.x & 0xffffu));
-						const T x2 = __ldg(xrow + (q2.x & 0xffffu)), x3 = __ldg(xrow + (q3.x & 0xffffu));
-						run = fma(flip_sign(m0, qp.y ^ q0.y), x0, run);
-						run = fma(flip_sign(m1, qp.y ^ q1.y), x1, run);
-						run = fma(flip_sign(m2, qp.y ^ q2.y), x2, run);
-						run = fma(flip_sign(m3, qp.y ^ q3.y), x3, run);
-					}
-					for (; j < n1; j++) {
+					for (uint32_t j = n0; j < n1; j++) {
 						const uint2 qn = __ldg(ent + j);
+						const int scol = (int)(qn.x & 0xffffu);
 						const T m = __ldg(mrow + (qn.y & MASK31));
-						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xrow + (qn.x & 0xffffu)), run);
+						run = fma(flip_sign(m, qp.y ^ qn.y), __ldg(xrow + scol), run);
 					}
 				}
 				add_fixed(lo, hi, rbase + drow * stride + dcol, to_fixed<T>(run * scale));
