@@ -55,6 +55,10 @@ struct jn_ctx {
 /* enqueue y (+)= H x on stream st */
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st);
 
+/* the block-tile product with caller-chosen scratch (see jn_matvec.cu) */
+jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st,
+			   cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32, int clear_acc);
+
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);
 

@@ -603,6 +603,43 @@ static jn_status ensure_f32(jn_ctx *c)
 }
 
 /* enqueue the two kernels of one product; `mid` (optional) is recorded between them */
+/* The block-tile product with caller-chosen scratch: gacc (dim 64-bit
+ * words, zero on entry unless clear_acc), ctrl (2 words: max|x| bits and
+ * the tile counter), x32 (dim floats, FP32 precision only).  Enqueues only;
+ * never allocates. */
+jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st,
+			   cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32, int clear_acc)
+{
+	const jn_plan_t *p = &c->plan;
+	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
+	const int f32 = c->precision == 32;
+	if (f32 && !c->d_me32) return fail(JN_ERR_INVALID, "FP32 matrix elements are not set up");
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (g < 1) g = 1;
+	const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
+	cudaError_t e0 = cudaMemsetAsync(ctrl, 0, 2 * sizeof(unsigned int), st);
+	if (e0 == cudaSuccess && clear_acc && p->dim)
+		e0 = cudaMemsetAsync(gacc, 0, (size_t)p->dim * sizeof(unsigned long long), st);
+	if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
+	if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? x32 : NULL, p->dim, ctrl);
+	if (p->nbtiles) {
+		if (f32)
+			jn_tile_kernel<float><<<c->tile_grid, TILE_THREADS, smem, st>>>(
+				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
+				c->d_walks, x32, c->d_me32, gacc, ctrl, p->abs_bound);
+		else
+			jn_tile_kernel<double><<<c->tile_grid, TILE_THREADS, smem, st>>>(
+				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
+				c->d_walks, d_x, c->d_me, gacc, ctrl, p->abs_bound);
+	}
+	if (mid) cudaEventRecord(mid, st);
+	if (p->dim) jn_finalize_kernel<<<g, 256, 0, st>>>(gacc, d_y, p->dim, ctrl, p->abs_bound, accumulate);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
 static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t mid)
 {
 	const jn_plan_t *p = &c->plan;
@@ -626,22 +663,8 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		if (mid) cudaEventRecord(mid, st);
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
 	} else {
-		const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
-		cudaError_t e0 = cudaMemsetAsync(c->d_xmax, 0, 2 * sizeof(unsigned int), st);
-		if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
-		if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? c->d_x32 : NULL, p->dim, c->d_xmax);
-		if (p->nbtiles) {
-			if (f32)
-				jn_tile_kernel<float><<<c->tile_grid, TILE_THREADS, smem, st>>>(P, c->d_btiles, p->nbtiles, c->d_xmax + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms, c->d_walks, c->d_x32,
-											   c->d_me32, c->d_gacc, c->d_xmax,
-											   p->abs_bound);
-			else
-				jn_tile_kernel<double><<<c->tile_grid, TILE_THREADS, smem, st>>>(P, c->d_btiles, p->nbtiles, c->d_xmax + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms, c->d_walks, d_x,
-												c->d_me, c->d_gacc, c->d_xmax,
-												p->abs_bound);
-		}
-		if (mid) cudaEventRecord(mid, st);
-		if (p->dim) jn_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, c->d_xmax, p->abs_bound, accumulate);
+		jn_status s = jn_enqueue_tiles(c, d_x, d_y, accumulate, st, mid, c->d_gacc, c->d_xmax, c->d_x32, 0);
+		if (s) return s;
 	}
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
