@@ -110,6 +110,24 @@ jn_status jn_matvec_device(jn_ctx *ctx, const double *d_x, double *d_y, int accu
  */
 jn_status jn_matvec_files(jn_ctx *ctx, const char *output_vector_directory, const char *input_vector_directory);
 
+/*
+ * y += H x (accumulate = 1) or y = H x (accumulate = 0) on DEVICE pointers,
+ * for callers that must not allocate device memory: a solver that has sized
+ * its Krylov basis to the memory it was granted, an application under a
+ * fixed device-memory budget, or a loop that cannot take the synchronisation
+ * an allocation may bring.  Same product as jn_matvec_device (block-tile
+ * engine, the context's precision); its scratch is a fixed array inside the
+ * library that every GPU loading the library holds until exit, so it serves
+ * dimensions up to JN_NOALLOC_MAX_DIM and rejects larger ones.  All calls
+ * share that array: calls whose kernels overlap on the GPU race, so
+ * serialise them.  The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress) and caches it; make that first call
+ * before any stream capture.  No counterpart in the reference, which has no
+ * device memory.
+ */
+#define JN_NOALLOC_MAX_DIM 262144
+jn_status jn_matvec_device_noalloc(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, void *stream);
+
 /* y (+)= H x on device pointers, on the context's stream, with CUDA events
  * around each of the two kernels of the product; waits for completion and
  * returns their durations in milliseconds (ms[0] the gather-multiply kernel,
