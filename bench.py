@@ -55,38 +55,100 @@ def measured_peaks():
         return None
 
 
-def profile_traffic(workload):
-    """dram bytes per launch of the gather kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"matvec_units_kernel_{workload}.md")
+def profile_traffic(workload, precision):
+    """DRAM bytes (read + write) per launch of the tile kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"jn_tile_kernel_{workload}.md")
     try:
-        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        m = re.search(rf"dram_bytes_per_launch_fp{precision}:\s*([0-9.eE+]+)", open(path).read())
         return float(m.group(1)) if m else None
     except OSError:
         return None
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    """SM clocks and throttle reasons sampled during the timed region.
+
+    NVML (libnvidia-ml, read-only queries) is polled every 2 ms from a thread,
+    so that even a timed region of a few milliseconds gets samples; where NVML
+    cannot be loaded, `nvidia-smi -lms 200` is used instead."""
+    SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason bits
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8 | 0x80, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40}
 
     def __init__(self, device):
         self.device = device
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        try:
+            self.nvml_index = int(vis.split(",")[device]) if vis else device
+        except (ValueError, IndexError):
+            self.nvml_index = device
         self.proc = None
         self.path = None
+        self.thread = None
+        self.samples = []
+        self.source = None
+
+    def _nvml(self):
+        import ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.nvml_index), ctypes.byref(h)) != 0:
+            raise OSError("nvmlDeviceGetHandleByIndex failed")
+        reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint(0)
+        lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx))
+        return lib, h, reasons_fn, mx.value
 
     def start(self):
+        import threading
+        try:
+            lib, h, reasons_fn, mx = self._nvml()
+        except Exception:
+            return self._start_smi()
+        import ctypes
+        self.source = "nvml (2 ms polling)"
+        self.max_mhz = mx
+        self.stop_flag = threading.Event()
+
+        def run():
+            sm, rs, pw = ctypes.c_uint(), ctypes.c_ulonglong(), ctypes.c_uint()
+            while not self.stop_flag.is_set():
+                if lib.nvmlDeviceGetClockInfo(h, ctypes.c_int(1), ctypes.byref(sm)) == 0 and \
+                        reasons_fn(h, ctypes.byref(rs)) == 0:
+                    lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw))
+                    self.samples.append((sm.value, rs.value, pw.value / 1000.0))
+                time.sleep(0.002)
+        self.thread = threading.Thread(target=run, daemon=True)
+        self.thread.start()
+
+    def _start_smi(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.nvml_index), f"--query-gpu={self.SMI_FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=fd, stderr=subprocess.DEVNULL)
             os.close(fd)
+            self.source = "nvidia-smi -lms 200"
         except Exception:
             self.proc = None
 
     def stop(self):
+        if self.thread:
+            self.stop_flag.set()
+            self.thread.join(timeout=5)
+            if not self.samples:
+                return None
+            sm = [s[0] for s in self.samples]
+            reasons = sorted({n for s in self.samples for n, b in self.REASON_BITS.items() if s[1] & b})
+            return {"sm_mhz": statistics.median(sm), "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                    "samples": len(self.samples), "sm_mhz_min": min(sm),
+                    "power_w_median": statistics.median(s[2] for s in self.samples), "source": self.source}
         if not self.proc:
             return None
         self.proc.terminate()
@@ -107,7 +169,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "source": self.source}
 
 
 def prepare(workload, workdir):
@@ -276,12 +338,12 @@ def main():
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = bytes_step / (main_r["kernel_ms"] / 1e3) / 1e9
-    traffic = profile_traffic(args.workload)
+    traffic = profile_traffic(args.workload, prec)
 
     def path_summary(r, p):
         b = bytes_for(p)
         return {"ms_per_step": r["ms_per_step"], "GB_per_s": b / (r["ms_per_step"] / 1e3) / 1e9,
-                "bytes_per_step": b, "gather_kernel_ms": r["kernel_ms"],
+                "bytes_per_step": b, "tile_kernel_ms": r["kernel_ms"],
                 "hbm_frac": b / (r["kernel_ms"] / 1e3) / 1e9 / peak,
                 "fp64_multiply_adds_per_s" if p == 64 else "multiply_adds_per_s":
                     st["multiply_adds"] / (r["kernel_ms"] / 1e3)}
@@ -300,11 +362,11 @@ def main():
             "paths": {"fp64": path_summary(r64, 64), "fp32": path_summary(r32, 32),
                       "fp32_max_rel_diff_vs_fp64": rel32},
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * D, "d2h_bytes_per_step": 8 * D},
-            "gpu_launches": (2 if prec == 64 else 3) * args.steps,
+            "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
-                         "kernel": "jn_pieces_kernel"},
+                         "kernel": "jn_tile_kernel<double>" if prec == 64 else "jn_tile_kernel<float>"},
             "clocks": main_r["clocks"]}
     if rank == 0:
         try:

@@ -129,9 +129,10 @@ jn_status jn_matvec_files(jn_ctx *ctx, const char *output_vector_directory, cons
 jn_status jn_matvec_device_noalloc(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, void *stream);
 
 /* y (+)= H x on device pointers, on the context's stream, with CUDA events
- * around each of the two kernels of the product; waits for completion and
- * returns their durations in milliseconds (ms[0] the gather-multiply kernel,
- * ms[1] the ordered reduction).  Used for roofline accounting. */
+ * around the gather-multiply kernel; waits for completion and returns
+ * durations in milliseconds: ms[0] the gather-multiply kernel alone, ms[1]
+ * everything else of the product (clearing, x preparation, the final
+ * conversion into y).  Used for roofline accounting. */
 jn_status jn_matvec_profile(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, float ms[2]);
 
 /* Arithmetic of the products of this context: 64 (default) computes every

@@ -159,7 +159,7 @@ class Hamiltonian:
                                           ctypes.c_void_p(stream)))
 
     def matvec_profile(self, d_x, d_y, accumulate=False):
-        """Device product on the context stream; returns (ms gather kernel, ms reduction kernel)."""
+        """Device product on the context stream; returns (ms of the gather-multiply kernel, ms of the rest)."""
         ms = (ctypes.c_float * 2)()
         _check(gpu_lib().jn_matvec_profile(self._h, ctypes.c_void_p(d_x), ctypes.c_void_p(d_y), int(accumulate), ms))
         return ms[0], ms[1]

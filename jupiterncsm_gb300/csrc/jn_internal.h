@@ -55,9 +55,12 @@ struct jn_ctx {
 /* enqueue y (+)= H x on stream st */
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st);
 
-/* the block-tile product with caller-chosen scratch (see jn_matvec.cu) */
+/* the block-tile product with caller-chosen scratch (see jn_matvec.cu); the
+ * optional events `pre` and `mid` are recorded just before and just after
+ * the tile kernel */
 jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st,
-			   cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32, int clear_acc);
+			   cudaEvent_t pre, cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32,
+			   int clear_acc);
 
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);

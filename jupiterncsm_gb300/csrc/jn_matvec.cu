@@ -608,7 +608,8 @@ static jn_status ensure_f32(jn_ctx *c)
  * the tile counter), x32 (dim floats, FP32 precision only).  Enqueues only;
  * never allocates. */
 jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st,
-			   cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32, int clear_acc)
+			   cudaEvent_t pre, cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32,
+			   int clear_acc)
 {
 	const jn_plan_t *p = &c->plan;
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
@@ -623,6 +624,7 @@ jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumu
 		e0 = cudaMemsetAsync(gacc, 0, (size_t)p->dim * sizeof(unsigned long long), st);
 	if (e0 != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e0));
 	if (p->dim) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, f32 ? x32 : NULL, p->dim, ctrl);
+	if (pre) cudaEventRecord(pre, st);
 	if (p->nbtiles) {
 		if (f32)
 			jn_tile_kernel<float><<<c->tile_grid, TILE_THREADS, smem, st>>>(
@@ -640,7 +642,8 @@ jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumu
 	return JN_OK;
 }
 
-static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t mid)
+static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
+		       cudaEvent_t mid)
 {
 	const jn_plan_t *p = &c->plan;
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
@@ -654,8 +657,9 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 	if (g < 1) g = 1;
 	if (c->engine == 2) {
 		const int ug = (p->nunits + WARPS - 1) / WARPS, tg = (p->ntiles + WARPS - 1) / WARPS;
+		if (f32 && p->dim) jn_to_f32_kernel<<<g, 256, 0, st>>>(d_x, c->d_x32, p->dim);
+		if (pre) cudaEventRecord(pre, st);
 		if (f32) {
-			if (p->dim) jn_to_f32_kernel<<<g, 256, 0, st>>>(d_x, c->d_x32, p->dim);
 			if (p->nunits) jn_pieces_kernel<true><<<ug, WARPS * 32, 0, st>>>(P, c->d_x32, c->d_me32, c->d_partial, p->nunits);
 		} else if (p->nunits) {
 			jn_pieces_kernel<false><<<ug, WARPS * 32, 0, st>>>(P, d_x, c->d_me, c->d_partial, p->nunits);
@@ -663,7 +667,7 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		if (mid) cudaEventRecord(mid, st);
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
 	} else {
-		jn_status s = jn_enqueue_tiles(c, d_x, d_y, accumulate, st, mid, c->d_gacc, c->d_xmax, c->d_x32, 0);
+		jn_status s = jn_enqueue_tiles(c, d_x, d_y, accumulate, st, pre, mid, c->d_gacc, c->d_xmax, c->d_x32, 0);
 		if (s) return s;
 	}
 	cudaError_t e = cudaGetLastError();
@@ -680,7 +684,7 @@ extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st)
 {
-	return enqueue(c, d_x, d_y, accumulate, st, NULL);
+	return enqueue(c, d_x, d_y, accumulate, st, NULL, NULL);
 }
 
 extern "C" jn_status jn_set_precision(jn_ctx *c, int precision)
@@ -705,16 +709,18 @@ extern "C" jn_status jn_matvec_profile(jn_ctx *c, const double *d_x, double *d_y
 {
 	if (!c || !d_x || !d_y || !ms) return fail(JN_ERR_INVALID, "null argument");
 	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
-	cudaEvent_t ev[3];
-	for (int i = 0; i < 3; i++) CUDA_TRY(cudaEventCreate(&ev[i]));
+	cudaEvent_t ev[4];
+	for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&ev[i]));
 	CUDA_TRY(cudaEventRecord(ev[0], c->stream));
-	jn_status s = enqueue(c, d_x, d_y, accumulate, c->stream, ev[1]);
+	jn_status s = enqueue(c, d_x, d_y, accumulate, c->stream, ev[1], ev[2]);
 	if (s) return s;
-	CUDA_TRY(cudaEventRecord(ev[2], c->stream));
-	CUDA_TRY(cudaEventSynchronize(ev[2]));
-	CUDA_TRY(cudaEventElapsedTime(&ms[0], ev[0], ev[1]));
-	CUDA_TRY(cudaEventElapsedTime(&ms[1], ev[1], ev[2]));
-	for (int i = 0; i < 3; i++) cudaEventDestroy(ev[i]);
+	CUDA_TRY(cudaEventRecord(ev[3], c->stream));
+	CUDA_TRY(cudaEventSynchronize(ev[3]));
+	float total = 0.f;
+	CUDA_TRY(cudaEventElapsedTime(&ms[0], ev[1], ev[2]));
+	CUDA_TRY(cudaEventElapsedTime(&total, ev[0], ev[3]));
+	ms[1] = total - ms[0];
+	for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
 	return JN_OK;
 }
 

@@ -75,6 +75,6 @@ extern "C" jn_status jn_matvec_device_noalloc(jn_ctx *c, const double *d_x, doub
 	unsigned long long *acc = (unsigned long long *)base;
 	float *x32 = (float *)(base + (size_t)JN_NOALLOC_MAX_DIM * 8);
 	unsigned int *ctrl = (unsigned int *)(base + (size_t)JN_NOALLOC_MAX_DIM * 12);
-	return jn_enqueue_tiles(c, d_x, d_y, accumulate, stream ? (cudaStream_t)stream : c->stream, NULL, acc, ctrl, x32,
-				1);
+	return jn_enqueue_tiles(c, d_x, d_y, accumulate, stream ? (cudaStream_t)stream : c->stream, NULL, NULL, acc, ctrl,
+				x32, 1);
 }
