@@ -233,6 +233,72 @@ jn_status jn_lanczos_save_eigenvectors(jn_ctx *ctx, const char *directory, int c
  * (Bacchus/eigensystem/eigensystem.c:99-113) for the given values. */
 void jn_print_eigensystem(const double *eigenvalues, int count);
 
+/* ------------------------------------------------------------------ */
+/* J-scheme -> M-scheme two-body transform (Mercury)                   */
+/* ------------------------------------------------------------------ */
+typedef struct jn_transform jn_transform;
+
+typedef struct {
+	int num_two_body_blocks;
+	int num_one_body_blocks;        /* written as zeros, as the reference does */
+	size_t num_elements;            /* two-body matrix elements computed per run */
+	size_t num_pair_states;         /* M-scheme pair states with their (J, T) expansion */
+	size_t num_configurations;      /* rows of the interaction file */
+	double dense_flops;             /* flops of the reference's dense S^T V S decoupling, for comparison */
+	double algorithmic_bytes;       /* compulsory device traffic of one run */
+	double plan_seconds;            /* host planning time of jn_transform_open */
+} jn_transform_stats;
+
+/*
+ * Plan the transform of a J-scheme two-body interaction in the Antoine
+ * format (src/Neptune/input/read_2nf_antoine_format.c:70-111) into the
+ * M-scheme matrix-element blocks that the combination table lists, and
+ * upload the plan to the current CUDA device.  Arguments are those of
+ * mercury_J_scheme_to_internal.x (src/Mercury/arguments/arguments.c:88-160):
+ * the combination table, the index-list base directory holding
+ * <p|n|pp|nn>_inds_index_lists/basis_energy_<E>, Z, N, the single- and
+ * two-particle energy limits, the interaction file, and whether the kinetic
+ * column is added (the reference's default; --exclude-kinetic-energy turns
+ * it off).  Replaces new_transform_2nf_block_manager + open_antoine_2nf_file
+ * (src/Mercury/transform_2nf_block_manager/transform_2nf_block_manager.c:89-111).
+ */
+jn_status jn_transform_open(const char *combination_table_file, const char *index_list_dir, int num_protons,
+			    int num_neutrons, int single_particle_energy, int two_particle_energy,
+			    const char *antoine_file, int include_kinetic_energy, jn_transform **transform);
+
+/* Enqueue the computation of every two-body block (one kernel) on `stream`
+ * (NULL: the transform's stream).  Replaces decouple_transform_2nf_block +
+ * get_transform_2nf_matrix_block over all blocks
+ * (transform_2nf_block_manager.c:113-268, compute_jt_block in
+ * src/Neptune/block_transform/block_transform.c:358-415). */
+jn_status jn_transform_run(jn_transform *transform, void *stream);
+
+/* One run on the transform's stream timed with CUDA events (milliseconds). */
+jn_status jn_transform_profile(jn_transform *transform, float *ms);
+
+/* Elements of matrix-element block `block_id` from the last run (count only
+ * when host_out is NULL). */
+jn_status jn_transform_elements(jn_transform *transform, int block_id, double *host_out, size_t capacity,
+				size_t *count);
+
+/* Run and write <output_dir>/<id>_matrix_elements for every one- and
+ * two-body block (save_mercury_matrix_block,
+ * src/Mercury/mercury_matrix_block/mercury_matrix_block.c:106-179). */
+jn_status jn_transform_write(jn_transform *transform, const char *output_dir);
+
+jn_status jn_transform_get_stats(const jn_transform *transform, jn_transform_stats *stats);
+void jn_transform_close(jn_transform *transform);
+
+/* open + write + close: the two-body part of mercury_J_scheme_to_internal.x
+ * (src/Mercury/programs/mercury_J_scheme_to_internal.c:65-202). */
+jn_status jn_transform_2nf(const char *combination_table_file, const char *index_list_dir, const char *output_dir,
+			   int num_protons, int num_neutrons, int single_particle_energy, int two_particle_energy,
+			   const char *antoine_file, int include_kinetic_energy);
+
+/* <j1 m1 j2 m2 | j3 m3> with all arguments doubled, as clebsch_gordan
+ * defines it (src/Neptune/clebsch_gordan/clebsch_gordan.c:31-42); host only. */
+double jn_clebsch_gordan(int j1, int j2, int j3, int m1, int m2, int m3);
+
 #ifdef __cplusplus
 }
 #endif

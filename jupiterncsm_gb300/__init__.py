@@ -23,8 +23,11 @@ GPU_LIB = os.path.join(LIBDIR, "libjncsm_gpu.so")
 GEN_LIB = os.path.join(LIBDIR, "libjncsm_gen.so")
 GEN_CLI = os.path.join(LIBDIR, "jn_gen")
 BACCHUS_CLI = os.path.join(LIBDIR, "jn_bacchus")
+MERCURY_CLI = os.path.join(LIBDIR, "jn_mercury")
 
 JN_OK = 0
+(JN_ERR_INVALID, JN_ERR_IO, JN_ERR_FORMAT, JN_ERR_CUDA, JN_ERR_NOMEM, JN_ERR_NOT_CONVERGED,
+ JN_ERR_TIMEOUT) = range(1, 8)
 STATUS_NAMES = {0: "JN_OK", 1: "JN_ERR_INVALID", 2: "JN_ERR_IO", 3: "JN_ERR_FORMAT", 4: "JN_ERR_CUDA",
                 5: "JN_ERR_NOMEM", 6: "JN_ERR_NOT_CONVERGED", 7: "JN_ERR_TIMEOUT"}
 
@@ -45,6 +48,13 @@ class PlanStats(ctypes.Structure):
                 ("list_entries", ctypes.c_size_t), ("me_elements", ctypes.c_size_t),
                 ("me_referenced", ctypes.c_size_t), ("multiply_adds", ctypes.c_double), ("algorithmic_bytes", ctypes.c_double),
                 ("num_work_units", ctypes.c_int), ("num_tiles", ctypes.c_int)]
+
+
+class TransformStats(ctypes.Structure):
+    _fields_ = [("num_two_body_blocks", ctypes.c_int), ("num_one_body_blocks", ctypes.c_int),
+                ("num_elements", ctypes.c_size_t), ("num_pair_states", ctypes.c_size_t),
+                ("num_configurations", ctypes.c_size_t), ("dense_flops", ctypes.c_double),
+                ("algorithmic_bytes", ctypes.c_double), ("plan_seconds", ctypes.c_double)]
 
 
 MAX_REPORTED = 64
@@ -100,9 +110,22 @@ def gpu_lib():
     L.jn_lanczos_save_eigenvectors.argtypes = [vp, cp, ci]
     L.jn_print_eigensystem.argtypes = [ctypes.POINTER(ctypes.c_double), ci]
     L.jn_print_eigensystem.restype = None
+    L.jn_transform_open.argtypes = [cp, cp, ci, ci, ci, ci, cp, ci, ctypes.POINTER(vp)]
+    L.jn_transform_run.argtypes = [vp, vp]
+    L.jn_transform_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.jn_transform_elements.argtypes = [vp, ci, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.jn_transform_write.argtypes = [vp, cp]
+    L.jn_transform_get_stats.argtypes = [vp, ctypes.POINTER(TransformStats)]
+    L.jn_transform_close.argtypes = [vp]
+    L.jn_transform_close.restype = None
+    L.jn_transform_2nf.argtypes = [cp, cp, cp, ci, ci, ci, ci, cp, ci]
+    L.jn_clebsch_gordan.argtypes = [ci] * 6
+    L.jn_clebsch_gordan.restype = ctypes.c_double
     for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
                  "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_set_engine", "jn_lanczos",
-                 "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors"):
+                 "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
+                 "jn_transform_open", "jn_transform_run", "jn_transform_profile", "jn_transform_elements",
+                 "jn_transform_write", "jn_transform_get_stats", "jn_transform_2nf"):
         getattr(L, name).restype = ci
     _gpu = L
     return L
@@ -225,6 +248,87 @@ class Hamiltonian:
         return out
 
 
+class Transform:
+    """J-scheme -> M-scheme two-body transform on the GPU (Mercury's two-body part)."""
+
+    def __init__(self, comb, index_list_dir, Z, N, single_particle_energy, two_particle_energy, antoine_file,
+                 include_kinetic=True):
+        L = gpu_lib()
+        h = ctypes.c_void_p()
+        _check(L.jn_transform_open(comb.encode(), index_list_dir.encode(), Z, N, single_particle_energy,
+                                   two_particle_energy, antoine_file.encode(), int(include_kinetic), ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_dir(cls, d, Z, N, single_particle_energy, two_particle_energy, include_kinetic=True):
+        """A generator output directory: comb.txt, anicr/ and antoine_2nf.bin."""
+        return cls(os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), Z, N, single_particle_energy,
+                   two_particle_energy, os.path.join(d, "antoine_2nf.bin"), include_kinetic)
+
+    def run(self, stream=None):
+        _check(gpu_lib().jn_transform_run(self._h, ctypes.c_void_p(stream)))
+
+    def profile(self):
+        ms = ctypes.c_float()
+        _check(gpu_lib().jn_transform_profile(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def block(self, block_id):
+        import numpy as np
+        L = gpu_lib()
+        n = ctypes.c_size_t()
+        _check(L.jn_transform_elements(self._h, block_id, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(L.jn_transform_elements(self._h, block_id, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n)))
+        return out
+
+    def write(self, output_dir):
+        _check(gpu_lib().jn_transform_write(self._h, output_dir.encode()))
+
+    def stats(self):
+        s = TransformStats()
+        _check(gpu_lib().jn_transform_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in TransformStats._fields_}
+
+    def close(self):
+        if self._h:
+            gpu_lib().jn_transform_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def transform_2nf(comb, index_list_dir, output_dir, Z, N, single_particle_energy, two_particle_energy, antoine_file,
+                  include_kinetic=True):
+    """The two-body part of mercury_J_scheme_to_internal.x: writes <output_dir>/<id>_matrix_elements."""
+    _check(gpu_lib().jn_transform_2nf(comb.encode(), index_list_dir.encode(), output_dir.encode(), Z, N,
+                                      single_particle_energy, two_particle_energy, antoine_file.encode(),
+                                      int(include_kinetic)))
+
+
+def transform_status(comb, index_list_dir, Z, N, single_particle_energy, two_particle_energy, antoine_file,
+                     include_kinetic=True):
+    """(status, message) of jn_transform_open without raising: host-side validation is
+    reported before any device is touched."""
+    L = gpu_lib()
+    h = ctypes.c_void_p()
+    st = L.jn_transform_open(comb.encode(), index_list_dir.encode(), Z, N, single_particle_energy,
+                             two_particle_energy, antoine_file.encode(), int(include_kinetic), ctypes.byref(h))
+    msg = L.jn_last_error().decode(errors="replace") if st else ""
+    if h.value:
+        L.jn_transform_close(h)
+    return st, msg
+
+
+def clebsch_gordan(j1, j2, j3, m1, m2, m3):
+    """<j1 m1 j2 m2 | j3 m3>, arguments doubled (host computation, no GPU)."""
+    return gpu_lib().jn_clebsch_gordan(j1, j2, j3, m1, m2, m3)
+
+
 def inspect(d, Z, N):
     """Plan statistics of a problem directory, computed on the host (no GPU)."""
     s = PlanStats()
@@ -240,7 +344,7 @@ class GenConfig(ctypes.Structure):
                 ("parity", ctypes.c_int), ("nbody", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("hbar_omega", ctypes.c_double), ("sigma2", ctypes.c_double), ("sigma3", ctypes.c_double),
                 ("me_only", ctypes.c_int), ("me_subdir", ctypes.c_char_p), ("write_basis_files", ctypes.c_int),
-                ("lanczos_iterations", ctypes.c_int)]
+                ("lanczos_iterations", ctypes.c_int), ("antoine", ctypes.c_int)]
 
 
 class GenSummary(ctypes.Structure):
@@ -248,7 +352,8 @@ class GenSummary(ctypes.Structure):
                 ("list_entries", ctypes.c_size_t), ("num_me_blocks", ctypes.c_size_t),
                 ("me_elements", ctypes.c_size_t), ("num_calc_blocks", ctypes.c_size_t),
                 ("multiplications", ctypes.c_ulonglong), ("num_orbitals", ctypes.c_int),
-                ("num_proton_sds", ctypes.c_int), ("num_neutron_sds", ctypes.c_int)]
+                ("num_proton_sds", ctypes.c_int), ("num_neutron_sds", ctypes.c_int),
+                ("emax_single", ctypes.c_int), ("emax_pair", ctypes.c_int)]
 
 
 _gen = None
@@ -265,12 +370,18 @@ def gen_lib():
         _gen.jn_gen_default_config.argtypes = [ctypes.POINTER(GenConfig)]
         _gen.jn_gen_pair_normal.restype = ctypes.c_double
         _gen.jn_gen_pair_normal.argtypes = [ctypes.c_uint64] * 4
+        _gen.jn_gen_antoine.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_uint64, ctypes.c_double]
     return _gen
 
 
 def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, hbar_omega=20.0, sigma2=1.0,
-             sigma3=0.1, me_only_subdir=None, basis_files=True, lanczos_iterations=200):
-    """Write a synthetic problem in the reference formats; returns the generator summary."""
+             sigma3=0.1, me_only_subdir=None, basis_files=True, lanczos_iterations=200, antoine=False):
+    """Write a synthetic problem in the reference formats; returns the generator summary.
+
+    With antoine=True the two-body interaction is written as a J-scheme
+    Antoine file (antoine_2nf.bin) and its M-scheme blocks are left to the
+    J->M transform."""
     G = gen_lib()
     c = GenConfig()
     G.jn_gen_default_config(ctypes.byref(c))
@@ -278,6 +389,7 @@ def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, h
     c.seed, c.hbar_omega, c.sigma2, c.sigma3 = seed, hbar_omega, sigma2, sigma3
     c.write_basis_files = int(basis_files)
     c.lanczos_iterations = lanczos_iterations
+    c.antoine = int(antoine)
     if me_only_subdir:
         c.me_only = 1
         c.me_subdir = me_only_subdir.encode()
@@ -286,3 +398,11 @@ def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, h
     if rc != 0:
         raise JnError(rc, G.jn_gen_last_error().decode())
     return {k: getattr(s, k) for k, _ in GenSummary._fields_}
+
+
+def write_antoine(path, emax1, emax2, num_particles, hbar_omega=20.0, seed=20261203, sigma=1.0):
+    """Write a seeded J-scheme two-body interaction in the Antoine format."""
+    G = gen_lib()
+    rc = G.jn_gen_antoine(path.encode(), emax1, emax2, num_particles, hbar_omega, seed, sigma)
+    if rc != 0:
+        raise JnError(rc, G.jn_gen_last_error().decode())

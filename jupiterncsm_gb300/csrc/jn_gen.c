@@ -63,6 +63,7 @@
  * diagonal two-body elements as hw (e_a + e_b)/(A-1).
  */
 #include "jn_gen.h"
+#include "jn_jt.h"
 
 #include <errno.h>
 #include <math.h>
@@ -1031,6 +1032,48 @@ static int cmp_calc_order(const void *a, const void *b)
 	return x->ln - y->ln;
 }
 
+static int fwrite_record(FILE *f, const void *data, int nbytes)
+{
+	return fwrite(&nbytes, 4, 1, f) != 1 || (nbytes && fwrite(data, (size_t)nbytes, 1, f) != 1) ||
+	       fwrite(&nbytes, 4, 1, f) != 1;
+}
+
+int jn_gen_antoine(const char *path, int emax1, int emax2, int num_particles, double hbar_omega, uint64_t seed,
+		   double sigma)
+{
+	if (num_particles < 2) FAIL(JN_GEN_EINVAL, "the Antoine kinetic column needs A >= 2 (A = %d)", num_particles);
+	jn_jt_basis_t B;
+	if (jn_jt_basis_build(emax1, emax2, &B)) FAIL(JN_GEN_EINVAL, "invalid JT basis emax1=%d emax2=%d", emax1, emax2);
+	if (B.nconfig > 0x7fffffff / 24) { jn_jt_basis_free(&B); FAIL(JN_GEN_EINVAL, "too many configurations"); }
+	const int ncol = 6;
+	float *rows = xcalloc((size_t)B.nconfig * ncol, sizeof(float));
+	const double A = num_particles;
+	for (int i = 0; i < B.n; i++)
+		for (int k = i; k < B.cfg_end[i]; k++) {
+			float *r = rows + (size_t)jn_jt_config(&B, i, k) * ncol;
+			if (i == k) {
+				int E = B.shells[B.st[i].a].e + B.shells[B.st[i].b].e;
+				r[0] = (float)(A * E / (2.0 * (A - 1.0)));
+			}
+			for (int c = 3; c < 6; c++) r[c] = (float)(sigma * jn_gen_pair_normal(seed, (uint64_t)c, i, k));
+		}
+	FILE *f = fopen(path, "wb");
+	int rc = 0;
+	if (!f) { rc = JN_GEN_EIO; snprintf(g_err, sizeof g_err, "open %s: %s", path, strerror(errno)); }
+	else {
+		struct { int ncol; float hw; int nrow; } hdr = { ncol, (float)hbar_omega, (int)B.nconfig };
+		int title[2] = { emax1, emax2 };
+		if (fwrite_record(f, title, sizeof title) || fwrite_record(f, &hdr, sizeof hdr) ||
+		    fwrite_record(f, rows, (int)(B.nconfig * ncol * sizeof(float)))) {
+			rc = JN_GEN_EIO; snprintf(g_err, sizeof g_err, "write %s", path);
+		}
+		if (fclose(f) && !rc) { rc = JN_GEN_EIO; snprintf(g_err, sizeof g_err, "close %s", path); }
+	}
+	free(rows);
+	jn_jt_basis_free(&B);
+	return rc;
+}
+
 int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *summary)
 {
 	gen_t G; memset(&G, 0, sizeof G);
@@ -1105,13 +1148,22 @@ int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *su
 		if (mkdir_p(path)) { rc = JN_GEN_EIO; snprintf(g_err, sizeof g_err, "mkdir %s", path); goto done; }
 		for (size_t i = 0; i < g->mes.n; i++) {
 			if (!M[i].id) continue;
+			if (cfg->antoine && M[i].kp + M[i].kn == 2) continue;   /* left to the J->M transform */
 			double sigma = (M[i].kp + M[i].kn == 3) ? cfg->sigma3 : cfg->sigma2;
 			uint64_t seed = cfg->seed * 1000003ull + (M[i].kp + M[i].kn);
 			if ((rc = write_me_block(g, &M[i], path, seed, sigma, cfg->hbar_omega != 0.0))) goto done;
 		}
 	}
+	if (cfg->antoine) {
+		snprintf(path, sizeof path, "%s/antoine_2nf.bin", outdir);
+		if ((rc = jn_gen_antoine(path, emax, Etot, cfg->Z + cfg->N, cfg->hbar_omega, cfg->seed * 1000003ull + 2,
+					 cfg->sigma2)))
+			goto done;
+	}
 	if (summary) {
 		memset(summary, 0, sizeof *summary);
+		summary->emax_single = emax;
+		summary->emax_pair = Etot;
 		summary->num_basis_blocks = g->nb;
 		for (int b = 0; b < g->nb; b++) summary->dimension += g->bb[b].np_ * g->bb[b].nn_;
 		for (size_t i = 0; i < g->lists.n; i++) if (L[i].len) { summary->num_lists++; summary->list_entries += L[i].len; }
@@ -1145,7 +1197,8 @@ static void usage(const char *p)
 {
 	fprintf(stderr,
 		"usage: %s --out DIR [--Z n] [--N n] [--nmax n] [--M2 n] [--parity 0|1] [--nbody 2|3]\n"
-		"          [--seed s] [--hw MeV] [--sigma2 s] [--sigma3 s] [--me-only SUBDIR] [--no-basis-files]\n", p);
+		"          [--seed s] [--hw MeV] [--sigma2 s] [--sigma3 s] [--me-only SUBDIR] [--no-basis-files]\n"
+		"          [--antoine]\n", p);
 }
 int main(int argc, char **argv)
 {
@@ -1167,15 +1220,17 @@ int main(int argc, char **argv)
 		else if (!strcmp(a, "--sigma3") && v) { c.sigma3 = atof(v); i++; }
 		else if (!strcmp(a, "--me-only") && v) { c.me_only = 1; c.me_subdir = v; i++; }
 		else if (!strcmp(a, "--no-basis-files")) c.write_basis_files = 0;
+		else if (!strcmp(a, "--antoine")) c.antoine = 1;
 		else { usage(argv[0]); return 2; }
 	}
 	if (!out) { usage(argv[0]); return 2; }
 	jn_gen_summary s;
 	int rc = jn_generate(&c, out, &s);
 	if (rc) { fprintf(stderr, "jn_gen: %s\n", jn_gen_last_error()); return 1; }
-	printf("dimension %zu blocks %d lists %zu entries %zu me_blocks %zu me_elements %zu calc_blocks %zu mults %llu\n",
+	printf("dimension %zu blocks %d lists %zu entries %zu me_blocks %zu me_elements %zu calc_blocks %zu mults %llu"
+	       " emax_single %d emax_pair %d\n",
 	       s.dimension, s.num_basis_blocks, s.num_lists, s.list_entries, s.num_me_blocks, s.me_elements,
-	       s.num_calc_blocks, (unsigned long long)s.multiplications);
+	       s.num_calc_blocks, (unsigned long long)s.multiplications, s.emax_single, s.emax_pair);
 	return 0;
 }
 #endif

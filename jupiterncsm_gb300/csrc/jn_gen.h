@@ -32,6 +32,9 @@ typedef struct {
 	const char *me_subdir;  /* default "matrix_elements" */
 	int write_basis_files;  /* Anicre basis_energy_<E> files under anicr/ */
 	int lanczos_iterations; /* written into bacchus.conf */
+	int antoine;            /* two-body interaction as a J-scheme Antoine file (antoine_2nf.bin)
+				   instead of M-scheme blocks: the two-body matrix-element blocks are
+				   then left to the J->M transform */
 } jn_gen_config;
 
 typedef struct {
@@ -42,11 +45,27 @@ typedef struct {
 	size_t num_calc_blocks;
 	unsigned long long multiplications;
 	int num_orbitals, num_proton_sds, num_neutron_sds;
+	int emax_single, emax_pair;     /* largest orbital and pair energies (the transform's
+					   --single-particle-energy and --two-particle-energy) */
 } jn_gen_summary;
 
 void jn_gen_default_config(jn_gen_config *cfg);
 int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *summary);
 const char *jn_gen_last_error(void);
+/*
+ * Write a seeded two-body interaction in the Antoine J-scheme format that
+ * Mercury reads (src/Neptune/input/read_2nf_antoine_format.c:13-257): three
+ * Fortran unformatted records, a title, the header {int ncol; float hw;
+ * int nrow} and float[nrow][ncol], one row per configuration of the JT basis
+ * built with (emax1, emax2).  Columns 3, 4 and 5 (Tz = -2, +2, 0) are
+ * sigma * N(0,1) deviates keyed by the configuration; column 0 is the
+ * coefficient k with 2 hw k / A = hw (e_a + e_b) / (A - 1) on diagonal
+ * configurations and 0 elsewhere, so that the transformed interaction
+ * carries the oscillator term hw * (number of quanta).  Columns 1 and 2 are 0.
+ */
+int jn_gen_antoine(const char *path, int emax1, int emax2, int num_particles, double hbar_omega, uint64_t seed,
+		   double sigma);
+
 /* the seeded N(0,1) deviate attached to the unordered pair {ka, kb} */
 double jn_gen_pair_normal(uint64_t seed, uint64_t tag, uint64_t ka, uint64_t kb);
 

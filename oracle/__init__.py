@@ -10,6 +10,12 @@ being measured or shipped.
                  _ref/libref_minerva.so when the reference tree is present
 * ``dense_h``    independent second-quantisation dense Hamiltonian
 * ``index_lists`` Python restatement of index-list construction
+* ``jt_transform`` Python restatement of the coupled basis, exact
+                 Clebsch-Gordan coefficients and the Antoine file layout
+* ``reference_transform``  the reference's own two-body J -> M transform,
+                 compiled unchanged into _ref/ref_mercury (with a stand-in
+                 for the absent wigxjpf library) when the reference tree is
+                 present
 """
 import ctypes
 import os
@@ -20,6 +26,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libminerva_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_minerva.so")
+REF_MERCURY = os.path.join(HERE, "_ref", "ref_mercury")
 
 
 def build():
@@ -28,6 +35,25 @@ def build():
 
 def reference_available():
     return os.path.exists(REF_LIB)
+
+
+def reference_transform_available():
+    return os.path.exists(REF_MERCURY)
+
+
+def reference_transform(comb, index_list_dir, output_dir, Z, N, e1, e2, antoine, include_kinetic=True):
+    """Run the reference's two-body transform; returns its wall time in seconds."""
+    os.makedirs(output_dir, exist_ok=True)
+    r = subprocess.run([REF_MERCURY, comb, index_list_dir, output_dir, str(Z), str(N), str(e1), str(e2), antoine,
+                        "0" if include_kinetic else "1"], capture_output=True, text=True, check=True)
+    return float(r.stdout.split()[-1])
+
+
+def read_me_file(path):
+    """(n_dim, p_dim, elements) of a <id>_matrix_elements file."""
+    raw = open(path, "rb").read()
+    nd_n, nd_p = np.frombuffer(raw[:16], dtype=np.uint64)
+    return int(nd_n), int(nd_p), np.frombuffer(raw[16:], dtype=np.float64).copy()
 
 
 class Port:

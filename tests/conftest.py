@@ -23,12 +23,9 @@ def _ensure_built():
         subprocess.run(["make", "-s", "-C", oracle.HERE, "port"], check=True)
     if os.path.isdir("/root/reference/src") and not os.path.exists(oracle.REF_LIB):
         subprocess.run(["make", "-s", "-C", oracle.HERE, "ref"], check=True)
-    emu = os.path.join(ROOT, "tests", "_build", "libplan_emu.so")
-    if not os.path.exists(emu):
-        os.makedirs(os.path.dirname(emu), exist_ok=True)
-        subprocess.run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-o", emu,
-                        os.path.join(ROOT, "tests", "native", "plan_emulator.c"),
-                        os.path.join(ROOT, "jupiterncsm_gb300", "csrc", "jn_problem.c"), "-lm"], check=True)
+    if os.path.isdir("/root/reference/src") and not os.path.exists(oracle.REF_MERCURY):
+        subprocess.run(["make", "-s", "-C", oracle.HERE, "ref"], check=True)
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "tests", "native")], check=True)
 
 
 _ensure_built()
@@ -63,6 +60,32 @@ def problem(problem_root):
             jn.generate(d, Z=Z, N=N, nmax=nmax, nbody=nbody, M2=M2, basis_files=False)
             _cache[name] = (d, Z, N, nmax, nbody)
         return _cache[name]
+    return get
+
+
+# J-scheme problems for the transform: name -> (Z, N, Nmax, 2M)
+TRANSFORM_PROBLEMS = {
+    "he4_n2": (2, 2, 2, 0),
+    "li6_n2": (3, 3, 2, 2),
+    "he4_n4": (2, 2, 4, 0),
+    "li6_n4": (3, 3, 4, 2),
+}
+_tcache = {}
+
+
+@pytest.fixture(scope="session")
+def jproblem(problem_root):
+    """jproblem(name) -> (directory, Z, N, emax_single, emax_pair): a generated
+    problem whose two-body interaction is an Antoine J-scheme file."""
+    import jupiterncsm_gb300 as jn
+
+    def get(name):
+        if name not in _tcache:
+            Z, N, nmax, M2 = TRANSFORM_PROBLEMS[name]
+            d = str(problem_root / ("j_" + name))
+            s = jn.generate(d, Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, antoine=True)
+            _tcache[name] = (d, Z, N, s["emax_single"], s["emax_pair"])
+        return _tcache[name]
     return get
 
 
