@@ -185,6 +185,57 @@ def prepare(workload, workdir):
     return d
 
 
+TRANSFORM_WORKLOAD = dict(Z=3, N=3, nmax=6, M2=2,
+                          label="6Li (Z=3,N=3) Nmax=6, 2M=2: seeded J-scheme 2NF N(0,1) MeV (Antoine format) -> "
+                                "all two-body M-scheme blocks of the combination table")
+
+
+def transform_leg(workdir, steps, warmup, flush, peak):
+    """The J -> M two-body transform on the GPU: one kernel computes every
+    two-body block; timed with CUDA events, L2 flushed between runs."""
+    import torch
+    import jupiterncsm_gb300 as jn
+    w = TRANSFORM_WORKLOAD
+    d = os.path.join(workdir, "li6_nmax6_jscheme")
+    stamp = os.path.join(d, ".complete")
+    if not os.path.exists(stamp):
+        t = time.time()
+        s = jn.generate(d, Z=w["Z"], N=w["N"], nmax=w["nmax"], M2=w["M2"], nbody=2, antoine=True)
+        open(stamp, "w").write(f"{s['emax_single']} {s['emax_pair']}\n")
+        log(f"generated the J-scheme workload in {time.time() - t:.1f} s")
+    e1, e2 = (int(v) for v in open(stamp).read().split())
+    t0 = time.perf_counter()
+    T = jn.Transform.from_dir(d, w["Z"], w["N"], e1, e2)
+    open_s = time.perf_counter() - t0
+    st = T.stats()
+    for _ in range(warmup):
+        T.profile()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(T.profile())
+    T.close()
+    kms = sum(ms) / len(ms)
+    # the drop-in call end to end: plan, upload, kernel, copy back, files written
+    out = os.path.join(d, "transformed")
+    t0 = time.perf_counter()
+    jn.transform_2nf(os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), out, w["Z"], w["N"], e1, e2,
+                     os.path.join(d, "antoine_2nf.bin"))
+    e2e_s = time.perf_counter() - t0
+    achieved = st["algorithmic_bytes"] / (kms / 1e3) / 1e9
+    return {"workload": w["label"], "elements": st["num_elements"], "two_body_blocks": st["num_two_body_blocks"],
+            "pair_states": st["num_pair_states"], "configurations": st["num_configurations"],
+            "kernel_ms": kms, "elements_per_s": st["num_elements"] / (kms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "bytes_per_run": st["algorithmic_bytes"], "kernel": "jn_jt_to_m_kernel"},
+            "dense_equivalent_flops": st["dense_flops"],
+            "dense_equivalent_tflop_per_s": st["dense_flops"] / (kms / 1e3) / 1e12,
+            "plan_seconds": st["plan_seconds"], "open_seconds": open_s,
+            "e2e": {"seconds": e2e_s, "what": "jn_transform_2nf: plan + upload + kernel + copy back + files"},
+            "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
+
+
 def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
     """The reference's CPU algorithm on all host threads over a time-bounded sample."""
     import numpy as np
@@ -229,6 +280,7 @@ def main():
     ap.add_argument("--workdir", default=os.environ.get("JNCSM_BENCH_DIR", os.path.join(tempfile.gettempdir(), "jncsm_bench")))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -368,6 +420,11 @@ def main():
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
                          "kernel": "jn_tile_kernel<double>" if prec == 64 else "jn_tile_kernel<float>"},
             "clocks": main_r["clocks"]}
+    if rank == 0 and not args.no_transform:
+        try:
+            line["transform"] = transform_leg(wd, args.steps, args.warmup, flush, peak)
+        except Exception as e:  # the transform leg must never hide the matvec line
+            line["transform"] = {"error": str(e)}
     if rank == 0:
         try:
             line["cpu_baseline"] = cpu_baseline(d, w, bytes_for(64), seconds=args.cpu_seconds)
