@@ -236,6 +236,78 @@ def transform_leg(workdir, steps, warmup, flush, peak):
             "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
 
 
+SOLVE_FAMILY = [  # (label, Z, N, Nmax, 2M): the bases of the batched-Hamiltonian workload
+    ("4He Nmax=2", 2, 2, 2, 0), ("4He Nmax=4", 2, 2, 4, 0), ("4He Nmax=6", 2, 2, 6, 0), ("6Li Nmax=4", 3, 3, 4, 2)]
+SOLVE_INSTANCES = 64
+SOLVE_COUPLINGS = 4
+
+
+def solves_leg(workdir, seed=20261203):
+    """Lanczos solves/s: 64 Hamiltonians H(c) = H0 + sum_{i=1..4} c_i H_i, c_i ~ U(-1,1),
+    16 on each of four bases, to 1e-6 MeV on the 10 lowest eigenvalues.
+    Plain: one FP64 Lanczos (full reorthogonalisation, FP64 products) after
+    another.  Batched: one call per basis, all its instances together, FP32
+    products, FP64 recurrence and FP64 Rayleigh-Ritz refinement, one captured
+    CUDA graph per step.  Both start from the same vector; the error of every
+    batched eigenvalue is measured against the plain FP64 solve."""
+    import numpy as np
+    import jupiterncsm_gb300 as jn
+    rng = np.random.default_rng(seed)
+    per = SOLVE_INSTANCES // len(SOLVE_FAMILY)
+    plain_s = batch_s = 0.0
+    worst = 0.0
+    iters_plain, iters_batch = [], []
+    details = []
+    for bi, (label, Z, N, nmax, M2) in enumerate(SOLVE_FAMILY):
+        d = os.path.join(workdir, f"family_{Z}_{N}_{nmax}_{M2}")
+        stamp = os.path.join(d, ".complete")
+        if not os.path.exists(stamp):
+            jn.generate(os.path.join(d, "h0"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, basis_files=False)
+            for i in range(1, SOLVE_COUPLINGS + 1):
+                jn.generate(os.path.join(d, f"h{i}"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, seed=seed + 1000 * i,
+                            hbar_omega=0.0, basis_files=False)
+            open(stamp, "w").write("ok\n")
+        H = jn.Hamiltonian.from_dir(os.path.join(d, "h0"), Z, N)
+        comps = [H.read_matrix_elements(os.path.join(d, f"h{i}", "matrix_elements"))
+                 for i in range(SOLVE_COUPLINGS + 1)]
+        cs = rng.uniform(-1.0, 1.0, size=(per, SOLVE_COUPLINGS))
+        mes = [comps[0] + sum(c[i] * comps[i + 1] for i in range(SOLVE_COUPLINGS)) for c in cs]
+        start = np.random.default_rng(seed + bi).standard_normal(H.dimension)
+        # plain FP64, sequential
+        plain = []
+        t0 = time.perf_counter()
+        for me in mes:
+            H.set_matrix_elements(me)
+            plain.append(H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, start_vector=start,
+                                   allow_unconverged=True))
+        t1 = time.perf_counter()
+        # batched mixed precision
+        res = H.lanczos_batch(mes, start_vectors=[start] * per, max_iterations=300, num_eigenvalues=10,
+                              tolerance=1e-6, precision=32, check_every=10, use_graph=True)
+        t2 = time.perf_counter()
+        H.close()
+        plain_s += t1 - t0
+        batch_s += t2 - t1
+        err = max(float(np.abs(r["eigenvalues"] - p["eigenvalues"]).max()) for r, p in zip(res, plain))
+        worst = max(worst, err)
+        iters_plain += [p["iterations"] for p in plain]
+        iters_batch += [r["iterations"] for r in res]
+        details.append({"basis": label, "dimension": int(len(start)), "instances": per,
+                        "plain_s": t1 - t0, "batched_s": t2 - t1, "max_eigenvalue_diff_MeV": err,
+                        "all_converged": all(r["converged"] for r in res) and all(p["converged"] for p in plain)})
+    return {"metric": "Lanczos solves/s at 1e-6 MeV (10 lowest) vs plain FP64",
+            "workload": f"{SOLVE_INSTANCES} H(c)=H0+sum_{{i=1..{SOLVE_COUPLINGS}}} c_i H_i, c~U(-1,1), "
+                        f"{per} on each of " + ", ".join(f[0] for f in SOLVE_FAMILY) + " (two-body, seeded)",
+            "batched_solves_per_s": SOLVE_INSTANCES / batch_s, "plain_fp64_solves_per_s": SOLVE_INSTANCES / plain_s,
+            "speedup": plain_s / batch_s, "batched_seconds": batch_s, "plain_seconds": plain_s,
+            "max_eigenvalue_diff_vs_plain_fp64_MeV": worst,
+            "mean_iterations": {"plain": float(np.mean(iters_plain)), "batched": float(np.mean(iters_batch))},
+            "batched": "FP32 products, FP64 recurrence + full reorthogonalisation + Rayleigh-Ritz refinement, "
+                       "CUDA graph per step, convergence checked every 10 steps",
+            "plain": "jn_lanczos full mode, FP64 products, convergence checked every step",
+            "per_basis": details}
+
+
 def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
     """The reference's CPU algorithm on all host threads over a time-bounded sample."""
     import numpy as np
@@ -281,6 +353,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
     ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
+    ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solves/s leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -425,6 +498,11 @@ def main():
             line["transform"] = transform_leg(wd, args.steps, args.warmup, flush, peak)
         except Exception as e:  # the transform leg must never hide the matvec line
             line["transform"] = {"error": str(e)}
+    if rank == 0 and not args.no_solves:
+        try:
+            line["solves"] = solves_leg(wd)
+        except Exception as e:  # the solves leg must never hide the matvec line
+            line["solves"] = {"error": str(e)}
     if rank == 0:
         try:
             line["cpu_baseline"] = cpu_baseline(d, w, bytes_for(64), seconds=args.cpu_seconds)

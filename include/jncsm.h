@@ -234,6 +234,61 @@ jn_status jn_lanczos_save_eigenvectors(jn_ctx *ctx, const char *directory, int c
 void jn_print_eigensystem(const double *eigenvalues, int count);
 
 /* ------------------------------------------------------------------ */
+/* Other matrix elements on the same lists: H(c) = H0 + sum_i c_i H_i   */
+/* ------------------------------------------------------------------ */
+/* Number of matrix elements of the context (all blocks, plan layout). */
+size_t jn_me_count(const jn_ctx *ctx);
+
+/* Read the <id>_matrix_elements files of another directory (same
+ * combination table, e.g. another operator H_i) into out, jn_me_count
+ * values in the context's layout (host only).  The reference reads its
+ * blocks with new_matrix_block (Minerva/matrix_block/matrix_block.c:22-62). */
+jn_status jn_read_matrix_elements(const jn_ctx *ctx, const char *matrix_file_base_directory, double *out);
+
+/* Replace the context's matrix elements (host array in the same layout);
+ * the lists, the plan and the vectors stay.  No counterpart in the
+ * reference, which reads its matrix elements from disk for every product. */
+jn_status jn_set_matrix_elements(jn_ctx *ctx, const double *matrix_elements);
+
+/*
+ * Batched Lanczos: num_instances Hamiltonians on the context's lists, each
+ * with its own matrix elements, solved together (one launch per kernel for
+ * all instances, one captured CUDA graph per Lanczos step).  Each instance
+ * runs the single solve's full mode: full reorthogonalisation, converged
+ * when min(r, r^2/gap) < tolerance for each of the num_eigenvalues lowest
+ * Ritz values (Bacchus/lanczos/lanczos.c:74-253 is the single-instance
+ * algorithm it extends).  precision 32: FP32 matrix elements and vectors in
+ * the products (exact fixed-point sums), FP64 everywhere else; the results
+ * are refined by FP64 products of the lowest num_eigenvalues + refine_extra
+ * Ritz vectors and an FP64 Rayleigh-Ritz solve.  No counterpart in the
+ * reference.
+ */
+typedef struct {
+	int num_instances;
+	const double *const *matrix_elements;   /* host, num_instances arrays of jn_me_count values */
+	const double *const *start_vectors;     /* host, NULL or num_instances vectors (NULL entries: default) */
+	int max_iterations;
+	int num_eigenvalues;                    /* <= JN_MAX_REPORTED */
+	double tolerance;                       /* MeV */
+	int precision;                          /* 32 or 64 */
+	int check_every;                        /* convergence test interval in steps (default 10) */
+	int use_graph;                          /* replay one captured graph per step */
+	int refine_extra;                       /* extra Ritz vectors in the refinement (default 4) */
+	double *const *ground_states;           /* host, NULL or num_instances outputs of length D */
+} jn_batch_options;
+
+typedef struct {
+	int iterations;
+	int converged;
+	int num_eigenvalues;
+	double eigenvalues[JN_MAX_REPORTED];    /* refined, FP64 Rayleigh-Ritz */
+	double ritz_values[JN_MAX_REPORTED];    /* of the solve's own (FP32 or FP64) operator */
+	double residual_norms[JN_MAX_REPORTED]; /* |H x - e x| / |x| of the refined vectors, FP64 H */
+} jn_batch_result;
+
+jn_status jn_lanczos_batch(jn_ctx *ctx, const jn_batch_options *options, jn_batch_result *results);
+
+/* ------------------------------------------------------------------ */
 /* J-scheme -> M-scheme two-body transform (Mercury)                   */
 /* ------------------------------------------------------------------ */
 typedef struct jn_transform jn_transform;

@@ -50,15 +50,29 @@ class PlanStats(ctypes.Structure):
                 ("num_work_units", ctypes.c_int), ("num_tiles", ctypes.c_int)]
 
 
+MAX_REPORTED = 64
+LANCZOS_FULL, LANCZOS_REFERENCE = 0, 1
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("num_instances", ctypes.c_int), ("matrix_elements", ctypes.c_void_p),
+                ("start_vectors", ctypes.c_void_p), ("max_iterations", ctypes.c_int),
+                ("num_eigenvalues", ctypes.c_int), ("tolerance", ctypes.c_double), ("precision", ctypes.c_int),
+                ("check_every", ctypes.c_int), ("use_graph", ctypes.c_int), ("refine_extra", ctypes.c_int),
+                ("ground_states", ctypes.c_void_p)]
+
+
+class BatchResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("num_eigenvalues", ctypes.c_int),
+                ("eigenvalues", ctypes.c_double * MAX_REPORTED), ("ritz_values", ctypes.c_double * MAX_REPORTED),
+                ("residual_norms", ctypes.c_double * MAX_REPORTED)]
+
+
 class TransformStats(ctypes.Structure):
     _fields_ = [("num_two_body_blocks", ctypes.c_int), ("num_one_body_blocks", ctypes.c_int),
                 ("num_elements", ctypes.c_size_t), ("num_pair_states", ctypes.c_size_t),
                 ("num_configurations", ctypes.c_size_t), ("dense_flops", ctypes.c_double),
                 ("algorithmic_bytes", ctypes.c_double), ("plan_seconds", ctypes.c_double)]
-
-
-MAX_REPORTED = 64
-LANCZOS_FULL, LANCZOS_REFERENCE = 0, 1
 
 
 class LanczosOptions(ctypes.Structure):
@@ -110,6 +124,11 @@ def gpu_lib():
     L.jn_lanczos_save_eigenvectors.argtypes = [vp, cp, ci]
     L.jn_print_eigensystem.argtypes = [ctypes.POINTER(ctypes.c_double), ci]
     L.jn_print_eigensystem.restype = None
+    L.jn_me_count.argtypes = [vp]
+    L.jn_me_count.restype = ctypes.c_size_t
+    L.jn_read_matrix_elements.argtypes = [vp, cp, vp]
+    L.jn_set_matrix_elements.argtypes = [vp, vp]
+    L.jn_lanczos_batch.argtypes = [vp, ctypes.POINTER(BatchOptions), vp]
     L.jn_transform_open.argtypes = [cp, cp, ci, ci, ci, ci, cp, ci, ctypes.POINTER(vp)]
     L.jn_transform_run.argtypes = [vp, vp]
     L.jn_transform_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
@@ -125,7 +144,8 @@ def gpu_lib():
                  "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_set_engine", "jn_lanczos",
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
                  "jn_transform_open", "jn_transform_run", "jn_transform_profile", "jn_transform_elements",
-                 "jn_transform_write", "jn_transform_get_stats", "jn_transform_2nf"):
+                 "jn_transform_write", "jn_transform_get_stats", "jn_transform_2nf", "jn_read_matrix_elements",
+                 "jn_set_matrix_elements", "jn_lanczos_batch"):
         getattr(L, name).restype = ci
     _gpu = L
     return L
@@ -207,6 +227,50 @@ class Hamiltonian:
         return {"iterations": r.iterations, "converged": bool(r.converged), "num_ritz_values": r.num_ritz_values,
                 "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
                 "residual_norms": np.array(r.residual_norms[:n]), "status": st}
+
+    def me_count(self):
+        return int(gpu_lib().jn_me_count(self._h))
+
+    def read_matrix_elements(self, directory):
+        """Matrix elements of another directory with the same combination table (host array)."""
+        out = np.zeros(self.me_count())
+        _check(gpu_lib().jn_read_matrix_elements(self._h, directory.encode(), out.ctypes.data))
+        return out
+
+    def set_matrix_elements(self, me):
+        me = np.ascontiguousarray(me, dtype=np.float64)
+        assert me.shape == (self.me_count(),)
+        _check(gpu_lib().jn_set_matrix_elements(self._h, me.ctypes.data))
+
+    def lanczos_batch(self, matrix_elements, start_vectors=None, max_iterations=200, num_eigenvalues=10,
+                      tolerance=1e-6, precision=32, check_every=10, use_graph=True, refine_extra=4,
+                      ground_states=False):
+        """Solve len(matrix_elements) Hamiltonians on these lists together; returns a list of dicts
+        (and the ground-state vectors when ground_states)."""
+        B = len(matrix_elements)
+        mes = [np.ascontiguousarray(m, dtype=np.float64) for m in matrix_elements]
+        me_ptrs = (ctypes.c_void_p * B)(*[m.ctypes.data for m in mes])
+        o = BatchOptions(B, ctypes.cast(me_ptrs, ctypes.c_void_p), None, max_iterations, num_eigenvalues, tolerance,
+                         precision, check_every, int(use_graph), refine_extra, None)
+        svs = None
+        if start_vectors is not None:
+            svs = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in start_vectors]
+            sv_ptrs = (ctypes.c_void_p * B)(*[None if v is None else v.ctypes.data for v in svs])
+            o.start_vectors = ctypes.cast(sv_ptrs, ctypes.c_void_p)
+        gs = None
+        if ground_states:
+            gs = [np.zeros(self.dimension) for _ in range(B)]
+            gs_ptrs = (ctypes.c_void_p * B)(*[g.ctypes.data for g in gs])
+            o.ground_states = ctypes.cast(gs_ptrs, ctypes.c_void_p)
+        res = (BatchResult * B)()
+        _check(gpu_lib().jn_lanczos_batch(self._h, ctypes.byref(o), res))
+        out = []
+        for r in res:
+            n = r.num_eigenvalues
+            out.append({"iterations": r.iterations, "converged": bool(r.converged),
+                        "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
+                        "residual_norms": np.array(r.residual_norms[:n])})
+        return (out, gs) if ground_states else out
 
     def ritz_values(self):
         cap = 4096

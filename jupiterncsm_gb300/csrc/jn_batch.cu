@@ -1,0 +1,711 @@
+/*
+ * jn_batch.cu — many Hamiltonians of one basis solved together: batched,
+ * mixed-precision Lanczos with a captured CUDA graph per step.
+ *
+ * The instances share the context's index lists and differ only in their
+ * matrix elements (H(c) = H0 + sum_i c_i H_i keeps the sparsity of the
+ * lists).  Every kernel runs all instances at once, instance = blockIdx.y;
+ * the step index k is read from device memory, so one captured graph of a
+ * Lanczos step is replayed for every step.  An instance that has converged
+ * is frozen (its kernels return at once) while the others go on.
+ *
+ * Arithmetic (precision 32): the products use FP32 copies of the matrix
+ * elements and of v_k with exact fixed-point sums (the block-tile engine);
+ * the three-term recurrence, full reorthogonalisation (classical
+ * Gram-Schmidt, twice), the tridiagonal eigenproblem and the final
+ * refinement are FP64.  Refinement: the lowest r Ritz vectors X of each
+ * instance are multiplied by the FP64 Hamiltonian, and the r x r pencil
+ * (X^T H X, X^T X) is solved in FP64 (Rayleigh-Ritz), which removes the
+ * error of the FP32 operator to second order.  Precision 64 runs the same
+ * solver with FP64 products.
+ *
+ * Reference: one instance of this is Bacchus' Lanczos
+ * (src/Bacchus/lanczos/lanczos.c:74-253) with full reorthogonalisation.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "jn_internal.h"
+#include "jn_tridiag.cuh"
+
+#define BT 256          /* threads of the vector kernels */
+#define BNB 16          /* reduction CTAs per instance */
+
+/* ------------------------------------------------------------------ */
+/* batched vector kernels (instance = blockIdx.y, k = *d_k)            */
+/* ------------------------------------------------------------------ */
+#define SKIP_INACTIVE() \
+	const int inst = blockIdx.y; \
+	if (active && !active[inst]) return
+
+__device__ __forceinline__ void slice(int64_t D, int64_t *i0, int64_t *i1)
+{
+	const int64_t chunk = (D + gridDim.x - 1) / gridDim.x;
+	*i0 = (int64_t)blockIdx.x * chunk;
+	*i1 = min(D, *i0 + chunk);
+}
+
+/* part[inst][blk] = x . y over this CTA's slice; x = X + inst*x_ld (+ k*D when xk) */
+__global__ void __launch_bounds__(BT) kb_dot(const double *__restrict__ X, int64_t x_ld, int xk,
+					      const double *__restrict__ Y, int64_t y_ld, int yk, const int *__restrict__ d_k,
+					      int64_t D, double *__restrict__ part, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	__shared__ double sh[BT];
+	const int k = *d_k;
+	const double *x = X + inst * x_ld + (xk ? (int64_t)k * D : 0);
+	const double *y = Y + inst * y_ld + (yk ? (int64_t)k * D : 0);
+	int64_t i0, i1;
+	slice(D, &i0, &i1);
+	double s = 0.0;
+	for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(x[i], y[i], s);
+	s = jn_block_sum(s, sh);
+	if (threadIdx.x == 0) part[(int64_t)inst * gridDim.x + blockIdx.x] = s;
+}
+
+/* out[inst*out_ld + (k when outk)] = sum of the CTA partials in order */
+__global__ void kb_finish_dot(const double *__restrict__ part, int nblk, double *__restrict__ out, int64_t out_ld,
+			      int outk, const int *__restrict__ d_k, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	if (threadIdx.x) return;
+	double s = 0.0;
+	for (int b = 0; b < nblk; b++) s += part[(int64_t)inst * nblk + b];
+	out[inst * out_ld + (outk ? *d_k : 0)] = s;
+}
+
+/* w -= alpha_k v_k + beta_{k-1} v_{k-1} */
+__global__ void kb_three_term(double *__restrict__ W, const double *__restrict__ V, int64_t ldV,
+			      const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
+			      const int *__restrict__ d_k, int64_t D, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int k = *d_k;
+	const double a = alpha[inst * ldab + k], b = k > 0 ? beta[inst * ldab + k - 1] : 0.0;
+	const double *v = V + inst * ldV + (int64_t)k * D, *u = k > 0 ? v - D : v;
+	double *w = W + inst * D;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double r = w[i] - a * v[i];
+		if (k > 0) r -= b * u[i];
+		w[i] = r;
+	}
+}
+
+/* part[inst][blk][j] = V_j . w over the slice, j <= k */
+__global__ void __launch_bounds__(BT) kb_gemv_t(const double *__restrict__ V, int64_t ldV, const double *__restrict__ W,
+						 const int *__restrict__ d_k, int64_t D, double *__restrict__ part, int ncol,
+						 const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	__shared__ double sh[BT];
+	const int nvec = *d_k + 1;
+	const double *w = W + inst * D;
+	int64_t i0, i1;
+	slice(D, &i0, &i1);
+	for (int j = 0; j < nvec; j++) {
+		const double *v = V + inst * ldV + (int64_t)j * D;
+		double s = 0.0;
+		for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
+		s = jn_block_sum(s, sh);
+		if (threadIdx.x == 0) part[((int64_t)inst * gridDim.x + blockIdx.x) * ncol + j] = s;
+	}
+}
+
+__global__ void kb_finish(const double *__restrict__ part, int nblk, int ncol, const int *__restrict__ d_k,
+			  double *__restrict__ h, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int j = blockIdx.x * blockDim.x + threadIdx.x;
+	if (j > *d_k) return;
+	double s = 0.0;
+	for (int b = 0; b < nblk; b++) s += part[((int64_t)inst * nblk + b) * ncol + j];
+	h[(int64_t)inst * ncol + j] = s;
+}
+
+/* w -= sum_{j<=k} V_j h_j */
+__global__ void kb_gemv_n_sub(const double *__restrict__ V, int64_t ldV, const double *__restrict__ h, int ncol,
+			      const int *__restrict__ d_k, int64_t D, double *__restrict__ W, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int nvec = *d_k + 1;
+	const double *hh = h + (int64_t)inst * ncol, *v = V + inst * ldV;
+	double *w = W + inst * D;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int j = 0; j < nvec; j++) s = fma(v[(int64_t)j * D + i], hh[j], s);
+		w[i] -= s;
+	}
+}
+
+/* v_{k+1} = w / |w|, beta_k = |w| (|w|^2 in nrm2[inst]) */
+__global__ void kb_normalize(double *__restrict__ V, int64_t ldV, const double *__restrict__ W,
+			     const double *__restrict__ nrm2, double *__restrict__ beta, int64_t ldab,
+			     const int *__restrict__ d_k, int64_t D, const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int k = *d_k;
+	const double b = sqrt(nrm2[inst]);
+	if (blockIdx.x == 0 && threadIdx.x == 0) beta[inst * ldab + k] = b;
+	const double inv = b > 0.0 ? 1.0 / b : 0.0;
+	double *v = V + inst * ldV + (int64_t)(k + 1) * D;
+	const double *w = W + inst * D;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		v[i] = w[i] * inv;
+}
+
+/* v_0 /= |v_0| (|v_0|^2 in nrm2[inst]) */
+__global__ void kb_scale_start(double *__restrict__ V, int64_t ldV, const double *__restrict__ nrm2, int64_t D)
+{
+	const int inst = blockIdx.y;
+	const double inv = 1.0 / sqrt(nrm2[inst]);
+	double *v = V + inst * ldV;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		v[i] *= inv;
+}
+
+__global__ void kb_advance(int *d_k) { if (threadIdx.x == 0 && blockIdx.x == 0) *d_k += 1; }
+
+/* ------------------------------------------------------------------ */
+/* batched tridiagonal work (n per instance)                            */
+/* ------------------------------------------------------------------ */
+__global__ void kb_tri_bisect(const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
+			      const int *__restrict__ n_arr, int want, double *__restrict__ theta, int ldt,
+			      const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int n = n_arr[inst];
+	if (i >= want || i >= n) return;
+	theta[(int64_t)inst * ldt + i] = jn_tri_bisect_one(alpha + inst * ldab, beta + inst * ldab, n, i);
+}
+
+__global__ void kb_tri_vectors(const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
+			       const int *__restrict__ n_arr, int want, const double *__restrict__ theta, int ldt,
+			       double *__restrict__ Z, int ldz, double *__restrict__ work, double *__restrict__ zlast,
+			       const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int n = n_arr[inst];
+	if (i >= want || i >= n) return;
+	double *z = Z + ((int64_t)inst * want + i) * ldz;
+	jn_tri_vector_one(alpha + inst * ldab, beta + inst * ldab, n, theta[(int64_t)inst * ldt + i], z,
+			  work + ((int64_t)inst * want + i) * 5 * ldz);
+	if (zlast) zlast[(int64_t)inst * ldt + i] = z[n - 1];
+}
+
+__global__ void kb_tri_mgs(double *__restrict__ Z, int ldz, const int *__restrict__ n_arr, int want,
+			   const int *__restrict__ active)
+{
+	SKIP_INACTIVE();
+	__shared__ double sh[BT];
+	const int n = n_arr[inst];
+	jn_tri_mgs(Z + (int64_t)inst * want * ldz, ldz, n, want < n ? want : n, sh);
+}
+
+/* converged[inst] = every one of the nev lowest Ritz values has
+ * min(r, r^2/gap) < tol, r = |beta_{n-1} z_i[n-1]| (the criterion of the
+ * single solve's full mode); theta holds nev+1 values when n > nev */
+__global__ void kb_converged(const double *__restrict__ theta, const double *__restrict__ zlast, int ldt,
+			     const double *__restrict__ beta, int64_t ldab, const int *__restrict__ n_arr, int nev,
+			     double tol, int *__restrict__ flag, const int *__restrict__ active, int B)
+{
+	const int inst = blockIdx.x * blockDim.x + threadIdx.x;
+	if (inst >= B) return;
+	if (active && !active[inst]) { flag[inst] = 0; return; }
+	const int n = n_arr[inst];
+	const double b = beta[inst * ldab + n - 1];
+	int ok = n >= nev;
+	const int have = nev < n ? nev + 1 : n;
+	const double *th = theta + (int64_t)inst * ldt;
+	for (int i = 0; i < nev && i < n && ok; i++) {
+		const double r = fabs(b * zlast[(int64_t)inst * ldt + i]);
+		double gap = 1e300;
+		if (i > 0) gap = fmin(gap, th[i] - th[i - 1]);
+		if (i + 1 < have) gap = fmin(gap, th[i + 1] - th[i]);
+		const double bound = fmin(r, r * r / fmax(gap, 1e-300));
+		if (!(bound < tol)) ok = 0;
+	}
+	flag[inst] = ok || b == 0.0;
+}
+
+/* X[inst][j] = sum_{l < n} V[inst][l] Z[inst][j][l], j < r */
+__global__ void kb_ritz(const double *__restrict__ V, int64_t ldV, const double *__restrict__ Z, int ldz,
+			const int *__restrict__ n_arr, int r, int64_t D, double *__restrict__ X)
+{
+	const int inst = blockIdx.y;
+	const int n = n_arr[inst];
+	const double *v = V + inst * ldV;
+	const double *z = Z + (int64_t)inst * r * ldz;
+	double *x = X + (int64_t)inst * r * D;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		for (int j = 0; j < r; j++) {
+			double s = 0.0;
+			if (j < n)
+				for (int l = 0; l < n; l++) s = fma(v[(int64_t)l * D + i], z[(int64_t)j * ldz + l], s);
+			x[(int64_t)j * D + i] = s;
+		}
+}
+
+/* G[inst][i][j] = A[inst][i] . Bm[inst][j]; one CTA per (i, j, inst) */
+__global__ void __launch_bounds__(BT) kb_gram(const double *__restrict__ A, const double *__restrict__ Bm, int r,
+					       int64_t D, double *__restrict__ G)
+{
+	__shared__ double sh[BT];
+	const int inst = blockIdx.y, i = blockIdx.x / r, j = blockIdx.x % r;
+	const double *a = A + ((int64_t)inst * r + i) * D, *b = Bm + ((int64_t)inst * r + j) * D;
+	double s = 0.0;
+	for (int64_t t = threadIdx.x; t < D; t += blockDim.x) s = fma(a[t], b[t], s);
+	s = jn_block_sum(s, sh);
+	if (threadIdx.x == 0) G[((int64_t)inst * r + i) * r + j] = s;
+}
+
+/* out[inst] = sum_j X[inst][j] C[inst][j] */
+__global__ void kb_combine(const double *__restrict__ X, const double *__restrict__ C, int r, int64_t D,
+			   double *__restrict__ out)
+{
+	const int inst = blockIdx.y;
+	const double *x = X + (int64_t)inst * r * D, *c = C + (int64_t)inst * r;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int j = 0; j < r; j++) s = fma(x[(int64_t)j * D + i], c[j], s);
+		out[inst * D + i] = s;
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* host: the r x r generalized symmetric eigenproblem A c = l G c       */
+/* ------------------------------------------------------------------ */
+/* Cholesky G = L L^T in place (lower); returns 0 or -1 when not positive */
+static int cholesky(double *G, int r)
+{
+	for (int j = 0; j < r; j++) {
+		double d = G[j * r + j];
+		for (int k = 0; k < j; k++) d -= G[j * r + k] * G[j * r + k];
+		if (!(d > 0)) return -1;
+		d = sqrt(d);
+		G[j * r + j] = d;
+		for (int i = j + 1; i < r; i++) {
+			double s = G[i * r + j];
+			for (int k = 0; k < j; k++) s -= G[i * r + k] * G[j * r + k];
+			G[i * r + j] = s / d;
+		}
+	}
+	return 0;
+}
+
+/* cyclic Jacobi: S (r x r symmetric) -> eigenvalues w (ascending) and eigenvectors Q (columns) */
+static void jacobi_eigen(double *S, int r, double *w, double *Q)
+{
+	for (int i = 0; i < r * r; i++) Q[i] = 0.0;
+	for (int i = 0; i < r; i++) Q[i * r + i] = 1.0;
+	for (int sweep = 0; sweep < 100; sweep++) {
+		double off = 0.0;
+		for (int p = 0; p < r; p++)
+			for (int q = p + 1; q < r; q++) off += S[p * r + q] * S[p * r + q];
+		if (off < 1e-300) break;
+		for (int p = 0; p < r; p++)
+			for (int q = p + 1; q < r; q++) {
+				const double apq = S[p * r + q];
+				if (apq == 0.0) continue;
+				const double theta = (S[q * r + q] - S[p * r + p]) / (2.0 * apq);
+				const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+				const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+				for (int k = 0; k < r; k++) {
+					const double skp = S[k * r + p], skq = S[k * r + q];
+					S[k * r + p] = c * skp - s * skq;
+					S[k * r + q] = s * skp + c * skq;
+				}
+				for (int k = 0; k < r; k++) {
+					const double spk = S[p * r + k], sqk = S[q * r + k];
+					S[p * r + k] = c * spk - s * sqk;
+					S[q * r + k] = s * spk + c * sqk;
+				}
+				for (int k = 0; k < r; k++) {
+					const double qkp = Q[k * r + p], qkq = Q[k * r + q];
+					Q[k * r + p] = c * qkp - s * qkq;
+					Q[k * r + q] = s * qkp + c * qkq;
+				}
+			}
+	}
+	/* sort ascending */
+	for (int i = 0; i < r; i++) w[i] = S[i * r + i];
+	for (int i = 0; i < r; i++) {
+		int m = i;
+		for (int j = i + 1; j < r; j++) if (w[j] < w[m]) m = j;
+		if (m != i) {
+			double t = w[i]; w[i] = w[m]; w[m] = t;
+			for (int k = 0; k < r; k++) { t = Q[k * r + i]; Q[k * r + i] = Q[k * r + m]; Q[k * r + m] = t; }
+		}
+	}
+}
+
+/* refined values lam[0..r), residual norms res[] and the coefficients c0 of
+ * the lowest refined vector, from G1 = X^T X, G2 = X^T H X, G3 = (HX)^T HX */
+static int rayleigh_ritz(const double *G1, const double *G2, const double *G3, int r, double *lam, double *res,
+			 double *c0)
+{
+	double *L = (double *)malloc(sizeof(double) * r * r), *S = (double *)malloc(sizeof(double) * r * r);
+	double *Q = (double *)malloc(sizeof(double) * r * r), *T = (double *)malloc(sizeof(double) * r * r);
+	double *c = (double *)malloc(sizeof(double) * r);
+	memcpy(L, G1, sizeof(double) * r * r);
+	int rc = cholesky(L, r);
+	if (!rc) {
+		/* T = L^-1 G2, S = T L^-T */
+		for (int j = 0; j < r; j++)
+			for (int i = 0; i < r; i++) {
+				double s = G2[i * r + j];
+				for (int k = 0; k < i; k++) s -= L[i * r + k] * T[k * r + j];
+				T[i * r + j] = s / L[i * r + i];
+			}
+		for (int i = 0; i < r; i++)
+			for (int j = 0; j < r; j++) {
+				double s = T[i * r + j];
+				for (int k = 0; k < j; k++) s -= S[i * r + k] * L[j * r + k];
+				S[i * r + j] = s / L[j * r + j];
+			}
+		for (int i = 0; i < r; i++)
+			for (int j = i + 1; j < r; j++) S[i * r + j] = S[j * r + i] = 0.5 * (S[i * r + j] + S[j * r + i]);
+		jacobi_eigen(S, r, lam, Q);
+		for (int e = 0; e < r; e++) {
+			/* c = L^-T q_e */
+			for (int i = r - 1; i >= 0; i--) {
+				double s = Q[i * r + e];
+				for (int k = i + 1; k < r; k++) s -= L[k * r + i] * c[k];
+				c[i] = s / L[i * r + i];
+			}
+			double h2 = 0, hx = 0, xx = 0;
+			for (int i = 0; i < r; i++)
+				for (int j = 0; j < r; j++) {
+					h2 += c[i] * G3[i * r + j] * c[j];
+					hx += c[i] * G2[i * r + j] * c[j];
+					xx += c[i] * G1[i * r + j] * c[j];
+				}
+			double r2 = h2 - 2.0 * lam[e] * hx + lam[e] * lam[e] * xx;
+			res[e] = sqrt(fmax(r2, 0.0) / fmax(xx, 1e-300));
+			if (e == 0 && c0) memcpy(c0, c, sizeof(double) * r);
+		}
+	}
+	free(L); free(S); free(Q); free(T); free(c);
+	return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* the solver                                                           */
+/* ------------------------------------------------------------------ */
+struct bstate {
+	double *V, *W, *me64, *x64, *alpha, *beta, *part, *h, *scal, *theta, *zlast, *Z, *work, *X, *HX, *G, *C, *GS;
+	float *me32, *x32;
+	unsigned long long *gacc;
+	unsigned int *ctrl;
+	int *k, *active, *flag, *narr;
+};
+
+static void bstate_free(struct bstate *s)
+{
+	void *p[] = { s->V, s->W, s->me64, s->x64, s->alpha, s->beta, s->part, s->h, s->scal, s->theta, s->zlast, s->Z,
+		      s->work, s->X, s->HX, s->G, s->C, s->GS, s->me32, s->x32, s->gacc, s->ctrl, s->k, s->active,
+		      s->flag, s->narr };
+	for (size_t i = 0; i < sizeof p / sizeof p[0]; i++) cudaFree(p[i]);
+}
+
+#define BALLOC(ptr, count)                                                                                    \
+	do {                                                                                                  \
+		if (!st && cudaMalloc((void **)&(ptr), (size_t)(count) * sizeof(*(ptr)) + 64) != cudaSuccess)   \
+			st = jn_fail(JN_ERR_NOMEM, "batched Lanczos: device allocation of %s failed", #ptr);   \
+	} while (0)
+
+extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_batch_result *res)
+{
+	if (!c || !o || !res || !o->matrix_elements) return jn_fail(JN_ERR_INVALID, "null argument");
+	const jn_plan_t *p = &c->plan;
+	const int B = o->num_instances;
+	const int64_t D = p->dim, nme = p->n_me;
+	if (B < 1 || B > 4096) return jn_fail(JN_ERR_INVALID, "num_instances must be in 1..4096");
+	if (D < 1) return jn_fail(JN_ERR_INVALID, "empty basis");
+	if (o->precision != 32 && o->precision != 64) return jn_fail(JN_ERR_INVALID, "precision must be 32 or 64");
+	int m = o->max_iterations > 0 ? o->max_iterations : 200;
+	if (m > D) m = (int)D;
+	int nev = o->num_eigenvalues > 0 ? o->num_eigenvalues : 10;
+	if (nev > JN_MAX_REPORTED) nev = JN_MAX_REPORTED;
+	if (nev > m) nev = m;
+	const int extra = o->refine_extra >= 0 ? o->refine_extra : 4;
+	int r = nev + extra;
+	if (r > m) r = m;
+	const int check_every = o->check_every > 0 ? o->check_every : 10;
+	const int f32 = o->precision == 32;
+	const int want = nev + 1 < m ? nev + 1 : m;
+	const int ldz = m + 1;
+	const int ncol = m + 2;
+	const int64_t ldV = (int64_t)(m + 1) * D, ldab = m + 1;
+	cudaStream_t q = c->stream;
+	jn_status st = JN_OK;
+	struct bstate s;
+	memset(&s, 0, sizeof s);
+	BALLOC(s.V, (size_t)B * ldV);
+	BALLOC(s.W, (size_t)B * D);
+	BALLOC(s.me64, (size_t)B * nme);
+	if (f32) { BALLOC(s.me32, (size_t)B * nme); BALLOC(s.x32, (size_t)B * D); }
+	else BALLOC(s.x64, (size_t)B * D);
+	BALLOC(s.alpha, (size_t)B * ldab);
+	BALLOC(s.beta, (size_t)B * ldab);
+	BALLOC(s.part, (size_t)B * BNB * ncol);
+	BALLOC(s.h, (size_t)B * ncol);
+	BALLOC(s.scal, (size_t)B);
+	BALLOC(s.theta, (size_t)B * (r + 1));
+	BALLOC(s.zlast, (size_t)B * (r + 1));
+	const int zrows = r > want ? r : want;  /* vectors per instance: r at the end, want in checks */
+	BALLOC(s.Z, (size_t)B * zrows * ldz);
+	BALLOC(s.work, (size_t)B * zrows * 5 * ldz);
+	BALLOC(s.gacc, (size_t)B * D);
+	BALLOC(s.ctrl, (size_t)2 * B);
+	BALLOC(s.k, 1);
+	BALLOC(s.active, B);
+	BALLOC(s.flag, B);
+	BALLOC(s.narr, B);
+	if (st) { bstate_free(&s); return st; }
+
+	/* matrix elements: FP64 for refinement, FP32 copies with the reference's
+	   |M| < 1e-12 skip of single-species blocks (matrix_vector_multiplication.c:52-53) */
+	double maxme = 0.0;
+	float *h32 = f32 ? (float *)malloc(nme * sizeof(float)) : NULL;
+	for (int i = 0; i < B && !st; i++) {
+		const double *me = o->matrix_elements[i];
+		if (!me) { st = jn_fail(JN_ERR_INVALID, "matrix_elements[%d] is NULL", i); break; }
+		for (int64_t e = 0; e < nme; e++) maxme = fmax(maxme, fabs(me[e]));
+		if (cudaMemcpyAsync(s.me64 + (size_t)i * nme, me, nme * sizeof(double), cudaMemcpyHostToDevice, q) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "upload of matrix elements");
+		if (f32 && !st) {
+			for (int b = 0; b < p->nmes; b++) {
+				const jn_me_t *M = &p->mes[b];
+				for (int64_t e = 0; e < M->len; e++) {
+					const double v = me[M->offset + e];
+					h32[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0f : (float)v;
+				}
+			}
+			if (cudaMemcpy(s.me32 + (size_t)i * nme, h32, nme * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+				st = jn_fail(JN_ERR_CUDA, "upload of FP32 matrix elements");
+		}
+	}
+	free(h32);
+	/* fixed-point scale bound valid for every instance */
+	const double abs_bound = jn_plan_abs_bound(p, NULL) * maxme;
+
+	/* start vectors: given, or one seeded pseudo-random vector for all */
+	double *hv = (double *)malloc(D * sizeof(double));
+	for (int i = 0; i < B && !st; i++) {
+		const double *sv = o->start_vectors ? o->start_vectors[i] : NULL;
+		if (!sv) {
+			uint64_t z = 0x9E3779B97F4A7C15ull;
+			for (int64_t e = 0; e < D; e++) {
+				z += 0x9E3779B97F4A7C15ull;
+				uint64_t v = z;
+				v = (v ^ (v >> 30)) * 0xBF58476D1CE4E5B9ull;
+				v = (v ^ (v >> 27)) * 0x94D049BB133111EBull;
+				v ^= v >> 31;
+				hv[e] = (double)(v >> 11) * 0x1.0p-53 - 0.5;
+			}
+			sv = hv;
+		}
+		if (cudaMemcpy(s.V + (size_t)i * ldV, sv, D * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "upload of start vectors");
+	}
+	free(hv);
+	int *hact = (int *)malloc(B * sizeof(int)), *hn = (int *)malloc(B * sizeof(int)), *hflag = (int *)malloc(B * sizeof(int));
+	for (int i = 0; i < B; i++) { hact[i] = 1; hn[i] = 0; }
+	cudaGraphExec_t gexec = NULL;
+	cudaGraph_t graph = NULL;
+	int k = 0, nactive = B;
+	const int vg = (int)((D + BT - 1) / BT < 64 ? (D + BT - 1) / BT : 64);
+	const dim3 gv(vg > 0 ? vg : 1, B), gr(BNB, B), g1(1, B);
+	if (!st) {
+		cudaMemsetAsync(s.k, 0, sizeof(int), q);
+		cudaMemsetAsync(s.gacc, 0, (size_t)B * D * sizeof(unsigned long long), q);
+		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
+		/* v_0 normalised */
+		kb_dot<<<gr, BT, 0, q>>>(s.V, ldV, 0, s.V, ldV, 0, s.k, D, s.part, NULL);
+		kb_finish_dot<<<g1, 32, 0, q>>>(s.part, BNB, s.scal, 1, 0, s.k, NULL);
+		kb_scale_start<<<gv, BT, 0, q>>>(s.V, ldV, s.scal, D);
+		if (cudaGetLastError() != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "batched Lanczos start");
+	}
+
+	/* one Lanczos step for every active instance, k read on the device */
+	auto step = [&](cudaStream_t qs) -> jn_status {
+		jn_status e = jn_enqueue_batched(c, B, f32, f32 ? (const void *)s.me32 : (const void *)s.me64, nme, s.V, ldV,
+						 s.k, D, s.W, D, s.x64, s.x32, s.gacc, s.ctrl, s.active, abs_bound, qs);
+		if (e) return e;
+		kb_dot<<<gr, BT, 0, qs>>>(s.V, ldV, 1, s.W, D, 0, s.k, D, s.part, s.active);
+		kb_finish_dot<<<g1, 32, 0, qs>>>(s.part, BNB, s.alpha, ldab, 1, s.k, s.active);
+		kb_three_term<<<gv, BT, 0, qs>>>(s.W, s.V, ldV, s.alpha, s.beta, ldab, s.k, D, s.active);
+		for (int pass = 0; pass < 2; pass++) {
+			kb_gemv_t<<<gr, BT, 0, qs>>>(s.V, ldV, s.W, s.k, D, s.part, ncol, s.active);
+			kb_finish<<<dim3((ncol + 127) / 128, B), 128, 0, qs>>>(s.part, BNB, ncol, s.k, s.h, s.active);
+			kb_gemv_n_sub<<<gv, BT, 0, qs>>>(s.V, ldV, s.h, ncol, s.k, D, s.W, s.active);
+		}
+		kb_dot<<<gr, BT, 0, qs>>>(s.W, D, 0, s.W, D, 0, s.k, D, s.part, s.active);
+		kb_finish_dot<<<g1, 32, 0, qs>>>(s.part, BNB, s.scal, 1, 0, s.k, s.active);
+		kb_normalize<<<gv, BT, 0, qs>>>(s.V, ldV, s.W, s.scal, s.beta, ldab, s.k, D, s.active);
+		kb_advance<<<1, 32, 0, qs>>>(s.k);
+		return cudaGetLastError() == cudaSuccess ? JN_OK : jn_fail(JN_ERR_CUDA, "batched Lanczos step launch");
+	};
+
+	if (!st && o->use_graph) {
+		if (cudaStreamBeginCapture(q, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "stream capture");
+		jn_status e = st ? st : step(q);
+		cudaError_t ce = cudaStreamEndCapture(q, &graph);
+		if (!st && (e || ce != cudaSuccess)) st = e ? e : jn_fail(JN_ERR_CUDA, "end capture: %s", cudaGetErrorString(ce));
+		if (!st && cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "graph instantiation");
+	}
+
+	while (!st && nactive > 0 && k < m) {
+		if (gexec) {
+			if (cudaGraphLaunch(gexec, q) != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "graph launch");
+		} else {
+			st = step(q);
+		}
+		k++;
+		if (st) break;
+		if (k % check_every && k < m) continue;
+		/* convergence of every active instance at n = k */
+		for (int i = 0; i < B; i++) hn[i] = hact[i] ? k : hn[i];
+		cudaMemcpyAsync(s.narr, hn, B * sizeof(int), cudaMemcpyHostToDevice, q);
+		const int wk = want < k ? want : k;
+		kb_tri_bisect<<<dim3((wk + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, wk, s.theta, r + 1, s.active);
+		kb_tri_vectors<<<dim3((wk + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, wk, s.theta, r + 1, s.Z,
+									ldz, s.work, s.zlast, s.active);
+		kb_converged<<<(B + 127) / 128, 128, 0, q>>>(s.theta, s.zlast, r + 1, s.beta, ldab, s.narr, nev, o->tolerance,
+							     s.flag, s.active, B);
+		if (cudaMemcpyAsync(hflag, s.flag, B * sizeof(int), cudaMemcpyDeviceToHost, q) != cudaSuccess ||
+		    cudaStreamSynchronize(q) != cudaSuccess) {
+			st = jn_fail(JN_ERR_CUDA, "convergence check: %s", cudaGetErrorString(cudaGetLastError()));
+			break;
+		}
+		for (int i = 0; i < B; i++)
+			if (hact[i] && (hflag[i] || k >= m)) {
+				hact[i] = 0;
+				hn[i] = k;
+				res[i].converged = hflag[i];
+				res[i].iterations = k;
+				nactive--;
+			}
+		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
+	}
+	if (gexec) cudaGraphExecDestroy(gexec);
+	if (graph) cudaGraphDestroy(graph);
+
+	/* Ritz vectors of the final T of each instance, FP64 products, Rayleigh-Ritz */
+	if (!st) {
+		BALLOC(s.X, (size_t)B * r * D);
+		BALLOC(s.HX, (size_t)B * r * D);
+		BALLOC(s.G, (size_t)B * 3 * r * r);
+		BALLOC(s.C, (size_t)B * r);
+		if (o->ground_states) BALLOC(s.GS, (size_t)B * D);
+	}
+	double *hG = NULL;
+	if (!st) {
+		for (int i = 0; i < B; i++) hact[i] = 1;
+		cudaMemcpyAsync(s.narr, hn, B * sizeof(int), cudaMemcpyHostToDevice, q);
+		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
+		kb_tri_bisect<<<dim3((r + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, NULL);
+		kb_tri_vectors<<<dim3((r + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, s.Z, ldz,
+								     s.work, NULL, NULL);
+		kb_tri_mgs<<<g1, BT, 0, q>>>(s.Z, ldz, s.narr, r, NULL);
+		kb_ritz<<<gv, BT, 0, q>>>(s.V, ldV, s.Z, ldz, s.narr, r, D, s.X);
+		/* H X in FP64, one batched product per Ritz index */
+		for (int j = 0; j < r && !st; j++)
+			st = jn_enqueue_batched(c, B, 0, s.me64, nme, s.X + (size_t)j * D, (int64_t)r * D, NULL, 0,
+						s.HX + (size_t)j * D, (int64_t)r * D, s.W, NULL, s.gacc, s.ctrl, NULL, abs_bound, q);
+	}
+	if (!st) {
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.X, r, D, s.G);
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.HX, r, D, s.G + (size_t)B * r * r);
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.HX, s.HX, r, D, s.G + (size_t)2 * B * r * r);
+		hG = (double *)malloc(sizeof(double) * 3 * B * r * r);
+		double *hth = (double *)malloc(sizeof(double) * B * (r + 1));
+		if (cudaMemcpyAsync(hG, s.G, sizeof(double) * 3 * B * r * r, cudaMemcpyDeviceToHost, q) != cudaSuccess ||
+		    cudaMemcpyAsync(hth, s.theta, sizeof(double) * B * (r + 1), cudaMemcpyDeviceToHost, q) != cudaSuccess ||
+		    cudaStreamSynchronize(q) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "refinement: %s", cudaGetErrorString(cudaGetLastError()));
+		double *hC = (double *)calloc((size_t)B * r, sizeof(double));
+		double *lam = (double *)malloc(sizeof(double) * r), *rn = (double *)malloc(sizeof(double) * r);
+		for (int i = 0; i < B && !st; i++) {
+			const int ri = hn[i] < r ? hn[i] : r;
+			double *G1 = (double *)malloc(sizeof(double) * ri * ri), *G2 = (double *)malloc(sizeof(double) * ri * ri),
+			       *G3 = (double *)malloc(sizeof(double) * ri * ri);
+			for (int a = 0; a < ri; a++)
+				for (int b2 = 0; b2 < ri; b2++) {
+					G1[a * ri + b2] = hG[((size_t)i * r + a) * r + b2];
+					G2[a * ri + b2] = 0.5 * (hG[(size_t)B * r * r + ((size_t)i * r + a) * r + b2] +
+								 hG[(size_t)B * r * r + ((size_t)i * r + b2) * r + a]);
+					G3[a * ri + b2] = hG[(size_t)2 * B * r * r + ((size_t)i * r + a) * r + b2];
+				}
+			if (rayleigh_ritz(G1, G2, G3, ri, lam, rn, hC + (size_t)i * r))
+				st = jn_fail(JN_ERR_NOT_CONVERGED, "instance %d: Ritz vectors are not independent", i);
+			res[i].num_eigenvalues = nev < ri ? nev : ri;
+			for (int e = 0; e < res[i].num_eigenvalues; e++) {
+				res[i].eigenvalues[e] = lam[e];
+				res[i].residual_norms[e] = rn[e];
+				res[i].ritz_values[e] = hth[(size_t)i * (r + 1) + e];
+			}
+			free(G1); free(G2); free(G3);
+		}
+		if (!st && o->ground_states) {
+			cudaMemcpyAsync(s.C, hC, sizeof(double) * B * r, cudaMemcpyHostToDevice, q);
+			kb_combine<<<gv, BT, 0, q>>>(s.X, s.C, r, D, s.GS);
+			for (int i = 0; i < B && !st; i++)
+				if (o->ground_states[i] &&
+				    cudaMemcpyAsync(o->ground_states[i], s.GS + (size_t)i * D, D * sizeof(double),
+						    cudaMemcpyDeviceToHost, q) != cudaSuccess)
+					st = jn_fail(JN_ERR_CUDA, "ground-state copy");
+			if (!st && cudaStreamSynchronize(q) != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "ground-state copy");
+		}
+		free(hC); free(lam); free(rn); free(hth);
+	}
+	free(hG);
+	free(hact); free(hn); free(hflag);
+	bstate_free(&s);
+	if (!st && cudaGetLastError() != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "batched Lanczos");
+	return st;
+}
+
+/* ------------------------------------------------------------------ */
+/* matrix-element sets on the context's lists                           */
+/* ------------------------------------------------------------------ */
+extern "C" size_t jn_me_count(const jn_ctx *c) { return c ? (size_t)c->plan.n_me : 0; }
+
+extern "C" jn_status jn_read_matrix_elements(const jn_ctx *c, const char *dir, double *out)
+{
+	if (!c || !dir || !out) return jn_fail(JN_ERR_INVALID, "null argument");
+	char err[1024] = "";
+	if (jn_plan_read_me(&c->plan, dir, out, err, sizeof err))
+		return jn_fail(strstr(err, "Could not open") ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
+	return JN_OK;
+}
+
+extern "C" jn_status jn_set_matrix_elements(jn_ctx *c, const double *me)
+{
+	if (!c || !me) return jn_fail(JN_ERR_INVALID, "null argument");
+	jn_plan_t *p = &c->plan;
+	memcpy(p->me, me, (size_t)p->n_me * sizeof(double));
+	p->abs_bound = jn_plan_abs_bound(p, p->me);
+	CUDA_TRY(cudaMemcpy(c->d_me, p->me, (size_t)p->n_me * sizeof(double), cudaMemcpyHostToDevice));
+	if (c->d_me32) {
+		float *h = (float *)malloc((p->n_me ? p->n_me : 1) * sizeof(float));
+		if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+		for (int b = 0; b < p->nmes; b++) {
+			const jn_me_t *M = &p->mes[b];
+			for (int64_t e = 0; e < M->len; e++) {
+				const double v = p->me[M->offset + e];
+				h[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0f : (float)v;
+			}
+		}
+		cudaError_t e = cudaMemcpy(c->d_me32, h, (size_t)p->n_me * sizeof(float), cudaMemcpyHostToDevice);
+		free(h);
+		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "FP32 matrix elements: %s", cudaGetErrorString(e));
+	}
+	return JN_OK;
+}

@@ -62,6 +62,17 @@ jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumu
 			   cudaEvent_t pre, cudaEvent_t mid, unsigned long long *gacc, unsigned int *ctrl, float *x32,
 			   int clear_acc);
 
+/* B products at once, instance i = blockIdx.y: y[i] = H_i x_i with the
+ * context's lists and the matrix elements me + i * me_ld (FP32 when f32),
+ * x_i = src + i * src_ld + (*d_sel) * sel_ld (d_sel may be NULL).
+ * Scratch: x64 or x32 (B x dim), gacc (B x dim, zero on entry, left zero),
+ * ctrl (2 B words).  Instances with d_active[i] == 0 are skipped.  abs_bound
+ * must bound every instance's matrix elements (jn_plan_abs_bound). */
+jn_status jn_enqueue_batched(jn_ctx *c, int B, int f32, const void *me, int64_t me_ld, const double *src,
+			     int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y, int64_t y_ld, double *x64,
+			     float *x32, unsigned long long *gacc, unsigned int *ctrl, const int *d_active, double abs_bound,
+			     cudaStream_t st);
+
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);
 

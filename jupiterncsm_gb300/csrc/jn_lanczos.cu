@@ -38,6 +38,7 @@
 #include <sys/types.h>
 
 #include "jn_internal.h"
+#include "jn_tridiag.cuh"
 
 #define RED_BLOCKS 304      /* 2 x 152 SMs */
 #define RED_THREADS 256
@@ -78,19 +79,7 @@ void jn_lanczos_release(jn_ctx *c)
 /* ------------------------------------------------------------------ */
 /* BLAS-1/2 kernels with fixed reduction order                         */
 /* ------------------------------------------------------------------ */
-__device__ __forceinline__ double block_sum(double v, double *sh)
-{
-	const int t = threadIdx.x;
-	sh[t] = v;
-	__syncthreads();
-	for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-		if (t < s) sh[t] += sh[t + s];
-		__syncthreads();
-	}
-	double r = sh[0];
-	__syncthreads();
-	return r;
-}
+#define block_sum jn_block_sum
 
 /* part[b*ncol + j] = sum over this block's slice of V[j] . w, j < nvec */
 __global__ void __launch_bounds__(RED_THREADS) k_gemv_t(const double *__restrict__ V, int64_t D, int nvec,
@@ -179,135 +168,30 @@ __global__ void k_axpy_neg(double *__restrict__ y, const double *__restrict__ x,
 /* ------------------------------------------------------------------ */
 /* tridiagonal eigenproblem                                            */
 /* ------------------------------------------------------------------ */
-/* number of eigenvalues of T (diag a, offdiag b, order n) below x */
-__device__ int sturm_count(const double *a, const double *b, int n, double x)
-{
-	int c = 0;
-	double q = a[0] - x;
-	if (q < 0) c++;
-	for (int i = 1; i < n; i++) {
-		double qq = q == 0.0 ? 1e-300 : q;
-		q = a[i] - x - b[i - 1] * b[i - 1] / qq;
-		if (q < 0) c++;
-	}
-	return c;
-}
-
 /* theta[i] for i < want: the i-th smallest eigenvalue, by bisection */
 __global__ void k_tri_bisect(const double *__restrict__ a, const double *__restrict__ b, int n, int want,
 			     double *__restrict__ theta)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= want) return;
-	double lo = a[0], hi = a[0];
-	for (int j = 0; j < n; j++) {
-		double r = (j > 0 ? fabs(b[j - 1]) : 0.0) + (j < n - 1 ? fabs(b[j]) : 0.0);
-		lo = fmin(lo, a[j] - r);
-		hi = fmax(hi, a[j] + r);
-	}
-	double span = fmax(fabs(lo), fabs(hi));
-	lo -= 1e-12 * span + 1e-300;
-	hi += 1e-12 * span + 1e-300;
-	for (int it = 0; it < 200; it++) {
-		double mid = 0.5 * (lo + hi);
-		if (mid <= lo || mid >= hi) break;
-		if (sturm_count(a, b, n, mid) > i) hi = mid; else lo = mid;
-	}
-	theta[i] = 0.5 * (lo + hi);
+	theta[i] = jn_tri_bisect_one(a, b, n, i);
 }
 
-/* eigenvector of T for theta[i] by inverse iteration (LU with partial
- * pivoting of T - theta I), normalised, component 0 made non-negative as
- * diagonalization.c:55-58 does.  Z row i holds the n components. */
+/* eigenvector of T for theta[i] by inverse iteration; Z row i holds the n components */
 __global__ void k_tri_vectors(const double *__restrict__ a, const double *__restrict__ b, int n, int want,
 			      const double *__restrict__ theta, double *__restrict__ Z, int ldz, double *__restrict__ work,
 			      int ldw)
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= want) return;
-	double *z = Z + (int64_t)i * ldz;
-	/* work: d (diag of U), u1, u2 (super diagonals of U), l (multipliers), piv flags */
-	double *d = work + (int64_t)i * ldw, *u1 = d + n, *u2 = u1 + n, *l = u2 + n, *pv = l + n;
-	double span = 0.0;
-	for (int j = 0; j < n; j++) span = fmax(span, fabs(a[j]) + (j < n - 1 ? fabs(b[j]) : 0.0));
-	const double eps = 2.2e-16 * fmax(span, 1e-300);
-	const double sh = theta[i];
-	/* factorisation of T - sh I with row interchanges */
-	double dd = a[0] - sh, e = n > 1 ? b[0] : 0.0, f = 0.0;
-	for (int j = 0; j < n - 1; j++) {
-		double sub = b[j];
-		double nd = a[j + 1] - sh, ne = (j + 1 < n - 1) ? b[j + 1] : 0.0;
-		if (fabs(dd) >= fabs(sub)) {
-			pv[j] = 0.0;
-			if (dd == 0.0) dd = eps;
-			double m = sub / dd;
-			l[j] = m;
-			d[j] = dd; u1[j] = e; u2[j] = 0.0;
-			dd = nd - m * e;
-			e = ne;
-		} else {
-			pv[j] = 1.0;
-			double m = dd / sub;
-			l[j] = m;
-			d[j] = sub; u1[j] = nd; u2[j] = ne;
-			dd = e - m * nd;
-			e = -m * ne;
-		}
-		(void)f;
-	}
-	if (dd == 0.0) dd = eps;
-	d[n - 1] = dd; u1[n - 1] = 0.0; u2[n - 1] = 0.0;
-	for (int j = 0; j < n; j++) z[j] = 1.0;
-	for (int iter = 0; iter < 3; iter++) {
-		/* forward: apply L^-1 with the interchanges */
-		for (int j = 0; j < n - 1; j++) {
-			if (pv[j] != 0.0) { double t = z[j]; z[j] = z[j + 1]; z[j + 1] = t - l[j] * z[j]; }
-			else z[j + 1] -= l[j] * z[j];
-		}
-		/* back substitution with U */
-		for (int j = n - 1; j >= 0; j--) {
-			double s = z[j];
-			if (j + 1 < n) s -= u1[j] * z[j + 1];
-			if (j + 2 < n) s -= u2[j] * z[j + 2];
-			z[j] = s / (fabs(d[j]) < eps ? (d[j] < 0 ? -eps : eps) : d[j]);
-		}
-		double nrm = 0.0;
-		for (int j = 0; j < n; j++) nrm = fma(z[j], z[j], nrm);
-		nrm = sqrt(nrm);
-		for (int j = 0; j < n; j++) z[j] /= nrm;
-	}
-	if (z[0] < 0)
-		for (int j = 0; j < n; j++) z[j] = -z[j];
+	jn_tri_vector_one(a, b, n, theta[i], Z + (int64_t)i * ldz, work + (int64_t)i * ldw);
 }
 
-/* modified Gram-Schmidt among the `want` tridiagonal eigenvectors (one CTA),
- * which repairs inverse-iteration vectors of close eigenvalues */
+/* modified Gram-Schmidt among the `want` tridiagonal eigenvectors (one CTA) */
 __global__ void k_tri_mgs(double *__restrict__ Z, int ldz, int n, int want)
 {
 	__shared__ double sh[RED_THREADS];
-	for (int i = 0; i < want; i++) {
-		double *zi = Z + (int64_t)i * ldz;
-		for (int j = 0; j < i; j++) {
-			const double *zj = Z + (int64_t)j * ldz;
-			double s = 0.0;
-			for (int t = threadIdx.x; t < n; t += blockDim.x) s = fma(zi[t], zj[t], s);
-			s = block_sum(s, sh);
-			for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] -= s * zj[t];
-			__syncthreads();
-		}
-		double s = 0.0;
-		for (int t = threadIdx.x; t < n; t += blockDim.x) s = fma(zi[t], zi[t], s);
-		s = block_sum(s, sh);
-		double inv = 1.0 / sqrt(s);
-		for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] *= inv;
-		__syncthreads();
-		if (threadIdx.x == 0 && zi[0] < 0) sh[0] = -1.0; else if (threadIdx.x == 0) sh[0] = 1.0;
-		__syncthreads();
-		double sg = sh[0];
-		__syncthreads();
-		for (int t = threadIdx.x; t < n; t += blockDim.x) zi[t] *= sg;
-		__syncthreads();
-	}
+	jn_tri_mgs(Z, ldz, n, want, sh);
 }
 
 /* ------------------------------------------------------------------ */

@@ -278,10 +278,23 @@ __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const 
 							       const uint2 *__restrict__ walks,
 							       const T *__restrict__ x, const T *__restrict__ me,
 							       unsigned long long *__restrict__ gacc,
-							       const unsigned int *__restrict__ xmax_bits, double abs_bound)
+							       const unsigned int *__restrict__ xmax_bits, double abs_bound,
+							       int64_t inst_stride, int64_t me_stride,
+							       const int *__restrict__ active)
 {
 	extern __shared__ unsigned int sacc[];
 	__shared__ int next_item, cur_tile;
+	/* batched products: instance blockIdx.y owns x, me and gacc at its strides
+	   and the control words (max|x| bits, tile counter) at 2 * instance */
+	if (gridDim.y > 1 || active) {
+		const int inst = blockIdx.y;
+		if (active && !active[inst]) return;
+		x += inst * inst_stride;
+		me += inst * me_stride;
+		gacc += inst * inst_stride;
+		tile_counter += 2 * inst;
+		xmax_bits += 2 * inst;
+	}
 	const int S = fixed_exponent(*xmax_bits, abs_bound);
 	const T scale = (T)ldexp(1.0, S);
 	const int lane = threadIdx.x & 31;
@@ -460,6 +473,45 @@ __global__ void jn_finalize_kernel(unsigned long long *__restrict__ gacc, double
 	}
 }
 
+/* Batched products (instance = blockIdx.y).  The source vector of instance
+ * i is src + i * src_ld + (*sel) * sel_ld: the Lanczos vector v_k of a batched
+ * solve, with k read on the device so that a captured graph can be replayed
+ * at every step.  It is copied to x64 (FP64 products) or converted to x32
+ * (FP32 products); max|x| goes to ctrl[2 i]. */
+__global__ void jn_prep_batched_kernel(const double *__restrict__ src, int64_t src_ld, const int *__restrict__ sel,
+				       int64_t sel_ld, double *__restrict__ x64, float *__restrict__ x32, int64_t n,
+				       unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = x[i];
+		if (x32) x32[inst * n + i] = (float)v;
+		else x64[inst * n + i] = v;
+		m = fmaxf(m, (float)fabs(v) * 1.0000002f);
+	}
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(ctrl + 2 * inst, __float_as_uint(m));
+}
+
+__global__ void jn_finalize_batched_kernel(unsigned long long *__restrict__ gacc, double *__restrict__ y,
+					   int64_t y_ld, int64_t n, const unsigned int *__restrict__ ctrl, double abs_bound,
+					   const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const int S = fixed_exponent(ctrl[2 * inst], abs_bound);
+	const double unit = ldexp(1.0, -S);
+	unsigned long long *g = gacc + inst * n;
+	double *yy = y + inst * y_ld;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		yy[i] = (double)(long long)g[i] * unit;
+		g[i] = 0ull;
+	}
+}
+
 /* ------------------------------------------------------------------ */
 /* host side                                                           */
 /* ------------------------------------------------------------------ */
@@ -629,16 +681,52 @@ jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumu
 		if (f32)
 			jn_tile_kernel<float><<<c->tile_grid, TILE_THREADS, smem, st>>>(
 				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
-				c->d_walks, x32, c->d_me32, gacc, ctrl, p->abs_bound);
+				c->d_walks, x32, c->d_me32, gacc, ctrl, p->abs_bound, 0, 0, NULL);
 		else
 			jn_tile_kernel<double><<<c->tile_grid, TILE_THREADS, smem, st>>>(
 				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
-				c->d_walks, d_x, c->d_me, gacc, ctrl, p->abs_bound);
+				c->d_walks, d_x, c->d_me, gacc, ctrl, p->abs_bound, 0, 0, NULL);
 	}
 	if (mid) cudaEventRecord(mid, st);
 	if (p->dim) jn_finalize_kernel<<<g, 256, 0, st>>>(gacc, d_y, p->dim, ctrl, p->abs_bound, accumulate);
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+jn_status jn_enqueue_batched(jn_ctx *c, int B, int f32, const void *me, int64_t me_ld, const double *src,
+			     int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y, int64_t y_ld, double *x64,
+			     float *x32, unsigned long long *gacc, unsigned int *ctrl, const int *d_active, double abs_bound,
+			     cudaStream_t st)
+{
+	const jn_plan_t *p = &c->plan;
+	if (B < 1 || B > 65535) return fail(JN_ERR_INVALID, "batch of %d instances", B);
+	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 256) g = 256;
+	if (g < 1) g = 1;
+	int gx = (c->tile_grid + B - 1) / B;
+	if (gx > p->nbtiles) gx = (int)p->nbtiles;
+	if (gx < 1) gx = 1;
+	const size_t smem = (size_t)(p->max_tile_elems ? p->max_tile_elems : 1) * 2 * sizeof(unsigned int);
+	cudaError_t e = cudaMemsetAsync(ctrl, 0, (size_t)2 * B * sizeof(unsigned int), st);
+	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+	if (!p->dim) return JN_OK;
+	jn_prep_batched_kernel<<<dim3(g, B), 256, 0, st>>>(src, src_ld, d_sel, sel_ld, x64, f32 ? x32 : NULL, p->dim, ctrl,
+							     d_active);
+	if (p->nbtiles) {
+		if (f32)
+			jn_tile_kernel<float><<<dim3(gx, B), TILE_THREADS, smem, st>>>(
+				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
+				c->d_walks, x32, (const float *)me, gacc, ctrl, abs_bound, p->dim, me_ld, d_active);
+		else
+			jn_tile_kernel<double><<<dim3(gx, B), TILE_THREADS, smem, st>>>(
+				P, c->d_btiles, p->nbtiles, ctrl + 1, (const uint2 *)c->d_items, c->d_pieces, c->d_tterms,
+				c->d_walks, x64, (const double *)me, gacc, ctrl, abs_bound, p->dim, me_ld, d_active);
+	}
+	jn_finalize_batched_kernel<<<dim3(g, B), 256, 0, st>>>(gacc, y, y_ld, p->dim, ctrl, abs_bound, d_active);
+	e = cudaGetLastError();
+	if (e != cudaSuccess) return fail(JN_ERR_CUDA, "batched product launch: %s", cudaGetErrorString(e));
 	return JN_OK;
 }
 

@@ -281,6 +281,27 @@ fail:
 	return NULL;
 }
 
+int jn_plan_read_me(const jn_plan_t *p, const char *dir, double *out, char *err, size_t errlen)
+{
+	for (int b = 0; b < p->nmes; b++) {
+		const jn_me_t *M = &p->mes[b];
+		uint64_t nd_n, nd_p;
+		int64_t len;
+		double *d = read_me_file(dir, M->id, &nd_n, &nd_p, &len, err, errlen);
+		if (!d) return 1;
+		if (nd_n != M->nd_n || nd_p != M->nd_p || len != M->len) {
+			free(d);
+			if (err) snprintf(err, errlen, "matrix file %d in %s has dimensions (%llu, %llu), the plan (%llu, %llu)", M->id,
+					  dir, (unsigned long long)nd_n, (unsigned long long)nd_p, (unsigned long long)M->nd_n,
+					  (unsigned long long)M->nd_p);
+			return 1;
+		}
+		memcpy(out + M->offset, d, (size_t)len * sizeof(double));
+		free(d);
+	}
+	return 0;
+}
+
 static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
 {
 	/* stable counting sort on the destination index; entries (source | destination << 16, matrix_index) */
@@ -311,7 +332,54 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->rowptr); free(p->ent); free(p->me);
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
 	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks); free(p->items);
+	free(p->term_dst);
 	memset(p, 0, sizeof *p);
+}
+
+double jn_plan_abs_bound(const jn_plan_t *p, const double *me)
+{
+	const uint32_t *rp = p->rowptr;
+	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
+	for (int t = 0; t < p->nterms; t++) {
+		const jn_me_t *M = &p->mes[p->instr[p->terms[t].instr].me];
+		double m = me ? 0.0 : 1.0;
+		if (me)
+			for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(me[M->offset + e]));
+		tmax[t] = m;
+	}
+	/* terms grouped by destination block */
+	int *cnt = calloc((size_t)p->nblocks + 1, sizeof(int));
+	int *byb = malloc((p->nterms > 0 ? (size_t)p->nterms : 1) * sizeof(int));
+	for (int t = 0; t < p->nterms; t++) cnt[p->term_dst[t] + 1]++;
+	for (int b = 0; b < p->nblocks; b++) cnt[b + 1] += cnt[b];
+	int *fl = malloc((p->nblocks + 1) * sizeof(int));
+	memcpy(fl, cnt, (p->nblocks + 1) * sizeof(int));
+	for (int t = 0; t < p->nterms; t++) byb[fl[p->term_dst[t]]++] = t;
+	free(fl);
+	double best = 0, *bound = NULL;
+	size_t bcap = 0;
+	for (int b = 0; b < p->nblocks; b++) {
+		const jn_block_t *B = &p->blocks[b];
+		size_t E = (size_t)(B->Np * B->Nn);
+		if (!E) continue;
+		if (E > bcap) { bcap = E; bound = realloc(bound, bcap * sizeof(double)); }
+		memset(bound, 0, E * sizeof(double));
+		for (int q = cnt[b]; q < cnt[b + 1]; q++) {
+			const int t = byb[q];
+			const jn_term_t *T = &p->terms[t];
+			for (int64_t r = 0; r < B->Np; r++) {
+				double np = T->kind == JN_KIND_N ? 1.0 : (double)(rp[T->p_ptr + r + 1] - rp[T->p_ptr + r]);
+				if (np == 0) continue;
+				for (int64_t c = 0; c < B->Nn; c++) {
+					double nn = T->kind == JN_KIND_P ? 1.0 : (double)(rp[T->n_ptr + c + 1] - rp[T->n_ptr + c]);
+					bound[r * B->Nn + c] += np * nn * tmax[t];
+				}
+			}
+		}
+		for (size_t e = 0; e < E; e++) best = fmax(best, bound[e]);
+	}
+	free(bound); free(tmax); free(cnt); free(byb);
+	return best;
 }
 
 /* warp pieces: R rows x W columns of one destination block, R*W <= 32 */
@@ -911,6 +979,7 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	/* terms: forward on the output block, transpose on the input block */
 	p->terms = malloc(2 * (size_t)p->ninstr * sizeof(jn_term_t));
 	int *term_dst = malloc(2 * (size_t)p->ninstr * sizeof(int));
+	p->term_dst = term_dst;
 	for (int i = 0; i < p->ninstr; i++) {
 		jn_instr_t *x = &p->instr[i];
 		for (int dir = 0; dir < 2; dir++) {
@@ -1075,7 +1144,6 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	}
 	/* block tiles for exact fixed-point accumulation */
 	if (build_block_tiles(p, term_dst, target_units, err, errlen)) goto fail;
-	free(term_dst);
 	free(slot_of_id); free(kind_of_id);
 	free(c.l); free(c.m); free(line);
 	return 0;

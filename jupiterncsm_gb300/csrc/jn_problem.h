@@ -181,6 +181,7 @@ typedef struct {
 	int64_t nitems;    uint32_t *items;    /* warp items {first task, width | ntasks << 8} */
 	int max_tile_elems;             /* shared-memory accumulator size needed */
 	double abs_bound;               /* max over y elements of sum |M| over its contributions */
+	int *term_dst;                  /* destination basis block of each term */
 	/* accounting */
 	int64_t list_entries;           /* sum of distinct list lengths */
 	int64_t me_elements;            /* sum of distinct ME block lengths */
@@ -206,6 +207,14 @@ int jn_read_runfile(const char *path, jn_runfile_t *rf, char *err, size_t errlen
 int jn_plan_build(jn_plan_t *plan, const char *comb, const char *order, const char *lists_dir,
 		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen);
 void jn_plan_free(jn_plan_t *plan);
+/* abs_bound of the plan's lists with another set of matrix elements (same
+ * layout as plan->me): the fixed-point scale of a product must use it.  With
+ * me == NULL every |M| counts as 1: the largest number of contributions to
+ * one element, so that abs_bound <= that * max|M| for any elements. */
+double jn_plan_abs_bound(const jn_plan_t *plan, const double *me);
+/* read the <id>_matrix_elements files of `dir` into out (plan->n_me values,
+ * the plan's layout); every block must have the plan's dimensions */
+int jn_plan_read_me(const jn_plan_t *plan, const char *dir, double *out, char *err, size_t errlen);
 
 #ifdef __cplusplus
 }

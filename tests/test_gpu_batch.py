@@ -1,0 +1,131 @@
+"""Batched mixed-precision Lanczos on H(c) = H0 + c H1 (many Hamiltonians on one
+set of index lists), checked against dense FP64 eigenvalues of the oracle.
+
+Tolerance: 1e-6 MeV on the ten lowest eigenvalues, the target of the solves
+the benchmark counts; with FP64 refinement the observed error is ~1e-12.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import jupiterncsm_gb300 as jn
+import oracle
+
+EIG_TOL = 1e-6
+
+
+def dense(d):
+    P = oracle.Port(d)
+    D = P.dimension
+    H = np.zeros((D, D))
+    for i in range(D):
+        e = np.zeros(D)
+        e[i] = 1.0
+        H[:, i] = P.matvec(e)
+    return H
+
+
+@pytest.fixture(scope="module")
+def family(tmp_path_factory):
+    """He4 Nmax 4 two-body: H0 (interaction + oscillator term) and H1 (another
+    seeded interaction, no oscillator term) on the same lists."""
+    root = tmp_path_factory.mktemp("family")
+    d0, d1 = str(root / "h0"), str(root / "h1")
+    jn.generate(d0, Z=2, N=2, nmax=4, nbody=2, basis_files=False)
+    jn.generate(d1, Z=2, N=2, nmax=4, nbody=2, seed=777, hbar_omega=0.0, basis_files=False)
+    return d0, d1, dense(d0), dense(d1)
+
+
+@pytest.mark.gpu
+def test_read_and_set_matrix_elements(family):
+    d0, d1, H0, H1 = family
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
+        assert me0.shape == (H.me_count(),) and not np.array_equal(me0, me1)
+        x = np.random.default_rng(3).standard_normal(H.dimension)
+        assert np.abs(H.matvec(x) - H0 @ x).max() <= 1e-12 * np.abs(H0 @ x).max()
+        H.set_matrix_elements(me0 + 0.5 * me1)
+        want = (H0 + 0.5 * H1) @ x
+        assert np.abs(H.matvec(x) - want).max() <= 1e-12 * np.abs(want).max()
+        H.set_precision(32)
+        assert np.abs(H.matvec(x) - want).max() <= 1e-6 * np.abs(want).max()
+    finally:
+        H.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [32, 64])
+def test_batch_matches_dense_eigenvalues(family, precision):
+    d0, d1, H0, H1 = family
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
+        cs = [0.0, 0.6, -0.8, 1.0, -0.3]
+        res = H.lanczos_batch([me0 + c * me1 for c in cs], precision=precision, num_eigenvalues=10,
+                              tolerance=1e-6, max_iterations=300)
+        for c, r in zip(cs, res):
+            want = np.linalg.eigvalsh(H0 + c * H1)[:10]
+            assert r["converged"], (c, r["iterations"])
+            assert len(r["eigenvalues"]) == 10
+            assert np.abs(r["eigenvalues"] - want).max() <= EIG_TOL, (c, r["eigenvalues"] - want)
+            assert r["residual_norms"].max() < 1e-2
+    finally:
+        H.close()
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_is_bit_identical(family):
+    d0, d1, H0, H1 = family
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
+        mes = [me0 + c * me1 for c in (0.2, -0.4, 0.9)]
+        a = H.lanczos_batch(mes, use_graph=True)
+        b = H.lanczos_batch(mes, use_graph=False)
+        for x, y in zip(a, b):
+            assert x["iterations"] == y["iterations"]
+            assert np.array_equal(x["eigenvalues"], y["eigenvalues"])
+    finally:
+        H.close()
+
+
+@pytest.mark.gpu
+def test_batch_ground_states_and_warm_start(family):
+    """Ground-state vectors come back normalised with the refined energy as their
+    Rayleigh quotient; started from them, a solve converges in fewer steps."""
+    d0, d1, H0, H1 = family
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
+        mes = [me0 + c * me1 for c in (0.1, 0.5)]
+        res, gs = H.lanczos_batch(mes, ground_states=True, num_eigenvalues=1, tolerance=1e-8)
+        for c, r, v in zip((0.1, 0.5), res, gs):
+            Hc = H0 + c * H1
+            assert abs(np.linalg.norm(v) - 1.0) < 1e-8
+            assert abs(v @ Hc @ v - r["eigenvalues"][0]) < 1e-7
+        warm = H.lanczos_batch(mes, start_vectors=gs, num_eigenvalues=1, tolerance=1e-8, check_every=2)
+        cold = H.lanczos_batch(mes, num_eigenvalues=1, tolerance=1e-8, check_every=2)
+        for w, c in zip(warm, cold):
+            assert w["converged"] and w["iterations"] < c["iterations"]
+    finally:
+        H.close()
+
+
+@pytest.mark.gpu
+def test_batch_rejects_bad_arguments(family):
+    d0 = family[0]
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        with pytest.raises(jn.JnError):
+            H.lanczos_batch([me0], precision=16)
+        with pytest.raises(jn.JnError):
+            H.read_matrix_elements(os.path.join(d0, "no_such_dir"))
+    finally:
+        H.close()
