@@ -274,7 +274,8 @@ typedef struct {
 	int check_every;                        /* convergence test interval in steps (default 10) */
 	int use_graph;                          /* replay one captured graph per step */
 	int refine_extra;                       /* extra Ritz vectors in the refinement (default 4) */
-	double *const *ground_states;           /* host, NULL or num_instances outputs of length D */
+	int num_eigenvectors;                   /* refined eigenvectors returned per instance (<= num_eigenvalues) */
+	double *const *eigenvectors;            /* host, num_instances outputs of num_eigenvectors x D (NULL entries skip) */
 } jn_batch_options;
 
 typedef struct {
@@ -353,6 +354,82 @@ jn_status jn_transform_2nf(const char *combination_table_file, const char *index
 /* <j1 m1 j2 m2 | j3 m3> with all arguments doubled, as clebsch_gordan
  * defines it (src/Neptune/clebsch_gordan/clebsch_gordan.c:31-42); host only. */
 double jn_clebsch_gordan(int j1, int j2, int j3, int m1, int m2, int m3);
+
+/* ------------------------------------------------------------------ */
+/* Learned warm start: an MLP from couplings c to a Lanczos start vector */
+/* ------------------------------------------------------------------ */
+/*
+ * A two-hidden-layer perceptron in FP32, trained and evaluated by the
+ * library's own CUDA kernels: x (num_inputs) -> gelu(W1 x + b1) (hidden) ->
+ * gelu(W2 h1 + b2) (hidden) -> W3 h2 + b3 (num_outputs), with
+ * gelu(a) = a (1 + erf(a / sqrt 2)) / 2.  Loss over n samples:
+ * sum_s |y_s - t_s|^2 / (2 n).  Parameters are one flat array
+ * [W1 (hidden x num_inputs), b1, W2 (hidden x hidden), b2,
+ * W3 (num_outputs x hidden), b3], row-major, output index first.  Gradients
+ * are summed over samples in sample order, so results repeat bit for bit.
+ * Adam (beta1 0.9, beta2 0.999, eps 1e-8) updates the parameters.  Samples
+ * are row-major: x is n x num_inputs, t and y are n x num_outputs.  No
+ * counterpart in the reference; the reduced-basis idea is that of Ceres
+ * (src/Ceres/programs/ceres.c:17-80), which projects operators onto
+ * vectors that earlier solves produced.
+ */
+typedef struct jn_mlp jn_mlp;
+
+jn_status jn_mlp_create(int num_inputs, int hidden, int num_outputs, uint64_t seed, jn_mlp **mlp);
+void jn_mlp_destroy(jn_mlp *mlp);
+size_t jn_mlp_num_params(const jn_mlp *mlp);
+jn_status jn_mlp_get_params(const jn_mlp *mlp, float *params);
+jn_status jn_mlp_set_params(jn_mlp *mlp, const float *params);
+/* loss and its gradient (num_params values) of the current parameters */
+jn_status jn_mlp_loss_and_gradient(jn_mlp *mlp, const float *x, const float *t, int n, float *loss, float *grad);
+/* `steps` full-batch Adam steps; final_loss = the loss after the last step */
+jn_status jn_mlp_train(jn_mlp *mlp, const float *x, const float *t, int n, int steps, float learning_rate,
+		       float *final_loss);
+jn_status jn_mlp_predict(jn_mlp *mlp, const float *x, int n, float *y);
+
+/*
+ * The warm start for jn_lanczos_batch.  Fitting takes solutions that the
+ * solver produced for sample couplings c_s: for each sample its
+ * num_vectors lowest eigenvectors.  The target of sample s is the
+ * projection of the solver's default start vector r onto them,
+ * u_s = sum_e v_e (v_e . r) / |.|, which does not depend on the signs of the
+ * v_e and varies smoothly with c.  The reduced basis is the leading
+ * basis_size left singular vectors of [u_1 .. u_S] (from the S x S Gram
+ * matrix, computed on the GPU).  The MLP learns the coordinates of u_s in
+ * that basis from c_s.  A start vector for new couplings is the expansion of
+ * the predicted coordinates (a GPU kernel), normalised, plus noise * r / |r|
+ * so that no eigenvector can be missing from the Krylov space.  Cold-start
+ * Lanczos (start vector r) stays the judge: the warm start only changes
+ * where the iteration begins.
+ */
+typedef struct jn_warm_start jn_warm_start;
+
+typedef struct {
+	int hidden;             /* hidden width (default 128) */
+	int basis_size;         /* reduced-basis size = MLP outputs (default 32, <= num_samples) */
+	int train_steps;        /* full-batch Adam steps (default 3000) */
+	float learning_rate;    /* default 1e-3 */
+	uint64_t seed;          /* MLP initialisation */
+	double noise;           /* weight of r in every start vector (default 0.01) */
+} jn_warm_start_options;
+
+/* couplings: num_samples x num_couplings (host, row-major); eigenvectors:
+ * num_samples host arrays of num_vectors x dim values (the
+ * jn_batch_options.eigenvectors layout).  num_samples <= 2048. */
+jn_status jn_warm_start_fit(const jn_warm_start_options *options, int64_t dim, int num_couplings, int num_samples,
+			    const double *couplings, int num_vectors, const double *const *eigenvectors,
+			    jn_warm_start **warm_start, float *final_loss);
+/* n start vectors (host arrays of dim values) for couplings (n x num_couplings) */
+jn_status jn_warm_start_vectors(jn_warm_start *warm_start, int n, const double *couplings,
+				double *const *start_vectors);
+/* the basis_size reduced-basis vectors (basis_size x dim, host) */
+jn_status jn_warm_start_basis(const jn_warm_start *warm_start, double *basis);
+int jn_warm_start_basis_size(const jn_warm_start *warm_start);
+void jn_warm_start_destroy(jn_warm_start *warm_start);
+
+/* The solver's default start vector (what jn_lanczos_batch uses when
+ * start_vectors is NULL), dim values, host. */
+void jn_default_start_vector(int64_t dim, double *out);
 
 #ifdef __cplusplus
 }

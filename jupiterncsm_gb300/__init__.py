@@ -59,7 +59,7 @@ class BatchOptions(ctypes.Structure):
                 ("start_vectors", ctypes.c_void_p), ("max_iterations", ctypes.c_int),
                 ("num_eigenvalues", ctypes.c_int), ("tolerance", ctypes.c_double), ("precision", ctypes.c_int),
                 ("check_every", ctypes.c_int), ("use_graph", ctypes.c_int), ("refine_extra", ctypes.c_int),
-                ("ground_states", ctypes.c_void_p)]
+                ("num_eigenvectors", ctypes.c_int), ("eigenvectors", ctypes.c_void_p)]
 
 
 class BatchResult(ctypes.Structure):
@@ -73,6 +73,11 @@ class TransformStats(ctypes.Structure):
                 ("num_elements", ctypes.c_size_t), ("num_pair_states", ctypes.c_size_t),
                 ("num_configurations", ctypes.c_size_t), ("dense_flops", ctypes.c_double),
                 ("algorithmic_bytes", ctypes.c_double), ("plan_seconds", ctypes.c_double)]
+
+
+class WarmStartOptions(ctypes.Structure):
+    _fields_ = [("hidden", ctypes.c_int), ("basis_size", ctypes.c_int), ("train_steps", ctypes.c_int),
+                ("learning_rate", ctypes.c_float), ("seed", ctypes.c_uint64), ("noise", ctypes.c_double)]
 
 
 class LanczosOptions(ctypes.Structure):
@@ -140,6 +145,30 @@ def gpu_lib():
     L.jn_transform_2nf.argtypes = [cp, cp, cp, ci, ci, ci, ci, cp, ci]
     L.jn_clebsch_gordan.argtypes = [ci] * 6
     L.jn_clebsch_gordan.restype = ctypes.c_double
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.jn_mlp_create.argtypes = [ci, ci, ci, ctypes.c_uint64, ctypes.POINTER(vp)]
+    L.jn_mlp_destroy.argtypes = [vp]
+    L.jn_mlp_destroy.restype = None
+    L.jn_mlp_num_params.argtypes = [vp]
+    L.jn_mlp_num_params.restype = csz
+    L.jn_mlp_get_params.argtypes = [vp, vp]
+    L.jn_mlp_set_params.argtypes = [vp, vp]
+    L.jn_mlp_loss_and_gradient.argtypes = [vp, vp, vp, ci, fp, vp]
+    L.jn_mlp_train.argtypes = [vp, vp, vp, ci, ci, ctypes.c_float, fp]
+    L.jn_mlp_predict.argtypes = [vp, vp, ci, vp]
+    L.jn_warm_start_fit.argtypes = [ctypes.POINTER(WarmStartOptions), ctypes.c_int64, ci, ci, vp, ci, vp,
+                                    ctypes.POINTER(vp), fp]
+    L.jn_warm_start_vectors.argtypes = [vp, ci, vp, vp]
+    L.jn_warm_start_basis.argtypes = [vp, vp]
+    L.jn_warm_start_basis_size.argtypes = [vp]
+    L.jn_warm_start_destroy.argtypes = [vp]
+    L.jn_warm_start_destroy.restype = None
+    L.jn_default_start_vector.argtypes = [ctypes.c_int64, vp]
+    L.jn_default_start_vector.restype = None
+    for name in ("jn_mlp_create", "jn_mlp_get_params", "jn_mlp_set_params", "jn_mlp_loss_and_gradient",
+                 "jn_mlp_train", "jn_mlp_predict", "jn_warm_start_fit", "jn_warm_start_vectors",
+                 "jn_warm_start_basis"):
+        getattr(L, name).restype = ci
     for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
                  "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_set_engine", "jn_lanczos",
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
@@ -244,24 +273,24 @@ class Hamiltonian:
 
     def lanczos_batch(self, matrix_elements, start_vectors=None, max_iterations=200, num_eigenvalues=10,
                       tolerance=1e-6, precision=32, check_every=10, use_graph=True, refine_extra=4,
-                      ground_states=False):
-        """Solve len(matrix_elements) Hamiltonians on these lists together; returns a list of dicts
-        (and the ground-state vectors when ground_states)."""
+                      eigenvectors=0):
+        """Solve len(matrix_elements) Hamiltonians on these lists together; returns a list of dicts, and
+        with eigenvectors=k also, per instance, the k lowest refined eigenvectors as a (k, D) array."""
         B = len(matrix_elements)
         mes = [np.ascontiguousarray(m, dtype=np.float64) for m in matrix_elements]
         me_ptrs = (ctypes.c_void_p * B)(*[m.ctypes.data for m in mes])
         o = BatchOptions(B, ctypes.cast(me_ptrs, ctypes.c_void_p), None, max_iterations, num_eigenvalues, tolerance,
-                         precision, check_every, int(use_graph), refine_extra, None)
+                         precision, check_every, int(use_graph), refine_extra, int(eigenvectors), None)
         svs = None
         if start_vectors is not None:
             svs = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in start_vectors]
             sv_ptrs = (ctypes.c_void_p * B)(*[None if v is None else v.ctypes.data for v in svs])
             o.start_vectors = ctypes.cast(sv_ptrs, ctypes.c_void_p)
         gs = None
-        if ground_states:
-            gs = [np.zeros(self.dimension) for _ in range(B)]
+        if eigenvectors:
+            gs = [np.zeros((eigenvectors, self.dimension)) for _ in range(B)]
             gs_ptrs = (ctypes.c_void_p * B)(*[g.ctypes.data for g in gs])
-            o.ground_states = ctypes.cast(gs_ptrs, ctypes.c_void_p)
+            o.eigenvectors = ctypes.cast(gs_ptrs, ctypes.c_void_p)
         res = (BatchResult * B)()
         _check(gpu_lib().jn_lanczos_batch(self._h, ctypes.byref(o), res))
         out = []
@@ -270,7 +299,7 @@ class Hamiltonian:
             out.append({"iterations": r.iterations, "converged": bool(r.converged),
                         "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
                         "residual_norms": np.array(r.residual_norms[:n])})
-        return (out, gs) if ground_states else out
+        return (out, gs) if eigenvectors else out
 
     def ritz_values(self):
         cap = 4096
@@ -309,6 +338,125 @@ class Hamiltonian:
             i, o, n = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()
             _check(L.jn_block_info(self._h, b, ctypes.byref(i), ctypes.byref(o), ctypes.byref(n)))
             out.append((i.value, o.value, n.value))
+        return out
+
+
+def _f32(a, cols):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim == 1:
+        a = a.reshape(1, -1)
+    assert a.shape[1] == cols, (a.shape, cols)
+    return a
+
+
+class MLP:
+    """The warm start's perceptron, trained and evaluated by the library's CUDA kernels (jn_mlp_*)."""
+
+    def __init__(self, num_inputs, hidden, num_outputs, seed=0):
+        self.shape = (num_inputs, hidden, num_outputs)
+        self._h = ctypes.c_void_p()
+        _check(gpu_lib().jn_mlp_create(num_inputs, hidden, num_outputs, seed, ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            gpu_lib().jn_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self):
+        return gpu_lib().jn_mlp_num_params(self._h)
+
+    def params(self):
+        p = np.zeros(self.num_params, dtype=np.float32)
+        _check(gpu_lib().jn_mlp_get_params(self._h, p.ctypes.data))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (self.num_params,)
+        _check(gpu_lib().jn_mlp_set_params(self._h, p.ctypes.data))
+
+    def loss_and_gradient(self, x, t):
+        x, t = _f32(x, self.shape[0]), _f32(t, self.shape[2])
+        loss = ctypes.c_float()
+        g = np.zeros(self.num_params, dtype=np.float32)
+        _check(gpu_lib().jn_mlp_loss_and_gradient(self._h, x.ctypes.data, t.ctypes.data, len(x), ctypes.byref(loss),
+                                                  g.ctypes.data))
+        return loss.value, g
+
+    def train(self, x, t, steps, learning_rate=1e-3):
+        x, t = _f32(x, self.shape[0]), _f32(t, self.shape[2])
+        loss = ctypes.c_float()
+        _check(gpu_lib().jn_mlp_train(self._h, x.ctypes.data, t.ctypes.data, len(x), int(steps),
+                                      ctypes.c_float(learning_rate), ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, x):
+        x = _f32(x, self.shape[0])
+        y = np.zeros((len(x), self.shape[2]), dtype=np.float32)
+        _check(gpu_lib().jn_mlp_predict(self._h, x.ctypes.data, len(x), y.ctypes.data))
+        return y
+
+
+def default_start_vector(dim):
+    """The batched solver's default start vector (jn_default_start_vector)."""
+    v = np.zeros(dim)
+    gpu_lib().jn_default_start_vector(int(dim), v.ctypes.data)
+    return v
+
+
+class WarmStart:
+    """Learned warm start for Hamiltonian.lanczos_batch (jn_warm_start_*): fitted on couplings and the
+    eigenvectors the solver returned for them; gives start vectors for new couplings."""
+
+    def __init__(self, couplings, eigenvectors, hidden=128, basis_size=32, train_steps=3000, learning_rate=1e-3,
+                 seed=0, noise=0.01):
+        c = np.ascontiguousarray(couplings, dtype=np.float64)
+        S, nc = c.shape
+        ev = [np.ascontiguousarray(v, dtype=np.float64) for v in eigenvectors]
+        assert len(ev) == S and all(v.shape == ev[0].shape for v in ev)
+        nv, dim = ev[0].shape
+        ptrs = (ctypes.c_void_p * S)(*[v.ctypes.data for v in ev])
+        o = WarmStartOptions(hidden, basis_size, train_steps, learning_rate, seed, noise)
+        self._h = ctypes.c_void_p()
+        loss = ctypes.c_float()
+        _check(gpu_lib().jn_warm_start_fit(ctypes.byref(o), dim, nc, S, c.ctypes.data, nv,
+                                           ctypes.cast(ptrs, ctypes.c_void_p), ctypes.byref(self._h),
+                                           ctypes.byref(loss)))
+        self.final_loss = loss.value
+        self.dim, self.num_couplings = dim, nc
+
+    def close(self):
+        if self._h:
+            gpu_lib().jn_warm_start_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def basis_size(self):
+        return gpu_lib().jn_warm_start_basis_size(self._h)
+
+    def basis(self):
+        b = np.zeros((self.basis_size, self.dim))
+        _check(gpu_lib().jn_warm_start_basis(self._h, b.ctypes.data))
+        return b
+
+    def start_vectors(self, couplings):
+        c = np.ascontiguousarray(couplings, dtype=np.float64).reshape(-1, self.num_couplings)
+        out = [np.zeros(self.dim) for _ in range(len(c))]
+        ptrs = (ctypes.c_void_p * len(c))(*[v.ctypes.data for v in out])
+        _check(gpu_lib().jn_warm_start_vectors(self._h, len(c), c.ctypes.data, ctypes.cast(ptrs, ctypes.c_void_p)))
         return out
 
 

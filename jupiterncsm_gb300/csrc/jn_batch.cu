@@ -262,17 +262,19 @@ __global__ void __launch_bounds__(BT) kb_gram(const double *__restrict__ A, cons
 	if (threadIdx.x == 0) G[((int64_t)inst * r + i) * r + j] = s;
 }
 
-/* out[inst] = sum_j X[inst][j] C[inst][j] */
-__global__ void kb_combine(const double *__restrict__ X, const double *__restrict__ C, int r, int64_t D,
+/* out[inst][e] = sum_j X[inst][j] C[inst][e][j], e < nv: the refined vectors */
+__global__ void kb_combine(const double *__restrict__ X, const double *__restrict__ C, int r, int nv, int64_t D,
 			   double *__restrict__ out)
 {
 	const int inst = blockIdx.y;
-	const double *x = X + (int64_t)inst * r * D, *c = C + (int64_t)inst * r;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
-		double s = 0.0;
-		for (int j = 0; j < r; j++) s = fma(x[(int64_t)j * D + i], c[j], s);
-		out[inst * D + i] = s;
-	}
+	const double *x = X + (int64_t)inst * r * D;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+		for (int e = 0; e < nv; e++) {
+			const double *c = C + ((int64_t)inst * r + e) * r;
+			double s = 0.0;
+			for (int j = 0; j < r; j++) s = fma(x[(int64_t)j * D + i], c[j], s);
+			out[((int64_t)inst * nv + e) * D + i] = s;
+		}
 }
 
 /* ------------------------------------------------------------------ */
@@ -342,10 +344,11 @@ static void jacobi_eigen(double *S, int r, double *w, double *Q)
 	}
 }
 
-/* refined values lam[0..r), residual norms res[] and the coefficients c0 of
- * the lowest refined vector, from G1 = X^T X, G2 = X^T H X, G3 = (HX)^T HX */
+/* refined values lam[0..r), residual norms res[] and the coefficients of
+ * the refined vectors (row e of cv, row length ldc, when cv is not NULL),
+ * from G1 = X^T X, G2 = X^T H X, G3 = (HX)^T HX */
 static int rayleigh_ritz(const double *G1, const double *G2, const double *G3, int r, double *lam, double *res,
-			 double *c0)
+			 double *cv, int ldc)
 {
 	double *L = (double *)malloc(sizeof(double) * r * r), *S = (double *)malloc(sizeof(double) * r * r);
 	double *Q = (double *)malloc(sizeof(double) * r * r), *T = (double *)malloc(sizeof(double) * r * r);
@@ -385,7 +388,7 @@ static int rayleigh_ritz(const double *G1, const double *G2, const double *G3, i
 				}
 			double r2 = h2 - 2.0 * lam[e] * hx + lam[e] * lam[e] * xx;
 			res[e] = sqrt(fmax(r2, 0.0) / fmax(xx, 1e-300));
-			if (e == 0 && c0) memcpy(c0, c, sizeof(double) * r);
+			if (cv) memcpy(cv + (size_t)e * ldc, c, sizeof(double) * r);
 		}
 	}
 	free(L); free(S); free(Q); free(T); free(c);
@@ -435,6 +438,9 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	int r = nev + extra;
 	if (r > m) r = m;
 	const int check_every = o->check_every > 0 ? o->check_every : 10;
+	if (o->num_eigenvectors < 0 || o->num_eigenvectors > nev || (o->num_eigenvectors && !o->eigenvectors))
+		return jn_fail(JN_ERR_INVALID, "num_eigenvectors must be in 0..num_eigenvalues with an output array");
+	const int nvo = o->num_eigenvectors;
 	const int f32 = o->precision == 32;
 	const int want = nev + 1 < m ? nev + 1 : m;
 	const int ldz = m + 1;
@@ -498,15 +504,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	for (int i = 0; i < B && !st; i++) {
 		const double *sv = o->start_vectors ? o->start_vectors[i] : NULL;
 		if (!sv) {
-			uint64_t z = 0x9E3779B97F4A7C15ull;
-			for (int64_t e = 0; e < D; e++) {
-				z += 0x9E3779B97F4A7C15ull;
-				uint64_t v = z;
-				v = (v ^ (v >> 30)) * 0xBF58476D1CE4E5B9ull;
-				v = (v ^ (v >> 27)) * 0x94D049BB133111EBull;
-				v ^= v >> 31;
-				hv[e] = (double)(v >> 11) * 0x1.0p-53 - 0.5;
-			}
+			jn_default_start_vector(D, hv);
 			sv = hv;
 		}
 		if (cudaMemcpy(s.V + (size_t)i * ldV, sv, D * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -602,8 +600,8 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		BALLOC(s.X, (size_t)B * r * D);
 		BALLOC(s.HX, (size_t)B * r * D);
 		BALLOC(s.G, (size_t)B * 3 * r * r);
-		BALLOC(s.C, (size_t)B * r);
-		if (o->ground_states) BALLOC(s.GS, (size_t)B * D);
+		BALLOC(s.C, (size_t)B * r * r);
+		if (nvo) BALLOC(s.GS, (size_t)B * nvo * D);
 	}
 	double *hG = NULL;
 	if (!st) {
@@ -630,7 +628,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		    cudaMemcpyAsync(hth, s.theta, sizeof(double) * B * (r + 1), cudaMemcpyDeviceToHost, q) != cudaSuccess ||
 		    cudaStreamSynchronize(q) != cudaSuccess)
 			st = jn_fail(JN_ERR_CUDA, "refinement: %s", cudaGetErrorString(cudaGetLastError()));
-		double *hC = (double *)calloc((size_t)B * r, sizeof(double));
+		double *hC = (double *)calloc((size_t)B * r * r, sizeof(double));
 		double *lam = (double *)malloc(sizeof(double) * r), *rn = (double *)malloc(sizeof(double) * r);
 		for (int i = 0; i < B && !st; i++) {
 			const int ri = hn[i] < r ? hn[i] : r;
@@ -643,7 +641,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 								 hG[(size_t)B * r * r + ((size_t)i * r + b2) * r + a]);
 					G3[a * ri + b2] = hG[(size_t)2 * B * r * r + ((size_t)i * r + a) * r + b2];
 				}
-			if (rayleigh_ritz(G1, G2, G3, ri, lam, rn, hC + (size_t)i * r))
+			if (rayleigh_ritz(G1, G2, G3, ri, lam, rn, hC + (size_t)i * r * r, r))
 				st = jn_fail(JN_ERR_NOT_CONVERGED, "instance %d: Ritz vectors are not independent", i);
 			res[i].num_eigenvalues = nev < ri ? nev : ri;
 			for (int e = 0; e < res[i].num_eigenvalues; e++) {
@@ -653,15 +651,15 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 			}
 			free(G1); free(G2); free(G3);
 		}
-		if (!st && o->ground_states) {
-			cudaMemcpyAsync(s.C, hC, sizeof(double) * B * r, cudaMemcpyHostToDevice, q);
-			kb_combine<<<gv, BT, 0, q>>>(s.X, s.C, r, D, s.GS);
+		if (!st && nvo) {
+			cudaMemcpyAsync(s.C, hC, sizeof(double) * B * r * r, cudaMemcpyHostToDevice, q);
+			kb_combine<<<gv, BT, 0, q>>>(s.X, s.C, r, nvo, D, s.GS);
 			for (int i = 0; i < B && !st; i++)
-				if (o->ground_states[i] &&
-				    cudaMemcpyAsync(o->ground_states[i], s.GS + (size_t)i * D, D * sizeof(double),
+				if (o->eigenvectors[i] &&
+				    cudaMemcpyAsync(o->eigenvectors[i], s.GS + (size_t)i * nvo * D, (size_t)nvo * D * sizeof(double),
 						    cudaMemcpyDeviceToHost, q) != cudaSuccess)
-					st = jn_fail(JN_ERR_CUDA, "ground-state copy");
-			if (!st && cudaStreamSynchronize(q) != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "ground-state copy");
+					st = jn_fail(JN_ERR_CUDA, "eigenvector copy");
+			if (!st && cudaStreamSynchronize(q) != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "eigenvector copy");
 		}
 		free(hC); free(lam); free(rn); free(hth);
 	}

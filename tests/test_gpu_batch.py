@@ -104,7 +104,8 @@ def test_batch_ground_states_and_warm_start(family):
         me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
         me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
         mes = [me0 + c * me1 for c in (0.1, 0.5)]
-        res, gs = H.lanczos_batch(mes, ground_states=True, num_eigenvalues=1, tolerance=1e-8)
+        res, vecs = H.lanczos_batch(mes, eigenvectors=1, num_eigenvalues=1, tolerance=1e-8)
+        gs = [v[0] for v in vecs]
         for c, r, v in zip((0.1, 0.5), res, gs):
             Hc = H0 + c * H1
             assert abs(np.linalg.norm(v) - 1.0) < 1e-8
@@ -113,6 +114,22 @@ def test_batch_ground_states_and_warm_start(family):
         cold = H.lanczos_batch(mes, num_eigenvalues=1, tolerance=1e-8, check_every=2)
         for w, c in zip(warm, cold):
             assert w["converged"] and w["iterations"] < c["iterations"]
+    finally:
+        H.close()
+
+
+@pytest.mark.gpu
+def test_batch_returns_orthonormal_low_lying_vectors(family):
+    d0, d1, H0, H1 = family
+    H = jn.Hamiltonian.from_dir(d0, 2, 2)
+    try:
+        me0 = H.read_matrix_elements(os.path.join(d0, "matrix_elements"))
+        me1 = H.read_matrix_elements(os.path.join(d1, "matrix_elements"))
+        res, vecs = H.lanczos_batch([me0 - 0.4 * me1], eigenvectors=5, num_eigenvalues=5, tolerance=1e-8)
+        X = vecs[0]
+        Hc = H0 - 0.4 * H1
+        assert np.abs(X @ X.T - np.eye(5)).max() < 1e-8
+        assert np.abs(np.diag(X @ Hc @ X.T) - res[0]["eigenvalues"]).max() < 1e-7
     finally:
         H.close()
 
