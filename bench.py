@@ -259,14 +259,7 @@ def solves_leg(workdir, seed=20261203):
     iters_plain, iters_batch = [], []
     details = []
     for bi, (label, Z, N, nmax, M2) in enumerate(SOLVE_FAMILY):
-        d = os.path.join(workdir, f"family_{Z}_{N}_{nmax}_{M2}")
-        stamp = os.path.join(d, ".complete")
-        if not os.path.exists(stamp):
-            jn.generate(os.path.join(d, "h0"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, basis_files=False)
-            for i in range(1, SOLVE_COUPLINGS + 1):
-                jn.generate(os.path.join(d, f"h{i}"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, seed=seed + 1000 * i,
-                            hbar_omega=0.0, basis_files=False)
-            open(stamp, "w").write("ok\n")
+        d = family_dir(workdir, Z, N, nmax, M2, seed)
         H = jn.Hamiltonian.from_dir(os.path.join(d, "h0"), Z, N)
         comps = [H.read_matrix_elements(os.path.join(d, f"h{i}", "matrix_elements"))
                  for i in range(SOLVE_COUPLINGS + 1)]
@@ -306,6 +299,86 @@ def solves_leg(workdir, seed=20261203):
                        "CUDA graph per step, convergence checked every 10 steps",
             "plain": "jn_lanczos full mode, FP64 products, convergence checked every step",
             "per_basis": details}
+
+
+WARM_BASIS = ("6Li Nmax=4", 3, 3, 4, 2)
+WARM_TRAIN, WARM_TEST, WARM_PLAIN = 256, 64, 16
+
+
+def family_dir(workdir, Z, N, nmax, M2, seed=20261203):
+    """H0 and the couplings' operators H_1..H_4 of one basis (generated once)."""
+    import jupiterncsm_gb300 as jn
+    d = os.path.join(workdir, f"family_{Z}_{N}_{nmax}_{M2}")
+    stamp = os.path.join(d, ".complete")
+    if not os.path.exists(stamp):
+        jn.generate(os.path.join(d, "h0"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, basis_files=False)
+        for i in range(1, SOLVE_COUPLINGS + 1):
+            jn.generate(os.path.join(d, f"h{i}"), Z=Z, N=N, nmax=nmax, M2=M2, nbody=2, seed=seed + 1000 * i,
+                        hbar_omega=0.0, basis_files=False)
+        open(stamp, "w").write("ok\n")
+    return d
+
+
+def warm_start_leg(workdir, seed=20261203, check_every=5):
+    """The learned warm start (6Li Nmax=4, 4 couplings): 256 training solves by
+    the batched solver give the snapshots; the MLP is trained on the GPU; 64
+    held-out Hamiltonians are solved from the default start and from the
+    network's start vectors.  Plain FP64 Lanczos on 16 of the held-out ones
+    gives the per-solve time of the plain method and the eigenvalue oracle."""
+    import numpy as np
+    import jupiterncsm_gb300 as jn
+    label, Z, N, nmax, M2 = WARM_BASIS
+    d = family_dir(workdir, Z, N, nmax, M2, seed)
+    rng = np.random.default_rng(seed + 77)
+    cs = rng.uniform(-1.0, 1.0, size=(WARM_TRAIN + WARM_TEST, SOLVE_COUPLINGS))
+    H = jn.Hamiltonian.from_dir(os.path.join(d, "h0"), Z, N)
+    try:
+        comps = [H.read_matrix_elements(os.path.join(d, f"h{i}", "matrix_elements"))
+                 for i in range(SOLVE_COUPLINGS + 1)]
+        mes = [comps[0] + sum(c[i] * comps[i + 1] for i in range(SOLVE_COUPLINGS)) for c in cs]
+        t0 = time.perf_counter()
+        _, vecs = H.lanczos_batch(mes[:WARM_TRAIN], max_iterations=300, num_eigenvalues=10, tolerance=1e-6,
+                                  eigenvectors=10, check_every=check_every)
+        t1 = time.perf_counter()
+        ws = jn.WarmStart(cs[:WARM_TRAIN], vecs, hidden=128, basis_size=32, train_steps=3000, seed=0)
+        t2 = time.perf_counter()
+        del vecs
+        test = mes[WARM_TRAIN:]
+        starts = ws.start_vectors(cs[WARM_TRAIN:])
+        t3 = time.perf_counter()
+        cold = H.lanczos_batch(test, max_iterations=300, num_eigenvalues=10, tolerance=1e-6, check_every=check_every)
+        t4 = time.perf_counter()
+        warm = H.lanczos_batch(test, start_vectors=starts, max_iterations=300, num_eigenvalues=10, tolerance=1e-6,
+                               check_every=check_every)
+        t5 = time.perf_counter()
+        plain = []
+        for me in test[:WARM_PLAIN]:
+            H.set_matrix_elements(me)
+            plain.append(H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, allow_unconverged=True))
+        t6 = time.perf_counter()
+        ws.close()
+    finally:
+        H.close()
+    err_w = max(float(np.abs(w["eigenvalues"] - p["eigenvalues"]).max()) for w, p in zip(warm, plain))
+    err_c = max(float(np.abs(c["eigenvalues"] - p["eigenvalues"]).max()) for c, p in zip(cold, plain))
+    plain_per = (t6 - t5) / WARM_PLAIN
+    return {"workload": f"{label}: H(c)=H0+sum_{{i=1..{SOLVE_COUPLINGS}}} c_i H_i, c~U(-1,1); MLP "
+                        f"{SOLVE_COUPLINGS}->128->128->32 (GELU) trained on {WARM_TRAIN} solves, {WARM_TEST} held out",
+            "dimension": int(len(starts[0])),
+            "snapshot_solves_seconds": t1 - t0, "fit_seconds": t2 - t1, "start_vectors_seconds": t3 - t2,
+            "final_training_loss": ws.final_loss,
+            "cold_batched_solves_per_s": WARM_TEST / (t4 - t3),
+            "warm_batched_solves_per_s": WARM_TEST / (t5 - t4 + t3 - t2),
+            "plain_fp64_solves_per_s": 1.0 / plain_per,
+            "warm_batched_vs_plain_fp64": plain_per * WARM_TEST / (t5 - t4 + t3 - t2),
+            "mean_iterations": {"cold": float(np.mean([c["iterations"] for c in cold])),
+                                "warm": float(np.mean([w["iterations"] for w in warm])),
+                                "plain_fp64": float(np.mean([p["iterations"] for p in plain]))},
+            "max_eigenvalue_diff_vs_plain_fp64_MeV": {"warm": err_w, "cold": err_c},
+            "all_converged": all(r["converged"] for r in cold + warm),
+            "check_every": check_every,
+            "note": "warm time includes computing the start vectors; plain FP64 timed on "
+                    f"{WARM_PLAIN} of the held-out Hamiltonians"}
 
 
 def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
@@ -503,6 +576,10 @@ def main():
             line["solves"] = solves_leg(wd)
         except Exception as e:  # the solves leg must never hide the matvec line
             line["solves"] = {"error": str(e)}
+        try:
+            line["warm_start"] = warm_start_leg(wd)
+        except Exception as e:
+            line["warm_start"] = {"error": str(e)}
     if rank == 0:
         try:
             line["cpu_baseline"] = cpu_baseline(d, w, bytes_for(64), seconds=args.cpu_seconds)

@@ -143,9 +143,13 @@ jn_status jn_matvec_profile(jn_ctx *ctx, const double *d_x, double *d_y, int acc
  * FP32 copy, which is the reference's skip (matrix_vector_multiplication.c:52-53). */
 jn_status jn_set_precision(jn_ctx *ctx, int precision);
 
-/* Product engine: 3 (default) — shared-memory block tiles with exact 64-bit
- * fixed-point sums (bit-identical results whatever the execution order);
- * 2 — one warp per 32-element piece, FP64 sums in fixed term order. */
+/* Product engine: 4 (default when the dimension is at most 28 672) — panels:
+ * every instruction's referenced matrix elements, signs applied, stored
+ * densely and streamed once, with the whole of y accumulated in shared
+ * memory as exact 64-bit fixed-point integers; 3 (default above that) —
+ * shared-memory block tiles with exact 64-bit fixed-point sums; both give
+ * bit-identical results whatever the execution order; 2 — one warp per
+ * 32-element piece, FP64 sums in fixed term order. */
 jn_status jn_set_engine(jn_ctx *ctx, int engine);
 
 /* Synchronise the context's stream. */

@@ -50,6 +50,12 @@ struct jn_ctx {
 	unsigned long long *d_gacc;     /* 64-bit fixed-point accumulator, zero between products */
 	unsigned int *d_xmax;           /* [0] max|x| of the current product (FP32 bits), [1] tile counter */
 	struct jn_lanczos_state *lz;
+	/* panel engine (engine 4, jn_panel.cu) */
+	jn_panel_t *d_panels;
+	uint32_t *d_ptasks, *d_pcta, *d_pflush, *d_pflush_ptr, *d_pmeta;
+	double *d_coef64;               /* panel coefficients, built on first FP64 use */
+	float *d_coef32;                /* and on first FP32 use */
+	int panel_grid;                 /* persistent CTAs; 0 until set up */
 };
 
 /* enqueue y (+)= H x on stream st */
@@ -72,6 +78,20 @@ jn_status jn_enqueue_batched(jn_ctx *c, int B, int f32, const void *me, int64_t 
 			     int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y, int64_t y_ld, double *x64,
 			     float *x32, unsigned long long *gacc, unsigned int *ctrl, const int *d_active, double abs_bound,
 			     cudaStream_t st);
+
+/* max|x| into ctrl[0] (zeroed before) and the optional FP32 copy of x */
+void jn_launch_prep(const double *d_x, float *x32, int64_t n, unsigned int *ctrl, cudaStream_t st);
+/* y (+)= gacc * 2^-S with S from ctrl[0]; gacc is cleared */
+void jn_launch_finalize(unsigned long long *gacc, double *d_y, int64_t n, const unsigned int *ctrl, double abs_bound,
+			int accumulate, cudaStream_t st);
+
+/* panel engine (jn_panel.cu): plan upload, coefficient reset after new
+ * matrix elements, release, and the product on the context's scratch */
+jn_status jn_panels_setup(jn_ctx *c);
+void jn_panels_invalidate(jn_ctx *c);
+void jn_panels_release(jn_ctx *c);
+jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
+			    cudaEvent_t mid);
 
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);

@@ -30,6 +30,7 @@
 #include <sys/stat.h>
 
 #include "jn_internal.h"
+#include "jn_fixed.cuh"
 
 #define JN_VERSION "jncsm-gb300 0.1"
 
@@ -207,18 +208,6 @@ __global__ void jn_to_f32_kernel(const double *__restrict__ x, float *__restrict
 /* ------------------------------------------------------------------ */
 #define TILE_THREADS 256
 
-/* exponent S of the fixed-point unit 2^-S: |y| <= abs_bound * max|x| <= 2^(62-S).
- * Integer arithmetic on the exponent field only, identical in every kernel. */
-__device__ __forceinline__ int fixed_exponent(unsigned int xmax_bits, double abs_bound)
-{
-	const double yb = abs_bound * (double)__uint_as_float(xmax_bits);
-	if (!(yb > 0.0)) return 0;
-	const long long bits = __double_as_longlong(yb);
-	int e = (int)((bits >> 52) & 0x7ff) - 1022;       /* yb < 2^e */
-	int S = 62 - e;
-	return S < -60 ? -60 : (S > 100 ? 100 : S);
-}
-
 /* x (FP64) -> optional FP32 copy, and max|x| into *xmax_bits (zeroed before) */
 __global__ void jn_prep_kernel(const double *__restrict__ x, float *__restrict__ x32, int64_t n,
 			       unsigned int *__restrict__ xmax_bits)
@@ -232,10 +221,6 @@ __global__ void jn_prep_kernel(const double *__restrict__ x, float *__restrict__
 	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
 	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(xmax_bits, __float_as_uint(m));
 }
-
-template <typename T> __device__ __forceinline__ long long to_fixed(T v);
-template <> __device__ __forceinline__ long long to_fixed<float>(float v) { return __float2ll_rn(v); }
-template <> __device__ __forceinline__ long long to_fixed<double>(double v) { return __double2ll_rn(v); }
 
 __device__ __forceinline__ int pow2_at_least(int v)
 {
@@ -255,20 +240,6 @@ __device__ __forceinline__ int pow2_at_least(int v)
  * 64-bit accumulator.  Integer addition is exact and associative, so the
  * result does not depend on the order in which warps and CTAs run.
  */
-/* 64-bit two's-complement add into separate low / high 32-bit shared words
- * with two native 32-bit atomics: the carry of each addition is taken from
- * the value its own atomic saw, so (high, low) holds the exact sum modulo
- * 2^64 once every addition has landed, whatever their interleaving. */
-__device__ __forceinline__ void add_fixed(unsigned int *lo, unsigned int *hi, int i, long long v)
-{
-	if (v == 0) return;
-	const unsigned int l = (unsigned int)(unsigned long long)v;
-	unsigned int h = (unsigned int)((unsigned long long)v >> 32);
-	const unsigned int old = atomicAdd(lo + i, l);
-	h += (unsigned int)(old + l < old);
-	if (h) atomicAdd(hi + i, h);
-}
-
 template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS) jn_tile_kernel(DevPlan P, const jn_btile_t *__restrict__ tiles, int ntiles,
 							       unsigned int *__restrict__ tile_counter,
@@ -473,6 +444,21 @@ __global__ void jn_finalize_kernel(unsigned long long *__restrict__ gacc, double
 	}
 }
 
+void jn_launch_prep(const double *d_x, float *x32, int64_t n, unsigned int *ctrl, cudaStream_t st)
+{
+	int g = (int)((n + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (n > 0) jn_prep_kernel<<<g, 256, 0, st>>>(d_x, x32, n, ctrl);
+}
+
+void jn_launch_finalize(unsigned long long *gacc, double *d_y, int64_t n, const unsigned int *ctrl, double abs_bound,
+			int accumulate, cudaStream_t st)
+{
+	int g = (int)((n + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (n > 0) jn_finalize_kernel<<<g, 256, 0, st>>>(gacc, d_y, n, ctrl, abs_bound, accumulate);
+}
+
 /* Batched products (instance = blockIdx.y).  The source vector of instance
  * i is src + i * src_ld + (*sel) * sel_ld: the Lanczos vector v_k of a batched
  * solve, with k read on the device so that a captured graph can be replayed
@@ -536,6 +522,7 @@ extern "C" void jn_close(jn_ctx *c)
 	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
 	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms); cudaFree(c->d_walks); cudaFree(c->d_items);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
+	jn_panels_release(c);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
 	jn_plan_free(&c->plan);
@@ -603,7 +590,12 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 		c->tile_grid = c->num_sms * per_sm;
 		if (c->tile_grid > p->nbtiles) c->tile_grid = p->nbtiles > 0 ? p->nbtiles : 1;
 	}
+	/* the panel engine where the whole accumulator fits in shared memory, else block tiles */
 	c->engine = 3;
+	if (p->dim <= JN_PANEL_MAX_DIM) {
+		if (jn_panels_setup(c) == JN_OK) c->engine = 4;
+		else jn_panels_release(c);
+	}
 	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
 	if (e != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
 	e = cudaMallocHost((void **)&c->h_pinned, (p->dim ? p->dim : 1) * sizeof(double));
@@ -754,6 +746,9 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		}
 		if (mid) cudaEventRecord(mid, st);
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
+	} else if (c->engine == 4) {
+		jn_status s = jn_enqueue_panels(c, d_x, d_y, accumulate, st, pre, mid);
+		if (s) return s;
 	} else {
 		jn_status s = jn_enqueue_tiles(c, d_x, d_y, accumulate, st, pre, mid, c->d_gacc, c->d_xmax, c->d_x32, 0);
 		if (s) return s;
@@ -765,7 +760,11 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 
 extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 {
-	if (!c || (engine != 2 && engine != 3)) return fail(JN_ERR_INVALID, "engine must be 2 or 3");
+	if (!c || engine < 2 || engine > 4) return fail(JN_ERR_INVALID, "engine must be 2, 3 or 4");
+	if (engine == 4) {
+		jn_status s = jn_panels_setup(c);
+		if (s) return s;
+	}
 	c->engine = engine;
 	return JN_OK;
 }

@@ -333,6 +333,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->terms); free(p->tiles); free(p->units); free(p->unit_terms);
 	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks); free(p->items);
 	free(p->term_dst);
+	jn_panels_free(p);
 	memset(p, 0, sizeof *p);
 }
 

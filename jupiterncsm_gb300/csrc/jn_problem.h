@@ -57,6 +57,7 @@ typedef struct {
 	int64_t ent_in;
 	int64_t walk_out, nwalk_out;    /* walks of the by-out view (first index, count) */
 	int64_t walk_in, nwalk_in;      /* walks of the by-in view */
+	int64_t pmeta;                  /* first packed entry in jn_plan_t.pmeta (by-out order) */
 } jn_list_t;
 
 typedef struct {
@@ -153,6 +154,33 @@ typedef struct {
 	int32_t pad0, pad1;
 } jn_tterm_t;
 
+/*
+ * Panel engine.  Each instruction is a panel of rows x columns: NP rows are
+ * the proton-list entries and columns the neutron-list entries, both in
+ * by-out order; an N instruction has the spectator proton rows and its
+ * neutron entries as columns; a P instruction its proton entries as rows and
+ * the spectator neutron columns.  The coefficient of (row j, column i) is
+ * s_p s_n M[k_n + Nd k_p] (NP), s_n M[k_n] (N, per column) or s_p M[k_p]
+ * (P, per row), with the single-species |M| < 1e-12 skip stored as 0.  NP
+ * coefficients are stored densely, row-major, so a product streams them
+ * once.  Forward: y[out + P_o Nn_out + N_o] += c x[in + P_i Nn_in + N_i];
+ * off-diagonal panels also add c x[out + P_o Nn_out + N_o] into
+ * y[in + P_i Nn_in + N_i].
+ */
+#define JN_PANEL_DIAG 8
+#define JN_PANEL_ITER 32        /* rows a lane walks per task */
+#define JN_PANEL_MAX_DIM 28672  /* the whole accumulator (8 B per state) lives in shared memory */
+
+typedef struct {
+	int64_t c_off;          /* first coefficient */
+	uint32_t row_meta;      /* first packed row entry (source | destination << 16) in pmeta (NP, P) */
+	uint32_t col_meta;      /* first packed column entry in pmeta (NP, N) */
+	int32_t out_off, in_off;        /* offsets of the output and input blocks */
+	int32_t Nn_out, Nn_in;
+	int32_t ncols, kind;    /* kind: JN_KIND_* | JN_PANEL_DIAG when input block == output block */
+	int32_t nrows, instr;   /* rows; the evaluation-order index of the instruction */
+} jn_panel_t;
+
 typedef struct {
 	/* problem */
 	int Z, N;
@@ -187,6 +215,14 @@ typedef struct {
 	int64_t me_elements;            /* sum of distinct ME block lengths */
 	int64_t me_referenced;          /* elements some list pair actually indexes */
 	double visits;                  /* multiply-adds per product (both directions) */
+	/* panel engine (built by jn_panels_build) */
+	int npanels;       jn_panel_t *panels;
+	int64_t nptasks;   uint32_t *ptasks;   /* 4 words per warp task: panel, j0, j1, i0 | log2(lanes per row) << 24 */
+	int pgrid;         uint32_t *pcta;     /* pgrid + 1 task offsets: CTA b runs [pcta[b], pcta[b+1]) */
+	uint32_t *pflush_ptr;                   /* pgrid + 1 offsets into pflush */
+	int64_t npflush;   uint32_t *pflush;   /* pairs {offset, length}: the ranges of y a CTA touches */
+	int64_t n_pmeta;   uint32_t *pmeta;
+	int64_t n_coef;                         /* coefficients of all panels */
 } jn_plan_t;
 
 typedef struct {
@@ -215,6 +251,12 @@ double jn_plan_abs_bound(const jn_plan_t *plan, const double *me);
 /* read the <id>_matrix_elements files of `dir` into out (plan->n_me values,
  * the plan's layout); every block must have the plan's dimensions */
 int jn_plan_read_me(const jn_plan_t *plan, const char *dir, double *out, char *err, size_t errlen);
+/* the panel plan for a persistent grid of `grid` CTAs (dimension <= JN_PANEL_MAX_DIM) */
+int jn_panels_build(jn_plan_t *plan, int grid, char *err, size_t errlen);
+void jn_panels_free(jn_plan_t *plan);
+/* panel coefficients from matrix elements in the plan's layout: FP64 into c64
+ * and/or FP32 into c32 (either may be NULL), n_coef values each */
+void jn_panels_coefficients(const jn_plan_t *plan, const double *me, double *c64, float *c32);
 
 #ifdef __cplusplus
 }

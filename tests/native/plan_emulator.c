@@ -262,3 +262,120 @@ void emu_task_stats(void *h, double *out)
 	out[0] = (double)P->npieces; out[1] = P->nbtiles; out[2] = lanes; out[3] = steps; out[4] = visits;
 	out[5] = kinds[0]; out[6] = kinds[1]; out[7] = kinds[2]; out[8] = kinds[3];
 }
+
+/* ------------------------------------------------------------------ */
+/* panel engine: CPU model of jn_panel_kernel, lane for lane, with every
+ * index checked.  Lane (r, c) of a task walks rows j0 + r, j0 + r + R, ...
+ * of column i0 + c, sums consecutive rows with one output row in T
+ * arithmetic and rounds each such run once; the transposed contribution of
+ * an off-diagonal panel is rounded per product.  The fixed-point sums are
+ * exact, so the model reproduces the GPU bit for bit. */
+static void panel_lane_model(const jn_plan_t *P, const jn_panel_t *pn, uint32_t j0, uint32_t j1, int R, int r, int i,
+			     const double *x64, const float *x32, const double *c64, const float *c32, int f32, int S,
+			     int64_t *acc)
+{
+	const int kind = pn->kind & 7, diag = (pn->kind & JN_PANEL_DIAG) != 0;
+	const double scale = ldexp(1.0, S);
+	const float scalef = (float)scale;
+	int Ni, No;
+	if (kind == JN_KIND_P) {
+		Ni = No = i;
+	} else {
+		CHECK((int64_t)pn->col_meta + i < P->n_pmeta);
+		const uint32_t m = P->pmeta[pn->col_meta + i];
+		Ni = (int)(m & 0xffffu);
+		No = (int)(m >> 16);
+	}
+	CHECK(Ni < pn->Nn_in && No < pn->Nn_out);
+	int cur = -1;
+	double run = 0;
+	float runf = 0;
+#define FLUSH_RUN() do { \
+		const int64_t at = pn->out_off + (int64_t)cur * pn->Nn_out + No; \
+		CHECK(at >= 0 && at < P->dim); \
+		acc[at] += f32 ? (int64_t)llrintf(runf * scalef) : (int64_t)llrint(run * scale); \
+	} while (0)
+	for (uint32_t j = j0 + r; j < j1; j += R) {
+		int Pi, Po;
+		int64_t ci;
+		if (kind == JN_KIND_N) {
+			Pi = Po = (int)j;
+			ci = pn->c_off + i;
+		} else {
+			CHECK((int64_t)pn->row_meta + j < P->n_pmeta);
+			const uint32_t m = P->pmeta[pn->row_meta + j];
+			Pi = (int)(m & 0xffffu);
+			Po = (int)(m >> 16);
+			ci = kind == JN_KIND_NP ? pn->c_off + (int64_t)j * pn->ncols + i : pn->c_off + j;
+		}
+		CHECK(ci >= 0 && ci < P->n_coef);
+		const int64_t xi_at = pn->in_off + (int64_t)Pi * pn->Nn_in + Ni, xo_at = pn->out_off + (int64_t)Po * pn->Nn_out + No;
+		CHECK(xi_at >= 0 && xi_at < P->dim && xo_at >= 0 && xo_at < P->dim);
+		if (Po != cur) {
+			if (cur >= 0) FLUSH_RUN();
+			cur = Po;
+			run = 0;
+			runf = 0;
+		}
+		if (f32) {
+			const float cv = c32[ci];
+			runf = fmaf(cv, x32[xi_at], runf);
+			if (!diag) {
+				float t = cv * x32[xo_at];
+				t = t * scalef;
+				acc[xi_at] += (int64_t)llrintf(t);
+			}
+		} else {
+			const double cv = c64[ci];
+			run = fma(cv, x64[xi_at], run);
+			if (!diag) {
+				double t = cv * x64[xo_at];
+				t = t * scale;
+				acc[xi_at] += (int64_t)llrint(t);
+			}
+		}
+	}
+	if (cur >= 0) FLUSH_RUN();
+#undef FLUSH_RUN
+}
+
+int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
+{
+	jn_plan_t *P = h;
+	char err[512];
+	emu_fail = 0;
+	if (!P->panels && jn_panels_build(P, 152 * 3, err, sizeof err)) {
+		fprintf(stderr, "plan emulator: %s\n", err);
+		return 1;
+	}
+	float xmax = 0;
+	float *x32 = malloc((P->dim ? P->dim : 1) * sizeof(float));
+	for (int64_t i = 0; i < P->dim; i++) {
+		x32[i] = (float)x[i];
+		float v = (float)fabs(x[i]) * 1.0000002f;
+		if (v > xmax) xmax = v;
+	}
+	double *c64 = f32 ? NULL : malloc((P->n_coef ? P->n_coef : 1) * sizeof(double));
+	float *c32 = f32 ? malloc((P->n_coef ? P->n_coef : 1) * sizeof(float)) : NULL;
+	jn_panels_coefficients(P, P->me, c64, c32);
+	const int S = fixed_exponent(xmax, P->abs_bound);
+	int64_t *acc = calloc(P->dim ? P->dim : 1, sizeof(int64_t));
+	/* every task once, every CTA's task range covering all of them */
+	if (P->pcta[0] != 0 || P->pcta[P->pgrid] != (uint32_t)P->nptasks) { emu_fail = 1; fprintf(stderr, "plan emulator: CTA ranges\n"); }
+	for (int64_t k = 0; k < P->nptasks && !emu_fail; k++) {
+		const uint32_t *T = P->ptasks + 4 * k;
+		if (T[0] >= (uint32_t)P->npanels) { emu_fail = 1; break; }
+		const jn_panel_t *pn = &P->panels[T[0]];
+		const int lg = (int)(T[3] >> 24), R = 32 >> lg;
+		if (lg > 5 || T[1] >= T[2] || T[2] > (uint32_t)pn->nrows) { emu_fail = 1; break; }
+		for (int lane = 0; lane < 32 && !emu_fail; lane++) {
+			const int i = (int)(T[3] & 0xffffffu) + (lane & ((1 << lg) - 1));
+			if (i >= pn->ncols) continue;
+			panel_lane_model(P, pn, T[1], T[2], R, lane >> lg, i, x, x32, c64, c32, f32, S, acc);
+		}
+	}
+	const double unit = ldexp(1.0, -S);
+	for (int64_t i = 0; i < P->dim; i++) y[i] = accumulate ? y[i] + (double)acc[i] * unit : (double)acc[i] * unit;
+	free(acc); free(x32); free(c64); free(c32);
+	return emu_fail;
+}

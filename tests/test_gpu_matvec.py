@@ -120,6 +120,7 @@ def test_block_tile_engine_is_exact_model(problem, name, bits):
     """The fixed-point engine gives bit for bit what its CPU model gives."""
     d, Z, N, *_ = problem(name)
     H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.set_engine(3)
     H.set_precision(bits)
     x = np.random.default_rng(21).standard_normal(H.dimension)
     got = H.matvec(x)
@@ -131,13 +132,63 @@ def test_block_tile_engine_is_exact_model(problem, name, bits):
     H.close()
 
 
+def emu4(d, Z, N, x, f32):
+    import ctypes
+    L = ctypes.CDLL(os.path.join(os.path.dirname(__file__), "_build", "libplan_emu.so"))
+    L.emu_open.restype = ctypes.c_void_p
+    L.emu_open.argtypes = [ctypes.c_char_p] * 4 + [ctypes.c_int] * 3 + [ctypes.c_char_p, ctypes.c_int]
+    L.emu_matvec4.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+    L.emu_close.argtypes = [ctypes.c_void_p]
+    err = ctypes.create_string_buffer(1024)
+    e = lambda s: s.encode()
+    h = L.emu_open(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+                   e(f"{d}/matrix_elements"), Z, N, 1216, err, 1024)
+    y = np.zeros(len(x))
+    assert L.emu_matvec4(h, x.ctypes.data, y.ctypes.data, 0, int(f32)) == 0
+    L.emu_close(h)
+    return y
+
+
+@pytest.mark.parametrize("name", ["he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
+@pytest.mark.parametrize("bits", [64, 32])
+def test_panel_engine_is_exact_model(problem, name, bits):
+    """The panel engine (the default at these sizes) gives bit for bit what its CPU model gives."""
+    d, Z, N, *_ = problem(name)
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.set_engine(4)
+    H.set_precision(bits)
+    x = np.random.default_rng(23).standard_normal(H.dimension)
+    got = H.matvec(x)
+    want = emu4(d, Z, N, x, bits == 32)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    ref = oracle.Port(d).matvec(x)
+    tol = 1e-12 if bits == 64 else 2e-6
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
+    H.close()
+
+
 def test_engines_agree(problem):
     d, Z, N, *_ = problem("he4_n6_3b")
     H = jn.Hamiltonian.from_dir(d, Z, N)
     x = np.random.default_rng(22).standard_normal(H.dimension)
-    H.set_engine(2)
+    ys = []
+    for engine in (2, 3, 4):
+        H.set_engine(engine)
+        ys.append(H.matvec(x))
+    for y in ys[1:]:
+        assert np.abs(y - ys[0]).max() <= 1e-12 * np.abs(ys[0]).max()
+    H.close()
+
+
+def test_panel_engine_after_new_matrix_elements(problem):
+    """Replacing the matrix elements rebuilds the panel coefficients."""
+    d, Z, N, *_ = problem("he4_n4_2b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.set_engine(4)
+    x = np.random.default_rng(24).standard_normal(H.dimension)
     a = H.matvec(x)
-    H.set_engine(3)
+    me = H.read_matrix_elements(os.path.join(d, "matrix_elements"))
+    H.set_matrix_elements(2.5 * me)
     b = H.matvec(x)
-    assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+    assert np.abs(b - 2.5 * a).max() <= 1e-12 * np.abs(b).max()
     H.close()

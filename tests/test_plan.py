@@ -131,3 +131,22 @@ def test_block_tile_plan_model_matches_port(problem, name, units):
         assert L.emu_matvec3(h, x.ctypes.data, y.ctypes.data, 0, f32) == 0
         assert np.abs(y - want).max() <= tol * np.abs(want).max()
     L.emu_close(h)
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b"])
+def test_panel_plan_model_matches_port(problem, name):
+    """CPU model of the panel kernel (compacted coefficients, runs rounded
+    once, transposes per product): every index checked, FP64 within 1e-12
+    and FP32 within 2e-6 of the oracle."""
+    d, Z, N, *_ = problem(name)
+    L, h, err = open_plan(d, Z, N)
+    assert h, err
+    L.emu_matvec4.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(7).standard_normal(D)
+    want = oracle.Port(d).matvec(x)
+    for f32, tol in ((0, 1e-12), (1, 2e-6)):
+        y = np.zeros(D)
+        assert L.emu_matvec4(h, x.ctypes.data, y.ctypes.data, 0, f32) == 0
+        assert np.abs(y - want).max() <= tol * np.abs(want).max()
+    L.emu_close(h)
