@@ -37,4 +37,14 @@ __device__ __forceinline__ void add_fixed(unsigned int *lo, unsigned int *hi, in
 	if (h) atomicAdd(hi + i, h);
 }
 
+/* the same for a 32-bit contribution: the high word takes the sign and the
+ * carry, and is touched only when they do not cancel */
+__device__ __forceinline__ void add_fixed32(unsigned int *lo, unsigned int *hi, int i, int v)
+{
+	const unsigned int u = (unsigned int)v;
+	const unsigned int old = atomicAdd(lo + i, u);
+	const int h = (v >> 31) + (int)(old + u < old);
+	if (h) atomicAdd(hi + i, (unsigned int)h);
+}
+
 #endif

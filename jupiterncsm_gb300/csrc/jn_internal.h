@@ -52,10 +52,14 @@ struct jn_ctx {
 	struct jn_lanczos_state *lz;
 	/* panel engine (engine 4, jn_panel.cu) */
 	jn_panel_t *d_panels;
-	uint32_t *d_ptasks, *d_pcta, *d_pflush, *d_pflush_ptr, *d_pmeta;
+	uint32_t *d_ptasks, *d_pcta, *d_pflush, *d_pflush_ptr, *d_pmeta, *d_pblocks;
 	double *d_coef64;               /* panel coefficients, built on first FP64 use */
-	float *d_coef32;                /* and on first FP32 use */
+	int32_t *d_coefi;               /* and as 32-bit fixed-point integers on first 32-bit use */
+	int32_t *d_xi;                  /* x as 32-bit fixed-point integers, [p][n] then transposed [n][p] */
+	double *d_xt64;                 /* x with every block transposed to [n][p] (FP64 panel product) */
+	int pint_sc, pint_k;            /* coefficient exponent and product shift of the 32-bit path */
 	int panel_grid;                 /* persistent CTAs; 0 until set up */
+	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
 };
 
 /* enqueue y (+)= H x on stream st */
@@ -88,6 +92,7 @@ void jn_launch_finalize(unsigned long long *gacc, double *d_y, int64_t n, const 
 /* panel engine (jn_panel.cu): plan upload, coefficient reset after new
  * matrix elements, release, and the product on the context's scratch */
 jn_status jn_panels_setup(jn_ctx *c);
+int jn_panels_fit(const jn_ctx *c, int f32);
 void jn_panels_invalidate(jn_ctx *c);
 void jn_panels_release(jn_ctx *c);
 jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,

@@ -746,7 +746,7 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 		}
 		if (mid) cudaEventRecord(mid, st);
 		if (p->ntiles) jn_reduce_kernel<<<tg, WARPS * 32, 0, st>>>(c->d_tiles, p->ntiles, c->d_partial, d_y, accumulate);
-	} else if (c->engine == 4) {
+	} else if (c->engine == 4 && jn_panels_fit(c, f32)) {
 		jn_status s = jn_enqueue_panels(c, d_x, d_y, accumulate, st, pre, mid);
 		if (s) return s;
 	} else {

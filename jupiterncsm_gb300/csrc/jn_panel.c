@@ -20,17 +20,14 @@
 
 void jn_panels_free(jn_plan_t *p)
 {
-	free(p->panels); free(p->ptasks); free(p->pcta); free(p->pflush_ptr); free(p->pflush); free(p->pmeta);
+	free(p->panels); free(p->ptasks); free(p->pcta); free(p->pflush_ptr); free(p->pflush); free(p->pmeta); free(p->pblocks);
 	p->panels = NULL; p->ptasks = NULL; p->pcta = NULL; p->pflush_ptr = NULL; p->pflush = NULL; p->pmeta = NULL;
-	p->npanels = 0; p->nptasks = 0; p->pgrid = 0; p->npflush = 0; p->n_pmeta = 0; p->n_coef = 0;
+	p->pblocks = NULL;
+	p->npanels = 0; p->nptasks = 0; p->pgrid = 0; p->npflush = 0; p->n_pmeta = 0; p->n_coef = 0; p->psmem_words = 0;
 }
 
-static int lanes_log2(int ncols)
-{
-	int lg = 0;
-	while ((1 << lg) < ncols && lg < 5) lg++;
-	return lg;
-}
+/* lanes per row: a narrow panel puts floor(32 / ncols) rows side by side */
+static int lanes_per_row(int ncols) { return ncols < 32 ? ncols : 32; }
 
 /* panels sorted by (output block, input block) so that a CTA's run of tasks touches few blocks */
 static const jn_plan_t *g_sort_plan;
@@ -50,6 +47,19 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 	jn_panels_free(p);
 	if (p->dim > JN_PANEL_MAX_DIM) ERR("dimension %lld is above the panel engine's %d", (long long)p->dim, JN_PANEL_MAX_DIM);
 	if (grid < 1) ERR("panel grid of %d CTAs", grid);
+	/* accumulator layout: block rows padded to an odd length, so that a warp
+	   walking a column (stride Nn) hits 32 different shared-memory banks */
+	p->pblocks = malloc((p->nblocks ? p->nblocks : 1) * 4 * sizeof(uint32_t));
+	if (!p->pblocks) ERR("out of host memory");
+	p->psmem_words = 0;
+	for (int b = 0; b < p->nblocks; b++) {
+		const jn_block_t *B = &p->blocks[b];
+		p->pblocks[4 * b] = (uint32_t)B->offset;
+		p->pblocks[4 * b + 1] = (uint32_t)p->psmem_words;
+		p->pblocks[4 * b + 2] = (uint32_t)B->Np;
+		p->pblocks[4 * b + 3] = (uint32_t)B->Nn;
+		p->psmem_words += B->Np * (B->Nn | 1);
+	}
 	/* packed list entries, by-out order: source | destination << 16 */
 	p->n_pmeta = 0;
 	for (int l = 0; l < p->nlists; l++) {
@@ -81,11 +91,17 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 		P->in_off = (int32_t)bi->offset;
 		P->Nn_out = (int32_t)bo->Nn;
 		P->Nn_in = (int32_t)bi->Nn;
+		P->Np_out = (int32_t)bo->Np;
+		P->Np_in = (int32_t)bi->Np;
+		P->out_soff = (int32_t)p->pblocks[4 * x->bout + 1];
+		P->in_soff = (int32_t)p->pblocks[4 * x->bin + 1];
 		P->kind = x->kind | (x->bin == x->bout ? JN_PANEL_DIAG : 0);
 		const jn_list_t *Ln = x->ln >= 0 ? &p->lists[x->ln] : NULL, *Lp = x->lp >= 0 ? &p->lists[x->lp] : NULL;
 		if (x->kind == JN_KIND_NP) {
-			P->nrows = (int32_t)Lp->len;
-			P->ncols = (int32_t)Ln->len;
+			const int rows_n = Ln->len > Lp->len;
+			P->nrows = (int32_t)(rows_n ? Ln->len : Lp->len);
+			P->ncols = (int32_t)(rows_n ? Lp->len : Ln->len);
+			if (rows_n) P->kind |= JN_PANEL_ROWS_N;
 			coef += (int64_t)P->nrows * P->ncols;
 		} else if (x->kind == JN_KIND_N) {
 			P->nrows = (int32_t)bo->Np;
@@ -98,8 +114,13 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 		}
 		P->row_meta = Lp ? (uint32_t)Lp->pmeta : 0;
 		P->col_meta = Ln ? (uint32_t)Ln->pmeta : 0;
+		if (P->kind & JN_PANEL_ROWS_N) {
+			P->row_meta = (uint32_t)Ln->pmeta;
+			P->col_meta = (uint32_t)Lp->pmeta;
+		}
+		if (x->kind == JN_KIND_N && P->nrows > 65535) ERR("instruction %d: %d spectator rows", order[q], P->nrows);
 		if (P->nrows > 0 && P->ncols > 0) {
-			const int lg = lanes_log2(P->ncols), R = 32 >> lg;
+			const int R = 32 / lanes_per_row(P->ncols);
 			const int64_t rows_per_task = (int64_t)R * JN_PANEL_ITER;
 			ntask += ((P->ncols + 31) / 32) * ((P->nrows + rows_per_task - 1) / rows_per_task);
 		}
@@ -114,7 +135,7 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 	for (int q = 0; q < p->npanels; q++) {
 		const jn_panel_t *P = &p->panels[q];
 		if (P->nrows <= 0 || P->ncols <= 0) continue;
-		const int lg = lanes_log2(P->ncols), R = 32 >> lg;
+		const int cw = lanes_per_row(P->ncols), R = 32 / cw;
 		const int64_t rows_per_task = (int64_t)R * JN_PANEL_ITER;
 		const int diag = (P->kind & JN_PANEL_DIAG) != 0;
 		for (int i0 = 0; i0 < P->ncols; i0 += 32)
@@ -124,9 +145,9 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 				T[0] = (uint32_t)q;
 				T[1] = (uint32_t)j0;
 				T[2] = (uint32_t)j1;
-				T[3] = (uint32_t)i0 | ((uint32_t)lg << 24);
+				T[3] = (uint32_t)i0 | ((uint32_t)cw << 24);
 				/* warp time: one pass per R rows, the transpose doubles the work, plus set-up */
-				cost[t] = (double)((j1 - j0 + R - 1) / R) * (diag ? 1.0 : 1.7) + 6.0;
+				cost[t] = (double)((j1 - j0 + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
 				t++;
 			}
 	}
@@ -150,7 +171,7 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 	touched = calloc(p->nblocks ? p->nblocks : 1, 1);
 	p->pflush_ptr = malloc((size_t)(grid + 1) * sizeof(uint32_t));
 	size_t fcap = 1024;
-	p->pflush = malloc(fcap * 2 * sizeof(uint32_t));
+	p->pflush = malloc(fcap * sizeof(uint32_t));
 	if (!touched || !p->pflush_ptr || !p->pflush) ERR("out of host memory");
 	p->npflush = 0;
 	for (int b = 0; b < grid; b++) {
@@ -161,23 +182,14 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 			touched[x->bout] = 1;
 			if (x->bin != x->bout) touched[x->bin] = 1;
 		}
-		/* blocks are laid out in index order: merge neighbours into ranges */
 		for (int i = 0; i < p->nblocks; i++) {
-			if (!touched[i]) continue;
-			const uint32_t off = (uint32_t)p->blocks[i].offset, len = (uint32_t)(p->blocks[i].Np * p->blocks[i].Nn);
-			if (!len) continue;
-			if (p->npflush > p->pflush_ptr[b] && p->pflush[2 * (p->npflush - 1)] + p->pflush[2 * (p->npflush - 1) + 1] == off) {
-				p->pflush[2 * (p->npflush - 1) + 1] += len;
-				continue;
-			}
+			if (!touched[i] || p->blocks[i].Np <= 0 || p->blocks[i].Nn <= 0) continue;
 			if ((size_t)p->npflush == fcap) {
 				fcap *= 2;
-				p->pflush = realloc(p->pflush, fcap * 2 * sizeof(uint32_t));
+				p->pflush = realloc(p->pflush, fcap * sizeof(uint32_t));
 				if (!p->pflush) ERR("out of host memory");
 			}
-			p->pflush[2 * p->npflush] = off;
-			p->pflush[2 * p->npflush + 1] = len;
-			p->npflush++;
+			p->pflush[p->npflush++] = (uint32_t)i;
 		}
 	}
 	p->pflush_ptr[grid] = (uint32_t)p->npflush;
@@ -189,6 +201,8 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 		if ((x->kind != JN_KIND_N && (int64_t)P->row_meta + P->nrows > p->n_pmeta) ||
 		    (x->kind != JN_KIND_P && (int64_t)P->col_meta + P->ncols > p->n_pmeta))
 			ERR("panel %d: list entries out of range", q);
+		if (x->kind == JN_KIND_NP && (int64_t)P->nrows * P->ncols != (int64_t)p->lists[x->ln].len * p->lists[x->lp].len)
+			ERR("panel %d: shape", q);
 		if (x->kind == JN_KIND_N && (bi->Np != bo->Np)) ERR("panel %d: spectator rows differ", q);
 		if (x->kind == JN_KIND_P && (bi->Nn != bo->Nn)) ERR("panel %d: spectator columns differ", q);
 	}
@@ -210,18 +224,17 @@ void jn_panels_coefficients(const jn_plan_t *p, const double *me, double *c64, f
 		const uint32_t *ent = p->ent;
 		if (x->kind == JN_KIND_NP) {
 			const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
-			for (int32_t j = 0; j < P->nrows; j++) {
-				const uint32_t mp = ent[2 * (Lp->ent_out + j) + 1];
-				const double *mrow = m + (int64_t)M->nd_n * (mp & 0x7fffffffu);
-				const int64_t base = P->c_off + (int64_t)j * P->ncols;
+			const int rows_n = (P->kind & JN_PANEL_ROWS_N) != 0;
+			for (int32_t j = 0; j < P->nrows; j++)
 				for (int32_t i = 0; i < P->ncols; i++) {
-					const uint32_t mn = ent[2 * (Ln->ent_out + i) + 1];
-					double v = mrow[mn & 0x7fffffffu];
+					const int32_t ep = rows_n ? i : j, en = rows_n ? j : i;
+					const uint32_t mp = ent[2 * (Lp->ent_out + ep) + 1], mn = ent[2 * (Ln->ent_out + en) + 1];
+					double v = m[(mn & 0x7fffffffu) + (int64_t)M->nd_n * (mp & 0x7fffffffu)];
 					if ((mp ^ mn) & 0x80000000u) v = -v;
-					if (c64) c64[base + i] = v;
-					if (c32) c32[base + i] = (float)v;
+					const int64_t at = P->c_off + (int64_t)j * P->ncols + i;
+					if (c64) c64[at] = v;
+					if (c32) c32[at] = (float)v;
 				}
-			}
 		} else {
 			const jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
 			for (int64_t e = 0; e < L->len; e++) {
@@ -235,4 +248,27 @@ void jn_panels_coefficients(const jn_plan_t *p, const double *me, double *c64, f
 			}
 		}
 	}
+}
+
+int jn_panels_coefficients_int(const jn_plan_t *p, const double *me, int32_t *ci, int *Sc, int *k)
+{
+	double *c = malloc((p->n_coef ? p->n_coef : 1) * sizeof(double));
+	if (!c) return 1;
+	jn_panels_coefficients(p, me, c, NULL);
+	double cmax = 0.0;
+	for (int64_t e = 0; e < p->n_coef; e++) cmax = fmax(cmax, fabs(c[e]));
+	int ec = 0, eb = 0;
+	if (cmax > 0.0) frexp(cmax, &ec);               /* cmax < 2^ec */
+	*Sc = cmax > 0.0 ? 30 - ec : 0;
+	if (p->abs_bound > 0.0) frexp(p->abs_bound, &eb); /* abs_bound < 2^eb */
+	/* |c_int x_int| <= 2^60: the shift 30 rounds every product to a 32-bit
+	   integer (|v| <= 2^30), whose 64-bit addition mostly touches only the low
+	   word (the high word takes a carry about |v| / 2^32 of the time); element sums stay below
+	   2^62 as long as sum |c_int x_int| < abs_bound 2^Sc 2^30 stays below
+	   2^(61 + k), which a larger shift guarantees where needed */
+	*k = 30;
+	if (p->abs_bound > 0.0 && eb + *Sc - 31 > *k) *k = eb + *Sc - 31;
+	for (int64_t e = 0; e < p->n_coef; e++) ci[e] = (int32_t)llrint(ldexp(c[e], *Sc));
+	free(c);
+	return 0;
 }

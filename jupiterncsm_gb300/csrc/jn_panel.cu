@@ -8,20 +8,23 @@
  * transposes :212-462, |M| < 1e-12 skip of single-species terms :52-53).
  *
  * GB300 organisation.  At set-up every instruction becomes a panel whose
- * coefficient of (proton entry j, neutron entry i) is s_p s_n M[k_n + Nd k_p],
- * stored densely and row-major: the product reads each coefficient once,
- * coalesced, with streaming (evict-first) loads, and the index lists only as
- * 4-byte packed (source, destination) pairs.  A warp task spreads up to 32
- * columns of a panel over its lanes (and 32 / columns rows side by side when
- * a panel is narrow) and walks rows; the x gathers hit L1.  The whole
- * output vector is accumulated in shared memory as 64-bit fixed-point
- * integers (two 32-bit atomics with carry): a lane sums the consecutive rows
- * that land on one output element in T arithmetic and adds the rounded run
- * once; the transposed contribution of an off-diagonal panel is rounded and
- * added per product.  Integer addition is exact and associative, so the
- * result is bit-identical whatever the order in which warps and CTAs run.
- * Persistent CTAs take contiguous runs of tasks that touch few blocks, and at
- * the end add only the touched ranges into the global accumulator.
+ * coefficient of (proton entry, neutron entry) is s_p s_n M[k_n + Nd k_p],
+ * stored densely and row-major with the shorter list as columns: the
+ * product reads each coefficient once, coalesced, with streaming
+ * (evict-first) loads, and the index lists only as 4-byte packed
+ * (source, destination) pairs.  A warp task spreads up to 32 columns of a
+ * panel over its lanes (and floor(32 / columns) rows side by side when a
+ * panel is narrow) and walks rows, with the row entries and coefficients of eight
+ * rows in flight per lane; the x gathers hit L1.  Each CTA holds the whole
+ * of y as 64-bit fixed-point integers in shared memory, with block rows
+ * padded to an odd length so that a warp walking a column touches 32
+ * different banks: every contribution is one rounding of c x 2^S to an
+ * integer, added as two 32-bit shared atomics with carry (the list walks are
+ * about one entry long, so there is nothing to sum before rounding).  Integer addition is exact and
+ * associative, so the result is bit-identical whatever the order in which
+ * warps and CTAs run.  Persistent CTAs take contiguous runs of tasks that
+ * touch few blocks, and at the end add only the touched ranges into the
+ * global accumulator.
  */
 #include "jn_internal.h"
 #include "jn_fixed.cuh"
@@ -31,32 +34,64 @@
 
 template <typename T> __device__ __forceinline__ T load_stream(const T *p) { return __ldcs(p); }
 
-template <typename T, int KIND, bool DIAG>
-__device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const uint4 pc, uint32_t j0, uint32_t j1,
-					   int R, int r, int i, unsigned int *__restrict__ lo, unsigned int *__restrict__ hi,
-					   const T *__restrict__ x, const T *__restrict__ coef,
-					   const uint32_t *__restrict__ meta, const T scale)
+/* One contribution c x as a 64-bit fixed-point integer.  FP64: (c x) 2^S
+ * rounded once.  32-bit: c and x are 32-bit fixed-point integers; the product
+ * is exact in 64 bits and is rounded once by the shift k. */
+struct FixFp64 {
+	double scale;
+	__device__ __forceinline__ long long operator()(double c, double x) const { return to_fixed<double>(c * x * scale); }
+};
+#define PANEL_INT_SHIFT 30       /* the 32-bit product's rounding shift (jn_panels_coefficients_int) */
+struct FixInt32 {
+	__device__ __forceinline__ int operator()(int c, int x) const
+	{
+		return (int)(((long long)c * x + (1ll << (PANEL_INT_SHIFT - 1))) >> PANEL_INT_SHIFT);
+	}
+};
+
+__device__ __forceinline__ void add_contribution(unsigned int *lo, unsigned int *hi, int i, long long v)
+{
+	add_fixed(lo, hi, i, v);
+}
+__device__ __forceinline__ void add_contribution(unsigned int *lo, unsigned int *hi, int i, int v)
+{
+	add_fixed32(lo, hi, i, v);
+}
+
+template <typename T, typename Fix, int KIND, bool DIAG>
+__device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const uint4 pc, const uint4 pd, uint32_t j0,
+					   uint32_t j1, int R, int r, int i, unsigned int *__restrict__ lo,
+					   unsigned int *__restrict__ hi, const T *__restrict__ x, const T *__restrict__ xt,
+					   const T *__restrict__ coef, const uint32_t *__restrict__ meta, const Fix fix)
 {
 	const int64_t c_off = (int64_t)pa.x | ((int64_t)pa.y << 32);
 	const uint32_t row_meta = pa.z, col_meta = pa.w;
 	const int out_off = (int)pb.x, in_off = (int)pb.y, Nn_out = (int)pb.z, Nn_in = (int)pb.w;
-	const int ncols = (int)pc.x;
-	int Ni, No;
-	T ccol = 1;
+	const int ncols = (int)pc.x, out_soff = (int)pc.z, in_soff = (int)pc.w;
+	const int Np_out = (int)pd.z, Np_in = (int)pd.w;
+	/* element (row entry sr -> dr, column entry sc -> dc) reads x at (sr, sc) of the input block and
+	   lands on y at (dr, dc) of the output block; the transpose swaps the two.  Lanes own columns, so
+	   x is read from the copy in which a column is contiguous: x itself ([p][n]) when rows are proton
+	   entries, the transposed copy ([n][p]) when they are neutron entries.  The accumulator keeps the
+	   [p][n] layout with rows padded to Nn | 1 (odd: a stride-Po walk hits 32 banks). */
+	const bool rows_n = KIND == JN_KIND_NP && (pc.y & JN_PANEL_ROWS_N);
+	const T *__restrict__ xv = rows_n ? xt : x;
+	const int Po = Nn_out | 1, Pi = Nn_in | 1;
+	const int MRo = rows_n ? Np_out : Nn_out, MRi = rows_n ? Np_in : Nn_in, MCo = 1, MCi = 1;
+	const int SRo = rows_n ? 1 : Po, SCo = rows_n ? Po : 1, SRi = rows_n ? 1 : Pi, SCi = rows_n ? Pi : 1;
+	int sc, dc;
 	if (KIND == JN_KIND_P) {
-		Ni = No = i;
+		sc = dc = i;
 	} else {
 		const uint32_t m = __ldg(meta + col_meta + i);
-		Ni = (int)(m & 0xffffu);
-		No = (int)(m >> 16);
+		sc = (int)(m & 0xffffu);
+		dc = (int)(m >> 16);
 	}
-	if (KIND == JN_KIND_N) ccol = __ldg(coef + c_off + i);
-	const T *__restrict__ xin = x + in_off + Ni;
-	const T *__restrict__ xout = x + out_off + No;
-	const int yin = in_off + Ni, yout = out_off + No;
+	const T *__restrict__ xi_base = xv + in_off + sc * MCi;
+	const T *__restrict__ xo_base = xv + out_off + dc * MCo;
+	const int ai_base = in_soff + sc * SCi, ao_base = out_soff + dc * SCo;
+	const T ccol = KIND == JN_KIND_N ? __ldg(coef + c_off + i) : (T)0;
 	const T *__restrict__ crow = coef + c_off + (KIND == JN_KIND_NP ? i : 0);
-	int cur = -1;
-	T run = 0;
 	for (uint32_t j = j0 + r; j < j1; j += PANEL_UNROLL * R) {
 		uint32_t mr[PANEL_UNROLL];
 		T cv[PANEL_UNROLL];
@@ -64,7 +99,7 @@ __device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const
 #pragma unroll
 		for (int u = 0; u < PANEL_UNROLL; u++) {
 			const uint32_t jj = j + u * R;
-			mr[u] = jj | (jj << 16);
+			mr[u] = jj * 0x10001u;
 			cv[u] = 0;
 			if (jj < j1) {
 				if (KIND != JN_KIND_N) mr[u] = __ldg(meta + row_meta + jj);
@@ -76,51 +111,37 @@ __device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const
 #pragma unroll
 		for (int u = 0; u < PANEL_UNROLL; u++) {
 			if (j + u * R >= j1) break;
-			const int Pi = (int)(mr[u] & 0xffffu), Po = (int)(mr[u] >> 16);
-			const T xi = __ldg(xin + Pi * Nn_in);
-			if (Po != cur) {
-				if (cur >= 0) add_fixed(lo, hi, yout + cur * Nn_out, to_fixed<T>(run * scale));
-				cur = Po;
-				run = 0;
-			}
-			run = fma(cv[u], xi, run);
-			if (!DIAG) {
-				const T xo = __ldg(xout + Po * Nn_out);
-				add_fixed(lo, hi, yin + Pi * Nn_in, to_fixed<T>(cv[u] * xo * scale));
-			}
+			const int sr = (int)(mr[u] & 0xffffu), dr = (int)(mr[u] >> 16);
+			add_contribution(lo, hi, ao_base + dr * SRo, fix(cv[u], __ldg(xi_base + sr * MRi)));
+			if (!DIAG) add_contribution(lo, hi, ai_base + sr * SRi, fix(cv[u], __ldg(xo_base + dr * MRo)));
 		}
 	}
-	if (cur >= 0) add_fixed(lo, hi, yout + cur * Nn_out, to_fixed<T>(run * scale));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(PANEL_THREADS) jn_panel_kernel(const uint4 *__restrict__ panels,
-								 const uint4 *__restrict__ tasks,
-								 const uint32_t *__restrict__ cta_ptr,
-								 const uint2 *__restrict__ flush,
-								 const uint32_t *__restrict__ flush_ptr,
-								 const uint32_t *__restrict__ meta, const T *__restrict__ coef,
-								 const T *__restrict__ x, unsigned long long *__restrict__ gacc,
-								 const unsigned int *__restrict__ xmax_bits, double abs_bound,
-								 int dim)
+template <typename T, typename Fix>
+__device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, const uint4 *__restrict__ tasks,
+					      const uint32_t *__restrict__ cta_ptr, const uint32_t *__restrict__ flush,
+					      const uint32_t *__restrict__ flush_ptr, const uint4 *__restrict__ blocks,
+					      const uint32_t *__restrict__ meta, const T *__restrict__ coef,
+					      const T *__restrict__ x, const T *__restrict__ xt,
+					      unsigned long long *__restrict__ gacc, const Fix fix, int words)
 {
 	extern __shared__ unsigned int sacc[];
 	__shared__ unsigned int next_task;
-	unsigned int *lo = sacc, *hi = sacc + dim;
+	unsigned int *lo = sacc, *hi = sacc + words;
 	const int lane = threadIdx.x & 31;
 	const uint32_t f0 = flush_ptr[blockIdx.x], f1 = flush_ptr[blockIdx.x + 1];
-	/* clear the ranges this CTA touches */
+	/* clear the blocks this CTA touches (padded rows) */
 	for (uint32_t f = f0; f < f1; f++) {
-		const uint2 rg = flush[f];
-		for (uint32_t e = threadIdx.x; e < rg.y; e += blockDim.x) {
-			lo[rg.x + e] = 0u;
-			hi[rg.x + e] = 0u;
+		const uint4 bk = __ldg(blocks + flush[f]);
+		const uint32_t n = bk.z * (bk.w | 1u);
+		for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+			lo[bk.y + e] = 0u;
+			hi[bk.y + e] = 0u;
 		}
 	}
 	if (threadIdx.x == 0) next_task = 0;
 	__syncthreads();
-	const int S = fixed_exponent(*xmax_bits, abs_bound);
-	const T scale = (T)ldexp(1.0, S);
 	const uint32_t t0 = cta_ptr[blockIdx.x], nt = cta_ptr[blockIdx.x + 1] - t0;
 	for (;;) {
 		uint32_t k = 0;
@@ -128,31 +149,115 @@ __global__ void __launch_bounds__(PANEL_THREADS) jn_panel_kernel(const uint4 *__
 		k = __shfl_sync(0xffffffffu, k, 0);
 		if (k >= nt) break;
 		const uint4 tk = __ldg(tasks + t0 + k);
-		const uint4 pa = __ldg(panels + 3 * tk.x), pb = __ldg(panels + 3 * tk.x + 1), pc = __ldg(panels + 3 * tk.x + 2);
-		const int lg = (int)(tk.w >> 24), R = 32 >> lg, r = lane >> lg;
-		const int i = (int)(tk.w & 0xffffffu) + (lane & ((1 << lg) - 1));
-		if (i >= (int)pc.x) continue;
+		const uint4 pa = __ldg(panels + 4 * tk.x), pb = __ldg(panels + 4 * tk.x + 1), pc = __ldg(panels + 4 * tk.x + 2);
+		const uint4 pd = __ldg(panels + 4 * tk.x + 3);
+		/* cw lanes per row, R = 32 / cw rows side by side: lane = r cw + c */
+		const int cw = (int)(tk.w >> 24), R = 32 / cw, r = lane / cw;
+		const int i = (int)(tk.w & 0xffffffu) + (lane - r * cw);
+		if (r >= R || i >= (int)pc.x) continue;
 		const int kind = (int)pc.y & 7;
 		const bool diag = (pc.y & JN_PANEL_DIAG) != 0;
 		if (kind == JN_KIND_NP) {
-			if (diag) panel_task<T, JN_KIND_NP, true>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
-			else panel_task<T, JN_KIND_NP, false>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
+			if (diag) panel_task<T, Fix, JN_KIND_NP, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			else panel_task<T, Fix, JN_KIND_NP, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
 		} else if (kind == JN_KIND_N) {
-			if (diag) panel_task<T, JN_KIND_N, true>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
-			else panel_task<T, JN_KIND_N, false>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
+			if (diag) panel_task<T, Fix, JN_KIND_N, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			else panel_task<T, Fix, JN_KIND_N, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
 		} else {
-			if (diag) panel_task<T, JN_KIND_P, true>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
-			else panel_task<T, JN_KIND_P, false>(pa, pb, pc, tk.y, tk.z, R, r, i, lo, hi, x, coef, meta, scale);
+			if (diag) panel_task<T, Fix, JN_KIND_P, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			else panel_task<T, Fix, JN_KIND_P, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
 		}
 	}
 	__syncthreads();
+	/* add the touched blocks into the global accumulator (unpadded layout) */
 	for (uint32_t f = f0; f < f1; f++) {
-		const uint2 rg = flush[f];
-		for (uint32_t e = threadIdx.x; e < rg.y; e += blockDim.x) {
-			const unsigned long long v = (unsigned long long)lo[rg.x + e] | ((unsigned long long)hi[rg.x + e] << 32);
-			if (v) atomicAdd(gacc + rg.x + e, v);
+		const uint4 bk = __ldg(blocks + flush[f]);
+		const uint32_t Nn = bk.w, Ns = bk.w | 1u, n = bk.z * Nn;
+		for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+			const uint32_t s = bk.y + (e / Nn) * Ns + e % Nn;
+			const unsigned long long v = (unsigned long long)lo[s] | ((unsigned long long)hi[s] << 32);
+			if (v) atomicAdd(gacc + bk.x + e, v);
 		}
 	}
+}
+
+/* the 32-bit product: coefficients and x are 32-bit fixed-point integers */
+__global__ void __launch_bounds__(PANEL_THREADS, 3) jn_panel_kernel_i32(const uint4 *__restrict__ panels,
+								     const uint4 *__restrict__ tasks,
+								     const uint32_t *__restrict__ cta_ptr,
+								     const uint32_t *__restrict__ flush,
+								     const uint32_t *__restrict__ flush_ptr,
+								     const uint4 *__restrict__ blocks,
+								     const uint32_t *__restrict__ meta, const int *__restrict__ coef,
+								     const int *__restrict__ x, const int *__restrict__ xt,
+								     unsigned long long *__restrict__ gacc, const FixInt32 fix, int words)
+{
+	jn_panel_body<int, FixInt32>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef, x, xt, gacc, fix,
+					    words);
+}
+
+/* the FP64 product: the fixed-point scale 2^S comes from max|x| on the device */
+__global__ void __launch_bounds__(PANEL_THREADS) jn_panel_kernel_fp64(const uint4 *__restrict__ panels,
+								      const uint4 *__restrict__ tasks,
+								      const uint32_t *__restrict__ cta_ptr,
+								      const uint32_t *__restrict__ flush,
+								      const uint32_t *__restrict__ flush_ptr,
+								      const uint4 *__restrict__ blocks,
+								      const uint32_t *__restrict__ meta,
+								      const double *__restrict__ coef, const double *__restrict__ x,
+								      const double *__restrict__ xt, unsigned long long *__restrict__ gacc,
+								      const unsigned int *__restrict__ xmax_bits, double abs_bound,
+								      int words)
+{
+	const FixFp64 fix = { ldexp(1.0, fixed_exponent(*xmax_bits, abs_bound)) };
+	jn_panel_body<double, FixFp64>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef, x, xt, gacc, fix,
+					      words);
+}
+
+/* exponent Sx of the 32-bit fixed-point x: |x| 2^Sx < 2^30 for the bound max|x| in xmax_bits */
+__device__ __forceinline__ int x_exponent(unsigned int xmax_bits)
+{
+	if (!(xmax_bits & 0x7fffffffu)) return 0;
+	const int ex = (int)((xmax_bits >> 23) & 0xff) - 126;   /* xmax < 2^ex */
+	const int Sx = 30 - ex;
+	return Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
+}
+
+/* block b = blockIdx.x: the panel kernels' copies of x, in the [p][n] layout
+ * (xn, 32-bit path only) and transposed to [n][p] (xt).  32-bit path: x as
+ * 32-bit fixed-point integers x 2^Sx; FP64: x itself. */
+template <typename T>
+__global__ void jn_panel_x_kernel(const double *__restrict__ x, T *__restrict__ xn, T *__restrict__ xt,
+				  const uint4 *__restrict__ blocks, const unsigned int *__restrict__ xmax_bits)
+{
+	const uint4 bk = blocks[blockIdx.x];
+	const uint32_t Np = bk.z, Nn = bk.w, n = Np * Nn;
+	const double s = sizeof(T) == 4 ? ldexp(1.0, x_exponent(*xmax_bits)) : 1.0;
+	for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+		const double v = x[bk.x + e];
+		const T t = sizeof(T) == 4 ? (T)__double2int_rn(v * s) : (T)v;
+		if (xn) xn[bk.x + e] = t;
+		xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+	}
+}
+
+/* y (+)= acc 2^(k - Sc - Sx); the accumulator is cleared for the next product */
+__global__ void jn_int_finalize_kernel(unsigned long long *__restrict__ gacc, double *__restrict__ y, int64_t n,
+				       const unsigned int *__restrict__ xmax_bits, int k_minus_sc, int accumulate)
+{
+	const double unit = ldexp(1.0, k_minus_sc - x_exponent(*xmax_bits));
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = (double)(long long)gacc[i] * unit;
+		y[i] = accumulate ? y[i] + v : v;
+		gacc[i] = 0ull;
+	}
+}
+
+/* the accumulator: two 32-bit words per padded state */
+static size_t panel_smem(const jn_plan_t *p, int f32)
+{
+	(void)f32;
+	return (size_t)(p->psmem_words ? p->psmem_words : 1) * 2 * sizeof(unsigned int);
 }
 
 /* ------------------------------------------------------------------ */
@@ -172,11 +277,18 @@ static jn_status upload_n(T **dst, const void *src, size_t n)
 void jn_panels_release(jn_ctx *c)
 {
 	cudaFree(c->d_panels); cudaFree(c->d_ptasks); cudaFree(c->d_pcta); cudaFree(c->d_pflush);
-	cudaFree(c->d_pflush_ptr); cudaFree(c->d_pmeta); cudaFree(c->d_coef64); cudaFree(c->d_coef32);
+	cudaFree(c->d_pflush_ptr); cudaFree(c->d_pmeta); cudaFree(c->d_coef64); cudaFree(c->d_coefi);
+	cudaFree(c->d_pblocks); cudaFree(c->d_xi); cudaFree(c->d_xt64);
+	c->d_pblocks = NULL;
+	c->d_xi = NULL;
+	c->d_xt64 = NULL;
 	c->d_panels = NULL; c->d_ptasks = NULL; c->d_pcta = NULL; c->d_pflush = NULL;
-	c->d_pflush_ptr = NULL; c->d_pmeta = NULL; c->d_coef64 = NULL; c->d_coef32 = NULL;
+	c->d_pflush_ptr = NULL; c->d_pmeta = NULL; c->d_coef64 = NULL; c->d_coefi = NULL;
 	c->panel_grid = 0;
+	c->panel_per_sm[0] = c->panel_per_sm[1] = 0;
 }
+
+int jn_panels_fit(const jn_ctx *c, int f32) { return c->panel_grid > 0 && c->panel_per_sm[f32 ? 1 : 0] > 0; }
 
 jn_status jn_panels_setup(jn_ctx *c)
 {
@@ -184,22 +296,35 @@ jn_status jn_panels_setup(jn_ctx *c)
 	if (p->dim > JN_PANEL_MAX_DIM) return jn_fail(JN_ERR_INVALID, "dimension %lld is above the panel engine's %d",
 						       (long long)p->dim, JN_PANEL_MAX_DIM);
 	if (c->panel_grid) return JN_OK;
-	const size_t smem = (size_t)(p->dim ? p->dim : 1) * 2 * sizeof(unsigned int);
-	int per_f = 0, per_d = 0;
-	CUDA_TRY(cudaFuncSetAttribute(jn_panel_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	CUDA_TRY(cudaFuncSetAttribute(jn_panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, jn_panel_kernel<float>, PANEL_THREADS, smem));
-	CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_d, jn_panel_kernel<double>, PANEL_THREADS, smem));
-	int per = per_f < per_d ? per_f : per_d;
-	if (per < 1) return jn_fail(JN_ERR_INVALID, "the panel kernel does not fit on an SM with %zu bytes of accumulator", smem);
+	/* CTAs per SM at each precision; the FP64 kernel may not fit where the FP32 one does */
+	int per[2] = { 0, 0 };
 	char err[512] = { 0 };
-	if (jn_panels_build(p, c->num_sms * per, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	/* the accumulator layout does not depend on the grid: plan once to size it */
+	if (jn_panels_build(p, 1, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	for (int f32 = 0; f32 < 2; f32++) {
+		const size_t smem = panel_smem(p, f32);
+		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+				    : cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		if (e == cudaSuccess)
+			e = f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], jn_panel_kernel_i32, PANEL_THREADS, smem)
+				: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], jn_panel_kernel_fp64, PANEL_THREADS, smem);
+		if (e != cudaSuccess) {
+			per[f32] = 0;
+			cudaGetLastError();
+		}
+	}
+	if (per[1] < 1) return jn_fail(JN_ERR_INVALID, "the panel kernel does not fit on an SM for dimension %lld", (long long)p->dim);
+	c->panel_per_sm[0] = per[0];
+	c->panel_per_sm[1] = per[1];
+	/* the task split is the same for every grid; CTAs take contiguous runs of the FP32 grid */
+	if (jn_panels_build(p, c->num_sms * per[1], err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
 	jn_status s;
 	if ((s = upload_n(&c->d_panels, p->panels, (size_t)p->npanels)) ||
 	    (s = upload_n(&c->d_ptasks, p->ptasks, (size_t)p->nptasks * 4)) ||
 	    (s = upload_n(&c->d_pcta, p->pcta, (size_t)p->pgrid + 1)) ||
 	    (s = upload_n(&c->d_pflush_ptr, p->pflush_ptr, (size_t)p->pgrid + 1)) ||
-	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush * 2)) ||
+	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush)) ||
+	    (s = upload_n(&c->d_pblocks, p->pblocks, (size_t)p->nblocks * 4)) ||
 	    (s = upload_n(&c->d_pmeta, p->pmeta, (size_t)p->n_pmeta))) {
 		jn_panels_release(c);
 		return s;
@@ -208,17 +333,27 @@ jn_status jn_panels_setup(jn_ctx *c)
 	return JN_OK;
 }
 
-/* coefficients of the context's matrix elements in the precision of the
- * context (built on first use and after the matrix elements change) */
+/* coefficients of the context's matrix elements (built on first use at each
+ * precision and after the matrix elements change): FP64, or 32-bit
+ * fixed-point integers with their exponent Sc and product shift k */
 static jn_status ensure_coefficients(jn_ctx *c, int f32)
 {
 	const jn_plan_t *p = &c->plan;
-	if (f32 ? c->d_coef32 != NULL : c->d_coef64 != NULL) return JN_OK;
+	if (f32 ? c->d_coefi != NULL : c->d_coef64 != NULL) return JN_OK;
 	const size_t n = (size_t)(p->n_coef ? p->n_coef : 1);
-	void *h = malloc(n * (f32 ? sizeof(float) : sizeof(double)));
+	void *h = malloc(n * (f32 ? sizeof(int32_t) : sizeof(double)));
 	if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %zu panel coefficients", n);
-	jn_panels_coefficients(p, p->me, f32 ? NULL : (double *)h, f32 ? (float *)h : NULL);
-	jn_status s = f32 ? upload_n(&c->d_coef32, h, (size_t)p->n_coef) : upload_n(&c->d_coef64, h, (size_t)p->n_coef);
+	jn_status s = JN_OK;
+	if (f32) {
+		if (jn_panels_coefficients_int(p, p->me, (int32_t *)h, &c->pint_sc, &c->pint_k))
+			s = jn_fail(JN_ERR_NOMEM, "out of host memory for %zu panel coefficients", n);
+		else if (c->pint_k != PANEL_INT_SHIFT)
+			s = jn_fail(JN_ERR_INVALID, "32-bit panel product: the matrix elements need a rounding shift of %d", c->pint_k);
+		if (!s) s = upload_n(&c->d_coefi, h, (size_t)p->n_coef);
+	} else {
+		jn_panels_coefficients(p, p->me, (double *)h, NULL);
+		s = upload_n(&c->d_coef64, h, (size_t)p->n_coef);
+	}
 	free(h);
 	return s;
 }
@@ -226,9 +361,9 @@ static jn_status ensure_coefficients(jn_ctx *c, int f32)
 void jn_panels_invalidate(jn_ctx *c)
 {
 	cudaFree(c->d_coef64);
-	cudaFree(c->d_coef32);
+	cudaFree(c->d_coefi);
 	c->d_coef64 = NULL;
-	c->d_coef32 = NULL;
+	c->d_coefi = NULL;
 }
 
 jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
@@ -237,26 +372,45 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 	const jn_plan_t *p = &c->plan;
 	const int f32 = c->precision == 32;
 	jn_status s = jn_panels_setup(c);
+	if (!s && !jn_panels_fit(c, f32)) s = jn_fail(JN_ERR_INVALID, "the FP64 panel kernel does not fit for dimension %lld",
+						      (long long)p->dim);
 	if (!s) s = ensure_coefficients(c, f32);
-	if (!s && f32 && !c->d_x32) s = upload_n(&c->d_x32, NULL, (size_t)p->dim);
+	if (!s && !c->d_xi) s = upload_n(&c->d_xi, NULL, (size_t)p->dim * 2);
+	if (!s && !c->d_xt64) s = upload_n(&c->d_xt64, NULL, (size_t)p->dim);
 	if (s) return s;
 	unsigned int *ctrl = c->d_xmax;
 	CUDA_TRY(cudaMemsetAsync(ctrl, 0, 2 * sizeof(unsigned int), st));
-	jn_launch_prep(d_x, f32 ? c->d_x32 : NULL, p->dim, ctrl, st);
-	if (pre) cudaEventRecord(pre, st);
-	const size_t smem = (size_t)(p->dim ? p->dim : 1) * 2 * sizeof(unsigned int);
-	if (p->nptasks) {
+	jn_launch_prep(d_x, NULL, p->dim, ctrl, st);
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (p->nblocks) {
 		if (f32)
-			jn_panel_kernel<float><<<c->panel_grid, PANEL_THREADS, smem, st>>>(
-				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, (const uint2 *)c->d_pflush,
-				c->d_pflush_ptr, c->d_pmeta, c->d_coef32, c->d_x32, c->d_gacc, ctrl, p->abs_bound, (int)p->dim);
+			jn_panel_x_kernel<int><<<p->nblocks, 256, 0, st>>>(d_x, c->d_xi, c->d_xi + p->dim, (const uint4 *)c->d_pblocks, ctrl);
 		else
-			jn_panel_kernel<double><<<c->panel_grid, PANEL_THREADS, smem, st>>>(
-				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, (const uint2 *)c->d_pflush,
-				c->d_pflush_ptr, c->d_pmeta, c->d_coef64, d_x, c->d_gacc, ctrl, p->abs_bound, (int)p->dim);
+			jn_panel_x_kernel<double><<<p->nblocks, 256, 0, st>>>(d_x, NULL, c->d_xt64, (const uint4 *)c->d_pblocks, ctrl);
+	}
+	if (pre) cudaEventRecord(pre, st);
+	const size_t smem = panel_smem(p, f32);
+	if (p->nptasks) {
+		if (f32) {
+			const FixInt32 fix = {};
+			jn_panel_kernel_i32<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
+				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
+				(const uint4 *)c->d_pblocks, c->d_pmeta, c->d_coefi, c->d_xi, c->d_xi + p->dim, c->d_gacc, fix,
+				(int)p->psmem_words);
+		} else {
+			jn_panel_kernel_fp64<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
+				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
+				(const uint4 *)c->d_pblocks, c->d_pmeta, c->d_coef64, d_x, c->d_xt64, c->d_gacc, ctrl,
+				p->abs_bound, (int)p->psmem_words);
+		}
 	}
 	if (mid) cudaEventRecord(mid, st);
-	jn_launch_finalize(c->d_gacc, d_y, p->dim, ctrl, p->abs_bound, accumulate, st);
+	if (f32) {
+		if (p->dim) jn_int_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, ctrl, c->pint_k - c->pint_sc, accumulate);
+	} else {
+		jn_launch_finalize(c->d_gacc, d_y, p->dim, ctrl, p->abs_bound, accumulate, st);
+	}
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "panel product launch: %s", cudaGetErrorString(e));
 	return JN_OK;

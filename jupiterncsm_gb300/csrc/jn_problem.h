@@ -163,13 +163,16 @@ typedef struct {
  * s_p s_n M[k_n + Nd k_p] (NP), s_n M[k_n] (N, per column) or s_p M[k_p]
  * (P, per row), with the single-species |M| < 1e-12 skip stored as 0.  NP
  * coefficients are stored densely, row-major, so a product streams them
- * once.  Forward: y[out + P_o Nn_out + N_o] += c x[in + P_i Nn_in + N_i];
+ * once; an NP panel whose neutron list is longer than its proton list is
+ * stored transposed (JN_PANEL_ROWS_N), so that the columns are the shorter
+ * list and a warp's lanes cover whole rows.  Forward: y[out + P_o Nn_out + N_o] += c x[in + P_i Nn_in + N_i];
  * off-diagonal panels also add c x[out + P_o Nn_out + N_o] into
  * y[in + P_i Nn_in + N_i].
  */
-#define JN_PANEL_DIAG 8
-#define JN_PANEL_ITER 32        /* rows a lane walks per task */
-#define JN_PANEL_MAX_DIM 28672  /* the whole accumulator (8 B per state) lives in shared memory */
+#define JN_PANEL_DIAG 8          /* input block == output block: no transpose */
+#define JN_PANEL_ROWS_N 16       /* NP panel stored transposed: rows are neutron entries, columns proton entries */
+#define JN_PANEL_ITER 32         /* rows a lane walks per task */
+#define JN_PANEL_MAX_DIM 26624   /* the accumulator (8 B per state, rows padded to an odd length) in shared memory */
 
 typedef struct {
 	int64_t c_off;          /* first coefficient */
@@ -178,7 +181,9 @@ typedef struct {
 	int32_t out_off, in_off;        /* offsets of the output and input blocks */
 	int32_t Nn_out, Nn_in;
 	int32_t ncols, kind;    /* kind: JN_KIND_* | JN_PANEL_DIAG when input block == output block */
+	int32_t out_soff, in_soff;      /* the blocks' offsets in the shared-memory accumulator */
 	int32_t nrows, instr;   /* rows; the evaluation-order index of the instruction */
+	int32_t Np_out, Np_in;  /* proton dimensions: strides of the blocks' transposed copy of x */
 } jn_panel_t;
 
 typedef struct {
@@ -217,10 +222,12 @@ typedef struct {
 	double visits;                  /* multiply-adds per product (both directions) */
 	/* panel engine (built by jn_panels_build) */
 	int npanels;       jn_panel_t *panels;
-	int64_t nptasks;   uint32_t *ptasks;   /* 4 words per warp task: panel, j0, j1, i0 | log2(lanes per row) << 24 */
+	int64_t nptasks;   uint32_t *ptasks;   /* 4 words per warp task: panel, j0, j1, i0 | lanes per row << 24 */
 	int pgrid;         uint32_t *pcta;     /* pgrid + 1 task offsets: CTA b runs [pcta[b], pcta[b+1]) */
 	uint32_t *pflush_ptr;                   /* pgrid + 1 offsets into pflush */
-	int64_t npflush;   uint32_t *pflush;   /* pairs {offset, length}: the ranges of y a CTA touches */
+	int64_t npflush;   uint32_t *pflush;   /* the blocks a CTA touches (block indices) */
+	uint32_t *pblocks;                      /* per block: {offset in y, offset in the accumulator, Np, Nn} */
+	int64_t psmem_words;                    /* accumulator length: sum of Np * (Nn | 1) */
 	int64_t n_pmeta;   uint32_t *pmeta;
 	int64_t n_coef;                         /* coefficients of all panels */
 } jn_plan_t;
@@ -257,6 +264,12 @@ void jn_panels_free(jn_plan_t *plan);
 /* panel coefficients from matrix elements in the plan's layout: FP64 into c64
  * and/or FP32 into c32 (either may be NULL), n_coef values each */
 void jn_panels_coefficients(const jn_plan_t *plan, const double *me, double *c64, float *c32);
+/* the 32-bit product's coefficients: c_int = round(c 2^Sc) with |c_int| <= 2^30,
+ * and the shift k (>= 30) that rounds each product (c_int x_int) to a 32-bit
+ * integer and keeps every element's sum below 2^62 for |x_int| <= 2^30
+ * (from the plan's abs_bound).  Returns 0, or 1 when the host runs out of
+ * memory. */
+int jn_panels_coefficients_int(const jn_plan_t *plan, const double *me, int32_t *ci, int *Sc, int *k);
 
 #ifdef __cplusplus
 }

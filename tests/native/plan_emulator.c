@@ -265,78 +265,69 @@ void emu_task_stats(void *h, double *out)
 
 /* ------------------------------------------------------------------ */
 /* panel engine: CPU model of jn_panel_kernel, lane for lane, with every
- * index checked.  Lane (r, c) of a task walks rows j0 + r, j0 + r + R, ...
- * of column i0 + c, sums consecutive rows with one output row in T
- * arithmetic and rounds each such run once; the transposed contribution of
- * an off-diagonal panel is rounded per product.  The fixed-point sums are
- * exact, so the model reproduces the GPU bit for bit. */
+ * index checked.  FP64: every contribution (c x) 2^S is rounded once to an
+ * integer and added.  32-bit: coefficients and x are 32-bit fixed-point
+ * integers, and every exact 64-bit product is rounded once by the shift k.  The fixed-point sums are exact, so the model reproduces the GPU
+ * bit for bit. */
 static void panel_lane_model(const jn_plan_t *P, const jn_panel_t *pn, uint32_t j0, uint32_t j1, int R, int r, int i,
-			     const double *x64, const float *x32, const double *c64, const float *c32, int f32, int S,
-			     int64_t *acc)
+			     const double *x64, const int32_t *xi, const double *c64, const int32_t *ci, int f32, int S,
+			     int k, int64_t *acc)
 {
 	const int kind = pn->kind & 7, diag = (pn->kind & JN_PANEL_DIAG) != 0;
+	const int rows_n = kind == JN_KIND_NP && (pn->kind & JN_PANEL_ROWS_N);
+	const int MRo = rows_n ? 1 : pn->Nn_out, MCo = rows_n ? pn->Nn_out : 1;
+	const int MRi = rows_n ? 1 : pn->Nn_in, MCi = rows_n ? pn->Nn_in : 1;
 	const double scale = ldexp(1.0, S);
-	const float scalef = (float)scale;
-	int Ni, No;
+	const int64_t bias = k > 0 ? (int64_t)1 << (k - 1) : 0;
+	/* the shared-memory accumulator holds each block with rows padded to Nn | 1 */
+	CHECK(pn->out_soff >= 0 && pn->in_soff >= 0 && pn->out_soff < P->psmem_words && pn->in_soff < P->psmem_words);
+	int sc, dc;
 	if (kind == JN_KIND_P) {
-		Ni = No = i;
+		sc = dc = i;
 	} else {
 		CHECK((int64_t)pn->col_meta + i < P->n_pmeta);
 		const uint32_t m = P->pmeta[pn->col_meta + i];
-		Ni = (int)(m & 0xffffu);
-		No = (int)(m >> 16);
+		sc = (int)(m & 0xffffu);
+		dc = (int)(m >> 16);
 	}
-	CHECK(Ni < pn->Nn_in && No < pn->Nn_out);
-	int cur = -1;
-	double run = 0;
-	float runf = 0;
-#define FLUSH_RUN() do { \
-		const int64_t at = pn->out_off + (int64_t)cur * pn->Nn_out + No; \
-		CHECK(at >= 0 && at < P->dim); \
-		acc[at] += f32 ? (int64_t)llrintf(runf * scalef) : (int64_t)llrint(run * scale); \
-	} while (0)
 	for (uint32_t j = j0 + r; j < j1; j += R) {
-		int Pi, Po;
-		int64_t ci;
+		int sr, dr;
+		int64_t cidx;
 		if (kind == JN_KIND_N) {
-			Pi = Po = (int)j;
-			ci = pn->c_off + i;
+			sr = dr = (int)j;
+			cidx = pn->c_off + i;
 		} else {
 			CHECK((int64_t)pn->row_meta + j < P->n_pmeta);
 			const uint32_t m = P->pmeta[pn->row_meta + j];
-			Pi = (int)(m & 0xffffu);
-			Po = (int)(m >> 16);
-			ci = kind == JN_KIND_NP ? pn->c_off + (int64_t)j * pn->ncols + i : pn->c_off + j;
+			sr = (int)(m & 0xffffu);
+			dr = (int)(m >> 16);
+			cidx = kind == JN_KIND_NP ? pn->c_off + (int64_t)j * pn->ncols + i : pn->c_off + j;
 		}
-		CHECK(ci >= 0 && ci < P->n_coef);
-		const int64_t xi_at = pn->in_off + (int64_t)Pi * pn->Nn_in + Ni, xo_at = pn->out_off + (int64_t)Po * pn->Nn_out + No;
-		CHECK(xi_at >= 0 && xi_at < P->dim && xo_at >= 0 && xo_at < P->dim);
-		if (Po != cur) {
-			if (cur >= 0) FLUSH_RUN();
-			cur = Po;
-			run = 0;
-			runf = 0;
-		}
+		CHECK(cidx >= 0 && cidx < P->n_coef);
+		/* the element stays inside its blocks */
+		CHECK(rows_n ? (sr < pn->Nn_in && dr < pn->Nn_out) : (sc < pn->Nn_in && dc < pn->Nn_out));
+		const int64_t at_i = pn->in_off + (int64_t)sr * MRi + (int64_t)sc * MCi;
+		const int64_t at_o = pn->out_off + (int64_t)dr * MRo + (int64_t)dc * MCo;
+		CHECK(at_i >= 0 && at_i < P->dim && at_o >= 0 && at_o < P->dim);
+		/* the padded shared-memory positions stay inside the accumulator */
+		const int64_t so = pn->out_soff + (int64_t)(rows_n ? dc : dr) * (pn->Nn_out | 1) + (rows_n ? dr : dc);
+		const int64_t si = pn->in_soff + (int64_t)(rows_n ? sc : sr) * (pn->Nn_in | 1) + (rows_n ? sr : sc);
+		CHECK(so < P->psmem_words && si < P->psmem_words);
 		if (f32) {
-			const float cv = c32[ci];
-			runf = fmaf(cv, x32[xi_at], runf);
-			if (!diag) {
-				float t = cv * x32[xo_at];
-				t = t * scalef;
-				acc[xi_at] += (int64_t)llrintf(t);
-			}
+			/* 32-bit fixed point: exact 64-bit product, rounded by the shift k */
+			const int64_t cv = ci[cidx];
+			acc[at_o] += (cv * xi[at_i] + bias) >> k;
+			if (!diag) acc[at_i] += (cv * xi[at_o] + bias) >> k;
 		} else {
-			const double cv = c64[ci];
-			run = fma(cv, x64[xi_at], run);
+			const double cv = c64[cidx];
+			double t = cv * x64[at_i];
+			acc[at_o] += (int64_t)llrint(t * scale);
 			if (!diag) {
-				double t = cv * x64[xo_at];
-				t = t * scale;
-				acc[xi_at] += (int64_t)llrint(t);
+				t = cv * x64[at_o];
+				acc[at_i] += (int64_t)llrint(t * scale);
 			}
 		}
 	}
-	if (cur >= 0) FLUSH_RUN();
-#undef FLUSH_RUN
 }
 
 int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
@@ -344,38 +335,49 @@ int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
 	jn_plan_t *P = h;
 	char err[512];
 	emu_fail = 0;
-	if (!P->panels && jn_panels_build(P, 152 * 3, err, sizeof err)) {
+	if (!P->panels && jn_panels_build(P, 152 * 2, err, sizeof err)) {
 		fprintf(stderr, "plan emulator: %s\n", err);
 		return 1;
 	}
 	float xmax = 0;
-	float *x32 = malloc((P->dim ? P->dim : 1) * sizeof(float));
 	for (int64_t i = 0; i < P->dim; i++) {
-		x32[i] = (float)x[i];
 		float v = (float)fabs(x[i]) * 1.0000002f;
 		if (v > xmax) xmax = v;
 	}
-	double *c64 = f32 ? NULL : malloc((P->n_coef ? P->n_coef : 1) * sizeof(double));
-	float *c32 = f32 ? malloc((P->n_coef ? P->n_coef : 1) * sizeof(float)) : NULL;
-	jn_panels_coefficients(P, P->me, c64, c32);
 	const int S = fixed_exponent(xmax, P->abs_bound);
+	/* 32-bit path: x as 32-bit fixed point, |x| 2^Sx < 2^30 for the FP32 bound xmax */
+	uint32_t xb;
+	memcpy(&xb, &xmax, 4);
+	int Sx = 0;
+	if (xb & 0x7fffffffu) {
+		Sx = 30 - ((int)((xb >> 23) & 0xff) - 126);
+		Sx = Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
+	}
+	int32_t *xi = malloc((P->dim ? P->dim : 1) * sizeof(int32_t));
+	for (int64_t i = 0; i < P->dim; i++) xi[i] = (int32_t)llrint(x[i] * ldexp(1.0, Sx));
+	double *c64 = f32 ? NULL : malloc((P->n_coef ? P->n_coef : 1) * sizeof(double));
+	int32_t *ci = f32 ? malloc((P->n_coef ? P->n_coef : 1) * sizeof(int32_t)) : NULL;
+	int Sc = 0, k = 0;
+	if (f32) jn_panels_coefficients_int(P, P->me, ci, &Sc, &k);
+	else jn_panels_coefficients(P, P->me, c64, NULL);
 	int64_t *acc = calloc(P->dim ? P->dim : 1, sizeof(int64_t));
 	/* every task once, every CTA's task range covering all of them */
 	if (P->pcta[0] != 0 || P->pcta[P->pgrid] != (uint32_t)P->nptasks) { emu_fail = 1; fprintf(stderr, "plan emulator: CTA ranges\n"); }
-	for (int64_t k = 0; k < P->nptasks && !emu_fail; k++) {
-		const uint32_t *T = P->ptasks + 4 * k;
+	for (int64_t t = 0; t < P->nptasks && !emu_fail; t++) {
+		const uint32_t *T = P->ptasks + 4 * t;
 		if (T[0] >= (uint32_t)P->npanels) { emu_fail = 1; break; }
 		const jn_panel_t *pn = &P->panels[T[0]];
-		const int lg = (int)(T[3] >> 24), R = 32 >> lg;
-		if (lg > 5 || T[1] >= T[2] || T[2] > (uint32_t)pn->nrows) { emu_fail = 1; break; }
+		const int cw = (int)(T[3] >> 24);
+		if (cw < 1 || cw > 32 || T[1] >= T[2] || T[2] > (uint32_t)pn->nrows) { emu_fail = 1; break; }
+		const int R = 32 / cw;
 		for (int lane = 0; lane < 32 && !emu_fail; lane++) {
-			const int i = (int)(T[3] & 0xffffffu) + (lane & ((1 << lg) - 1));
-			if (i >= pn->ncols) continue;
-			panel_lane_model(P, pn, T[1], T[2], R, lane >> lg, i, x, x32, c64, c32, f32, S, acc);
+			const int r = lane / cw, i = (int)(T[3] & 0xffffffu) + (lane - r * cw);
+			if (r >= R || i >= pn->ncols) continue;
+			panel_lane_model(P, pn, T[1], T[2], R, r, i, x, xi, c64, ci, f32, S, k, acc);
 		}
 	}
-	const double unit = ldexp(1.0, -S);
+	const double unit = f32 ? ldexp(1.0, k - Sc - Sx) : ldexp(1.0, -S);
 	for (int64_t i = 0; i < P->dim; i++) y[i] = accumulate ? y[i] + (double)acc[i] * unit : (double)acc[i] * unit;
-	free(acc); free(x32); free(c64); free(c32);
+	free(acc); free(xi); free(c64); free(ci);
 	return emu_fail;
 }
