@@ -55,11 +55,19 @@ def measured_peaks():
         return None
 
 
-def profile_traffic(workload, precision):
-    """DRAM bytes (read + write) per launch of the tile kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"jn_tile_kernel_{workload}.md")
+KERNELS = {(4, 32): "jn_panel_kernel_i32", (4, 64): "jn_panel_kernel_fp64",
+           (3, 32): "jn_tile_kernel<float>", (3, 64): "jn_tile_kernel<double>"}
+# kernels launched per product: max|x|, [the panel engine's copies of x], the product, the conversion into y
+LAUNCHES = {4: 4, 3: 3, 2: 3}
+
+
+def profile_traffic(workload, engine, precision):
+    """DRAM bytes (read + write) per launch of the product kernel from the committed ncu summary, if any."""
+    name = "jn_panel_kernel" if engine == 4 else "jn_tile_kernel"
+    key = ("i32" if precision == 32 else "fp64") if engine == 4 else f"fp{precision}"
+    path = os.path.join(ROOT, "profiles", f"{name}_{workload}.md")
     try:
-        m = re.search(rf"dram_bytes_per_launch_fp{precision}:\s*([0-9.eE+]+)", open(path).read())
+        m = re.search(rf"dram_bytes_per_launch_{key}:\s*([0-9.eE+]+)", open(path).read())
         return float(m.group(1)) if m else None
     except OSError:
         return None
@@ -424,7 +432,8 @@ def main():
     ap.add_argument("--workload", default="he4_nmax6_2nf3nf", choices=sorted(WORKLOADS))
     ap.add_argument("--workdir", default=os.environ.get("JNCSM_BENCH_DIR", os.path.join(tempfile.gettempdir(), "jncsm_bench")))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--precision", type=int, default=64, choices=[64, 32])
+    ap.add_argument("--precision", type=int, default=32, choices=[64, 32],
+                    help="32: 32-bit fixed-point matrix elements and x with exact 64-bit sums (the headline); 64: FP64")
     ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
     ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solves/s leg")
     args = ap.parse_args()
@@ -536,12 +545,13 @@ def main():
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = bytes_step / (main_r["kernel_ms"] / 1e3) / 1e9
-    traffic = profile_traffic(args.workload, prec)
+    engine = H.active_engine()
+    traffic = profile_traffic(args.workload, engine, prec)
 
     def path_summary(r, p):
         b = bytes_for(p)
         return {"ms_per_step": r["ms_per_step"], "GB_per_s": b / (r["ms_per_step"] / 1e3) / 1e9,
-                "bytes_per_step": b, "tile_kernel_ms": r["kernel_ms"],
+                "bytes_per_step": b, "product_kernel_ms": r["kernel_ms"],
                 "hbm_frac": b / (r["kernel_ms"] / 1e3) / 1e9 / peak,
                 "fp64_multiply_adds_per_s" if p == 64 else "multiply_adds_per_s":
                     st["multiply_adds"] / (r["kernel_ms"] / 1e3)}
@@ -549,7 +559,9 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": main_r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == 64 else "f32 (matrix elements and x; compensated sums; f64 in/out)",
+            "dtype": "f64" if prec == 64 else "i32",
+            "arithmetic": "FP64 products, exact 64-bit fixed-point sums" if prec == 64 else
+                          "32-bit fixed-point matrix elements and x, exact 64-bit products and sums; FP64 x and y at the interface",
             "data": "synthetic",
             "config": {"workload": w["label"], "dimension": D, "instructions": st["num_instructions"],
                        "list_entries": st["list_entries"], "me_elements": st["me_elements"],
@@ -557,14 +569,15 @@ def main():
                        "multiply_adds": st["multiply_adds"], "bytes_per_step": bytes_step,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                        "precision": prec, "work_units": st["num_work_units"], "pieces": st["num_tiles"]},
-            "paths": {"fp64": path_summary(r64, 64), "fp32": path_summary(r32, 32),
-                      "fp32_max_rel_diff_vs_fp64": rel32},
+            "paths": {"fp64": path_summary(r64, 64), "i32": path_summary(r32, 32),
+                      "i32_max_rel_diff_vs_fp64": rel32},
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * D, "d2h_bytes_per_step": 8 * D},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": LAUNCHES.get(engine, 3) * args.steps,
+            "engine": engine,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
-                         "kernel": "jn_tile_kernel<double>" if prec == 64 else "jn_tile_kernel<float>"},
+                         "kernel": KERNELS.get((engine, prec))},
             "clocks": main_r["clocks"]}
     if rank == 0 and not args.no_transform:
         try:

@@ -152,6 +152,11 @@ jn_status jn_set_precision(jn_ctx *ctx, int precision);
  * 32-element piece, FP64 sums in fixed term order. */
 jn_status jn_set_engine(jn_ctx *ctx, int engine);
 
+/* The engine the next product of this context runs at its current
+ * precision (the panel engine falls back to block tiles where its
+ * accumulator does not fit), or -1 for a NULL context. */
+int jn_active_engine(const jn_ctx *ctx);
+
 /* Synchronise the context's stream. */
 jn_status jn_synchronize(jn_ctx *ctx);
 

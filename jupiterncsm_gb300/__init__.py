@@ -145,6 +145,8 @@ def gpu_lib():
     L.jn_transform_2nf.argtypes = [cp, cp, cp, ci, ci, ci, ci, cp, ci]
     L.jn_clebsch_gordan.argtypes = [ci] * 6
     L.jn_clebsch_gordan.restype = ctypes.c_double
+    L.jn_active_engine.argtypes = [vp]
+    L.jn_active_engine.restype = ci
     fp = ctypes.POINTER(ctypes.c_float)
     L.jn_mlp_create.argtypes = [ci, ci, ci, ctypes.c_uint64, ctypes.POINTER(vp)]
     L.jn_mlp_destroy.argtypes = [vp]
@@ -316,8 +318,12 @@ class Hamiltonian:
     def save_eigenvectors(self, directory, count):
         _check(gpu_lib().jn_lanczos_save_eigenvectors(self._h, directory.encode(), int(count)))
 
+    def active_engine(self):
+        """The engine the next product runs (4 panels, 3 block tiles, 2 warp pieces)."""
+        return gpu_lib().jn_active_engine(self._h)
+
     def set_engine(self, engine):
-        """3: block tiles with exact fixed-point sums (default); 2: warp pieces."""
+        """4: panels (default where the accumulator fits in shared memory); 3: block tiles; 2: warp pieces."""
         _check(gpu_lib().jn_set_engine(self._h, int(engine)))
 
     def matvec_files(self, out_dir, in_dir):

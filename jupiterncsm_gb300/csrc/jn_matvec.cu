@@ -769,6 +769,13 @@ extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 	return JN_OK;
 }
 
+extern "C" int jn_active_engine(const jn_ctx *c)
+{
+	if (!c) return -1;
+	if (c->engine == 4 && !jn_panels_fit(c, c->precision == 32)) return 3;
+	return c->engine;
+}
+
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st)
 {
 	return enqueue(c, d_x, d_y, accumulate, st, NULL, NULL);
