@@ -152,6 +152,30 @@ jn_status jn_set_precision(jn_ctx *ctx, int precision);
  * 32-element piece, FP64 sums in fixed term order. */
 jn_status jn_set_engine(jn_ctx *ctx, int engine);
 
+/*
+ * Autotuner.  Times candidate schedules of the product on the context's own
+ * problem and precision: for the panel engine, rows per lane per warp task
+ * (8 ... 128) x persistent CTAs per SM; with tune_engine also the
+ * block-tile engine.  The fastest (median of `trials` CUDA-event timings of
+ * the product kernel, caches warm) is installed.  The panel engine's
+ * schedule never changes a result bit (each contribution is rounded on its
+ * own); switching engines changes results at the 1e-15 level, so
+ * tune_engine = 0 keeps them bit-identical to the untuned context.  No
+ * counterpart in the reference, whose evaluation order comes from Mars
+ * (src/Mars/programs/mars.c:92-170).
+ */
+typedef struct {
+	int engine;             /* 4 panels, 3 block tiles */
+	int rows_per_lane;      /* panel tasks: rows a lane walks */
+	int ctas_per_sm;        /* panel kernels: persistent CTAs per SM */
+	float ms;               /* product-kernel time of the choice */
+	int candidates;         /* schedules timed */
+} jn_tuning;
+jn_status jn_autotune(jn_ctx *ctx, int trials, int tune_engine, jn_tuning *tuning);
+
+/* Install a panel schedule directly (rows per lane, CTAs per SM). */
+jn_status jn_set_panel_schedule(jn_ctx *ctx, int rows_per_lane, int ctas_per_sm);
+
 /* The engine the next product of this context runs at its current
  * precision (the panel engine falls back to block tiles where its
  * accumulator does not fit), or -1 for a NULL context. */

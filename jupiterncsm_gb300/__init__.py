@@ -75,6 +75,11 @@ class TransformStats(ctypes.Structure):
                 ("algorithmic_bytes", ctypes.c_double), ("plan_seconds", ctypes.c_double)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("engine", ctypes.c_int), ("rows_per_lane", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
+                ("ms", ctypes.c_float), ("candidates", ctypes.c_int)]
+
+
 class WarmStartOptions(ctypes.Structure):
     _fields_ = [("hidden", ctypes.c_int), ("basis_size", ctypes.c_int), ("train_steps", ctypes.c_int),
                 ("learning_rate", ctypes.c_float), ("seed", ctypes.c_uint64), ("noise", ctypes.c_double)]
@@ -145,6 +150,10 @@ def gpu_lib():
     L.jn_transform_2nf.argtypes = [cp, cp, cp, ci, ci, ci, ci, cp, ci]
     L.jn_clebsch_gordan.argtypes = [ci] * 6
     L.jn_clebsch_gordan.restype = ctypes.c_double
+    L.jn_autotune.argtypes = [vp, ci, ci, ctypes.POINTER(Tuning)]
+    L.jn_autotune.restype = ci
+    L.jn_set_panel_schedule.argtypes = [vp, ci, ci]
+    L.jn_set_panel_schedule.restype = ci
     L.jn_active_engine.argtypes = [vp]
     L.jn_active_engine.restype = ci
     fp = ctypes.POINTER(ctypes.c_float)
@@ -317,6 +326,15 @@ class Hamiltonian:
 
     def save_eigenvectors(self, directory, count):
         _check(gpu_lib().jn_lanczos_save_eigenvectors(self._h, directory.encode(), int(count)))
+
+    def autotune(self, trials=5, tune_engine=False):
+        """Time candidate product schedules on this problem and install the fastest (jn_autotune)."""
+        t = Tuning()
+        _check(gpu_lib().jn_autotune(self._h, int(trials), int(tune_engine), ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in Tuning._fields_}
+
+    def set_panel_schedule(self, rows_per_lane, ctas_per_sm):
+        _check(gpu_lib().jn_set_panel_schedule(self._h, int(rows_per_lane), int(ctas_per_sm)))
 
     def active_engine(self):
         """The engine the next product runs (4 panels, 3 block tiles, 2 warp pieces)."""

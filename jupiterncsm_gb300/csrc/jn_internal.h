@@ -60,6 +60,7 @@ struct jn_ctx {
 	int pint_sc, pint_k;            /* coefficient exponent and product shift of the 32-bit path */
 	int panel_grid;                 /* persistent CTAs; 0 until set up */
 	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
+	int panel_iter;                 /* rows a lane walks per panel task */
 };
 
 /* enqueue y (+)= H x on stream st */

@@ -39,7 +39,7 @@ static int cmp_panel(const void *a, const void *b)
 	return *(const int *)a - *(const int *)b;
 }
 
-int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
+int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 {
 	int *order = NULL;
 	double *cost = NULL;
@@ -47,6 +47,7 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 	jn_panels_free(p);
 	if (p->dim > JN_PANEL_MAX_DIM) ERR("dimension %lld is above the panel engine's %d", (long long)p->dim, JN_PANEL_MAX_DIM);
 	if (grid < 1) ERR("panel grid of %d CTAs", grid);
+	if (iter < 1 || iter > 4096) ERR("panel tasks of %d rows per lane", iter);
 	/* accumulator layout: block rows padded to an odd length, so that a warp
 	   walking a column (stride Nn) hits 32 different shared-memory banks */
 	p->pblocks = malloc((p->nblocks ? p->nblocks : 1) * 4 * sizeof(uint32_t));
@@ -121,7 +122,7 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 		if (x->kind == JN_KIND_N && P->nrows > 65535) ERR("instruction %d: %d spectator rows", order[q], P->nrows);
 		if (P->nrows > 0 && P->ncols > 0) {
 			const int R = 32 / lanes_per_row(P->ncols);
-			const int64_t rows_per_task = (int64_t)R * JN_PANEL_ITER;
+			const int64_t rows_per_task = (int64_t)R * iter;
 			ntask += ((P->ncols + 31) / 32) * ((P->nrows + rows_per_task - 1) / rows_per_task);
 		}
 	}
@@ -136,7 +137,7 @@ int jn_panels_build(jn_plan_t *p, int grid, char *err, size_t errlen)
 		const jn_panel_t *P = &p->panels[q];
 		if (P->nrows <= 0 || P->ncols <= 0) continue;
 		const int cw = lanes_per_row(P->ncols), R = 32 / cw;
-		const int64_t rows_per_task = (int64_t)R * JN_PANEL_ITER;
+		const int64_t rows_per_task = (int64_t)R * iter;
 		const int diag = (P->kind & JN_PANEL_DIAG) != 0;
 		for (int i0 = 0; i0 < P->ncols; i0 += 32)
 			for (int64_t j0 = 0; j0 < P->nrows; j0 += rows_per_task) {

@@ -300,7 +300,7 @@ jn_status jn_panels_setup(jn_ctx *c)
 	int per[2] = { 0, 0 };
 	char err[512] = { 0 };
 	/* the accumulator layout does not depend on the grid: plan once to size it */
-	if (jn_panels_build(p, 1, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	if (jn_panels_build(p, 1, JN_PANEL_ITER, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
 	for (int f32 = 0; f32 < 2; f32++) {
 		const size_t smem = panel_smem(p, f32);
 		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
@@ -317,7 +317,9 @@ jn_status jn_panels_setup(jn_ctx *c)
 	c->panel_per_sm[0] = per[0];
 	c->panel_per_sm[1] = per[1];
 	/* the task split is the same for every grid; CTAs take contiguous runs of the FP32 grid */
-	if (jn_panels_build(p, c->num_sms * per[1], err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	if (jn_panels_build(p, c->num_sms * per[1], JN_PANEL_ITER, err, sizeof err))
+		return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	c->panel_iter = JN_PANEL_ITER;
 	jn_status s;
 	if ((s = upload_n(&c->d_panels, p->panels, (size_t)p->npanels)) ||
 	    (s = upload_n(&c->d_ptasks, p->ptasks, (size_t)p->nptasks * 4)) ||
@@ -413,5 +415,115 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 	}
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "panel product launch: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* schedule and autotuner                                              */
+/* ------------------------------------------------------------------ */
+/* replace the task split and the persistent grid of the panel plan (the
+ * panels, list entries, blocks and coefficients stay) */
+static jn_status panel_schedule(jn_ctx *c, int iter, int per_sm)
+{
+	jn_plan_t *p = &c->plan;
+	char err[512] = { 0 };
+	if (per_sm < 1 || per_sm > c->panel_per_sm[1] || (c->panel_per_sm[0] && per_sm > c->panel_per_sm[0]))
+		return jn_fail(JN_ERR_INVALID, "%d CTAs per SM: the panel kernels fit %d (FP64 %d)", per_sm, c->panel_per_sm[1],
+			       c->panel_per_sm[0]);
+	if (iter < 1 || iter > 4096) return jn_fail(JN_ERR_INVALID, "%d rows per lane: must be in 1..4096", iter);
+	if (jn_panels_build(p, c->num_sms * per_sm, iter, err, sizeof err)) {
+		/* the host plan is gone: drop the device side too, products fall back to block tiles */
+		jn_panels_release(c);
+		return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
+	}
+	cudaFree(c->d_ptasks); cudaFree(c->d_pcta); cudaFree(c->d_pflush); cudaFree(c->d_pflush_ptr);
+	c->d_ptasks = c->d_pcta = c->d_pflush = c->d_pflush_ptr = NULL;
+	jn_status s;
+	if ((s = upload_n(&c->d_ptasks, p->ptasks, (size_t)p->nptasks * 4)) ||
+	    (s = upload_n(&c->d_pcta, p->pcta, (size_t)p->pgrid + 1)) ||
+	    (s = upload_n(&c->d_pflush_ptr, p->pflush_ptr, (size_t)p->pgrid + 1)) ||
+	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush))) {
+		jn_panels_release(c);
+		return s;
+	}
+	c->panel_grid = p->pgrid;
+	c->panel_iter = iter;
+	return JN_OK;
+}
+
+extern "C" jn_status jn_set_panel_schedule(jn_ctx *c, int rows_per_lane, int ctas_per_sm)
+{
+	if (!c) return jn_fail(JN_ERR_INVALID, "null argument");
+	jn_status s = jn_panels_setup(c);
+	return s ? s : panel_schedule(c, rows_per_lane, ctas_per_sm);
+}
+
+/* median CUDA-event time of the product kernel over `trials` products (after one warm-up) */
+static jn_status time_product(jn_ctx *c, int trials, float *ms)
+{
+	float t[64];
+	if (trials > 64) trials = 64;
+	for (int k = -1; k < trials; k++) {
+		float m[2];
+		jn_status s = jn_matvec_profile(c, c->d_x, c->d_y, 0, m);
+		if (s) return s;
+		if (k >= 0) t[k] = m[0];
+	}
+	for (int i = 1; i < trials; i++)
+		for (int j = i; j > 0 && t[j] < t[j - 1]; j--) { float u = t[j]; t[j] = t[j - 1]; t[j - 1] = u; }
+	*ms = t[trials / 2];
+	return JN_OK;
+}
+
+__global__ void jn_tune_x_kernel(double *x, int64_t n)
+{
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		x[i] = 1.0 + 0.5 * sin(0.37 * (double)i);
+}
+
+extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out)
+{
+	if (!c || !out) return jn_fail(JN_ERR_INVALID, "null argument");
+	if (trials < 1) trials = 5;
+	memset(out, 0, sizeof *out);
+	const jn_plan_t *p = &c->plan;
+	const int f32 = c->precision == 32;
+	jn_tune_x_kernel<<<64, 256, 0, c->stream>>>(c->d_x, p->dim);
+	CUDA_TRY(cudaGetLastError());
+	const int engine0 = c->engine;
+	float best = 3.4e38f;
+	int best_engine = engine0, best_iter = c->panel_iter, best_per = c->panel_grid / (c->num_sms ? c->num_sms : 1);
+	if (jn_panels_setup(c) == JN_OK && jn_panels_fit(c, f32) && (engine0 == 4 || tune_engine)) {
+		const int iters[] = { 8, 16, 32, 64, 128 };
+		const int maxper = c->panel_per_sm[0] && c->panel_per_sm[0] < c->panel_per_sm[1] ? c->panel_per_sm[0]
+												    : c->panel_per_sm[1];
+		c->engine = 4;
+		for (size_t a = 0; a < sizeof iters / sizeof iters[0]; a++)
+			for (int per = 1; per <= maxper; per++) {
+				float ms;
+				jn_status s = panel_schedule(c, iters[a], per);
+				if (!s) s = time_product(c, trials, &ms);
+				if (s) { c->engine = engine0; return s; }
+				out->candidates++;
+				if (ms < best) { best = ms; best_engine = 4; best_iter = iters[a]; best_per = per; }
+			}
+	}
+	if (tune_engine || engine0 != 4) {
+		float ms;
+		c->engine = 3;
+		jn_status s = time_product(c, trials, &ms);
+		if (s) { c->engine = engine0; return s; }
+		out->candidates++;
+		if (ms < best) { best = ms; best_engine = 3; }
+	}
+	c->engine = best_engine;
+	if (best_engine == 4) {
+		jn_status s = panel_schedule(c, best_iter, best_per);
+		if (s) return s;
+	}
+	out->engine = best_engine;
+	out->rows_per_lane = best_engine == 4 ? best_iter : 0;
+	out->ctas_per_sm = best_engine == 4 ? best_per : 0;
+	out->ms = best;
 	return JN_OK;
 }

@@ -171,7 +171,7 @@ typedef struct {
  */
 #define JN_PANEL_DIAG 8          /* input block == output block: no transpose */
 #define JN_PANEL_ROWS_N 16       /* NP panel stored transposed: rows are neutron entries, columns proton entries */
-#define JN_PANEL_ITER 32         /* rows a lane walks per task */
+#define JN_PANEL_ITER 32         /* rows a lane walks per task (default; the autotuner may choose another) */
 #define JN_PANEL_MAX_DIM 26624   /* the accumulator (8 B per state, rows padded to an odd length) in shared memory */
 
 typedef struct {
@@ -258,8 +258,11 @@ double jn_plan_abs_bound(const jn_plan_t *plan, const double *me);
 /* read the <id>_matrix_elements files of `dir` into out (plan->n_me values,
  * the plan's layout); every block must have the plan's dimensions */
 int jn_plan_read_me(const jn_plan_t *plan, const char *dir, double *out, char *err, size_t errlen);
-/* the panel plan for a persistent grid of `grid` CTAs (dimension <= JN_PANEL_MAX_DIM) */
-int jn_panels_build(jn_plan_t *plan, int grid, char *err, size_t errlen);
+/* the panel plan for a persistent grid of `grid` CTAs whose warp tasks walk
+ * `iter` rows per lane (dimension <= JN_PANEL_MAX_DIM).  The tasks and the
+ * grid decide only who computes a contribution, never its rounding: every
+ * schedule gives bit-identical products. */
+int jn_panels_build(jn_plan_t *plan, int grid, int iter, char *err, size_t errlen);
 void jn_panels_free(jn_plan_t *plan);
 /* panel coefficients from matrix elements in the plan's layout: FP64 into c64
  * and/or FP32 into c32 (either may be NULL), n_coef values each */

@@ -335,7 +335,7 @@ int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
 	jn_plan_t *P = h;
 	char err[512];
 	emu_fail = 0;
-	if (!P->panels && jn_panels_build(P, 152 * 2, err, sizeof err)) {
+	if (!P->panels && jn_panels_build(P, 152 * 2, JN_PANEL_ITER, err, sizeof err)) {
 		fprintf(stderr, "plan emulator: %s\n", err);
 		return 1;
 	}

@@ -192,3 +192,38 @@ def test_panel_engine_after_new_matrix_elements(problem):
     b = H.matvec(x)
     assert np.abs(b - 2.5 * a).max() <= 1e-12 * np.abs(b).max()
     H.close()
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_panel_schedules_do_not_change_a_bit(problem, bits):
+    """Every panel schedule (rows per lane, CTAs per SM) gives the same bits, and
+    the autotuner installs one of them without changing the product."""
+    d, Z, N, *_ = problem("he4_n6_3b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.set_precision(bits)
+    x = np.random.default_rng(25).standard_normal(H.dimension)
+    want = H.matvec(x)
+    for rows, per in ((8, 1), (64, 2), (128, 3)):
+        H.set_panel_schedule(rows, per)
+        assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
+    t = H.autotune(trials=3)
+    assert t["engine"] == 4 and t["candidates"] >= 5 and t["ms"] > 0
+    assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
+    with pytest.raises(jn.JnError):
+        H.set_panel_schedule(0, 1)
+    with pytest.raises(jn.JnError):
+        H.set_panel_schedule(32, 99)
+    # the context still works after a rejected schedule
+    assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
+    H.close()
+
+
+def test_autotune_may_choose_the_engine(problem):
+    d, Z, N, *_ = problem("he4_n4_2b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    x = np.random.default_rng(26).standard_normal(H.dimension)
+    t = H.autotune(trials=3, tune_engine=True)
+    assert t["engine"] in (3, 4) and H.active_engine() == t["engine"]
+    ref = oracle.Port(d).matvec(x)
+    assert np.abs(H.matvec(x) - ref).max() <= 1e-12 * np.abs(ref).max()
+    H.close()
