@@ -464,6 +464,38 @@ void jn_warm_start_destroy(jn_warm_start *warm_start);
  * start_vectors is NULL), dim values, host. */
 void jn_default_start_vector(int64_t dim, double *out);
 
+/* ------------------------------------------------------------------ */
+/* File tools around the product (host only, no GPU needed)            */
+/* ------------------------------------------------------------------ */
+/* Aurora: convert the Anicre index lists under anicre_dir,
+ * <type>_inds_index_lists/index_list_E_in<Eb>_E_out<Ek>_M_in<Mb>_M_out<Mk>_dE<dE>_dM<dM>_depth<d>
+ * (raw {in, out, k} int triples, or rows "in out +k" / "in out -k" when
+ * human_readable), into <output_dir>/index_list_<id> for every list row of
+ * the combination table; with skip_three_body the three-particle lists are
+ * left out.  Lists Anicre did not write are reported on stderr and skipped,
+ * as aurora.x does (src/Aurora/programs/aurora.c:21-96,
+ * src/Aurora/index_list/index_list.c:21-112).  converted (may be NULL)
+ * receives the number of lists written. */
+jn_status jn_aurora(const char *combination_table_file, const char *anicre_dir, const char *output_dir,
+		    int num_protons, int num_neutrons, int human_readable, int skip_three_body, int *converted);
+
+/* Mars: an evaluation order ("BLOCK: in out list [list] me" rows) from the
+ * CALCBLOCK rows of the combination table, two-body blocks and, unless
+ * two_body_only, three-body blocks; one-body blocks are zero and left out
+ * (src/Mars/programs/mars.c:64-199).  The rows come in the panel engine's
+ * schedule order (output block, input block, most multiplications first)
+ * instead of Mars' cache-reuse sort; the reference's Bacchus accepts any
+ * order.  num_rows (may be NULL) receives the number of rows written. */
+jn_status jn_mars(const char *combination_table_file, int num_protons, int num_neutrons, const char *output_file,
+		  int two_body_only, int *num_rows);
+
+/* Vulcan: <output_dir>/<id>_matrix_elements = sum_i coefficients[i] *
+ * <operator_dirs[i]>/<id>_matrix_elements for every matrix-element block of
+ * the combination table, a missing block counting as zero, in the
+ * reference's block format (src/Vulcan/programs/vulcan.c:47-207). */
+jn_status jn_vulcan(const char *combination_table_file, int num_protons, int num_neutrons, int num_operators,
+		    const char *const *operator_dirs, const double *coefficients, const char *output_dir);
+
 #ifdef __cplusplus
 }
 #endif

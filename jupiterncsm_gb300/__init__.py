@@ -180,6 +180,11 @@ def gpu_lib():
                  "jn_mlp_train", "jn_mlp_predict", "jn_warm_start_fit", "jn_warm_start_vectors",
                  "jn_warm_start_basis"):
         getattr(L, name).restype = ci
+    L.jn_aurora.argtypes = [cp, cp, cp, ci, ci, ci, ci, ctypes.POINTER(ci)]
+    L.jn_mars.argtypes = [cp, ci, ci, cp, ci, ctypes.POINTER(ci)]
+    L.jn_vulcan.argtypes = [cp, ci, ci, ci, vp, vp, cp]
+    for name in ("jn_aurora", "jn_mars", "jn_vulcan"):
+        getattr(L, name).restype = ci
     for name in ("jn_open", "jn_open_files", "jn_block_info", "jn_matvec", "jn_matvec_device", "jn_matvec_files",
                  "jn_synchronize", "jn_get_plan_stats", "jn_matvec_profile", "jn_inspect_files", "jn_set_precision", "jn_set_engine", "jn_lanczos",
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
@@ -428,6 +433,31 @@ class MLP:
         return y
 
 
+def aurora(comb, anicre_dir, output_dir, Z, N, human_readable=False, skip_three_body=False):
+    """Anicre index lists -> index_list_<id> (jn_aurora, the aurora.x drop-in); returns the lists written."""
+    n = ctypes.c_int()
+    _check(gpu_lib().jn_aurora(comb.encode(), anicre_dir.encode(), output_dir.encode(), Z, N, int(human_readable),
+                               int(skip_three_body), ctypes.byref(n)))
+    return n.value
+
+
+def mars(comb, Z, N, output_file, two_body_only=False):
+    """Evaluation order from the combination table's CALCBLOCK rows (jn_mars, the mars.x drop-in)."""
+    n = ctypes.c_int()
+    _check(gpu_lib().jn_mars(comb.encode(), Z, N, output_file.encode(), int(two_body_only), ctypes.byref(n)))
+    return n.value
+
+
+def vulcan(comb, Z, N, operators, output_dir):
+    """sum_i c_i * operator_i over every matrix-element block (jn_vulcan, the vulcan.x drop-in);
+    operators: [(directory, coefficient), ...]."""
+    dirs = [d.encode() for d, _ in operators]
+    dp = (ctypes.c_char_p * max(1, len(dirs)))(*dirs)
+    cf = (ctypes.c_double * max(1, len(dirs)))(*[c for _, c in operators])
+    _check(gpu_lib().jn_vulcan(comb.encode(), Z, N, len(dirs), ctypes.cast(dp, ctypes.c_void_p),
+                               ctypes.cast(cf, ctypes.c_void_p), output_dir.encode()))
+
+
 def default_start_vector(dim):
     """The batched solver's default start vector (jn_default_start_vector)."""
     v = np.zeros(dim)
@@ -580,7 +610,7 @@ class GenConfig(ctypes.Structure):
                 ("parity", ctypes.c_int), ("nbody", ctypes.c_int), ("seed", ctypes.c_uint64),
                 ("hbar_omega", ctypes.c_double), ("sigma2", ctypes.c_double), ("sigma3", ctypes.c_double),
                 ("me_only", ctypes.c_int), ("me_subdir", ctypes.c_char_p), ("write_basis_files", ctypes.c_int),
-                ("lanczos_iterations", ctypes.c_int), ("antoine", ctypes.c_int)]
+                ("lanczos_iterations", ctypes.c_int), ("antoine", ctypes.c_int), ("anicre_lists", ctypes.c_int)]
 
 
 class GenSummary(ctypes.Structure):
@@ -612,12 +642,15 @@ def gen_lib():
 
 
 def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, hbar_omega=20.0, sigma2=1.0,
-             sigma3=0.1, me_only_subdir=None, basis_files=True, lanczos_iterations=200, antoine=False):
+             sigma3=0.1, me_only_subdir=None, basis_files=True, lanczos_iterations=200, antoine=False,
+             anicre_lists=0):
     """Write a synthetic problem in the reference formats; returns the generator summary.
 
     With antoine=True the two-body interaction is written as a J-scheme
     Antoine file (antoine_2nf.bin) and its M-scheme blocks are left to the
-    J->M transform."""
+    J->M transform.  anicre_lists=1 (raw) or 2 (text rows) also writes the
+    index lists under the names Anicre gives them (anicr_lists/), the input
+    of aurora.x / jn_aurora."""
     G = gen_lib()
     c = GenConfig()
     G.jn_gen_default_config(ctypes.byref(c))
@@ -626,6 +659,7 @@ def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, h
     c.write_basis_files = int(basis_files)
     c.lanczos_iterations = lanczos_iterations
     c.antoine = int(antoine)
+    c.anicre_lists = int(anicre_lists)
     if me_only_subdir:
         c.me_only = 1
         c.me_subdir = me_only_subdir.encode()

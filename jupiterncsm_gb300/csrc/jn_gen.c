@@ -1004,6 +1004,37 @@ static int write_lists(const gen_t *g, const char *dir)
 	return 0;
 }
 
+/* the lists as Anicre writes them, the input of aurora.x
+ * (src/Aurora/programs/aurora.c:64-96): raw {in, out, k} triples, or rows
+ * "in out +k" / "in out -k" with the sign taken out of bit 31 */
+static int write_anicre_lists(const gen_t *g, const char *outdir, int human_readable)
+{
+	char path[4096];
+	const ilist_t *L = g->lists.a;
+	for (size_t i = 0; i < g->lists.n; i++) {
+		if (!L[i].len) continue;
+		snprintf(path, sizeof path, "%s/anicr_lists/%s_inds_index_lists", outdir, ptype(L[i].species, L[i].k));
+		if (mkdir_p(path)) FAIL(JN_GEN_EIO, "mkdir %s", path);
+		snprintf(path, sizeof path, "%s/anicr_lists/%s_inds_index_lists/index_list_E_in%d_E_out%d_M_in%d_M_out%d_dE%d_dM%d_depth%d",
+			 outdir, ptype(L[i].species, L[i].k), L[i].Ein, L[i].Eout, L[i].Min, L[i].Mout, L[i].Eout - L[i].Ein,
+			 L[i].Mout - L[i].Min, L[i].depth);
+		FILE *f = fopen(path, human_readable ? "w" : "wb");
+		if (!f) FAIL(JN_GEN_EIO, "open %s: %s", path, strerror(errno));
+		int bad = 0;
+		if (!human_readable) {
+			bad = fwrite(L[i].data, 12, L[i].len, f) != L[i].len;
+		} else {
+			for (size_t e = 0; e < L[i].len && !bad; e++) {
+				const uint32_t k = L[i].data[3 * e + 2];
+				bad = fprintf(f, "%d %d %c%u\n", (int)L[i].data[3 * e], (int)L[i].data[3 * e + 1],
+					      (k & 0x80000000u) ? '-' : '+', k & 0x7fffffffu) < 0;
+			}
+		}
+		if (fclose(f) != 0 || bad) FAIL(JN_GEN_EIO, "write %s", path);
+	}
+	return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* public entry points                                                 */
 /* ------------------------------------------------------------------ */
@@ -1141,6 +1172,7 @@ int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *su
 		if ((rc = write_eval_order(g, path, order))) goto done;
 		if ((rc = write_conf(g, outdir))) goto done;
 		if (cfg->write_basis_files && (rc = write_basis_files(g, outdir))) goto done;
+		if (cfg->anicre_lists && (rc = write_anicre_lists(g, outdir, cfg->anicre_lists == 2))) goto done;
 	}
 	{
 		const char *medir = cfg->me_subdir && cfg->me_subdir[0] ? cfg->me_subdir : "matrix_elements";

@@ -35,6 +35,9 @@ typedef struct {
 	int antoine;            /* two-body interaction as a J-scheme Antoine file (antoine_2nf.bin)
 				   instead of M-scheme blocks: the two-body matrix-element blocks are
 				   then left to the J->M transform */
+	int anicre_lists;       /* also write the index lists as Anicre names them, under
+				   anicr_lists/<type>_inds_index_lists/: 1 raw triples, 2 rows "in out +-k"
+				   (the input of aurora.x) */
 } jn_gen_config;
 
 typedef struct {

@@ -10,8 +10,9 @@
 #include "../../include/jncsm.h"
 #include "jn_problem.h"
 
-/* records the message of a failure for jn_last_error() and returns s */
-jn_status jn_fail(jn_status s, const char *fmt, ...);
+/* records the message of a failure for jn_last_error() and returns s (C
+ * linkage: the host tools in C record their failures through it too) */
+extern "C" jn_status jn_fail(jn_status s, const char *fmt, ...);
 
 #define CUDA_TRY(call)                                                                          \
 	do {                                                                                    \

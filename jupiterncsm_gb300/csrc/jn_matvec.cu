@@ -36,7 +36,7 @@
 
 static thread_local char g_last_error[1024];
 
-jn_status jn_fail(jn_status s, const char *fmt, ...)
+extern "C" jn_status jn_fail(jn_status s, const char *fmt, ...)
 {
 	va_list ap;
 	va_start(ap, fmt);

@@ -12,6 +12,8 @@ being measured or shipped.
 * ``index_lists`` Python restatement of index-list construction
 * ``jt_transform`` Python restatement of the coupled basis, exact
                  Clebsch-Gordan coefficients and the Antoine file layout
+* ``reference_tool``  the reference's aurora.x, mars.x and vulcan.x, compiled
+                 unchanged into _ref/ when the reference tree is present
 * ``reference_transform``  the reference's own two-body J -> M transform,
                  compiled unchanged into _ref/ref_mercury (with a stand-in
                  for the absent wigxjpf library) when the reference tree is
@@ -31,6 +33,18 @@ REF_MERCURY = os.path.join(HERE, "_ref", "ref_mercury")
 
 def build():
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+
+
+REF_TOOLS = {name: os.path.join(HERE, "_ref", name) for name in ("aurora", "mars", "vulcan")}
+
+
+def reference_tool_available(name):
+    return os.path.exists(REF_TOOLS[name])
+
+
+def reference_tool(name, *args):
+    """Run the reference program `name` (aurora, mars or vulcan) with args; returns the completed process."""
+    return subprocess.run([REF_TOOLS[name], *map(str, args)], capture_output=True, text=True)
 
 
 def reference_available():
@@ -75,9 +89,10 @@ class Port:
             cls._lib = L
         return cls._lib
 
-    def __init__(self, d):
+    def __init__(self, d, order=None):
         e = lambda s: s.encode()
-        self.h = self.lib().port_open(e(f"{d}/comb.txt"), e(f"{d}/evaluation_order.txt"), e(f"{d}/index_lists"),
+        order = order or f"{d}/evaluation_order.txt"
+        self.h = self.lib().port_open(e(f"{d}/comb.txt"), e(order), e(f"{d}/index_lists"),
                                       e(f"{d}/matrix_elements"))
         if not self.h:
             raise RuntimeError(f"oracle port could not open {d}")

@@ -227,3 +227,20 @@ def test_autotune_may_choose_the_engine(problem):
     ref = oracle.Port(d).matvec(x)
     assert np.abs(H.matvec(x) - ref).max() <= 1e-12 * np.abs(ref).max()
     H.close()
+
+
+def test_mars_order_gives_the_same_product_bits(problem, tmp_path):
+    """The evaluation order jn_mars writes gives the panel engine's product bit for bit."""
+    d, Z, N, *_ = problem("he4_n6_3b")
+    order = str(tmp_path / "order.txt")
+    jn.mars(f"{d}/comb.txt", Z, N, order)
+    a = jn.Hamiltonian.from_dir(d, Z, N)
+    b = jn.Hamiltonian(comb=f"{d}/comb.txt", order=order, lists=f"{d}/index_lists", mes=f"{d}/matrix_elements",
+                       Z=Z, N=N)
+    x = np.random.default_rng(27).standard_normal(a.dimension)
+    for bits in (32, 64):
+        a.set_precision(bits)
+        b.set_precision(bits)
+        assert np.array_equal(a.matvec(x).view(np.uint64), b.matvec(x).view(np.uint64))
+    a.close()
+    b.close()
