@@ -93,23 +93,25 @@ __global__ void kb_three_term(double *__restrict__ W, const double *__restrict__
 	}
 }
 
-/* part[inst][blk][j] = V_j . w over the slice, j <= k */
+/* part[inst][blk][j] = V_j . w over the slice, j <= k: warp j % 8 owns
+ * vector j and reduces it with shuffles in a fixed order, so no CTA-wide
+ * barrier is taken per vector */
 __global__ void __launch_bounds__(BT) kb_gemv_t(const double *__restrict__ V, int64_t ldV, const double *__restrict__ W,
 						 const int *__restrict__ d_k, int64_t D, double *__restrict__ part, int ncol,
 						 const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
-	__shared__ double sh[BT];
 	const int nvec = *d_k + 1;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 	const double *w = W + inst * D;
 	int64_t i0, i1;
 	slice(D, &i0, &i1);
-	for (int j = 0; j < nvec; j++) {
+	for (int j = warp; j < nvec; j += nwarps) {
 		const double *v = V + inst * ldV + (int64_t)j * D;
 		double s = 0.0;
-		for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
-		s = jn_block_sum(s, sh);
-		if (threadIdx.x == 0) part[((int64_t)inst * gridDim.x + blockIdx.x) * ncol + j] = s;
+		for (int64_t i = i0 + lane; i < i1; i += 32) s = fma(v[i], w[i], s);
+		for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (lane == 0) part[((int64_t)inst * gridDim.x + blockIdx.x) * ncol + j] = s;
 	}
 }
 
@@ -170,15 +172,17 @@ __global__ void kb_advance(int *d_k) { if (threadIdx.x == 0 && blockIdx.x == 0) 
 /* ------------------------------------------------------------------ */
 /* batched tridiagonal work (n per instance)                            */
 /* ------------------------------------------------------------------ */
+/* one warp per eigenvalue i = blockIdx.x (multisection) */
 __global__ void kb_tri_bisect(const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
 			      const int *__restrict__ n_arr, int want, double *__restrict__ theta, int ldt,
 			      const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int i = blockIdx.x;
 	const int n = n_arr[inst];
 	if (i >= want || i >= n) return;
-	theta[(int64_t)inst * ldt + i] = jn_tri_bisect_one(alpha + inst * ldab, beta + inst * ldab, n, i);
+	const double v = jn_tri_multisect_warp(alpha + inst * ldab, beta + inst * ldab, n, i);
+	if (threadIdx.x == 0) theta[(int64_t)inst * ldt + i] = v;
 }
 
 __global__ void kb_tri_vectors(const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
@@ -404,13 +408,15 @@ struct bstate {
 	unsigned long long *gacc;
 	unsigned int *ctrl;
 	int *k, *active, *flag, *narr;
+	int *pcoef, *pxbuf;             /* panel engine: 32-bit coefficients and x of every instance */
+	unsigned long long *pcmax;
 };
 
 static void bstate_free(struct bstate *s)
 {
 	void *p[] = { s->V, s->W, s->me64, s->x64, s->alpha, s->beta, s->part, s->h, s->scal, s->theta, s->zlast, s->Z,
 		      s->work, s->X, s->HX, s->G, s->C, s->GS, s->me32, s->x32, s->gacc, s->ctrl, s->k, s->active,
-		      s->flag, s->narr };
+		      s->flag, s->narr, s->pcoef, s->pxbuf, s->pcmax };
 	for (size_t i = 0; i < sizeof p / sizeof p[0]; i++) cudaFree(p[i]);
 }
 
@@ -453,7 +459,9 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	BALLOC(s.V, (size_t)B * ldV);
 	BALLOC(s.W, (size_t)B * D);
 	BALLOC(s.me64, (size_t)B * nme);
-	if (f32) { BALLOC(s.me32, (size_t)B * nme); BALLOC(s.x32, (size_t)B * D); }
+	/* 32-bit products on the panel engine where it is this context's engine */
+	const int panels = f32 && c->engine == 4 && jn_panels_setup(c) == JN_OK && jn_panels_fit(c, 1);
+	if (f32 && !panels) { BALLOC(s.me32, (size_t)B * nme); BALLOC(s.x32, (size_t)B * D); }
 	else BALLOC(s.x64, (size_t)B * D);
 	BALLOC(s.alpha, (size_t)B * ldab);
 	BALLOC(s.beta, (size_t)B * ldab);
@@ -471,19 +479,24 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	BALLOC(s.active, B);
 	BALLOC(s.flag, B);
 	BALLOC(s.narr, B);
+	if (panels) {
+		BALLOC(s.pcoef, (size_t)B * (p->n_coef ? p->n_coef : 1));
+		BALLOC(s.pxbuf, (size_t)B * 2 * D);
+		BALLOC(s.pcmax, B);
+	}
 	if (st) { bstate_free(&s); return st; }
 
 	/* matrix elements: FP64 for refinement, FP32 copies with the reference's
 	   |M| < 1e-12 skip of single-species blocks (matrix_vector_multiplication.c:52-53) */
 	double maxme = 0.0;
-	float *h32 = f32 ? (float *)malloc(nme * sizeof(float)) : NULL;
+	float *h32 = f32 && !panels ? (float *)malloc(nme * sizeof(float)) : NULL;
 	for (int i = 0; i < B && !st; i++) {
 		const double *me = o->matrix_elements[i];
 		if (!me) { st = jn_fail(JN_ERR_INVALID, "matrix_elements[%d] is NULL", i); break; }
 		for (int64_t e = 0; e < nme; e++) maxme = fmax(maxme, fabs(me[e]));
 		if (cudaMemcpyAsync(s.me64 + (size_t)i * nme, me, nme * sizeof(double), cudaMemcpyHostToDevice, q) != cudaSuccess)
 			st = jn_fail(JN_ERR_CUDA, "upload of matrix elements");
-		if (f32 && !st) {
+		if (h32 && !st) {
 			for (int b = 0; b < p->nmes; b++) {
 				const jn_me_t *M = &p->mes[b];
 				for (int64_t e = 0; e < M->len; e++) {
@@ -498,6 +511,14 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	free(h32);
 	/* fixed-point scale bound valid for every instance */
 	const double abs_bound = jn_plan_abs_bound(p, NULL) * maxme;
+	if (!st && panels) st = jn_panels_batched_coefficients(c, B, s.me64, nme, s.pcoef, s.pcmax, q);
+	/* each instance gets about (resident CTAs) / B persistent CTAs */
+	jn_panel_partition part;
+	memset(&part, 0, sizeof part);
+	if (!st && panels) {
+		int g = c->num_sms * c->panel_per_sm[1] / B;
+		st = jn_panels_partition_upload(c, g < 8 ? 8 : g, &part);
+	}
 
 	/* start vectors: given, or one seeded pseudo-random vector for all */
 	double *hv = (double *)malloc(D * sizeof(double));
@@ -531,8 +552,11 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 
 	/* one Lanczos step for every active instance, k read on the device */
 	auto step = [&](cudaStream_t qs) -> jn_status {
-		jn_status e = jn_enqueue_batched(c, B, f32, f32 ? (const void *)s.me32 : (const void *)s.me64, nme, s.V, ldV,
-						 s.k, D, s.W, D, s.x64, s.x32, s.gacc, s.ctrl, s.active, abs_bound, qs);
+		jn_status e = panels ? jn_enqueue_panels_batched(c, B, s.pcoef, s.pcmax, s.V, ldV, s.k, D, s.W, D, s.pxbuf,
+								 s.gacc, s.ctrl, s.active, &part, qs)
+				     : jn_enqueue_batched(c, B, f32, f32 ? (const void *)s.me32 : (const void *)s.me64, nme,
+							  s.V, ldV, s.k, D, s.W, D, s.x64, s.x32, s.gacc, s.ctrl, s.active,
+							  abs_bound, qs);
 		if (e) return e;
 		kb_dot<<<gr, BT, 0, qs>>>(s.V, ldV, 1, s.W, D, 0, s.k, D, s.part, s.active);
 		kb_finish_dot<<<g1, 32, 0, qs>>>(s.part, BNB, s.alpha, ldab, 1, s.k, s.active);
@@ -572,7 +596,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		for (int i = 0; i < B; i++) hn[i] = hact[i] ? k : hn[i];
 		cudaMemcpyAsync(s.narr, hn, B * sizeof(int), cudaMemcpyHostToDevice, q);
 		const int wk = want < k ? want : k;
-		kb_tri_bisect<<<dim3((wk + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, wk, s.theta, r + 1, s.active);
+		kb_tri_bisect<<<dim3(wk, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, wk, s.theta, r + 1, s.active);
 		kb_tri_vectors<<<dim3((wk + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, wk, s.theta, r + 1, s.Z,
 									ldz, s.work, s.zlast, s.active);
 		kb_converged<<<(B + 127) / 128, 128, 0, q>>>(s.theta, s.zlast, r + 1, s.beta, ldab, s.narr, nev, o->tolerance,
@@ -608,7 +632,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		for (int i = 0; i < B; i++) hact[i] = 1;
 		cudaMemcpyAsync(s.narr, hn, B * sizeof(int), cudaMemcpyHostToDevice, q);
 		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
-		kb_tri_bisect<<<dim3((r + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, NULL);
+		kb_tri_bisect<<<dim3(r, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, NULL);
 		kb_tri_vectors<<<dim3((r + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, s.Z, ldz,
 								     s.work, NULL, NULL);
 		kb_tri_mgs<<<g1, BT, 0, q>>>(s.Z, ldz, s.narr, r, NULL);
@@ -666,6 +690,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	free(hG);
 	free(hact); free(hn); free(hflag);
 	bstate_free(&s);
+	jn_panels_partition_free(&part);
 	if (!st && cudaGetLastError() != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "batched Lanczos");
 	return st;
 }

@@ -62,6 +62,7 @@ struct jn_ctx {
 	int panel_grid;                 /* persistent CTAs; 0 until set up */
 	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
 	int panel_iter;                 /* rows a lane walks per panel task */
+	uint32_t *d_pgather;            /* per coefficient: its matrix element | sign << 31 | skip << 30 (batched) */
 };
 
 /* enqueue y (+)= H x on stream st */
@@ -99,6 +100,28 @@ void jn_panels_invalidate(jn_ctx *c);
 void jn_panels_release(jn_ctx *c);
 jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
 			    cudaEvent_t mid);
+
+/* batched panel products (jn_panel.cu): the 32-bit coefficients of B
+ * instances' matrix elements (device, me + i me_ld, the context's layout)
+ * into d_coef (B x n_coef) with their max|c| bits in d_cmax (B words); then
+ * per step y_i = H_i x_i with x_i = src + i src_ld + (*d_sel) sel_ld.
+ * Scratch: xbuf (B x 2 dim ints), gacc (B x dim, zero on entry, left zero),
+ * ctrl (2 B words). */
+typedef struct {
+	int grid;               /* persistent CTAs per instance */
+	uint32_t *cta, *flush_ptr, *flush;      /* device copies of the partition */
+} jn_panel_partition;
+jn_status jn_panels_partition_upload(jn_ctx *c, int grid, jn_panel_partition *pp);
+void jn_panels_partition_free(jn_panel_partition *pp);
+jn_status jn_panels_batched_coefficients(jn_ctx *c, int B, const double *d_me, int64_t me_ld, int *d_coef,
+					 unsigned long long *d_cmax, cudaStream_t st);
+/* pp: the CTA partition of each instance (a batch gives each instance fewer,
+ * larger chunks than a single product, so fewer blocks are cleared and
+ * flushed); NULL for the context's own */
+jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const unsigned long long *d_cmax,
+				    const double *src, int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y,
+				    int64_t y_ld, int *xbuf, unsigned long long *gacc, unsigned int *ctrl,
+				    const int *d_active, const jn_panel_partition *pp, cudaStream_t st);
 
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);

@@ -42,8 +42,6 @@ static int cmp_panel(const void *a, const void *b)
 int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 {
 	int *order = NULL;
-	double *cost = NULL;
-	unsigned char *touched = NULL;
 	jn_panels_free(p);
 	if (p->dim > JN_PANEL_MAX_DIM) ERR("dimension %lld is above the panel engine's %d", (long long)p->dim, JN_PANEL_MAX_DIM);
 	if (grid < 1) ERR("panel grid of %d CTAs", grid);
@@ -130,15 +128,13 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	p->n_coef = coef;
 	p->nptasks = ntask;
 	p->ptasks = malloc((ntask ? ntask : 1) * 4 * sizeof(uint32_t));
-	cost = malloc((ntask ? ntask : 1) * sizeof(double));
-	if (!p->ptasks || !cost) ERR("out of host memory");
+	if (!p->ptasks) ERR("out of host memory");
 	int64_t t = 0;
 	for (int q = 0; q < p->npanels; q++) {
 		const jn_panel_t *P = &p->panels[q];
 		if (P->nrows <= 0 || P->ncols <= 0) continue;
 		const int cw = lanes_per_row(P->ncols), R = 32 / cw;
 		const int64_t rows_per_task = (int64_t)R * iter;
-		const int diag = (P->kind & JN_PANEL_DIAG) != 0;
 		for (int i0 = 0; i0 < P->ncols; i0 += 32)
 			for (int64_t j0 = 0; j0 < P->nrows; j0 += rows_per_task) {
 				const int64_t j1 = j0 + rows_per_task < P->nrows ? j0 + rows_per_task : P->nrows;
@@ -147,53 +143,11 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 				T[1] = (uint32_t)j0;
 				T[2] = (uint32_t)j1;
 				T[3] = (uint32_t)i0 | ((uint32_t)cw << 24);
-				/* warp time: one pass per R rows, the transpose doubles the work, plus set-up */
-				cost[t] = (double)((j1 - j0 + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
 				t++;
 			}
 	}
-	/* persistent CTAs: contiguous runs of tasks of equal cost */
 	p->pgrid = grid;
-	p->pcta = malloc((size_t)(grid + 1) * sizeof(uint32_t));
-	if (!p->pcta) ERR("out of host memory");
-	double total = 0;
-	for (int64_t k = 0; k < ntask; k++) total += cost[k];
-	{
-		double acc = 0;
-		int64_t k = 0;
-		p->pcta[0] = 0;
-		for (int b = 1; b <= grid; b++) {
-			const double target = total * b / grid;
-			while (k < ntask && acc + 0.5 * cost[k] < target) acc += cost[k++];
-			p->pcta[b] = (uint32_t)(b == grid ? ntask : k);
-		}
-	}
-	/* the blocks each CTA touches: forward into the output block, transpose into the input block */
-	touched = calloc(p->nblocks ? p->nblocks : 1, 1);
-	p->pflush_ptr = malloc((size_t)(grid + 1) * sizeof(uint32_t));
-	size_t fcap = 1024;
-	p->pflush = malloc(fcap * sizeof(uint32_t));
-	if (!touched || !p->pflush_ptr || !p->pflush) ERR("out of host memory");
-	p->npflush = 0;
-	for (int b = 0; b < grid; b++) {
-		p->pflush_ptr[b] = (uint32_t)p->npflush;
-		memset(touched, 0, p->nblocks);
-		for (uint32_t k = p->pcta[b]; k < p->pcta[b + 1]; k++) {
-			const jn_instr_t *x = &p->instr[p->panels[p->ptasks[4 * k]].instr];
-			touched[x->bout] = 1;
-			if (x->bin != x->bout) touched[x->bin] = 1;
-		}
-		for (int i = 0; i < p->nblocks; i++) {
-			if (!touched[i] || p->blocks[i].Np <= 0 || p->blocks[i].Nn <= 0) continue;
-			if ((size_t)p->npflush == fcap) {
-				fcap *= 2;
-				p->pflush = realloc(p->pflush, fcap * sizeof(uint32_t));
-				if (!p->pflush) ERR("out of host memory");
-			}
-			p->pflush[p->npflush++] = (uint32_t)i;
-		}
-	}
-	p->pflush_ptr[grid] = (uint32_t)p->npflush;
+	if (jn_panels_partition(p, grid, &p->pcta, &p->pflush_ptr, &p->pflush, &p->npflush)) ERR("out of host memory");
 	/* every device index stays inside its buffer: checked once here */
 	for (int q = 0; q < p->npanels; q++) {
 		const jn_panel_t *P = &p->panels[q];
@@ -207,11 +161,72 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 		if (x->kind == JN_KIND_N && (bi->Np != bo->Np)) ERR("panel %d: spectator rows differ", q);
 		if (x->kind == JN_KIND_P && (bi->Nn != bo->Nn)) ERR("panel %d: spectator columns differ", q);
 	}
-	free(order); free(cost); free(touched);
+	free(order);
 	return 0;
 fail:
-	free(order); free(cost); free(touched);
+	free(order);
 	jn_panels_free(p);
+	return 1;
+}
+
+int jn_panels_partition(const jn_plan_t *p, int grid, uint32_t **cta_out, uint32_t **flush_ptr_out,
+			uint32_t **flush_out, int64_t *nflush_out)
+{
+	const int64_t ntask = p->nptasks;
+	uint32_t *cta = malloc((size_t)(grid + 1) * sizeof(uint32_t));
+	uint32_t *fptr = malloc((size_t)(grid + 1) * sizeof(uint32_t));
+	double *cost = malloc((ntask ? ntask : 1) * sizeof(double));
+	unsigned char *touched = calloc(p->nblocks ? p->nblocks : 1, 1);
+	size_t fcap = 1024;
+	int64_t nf = 0;
+	uint32_t *flush = malloc(fcap * sizeof(uint32_t));
+	if (grid < 1 || !cta || !fptr || !cost || !touched || !flush) goto fail;
+	/* warp time of a task: one pass per R rows, the transpose doubles the work, plus set-up */
+	double total = 0;
+	for (int64_t k = 0; k < ntask; k++) {
+		const uint32_t *T = p->ptasks + 4 * k;
+		const int R = 32 / (int)(T[3] >> 24);
+		const int diag = (p->panels[T[0]].kind & JN_PANEL_DIAG) != 0;
+		cost[k] = (double)((T[2] - T[1] + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
+		total += cost[k];
+	}
+	/* persistent CTAs: contiguous runs of tasks of equal cost */
+	{
+		double acc = 0;
+		int64_t k = 0;
+		cta[0] = 0;
+		for (int b = 1; b <= grid; b++) {
+			const double target = total * b / grid;
+			while (k < ntask && acc + 0.5 * cost[k] < target) acc += cost[k++];
+			cta[b] = (uint32_t)(b == grid ? ntask : k);
+		}
+	}
+	/* the blocks each CTA touches: forward into the output block, transpose into the input block */
+	for (int b = 0; b < grid; b++) {
+		fptr[b] = (uint32_t)nf;
+		memset(touched, 0, p->nblocks);
+		for (uint32_t k = cta[b]; k < cta[b + 1]; k++) {
+			const jn_instr_t *x = &p->instr[p->panels[p->ptasks[4 * k]].instr];
+			touched[x->bout] = 1;
+			if (x->bin != x->bout) touched[x->bin] = 1;
+		}
+		for (int i = 0; i < p->nblocks; i++) {
+			if (!touched[i] || p->blocks[i].Np <= 0 || p->blocks[i].Nn <= 0) continue;
+			if ((size_t)nf == fcap) {
+				fcap *= 2;
+				uint32_t *g = realloc(flush, fcap * sizeof(uint32_t));
+				if (!g) goto fail;
+				flush = g;
+			}
+			flush[nf++] = (uint32_t)i;
+		}
+	}
+	fptr[grid] = (uint32_t)nf;
+	free(cost); free(touched);
+	*cta_out = cta; *flush_ptr_out = fptr; *flush_out = flush; *nflush_out = nf;
+	return 0;
+fail:
+	free(cta); free(fptr); free(cost); free(touched); free(flush);
 	return 1;
 }
 
@@ -272,4 +287,31 @@ int jn_panels_coefficients_int(const jn_plan_t *p, const double *me, int32_t *ci
 	for (int64_t e = 0; e < p->n_coef; e++) ci[e] = (int32_t)llrint(ldexp(c[e], *Sc));
 	free(c);
 	return 0;
+}
+
+void jn_panels_gather_index(const jn_plan_t *p, uint32_t *gather)
+{
+	const uint32_t *ent = p->ent;
+	for (int q = 0; q < p->npanels; q++) {
+		const jn_panel_t *P = &p->panels[q];
+		const jn_instr_t *x = &p->instr[P->instr];
+		const jn_me_t *M = &p->mes[x->me];
+		if (x->kind == JN_KIND_NP) {
+			const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+			const int rows_n = (P->kind & JN_PANEL_ROWS_N) != 0;
+			for (int32_t j = 0; j < P->nrows; j++)
+				for (int32_t i = 0; i < P->ncols; i++) {
+					const int32_t ep = rows_n ? i : j, en = rows_n ? j : i;
+					const uint32_t mp = ent[2 * (Lp->ent_out + ep) + 1], mn = ent[2 * (Ln->ent_out + en) + 1];
+					const uint64_t at = (uint64_t)M->offset + (mn & 0x7fffffffu) + M->nd_n * (mp & 0x7fffffffu);
+					gather[P->c_off + (int64_t)j * P->ncols + i] = (uint32_t)at | ((mp ^ mn) & 0x80000000u);
+				}
+		} else {
+			const jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
+			for (int64_t e = 0; e < L->len; e++) {
+				const uint32_t mi = ent[2 * (L->ent_out + e) + 1];
+				gather[P->c_off + e] = (uint32_t)(M->offset + (mi & 0x7fffffffu)) | (mi & 0x80000000u) | 0x40000000u;
+			}
+		}
+	}
 }

@@ -181,7 +181,10 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 	}
 }
 
-/* the 32-bit product: coefficients and x are 32-bit fixed-point integers */
+/* the 32-bit product: coefficients and x are 32-bit fixed-point integers.
+ * Batched products (many Hamiltonians on one set of lists) run instance
+ * blockIdx.y with its own coefficients, x and accumulator at the given
+ * strides; instances with active[i] == 0 are skipped. */
 __global__ void __launch_bounds__(PANEL_THREADS, 3) jn_panel_kernel_i32(const uint4 *__restrict__ panels,
 								     const uint4 *__restrict__ tasks,
 								     const uint32_t *__restrict__ cta_ptr,
@@ -190,10 +193,14 @@ __global__ void __launch_bounds__(PANEL_THREADS, 3) jn_panel_kernel_i32(const ui
 								     const uint4 *__restrict__ blocks,
 								     const uint32_t *__restrict__ meta, const int *__restrict__ coef,
 								     const int *__restrict__ x, const int *__restrict__ xt,
-								     unsigned long long *__restrict__ gacc, const FixInt32 fix, int words)
+								     unsigned long long *__restrict__ gacc, const FixInt32 fix, int words,
+								     int64_t coef_ld, int64_t x_ld, int64_t acc_ld,
+								     const int *__restrict__ active)
 {
-	jn_panel_body<int, FixInt32>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef, x, xt, gacc, fix,
-					    words);
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	jn_panel_body<int, FixInt32>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef + inst * coef_ld,
+				     x + inst * x_ld, xt + inst * x_ld, gacc + inst * acc_ld, fix, words);
 }
 
 /* the FP64 product: the fixed-point scale 2^S comes from max|x| on the device */
@@ -278,7 +285,8 @@ void jn_panels_release(jn_ctx *c)
 {
 	cudaFree(c->d_panels); cudaFree(c->d_ptasks); cudaFree(c->d_pcta); cudaFree(c->d_pflush);
 	cudaFree(c->d_pflush_ptr); cudaFree(c->d_pmeta); cudaFree(c->d_coef64); cudaFree(c->d_coefi);
-	cudaFree(c->d_pblocks); cudaFree(c->d_xi); cudaFree(c->d_xt64);
+	cudaFree(c->d_pblocks); cudaFree(c->d_xi); cudaFree(c->d_xt64); cudaFree(c->d_pgather);
+	c->d_pgather = NULL;
 	c->d_pblocks = NULL;
 	c->d_xi = NULL;
 	c->d_xt64 = NULL;
@@ -399,7 +407,7 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 			jn_panel_kernel_i32<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
 				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
 				(const uint4 *)c->d_pblocks, c->d_pmeta, c->d_coefi, c->d_xi, c->d_xi + p->dim, c->d_gacc, fix,
-				(int)p->psmem_words);
+				(int)p->psmem_words, 0, 0, 0, NULL);
 		} else {
 			jn_panel_kernel_fp64<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
 				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
@@ -525,5 +533,186 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 	out->rows_per_lane = best_engine == 4 ? best_iter : 0;
 	out->ctas_per_sm = best_engine == 4 ? best_per : 0;
 	out->ms = best;
+	return JN_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* batched products: many Hamiltonians on the context's lists           */
+/* ------------------------------------------------------------------ */
+/* per coefficient: the matrix element it comes from, bit 31 its sign, bit 30
+ * the single-species |M| < 1e-12 skip */
+jn_status jn_panels_gather(jn_ctx *c)
+{
+	jn_plan_t *p = &c->plan;
+	if (c->d_pgather) return JN_OK;
+	jn_status s = jn_panels_setup(c);
+	if (s) return s;
+	if (p->n_me >= (1ll << 30)) return jn_fail(JN_ERR_INVALID, "%lld matrix elements: too many for the batched panel product",
+						 (long long)p->n_me);
+	uint32_t *g = (uint32_t *)malloc((p->n_coef ? p->n_coef : 1) * sizeof(uint32_t));
+	if (!g) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	jn_panels_gather_index(p, g);
+	s = upload_n(&c->d_pgather, g, (size_t)p->n_coef);
+	free(g);
+	return s;
+}
+
+/* bits of max |coefficient| of instance blockIdx.y (non-negative doubles order as their bits) */
+__global__ void jn_coef_max_kernel(const uint32_t *__restrict__ gather, int64_t n, const double *__restrict__ me,
+				   int64_t me_ld, unsigned long long *__restrict__ cmax)
+{
+	const int inst = blockIdx.y;
+	const double *m = me + inst * me_ld;
+	double v = 0.0;
+	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+		const uint32_t g = gather[e];
+		double a = fabs(m[g & 0x3fffffffu]);
+		if ((g & 0x40000000u) && a < 1e-12) a = 0.0;
+		v = fmax(v, a);
+	}
+	for (int o = 16; o; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+	if ((threadIdx.x & 31) == 0 && v > 0.0) atomicMax(cmax + inst, (unsigned long long)__double_as_longlong(v));
+}
+
+/* coefficient exponent Sc = 30 - e with cmax < 2^e (0 for an all-zero instance) */
+__device__ __forceinline__ int coef_exponent(unsigned long long cmax_bits)
+{
+	if (!cmax_bits) return 0;
+	return 30 - ((int)((cmax_bits >> 52) & 0x7ff) - 1022);
+}
+
+__global__ void jn_coef_build_kernel(const uint32_t *__restrict__ gather, int64_t n, const double *__restrict__ me,
+				     int64_t me_ld, const unsigned long long *__restrict__ cmax, int *__restrict__ coef,
+				     int64_t coef_ld)
+{
+	const int inst = blockIdx.y;
+	const double *m = me + inst * me_ld;
+	const double s = ldexp(1.0, coef_exponent(cmax[inst]));
+	int *out = coef + inst * coef_ld;
+	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+		const uint32_t g = gather[e];
+		double v = m[g & 0x3fffffffu];
+		if ((g & 0x40000000u) && fabs(v) < 1e-12) v = 0.0;
+		if (g & 0x80000000u) v = -v;
+		out[e] = (int)__double2ll_rn(v * s);
+	}
+}
+
+jn_status jn_panels_batched_coefficients(jn_ctx *c, int B, const double *d_me, int64_t me_ld, int *d_coef,
+					 unsigned long long *d_cmax, cudaStream_t st)
+{
+	const jn_plan_t *p = &c->plan;
+	jn_status s = jn_panels_gather(c);
+	if (s) return s;
+	CUDA_TRY(cudaMemsetAsync(d_cmax, 0, (size_t)B * sizeof(unsigned long long), st));
+	const int g = (int)(p->n_coef / 256 + 1 < 256 ? p->n_coef / 256 + 1 : 256);
+	if (p->n_coef) {
+		jn_coef_max_kernel<<<dim3(g, B), 256, 0, st>>>(c->d_pgather, p->n_coef, d_me, me_ld, d_cmax);
+		jn_coef_build_kernel<<<dim3(g, B), 256, 0, st>>>(c->d_pgather, p->n_coef, d_me, me_ld, d_cmax, d_coef,
+								   p->n_coef);
+	}
+	CUDA_TRY(cudaGetLastError());
+	return JN_OK;
+}
+
+/* instance blockIdx.y: max|x| of x_i = src + i src_ld + (*sel) sel_ld into ctrl[2 i] */
+__global__ void jn_xmax_batched_kernel(const double *__restrict__ src, int64_t src_ld, const int *__restrict__ sel,
+				       int64_t sel_ld, int64_t n, unsigned int *__restrict__ ctrl,
+				       const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		m = fmaxf(m, (float)fabs(x[i]) * 1.0000002f);
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(ctrl + 2 * inst, __float_as_uint(m));
+}
+
+/* block blockIdx.x of instance blockIdx.y: x_i as 32-bit fixed point, [p][n] and transposed [n][p] */
+__global__ void jn_panel_x_batched_kernel(const double *__restrict__ src, int64_t src_ld, const int *__restrict__ sel,
+					  int64_t sel_ld, int *__restrict__ xi, int64_t dim, const uint4 *__restrict__ blocks,
+					  const unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	int *xn = xi + inst * 2 * dim, *xt = xn + dim;
+	const uint4 bk = blocks[blockIdx.x];
+	const uint32_t Np = bk.z, Nn = bk.w, n = Np * Nn;
+	const double s = ldexp(1.0, x_exponent(ctrl[2 * inst]));
+	for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+		const int t = __double2int_rn(x[bk.x + e] * s);
+		xn[bk.x + e] = t;
+		xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+	}
+}
+
+/* y_i (=) acc_i 2^(30 - Sc_i - Sx_i); the accumulator is cleared */
+__global__ void jn_int_finalize_batched_kernel(unsigned long long *__restrict__ gacc, double *__restrict__ y, int64_t y_ld,
+					       int64_t n, const unsigned int *__restrict__ ctrl,
+					       const unsigned long long *__restrict__ cmax, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const double unit = ldexp(1.0, PANEL_INT_SHIFT - coef_exponent(cmax[inst]) - x_exponent(ctrl[2 * inst]));
+	unsigned long long *g = gacc + inst * n;
+	double *yy = y + inst * y_ld;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		yy[i] = (double)(long long)g[i] * unit;
+		g[i] = 0ull;
+	}
+}
+
+jn_status jn_panels_partition_upload(jn_ctx *c, int grid, jn_panel_partition *pp)
+{
+	memset(pp, 0, sizeof *pp);
+	jn_status s = jn_panels_setup(c);
+	if (s) return s;
+	uint32_t *cta = NULL, *fptr = NULL, *flush = NULL;
+	int64_t nf = 0;
+	if (jn_panels_partition(&c->plan, grid, &cta, &fptr, &flush, &nf)) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	if ((s = upload_n(&pp->cta, cta, (size_t)grid + 1)) || (s = upload_n(&pp->flush_ptr, fptr, (size_t)grid + 1)) ||
+	    (s = upload_n(&pp->flush, flush, (size_t)nf)))
+		jn_panels_partition_free(pp);
+	else
+		pp->grid = grid;
+	free(cta); free(fptr); free(flush);
+	return s;
+}
+
+void jn_panels_partition_free(jn_panel_partition *pp)
+{
+	cudaFree(pp->cta); cudaFree(pp->flush_ptr); cudaFree(pp->flush);
+	memset(pp, 0, sizeof *pp);
+}
+
+jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const unsigned long long *d_cmax,
+				    const double *src, int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y,
+				    int64_t y_ld, int *xbuf, unsigned long long *gacc, unsigned int *ctrl,
+				    const int *d_active, const jn_panel_partition *pp, cudaStream_t st)
+{
+	const jn_plan_t *p = &c->plan;
+	if (!jn_panels_fit(c, 1)) return jn_fail(JN_ERR_INVALID, "the panel engine is not set up for this context");
+	if (B < 1 || B > 65535) return jn_fail(JN_ERR_INVALID, "batch of %d instances", B);
+	if (!p->dim) return JN_OK;
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 256) g = 256;
+	CUDA_TRY(cudaMemsetAsync(ctrl, 0, (size_t)2 * B * sizeof(unsigned int), st));
+	jn_xmax_batched_kernel<<<dim3(g, B), 256, 0, st>>>(src, src_ld, d_sel, sel_ld, p->dim, ctrl, d_active);
+	jn_panel_x_batched_kernel<<<dim3(p->nblocks, B), 256, 0, st>>>(src, src_ld, d_sel, sel_ld, xbuf, p->dim,
+									 (const uint4 *)c->d_pblocks, ctrl, d_active);
+	if (p->nptasks) {
+		const FixInt32 fix = {};
+		const int grid = pp ? pp->grid : c->panel_grid;
+		jn_panel_kernel_i32<<<dim3(grid, B), PANEL_THREADS, panel_smem(p, 1), st>>>(
+			(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, pp ? pp->cta : c->d_pcta,
+			pp ? pp->flush : c->d_pflush, pp ? pp->flush_ptr : c->d_pflush_ptr,
+			(const uint4 *)c->d_pblocks, c->d_pmeta, d_coef, xbuf, xbuf + p->dim, gacc, fix, (int)p->psmem_words,
+			p->n_coef, 2 * p->dim, p->dim, d_active);
+	}
+	jn_int_finalize_batched_kernel<<<dim3(g, B), 256, 0, st>>>(gacc, y, y_ld, p->dim, ctrl, d_cmax, d_active);
+	CUDA_TRY(cudaGetLastError());
 	return JN_OK;
 }

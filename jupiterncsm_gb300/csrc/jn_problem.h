@@ -264,6 +264,10 @@ int jn_plan_read_me(const jn_plan_t *plan, const char *dir, double *out, char *e
  * schedule gives bit-identical products. */
 int jn_panels_build(jn_plan_t *plan, int grid, int iter, char *err, size_t errlen);
 void jn_panels_free(jn_plan_t *plan);
+/* the CTA ranges and flush lists of the plan's tasks for a grid of `grid`
+ * persistent CTAs (malloc'ed; the plan's own are those of plan->pgrid) */
+int jn_panels_partition(const jn_plan_t *plan, int grid, uint32_t **cta, uint32_t **flush_ptr, uint32_t **flush,
+			int64_t *nflush);
 /* panel coefficients from matrix elements in the plan's layout: FP64 into c64
  * and/or FP32 into c32 (either may be NULL), n_coef values each */
 void jn_panels_coefficients(const jn_plan_t *plan, const double *me, double *c64, float *c32);
@@ -273,6 +277,10 @@ void jn_panels_coefficients(const jn_plan_t *plan, const double *me, double *c64
  * (from the plan's abs_bound).  Returns 0, or 1 when the host runs out of
  * memory. */
 int jn_panels_coefficients_int(const jn_plan_t *plan, const double *me, int32_t *ci, int *Sc, int *k);
+/* for every coefficient the matrix element it copies: index | sign << 31 |
+ * (single-species block, where |M| < 1e-12 counts as zero) << 30; the plan
+ * must hold fewer than 2^30 matrix elements */
+void jn_panels_gather_index(const jn_plan_t *plan, uint32_t *gather);
 
 #ifdef __cplusplus
 }
