@@ -168,13 +168,14 @@ __global__ void k_axpy_neg(double *__restrict__ y, const double *__restrict__ x,
 /* ------------------------------------------------------------------ */
 /* tridiagonal eigenproblem                                            */
 /* ------------------------------------------------------------------ */
-/* theta[i] for i < want: the i-th smallest eigenvalue, by bisection */
+/* theta[i] for i = blockIdx.x < want: the i-th smallest eigenvalue, by warp multisection */
 __global__ void k_tri_bisect(const double *__restrict__ a, const double *__restrict__ b, int n, int want,
 			     double *__restrict__ theta)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int i = blockIdx.x;
 	if (i >= want) return;
-	theta[i] = jn_tri_bisect_one(a, b, n, i);
+	const double v = jn_tri_multisect_warp(a, b, n, i);
+	if (threadIdx.x == 0) theta[i] = v;
 }
 
 /* eigenvector of T for theta[i] by inverse iteration; Z row i holds the n components */
@@ -261,7 +262,7 @@ static jn_status tri_eig(jn_ctx *c, int n, int want, int vectors)
 {
 	struct jn_lanczos_state *s = c->lz;
 	if (want > n) want = n;
-	k_tri_bisect<<<(want + 63) / 64, 64, 0, c->stream>>>(s->d_alpha, s->d_beta, n, want, s->d_theta);
+	k_tri_bisect<<<want, 32, 0, c->stream>>>(s->d_alpha, s->d_beta, n, want, s->d_theta);
 	if (vectors) {
 		int ldz = s->mmax + 1;
 		double *work = s->d_Z + (size_t)s->nev_cap * ldz;

@@ -24,26 +24,6 @@ __device__ __forceinline__ int jn_sturm_count(const double *a, const double *b, 
 	return c;
 }
 
-/* the i-th smallest eigenvalue by bisection on the Gershgorin interval */
-__device__ __forceinline__ double jn_tri_bisect_one(const double *a, const double *b, int n, int i)
-{
-	double lo = a[0], hi = a[0];
-	for (int j = 0; j < n; j++) {
-		double r = (j > 0 ? fabs(b[j - 1]) : 0.0) + (j < n - 1 ? fabs(b[j]) : 0.0);
-		lo = fmin(lo, a[j] - r);
-		hi = fmax(hi, a[j] + r);
-	}
-	double span = fmax(fabs(lo), fabs(hi));
-	lo -= 1e-12 * span + 1e-300;
-	hi += 1e-12 * span + 1e-300;
-	for (int it = 0; it < 200; it++) {
-		double mid = 0.5 * (lo + hi);
-		if (mid <= lo || mid >= hi) break;
-		if (jn_sturm_count(a, b, n, mid) > i) hi = mid; else lo = mid;
-	}
-	return 0.5 * (lo + hi);
-}
-
 /* the i-th smallest eigenvalue by multisection, one warp per eigenvalue:
  * each round the 32 lanes evaluate the Sturm count at 32 points of the
  * bracket, which shrinks 32-fold, so about 11 rounds reach full precision
