@@ -244,6 +244,61 @@ def transform_leg(workdir, steps, warmup, flush, peak):
             "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
 
 
+def large_basis_leg(workdir, steps, warmup, flush, peak):
+    """6Li Nmax=6, 2M=2 (D = 186 894): the two-body interaction comes from the
+    GPU J -> M transform (the transform leg's output files) and feeds the
+    product and the Lanczos solves: one FP32-product mixed-precision solve
+    and one plain FP64 solve, 300 iterations at most, 10 lowest eigenvalues."""
+    import torch
+    import numpy as np
+    import jupiterncsm_gb300 as jn
+    w = TRANSFORM_WORKLOAD
+    d = os.path.join(workdir, "li6_nmax6_jscheme")
+    mes = os.path.join(d, "transformed")
+    H = jn.Hamiltonian(comb=f"{d}/comb.txt", order=f"{d}/evaluation_order.txt", lists=f"{d}/index_lists", mes=mes,
+                       Z=w["Z"], N=w["N"])
+    try:
+        st = H.stats()
+        D = H.dimension
+        dev = torch.device("cuda", torch.cuda.current_device())
+        x = torch.randn(D, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(11))
+        y = torch.zeros(D, dtype=torch.float64, device=dev)
+        paths = {}
+        for prec in (32, 64):
+            H.set_precision(prec)
+            for _ in range(warmup):
+                H.matvec_profile(x.data_ptr(), y.data_ptr())
+            ks = []
+            for _ in range(steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ks.append(H.matvec_profile(x.data_ptr(), y.data_ptr())[0])
+            kms = sum(ks) / len(ks)
+            b = 12.0 * st["list_entries"] + (4 if prec == 32 else 8) * st["me_referenced"] + 16.0 * D
+            paths["i32" if prec == 32 else "fp64"] = {
+                "engine": H.active_engine(), "product_kernel_ms": kms, "GB_per_s": b / (kms / 1e3) / 1e9,
+                "hbm_frac": b / (kms / 1e3) / 1e9 / peak, "multiply_adds_per_s": st["multiply_adds"] / (kms / 1e3)}
+        me = H.read_matrix_elements(mes)
+        t0 = time.perf_counter()
+        mixed = H.lanczos_batch([me], max_iterations=300, num_eigenvalues=10, tolerance=1e-6, precision=32)[0]
+        t1 = time.perf_counter()
+        H.set_precision(64)
+        plain = H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, allow_unconverged=True)
+        t2 = time.perf_counter()
+    finally:
+        H.close()
+    return {"workload": "6Li (Z=3,N=3) Nmax=6, 2M=2, two-body interaction from the GPU J->M transform of a seeded "
+                        "J-scheme file", "dimension": int(D), "instructions": st["num_instructions"],
+            "list_entries": st["list_entries"], "me_referenced": st["me_referenced"],
+            "multiply_adds": st["multiply_adds"], "paths": paths,
+            "solve": {"mixed_seconds": t1 - t0, "mixed_iterations": mixed["iterations"],
+                      "mixed_converged": mixed["converged"], "plain_fp64_seconds": t2 - t1,
+                      "plain_fp64_iterations": plain["iterations"], "plain_fp64_converged": plain["converged"],
+                      "max_eigenvalue_diff_MeV": float(np.abs(mixed["eigenvalues"] - plain["eigenvalues"]).max()),
+                      "lowest_eigenvalues_MeV": [float(v) for v in plain["eigenvalues"][:3]]},
+            "l2": "flushed between timed products (256 MiB write)"}
+
+
 SOLVE_FAMILY = [  # (label, Z, N, Nmax, 2M): the bases of the batched-Hamiltonian workload
     ("4He Nmax=2", 2, 2, 2, 0), ("4He Nmax=4", 2, 2, 4, 0), ("4He Nmax=6", 2, 2, 6, 0), ("6Li Nmax=4", 3, 3, 4, 2)]
 SOLVE_INSTANCES = 64
@@ -587,6 +642,11 @@ def main():
             line["transform"] = transform_leg(wd, args.steps, args.warmup, flush, peak)
         except Exception as e:  # the transform leg must never hide the matvec line
             line["transform"] = {"error": str(e)}
+        if "error" not in line["transform"]:
+            try:
+                line["large_basis"] = large_basis_leg(wd, min(args.steps, 10), args.warmup, flush, peak)
+            except Exception as e:
+                line["large_basis"] = {"error": str(e)}
     if rank == 0 and not args.no_solves:
         try:
             line["solves"] = solves_leg(wd)

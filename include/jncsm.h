@@ -465,6 +465,24 @@ void jn_warm_start_destroy(jn_warm_start *warm_start);
 void jn_default_start_vector(int64_t dim, double *out);
 
 /* ------------------------------------------------------------------ */
+/* Subspace matrices of training vectors (Ceres)                        */
+/* ------------------------------------------------------------------ */
+/* norm[i][j] = <v_i|v_j> and op[i][j] = <v_j|H v_i> for j >= i, mirrored
+ * (src/Ceres/norm_matrix/norm_matrix.c:4-28,
+ * src/Ceres/subspace_operator/subspace_operator.c:7-61), with H the
+ * context's operator at its precision and engine.  vectors: n host arrays of
+ * jn_dimension values; norm, op: n x n row-major host outputs (either may be
+ * NULL).  The products and dot products run on the GPU. */
+jn_status jn_subspace_matrices(jn_ctx *ctx, int n, const double *const *vectors, double *norm, double *op);
+
+/* The same from training-vector directories (<dir>/vec_<block id>, as
+ * Bacchus writes them), written as .npy files in the reference's layout
+ * (src/Ceres/numpy_matrix/numpy_matrix.c:7-35); either path may be NULL.
+ * One call per operator: the reference's ceres.x loops over operators. */
+jn_status jn_ceres_files(jn_ctx *ctx, int n, const char *const *vector_dirs, const char *norm_matrix_path,
+			 const char *subspace_operator_path);
+
+/* ------------------------------------------------------------------ */
 /* File tools around the product (host only, no GPU needed)            */
 /* ------------------------------------------------------------------ */
 /* Aurora: convert the Anicre index lists under anicre_dir,

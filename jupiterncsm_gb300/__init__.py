@@ -180,6 +180,10 @@ def gpu_lib():
                  "jn_mlp_train", "jn_mlp_predict", "jn_warm_start_fit", "jn_warm_start_vectors",
                  "jn_warm_start_basis"):
         getattr(L, name).restype = ci
+    L.jn_subspace_matrices.argtypes = [vp, ci, vp, vp, vp]
+    L.jn_subspace_matrices.restype = ci
+    L.jn_ceres_files.argtypes = [vp, ci, vp, cp, cp]
+    L.jn_ceres_files.restype = ci
     L.jn_aurora.argtypes = [cp, cp, cp, ci, ci, ci, ci, ctypes.POINTER(ci)]
     L.jn_mars.argtypes = [cp, ci, ci, cp, ci, ctypes.POINTER(ci)]
     L.jn_vulcan.argtypes = [cp, ci, ci, ci, vp, vp, cp]
@@ -340,6 +344,23 @@ class Hamiltonian:
 
     def set_panel_schedule(self, rows_per_lane, ctas_per_sm):
         _check(gpu_lib().jn_set_panel_schedule(self._h, int(rows_per_lane), int(ctas_per_sm)))
+
+    def subspace_matrices(self, vectors):
+        """(norm, op): <v_i|v_j> and <v_j|H v_i> of the given vectors, computed on the GPU (jn_subspace_matrices)."""
+        vs = [np.ascontiguousarray(v, dtype=np.float64) for v in vectors]
+        n = len(vs)
+        ptrs = (ctypes.c_void_p * n)(*[v.ctypes.data for v in vs])
+        N, O = np.zeros((n, n)), np.zeros((n, n))
+        _check(gpu_lib().jn_subspace_matrices(self._h, n, ctypes.cast(ptrs, ctypes.c_void_p), N.ctypes.data,
+                                              O.ctypes.data))
+        return N, O
+
+    def ceres_files(self, vector_dirs, norm_matrix_path, subspace_operator_path):
+        """The Ceres drop-in: .npy norm and subspace-operator matrices from vec_<block> directories."""
+        dirs = (ctypes.c_char_p * len(vector_dirs))(*[d.encode() for d in vector_dirs])
+        _check(gpu_lib().jn_ceres_files(self._h, len(vector_dirs), ctypes.cast(dirs, ctypes.c_void_p),
+                                        norm_matrix_path.encode() if norm_matrix_path else None,
+                                        subspace_operator_path.encode() if subspace_operator_path else None))
 
     def active_engine(self):
         """The engine the next product runs (4 panels, 3 block tiles, 2 warp pieces)."""

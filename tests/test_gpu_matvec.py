@@ -244,3 +244,29 @@ def test_mars_order_gives_the_same_product_bits(problem, tmp_path):
         assert np.array_equal(a.matvec(x).view(np.uint64), b.matvec(x).view(np.uint64))
     a.close()
     b.close()
+
+
+def test_subspace_matrices_and_ceres_files(problem, tmp_path):
+    """Norm and projected-operator matrices of training vectors (the Ceres
+    analogue) against the dense oracle, in memory and through .npy files."""
+    d, Z, N, *_ = problem("he4_n4_2b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    Hd = np.array([oracle.Port(d).matvec(e) for e in np.eye(H.dimension)]).T
+    rng = np.random.default_rng(28)
+    V = rng.standard_normal((5, H.dimension))
+    Nm, Om = H.subspace_matrices(list(V))
+    assert np.abs(Nm - V @ V.T).max() <= 1e-12 * np.abs(V @ V.T).max()
+    want = V @ Hd @ V.T
+    assert np.abs(Om - want).max() <= 1e-12 * np.abs(want).max()
+    assert np.array_equal(Om, Om.T) and np.array_equal(Nm, Nm.T)
+    dirs = []
+    for i, v in enumerate(V):
+        vd = tmp_path / f"v{i}"
+        vd.mkdir()
+        for bid, off, n in H.blocks():
+            v[off:off + n].tofile(str(vd / f"vec_{bid}"))
+        dirs.append(str(vd))
+    H.ceres_files(dirs, str(tmp_path / "norm.npy"), str(tmp_path / "op.npy"))
+    assert np.array_equal(np.load(str(tmp_path / "norm.npy")), Nm)
+    assert np.array_equal(np.load(str(tmp_path / "op.npy")), Om)
+    H.close()
