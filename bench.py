@@ -57,8 +57,8 @@ def measured_peaks():
 
 KERNELS = {(4, 32): "jn_panel_kernel_i32", (4, 64): "jn_panel_kernel_fp64",
            (3, 32): "jn_tile_kernel<float>", (3, 64): "jn_tile_kernel<double>"}
-# kernels launched per product: max|x|, [the panel engine's copies of x], the product, the conversion into y
-LAUNCHES = {4: 4, 3: 3, 2: 3}
+# kernels launched per product: max|x| (with the panel engine's copies of x), the product, the conversion into y
+LAUNCHES = {4: 3, 3: 3, 2: 3}
 
 
 def profile_traffic(workload, engine, precision):

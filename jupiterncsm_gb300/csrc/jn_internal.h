@@ -63,7 +63,15 @@ struct jn_ctx {
 	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
 	int panel_iter;                 /* rows a lane walks per panel task */
 	uint32_t *d_pgather;            /* per coefficient: its matrix element | sign << 31 | skip << 30 (batched) */
+	uint16_t *d_pelem;              /* per state: its basis block (the prep kernel's transposed copy) */
+	/* products replayed as CUDA graphs, keyed by every argument their kernels take */
+	struct jn_product_graph *graphs;
+	int ngraphs, graph_next;
+	cudaEvent_t prof_ev[4];         /* start, before and after the product kernel, end: recorded inside product graphs */
 };
+
+/* drop the cached product graphs (before any product buffer is freed) */
+void jn_product_graphs_clear(jn_ctx *c);
 
 /* enqueue y (+)= H x on stream st */
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st);

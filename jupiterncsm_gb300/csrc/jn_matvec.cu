@@ -522,6 +522,9 @@ extern "C" void jn_close(jn_ctx *c)
 	cudaFree(c->d_x); cudaFree(c->d_y); cudaFree(c->d_me32); cudaFree(c->d_x32);
 	cudaFree(c->d_btiles); cudaFree(c->d_pieces); cudaFree(c->d_gacc); cudaFree(c->d_xmax); cudaFree(c->d_tterms); cudaFree(c->d_walks); cudaFree(c->d_items);
 	if (c->h_pinned) cudaFreeHost(c->h_pinned);
+	jn_product_graphs_clear(c);
+	for (int i = 0; i < 4; i++)
+		if (c->prof_ev[i]) cudaEventDestroy(c->prof_ev[i]);
 	jn_panels_release(c);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
@@ -803,18 +806,23 @@ extern "C" jn_status jn_matvec_profile(jn_ctx *c, const double *d_x, double *d_y
 {
 	if (!c || !d_x || !d_y || !ms) return fail(JN_ERR_INVALID, "null argument");
 	if (d_x == d_y) return fail(JN_ERR_INVALID, "x and y must not alias");
-	cudaEvent_t ev[4];
-	for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&ev[i]));
-	CUDA_TRY(cudaEventRecord(ev[0], c->stream));
-	jn_status s = enqueue(c, d_x, d_y, accumulate, c->stream, ev[1], ev[2]);
+	/* the events belong to the context, so that a product that runs as a
+	 * cached graph records them from inside it: ms[0] is the product kernel,
+	 * ms[1] the rest of the product (its other kernels and the gaps between
+	 * them), both device time.  Engines launched kernel by kernel record the
+	 * start and end events from the host around the launches. */
+	for (int i = 0; i < 4; i++)
+		if (!c->prof_ev[i]) CUDA_TRY(cudaEventCreate(&c->prof_ev[i]));
+	const int in_graph = c->engine == 4 && jn_panels_fit(c, c->precision == 32);
+	if (!in_graph) CUDA_TRY(cudaEventRecord(c->prof_ev[0], c->stream));
+	jn_status s = enqueue(c, d_x, d_y, accumulate, c->stream, c->prof_ev[1], c->prof_ev[2]);
 	if (s) return s;
-	CUDA_TRY(cudaEventRecord(ev[3], c->stream));
-	CUDA_TRY(cudaEventSynchronize(ev[3]));
+	if (!in_graph) CUDA_TRY(cudaEventRecord(c->prof_ev[3], c->stream));
+	CUDA_TRY(cudaEventSynchronize(c->prof_ev[3]));
 	float total = 0.f;
-	CUDA_TRY(cudaEventElapsedTime(&ms[0], ev[1], ev[2]));
-	CUDA_TRY(cudaEventElapsedTime(&total, ev[0], ev[3]));
+	CUDA_TRY(cudaEventElapsedTime(&ms[0], c->prof_ev[1], c->prof_ev[2]));
+	CUDA_TRY(cudaEventElapsedTime(&total, c->prof_ev[0], c->prof_ev[3]));
 	ms[1] = total - ms[0];
-	for (int i = 0; i < 4; i++) cudaEventDestroy(ev[i]);
 	return JN_OK;
 }
 

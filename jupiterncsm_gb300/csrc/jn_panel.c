@@ -29,8 +29,23 @@ void jn_panels_free(jn_plan_t *p)
 /* lanes per row: a narrow panel puts floor(32 / ncols) rows side by side */
 static int lanes_per_row(int ncols) { return ncols < 32 ? ncols : 32; }
 
-/* panels sorted by (output block, input block) so that a CTA's run of tasks touches few blocks */
+/* warp passes of a task: one per R rows, twice for an off-diagonal panel */
+static double task_cost(const jn_plan_t *p, const uint32_t *T)
+{
+	const int R = 32 / (int)(T[3] >> 24);
+	const int diag = (p->panels[T[0]].kind & JN_PANEL_DIAG) != 0;
+	return (double)((T[2] - T[1] + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
+}
+
 static const jn_plan_t *g_sort_plan;
+static int cmp_task_cost(const void *a, const void *b)
+{
+	const double ca = task_cost(g_sort_plan, a), cb = task_cost(g_sort_plan, b);
+	if (ca != cb) return ca > cb ? -1 : 1;
+	return memcmp(a, b, 4 * sizeof(uint32_t));
+}
+
+/* panels sorted by (output block, input block) so that a CTA's run of tasks touches few blocks */
 static int cmp_panel(const void *a, const void *b)
 {
 	const jn_instr_t *x = &g_sort_plan->instr[*(const int *)a], *y = &g_sort_plan->instr[*(const int *)b];
@@ -148,6 +163,12 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	}
 	p->pgrid = grid;
 	if (jn_panels_partition(p, grid, &p->pcta, &p->pflush_ptr, &p->pflush, &p->npflush)) ERR("out of host memory");
+	/* within each CTA's run, heaviest tasks first: the warps that finish last
+	   then finish with small tasks (the order never changes a result bit) */
+	for (int b = 0; b < grid; b++) {
+		g_sort_plan = p;
+		qsort(p->ptasks + 4 * (size_t)p->pcta[b], p->pcta[b + 1] - p->pcta[b], 4 * sizeof(uint32_t), cmp_task_cost);
+	}
 	/* every device index stays inside its buffer: checked once here */
 	for (int q = 0; q < p->npanels; q++) {
 		const jn_panel_t *P = &p->panels[q];
@@ -181,13 +202,9 @@ int jn_panels_partition(const jn_plan_t *p, int grid, uint32_t **cta_out, uint32
 	int64_t nf = 0;
 	uint32_t *flush = malloc(fcap * sizeof(uint32_t));
 	if (grid < 1 || !cta || !fptr || !cost || !touched || !flush) goto fail;
-	/* warp time of a task: one pass per R rows, the transpose doubles the work, plus set-up */
 	double total = 0;
 	for (int64_t k = 0; k < ntask; k++) {
-		const uint32_t *T = p->ptasks + 4 * k;
-		const int R = 32 / (int)(T[3] >> 24);
-		const int diag = (p->panels[T[0]].kind & JN_PANEL_DIAG) != 0;
-		cost[k] = (double)((T[2] - T[1] + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
+		cost[k] = task_cost(p, p->ptasks + 4 * k);
 		total += cost[k];
 	}
 	/* persistent CTAs: contiguous runs of tasks of equal cost */

@@ -26,6 +26,8 @@
  * touch few blocks, and at the end add only the touched ranges into the
  * global accumulator.
  */
+#include <cooperative_groups.h>
+
 #include "jn_internal.h"
 #include "jn_fixed.cuh"
 
@@ -230,22 +232,71 @@ __device__ __forceinline__ int x_exponent(unsigned int xmax_bits)
 	return Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
 }
 
-/* block b = blockIdx.x: the panel kernels' copies of x, in the [p][n] layout
- * (xn, 32-bit path only) and transposed to [n][p] (xt).  32-bit path: x as
- * 32-bit fixed-point integers x 2^Sx; FP64: x itself. */
+/* One cluster of PREP_CTAS CTAs: max|x| into ctrl[0] (with the FP32 round-up
+ * margin of the other engines' scale), then the panel kernels' copies of x:
+ * the 32-bit fixed-point x in the [p][n] layout (xn, when not NULL) and the
+ * copy with every block transposed to [n][p] (xt); FP64 copies x itself.
+ * Each thread holds its PREP_PER states in registers across the cluster-wide
+ * max (partial maxima meet in distributed shared memory), so x is read once;
+ * elem[i] is the basis block of state i. */
+#define PREP_THREADS 1024
+#define PREP_CTAS 8
+#define PREP_PER 4
+static_assert(PREP_THREADS * PREP_CTAS * PREP_PER >= JN_PANEL_MAX_DIM, "the prep cluster covers the panel engine's bases");
 template <typename T>
-__global__ void jn_panel_x_kernel(const double *__restrict__ x, T *__restrict__ xn, T *__restrict__ xt,
-				  const uint4 *__restrict__ blocks, const unsigned int *__restrict__ xmax_bits)
+__global__ void __cluster_dims__(PREP_CTAS, 1, 1) __launch_bounds__(PREP_THREADS)
+	jn_panel_prep_kernel(const double *__restrict__ x, T *__restrict__ xn, T *__restrict__ xt,
+			     const uint4 *__restrict__ blocks, const uint16_t *__restrict__ elem, int64_t dim,
+			     unsigned int *__restrict__ ctrl)
 {
-	const uint4 bk = blocks[blockIdx.x];
-	const uint32_t Np = bk.z, Nn = bk.w, n = Np * Nn;
-	const double s = sizeof(T) == 4 ? ldexp(1.0, x_exponent(*xmax_bits)) : 1.0;
-	for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-		const double v = x[bk.x + e];
-		const T t = sizeof(T) == 4 ? (T)__double2int_rn(v * s) : (T)v;
-		if (xn) xn[bk.x + e] = t;
-		xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+	namespace cg = cooperative_groups;
+	cg::cluster_group cluster = cg::this_cluster();
+	__shared__ float wmax[PREP_THREADS / 32];
+	__shared__ float cta_max, all_max;
+	const int rank = (int)cluster.block_rank();
+	double v[PREP_PER];
+	float m = 0.0f;
+#pragma unroll
+	for (int u = 0; u < PREP_PER; u++) {
+		const int64_t i = ((int64_t)u * PREP_CTAS + rank) * PREP_THREADS + threadIdx.x;
+		v[u] = i < dim ? x[i] : 0.0;
+		m = fmaxf(m, (float)fabs(v[u]) * 1.0000002f);
 	}
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		m = wmax[threadIdx.x];
+		for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+		if (threadIdx.x == 0) cta_max = m;
+	}
+	cluster.sync();
+	if (threadIdx.x < 32) {
+		m = threadIdx.x < PREP_CTAS ? *cluster.map_shared_rank(&cta_max, (unsigned int)threadIdx.x) : 0.0f;
+		for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+		if (threadIdx.x == 0) {
+			all_max = m;
+			if (rank == 0) {
+				ctrl[0] = __float_as_uint(m);
+				ctrl[1] = 0u;
+			}
+		}
+	}
+	__syncthreads();
+	const double s = sizeof(T) == 4 ? ldexp(1.0, x_exponent(__float_as_uint(all_max))) : 1.0;
+#pragma unroll
+	for (int u = 0; u < PREP_PER; u++) {
+		const int64_t i = ((int64_t)u * PREP_CTAS + rank) * PREP_THREADS + threadIdx.x;
+		if (i < dim) {
+			const uint4 bk = __ldg(blocks + __ldg(elem + i));
+			const uint32_t e = (uint32_t)(i - bk.x), Nn = bk.w, Np = bk.z;
+			const T t = sizeof(T) == 4 ? (T)__double2int_rn(v[u] * s) : (T)v[u];
+			if (xn) xn[i] = t;
+			xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+		}
+	}
+	/* no CTA leaves while another may still read its partial maximum */
+	cluster.sync();
 }
 
 /* y (+)= acc 2^(k - Sc - Sx); the accumulator is cleared for the next product */
@@ -285,8 +336,9 @@ void jn_panels_release(jn_ctx *c)
 {
 	cudaFree(c->d_panels); cudaFree(c->d_ptasks); cudaFree(c->d_pcta); cudaFree(c->d_pflush);
 	cudaFree(c->d_pflush_ptr); cudaFree(c->d_pmeta); cudaFree(c->d_coef64); cudaFree(c->d_coefi);
-	cudaFree(c->d_pblocks); cudaFree(c->d_xi); cudaFree(c->d_xt64); cudaFree(c->d_pgather);
+	cudaFree(c->d_pblocks); cudaFree(c->d_xi); cudaFree(c->d_xt64); cudaFree(c->d_pgather); cudaFree(c->d_pelem);
 	c->d_pgather = NULL;
+	c->d_pelem = NULL;
 	c->d_pblocks = NULL;
 	c->d_xi = NULL;
 	c->d_xt64 = NULL;
@@ -339,6 +391,21 @@ jn_status jn_panels_setup(jn_ctx *c)
 		jn_panels_release(c);
 		return s;
 	}
+	{
+		uint16_t *elem = (uint16_t *)malloc((size_t)(p->dim ? p->dim : 1) * sizeof(uint16_t));
+		if (!elem) {
+			jn_panels_release(c);
+			return jn_fail(JN_ERR_NOMEM, "out of host memory");
+		}
+		for (int b = 0; b < p->nblocks; b++)
+			for (int64_t i = 0; i < p->blocks[b].Np * p->blocks[b].Nn; i++) elem[p->blocks[b].offset + i] = (uint16_t)b;
+		s = upload_n(&c->d_pelem, elem, (size_t)p->dim);
+		free(elem);
+		if (s) {
+			jn_panels_release(c);
+			return s;
+		}
+	}
 	c->panel_grid = p->pgrid;
 	return JN_OK;
 }
@@ -376,6 +443,76 @@ void jn_panels_invalidate(jn_ctx *c)
 	c->d_coefi = NULL;
 }
 
+/* Everything the three kernels of one product take: a cached graph whose
+ * signature equals the current one launches exactly what direct launches
+ * would (device arrays are read when the graph runs, not when it is made). */
+typedef struct {
+	const void *x, *y, *panels, *tasks, *cta, *flush, *flush_ptr, *blocks, *meta, *coef, *xi, *xt, *gacc, *ctrl, *elem;
+	const void *stream, *start, *pre, *mid, *end;
+	int64_t dim;
+	double abs_bound;
+	size_t smem;
+	int f32, accumulate, grid, words, kshift, fin_grid;
+} panel_sig_t;
+
+struct jn_product_graph {
+	panel_sig_t sig;
+	cudaGraphExec_t exec;
+};
+
+#define PRODUCT_GRAPHS 8
+
+void jn_product_graphs_clear(jn_ctx *c)
+{
+	for (int i = 0; i < c->ngraphs; i++) cudaGraphExecDestroy(c->graphs[i].exec);
+	free(c->graphs);
+	c->graphs = NULL;
+	c->ngraphs = c->graph_next = 0;
+}
+
+static void panel_launch(const panel_sig_t *g, int has_tasks, int capturing)
+{
+	const unsigned int evflags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+	cudaStream_t st = (cudaStream_t)g->stream;
+	const uint4 *blocks = (const uint4 *)g->blocks;
+	unsigned int *ctrl = (unsigned int *)g->ctrl;
+	if (g->start) cudaEventRecordWithFlags((cudaEvent_t)g->start, st, evflags);
+	if (g->f32)
+		jn_panel_prep_kernel<int><<<PREP_CTAS, PREP_THREADS, 0, st>>>((const double *)g->x, (int *)g->xi, (int *)g->xt, blocks,
+									 (const uint16_t *)g->elem, g->dim, ctrl);
+	else
+		jn_panel_prep_kernel<double><<<PREP_CTAS, PREP_THREADS, 0, st>>>((const double *)g->x, NULL, (double *)g->xt, blocks,
+									    (const uint16_t *)g->elem, g->dim, ctrl);
+	if (g->pre) cudaEventRecordWithFlags((cudaEvent_t)g->pre, st, evflags);
+	if (has_tasks) {
+		if (g->f32) {
+			const FixInt32 fix = {};
+			jn_panel_kernel_i32<<<g->grid, PANEL_THREADS, g->smem, st>>>(
+				(const uint4 *)g->panels, (const uint4 *)g->tasks, (const uint32_t *)g->cta, (const uint32_t *)g->flush,
+				(const uint32_t *)g->flush_ptr, blocks, (const uint32_t *)g->meta, (const int *)g->coef,
+				(const int *)g->xi, (const int *)g->xt, (unsigned long long *)g->gacc, fix, g->words, 0, 0, 0, NULL);
+		} else {
+			jn_panel_kernel_fp64<<<g->grid, PANEL_THREADS, g->smem, st>>>(
+				(const uint4 *)g->panels, (const uint4 *)g->tasks, (const uint32_t *)g->cta, (const uint32_t *)g->flush,
+				(const uint32_t *)g->flush_ptr, blocks, (const uint32_t *)g->meta, (const double *)g->coef,
+				(const double *)g->x, (const double *)g->xt, (unsigned long long *)g->gacc, ctrl, g->abs_bound, g->words);
+		}
+	}
+	if (g->mid) cudaEventRecordWithFlags((cudaEvent_t)g->mid, st, evflags);
+	if (g->f32)
+		jn_int_finalize_kernel<<<g->fin_grid, 256, 0, st>>>((unsigned long long *)g->gacc, (double *)g->y, g->dim, ctrl,
+								   g->kshift, g->accumulate);
+	else
+		jn_launch_finalize((unsigned long long *)g->gacc, (double *)g->y, g->dim, ctrl, g->abs_bound, g->accumulate, st);
+	if (g->end) cudaEventRecordWithFlags((cudaEvent_t)g->end, st, evflags);
+}
+
+/* y (+)= H x on the panel engine.  The product runs as a cached CUDA graph
+ * (one launch instead of three kernels) unless the stream is already being
+ * captured, in which case its kernels join that capture.  Profiled
+ * products (the context's profiling events as `pre` and `mid`) record their
+ * start, kernel and end events from inside the graph; other events are
+ * recorded by direct launches. */
 jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
 			    cudaEvent_t mid)
 {
@@ -388,38 +525,67 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 	if (!s && !c->d_xi) s = upload_n(&c->d_xi, NULL, (size_t)p->dim * 2);
 	if (!s && !c->d_xt64) s = upload_n(&c->d_xt64, NULL, (size_t)p->dim);
 	if (s) return s;
-	unsigned int *ctrl = c->d_xmax;
-	CUDA_TRY(cudaMemsetAsync(ctrl, 0, 2 * sizeof(unsigned int), st));
-	jn_launch_prep(d_x, NULL, p->dim, ctrl, st);
-	int g = (int)((p->dim + 255) / 256);
-	if (g > 1024) g = 1024;
-	if (p->nblocks) {
-		if (f32)
-			jn_panel_x_kernel<int><<<p->nblocks, 256, 0, st>>>(d_x, c->d_xi, c->d_xi + p->dim, (const uint4 *)c->d_pblocks, ctrl);
-		else
-			jn_panel_x_kernel<double><<<p->nblocks, 256, 0, st>>>(d_x, NULL, c->d_xt64, (const uint4 *)c->d_pblocks, ctrl);
+	if (!p->dim) return JN_OK;
+	panel_sig_t g;
+	memset(&g, 0, sizeof g);
+	g.x = d_x; g.y = d_y; g.panels = c->d_panels; g.tasks = c->d_ptasks; g.cta = c->d_pcta; g.flush = c->d_pflush;
+	g.flush_ptr = c->d_pflush_ptr; g.blocks = c->d_pblocks; g.meta = c->d_pmeta; g.gacc = c->d_gacc; g.ctrl = c->d_xmax;
+	g.elem = c->d_pelem; g.stream = st; g.pre = pre; g.mid = mid; g.dim = p->dim; g.f32 = f32;
+	if (pre == c->prof_ev[1] && mid == c->prof_ev[2]) {
+		/* profiled: the product's own start and end, recorded on the device */
+		g.start = c->prof_ev[0];
+		g.end = c->prof_ev[3];
 	}
-	if (pre) cudaEventRecord(pre, st);
-	const size_t smem = panel_smem(p, f32);
-	if (p->nptasks) {
-		if (f32) {
-			const FixInt32 fix = {};
-			jn_panel_kernel_i32<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
-				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
-				(const uint4 *)c->d_pblocks, c->d_pmeta, c->d_coefi, c->d_xi, c->d_xi + p->dim, c->d_gacc, fix,
-				(int)p->psmem_words, 0, 0, 0, NULL);
-		} else {
-			jn_panel_kernel_fp64<<<c->panel_grid, PANEL_THREADS, smem, st>>>(
-				(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, c->d_pcta, c->d_pflush, c->d_pflush_ptr,
-				(const uint4 *)c->d_pblocks, c->d_pmeta, c->d_coef64, d_x, c->d_xt64, c->d_gacc, ctrl,
-				p->abs_bound, (int)p->psmem_words);
-		}
-	}
-	if (mid) cudaEventRecord(mid, st);
+	g.accumulate = accumulate; g.grid = c->panel_grid; g.words = (int)p->psmem_words; g.smem = panel_smem(p, f32);
+	g.fin_grid = (int)((p->dim + 255) / 256);
+	if (g.fin_grid > 1024) g.fin_grid = 1024;
 	if (f32) {
-		if (p->dim) jn_int_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, ctrl, c->pint_k - c->pint_sc, accumulate);
+		g.coef = c->d_coefi; g.xi = c->d_xi; g.xt = c->d_xi + p->dim; g.kshift = c->pint_k - c->pint_sc;
 	} else {
-		jn_launch_finalize(c->d_gacc, d_y, p->dim, ctrl, p->abs_bound, accumulate, st);
+		g.coef = c->d_coef64; g.xt = c->d_xt64; g.abs_bound = p->abs_bound;
+	}
+	const int has_tasks = p->nptasks > 0;
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	const int graphable = (!pre || pre == c->prof_ev[1]) && (!mid || mid == c->prof_ev[2]) &&
+			      cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone;
+	cudaGetLastError();
+	if (!graphable) {
+		panel_launch(&g, has_tasks, 0);
+	} else {
+		int hit = -1;
+		for (int i = 0; i < c->ngraphs && hit < 0; i++)
+			if (!memcmp(&c->graphs[i].sig, &g, sizeof g)) hit = i;
+		if (hit < 0) {
+			cudaGraph_t graph = NULL;
+			cudaGraphExec_t exec = NULL;
+			if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+				panel_launch(&g, has_tasks, 1);
+				if (cudaStreamEndCapture(st, &graph) == cudaSuccess && graph &&
+				    cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+					exec = NULL;
+				if (graph) cudaGraphDestroy(graph);
+			}
+			cudaGetLastError();
+			if (exec) {
+				if (!c->graphs) c->graphs = (struct jn_product_graph *)calloc(PRODUCT_GRAPHS, sizeof *c->graphs);
+				if (c->graphs) {
+					hit = c->ngraphs < PRODUCT_GRAPHS ? c->ngraphs++ : c->graph_next;
+					if (hit == c->graph_next && c->ngraphs == PRODUCT_GRAPHS && c->graphs[hit].exec)
+						cudaGraphExecDestroy(c->graphs[hit].exec);
+					c->graph_next = (hit + 1) % PRODUCT_GRAPHS;
+					c->graphs[hit].sig = g;
+					c->graphs[hit].exec = exec;
+				} else {
+					cudaGraphExecDestroy(exec);
+				}
+			}
+		}
+		if (hit >= 0) {
+			cudaError_t e = cudaGraphLaunch(c->graphs[hit].exec, st);
+			if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "panel product graph launch: %s", cudaGetErrorString(e));
+		} else {
+			panel_launch(&g, has_tasks, 0);   /* capture unavailable: launch directly */
+		}
 	}
 	cudaError_t e = cudaGetLastError();
 	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "panel product launch: %s", cudaGetErrorString(e));

@@ -18,6 +18,8 @@ being measured or shipped.
                  compiled unchanged into _ref/ref_mercury (with a stand-in
                  for the absent wigxjpf library) when the reference tree is
                  present
+* ``reference_transform3``  the reference's own three-body J -> M transform
+                 with its ASCII J-scheme reader (_ref/ref_mercury3)
 """
 import ctypes
 import os
@@ -29,6 +31,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libminerva_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_minerva.so")
 REF_MERCURY = os.path.join(HERE, "_ref", "ref_mercury")
+REF_MERCURY3 = os.path.join(HERE, "_ref", "ref_mercury3")
 
 
 def build():
@@ -43,8 +46,14 @@ def reference_tool_available(name):
 
 
 def reference_tool(name, *args):
-    """Run the reference program `name` (aurora, mars or vulcan) with args; returns the completed process."""
-    return subprocess.run([REF_TOOLS[name], *map(str, args)], capture_output=True, text=True)
+    """Run the reference program `name` (aurora, mars or vulcan) with args; returns the completed process.
+
+    The programs write <name>.log into their working directory, so they run in
+    a scratch directory; relative paths in args are made absolute first."""
+    import tempfile
+    args = [os.path.abspath(a) if isinstance(a, str) and os.path.exists(a) else str(a) for a in args]
+    with tempfile.TemporaryDirectory() as wd:
+        return subprocess.run([REF_TOOLS[name], *args], capture_output=True, text=True, cwd=wd)
 
 
 def reference_available():
@@ -60,6 +69,23 @@ def reference_transform(comb, index_list_dir, output_dir, Z, N, e1, e2, antoine,
     os.makedirs(output_dir, exist_ok=True)
     r = subprocess.run([REF_MERCURY, comb, index_list_dir, output_dir, str(Z), str(N), str(e1), str(e2), antoine,
                         "0" if include_kinetic else "1"], capture_output=True, text=True, check=True)
+    return float(r.stdout.split()[-1])
+
+
+def reference_transform3_available():
+    return os.path.exists(REF_MERCURY3)
+
+
+def reference_transform3(comb, index_list_dir, output_dir, Z, N, e_single, jscheme_dir):
+    """Run the reference's three-body transform (ASCII J-scheme input); returns its wall time in seconds.
+
+    It writes a log file into its working directory, so it runs in a scratch directory."""
+    import tempfile
+    os.makedirs(output_dir, exist_ok=True)
+    args = [os.path.abspath(a) for a in (comb, index_list_dir, output_dir)]
+    with tempfile.TemporaryDirectory() as wd:
+        r = subprocess.run([REF_MERCURY3, *args, str(Z), str(N), str(e_single), os.path.abspath(jscheme_dir)],
+                           capture_output=True, text=True, check=True, cwd=wd)
     return float(r.stdout.split()[-1])
 
 
