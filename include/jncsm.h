@@ -384,6 +384,71 @@ jn_status jn_transform_2nf(const char *combination_table_file, const char *index
 			   int num_protons, int num_neutrons, int single_particle_energy, int two_particle_energy,
 			   const char *antoine_file, int include_kinetic_energy);
 
+/* ------------------------------------------------------------------ */
+/* J-scheme -> M-scheme three-body transform (Mercury, three-body part) */
+/* ------------------------------------------------------------------ */
+typedef struct jn_transform3 jn_transform3;
+
+typedef struct {
+	int num_three_body_blocks;
+	size_t num_elements;            /* three-body matrix elements computed per run */
+	size_t num_states;              /* M-scheme three-particle states with their coupled expansions */
+	size_t num_terms;               /* expansion terms over all states */
+	size_t num_coupled_states;      /* coupled states over all total-M blocks */
+	size_t num_m_blocks;            /* total-M blocks over all bases */
+	size_t file_states;             /* coupled states of the J-scheme file */
+	size_t file_elements;           /* rows of its matrix file */
+	size_t v_entries;               /* J-scheme matrix entries held on the device */
+	double dense_flops;             /* flops of the reference's dense S^T V S decoupling, for comparison */
+	double algorithmic_bytes;       /* compulsory device traffic of one run */
+	double plan_seconds;            /* host planning time of jn_transform3_open */
+} jn_transform3_stats;
+
+/*
+ * Plan the transform of a jjj-coupled three-body interaction into the
+ * M-scheme three-body blocks that the combination table lists, and upload
+ * the plan to the current CUDA device.  The interaction is a directory in
+ * the reference's ASCII format: one .cnf file (single-particle shells, then
+ * jjj-coupled three-particle states) and one .mat file ("bra ket element"
+ * rows over those states) (src/Neptune/input/read_3nf_ascii_format.c:14-279).
+ * The index-list base directory holds <ppp|pp|p|nnn|nn|n>_inds_index_lists/
+ * basis_energy_<E>; single_particle_energy is the shell limit of the
+ * manager (src/Mercury/arguments/arguments.c:88-160).  Replaces
+ * new_transform_3nf_block_manager + open_data_file
+ * (src/Mercury/transform_3nf_block_manager/transform_3nf_block_manager.c:109-124,
+ * src/Neptune/input/read_3nf_file.c:12-44).
+ */
+jn_status jn_transform3_open(const char *combination_table_file, const char *index_list_dir, int num_protons,
+			     int num_neutrons, int single_particle_energy, const char *jscheme_dir,
+			     jn_transform3 **transform);
+
+/* Enqueue the computation of every three-body block (one kernel) on
+ * `stream` (NULL: the transform's stream).  Replaces get_transformed_block
+ * + get_3nf_mercury_matrix over all blocks
+ * (transform_3nf_block_manager.c:233-284, src/Mercury/transformed_block/transformed_block.c:113-147,
+ * compute_jjj_block in src/Neptune/block_transform/block_transform.c:147-356). */
+jn_status jn_transform3_run(jn_transform3 *transform, void *stream);
+
+/* One run on the transform's stream timed with CUDA events (milliseconds). */
+jn_status jn_transform3_profile(jn_transform3 *transform, float *ms);
+
+/* Elements of three-body block `block_id` from the last run (count only
+ * when host_out is NULL). */
+jn_status jn_transform3_elements(jn_transform3 *transform, int block_id, double *host_out, size_t capacity,
+				 size_t *count);
+
+/* Run and write <output_dir>/<id>_matrix_elements for every three-body block. */
+jn_status jn_transform3_write(jn_transform3 *transform, const char *output_dir);
+
+jn_status jn_transform3_get_stats(const jn_transform3 *transform, jn_transform3_stats *stats);
+void jn_transform3_close(jn_transform3 *transform);
+
+/* One call: plan, run and write every three-body block (the three-body part
+ * of mercury_J_scheme_to_internal.x,
+ * src/Mercury/programs/mercury_J_scheme_to_internal.c:306-398). */
+jn_status jn_transform_3nf(const char *combination_table_file, const char *index_list_dir, const char *output_dir,
+			   int num_protons, int num_neutrons, int single_particle_energy, const char *jscheme_dir);
+
 /* <j1 m1 j2 m2 | j3 m3> with all arguments doubled, as clebsch_gordan
  * defines it (src/Neptune/clebsch_gordan/clebsch_gordan.c:31-42); host only. */
 double jn_clebsch_gordan(int j1, int j2, int j3, int m1, int m2, int m3);

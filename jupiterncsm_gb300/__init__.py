@@ -75,6 +75,15 @@ class TransformStats(ctypes.Structure):
                 ("algorithmic_bytes", ctypes.c_double), ("plan_seconds", ctypes.c_double)]
 
 
+class Transform3Stats(ctypes.Structure):
+    _fields_ = [("num_three_body_blocks", ctypes.c_int), ("num_elements", ctypes.c_size_t),
+                ("num_states", ctypes.c_size_t), ("num_terms", ctypes.c_size_t),
+                ("num_coupled_states", ctypes.c_size_t), ("num_m_blocks", ctypes.c_size_t),
+                ("file_states", ctypes.c_size_t), ("file_elements", ctypes.c_size_t), ("v_entries", ctypes.c_size_t),
+                ("dense_flops", ctypes.c_double), ("algorithmic_bytes", ctypes.c_double),
+                ("plan_seconds", ctypes.c_double)]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("engine", ctypes.c_int), ("rows_per_lane", ctypes.c_int), ("ctas_per_sm", ctypes.c_int),
                 ("ms", ctypes.c_float), ("candidates", ctypes.c_int)]
@@ -148,6 +157,15 @@ def gpu_lib():
     L.jn_transform_close.argtypes = [vp]
     L.jn_transform_close.restype = None
     L.jn_transform_2nf.argtypes = [cp, cp, cp, ci, ci, ci, ci, cp, ci]
+    L.jn_transform3_open.argtypes = [cp, cp, ci, ci, ci, cp, ctypes.POINTER(vp)]
+    L.jn_transform3_run.argtypes = [vp, vp]
+    L.jn_transform3_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.jn_transform3_elements.argtypes = [vp, ci, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.jn_transform3_write.argtypes = [vp, cp]
+    L.jn_transform3_get_stats.argtypes = [vp, ctypes.POINTER(Transform3Stats)]
+    L.jn_transform3_close.argtypes = [vp]
+    L.jn_transform3_close.restype = None
+    L.jn_transform_3nf.argtypes = [cp, cp, cp, ci, ci, ci, cp]
     L.jn_clebsch_gordan.argtypes = [ci] * 6
     L.jn_clebsch_gordan.restype = ctypes.c_double
     L.jn_autotune.argtypes = [vp, ci, ci, ctypes.POINTER(Tuning)]
@@ -194,7 +212,9 @@ def gpu_lib():
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
                  "jn_transform_open", "jn_transform_run", "jn_transform_profile", "jn_transform_elements",
                  "jn_transform_write", "jn_transform_get_stats", "jn_transform_2nf", "jn_read_matrix_elements",
-                 "jn_set_matrix_elements", "jn_lanczos_batch"):
+                 "jn_set_matrix_elements", "jn_lanczos_batch", "jn_transform3_open", "jn_transform3_run",
+                 "jn_transform3_profile", "jn_transform3_elements", "jn_transform3_write", "jn_transform3_get_stats",
+                 "jn_transform_3nf"):
         getattr(L, name).restype = ci
     _gpu = L
     return L
@@ -597,6 +617,79 @@ def transform_2nf(comb, index_list_dir, output_dir, Z, N, single_particle_energy
                                       int(include_kinetic)))
 
 
+class Transform3:
+    """J-scheme -> M-scheme three-body transform on the GPU (Mercury's three-body
+    part, J-scheme elements in the reference's ASCII format)."""
+
+    def __init__(self, comb, index_list_dir, Z, N, single_particle_energy, jscheme_dir):
+        h = ctypes.c_void_p()
+        _check(gpu_lib().jn_transform3_open(comb.encode(), index_list_dir.encode(), Z, N, single_particle_energy,
+                                            jscheme_dir.encode(), ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_dir(cls, d, Z, N, single_particle_energy, jscheme_subdir="jjj"):
+        """A generator output directory: comb.txt, anicr/ and the J-scheme directory."""
+        return cls(os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), Z, N, single_particle_energy,
+                   os.path.join(d, jscheme_subdir))
+
+    def run(self, stream=None):
+        _check(gpu_lib().jn_transform3_run(self._h, ctypes.c_void_p(stream)))
+
+    def profile(self):
+        ms = ctypes.c_float()
+        _check(gpu_lib().jn_transform3_profile(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def block(self, block_id):
+        import numpy as np
+        L = gpu_lib()
+        n = ctypes.c_size_t()
+        _check(L.jn_transform3_elements(self._h, block_id, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        _check(L.jn_transform3_elements(self._h, block_id, out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                        ctypes.byref(n)))
+        return out
+
+    def write(self, output_dir):
+        _check(gpu_lib().jn_transform3_write(self._h, output_dir.encode()))
+
+    def stats(self):
+        s = Transform3Stats()
+        _check(gpu_lib().jn_transform3_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in Transform3Stats._fields_}
+
+    def close(self):
+        if self._h:
+            gpu_lib().jn_transform3_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def transform_3nf(comb, index_list_dir, output_dir, Z, N, single_particle_energy, jscheme_dir):
+    """The three-body part of mercury_J_scheme_to_internal.x: writes <output_dir>/<id>_matrix_elements."""
+    _check(gpu_lib().jn_transform_3nf(comb.encode(), index_list_dir.encode(), output_dir.encode(), Z, N,
+                                      single_particle_energy, jscheme_dir.encode()))
+
+
+def transform3_status(comb, index_list_dir, Z, N, single_particle_energy, jscheme_dir):
+    """(status, message) of jn_transform3_open without raising: the host plan
+    validates its inputs before any device is touched."""
+    L = gpu_lib()
+    h = ctypes.c_void_p()
+    st = L.jn_transform3_open(comb.encode(), index_list_dir.encode(), Z, N, single_particle_energy,
+                              jscheme_dir.encode(), ctypes.byref(h))
+    msg = L.jn_last_error().decode(errors="replace") if st else ""
+    if h.value:
+        L.jn_transform3_close(h)
+    return st, msg
+
+
 def transform_status(comb, index_list_dir, Z, N, single_particle_energy, two_particle_energy, antoine_file,
                      include_kinetic=True):
     """(status, message) of jn_transform_open without raising: host-side validation is
@@ -659,6 +752,8 @@ def gen_lib():
         _gen.jn_gen_pair_normal.argtypes = [ctypes.c_uint64] * 4
         _gen.jn_gen_antoine.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                         ctypes.c_uint64, ctypes.c_double]
+        _gen.jn_gen_jjj_ascii.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, ctypes.c_double,
+                                          ctypes.c_void_p, ctypes.c_void_p]
     return _gen
 
 
@@ -689,6 +784,42 @@ def generate(outdir, Z=2, N=2, nmax=4, M2=0, parity=0, nbody=2, seed=20261203, h
     if rc != 0:
         raise JnError(rc, G.jn_gen_last_error().decode())
     return {k: getattr(s, k) for k, _ in GenSummary._fields_}
+
+
+def three_body_energy(comb):
+    """Largest three-particle energy (ket or bra side) among the three-body
+    matrix-element blocks of a combination table (0 when there are none)."""
+    e3, sec = 0, 0
+    with open(comb) as f:
+        for row in f:
+            if "***" in row:
+                sec = 1 if "Matrix-elements V (cross p-n)" in row else 2 if "Matrix-elements V (same p/n)" in row else 0
+                continue
+            if not sec or "ARRAY:" not in row:
+                continue
+            w = row.split()
+            if sec == 1:
+                k = w[0].count("p") + w[4].count("n")
+                dEp, dp, dEn, dn = int(w[1]), int(w[3]), int(w[5]), int(w[7])
+                lo, hi = dp + dn, dp + dEp + dn + dEn
+            else:
+                k = len(w[0])
+                dE, d = int(w[1]), int(w[3])
+                lo, hi = d, d + dE
+            if k == 3:
+                e3 = max(e3, lo, hi)
+    return e3
+
+
+def write_jjj(dirname, emax, e3max, seed=20261203, sigma=0.1):
+    """Write a seeded jjj-coupled three-body interaction in the reference's
+    ASCII format (dirname/jjj.cnf, dirname/jjj.mat); returns (states, elements)."""
+    G = gen_lib()
+    ns, ne = ctypes.c_int64(), ctypes.c_int64()
+    rc = G.jn_gen_jjj_ascii(dirname.encode(), emax, e3max, seed, sigma, ctypes.byref(ns), ctypes.byref(ne))
+    if rc != 0:
+        raise JnError(rc, G.jn_gen_last_error().decode())
+    return ns.value, ne.value
 
 
 def write_antoine(path, emax1, emax2, num_particles, hbar_omega=20.0, seed=20261203, sigma=1.0):

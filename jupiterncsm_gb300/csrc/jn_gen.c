@@ -1105,6 +1105,101 @@ int jn_gen_antoine(const char *path, int emax1, int emax2, int num_particles, do
 	return rc;
 }
 
+/*
+ * A jjj-coupled three-body interaction in the reference's ASCII format
+ * (src/Neptune/input/read_3nf_ascii_format.c:14-279): <dir>/jjj.cnf lists the
+ * single-particle shells ("i n l j tz", j doubled, tz -1 proton) and the
+ * coupled states ("i a b c Jab Jabc", doubled), <dir>/jjj.mat one
+ * "bra ket element" row per ordered pair of states in the same
+ * (Jabc, Tz, parity) channel.  The states are those the three-body manager
+ * can reach (src/Neptune/bases/jjj_coupled_3p.c:228-357): with shells
+ * numbered as the manager numbers them (e; l and j descending; tz),
+ * (s s s), (s1 s2 s1), (s1 s2 s2) and (s1 s2 s3) for s1 < s2 < s3, all
+ * Jab and Jabc the triangle rules allow, three-particle energy <= e3max.
+ * The file numbers its shells in another order (e; l and j ascending), so
+ * the reader's shell matching and its a <-> b phase are exercised.  Elements
+ * are normal deviates of width sigma, symmetric under bra <-> ket.
+ */
+typedef struct { int e, n, l, j, tz; } gshell_t;
+
+int jn_gen_jjj_ascii(const char *dir, int emax, int e3max, uint64_t seed, double sigma, int64_t *num_states,
+		     int64_t *num_elements)
+{
+	if (emax < 0 || emax > 7 || e3max < 0 || e3max > 3 * emax) FAIL(JN_GEN_EINVAL, "energies out of range (%d, %d)", emax, e3max);
+	/* the manager's order and the file's order of the same shells */
+	gshell_t mg[128], fl[128];
+	int nm = 0, nf = 0;
+	for (int e = 0; e <= emax; e++)
+		for (int l = e; l >= (e & 1); l -= 2)
+			for (int j = 2 * l + 1; j >= abs(2 * l - 1); j -= 2)
+				for (int tz = -1; tz <= 1; tz += 2) { gshell_t g = { e, (e - l) / 2, l, j, tz }; mg[nm++] = g; }
+	for (int e = 0; e <= emax; e++)
+		for (int l = e & 1; l <= e; l += 2)
+			for (int j = abs(2 * l - 1); j <= 2 * l + 1; j += 2)
+				for (int tz = -1; tz <= 1; tz += 2) { gshell_t g = { e, (e - l) / 2, l, j, tz }; fl[nf++] = g; }
+	int m2f[128];
+	for (int a = 0; a < nm; a++)
+		for (int b = 0; b < nf; b++)
+			if (mg[a].e == fl[b].e && mg[a].l == fl[b].l && mg[a].j == fl[b].j && mg[a].tz == fl[b].tz) m2f[a] = b;
+	if (mkdir_p(dir)) FAIL(JN_GEN_EIO, "mkdir %s", dir);
+	/* states: (file a, file b, file c, jab, jabc) and the channel (jabc, tz, parity) */
+	vec_t st = { 0 };
+	st.es = 6 * sizeof(int);
+	for (int a = 0; a < nm; a++)
+		for (int b = a; b < nm; b++)
+			for (int c = 0; c < nm; c++) {
+				if (a == b ? c != a : !(c == a || c == b || c > b)) continue;
+				if (mg[a].e + mg[b].e + mg[c].e > e3max) continue;
+				const int ja = mg[a].j, jb = mg[b].j, jc = mg[c].j;
+				const int tz = mg[a].tz + mg[b].tz + mg[c].tz, par = (mg[a].l + mg[b].l + mg[c].l) & 1;
+				for (int jab = abs(ja - jb); jab <= ja + jb; jab += 2)
+					for (int jabc = abs(jab - jc); jabc <= jab + jc; jabc += 2) {
+						int fa = m2f[a], fb = m2f[b];
+						if (fa > fb) { int t = fa; fa = fb; fb = t; }    /* the file's own a <= b */
+						int r[6] = { fa, fb, m2f[c], jab, jabc, (jabc * 8 + (tz + 3)) * 2 + par };
+						if (vpush(&st, r)) { free(st.a); FAIL(JN_GEN_ENOMEM, "out of memory"); }
+					}
+			}
+	char path[4096];
+	snprintf(path, sizeof path, "%s/jjj.cnf", dir);
+	FILE *f = fopen(path, "w");
+	if (!f) { free(st.a); FAIL(JN_GEN_EIO, "open %s: %s", path, strerror(errno)); }
+	fprintf(f, "---single-particle-states---\n---i---n---l---j---tz---\n");
+	for (int i = 0; i < nf; i++) fprintf(f, "%d %d %d %d %d\n", i, fl[i].n, fl[i].l, fl[i].j, fl[i].tz);
+	fprintf(f, "---three-particle-states---\n---i---a---b---c---Jab-Jabc---\n");
+	const int *S = (const int *)st.a;
+	for (size_t i = 0; i < st.n; i++)
+		fprintf(f, "%zu %d %d %d %d %d\n", i, S[6 * i], S[6 * i + 1], S[6 * i + 2], S[6 * i + 3], S[6 * i + 4]);
+	if (fclose(f)) { free(st.a); FAIL(JN_GEN_EIO, "write %s", path); }
+	/* channels: states grouped by their channel key, in state order */
+	int maxch = 0;
+	for (size_t i = 0; i < st.n; i++) if (S[6 * i + 5] > maxch) maxch = S[6 * i + 5];
+	int *cnt = xcalloc(maxch + 2, sizeof(int)), *first = xcalloc(maxch + 2, sizeof(int));
+	int *members = xcalloc(st.n ? st.n : 1, sizeof(int));
+	for (size_t i = 0; i < st.n; i++) cnt[S[6 * i + 5]]++;
+	for (int c = 1; c <= maxch + 1; c++) first[c] = first[c - 1] + cnt[c - 1];
+	memset(cnt, 0, (maxch + 2) * sizeof(int));
+	for (size_t i = 0; i < st.n; i++) { int c = S[6 * i + 5]; members[first[c] + cnt[c]++] = (int)i; }
+	snprintf(path, sizeof path, "%s/jjj.mat", dir);
+	f = fopen(path, "w");
+	if (!f) { free(st.a); free(cnt); free(first); free(members); FAIL(JN_GEN_EIO, "open %s: %s", path, strerror(errno)); }
+	fprintf(f, "---bra---ket---element---\n");
+	int64_t ne = 0;
+	for (int c = 0; c <= maxch; c++)
+		for (int x = 0; x < cnt[c]; x++)
+			for (int y = 0; y < cnt[c]; y++) {
+				const int b = members[first[c] + x], k = members[first[c] + y];
+				fprintf(f, "%d %d %.17g\n", b, k, sigma * jn_gen_pair_normal(seed, 3, (uint64_t)b, (uint64_t)k));
+				ne++;
+			}
+	int bad = fclose(f) != 0;
+	if (num_states) *num_states = (int64_t)st.n;
+	if (num_elements) *num_elements = ne;
+	free(st.a); free(cnt); free(first); free(members);
+	if (bad) FAIL(JN_GEN_EIO, "write %s", path);
+	return 0;
+}
+
 int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *summary)
 {
 	gen_t G; memset(&G, 0, sizeof G);

@@ -72,6 +72,14 @@ int jn_gen_antoine(const char *path, int emax1, int emax2, int num_particles, do
 /* the seeded N(0,1) deviate attached to the unordered pair {ka, kb} */
 double jn_gen_pair_normal(uint64_t seed, uint64_t tag, uint64_t ka, uint64_t kb);
 
+/* A seeded jjj-coupled three-body interaction in the reference's ASCII
+ * format: <dir>/jjj.cnf and <dir>/jjj.mat, every coupled state the
+ * three-body transform can reach with shells up to emax and three-particle
+ * energy up to e3max, elements ~ N(0, sigma^2) symmetric in bra <-> ket.
+ * Returns 0 or an error code (jn_gen_last_error). */
+int jn_gen_jjj_ascii(const char *dir, int emax, int e3max, uint64_t seed, double sigma, int64_t *num_states,
+		     int64_t *num_elements);
+
 #ifdef __cplusplus
 }
 #endif

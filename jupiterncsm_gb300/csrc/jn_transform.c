@@ -355,6 +355,21 @@ static int read_me_rows(const char *comb, tvec_t *out, char *err, size_t errlen)
 	return 0;
 }
 
+int jn_read_me_blocks(const char *comb, jn_meblock_info_t **rows, int *n, char *err, size_t errlen)
+{
+	tvec_t v = { 0 };
+	v.es = sizeof(jn_meblock_info_t);
+	*rows = NULL;
+	*n = 0;
+	if (read_me_rows(comb, &v, err, errlen)) {
+		free(v.a);
+		return -1;
+	}
+	*rows = (jn_meblock_info_t *)v.a;
+	*n = (int)v.n;
+	return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* Antoine file (three Fortran records)                                 */
 /* ------------------------------------------------------------------ */

@@ -104,6 +104,10 @@ typedef struct {
 	double dense_flops;     /* flops of the reference's dense formulation, for comparison */
 } jn_tplan_t;
 
+/* The matrix-element rows of a combination table ("Matrix-elements V"
+ * sections), in table order; *rows is malloc'ed.  Returns 0 or sets *err. */
+int jn_read_me_blocks(const char *comb, jn_meblock_info_t **rows, int *n, char *err, size_t errlen);
+
 /* Build the plan; returns 0 or sets *err (static text) and returns -1. */
 int jn_tplan_build(jn_tplan_t *p, const char *comb, const char *lists_dir, int Z, int N, int emax1, int emax2,
 		   const char *antoine, int include_kinetic, char *err, size_t errlen);
