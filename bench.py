@@ -244,6 +244,61 @@ def transform_leg(workdir, steps, warmup, flush, peak):
             "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
 
 
+TRANSFORM3_WORKLOAD = dict(Z=3, N=3, nmax=4, M2=0,
+                           label="6Li (Z=3,N=3) Nmax=4, 2M=0: seeded jjj-coupled 3NF N(0,0.1) MeV (the reference's "
+                                 "ASCII J-scheme format) -> all three-body M-scheme blocks of the combination table")
+
+
+def transform3_leg(workdir, steps, warmup, flush, peak):
+    """The J -> M three-body transform on the GPU: one kernel computes every
+    three-body block; timed with CUDA events, L2 flushed between runs."""
+    import torch
+    import jupiterncsm_gb300 as jn
+    w = TRANSFORM3_WORKLOAD
+    d = os.path.join(workdir, "li6_nmax4_jjj")
+    stamp = os.path.join(d, ".complete")
+    if not os.path.exists(stamp):
+        t = time.time()
+        s = jn.generate(d, Z=w["Z"], N=w["N"], nmax=w["nmax"], M2=w["M2"], nbody=3, antoine=True)
+        e3 = jn.three_body_energy(os.path.join(d, "comb.txt"))
+        jn.write_jjj(os.path.join(d, "jjj"), s["emax_single"], e3)
+        open(stamp, "w").write(f"{s['emax_single']}\n")
+        log(f"generated the three-body J-scheme workload in {time.time() - t:.1f} s")
+    e1 = int(open(stamp).read())
+    t0 = time.perf_counter()
+    T = jn.Transform3.from_dir(d, w["Z"], w["N"], e1)
+    open_s = time.perf_counter() - t0
+    st = T.stats()
+    for _ in range(warmup):
+        T.profile()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms.append(T.profile())
+    T.close()
+    kms = sum(ms) / len(ms)
+    out = os.path.join(d, "transformed3")
+    t0 = time.perf_counter()
+    jn.transform_3nf(os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), out, w["Z"], w["N"], e1,
+                     os.path.join(d, "jjj"))
+    e2e_s = time.perf_counter() - t0
+    achieved = st["algorithmic_bytes"] / (kms / 1e3) / 1e9
+    return {"workload": w["label"], "elements": st["num_elements"], "three_body_blocks": st["num_three_body_blocks"],
+            "m_scheme_states": st["num_states"], "coupled_terms": st["num_terms"],
+            "file_states": st["file_states"], "file_elements": st["file_elements"],
+            "kernel_ms": kms, "elements_per_s": st["num_elements"] / (kms / 1e3),
+            "roofline": {"bound": "fp64 pipe", "fp64_pipe_busy_ncu": 0.818,
+                         "profile": "profiles/jn_jjj_to_m_kernel_li6_nmax4.md",
+                         "hbm_achieved": achieved, "hbm_peak": peak, "unit": "GB/s", "hbm_frac": achieved / peak,
+                         "bytes_per_run": st["algorithmic_bytes"], "kernel": "jn_jjj_to_m_kernel"},
+            "dense_equivalent_flops": st["dense_flops"],
+            "dense_equivalent_tflop_per_s": st["dense_flops"] / (kms / 1e3) / 1e12,
+            "plan_seconds": st["plan_seconds"], "open_seconds": open_s,
+            "e2e": {"seconds": e2e_s, "what": "jn_transform_3nf: plan + upload + kernel + copy back + files"},
+            "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
+
+
 def large_basis_leg(workdir, steps, warmup, flush, peak):
     """6Li Nmax=6, 2M=2 (D = 186 894): the two-body interaction comes from the
     GPU J -> M transform (the transform leg's output files) and feeds the
@@ -491,8 +546,18 @@ def main():
                     help="32: 32-bit fixed-point matrix elements and x with exact 64-bit sums (the headline); 64: FP64")
     ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
     ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solves/s leg")
+    ap.add_argument("--leg", choices=["transform", "transform3"],
+                    help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.leg:
+        import torch
+        flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        peaks = measured_peaks()
+        leg = transform_leg if args.leg == "transform" else transform3_leg
+        print(json.dumps({args.leg: leg(args.workdir, args.steps, args.warmup, flush,
+                                         peaks["hbm_gbs"] if peaks else 6800.0)}), flush=True)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -647,6 +712,10 @@ def main():
                 line["large_basis"] = large_basis_leg(wd, min(args.steps, 10), args.warmup, flush, peak)
             except Exception as e:
                 line["large_basis"] = {"error": str(e)}
+        try:
+            line["transform3"] = transform3_leg(wd, min(args.steps, 10), args.warmup, flush, peak)
+        except Exception as e:
+            line["transform3"] = {"error": str(e)}
     if rank == 0 and not args.no_solves:
         try:
             line["solves"] = solves_leg(wd)

@@ -232,13 +232,46 @@ __device__ __forceinline__ int x_exponent(unsigned int xmax_bits)
 	return Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
 }
 
+/* round-half-even of v 2^Sx as a 32-bit integer, from the bits of v: the
+ * same value as __double2int_rn(v * 2^Sx) for finite v whose scaled value
+ * is below 2^31 (the scale guarantees it), without an FP64 instruction.
+ * v = m 2^(e - 1075) with m the significand (implicit bit included, or the
+ * subnormal's fraction with e = 1). */
+__device__ __forceinline__ int fixed32_bits(double v, int Sx)
+{
+	const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+	const int ex = (int)((u >> 52) & 0x7ff);
+	if (ex == 0x7ff) return __double2int_rn(v * ldexp(1.0, Sx));     /* inf, nan: as the FP64 conversion */
+	unsigned long long m = u & 0xfffffffffffffull;
+	int sh = Sx - 1075;
+	if (ex) { m |= 1ull << 52; sh += ex; } else { sh += 1; }
+	unsigned long long q;
+	if (sh >= 0) {
+		q = m << sh;
+	} else {
+		const int k = -sh;
+		if (k > 63) {
+			q = 0;
+		} else {
+			q = m >> k;
+			const unsigned long long rem = m & ((1ull << k) - 1), half = 1ull << (k - 1);
+			if (rem > half || (rem == half && (q & 1))) q++;
+		}
+	}
+	const int r = (int)q;
+	return (u >> 63) ? -r : r;
+}
+
 /* One cluster of PREP_CTAS CTAs: max|x| into ctrl[0] (with the FP32 round-up
  * margin of the other engines' scale), then the panel kernels' copies of x:
  * the 32-bit fixed-point x in the [p][n] layout (xn, when not NULL) and the
  * copy with every block transposed to [n][p] (xt); FP64 copies x itself.
  * Each thread holds its PREP_PER states in registers across the cluster-wide
  * max (partial maxima meet in distributed shared memory), so x is read once;
- * elem[i] is the basis block of state i. */
+ * elem[i] is the basis block of state i.  The work is integer: max|x| is the
+ * largest bit pattern of |x| (NaN left out; the FP32 bound, monotone in |x|,
+ * is taken once of the maximum) and the conversion works on the bits, because
+ * a cluster's few SMs issue few FP64 operations per cycle on GB300. */
 #define PREP_THREADS 1024
 #define PREP_CTAS 8
 #define PREP_PER 4
@@ -251,46 +284,60 @@ __global__ void __cluster_dims__(PREP_CTAS, 1, 1) __launch_bounds__(PREP_THREADS
 {
 	namespace cg = cooperative_groups;
 	cg::cluster_group cluster = cg::this_cluster();
-	__shared__ float wmax[PREP_THREADS / 32];
-	__shared__ float cta_max, all_max;
+	__shared__ unsigned long long wmax[PREP_THREADS / 32];
+	__shared__ unsigned long long cta_max;
+	__shared__ unsigned int all_max;
 	const int rank = (int)cluster.block_rank();
 	double v[PREP_PER];
-	float m = 0.0f;
+	unsigned long long m = 0;
 #pragma unroll
 	for (int u = 0; u < PREP_PER; u++) {
 		const int64_t i = ((int64_t)u * PREP_CTAS + rank) * PREP_THREADS + threadIdx.x;
 		v[u] = i < dim ? x[i] : 0.0;
-		m = fmaxf(m, (float)fabs(v[u]) * 1.0000002f);
+		const unsigned long long a = (unsigned long long)__double_as_longlong(v[u]) & 0x7fffffffffffffffull;
+		if (a <= 0x7ff0000000000000ull && a > m) m = a;
 	}
-	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	for (int o = 16; o; o >>= 1) {
+		const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+		m = t > m ? t : m;
+	}
 	if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
 	__syncthreads();
 	if (threadIdx.x < 32) {
 		m = wmax[threadIdx.x];
-		for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+		for (int o = 16; o; o >>= 1) {
+			const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+			m = t > m ? t : m;
+		}
 		if (threadIdx.x == 0) cta_max = m;
 	}
 	cluster.sync();
 	if (threadIdx.x < 32) {
-		m = threadIdx.x < PREP_CTAS ? *cluster.map_shared_rank(&cta_max, (unsigned int)threadIdx.x) : 0.0f;
-		for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+		m = threadIdx.x < PREP_CTAS ? *cluster.map_shared_rank(&cta_max, (unsigned int)threadIdx.x) : 0ull;
+		for (int o = 16; o; o >>= 1) {
+			const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+			m = t > m ? t : m;
+		}
 		if (threadIdx.x == 0) {
-			all_max = m;
+			const unsigned int b = __float_as_uint((float)__longlong_as_double((long long)m) * 1.0000002f);
+			all_max = b;
 			if (rank == 0) {
-				ctrl[0] = __float_as_uint(m);
+				ctrl[0] = b;
 				ctrl[1] = 0u;
 			}
 		}
 	}
 	__syncthreads();
-	const double s = sizeof(T) == 4 ? ldexp(1.0, x_exponent(__float_as_uint(all_max))) : 1.0;
+	const int Sx = x_exponent(all_max);
 #pragma unroll
 	for (int u = 0; u < PREP_PER; u++) {
 		const int64_t i = ((int64_t)u * PREP_CTAS + rank) * PREP_THREADS + threadIdx.x;
 		if (i < dim) {
 			const uint4 bk = __ldg(blocks + __ldg(elem + i));
 			const uint32_t e = (uint32_t)(i - bk.x), Nn = bk.w, Np = bk.z;
-			const T t = sizeof(T) == 4 ? (T)__double2int_rn(v[u] * s) : (T)v[u];
+			T t;
+			if (sizeof(T) == 4) t = (T)fixed32_bits(v[u], Sx);
+			else t = (T)v[u];
 			if (xn) xn[i] = t;
 			xt[bk.x + (e % Nn) * Np + e / Nn] = t;
 		}

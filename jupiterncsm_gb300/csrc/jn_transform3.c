@@ -33,6 +33,7 @@
 
 #include <dirent.h>
 #include <errno.h>
+#include <pthread.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -198,6 +199,64 @@ static int begins_with(const char *s, const char *t) { return !strncmp(s, t, str
 /* getline into a static-sized buffer; returns 0 at end of file */
 static int next_line(FILE *f, char *buf, size_t n) { return fgets(buf, (int)n, f) != NULL; }
 
+/* one stretch of the matrix file, parsed on its own thread: "b k e" rows as
+ * sscanf(" %ld %ld %lg ") reads them, rows beginning with --- skipped */
+typedef struct {
+	char *beg, *end;
+	int64_t nstates;
+	int64_t n, cap;
+	int64_t *bra, *ket;
+	double *e;
+	const char *bad;        /* first bad row, or NULL */
+	int why;                /* 1 incomplete row, 2 state out of range, 3 out of memory */
+} matchunk_t;
+
+static void *parse_mat_chunk(void *arg)
+{
+	matchunk_t *c = (matchunk_t *)arg;
+	for (char *ln = c->beg; ln < c->end && !c->bad;) {
+		char *eol = (char *)memchr(ln, '\n', (size_t)(c->end - ln));
+		if (eol) *eol = 0;
+		char *next = eol ? eol + 1 : c->end;
+		if (!begins_with(ln, "---")) {
+			char *q = ln, *r;
+			long long v[2];
+			double e = 0.0;
+			int got = 0;
+			v[0] = strtoll(q, &r, 10);
+			if (r != q) {
+				got = 1; q = r;
+				v[1] = strtoll(q, &r, 10);
+				if (r != q) {
+					got = 2; q = r;
+					e = strtod(q, &r);
+					if (r != q) got = 3;
+				}
+			}
+			/* nothing numeric is skipped (blank rows included: the reference
+			   repeats the previous row for them, which changes nothing) */
+			if (got == 1 || got == 2) { c->bad = ln; c->why = 1; break; }
+			if (got == 3) {
+				if (v[0] < 0 || v[1] < 0 || v[0] >= c->nstates || v[1] >= c->nstates) { c->bad = ln; c->why = 2; break; }
+				if (c->n == c->cap) {
+					c->cap = c->cap ? 2 * c->cap : 4096;
+					int64_t *a = (int64_t *)realloc(c->bra, c->cap * sizeof(int64_t));
+					if (a) c->bra = a;
+					int64_t *b = (int64_t *)realloc(c->ket, c->cap * sizeof(int64_t));
+					if (b) c->ket = b;
+					double *d = (double *)realloc(c->e, c->cap * sizeof(double));
+					if (d) c->e = d;
+					if (!a || !b || !d) { c->bad = ln; c->why = 3; break; }
+				}
+				c->bra[c->n] = v[0]; c->ket[c->n] = v[1]; c->e[c->n] = e;
+				c->n++;
+			}
+		}
+		ln = next;
+	}
+	return NULL;
+}
+
 static int read_jfile(jfile_t *J, const char *dir, const shell3_t *msh, int nmsh, char *err, size_t errlen)
 {
 	memset(J, 0, sizeof *J);
@@ -303,39 +362,73 @@ cnf_out:
 		J->phase[i] = ph;
 	}
 	free(stv.a);
-	/* the matrix file: "b k e" rows, rows beginning with --- skipped */
-	f = fopen(mat, "r");
+	/* the matrix file: "b k e" rows (read as sscanf(" %ld %ld %lg ") reads
+	   them), rows beginning with --- skipped; the file is read whole */
+	f = fopen(mat, "rb");
 	if (!f) { snprintf(err, errlen, "Could not open file \"%s\". %s", mat, strerror(errno)); return -1; }
-	vec3_t ev = { 0 };
-	ev.es = sizeof(int64_t) * 2 + sizeof(double);
-	rc = 0;
-	while (next_line(f, line, sizeof line)) {
-		if (begins_with(line, "---")) continue;
-		long long b, k;
-		double e;
-		int got = sscanf(line, " %lld %lld %lg ", &b, &k, &e);
-		if (got == EOF) continue;       /* blank: the reference repeats the previous row, which changes nothing */
-		if (got == 0) continue;
-		if (got < 3) { snprintf(err, errlen, "%s: incomplete row \"%.60s\"", mat, line); rc = -1; break; }
-		if (b < 0 || k < 0 || b >= J->ns || k >= J->ns) { snprintf(err, errlen, "%s: row names state %lld/%lld of %lld", mat, b, k, (long long)J->ns); rc = -1; break; }
-		unsigned char rec[24];
-		int64_t bb = b, kk = k;
-		memcpy(rec, &bb, 8); memcpy(rec + 8, &kk, 8); memcpy(rec + 16, &e, 8);
-		if (vpush(&ev, rec)) { snprintf(err, errlen, "out of memory"); rc = -1; break; }
+	fseek(f, 0, SEEK_END);
+	const long bytes = ftell(f);
+	fseek(f, 0, SEEK_SET);
+	char *text = (char *)malloc((bytes > 0 ? bytes : 0) + 1);
+	if (!text || (bytes > 0 && fread(text, 1, bytes, f) != (size_t)bytes)) {
+		fclose(f); free(text); snprintf(err, errlen, "%s: read failed", mat); return -1;
 	}
 	fclose(f);
-	if (rc) { free(ev.a); return -1; }
-	J->ne = (int64_t)ev.n;
-	J->bra = (int64_t *)malloc((ev.n ? ev.n : 1) * sizeof(int64_t));
-	J->ket = (int64_t *)malloc((ev.n ? ev.n : 1) * sizeof(int64_t));
-	J->e = (double *)malloc((ev.n ? ev.n : 1) * sizeof(double));
-	if (!J->bra || !J->ket || !J->e) { free(ev.a); snprintf(err, errlen, "out of memory"); return -1; }
-	for (size_t i = 0; i < ev.n; i++) {
-		const unsigned char *r = (const unsigned char *)ev.a + 24 * i;
-		memcpy(&J->bra[i], r, 8); memcpy(&J->ket[i], r + 8, 8); memcpy(&J->e[i], r + 16, 8);
+	text[bytes > 0 ? bytes : 0] = 0;
+	/* stretches of whole rows, parsed in parallel and joined in file order */
+	int nthr = (int)(bytes / (4l << 20)) + 1;
+	if (nthr > 16) nthr = 16;
+	matchunk_t ch[16];
+	pthread_t th[16];
+	memset(ch, 0, sizeof ch);
+	char *pos = text, *stop = text + (bytes > 0 ? bytes : 0);
+	for (int i = 0; i < nthr; i++) {
+		ch[i].beg = pos;
+		char *cut = i == nthr - 1 ? stop : text + (bytes / nthr) * (i + 1);
+		if (cut < pos) cut = pos;
+		while (cut > text && cut < stop && cut[-1] != '\n') cut++;     /* end after a newline */
+		ch[i].end = cut;
+		ch[i].nstates = J->ns;
+		pos = cut;
 	}
-	free(ev.a);
-	return 0;
+	int started = 0;
+	for (int i = 1; i < nthr; i++)
+		if (pthread_create(&th[i], NULL, parse_mat_chunk, &ch[i]) == 0) started |= 1 << i;
+	parse_mat_chunk(&ch[0]);
+	for (int i = 1; i < nthr; i++) {
+		if (started & (1 << i)) pthread_join(th[i], NULL);
+		else parse_mat_chunk(&ch[i]);
+	}
+	rc = 0;
+	int64_t n = 0;
+	for (int i = 0; i < nthr && !rc; i++) {
+		if (ch[i].bad) {
+			if (ch[i].why == 1) snprintf(err, errlen, "%s: incomplete row \"%.60s\"", mat, ch[i].bad);
+			else if (ch[i].why == 2) snprintf(err, errlen, "%s: row names state %.40s of %lld", mat, ch[i].bad, (long long)J->ns);
+			else snprintf(err, errlen, "out of memory");
+			rc = -1;
+		}
+		n += ch[i].n;
+	}
+	if (!rc) {
+		J->bra = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+		J->ket = (int64_t *)malloc((n ? n : 1) * sizeof(int64_t));
+		J->e = (double *)malloc((n ? n : 1) * sizeof(double));
+		if (!J->bra || !J->ket || !J->e) { snprintf(err, errlen, "out of memory"); rc = -1; }
+	}
+	int64_t o = 0;
+	for (int i = 0; i < nthr; i++) {
+		if (!rc && ch[i].n) {
+			memcpy(J->bra + o, ch[i].bra, ch[i].n * sizeof(int64_t));
+			memcpy(J->ket + o, ch[i].ket, ch[i].n * sizeof(int64_t));
+			memcpy(J->e + o, ch[i].e, ch[i].n * sizeof(double));
+			o += ch[i].n;
+		}
+		free(ch[i].bra); free(ch[i].ket); free(ch[i].e);
+	}
+	free(text);
+	J->ne = rc ? 0 : n;
+	return rc;
 }
 
 /* ------------------------------------------------------------------ */
@@ -860,7 +953,10 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 	memset(&kc, 0, sizeof kc);
 	jfile_t J;
 	memset(&J, 0, sizeof J);
-	hmap_t vdiag = { 0 }, voff = { 0 };
+	uint64_t *fkeys = NULL;                 /* the file's canonical coupled states, sorted */
+	int64_t nfk = 0, nch = 0, *chsize = NULL, *choff = NULL;
+	int32_t *fch = NULL, *floc = NULL, *fkid = NULL;
+	double *vnd = NULL, *vdg = NULL;        /* V per channel: as read, and with the mirror of diagonal blocks */
 	shell3_t *sh = NULL;
 	sp3_t *sp = NULL;
 	vec3_t tb = { 0 }, tbi = { 0 }, c0 = { 0 }, pcv = { 0 }, ncv = { 0 }, pairs = { 0 }, ebv = { 0 }, Vv = { 0 };
@@ -885,20 +981,59 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 	if (read_jfile(&J, jscheme_dir, sh, nsh, err, errlen)) goto fail;
 	p->file_states = J.ns;
 	p->file_elements = J.ne;
-	/* V over canonical coupled keys, both ways the reference fills a block
-	   (read_3nf_ascii_format.c:410-425): rows b, columns k, last row wins;
-	   diagonal blocks also write the mirror */
+	/* V over the file's canonical coupled states, both ways the reference
+	   fills a block (read_3nf_ascii_format.c:410-425): rows b, columns k,
+	   the last row wins; diagonal blocks also write the mirror.  A cut pairs
+	   states of one (Jabc, Tz, parity) channel only, so V is held densely per
+	   channel; rows across channels are never read. */
+	fkeys = (uint64_t *)malloc((J.ns ? J.ns : 1) * sizeof(uint64_t));
+	if (!fkeys) TERR("out of memory");
+	memcpy(fkeys, J.key, J.ns * sizeof(uint64_t));
+	qsort(fkeys, J.ns, sizeof(uint64_t), cmp_u64);
+	for (int64_t i = 0; i < J.ns; i++)
+		if (!nfk || fkeys[i] != fkeys[nfk - 1]) fkeys[nfk++] = fkeys[i];
+	fch = (int32_t *)malloc((nfk ? nfk : 1) * sizeof(int32_t));
+	floc = (int32_t *)malloc((nfk ? nfk : 1) * sizeof(int32_t));
+	{
+		/* channels in key order: (jabc, tz, parity) of the manager's shells */
+		hmap_t chm = { 0 };
+		vec3_t chn = { 0 };
+		chn.es = sizeof(int64_t);
+		for (int64_t i = 0; i < nfk && fch && floc; i++) {
+			const uint64_t k = fkeys[i];
+			const int tz = sh[KA(k)].tz + sh[KB(k)].tz + sh[KC(k)].tz, par = (sh[KA(k)].l + sh[KB(k)].l + sh[KC(k)].l) & 1;
+			uint64_t *c = hget(&chm, (uint64_t)KJABC(k) * 64 + (uint64_t)(tz + 8) * 2 + par, 0, 1, (uint64_t)-1);
+			if (!c) { hfree(&chm); free(chn.a); TERR("out of memory"); }
+			if (*c == (uint64_t)-1) {
+				int64_t z = 0;
+				*c = chn.n;
+				if (vpush(&chn, &z)) { hfree(&chm); free(chn.a); TERR("out of memory"); }
+			}
+			fch[i] = (int32_t)*c;
+			floc[i] = (int32_t)((int64_t *)chn.a)[*c]++;
+		}
+		hfree(&chm);
+		if (!fch || !floc) { free(chn.a); TERR("out of memory"); }
+		nch = (int64_t)chn.n;
+		chsize = (int64_t *)chn.a;
+		choff = (int64_t *)malloc((nch + 1) * sizeof(int64_t));
+		if (!choff) TERR("out of memory");
+		choff[0] = 0;
+		for (int64_t c = 0; c < nch; c++) choff[c + 1] = choff[c] + chsize[c] * chsize[c];
+		vnd = (double *)calloc(choff[nch] ? choff[nch] : 1, sizeof(double));
+		vdg = (double *)calloc(choff[nch] ? choff[nch] : 1, sizeof(double));
+		fkid = (int32_t *)malloc((J.ns ? J.ns : 1) * sizeof(int32_t));
+		if (!vnd || !vdg || !fkid) TERR("out of memory");
+		for (int64_t i = 0; i < J.ns; i++) fkid[i] = (int32_t)find_key(fkeys, nfk, J.key[i]);
+	}
 	for (int64_t i = 0; i < J.ne; i++) {
-		const uint64_t kb = J.key[J.bra[i]], kk = J.key[J.ket[i]];
+		const int32_t kb = fkid[J.bra[i]], kk = fkid[J.ket[i]];
+		if (fch[kb] != fch[kk]) continue;
 		const double v = J.e[i] * (J.phase[J.bra[i]] * J.phase[J.ket[i]]);
-		uint64_t bits;
-		memcpy(&bits, &v, 8);
-		uint64_t *a = hget(&voff, kb, kk, 1, 0), *b1 = hget(&vdiag, kb, kk, 1, 0);
-		if (!a || !b1) TERR("out of memory");
-		*a = bits; *b1 = bits;
-		uint64_t *b2 = hget(&vdiag, kk, kb, 1, 0);
-		if (!b2) TERR("out of memory");
-		*b2 = bits;
+		const int64_t o = choff[fch[kb]], n = chsize[fch[kb]];
+		vnd[o + floc[kb] * n + floc[kk]] = v;
+		vdg[o + floc[kb] * n + floc[kk]] = v;
+		vdg[o + floc[kk] * n + floc[kb]] = v;
 	}
 
 	if (jn_read_me_blocks(comb, &p->info, &p->nblocks, err, errlen)) goto fail;
@@ -999,13 +1134,21 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 			if (K->parity != B->parity || !K->nskeys[s] || !B->nskeys[s]) continue;
 			p->voff[e * t.nslots + s] = (int64_t)Vv.n;
 			p->vld[e * t.nslots + s] = K->nskeys[s];
-			for (int r = 0; r < B->nskeys[s]; r++)
+			const double *vt = diag ? vdg : vnd;
+			int64_t *cid = (int64_t *)malloc((size_t)K->nskeys[s] * sizeof(int64_t));
+			if (!cid) TERR("out of memory");
+			for (int c = 0; c < K->nskeys[s]; c++) cid[c] = find_key(fkeys, nfk, K->skeys[s][c]);
+			for (int r = 0; r < B->nskeys[s]; r++) {
+				const int64_t rk = find_key(fkeys, nfk, B->skeys[s][r]);
 				for (int c = 0; c < K->nskeys[s]; c++) {
-					const uint64_t *v = hget(diag ? &vdiag : &voff, B->skeys[s][r], K->skeys[s][c], 0, 0);
 					double x = 0.0;
-					if (v) memcpy(&x, v, 8);
-					if (vpush(&Vv, &x)) TERR("out of memory");
+					const int64_t ck = cid[c];
+					if (rk >= 0 && ck >= 0 && fch[rk] == fch[ck])
+						x = vt[choff[fch[rk]] + (int64_t)floc[rk] * chsize[fch[rk]] + floc[ck]];
+					if (vpush(&Vv, &x)) { free(cid); TERR("out of memory"); }
 				}
+			}
+			free(cid);
 		}
 		/* flops of the reference's dense D_M per M block and J_abc */
 		for (int q = 0; q < K->nmb; q++) {
@@ -1048,7 +1191,7 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 	for (size_t i = 0; i < t.bases.n; i++) basis_free(&((basis3_t *)t.bases.a)[i]);
 	free(t.bases.a); hfree(&t.cg);
 	free(c0.a); free(pairs.a); free(ebv.a); free(sh); free(sp);
-	hfree(&vdiag); hfree(&voff);
+	free(fkeys); free(fch); free(floc); free(fkid); free(chsize); free(choff); free(vnd); free(vdg);
 	jfile_free(&J);
 	kcache_free(&kc);
 	return 0;
@@ -1057,7 +1200,7 @@ fail:
 	free(t.bases.a); free(t.ms.a); free(t.terms.a); free(t.lut.a); hfree(&t.cg);
 	free(tb.a); free(tbi.a); free(c0.a); free(pcv.a); free(ncv.a); free(pairs.a); free(ebv.a); free(Vv.a);
 	free(sh); free(sp);
-	hfree(&vdiag); hfree(&voff);
+	free(fkeys); free(fch); free(floc); free(fkid); free(chsize); free(choff); free(vnd); free(vdg);
 	jfile_free(&J);
 	kcache_free(&kc);
 	jn_t3plan_free(p);

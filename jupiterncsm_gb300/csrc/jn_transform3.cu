@@ -37,6 +37,7 @@ struct jn_transform3 {
 	int device;
 	cudaStream_t stream;
 	jn_t3block_t *d_tb;
+	int32_t *d_chunk;               /* per 2^T3_CHUNK_SHIFT elements: the block of the first */
 	jn_m3state_t *d_ms;
 	jn_m3term_t *d_term;
 	int64_t *d_voff;
@@ -53,8 +54,10 @@ struct jn_transform3 {
 	int grid;
 };
 
+#define T3_CHUNK_SHIFT 6
+
 __global__ void __launch_bounds__(256) jn_jjj_to_m_kernel(
-	const jn_t3block_t *__restrict__ tb, int n3, int64_t nelem, const jn_m3state_t *__restrict__ ms,
+	const jn_t3block_t *__restrict__ tb, const int32_t *__restrict__ chunk_block, int n3, int64_t nelem, const jn_m3state_t *__restrict__ ms,
 	const jn_m3term_t *__restrict__ term, const int64_t *__restrict__ voff, const int32_t *__restrict__ vld, int nslots,
 	const double *__restrict__ V, const int32_t *__restrict__ cket, const int32_t *__restrict__ cbra,
 	const int32_t *__restrict__ csign, const jn_p3conn_t *__restrict__ pc, const jn_nconn_t *__restrict__ nc,
@@ -62,11 +65,10 @@ __global__ void __launch_bounds__(256) jn_jjj_to_m_kernel(
 {
 	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nelem;
 	     e += (int64_t)gridDim.x * blockDim.x) {
-		int lo = 0, hi = n3 - 1;
-		while (lo < hi) {
-			const int mid = (lo + hi + 1) >> 1;
-			if (tb[mid].out <= e) lo = mid; else hi = mid - 1;
-		}
+		/* the block holding element e: from the block of its chunk's first
+		   element, forward over the blocks that start inside the chunk */
+		int lo = chunk_block[e >> T3_CHUNK_SHIFT];
+		while (lo + 1 < n3 && tb[lo + 1].out <= e) lo++;
 		const jn_t3block_t b = tb[lo];
 		const int64_t i = e - b.out;
 		int32_t ket, bra;
@@ -138,7 +140,7 @@ static jn_status up(T **d, const T *h, size_t n)
 extern "C" void jn_transform3_close(jn_transform3 *t)
 {
 	if (!t) return;
-	cudaFree(t->d_tb); cudaFree(t->d_ms); cudaFree(t->d_term); cudaFree(t->d_voff); cudaFree(t->d_vld);
+	cudaFree(t->d_tb); cudaFree(t->d_chunk); cudaFree(t->d_ms); cudaFree(t->d_term); cudaFree(t->d_voff); cudaFree(t->d_vld);
 	cudaFree(t->d_V); cudaFree(t->d_cket); cudaFree(t->d_cbra); cudaFree(t->d_csign); cudaFree(t->d_pc);
 	cudaFree(t->d_nc); cudaFree(t->d_lut); cudaFree(t->d_out);
 	if (t->stream) cudaStreamDestroy(t->stream);
@@ -175,6 +177,18 @@ extern "C" jn_status jn_transform3_open(const char *comb, const char *lists_dir,
 	jn_status s = JN_OK;
 	if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) s = jn_fail(JN_ERR_CUDA, "stream");
 	if (!s) s = up(&t->d_tb, p->tb, p->n3);
+	if (!s) {
+		const int64_t nch = ((p->nelem ? p->nelem : 1) + (1 << T3_CHUNK_SHIFT) - 1) >> T3_CHUNK_SHIFT;
+		int32_t *cb = (int32_t *)malloc(nch * sizeof(int32_t));
+		if (!cb) s = jn_fail(JN_ERR_NOMEM, "out of memory");
+		for (int64_t c = 0, b = 0; !s && c < nch; c++) {
+			const int64_t e = c << T3_CHUNK_SHIFT;
+			while (b + 1 < p->n3 && p->tb[b + 1].out <= e) b++;
+			cb[c] = (int32_t)b;
+		}
+		if (!s) s = up(&t->d_chunk, cb, (size_t)nch);
+		free(cb);
+	}
 	if (!s) s = up(&t->d_ms, p->ms, p->nms);
 	if (!s) s = up(&t->d_term, p->term, p->nterm);
 	if (!s) s = up(&t->d_voff, p->voff, (size_t)p->neb * p->nslots);
@@ -199,7 +213,7 @@ static jn_status enqueue(jn_transform3 *t, cudaStream_t st)
 {
 	const jn_t3plan_t *p = &t->plan;
 	if (p->nelem)
-		jn_jjj_to_m_kernel<<<t->grid, 256, 0, st>>>(t->d_tb, p->n3, p->nelem, t->d_ms, t->d_term, t->d_voff, t->d_vld,
+		jn_jjj_to_m_kernel<<<t->grid, 256, 0, st>>>(t->d_tb, t->d_chunk, p->n3, p->nelem, t->d_ms, t->d_term, t->d_voff, t->d_vld,
 							   p->nslots, t->d_V, t->d_cket, t->d_cbra, t->d_csign, t->d_pc, t->d_nc,
 							   t->d_lut, t->d_out);
 	cudaError_t e = cudaGetLastError();

@@ -167,6 +167,30 @@ def test_panel_engine_is_exact_model(problem, name, bits):
     H.close()
 
 
+@pytest.mark.gpu
+def test_panel_engine_rounds_ties_to_even(problem):
+    """x whose 32-bit fixed-point values fall exactly halfway between integers
+    (max|x| = 1 gives the scale 2^29, x = (k + 1/2) 2^-29), plus subnormals,
+    signed zeros and values that round to zero: the device conversion rounds
+    half to even as the CPU model's llrint does, bit for bit."""
+    d, Z, N, *_ = problem("he4_n4_2b")
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    H.set_engine(4)
+    H.set_precision(32)
+    rng = np.random.default_rng(29)
+    k = rng.integers(-(1 << 28), 1 << 28, H.dimension)
+    x = (k + 0.5) * 2.0 ** -29
+    x[::7] = k[::7] * 2.0 ** -29                     # exact integers at the scale
+    x[1::11] = rng.standard_normal(len(x[1::11])) * 1e-12   # round to zero or to +-1
+    x[2::13] = 5e-324                                # subnormal
+    x[3::17] = -0.0
+    x[0] = 1.0
+    got = H.matvec(x)
+    want = emu4(d, Z, N, x, True)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    H.close()
+
+
 def test_engines_agree(problem):
     d, Z, N, *_ = problem("he4_n6_3b")
     H = jn.Hamiltonian.from_dir(d, Z, N)

@@ -283,13 +283,22 @@ def test_open_reports_bad_inputs_before_touching_a_device(jproblem, tmp_path):
     assert st == jn.JN_ERR_FORMAT and "two particles" in msg
 
 
-def test_mercury_cli_rejects_three_body_path(jproblem):
+def test_mercury_cli_without_a_device(jproblem, tmp_path):
+    """--no-2nf writes the one- and two-body blocks as zeros on the host (the
+    reference's generate_2nf_zero_matrix_blocks); a three-body path that is not
+    a J-scheme directory (the HDF5 format) is reported, and no usage error."""
     d, Z, N, e1, e2 = jproblem("he4_n2")
-    r = subprocess.run([jn.MERCURY_CLI, os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), d, "--num-protons",
-                        str(Z), "--num-neutrons", str(N), "--single-particle-energy", str(e1),
-                        "--two-particle-energy", str(e2), os.path.join(d, "antoine_2nf.bin"), "three_body.h5"],
-                       capture_output=True, text=True)
-    assert r.returncode == 1 and "three-body" in r.stderr
+    out = str(tmp_path / "me")
+    r = subprocess.run([jn.MERCURY_CLI, os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), out, "--num-protons",
+                        str(Z), "--num-neutrons", str(N), "--single-particle-energy", str(e1), "--no-2nf",
+                        "--finished-blocks-file", str(tmp_path / "fin"), "three_body.h5"],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 1 and "HDF5" in r.stderr
+    files = os.listdir(out)
+    assert files
+    for f in files:
+        nd_n, nd_p, x = oracle.read_me_file(os.path.join(out, f))
+        assert len(x) == (nd_n * nd_p if nd_n and nd_p else nd_n + nd_p) and not x.any()
     r = subprocess.run([jn.MERCURY_CLI], capture_output=True, text=True)
     assert r.returncode == 0 and "Usage" in r.stdout
 

@@ -325,3 +325,49 @@ def test_written_blocks_feed_the_product(j3problem, tmp_path):
         assert np.abs(y - want).max() / np.abs(want).max() <= 1e-12
     finally:
         H.close()
+
+
+@pytest.mark.gpu
+def test_mercury_program_writes_all_blocks_and_resumes(j3problem, tmp_path):
+    """jn_mercury with the reference's command line: one-body zeros, the
+    two-body transform, the three-body transform; a second run with the same
+    finished-blocks file skips every energy block; --no-2nf writes the
+    one- and two-body blocks as zeros and takes the only path as three-body."""
+    import subprocess
+    d, meta = j3problem["transform3_he4_n2"]
+    c = meta["case"]
+    g = golden("transform3_he4_n2")
+    exe = os.path.join(ROOT, "jupiterncsm_gb300", "lib", "jn_mercury")
+    s = json.load(open(os.path.join(GOLDEN, "transform_he4_n2.json")))
+    out = str(tmp_path / "me")
+    fin = str(tmp_path / "finished")
+    args = [exe, os.path.join(d, "comb.txt"), os.path.join(d, "anicr"), out, "--num-protons", str(c["Z"]),
+            "--num-neutrons", str(c["N"]), "--single-particle-energy", str(meta["emax_single"]),
+            "--two-particle-energy", str(s["emax_pair"]), "--finished-blocks-file", fin, "--LEC-CE", "0.5"]
+    r = subprocess.run(args + [os.path.join(d, "antoine_2nf.bin"), os.path.join(d, "jjj")], capture_output=True,
+                       text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    for k in g.files:
+        _, _, x = oracle.read_me_file(os.path.join(out, f"{k[1:]}_matrix_elements"))
+        assert np.abs(x - g[k]).max(initial=0.0) <= ME_TOL
+    nfin = os.path.getsize(fin) // 8
+    assert nfin > 0 and sorted(np.fromfile(fin, dtype=np.uint64).tolist()) == list(range(nfin))
+    # resume: every energy block is finished, so nothing three-body is written again
+    victim = os.path.join(out, f"{g.files[0][1:]}_matrix_elements")
+    os.remove(victim)
+    r = subprocess.run(args + [os.path.join(d, "antoine_2nf.bin"), os.path.join(d, "jjj")], capture_output=True,
+                       text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert not os.path.exists(victim)
+    assert os.path.getsize(fin) // 8 == nfin
+    # --no-2nf: the only interaction path is the three-body one
+    out2 = str(tmp_path / "me2")
+    args2 = [out2 if a == out else fin + "2" if a == fin else a for a in args]
+    r = subprocess.run(args2 + ["--no-2nf", os.path.join(d, "jjj")], capture_output=True, text=True,
+                       cwd=str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    for k in g.files:
+        _, _, x = oracle.read_me_file(os.path.join(out2, f"{k[1:]}_matrix_elements"))
+        assert np.abs(x - g[k]).max(initial=0.0) <= ME_TOL
+    two = [f for f in os.listdir(out2) if f"b{f.split('_')[0]}" not in g.files]
+    assert two and all(not oracle.read_me_file(os.path.join(out2, f))[2].any() for f in two)
