@@ -29,7 +29,27 @@ void jn_panels_free(jn_plan_t *p)
 /* lanes per row: a narrow panel puts floor(32 / ncols) rows side by side */
 static int lanes_per_row(int ncols) { return ncols < 32 ? ncols : 32; }
 
-/* warp passes of a task: one per R rows, twice for an off-diagonal panel */
+/* Column chunks of a panel: 32-column chunks, then the rest.  A chunk of w
+ * columns runs floor(32 / w) rows side by side in a warp; when that leaves
+ * more than an eighth of the lanes idle, the largest power of two below w is
+ * split off as its own chunk (its rows fill the warp exactly) and the rest
+ * is chunked the same way.  Chunk k starts at column i0[k] and is cw[k]
+ * wide; returns the number of chunks after the 32-column ones (at most 6),
+ * whose count is ncols / 32. */
+static int tail_chunks(int ncols, int *i0, int *cw)
+{
+	int n = 0, at = ncols - ncols % 32, w = ncols % 32;
+	while (w > 0) {
+		if (8 * (w * (32 / w)) >= 7 * 32) { i0[n] = at; cw[n++] = w; break; }
+		int p = 1;
+		while (2 * p < w) p *= 2;
+		i0[n] = at; cw[n++] = p;
+		at += p;
+		w -= p;
+	}
+	return n;
+}
+
 static double task_cost(const jn_plan_t *p, const uint32_t *T)
 {
 	const int R = 32 / (int)(T[3] >> 24);
@@ -134,9 +154,13 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 		}
 		if (x->kind == JN_KIND_N && P->nrows > 65535) ERR("instruction %d: %d spectator rows", order[q], P->nrows);
 		if (P->nrows > 0 && P->ncols > 0) {
-			const int R = 32 / lanes_per_row(P->ncols);
-			const int64_t rows_per_task = (int64_t)R * iter;
-			ntask += ((P->ncols + 31) / 32) * ((P->nrows + rows_per_task - 1) / rows_per_task);
+			int ci[8], cwv[8];
+			const int nc = tail_chunks(P->ncols, ci, cwv);
+			ntask += (int64_t)(P->ncols / 32) * ((P->nrows + iter - 1) / iter);
+			for (int k = 0; k < nc; k++) {
+				const int64_t rows_per_task = (int64_t)(32 / cwv[k]) * iter;
+				ntask += (P->nrows + rows_per_task - 1) / rows_per_task;
+			}
 		}
 	}
 	p->npanels = p->ninstr;
@@ -148,9 +172,11 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	for (int q = 0; q < p->npanels; q++) {
 		const jn_panel_t *P = &p->panels[q];
 		if (P->nrows <= 0 || P->ncols <= 0) continue;
-		const int cw = lanes_per_row(P->ncols), R = 32 / cw;
-		const int64_t rows_per_task = (int64_t)R * iter;
-		for (int i0 = 0; i0 < P->ncols; i0 += 32)
+		int ci[8], cwv[8];
+		const int nt = tail_chunks(P->ncols, ci, cwv), nfull = P->ncols / 32;
+		for (int k = 0; k < nfull + nt; k++) {
+			const int cw = k < nfull ? 32 : cwv[k - nfull], R = 32 / cw, i0 = k < nfull ? 32 * k : ci[k - nfull];
+			const int64_t rows_per_task = (int64_t)R * iter;
 			for (int64_t j0 = 0; j0 < P->nrows; j0 += rows_per_task) {
 				const int64_t j1 = j0 + rows_per_task < P->nrows ? j0 + rows_per_task : P->nrows;
 				uint32_t *T = p->ptasks + 4 * t;
@@ -160,6 +186,7 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 				T[3] = (uint32_t)i0 | ((uint32_t)cw << 24);
 				t++;
 			}
+		}
 	}
 	p->pgrid = grid;
 	if (jn_panels_partition(p, grid, &p->pcta, &p->pflush_ptr, &p->pflush, &p->npflush)) ERR("out of host memory");
