@@ -117,6 +117,7 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
  * ctrl (2 B words). */
 typedef struct {
 	int grid;               /* persistent CTAs per instance */
+	int words;              /* the largest CTA accumulator of the partition */
 	uint32_t *cta, *flush_ptr, *flush;      /* device copies of the partition */
 } jn_panel_partition;
 jn_status jn_panels_partition_upload(jn_ctx *c, int grid, jn_panel_partition *pp);

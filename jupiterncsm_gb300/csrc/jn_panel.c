@@ -127,8 +127,8 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 		P->Nn_in = (int32_t)bi->Nn;
 		P->Np_out = (int32_t)bo->Np;
 		P->Np_in = (int32_t)bi->Np;
-		P->out_soff = (int32_t)p->pblocks[4 * x->bout + 1];
-		P->in_soff = (int32_t)p->pblocks[4 * x->bin + 1];
+		P->out_blk = x->bout;
+		P->in_blk = x->bin;
 		P->kind = x->kind | (x->bin == x->bout ? JN_PANEL_DIAG : 0);
 		const jn_list_t *Ln = x->ln >= 0 ? &p->lists[x->ln] : NULL, *Lp = x->lp >= 0 ? &p->lists[x->lp] : NULL;
 		if (x->kind == JN_KIND_NP) {
@@ -189,7 +189,8 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 		}
 	}
 	p->pgrid = grid;
-	if (jn_panels_partition(p, grid, &p->pcta, &p->pflush_ptr, &p->pflush, &p->npflush)) ERR("out of host memory");
+	if (jn_panels_partition(p, grid, &p->pcta, &p->pflush_ptr, &p->pflush, &p->npflush, &p->pcta_words))
+		ERR("out of host memory");
 	/* within each CTA's run, heaviest tasks first: the warps that finish last
 	   then finish with small tasks (the order never changes a result bit) */
 	for (int b = 0; b < grid; b++) {
@@ -218,8 +219,9 @@ fail:
 }
 
 int jn_panels_partition(const jn_plan_t *p, int grid, uint32_t **cta_out, uint32_t **flush_ptr_out,
-			uint32_t **flush_out, int64_t *nflush_out)
+			uint32_t **flush_out, int64_t *nflush_out, int64_t *words_out)
 {
+	int64_t words_max = 0;
 	const int64_t ntask = p->nptasks;
 	uint32_t *cta = malloc((size_t)(grid + 1) * sizeof(uint32_t));
 	uint32_t *fptr = malloc((size_t)(grid + 1) * sizeof(uint32_t));
@@ -245,7 +247,9 @@ int jn_panels_partition(const jn_plan_t *p, int grid, uint32_t **cta_out, uint32
 			cta[b] = (uint32_t)(b == grid ? ntask : k);
 		}
 	}
-	/* the blocks each CTA touches: forward into the output block, transpose into the input block */
+	/* the blocks each CTA touches (forward into the output block, transpose
+	   into the input block), each at its place in the CTA's own accumulator:
+	   rows padded to Nn | 1, blocks one after another */
 	for (int b = 0; b < grid; b++) {
 		fptr[b] = (uint32_t)nf;
 		memset(touched, 0, p->nblocks);
@@ -254,20 +258,26 @@ int jn_panels_partition(const jn_plan_t *p, int grid, uint32_t **cta_out, uint32
 			touched[x->bout] = 1;
 			if (x->bin != x->bout) touched[x->bin] = 1;
 		}
+		int64_t words = 0;
 		for (int i = 0; i < p->nblocks; i++) {
 			if (!touched[i] || p->blocks[i].Np <= 0 || p->blocks[i].Nn <= 0) continue;
-			if ((size_t)nf == fcap) {
+			if ((size_t)(2 * nf + 2) > fcap) {
 				fcap *= 2;
 				uint32_t *g = realloc(flush, fcap * sizeof(uint32_t));
 				if (!g) goto fail;
 				flush = g;
 			}
-			flush[nf++] = (uint32_t)i;
+			flush[2 * nf] = (uint32_t)i;
+			flush[2 * nf + 1] = (uint32_t)words;
+			nf++;
+			words += p->blocks[i].Np * (p->blocks[i].Nn | 1);
 		}
+		if (words > words_max) words_max = words;
 	}
 	fptr[grid] = (uint32_t)nf;
 	free(cost); free(touched);
 	*cta_out = cta; *flush_ptr_out = fptr; *flush_out = flush; *nflush_out = nf;
+	if (words_out) *words_out = words_max;
 	return 0;
 fail:
 	free(cta); free(fptr); free(cost); free(touched); free(flush);

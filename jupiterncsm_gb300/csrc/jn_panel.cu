@@ -64,12 +64,13 @@ template <typename T, typename Fix, int KIND, bool DIAG>
 __device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const uint4 pc, const uint4 pd, uint32_t j0,
 					   uint32_t j1, int R, int r, int i, unsigned int *__restrict__ lo,
 					   unsigned int *__restrict__ hi, const T *__restrict__ x, const T *__restrict__ xt,
-					   const T *__restrict__ coef, const uint32_t *__restrict__ meta, const Fix fix)
+					   const T *__restrict__ coef, const uint32_t *__restrict__ meta, const Fix fix,
+					   int out_soff, int in_soff)
 {
 	const int64_t c_off = (int64_t)pa.x | ((int64_t)pa.y << 32);
 	const uint32_t row_meta = pa.z, col_meta = pa.w;
 	const int out_off = (int)pb.x, in_off = (int)pb.y, Nn_out = (int)pb.z, Nn_in = (int)pb.w;
-	const int ncols = (int)pc.x, out_soff = (int)pc.z, in_soff = (int)pc.w;
+	const int ncols = (int)pc.x;
 	const int Np_out = (int)pd.z, Np_in = (int)pd.w;
 	/* element (row entry sr -> dr, column entry sc -> dc) reads x at (sr, sc) of the input block and
 	   lands on y at (dr, dc) of the output block; the transpose swaps the two.  Lanes own columns, so
@@ -128,18 +129,22 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 					      const T *__restrict__ x, const T *__restrict__ xt,
 					      unsigned long long *__restrict__ gacc, const Fix fix, int words)
 {
+	/* the CTA's accumulator holds only the blocks it touches (flush pairs
+	   {block, offset}); bmap[block] is the block's offset in it */
 	extern __shared__ unsigned int sacc[];
 	__shared__ unsigned int next_task;
-	unsigned int *lo = sacc, *hi = sacc + words;
+	unsigned int *lo = sacc, *hi = sacc + words, *bmap = sacc + 2 * words;
 	const int lane = threadIdx.x & 31;
 	const uint32_t f0 = flush_ptr[blockIdx.x], f1 = flush_ptr[blockIdx.x + 1];
 	/* clear the blocks this CTA touches (padded rows) */
 	for (uint32_t f = f0; f < f1; f++) {
-		const uint4 bk = __ldg(blocks + flush[f]);
+		const uint32_t b = __ldg(flush + 2 * f), so = __ldg(flush + 2 * f + 1);
+		const uint4 bk = __ldg(blocks + b);
 		const uint32_t n = bk.z * (bk.w | 1u);
+		if (threadIdx.x == 0) bmap[b] = so;
 		for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-			lo[bk.y + e] = 0u;
-			hi[bk.y + e] = 0u;
+			lo[so + e] = 0u;
+			hi[so + e] = 0u;
 		}
 	}
 	if (threadIdx.x == 0) next_task = 0;
@@ -159,24 +164,26 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 		if (r >= R || i >= (int)pc.x) continue;
 		const int kind = (int)pc.y & 7;
 		const bool diag = (pc.y & JN_PANEL_DIAG) != 0;
+		const int so = (int)bmap[pc.z], si = (int)bmap[pc.w];
 		if (kind == JN_KIND_NP) {
-			if (diag) panel_task<T, Fix, JN_KIND_NP, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
-			else panel_task<T, Fix, JN_KIND_NP, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			if (diag) panel_task<T, Fix, JN_KIND_NP, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			else panel_task<T, Fix, JN_KIND_NP, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
 		} else if (kind == JN_KIND_N) {
-			if (diag) panel_task<T, Fix, JN_KIND_N, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
-			else panel_task<T, Fix, JN_KIND_N, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			if (diag) panel_task<T, Fix, JN_KIND_N, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			else panel_task<T, Fix, JN_KIND_N, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
 		} else {
-			if (diag) panel_task<T, Fix, JN_KIND_P, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
-			else panel_task<T, Fix, JN_KIND_P, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix);
+			if (diag) panel_task<T, Fix, JN_KIND_P, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			else panel_task<T, Fix, JN_KIND_P, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
 		}
 	}
 	__syncthreads();
 	/* add the touched blocks into the global accumulator (unpadded layout) */
 	for (uint32_t f = f0; f < f1; f++) {
-		const uint4 bk = __ldg(blocks + flush[f]);
+		const uint32_t so = __ldg(flush + 2 * f + 1);
+		const uint4 bk = __ldg(blocks + __ldg(flush + 2 * f));
 		const uint32_t Nn = bk.w, Ns = bk.w | 1u, n = bk.z * Nn;
 		for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
-			const uint32_t s = bk.y + (e / Nn) * Ns + e % Nn;
+			const uint32_t s = so + (e / Nn) * Ns + e % Nn;
 			const unsigned long long v = (unsigned long long)lo[s] | ((unsigned long long)hi[s] << 32);
 			if (v) atomicAdd(gacc + bk.x + e, v);
 		}
@@ -358,11 +365,16 @@ __global__ void jn_int_finalize_kernel(unsigned long long *__restrict__ gacc, do
 	}
 }
 
-/* the accumulator: two 32-bit words per padded state */
+/* a CTA's accumulator (two 32-bit words per padded state of the blocks it
+ * touches, at most `words`) and its block map (one word per block) */
+static size_t panel_smem_words(const jn_plan_t *p, int64_t words)
+{
+	return (size_t)((words ? words : 1) * 2 + p->nblocks) * sizeof(unsigned int);
+}
 static size_t panel_smem(const jn_plan_t *p, int f32)
 {
 	(void)f32;
-	return (size_t)(p->psmem_words ? p->psmem_words : 1) * 2 * sizeof(unsigned int);
+	return panel_smem_words(p, p->pcta_words);
 }
 
 /* ------------------------------------------------------------------ */
@@ -397,6 +409,34 @@ void jn_panels_release(jn_ctx *c)
 
 int jn_panels_fit(const jn_ctx *c, int f32) { return c->panel_grid > 0 && c->panel_per_sm[f32 ? 1 : 0] > 0; }
 
+/* Ask for the smallest shared-memory carveout that still holds the CTAs an
+ * SM runs: the rest of the SM's unified memory serves as L1, which caches x
+ * and the list entries for the product kernels.  The carveout is an
+ * attribute of the kernel, shared by every context of the process, so it
+ * only grows: the largest any context needs (occupancy queries run at the
+ * full carveout, see jn_panels_setup).  A hint: the runtime takes a larger
+ * carveout where a launch needs one. */
+static int g_carveout[2];
+static void set_carveout(jn_ctx *c)
+{
+	int max_smem = 0;
+	if (cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess ||
+	    max_smem <= 0) {
+		cudaGetLastError();
+		return;
+	}
+	const size_t smem = panel_smem(&c->plan, 1) + 1024;     /* and the runtime's per-CTA reserve */
+	for (int f32 = 0; f32 < 2; f32++) {
+		const int per = c->panel_per_sm[f32] > 0 ? c->panel_per_sm[f32] : 1;
+		int pct = (int)((100 * per * smem + max_smem - 1) / max_smem);
+		if (pct > 100) pct = 100;
+		if (pct > g_carveout[f32]) g_carveout[f32] = pct;
+		if (f32) cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[1]);
+		else cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[0]);
+	}
+	cudaGetLastError();
+}
+
 jn_status jn_panels_setup(jn_ctx *c)
 {
 	jn_plan_t *p = &c->plan;
@@ -410,8 +450,17 @@ jn_status jn_panels_setup(jn_ctx *c)
 	if (jn_panels_build(p, 1, JN_PANEL_ITER, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
 	for (int f32 = 0; f32 < 2; f32++) {
 		const size_t smem = panel_smem(p, f32);
-		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-				    : cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+		/* the occupancy query follows the carveout hint: ask at the full carveout */
+		if (f32) cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+		else cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+		/* the kernels' dynamic shared-memory limit is shared by every context of the
+		   process as well: it only grows */
+		static size_t g_smem_limit[2];
+		if (smem > g_smem_limit[f32]) g_smem_limit[f32] = smem;
+		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+							   (int)g_smem_limit[1])
+				    : cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+							   (int)g_smem_limit[0]);
 		if (e == cudaSuccess)
 			e = f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], jn_panel_kernel_i32, PANEL_THREADS, smem)
 				: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], jn_panel_kernel_fp64, PANEL_THREADS, smem);
@@ -432,7 +481,7 @@ jn_status jn_panels_setup(jn_ctx *c)
 	    (s = upload_n(&c->d_ptasks, p->ptasks, (size_t)p->nptasks * 4)) ||
 	    (s = upload_n(&c->d_pcta, p->pcta, (size_t)p->pgrid + 1)) ||
 	    (s = upload_n(&c->d_pflush_ptr, p->pflush_ptr, (size_t)p->pgrid + 1)) ||
-	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush)) ||
+	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush * 2)) ||
 	    (s = upload_n(&c->d_pblocks, p->pblocks, (size_t)p->nblocks * 4)) ||
 	    (s = upload_n(&c->d_pmeta, p->pmeta, (size_t)p->n_pmeta))) {
 		jn_panels_release(c);
@@ -454,6 +503,7 @@ jn_status jn_panels_setup(jn_ctx *c)
 		}
 	}
 	c->panel_grid = p->pgrid;
+	set_carveout(c);
 	return JN_OK;
 }
 
@@ -583,7 +633,7 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 		g.start = c->prof_ev[0];
 		g.end = c->prof_ev[3];
 	}
-	g.accumulate = accumulate; g.grid = c->panel_grid; g.words = (int)p->psmem_words; g.smem = panel_smem(p, f32);
+	g.accumulate = accumulate; g.grid = c->panel_grid; g.words = (int)p->pcta_words; g.smem = panel_smem(p, f32);
 	g.fin_grid = (int)((p->dim + 255) / 256);
 	if (g.fin_grid > 1024) g.fin_grid = 1024;
 	if (f32) {
@@ -663,12 +713,13 @@ static jn_status panel_schedule(jn_ctx *c, int iter, int per_sm)
 	if ((s = upload_n(&c->d_ptasks, p->ptasks, (size_t)p->nptasks * 4)) ||
 	    (s = upload_n(&c->d_pcta, p->pcta, (size_t)p->pgrid + 1)) ||
 	    (s = upload_n(&c->d_pflush_ptr, p->pflush_ptr, (size_t)p->pgrid + 1)) ||
-	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush))) {
+	    (s = upload_n(&c->d_pflush, p->pflush, (size_t)p->npflush * 2))) {
 		jn_panels_release(c);
 		return s;
 	}
 	c->panel_grid = p->pgrid;
 	c->panel_iter = iter;
+	set_carveout(c);
 	return JN_OK;
 }
 
@@ -884,10 +935,12 @@ jn_status jn_panels_partition_upload(jn_ctx *c, int grid, jn_panel_partition *pp
 	jn_status s = jn_panels_setup(c);
 	if (s) return s;
 	uint32_t *cta = NULL, *fptr = NULL, *flush = NULL;
-	int64_t nf = 0;
-	if (jn_panels_partition(&c->plan, grid, &cta, &fptr, &flush, &nf)) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	int64_t nf = 0, words = 0;
+	if (jn_panels_partition(&c->plan, grid, &cta, &fptr, &flush, &nf, &words))
+		return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	pp->words = (int)words;
 	if ((s = upload_n(&pp->cta, cta, (size_t)grid + 1)) || (s = upload_n(&pp->flush_ptr, fptr, (size_t)grid + 1)) ||
-	    (s = upload_n(&pp->flush, flush, (size_t)nf)))
+	    (s = upload_n(&pp->flush, flush, (size_t)nf * 2)))
 		jn_panels_partition_free(pp);
 	else
 		pp->grid = grid;
@@ -919,10 +972,11 @@ jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const u
 	if (p->nptasks) {
 		const FixInt32 fix = {};
 		const int grid = pp ? pp->grid : c->panel_grid;
-		jn_panel_kernel_i32<<<dim3(grid, B), PANEL_THREADS, panel_smem(p, 1), st>>>(
+		const int64_t words = pp ? pp->words : p->pcta_words;
+		jn_panel_kernel_i32<<<dim3(grid, B), PANEL_THREADS, panel_smem_words(p, words), st>>>(
 			(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, pp ? pp->cta : c->d_pcta,
 			pp ? pp->flush : c->d_pflush, pp ? pp->flush_ptr : c->d_pflush_ptr,
-			(const uint4 *)c->d_pblocks, c->d_pmeta, d_coef, xbuf, xbuf + p->dim, gacc, fix, (int)p->psmem_words,
+			(const uint4 *)c->d_pblocks, c->d_pmeta, d_coef, xbuf, xbuf + p->dim, gacc, fix, (int)words,
 			p->n_coef, 2 * p->dim, p->dim, d_active);
 	}
 	jn_int_finalize_batched_kernel<<<dim3(g, B), 256, 0, st>>>(gacc, y, y_ld, p->dim, ctrl, d_cmax, d_active);

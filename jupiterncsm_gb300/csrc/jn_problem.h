@@ -181,7 +181,7 @@ typedef struct {
 	int32_t out_off, in_off;        /* offsets of the output and input blocks */
 	int32_t Nn_out, Nn_in;
 	int32_t ncols, kind;    /* kind: JN_KIND_* | JN_PANEL_DIAG when input block == output block */
-	int32_t out_soff, in_soff;      /* the blocks' offsets in the shared-memory accumulator */
+	int32_t out_blk, in_blk;        /* the output and input blocks (a CTA maps them to its accumulator) */
 	int32_t nrows, instr;   /* rows; the evaluation-order index of the instruction */
 	int32_t Np_out, Np_in;  /* proton dimensions: strides of the blocks' transposed copy of x */
 } jn_panel_t;
@@ -224,10 +224,11 @@ typedef struct {
 	int npanels;       jn_panel_t *panels;
 	int64_t nptasks;   uint32_t *ptasks;   /* 4 words per warp task: panel, j0, j1, i0 | lanes per row << 24 */
 	int pgrid;         uint32_t *pcta;     /* pgrid + 1 task offsets: CTA b runs [pcta[b], pcta[b+1]) */
-	uint32_t *pflush_ptr;                   /* pgrid + 1 offsets into pflush */
-	int64_t npflush;   uint32_t *pflush;   /* the blocks a CTA touches (block indices) */
-	uint32_t *pblocks;                      /* per block: {offset in y, offset in the accumulator, Np, Nn} */
-	int64_t psmem_words;                    /* accumulator length: sum of Np * (Nn | 1) */
+	uint32_t *pflush_ptr;                   /* pgrid + 1 offsets (in pairs) into pflush */
+	int64_t npflush;   uint32_t *pflush;   /* the blocks a CTA touches: pairs {block, its offset in the CTA's accumulator} */
+	int64_t pcta_words;                     /* the largest CTA accumulator: sum of Np * (Nn | 1) over its blocks */
+	uint32_t *pblocks;                      /* per block: {offset in y, unused, Np, Nn} */
+	int64_t psmem_words;                    /* the whole vector's accumulator length: sum of Np * (Nn | 1) */
 	int64_t n_pmeta;   uint32_t *pmeta;
 	int64_t n_coef;                         /* coefficients of all panels */
 } jn_plan_t;
@@ -267,7 +268,7 @@ void jn_panels_free(jn_plan_t *plan);
 /* the CTA ranges and flush lists of the plan's tasks for a grid of `grid`
  * persistent CTAs (malloc'ed; the plan's own are those of plan->pgrid) */
 int jn_panels_partition(const jn_plan_t *plan, int grid, uint32_t **cta, uint32_t **flush_ptr, uint32_t **flush,
-			int64_t *nflush);
+			int64_t *nflush, int64_t *words);
 /* panel coefficients from matrix elements in the plan's layout: FP64 into c64
  * and/or FP32 into c32 (either may be NULL), n_coef values each */
 void jn_panels_coefficients(const jn_plan_t *plan, const double *me, double *c64, float *c32);

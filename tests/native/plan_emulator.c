@@ -279,8 +279,8 @@ static void panel_lane_model(const jn_plan_t *P, const jn_panel_t *pn, uint32_t 
 	const int MRi = rows_n ? 1 : pn->Nn_in, MCi = rows_n ? pn->Nn_in : 1;
 	const double scale = ldexp(1.0, S);
 	const int64_t bias = k > 0 ? (int64_t)1 << (k - 1) : 0;
-	/* the shared-memory accumulator holds each block with rows padded to Nn | 1 */
-	CHECK(pn->out_soff >= 0 && pn->in_soff >= 0 && pn->out_soff < P->psmem_words && pn->in_soff < P->psmem_words);
+	/* a CTA's shared-memory accumulator holds each block it touches with rows padded to Nn | 1 */
+	CHECK(pn->out_blk >= 0 && pn->in_blk >= 0 && pn->out_blk < P->nblocks && pn->in_blk < P->nblocks);
 	int sc, dc;
 	if (kind == JN_KIND_P) {
 		sc = dc = i;
@@ -309,10 +309,10 @@ static void panel_lane_model(const jn_plan_t *P, const jn_panel_t *pn, uint32_t 
 		const int64_t at_i = pn->in_off + (int64_t)sr * MRi + (int64_t)sc * MCi;
 		const int64_t at_o = pn->out_off + (int64_t)dr * MRo + (int64_t)dc * MCo;
 		CHECK(at_i >= 0 && at_i < P->dim && at_o >= 0 && at_o < P->dim);
-		/* the padded shared-memory positions stay inside the accumulator */
-		const int64_t so = pn->out_soff + (int64_t)(rows_n ? dc : dr) * (pn->Nn_out | 1) + (rows_n ? dr : dc);
-		const int64_t si = pn->in_soff + (int64_t)(rows_n ? sc : sr) * (pn->Nn_in | 1) + (rows_n ? sr : sc);
-		CHECK(so < P->psmem_words && si < P->psmem_words);
+		/* the padded shared-memory positions stay inside their blocks */
+		const int64_t so = (int64_t)(rows_n ? dc : dr) * (pn->Nn_out | 1) + (rows_n ? dr : dc);
+		const int64_t si = (int64_t)(rows_n ? sc : sr) * (pn->Nn_in | 1) + (rows_n ? sr : sc);
+		CHECK(so >= 0 && so < (int64_t)pn->Np_out * (pn->Nn_out | 1) && si >= 0 && si < (int64_t)pn->Np_in * (pn->Nn_in | 1));
 		if (f32) {
 			/* 32-bit fixed point: exact 64-bit product, rounded by the shift k */
 			const int64_t cv = ci[cidx];
@@ -363,6 +363,28 @@ int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
 	int64_t *acc = calloc(P->dim ? P->dim : 1, sizeof(int64_t));
 	/* every task once, every CTA's task range covering all of them */
 	if (P->pcta[0] != 0 || P->pcta[P->pgrid] != (uint32_t)P->nptasks) { emu_fail = 1; fprintf(stderr, "plan emulator: CTA ranges\n"); }
+	/* each CTA's accumulator: its blocks one after another within pcta_words, and
+	   every block a task of the CTA writes among them */
+	{
+		int64_t *at = malloc((P->nblocks ? P->nblocks : 1) * sizeof(int64_t));
+		for (int b = 0; b < P->pgrid && !emu_fail; b++) {
+			for (int q = 0; q < P->nblocks; q++) at[q] = -1;
+			int64_t next = 0;
+			for (uint32_t f = P->pflush_ptr[b]; f < P->pflush_ptr[b + 1] && !emu_fail; f++) {
+				const uint32_t blk = P->pflush[2 * f], off = P->pflush[2 * f + 1];
+				if (blk >= (uint32_t)P->nblocks || off != next || at[blk] >= 0) { emu_fail = 1; break; }
+				at[blk] = off;
+				next += P->blocks[blk].Np * (P->blocks[blk].Nn | 1);
+			}
+			if (next > P->pcta_words) emu_fail = 1;
+			for (uint32_t t = P->pcta[b]; t < P->pcta[b + 1] && !emu_fail; t++) {
+				const jn_panel_t *pn = &P->panels[P->ptasks[4 * t]];
+				if (at[pn->out_blk] < 0 || (!(pn->kind & JN_PANEL_DIAG) && at[pn->in_blk] < 0)) emu_fail = 1;
+			}
+			if (emu_fail) fprintf(stderr, "plan emulator: accumulator layout of CTA %d\n", b);
+		}
+		free(at);
+	}
 	for (int64_t t = 0; t < P->nptasks && !emu_fail; t++) {
 		const uint32_t *T = P->ptasks + 4 * t;
 		if (T[0] >= (uint32_t)P->npanels) { emu_fail = 1; break; }
