@@ -546,6 +546,9 @@ def main():
                     help="32: 32-bit fixed-point matrix elements and x with exact 64-bit sums (the headline); 64: FP64")
     ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
     ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solves/s leg")
+    ap.add_argument("--schedule", metavar="ROWS,CTAS",
+                    help="fix the panel schedule (rows per lane, CTAs per SM) instead of autotuning it, "
+                         "e.g. to profile the schedule a plain run chose")
     ap.add_argument("--leg", choices=["transform", "transform3"],
                     help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line)")
     args = ap.parse_args()
@@ -658,7 +661,12 @@ def main():
 
     # the product's schedule is chosen by the library's autotuner at the headline precision
     H.set_precision(args.precision)
-    tuning = H.autotune(trials=5)
+    if args.schedule:
+        rows, ctas = (int(v) for v in args.schedule.split(","))
+        H.set_panel_schedule(rows, ctas)
+        tuning = {"engine": 4, "rows_per_lane": rows, "ctas_per_sm": ctas, "ms": None, "candidates": 0, "fixed": True}
+    else:
+        tuning = H.autotune(trials=5)
     r64 = timed(64)
     r32 = timed(32)
     rel32 = float((r32["y"] - r64["y"]).abs().max() / r64["y"].abs().max())

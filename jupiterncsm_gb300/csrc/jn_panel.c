@@ -21,8 +21,9 @@
 void jn_panels_free(jn_plan_t *p)
 {
 	free(p->panels); free(p->ptasks); free(p->pcta); free(p->pflush_ptr); free(p->pflush); free(p->pmeta); free(p->pblocks);
+	free(p->pperm);
 	p->panels = NULL; p->ptasks = NULL; p->pcta = NULL; p->pflush_ptr = NULL; p->pflush = NULL; p->pmeta = NULL;
-	p->pblocks = NULL;
+	p->pblocks = NULL; p->pperm = NULL;
 	p->npanels = 0; p->nptasks = 0; p->pgrid = 0; p->npflush = 0; p->n_pmeta = 0; p->n_coef = 0; p->psmem_words = 0;
 }
 
@@ -48,6 +49,81 @@ static int tail_chunks(int ncols, int *i0, int *cw)
 		w -= p;
 	}
 	return n;
+}
+
+/* The order of a list's entries in every panel that uses the list.  A warp
+ * adds the contributions of up to 32 consecutive rows at once (narrow
+ * panels put several rows side by side), and each 32-column chunk of a wide
+ * panel is one set of entries.  Lanes whose contributions land on the same
+ * shared-memory word serialise, and in by-out order equal destinations sit
+ * next to each other.  So the entries are dealt out greedily: the
+ * destination with the most entries left among those not used in the last
+ * LIST_GAP - 1 positions (a repeat only when none is left), and within it the
+ * first entry whose source was not used in that window either (else the one
+ * used longest ago).  On the 4He Nmax 6 two- plus three-body workload this
+ * halves the shared-memory wavefronts of the product's atomics.  The sums
+ * are exact integers, so the order never changes a result bit.
+ *
+ * m: the list's packed entries (source | destination << 16) in by-out
+ * order; writes perm[k] = the by-out index of the entry at position k.
+ * last_src: 65 536 positions in the running count *clock, which advances
+ * past each list so that no state carries over. */
+#define LIST_GAP 32
+typedef struct { int64_t *last_src; int64_t clock; int32_t *run0, *left, *heap, *queue; int64_t *release; } list_order_t;
+
+static int heap_before(const int32_t *left, int32_t a, int32_t b) { return left[a] != left[b] ? left[a] > left[b] : a < b; }
+static void heap_push(int32_t *h, int *nh, const int32_t *left, int32_t r)
+{
+	int k = (*nh)++;
+	h[k] = r;
+	while (k > 0 && heap_before(left, h[k], h[(k - 1) / 2])) { int32_t t = h[k]; h[k] = h[(k - 1) / 2]; h[(k - 1) / 2] = t; k = (k - 1) / 2; }
+}
+static int32_t heap_pop(int32_t *h, int *nh, const int32_t *left)
+{
+	const int32_t top = h[0];
+	h[0] = h[--(*nh)];
+	for (int k = 0;;) {
+		int c = 2 * k + 1;
+		if (c >= *nh) break;
+		if (c + 1 < *nh && heap_before(left, h[c + 1], h[c])) c++;
+		if (!heap_before(left, h[c], h[k])) break;
+		int32_t t = h[k]; h[k] = h[c]; h[c] = t; k = c;
+	}
+	return top;
+}
+
+static void list_order(const uint32_t *m, int64_t n, uint32_t *perm, list_order_t *w)
+{
+	/* runs of equal destination; a run's entries not yet placed are kept in perm-sized scratch: run r owns
+	   [run0[r], run0[r] + left[r]) of `rest`, which starts as the by-out indices */
+	int32_t nr = 0;
+	for (int64_t e = 0; e < n; e++)
+		if (e == 0 || (m[e] >> 16) != (m[e - 1] >> 16)) w->run0[nr++] = (int32_t)e;
+	for (int32_t r = 0; r < nr; r++) w->left[r] = (int32_t)((r + 1 < nr ? w->run0[r + 1] : n) - w->run0[r]);
+	int32_t *rest = w->heap + nr;   /* n slots after the heap's nr */
+	for (int64_t e = 0; e < n; e++) rest[e] = (int32_t)e;
+	int nh = 0, q0 = 0, q1 = 0;
+	for (int32_t r = 0; r < nr; r++) heap_push(w->heap, &nh, w->left, r);
+	const int64_t base = w->clock;
+	for (int64_t k = 0; k < n; k++) {
+		const int64_t now = base + k;
+		while (q0 < q1 && w->release[q0] <= now) heap_push(w->heap, &nh, w->left, w->queue[q0++]);
+		const int32_t r = nh ? heap_pop(w->heap, &nh, w->left) : w->queue[q0++];
+		int32_t *s = rest + w->run0[r];
+		int best = 0;
+		for (int a = 0; a < w->left[r]; a++) {
+			const int64_t t = w->last_src[m[s[a]] & 0xffffu];
+			if (now - t >= LIST_GAP) { best = a; break; }
+			if (t < w->last_src[m[s[best]] & 0xffffu]) best = a;
+		}
+		const int32_t e = s[best];
+		memmove(s + best, s + best + 1, (size_t)(w->left[r] - best - 1) * sizeof(int32_t));
+		w->left[r]--;
+		perm[k] = (uint32_t)e;
+		w->last_src[m[e] & 0xffffu] = now;
+		if (w->left[r] > 0) { w->queue[q1] = r; w->release[q1++] = now + LIST_GAP; }
+	}
+	w->clock = base + n + LIST_GAP;
 }
 
 static double task_cost(const jn_plan_t *p, const uint32_t *T)
@@ -102,10 +178,32 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	}
 	if (p->n_pmeta > 0xffffffffll) ERR("index lists too long for the panel engine");
 	p->pmeta = malloc((p->n_pmeta ? p->n_pmeta : 1) * sizeof(uint32_t));
-	if (!p->pmeta) ERR("out of host memory");
-	for (int l = 0; l < p->nlists; l++) {
-		const jn_list_t *L = &p->lists[l];
-		for (int64_t e = 0; e < L->len; e++) p->pmeta[L->pmeta + e] = p->ent[2 * (L->ent_out + e)];
+	p->pperm = malloc((p->n_pmeta ? p->n_pmeta : 1) * sizeof(uint32_t));
+	if (!p->pmeta || !p->pperm) ERR("out of host memory");
+	{
+		int64_t lmax = 1;
+		for (int l = 0; l < p->nlists; l++) lmax = p->lists[l].len > lmax ? p->lists[l].len : lmax;
+		list_order_t w = {0};
+		uint32_t *bym = malloc((size_t)lmax * sizeof(uint32_t));
+		w.last_src = malloc(65536 * sizeof(int64_t));
+		w.run0 = malloc((size_t)lmax * sizeof(int32_t));
+		w.left = malloc((size_t)lmax * sizeof(int32_t));
+		w.heap = malloc((size_t)(2 * lmax) * sizeof(int32_t));
+		w.queue = malloc((size_t)lmax * sizeof(int32_t));
+		w.release = malloc((size_t)lmax * sizeof(int64_t));
+		const int ok = bym && w.last_src && w.run0 && w.left && w.heap && w.queue && w.release;
+		if (ok) {
+			for (int s = 0; s < 65536; s++) w.last_src[s] = -(int64_t)LIST_GAP;
+			w.clock = 0;
+			for (int l = 0; l < p->nlists; l++) {
+				const jn_list_t *L = &p->lists[l];
+				for (int64_t e = 0; e < L->len; e++) bym[e] = p->ent[2 * (L->ent_out + e)];
+				list_order(bym, L->len, p->pperm + L->pmeta, &w);
+				for (int64_t k = 0; k < L->len; k++) p->pmeta[L->pmeta + k] = bym[p->pperm[L->pmeta + k]];
+			}
+		}
+		free(bym); free(w.last_src); free(w.run0); free(w.left); free(w.heap); free(w.queue); free(w.release);
+		if (!ok) ERR("out of host memory");
 	}
 	/* panels */
 	order = malloc((p->ninstr ? p->ninstr : 1) * sizeof(int));
@@ -298,7 +396,8 @@ void jn_panels_coefficients(const jn_plan_t *p, const double *me, double *c64, f
 			for (int32_t j = 0; j < P->nrows; j++)
 				for (int32_t i = 0; i < P->ncols; i++) {
 					const int32_t ep = rows_n ? i : j, en = rows_n ? j : i;
-					const uint32_t mp = ent[2 * (Lp->ent_out + ep) + 1], mn = ent[2 * (Ln->ent_out + en) + 1];
+					const uint32_t mp = ent[2 * (Lp->ent_out + p->pperm[Lp->pmeta + ep]) + 1];
+					const uint32_t mn = ent[2 * (Ln->ent_out + p->pperm[Ln->pmeta + en]) + 1];
 					double v = m[(mn & 0x7fffffffu) + (int64_t)M->nd_n * (mp & 0x7fffffffu)];
 					if ((mp ^ mn) & 0x80000000u) v = -v;
 					const int64_t at = P->c_off + (int64_t)j * P->ncols + i;
@@ -308,7 +407,7 @@ void jn_panels_coefficients(const jn_plan_t *p, const double *me, double *c64, f
 		} else {
 			const jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
 			for (int64_t e = 0; e < L->len; e++) {
-				const uint32_t mi = ent[2 * (L->ent_out + e) + 1];
+				const uint32_t mi = ent[2 * (L->ent_out + p->pperm[L->pmeta + e]) + 1];
 				double v = m[mi & 0x7fffffffu];
 				/* single-species terms skip |M| < 1e-12 (matrix_vector_multiplication.c:52-53) */
 				if (fabs(v) < 1e-12) v = 0.0;
@@ -356,14 +455,15 @@ void jn_panels_gather_index(const jn_plan_t *p, uint32_t *gather)
 			for (int32_t j = 0; j < P->nrows; j++)
 				for (int32_t i = 0; i < P->ncols; i++) {
 					const int32_t ep = rows_n ? i : j, en = rows_n ? j : i;
-					const uint32_t mp = ent[2 * (Lp->ent_out + ep) + 1], mn = ent[2 * (Ln->ent_out + en) + 1];
+					const uint32_t mp = ent[2 * (Lp->ent_out + p->pperm[Lp->pmeta + ep]) + 1];
+					const uint32_t mn = ent[2 * (Ln->ent_out + p->pperm[Ln->pmeta + en]) + 1];
 					const uint64_t at = (uint64_t)M->offset + (mn & 0x7fffffffu) + M->nd_n * (mp & 0x7fffffffu);
 					gather[P->c_off + (int64_t)j * P->ncols + i] = (uint32_t)at | ((mp ^ mn) & 0x80000000u);
 				}
 		} else {
 			const jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
 			for (int64_t e = 0; e < L->len; e++) {
-				const uint32_t mi = ent[2 * (L->ent_out + e) + 1];
+				const uint32_t mi = ent[2 * (L->ent_out + p->pperm[L->pmeta + e]) + 1];
 				gather[P->c_off + e] = (uint32_t)(M->offset + (mi & 0x7fffffffu)) | (mi & 0x80000000u) | 0x40000000u;
 			}
 		}

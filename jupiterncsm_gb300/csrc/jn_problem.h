@@ -229,7 +229,8 @@ typedef struct {
 	int64_t pcta_words;                     /* the largest CTA accumulator: sum of Np * (Nn | 1) over its blocks */
 	uint32_t *pblocks;                      /* per block: {offset in y, unused, Np, Nn} */
 	int64_t psmem_words;                    /* the whole vector's accumulator length: sum of Np * (Nn | 1) */
-	int64_t n_pmeta;   uint32_t *pmeta;
+	int64_t n_pmeta;   uint32_t *pmeta;    /* each list's entries in panel order (list_order in jn_panel.c) */
+	uint32_t *pperm;                        /* per packed entry: its index in the list's by-out order */
 	int64_t n_coef;                         /* coefficients of all panels */
 } jn_plan_t;
 

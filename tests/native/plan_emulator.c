@@ -403,3 +403,67 @@ int emu_matvec4(void *h, const double *x, double *y, int accumulate, int f32)
 	free(acc); free(xi); free(c64); free(ci);
 	return emu_fail;
 }
+
+/* Shared-memory wavefronts of the panel kernel's atomics, warp instruction by
+ * warp instruction, under the plan's schedule: lanes whose words share a
+ * bank (32 banks of 4 bytes) serialise, the same word included.  out:
+ * {forward instructions, forward wavefronts, transpose instructions,
+ * transpose wavefronts}.  by_out != 0 counts them with every list in by-out
+ * order instead of the plan's panel order.  Returns 1 if pperm is not a
+ * permutation of some list or pmeta disagrees with it. */
+int emu_panel_wavefronts(void *h, int by_out, double *out)
+{
+	jn_plan_t *P = h;
+	char err[512];
+	if (!P->panels && jn_panels_build(P, 152 * 3, JN_PANEL_ITER, err, sizeof err)) return 1;
+	uint32_t *meta = malloc((P->n_pmeta ? P->n_pmeta : 1) * sizeof(uint32_t));
+	unsigned char *seen = calloc(P->n_pmeta ? P->n_pmeta : 1, 1);
+	int bad = 0;
+	for (int l = 0; l < P->nlists; l++) {
+		const jn_list_t *L = &P->lists[l];
+		for (int64_t k = 0; k < L->len; k++) {
+			const uint32_t e = P->pperm[L->pmeta + k];
+			if (e >= (uint32_t)L->len || seen[L->pmeta + e]) { bad = 1; break; }
+			seen[L->pmeta + e] = 1;
+			if (P->pmeta[L->pmeta + k] != P->ent[2 * (L->ent_out + e)]) bad = 1;
+			meta[L->pmeta + k] = by_out ? P->ent[2 * (L->ent_out + k)] : P->pmeta[L->pmeta + k];
+		}
+	}
+	int64_t *at = malloc((P->nblocks ? P->nblocks : 1) * sizeof(int64_t));
+	for (int q = 0; q < 4; q++) out[q] = 0;
+	for (int b = 0; b < P->pgrid && !bad; b++) {
+		for (uint32_t f = P->pflush_ptr[b]; f < P->pflush_ptr[b + 1]; f++) at[P->pflush[2 * f]] = P->pflush[2 * f + 1];
+		for (uint32_t t = P->pcta[b]; t < P->pcta[b + 1]; t++) {
+			const uint32_t *T = P->ptasks + 4 * t;
+			const jn_panel_t *pn = &P->panels[T[0]];
+			const int cw = (int)(T[3] >> 24), R = 32 / cw, i0 = (int)(T[3] & 0xffffffu);
+			const int kind = pn->kind & 7, diag = (pn->kind & JN_PANEL_DIAG) != 0;
+			const int rows_n = kind == JN_KIND_NP && (pn->kind & JN_PANEL_ROWS_N);
+			const int64_t so = at[pn->out_blk], si = at[pn->in_blk];
+			const int Po = pn->Nn_out | 1, Pi = pn->Nn_in | 1;
+			for (uint32_t g = 0; T[1] + g * R < T[2]; g++) {
+				int cnt[2][32] = {{0}};
+				for (int lane = 0; lane < 32; lane++) {
+					const int r = lane / cw, i = i0 + lane - r * cw;
+					const uint32_t j = T[1] + g * R + r;
+					if (r >= R || i >= pn->ncols || j >= T[2]) continue;
+					int sc, dc, sr, dr;
+					if (kind == JN_KIND_P) sc = dc = i;
+					else { const uint32_t m = meta[pn->col_meta + i]; sc = m & 0xffff; dc = m >> 16; }
+					if (kind == JN_KIND_N) sr = dr = (int)j;
+					else { const uint32_t m = meta[pn->row_meta + j]; sr = m & 0xffff; dr = m >> 16; }
+					cnt[0][(rows_n ? so + (int64_t)dc * Po + dr : so + (int64_t)dr * Po + dc) & 31]++;
+					cnt[1][(rows_n ? si + (int64_t)sc * Pi + sr : si + (int64_t)sr * Pi + sc) & 31]++;
+				}
+				for (int k = 0; k < 2 - diag; k++) {
+					int mx = 0;
+					for (int q = 0; q < 32; q++) mx = cnt[k][q] > mx ? cnt[k][q] : mx;
+					out[2 * k] += 1;
+					out[2 * k + 1] += mx;
+				}
+			}
+		}
+	}
+	free(meta); free(seen); free(at);
+	return bad;
+}

@@ -150,3 +150,22 @@ def test_panel_plan_model_matches_port(problem, name):
         assert L.emu_matvec4(h, x.ctypes.data, y.ctypes.data, 0, f32) == 0
         assert np.abs(y - want).max() <= tol * np.abs(want).max()
     L.emu_close(h)
+
+
+@pytest.mark.parametrize("name", ["he4_n4_2b", "he4_n2_3b", "li6_n2_3b"])
+def test_panel_list_order_spreads_atomics(problem, name):
+    """Each list's panel order is a permutation of its entries, and it keeps
+    equal destinations (and sources) apart: the product's shared-memory
+    atomics take fewer bank wavefronts than with the lists in by-out order."""
+    d, Z, N, *_ = problem(name)
+    L, h, err = open_plan(d, Z, N)
+    assert h, err
+    L.emu_panel_wavefronts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    got, ref = np.zeros(4), np.zeros(4)
+    assert L.emu_panel_wavefronts(h, 0, got.ctypes.data) == 0
+    assert L.emu_panel_wavefronts(h, 1, ref.ctypes.data) == 0
+    assert got[0] == ref[0] and got[2] == ref[2] and got[0] > 0
+    print(name, "wavefronts per atomic: forward %.2f -> %.2f, transpose %.2f -> %.2f"
+          % (ref[1] / ref[0], got[1] / got[0], ref[3] / max(ref[2], 1), got[3] / max(got[2], 1)))
+    assert got[1] + got[3] < 0.8 * (ref[1] + ref[3])
+    L.emu_close(h)
