@@ -61,6 +61,8 @@ struct jn_ctx {
 	int pint_sc, pint_k;            /* coefficient exponent and product shift of the 32-bit path */
 	int panel_grid;                 /* persistent CTAs; 0 until set up */
 	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
+	int panel_xs_limit;             /* dynamic shared memory the 32-bit kernel may take with x staged in it (0: never) */
+	int smem_per_sm;                /* shared memory of an SM, bytes */
 	int panel_iter;                 /* rows a lane walks per panel task */
 	uint32_t *d_pgather;            /* per coefficient: its matrix element | sign << 31 | skip << 30 (batched) */
 	uint16_t *d_pelem;              /* per state: its basis block (the prep kernel's transposed copy) */

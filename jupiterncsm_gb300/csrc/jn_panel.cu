@@ -14,11 +14,12 @@
  * (evict-first) loads, and the index lists only as 4-byte packed
  * (source, destination) pairs.  A warp task spreads up to 32 columns of a
  * panel over its lanes (and floor(32 / columns) rows side by side when a
- * panel is narrow) and walks rows, with the row entries and coefficients of eight
- * rows in flight per lane; the x gathers hit L1.  Each CTA holds the whole
- * of y as 64-bit fixed-point integers in shared memory, with block rows
- * padded to an odd length so that a warp walking a column touches 32
- * different banks: every contribution is one rounding of c x 2^S to an
+ * panel is narrow) and walks rows, with the row entries and coefficients of four
+ * rows in flight per lane.  Each CTA holds the blocks of y it touches as
+ * 64-bit fixed-point integers in shared memory (the 32-bit product also
+ * holds x there, on the same blocks), with block rows padded to an odd
+ * length so that a warp walking a column touches 32 different banks: every
+ * contribution is one rounding of c x 2^S to an
  * integer, added as two 32-bit shared atomics with carry (the list walks are
  * about one entry long, so there is nothing to sum before rounding).  Integer addition is exact and
  * associative, so the result is bit-identical whatever the order in which
@@ -60,12 +61,51 @@ __device__ __forceinline__ void add_contribution(unsigned int *lo, unsigned int 
 	add_fixed32(lo, hi, i, v);
 }
 
-template <typename T, typename Fix, int KIND, bool DIAG>
+/* exponent Sx of the 32-bit fixed-point x: |x| 2^Sx < 2^30 for the bound max|x| in xmax_bits */
+__device__ __forceinline__ int x_exponent(unsigned int xmax_bits)
+{
+	if (!(xmax_bits & 0x7fffffffu)) return 0;
+	const int ex = (int)((xmax_bits >> 23) & 0xff) - 126;   /* xmax < 2^ex */
+	const int Sx = 30 - ex;
+	return Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
+}
+
+/* round-half-even of v 2^Sx as a 32-bit integer, from the bits of v: the
+ * same value as __double2int_rn(v * 2^Sx) for finite v whose scaled value
+ * is below 2^31 (the scale guarantees it), without an FP64 instruction.
+ * v = m 2^(e - 1075) with m the significand (implicit bit included, or the
+ * subnormal's fraction with e = 1). */
+__device__ __forceinline__ int fixed32_bits(double v, int Sx)
+{
+	const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+	const int ex = (int)((u >> 52) & 0x7ff);
+	if (ex == 0x7ff) return __double2int_rn(v * ldexp(1.0, Sx));     /* inf, nan: as the FP64 conversion */
+	unsigned long long m = u & 0xfffffffffffffull;
+	int sh = Sx - 1075;
+	if (ex) { m |= 1ull << 52; sh += ex; } else { sh += 1; }
+	unsigned long long q;
+	if (sh >= 0) {
+		q = m << sh;
+	} else {
+		const int k = -sh;
+		if (k > 63) {
+			q = 0;
+		} else {
+			q = m >> k;
+			const unsigned long long rem = m & ((1ull << k) - 1), half = 1ull << (k - 1);
+			if (rem > half || (rem == half && (q & 1))) q++;
+		}
+	}
+	const int r = (int)q;
+	return (u >> 63) ? -r : r;
+}
+
+template <typename T, typename Fix, int KIND, bool DIAG, bool XS>
 __device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const uint4 pc, const uint4 pd, uint32_t j0,
 					   uint32_t j1, int R, int r, int i, unsigned int *__restrict__ lo,
 					   unsigned int *__restrict__ hi, const T *__restrict__ x, const T *__restrict__ xt,
 					   const T *__restrict__ coef, const uint32_t *__restrict__ meta, const Fix fix,
-					   int out_soff, int in_soff)
+					   int out_soff, int in_soff, const T *__restrict__ xs)
 {
 	const int64_t c_off = (int64_t)pa.x | ((int64_t)pa.y << 32);
 	const uint32_t row_meta = pa.z, col_meta = pa.w;
@@ -115,13 +155,16 @@ __device__ __forceinline__ void panel_task(const uint4 pa, const uint4 pb, const
 		for (int u = 0; u < PANEL_UNROLL; u++) {
 			if (j + u * R >= j1) break;
 			const int sr = (int)(mr[u] & 0xffffu), dr = (int)(mr[u] >> 16);
-			add_contribution(lo, hi, ao_base + dr * SRo, fix(cv[u], __ldg(xi_base + sr * MRi)));
-			if (!DIAG) add_contribution(lo, hi, ai_base + sr * SRi, fix(cv[u], __ldg(xo_base + dr * MRo)));
+			/* x staged in shared memory sits at the accumulator's positions: x of the input
+			   element where the transpose adds, x of the output element where the forward adds */
+			const int ao = ao_base + dr * SRo, ai = ai_base + sr * SRi;
+			add_contribution(lo, hi, ao, fix(cv[u], XS ? xs[ai] : __ldg(xi_base + sr * MRi)));
+			if (!DIAG) add_contribution(lo, hi, ai, fix(cv[u], XS ? xs[ao] : __ldg(xo_base + dr * MRo)));
 		}
 	}
 }
 
-template <typename T, typename Fix>
+template <typename T, typename Fix, bool XS>
 __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, const uint4 *__restrict__ tasks,
 					      const uint32_t *__restrict__ cta_ptr, const uint32_t *__restrict__ flush,
 					      const uint32_t *__restrict__ flush_ptr, const uint4 *__restrict__ blocks,
@@ -130,10 +173,13 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 					      unsigned long long *__restrict__ gacc, const Fix fix, int words)
 {
 	/* the CTA's accumulator holds only the blocks it touches (flush pairs
-	   {block, offset}); bmap[block] is the block's offset in it */
+	   {block, offset}); bmap[block] is the block's offset in it.  With XS,
+	   x of those blocks follows in the same padded layout (a CTA reads x
+	   only on the blocks it adds into). */
 	extern __shared__ unsigned int sacc[];
 	__shared__ unsigned int next_task;
-	unsigned int *lo = sacc, *hi = sacc + words, *bmap = sacc + 2 * words;
+	unsigned int *lo = sacc, *hi = sacc + words, *bmap = sacc + (XS ? 3 : 2) * words;
+	T *xs = XS ? (T *)(sacc + 2 * words) : NULL;
 	const int lane = threadIdx.x & 31;
 	const uint32_t f0 = flush_ptr[blockIdx.x], f1 = flush_ptr[blockIdx.x + 1];
 	/* clear the blocks this CTA touches (padded rows) */
@@ -145,6 +191,10 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 		for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
 			lo[so + e] = 0u;
 			hi[so + e] = 0u;
+			if (XS) {
+				const uint32_t Ns = bk.w | 1u, row = e / Ns, col = e - row * Ns;
+				xs[so + e] = col < bk.w ? __ldg(x + bk.x + row * bk.w + col) : (T)0;
+			}
 		}
 	}
 	if (threadIdx.x == 0) next_task = 0;
@@ -166,14 +216,14 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 		const bool diag = (pc.y & JN_PANEL_DIAG) != 0;
 		const int so = (int)bmap[pc.z], si = (int)bmap[pc.w];
 		if (kind == JN_KIND_NP) {
-			if (diag) panel_task<T, Fix, JN_KIND_NP, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
-			else panel_task<T, Fix, JN_KIND_NP, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			if (diag) panel_task<T, Fix, JN_KIND_NP, true, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
+			else panel_task<T, Fix, JN_KIND_NP, false, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
 		} else if (kind == JN_KIND_N) {
-			if (diag) panel_task<T, Fix, JN_KIND_N, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
-			else panel_task<T, Fix, JN_KIND_N, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			if (diag) panel_task<T, Fix, JN_KIND_N, true, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
+			else panel_task<T, Fix, JN_KIND_N, false, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
 		} else {
-			if (diag) panel_task<T, Fix, JN_KIND_P, true>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
-			else panel_task<T, Fix, JN_KIND_P, false>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si);
+			if (diag) panel_task<T, Fix, JN_KIND_P, true, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
+			else panel_task<T, Fix, JN_KIND_P, false, XS>(pa, pb, pc, pd, tk.y, tk.z, R, r, i, lo, hi, x, xt, coef, meta, fix, so, si, xs);
 		}
 	}
 	__syncthreads();
@@ -193,7 +243,9 @@ __device__ __forceinline__ void jn_panel_body(const uint4 *__restrict__ panels, 
 /* the 32-bit product: coefficients and x are 32-bit fixed-point integers.
  * Batched products (many Hamiltonians on one set of lists) run instance
  * blockIdx.y with its own coefficients, x and accumulator at the given
- * strides; instances with active[i] == 0 are skipped. */
+ * strides; instances with active[i] == 0 are skipped.  XS: x staged in
+ * shared memory (one more word per state) instead of gathered through L1. */
+template <bool XS>
 __global__ void __launch_bounds__(PANEL_THREADS, 3) jn_panel_kernel_i32(const uint4 *__restrict__ panels,
 								     const uint4 *__restrict__ tasks,
 								     const uint32_t *__restrict__ cta_ptr,
@@ -208,8 +260,8 @@ __global__ void __launch_bounds__(PANEL_THREADS, 3) jn_panel_kernel_i32(const ui
 {
 	const int inst = blockIdx.y;
 	if (active && !active[inst]) return;
-	jn_panel_body<int, FixInt32>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef + inst * coef_ld,
-				     x + inst * x_ld, xt + inst * x_ld, gacc + inst * acc_ld, fix, words);
+	jn_panel_body<int, FixInt32, XS>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef + inst * coef_ld,
+					 x + inst * x_ld, xt + inst * x_ld, gacc + inst * acc_ld, fix, words);
 }
 
 /* the FP64 product: the fixed-point scale 2^S comes from max|x| on the device */
@@ -226,48 +278,11 @@ __global__ void __launch_bounds__(PANEL_THREADS) jn_panel_kernel_fp64(const uint
 								      int words)
 {
 	const FixFp64 fix = { ldexp(1.0, fixed_exponent(*xmax_bits, abs_bound)) };
-	jn_panel_body<double, FixFp64>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef, x, xt, gacc, fix,
+	jn_panel_body<double, FixFp64, false>(panels, tasks, cta_ptr, flush, flush_ptr, blocks, meta, coef, x, xt, gacc, fix,
 					      words);
 }
 
-/* exponent Sx of the 32-bit fixed-point x: |x| 2^Sx < 2^30 for the bound max|x| in xmax_bits */
-__device__ __forceinline__ int x_exponent(unsigned int xmax_bits)
-{
-	if (!(xmax_bits & 0x7fffffffu)) return 0;
-	const int ex = (int)((xmax_bits >> 23) & 0xff) - 126;   /* xmax < 2^ex */
-	const int Sx = 30 - ex;
-	return Sx < -900 ? -900 : (Sx > 900 ? 900 : Sx);
-}
 
-/* round-half-even of v 2^Sx as a 32-bit integer, from the bits of v: the
- * same value as __double2int_rn(v * 2^Sx) for finite v whose scaled value
- * is below 2^31 (the scale guarantees it), without an FP64 instruction.
- * v = m 2^(e - 1075) with m the significand (implicit bit included, or the
- * subnormal's fraction with e = 1). */
-__device__ __forceinline__ int fixed32_bits(double v, int Sx)
-{
-	const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-	const int ex = (int)((u >> 52) & 0x7ff);
-	if (ex == 0x7ff) return __double2int_rn(v * ldexp(1.0, Sx));     /* inf, nan: as the FP64 conversion */
-	unsigned long long m = u & 0xfffffffffffffull;
-	int sh = Sx - 1075;
-	if (ex) { m |= 1ull << 52; sh += ex; } else { sh += 1; }
-	unsigned long long q;
-	if (sh >= 0) {
-		q = m << sh;
-	} else {
-		const int k = -sh;
-		if (k > 63) {
-			q = 0;
-		} else {
-			q = m >> k;
-			const unsigned long long rem = m & ((1ull << k) - 1), half = 1ull << (k - 1);
-			if (rem > half || (rem == half && (q & 1))) q++;
-		}
-	}
-	const int r = (int)q;
-	return (u >> 63) ? -r : r;
-}
 
 /* One cluster of PREP_CTAS CTAs: max|x| into ctrl[0] (with the FP32 round-up
  * margin of the other engines' scale), then the panel kernels' copies of x:
@@ -366,16 +381,21 @@ __global__ void jn_int_finalize_kernel(unsigned long long *__restrict__ gacc, do
 }
 
 /* a CTA's accumulator (two 32-bit words per padded state of the blocks it
- * touches, at most `words`) and its block map (one word per block) */
-static size_t panel_smem_words(const jn_plan_t *p, int64_t words)
+ * touches, at most `words`), with xs the staged 32-bit x (one word more),
+ * and its block map (one word per block) */
+static size_t panel_smem_words(const jn_plan_t *p, int64_t words, int xs)
 {
-	return (size_t)((words ? words : 1) * 2 + p->nblocks) * sizeof(unsigned int);
+	return (size_t)((words ? words : 1) * (xs ? 3 : 2) + p->nblocks) * sizeof(unsigned int);
 }
-static size_t panel_smem(const jn_plan_t *p, int f32)
+/* The 32-bit kernel stages x in shared memory when its CTAs, `per` to an SM,
+ * still fit; else it gathers x through L1. */
+static int panel_use_xs(const jn_ctx *c, int64_t words, int per)
 {
-	(void)f32;
-	return panel_smem_words(p, p->pcta_words);
+	const size_t s = panel_smem_words(&c->plan, words, 1);
+	return c->panel_xs_limit > 0 && s <= (size_t)c->panel_xs_limit &&
+	       (size_t)(per > 0 ? per : 1) * (s + 1024) <= (size_t)c->smem_per_sm;
 }
+static int panel_per_sm_of(const jn_ctx *c, int grid) { return c->num_sms > 0 ? (grid + c->num_sms - 1) / c->num_sms : 1; }
 
 /* ------------------------------------------------------------------ */
 template <typename T>
@@ -416,23 +436,22 @@ int jn_panels_fit(const jn_ctx *c, int f32) { return c->panel_grid > 0 && c->pan
  * only grows: the largest any context needs (occupancy queries run at the
  * full carveout, see jn_panels_setup).  A hint: the runtime takes a larger
  * carveout where a launch needs one. */
-static int g_carveout[2];
+static int g_carveout[3];
 static void set_carveout(jn_ctx *c)
 {
-	int max_smem = 0;
-	if (cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess ||
-	    max_smem <= 0) {
-		cudaGetLastError();
-		return;
-	}
-	const size_t smem = panel_smem(&c->plan, 1) + 1024;     /* and the runtime's per-CTA reserve */
-	for (int f32 = 0; f32 < 2; f32++) {
-		const int per = c->panel_per_sm[f32] > 0 ? c->panel_per_sm[f32] : 1;
+	const int max_smem = c->smem_per_sm;
+	if (max_smem <= 0) return;
+	const int per = panel_per_sm_of(c, c->panel_grid);
+	/* [0] FP64, [1] 32-bit with x through L1, [2] 32-bit with x in shared memory */
+	for (int v = 0; v < 3; v++) {
+		if (v == 2 && !panel_use_xs(c, c->plan.pcta_words, per)) continue;
+		const size_t smem = panel_smem_words(&c->plan, c->plan.pcta_words, v == 2) + 1024;   /* and the runtime's per-CTA reserve */
 		int pct = (int)((100 * per * smem + max_smem - 1) / max_smem);
 		if (pct > 100) pct = 100;
-		if (pct > g_carveout[f32]) g_carveout[f32] = pct;
-		if (f32) cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[1]);
-		else cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[0]);
+		if (pct > g_carveout[v]) g_carveout[v] = pct;
+		if (v == 0) cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[0]);
+		else if (v == 1) cudaFuncSetAttribute(jn_panel_kernel_i32<false>, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[1]);
+		else cudaFuncSetAttribute(jn_panel_kernel_i32<true>, cudaFuncAttributePreferredSharedMemoryCarveout, g_carveout[2]);
 	}
 	cudaGetLastError();
 }
@@ -449,20 +468,20 @@ jn_status jn_panels_setup(jn_ctx *c)
 	/* the accumulator layout does not depend on the grid: plan once to size it */
 	if (jn_panels_build(p, 1, JN_PANEL_ITER, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
 	for (int f32 = 0; f32 < 2; f32++) {
-		const size_t smem = panel_smem(p, f32);
+		const size_t smem = panel_smem_words(p, p->pcta_words, 0);
 		/* the occupancy query follows the carveout hint: ask at the full carveout */
-		if (f32) cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+		if (f32) cudaFuncSetAttribute(jn_panel_kernel_i32<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 		else cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 		/* the kernels' dynamic shared-memory limit is shared by every context of the
 		   process as well: it only grows */
 		static size_t g_smem_limit[2];
 		if (smem > g_smem_limit[f32]) g_smem_limit[f32] = smem;
-		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		cudaError_t e = f32 ? cudaFuncSetAttribute(jn_panel_kernel_i32<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 							   (int)g_smem_limit[1])
 				    : cudaFuncSetAttribute(jn_panel_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
 							   (int)g_smem_limit[0]);
 		if (e == cudaSuccess)
-			e = f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], jn_panel_kernel_i32, PANEL_THREADS, smem)
+			e = f32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], jn_panel_kernel_i32<false>, PANEL_THREADS, smem)
 				: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], jn_panel_kernel_fp64, PANEL_THREADS, smem);
 		if (e != cudaSuccess) {
 			per[f32] = 0;
@@ -472,6 +491,25 @@ jn_status jn_panels_setup(jn_ctx *c)
 	if (per[1] < 1) return jn_fail(JN_ERR_INVALID, "the panel kernel does not fit on an SM for dimension %lld", (long long)p->dim);
 	c->panel_per_sm[0] = per[0];
 	c->panel_per_sm[1] = per[1];
+	/* the 32-bit kernel with x in shared memory: allowed up to the whole
+	   vector's need (the grid-1 plan above), within the per-CTA maximum;
+	   each launch takes it where its CTAs still fit (panel_use_xs) */
+	{
+		int optin = 0, smsm = 0;
+		if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device) != cudaSuccess ||
+		    cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device) != cudaSuccess)
+			optin = smsm = 0;
+		c->smem_per_sm = smsm;
+		size_t want = panel_smem_words(p, p->pcta_words, 1);
+		if (want > (size_t)optin) want = (size_t)optin;
+		static size_t g_xs_limit;
+		if (want > g_xs_limit) g_xs_limit = want;
+		c->panel_xs_limit = 0;
+		if (g_xs_limit > 0 && cudaFuncSetAttribute(jn_panel_kernel_i32<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+							   (int)g_xs_limit) == cudaSuccess)
+			c->panel_xs_limit = (int)g_xs_limit;
+		cudaGetLastError();
+	}
 	/* the task split is the same for every grid; CTAs take contiguous runs of the FP32 grid */
 	if (jn_panels_build(p, c->num_sms * per[1], JN_PANEL_ITER, err, sizeof err))
 		return jn_fail(JN_ERR_NOMEM, "panel plan: %s", err);
@@ -549,7 +587,7 @@ typedef struct {
 	int64_t dim;
 	double abs_bound;
 	size_t smem;
-	int f32, accumulate, grid, words, kshift, fin_grid;
+	int f32, xs, accumulate, grid, words, kshift, fin_grid;
 } panel_sig_t;
 
 struct jn_product_graph {
@@ -584,7 +622,7 @@ static void panel_launch(const panel_sig_t *g, int has_tasks, int capturing)
 	if (has_tasks) {
 		if (g->f32) {
 			const FixInt32 fix = {};
-			jn_panel_kernel_i32<<<g->grid, PANEL_THREADS, g->smem, st>>>(
+			(g->xs ? jn_panel_kernel_i32<true> : jn_panel_kernel_i32<false>)<<<g->grid, PANEL_THREADS, g->smem, st>>>(
 				(const uint4 *)g->panels, (const uint4 *)g->tasks, (const uint32_t *)g->cta, (const uint32_t *)g->flush,
 				(const uint32_t *)g->flush_ptr, blocks, (const uint32_t *)g->meta, (const int *)g->coef,
 				(const int *)g->xi, (const int *)g->xt, (unsigned long long *)g->gacc, fix, g->words, 0, 0, 0, NULL);
@@ -633,7 +671,9 @@ jn_status jn_enqueue_panels(jn_ctx *c, const double *d_x, double *d_y, int accum
 		g.start = c->prof_ev[0];
 		g.end = c->prof_ev[3];
 	}
-	g.accumulate = accumulate; g.grid = c->panel_grid; g.words = (int)p->pcta_words; g.smem = panel_smem(p, f32);
+	g.accumulate = accumulate; g.grid = c->panel_grid; g.words = (int)p->pcta_words;
+	g.xs = f32 && panel_use_xs(c, p->pcta_words, panel_per_sm_of(c, c->panel_grid));
+	g.smem = panel_smem_words(p, p->pcta_words, g.xs);
 	g.fin_grid = (int)((p->dim + 255) / 256);
 	if (g.fin_grid > 1024) g.fin_grid = 1024;
 	if (f32) {
@@ -973,7 +1013,9 @@ jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const u
 		const FixInt32 fix = {};
 		const int grid = pp ? pp->grid : c->panel_grid;
 		const int64_t words = pp ? pp->words : p->pcta_words;
-		jn_panel_kernel_i32<<<dim3(grid, B), PANEL_THREADS, panel_smem_words(p, words), st>>>(
+		const int xs = panel_use_xs(c, words, panel_per_sm_of(c, grid));
+		(xs ? jn_panel_kernel_i32<true> : jn_panel_kernel_i32<false>)<<<dim3(grid, B), PANEL_THREADS,
+									      panel_smem_words(p, words, xs), st>>>(
 			(const uint4 *)c->d_panels, (const uint4 *)c->d_ptasks, pp ? pp->cta : c->d_pcta,
 			pp ? pp->flush : c->d_pflush, pp ? pp->flush_ptr : c->d_pflush_ptr,
 			(const uint4 *)c->d_pblocks, c->d_pmeta, d_coef, xbuf, xbuf + p->dim, gacc, fix, (int)words,
