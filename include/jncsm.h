@@ -157,7 +157,8 @@ jn_status jn_set_engine(jn_ctx *ctx, int engine);
  * problem and precision: for the panel engine, rows per lane per warp task
  * (8 ... 128) x persistent CTAs per SM; with tune_engine also the
  * block-tile engine.  The fastest (median of `trials` CUDA-event timings of
- * the product kernel, caches warm) is installed.  The panel engine's
+ * the product kernel, each after a write of twice the L2 size, so that the
+ * product's data streams from HBM) is installed.  The panel engine's
  * schedule never changes a result bit (each contribution is rounded on its
  * own); switching engines changes results at the 1e-15 level, so
  * tune_engine = 0 keeps them bit-identical to the untuned context.  No

@@ -19,9 +19,9 @@
  * 64-bit fixed-point integers in shared memory (the 32-bit product also
  * holds x there, on the same blocks), with block rows padded to an odd
  * length so that a warp walking a column touches 32 different banks: every
- * contribution is one rounding of c x 2^S to an
- * integer, added as two 32-bit shared atomics with carry (the list walks are
- * about one entry long, so there is nothing to sum before rounding).  Integer addition is exact and
+ * contribution is one rounding of c x 2^S to an integer (each has its own
+ * coefficient), added as a 32-bit shared atomic whose rare carry goes to the
+ * high word.  Integer addition is exact and
  * associative, so the result is bit-identical whatever the order in which
  * warps and CTAs run.  Persistent CTAs take contiguous runs of tasks that
  * touch few blocks, and at the end add only the touched ranges into the
@@ -770,13 +770,16 @@ extern "C" jn_status jn_set_panel_schedule(jn_ctx *c, int rows_per_lane, int cta
 	return s ? s : panel_schedule(c, rows_per_lane, ctas_per_sm);
 }
 
-/* median CUDA-event time of the product kernel over `trials` products (after one warm-up) */
-static jn_status time_product(jn_ctx *c, int trials, float *ms)
+/* median CUDA-event time of the product kernel over `trials` products (after
+ * one warm-up), each product after a write of `flush_bytes` at `flush` (when
+ * not NULL) that leaves L2 holding none of the product's data */
+static jn_status time_product(jn_ctx *c, int trials, float *ms, void *flush, size_t flush_bytes)
 {
 	float t[64];
 	if (trials > 64) trials = 64;
 	for (int k = -1; k < trials; k++) {
 		float m[2];
+		if (flush) CUDA_TRY(cudaMemsetAsync(flush, k & 0xff, flush_bytes, c->stream));
 		jn_status s = jn_matvec_profile(c, c->d_x, c->d_y, 0, m);
 		if (s) return s;
 		if (k >= 0) t[k] = m[0];
@@ -793,9 +796,32 @@ __global__ void jn_tune_x_kernel(double *x, int64_t n)
 		x[i] = 1.0 + 0.5 * sin(0.37 * (double)i);
 }
 
+static jn_status autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out, void *flush, size_t flush_bytes);
+
+/* The candidates are timed with L2 flushed before every product: the
+ * schedule that is fastest with the coefficients resident in L2 (they fit
+ * there for small bases) can be a slow one when they stream from HBM. */
 extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out)
 {
 	if (!c || !out) return jn_fail(JN_ERR_INVALID, "null argument");
+	int l2 = 0;
+	void *flush = NULL;
+	size_t bytes = 0;
+	if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device) == cudaSuccess && l2 > 0) {
+		bytes = 2 * (size_t)l2;
+		if (cudaMalloc(&flush, bytes) != cudaSuccess) flush = NULL;
+	}
+	cudaGetLastError();
+	const jn_status s = autotune(c, trials, tune_engine, out, flush, bytes);
+	if (flush) {
+		cudaStreamSynchronize(c->stream);
+		cudaFree(flush);
+	}
+	return s;
+}
+
+static jn_status autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out, void *flush, size_t flush_bytes)
+{
 	if (trials < 1) trials = 5;
 	memset(out, 0, sizeof *out);
 	const jn_plan_t *p = &c->plan;
@@ -814,7 +840,7 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 			for (int per = 1; per <= maxper; per++) {
 				float ms;
 				jn_status s = panel_schedule(c, iters[a], per);
-				if (!s) s = time_product(c, trials, &ms);
+				if (!s) s = time_product(c, trials, &ms, flush, flush_bytes);
 				if (s) { c->engine = engine0; return s; }
 				out->candidates++;
 				if (ms < best) { best = ms; best_engine = 4; best_iter = iters[a]; best_per = per; }
@@ -823,7 +849,7 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 	if (tune_engine || engine0 != 4) {
 		float ms;
 		c->engine = 3;
-		jn_status s = time_product(c, trials, &ms);
+		jn_status s = time_product(c, trials, &ms, flush, flush_bytes);
 		if (s) { c->engine = engine0; return s; }
 		out->candidates++;
 		if (ms < best) { best = ms; best_engine = 3; }
