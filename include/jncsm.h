@@ -158,7 +158,10 @@ jn_status jn_set_engine(jn_ctx *ctx, int engine);
  * (8 ... 128) x persistent CTAs per SM; with tune_engine also the
  * block-tile engine.  The fastest (median of `trials` CUDA-event timings of
  * the product kernel, each after a write of twice the L2 size, so that the
- * product's data streams from HBM) is installed.  The panel engine's
+ * product's data streams from HBM) is installed.  The panel schedule is
+ * tuned at both precisions (when the FP64 kernel fits): `tuning` reports the
+ * context's own, and jn_set_precision installs the other's when the
+ * precision changes.  jn_set_panel_schedule sets one schedule for both.  The panel engine's
  * schedule never changes a result bit (each contribution is rounded on its
  * own); switching engines changes results at the 1e-15 level, so
  * tune_engine = 0 keeps them bit-identical to the untuned context.  No

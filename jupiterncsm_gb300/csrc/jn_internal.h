@@ -62,6 +62,7 @@ struct jn_ctx {
 	int panel_grid;                 /* persistent CTAs; 0 until set up */
 	int panel_per_sm[2];            /* CTAs per SM of the FP64 [0] and FP32 [1] panel kernels (0: does not fit) */
 	int panel_xs_limit;             /* dynamic shared memory the 32-bit kernel may take with x staged in it (0: never) */
+	int tuned_iter[2], tuned_per[2]; /* the autotuner's panel schedule for FP64 [0] and 32-bit [1] (0: none) */
 	int smem_per_sm;                /* shared memory of an SM, bytes */
 	int panel_iter;                 /* rows a lane walks per panel task */
 	uint32_t *d_pgather;            /* per coefficient: its matrix element | sign << 31 | skip << 30 (batched) */
@@ -74,6 +75,8 @@ struct jn_ctx {
 
 /* drop the cached product graphs (before any product buffer is freed) */
 void jn_product_graphs_clear(jn_ctx *c);
+/* install the autotuner's panel schedule for the context's precision, if it has one */
+jn_status jn_panels_apply_tuned(jn_ctx *c);
 
 /* enqueue y (+)= H x on stream st */
 jn_status jn_launch_matvec(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st);

@@ -792,7 +792,7 @@ extern "C" jn_status jn_set_precision(jn_ctx *c, int precision)
 		if (s) return s;
 	}
 	c->precision = precision;
-	return JN_OK;
+	return jn_panels_apply_tuned(c);
 }
 
 extern "C" jn_status jn_matvec_device(jn_ctx *c, const double *d_x, double *d_y, int accumulate, void *stream)

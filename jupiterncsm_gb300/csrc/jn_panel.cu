@@ -767,7 +767,17 @@ extern "C" jn_status jn_set_panel_schedule(jn_ctx *c, int rows_per_lane, int cta
 {
 	if (!c) return jn_fail(JN_ERR_INVALID, "null argument");
 	jn_status s = jn_panels_setup(c);
+	/* an explicit schedule holds at both precisions */
+	c->tuned_iter[0] = c->tuned_iter[1] = 0;
 	return s ? s : panel_schedule(c, rows_per_lane, ctas_per_sm);
+}
+
+jn_status jn_panels_apply_tuned(jn_ctx *c)
+{
+	const int f32 = c->precision == 32;
+	const int it = c->tuned_iter[f32], per = c->tuned_per[f32];
+	if (!c->panel_grid || !it || (it == c->panel_iter && c->num_sms * per == c->panel_grid)) return JN_OK;
+	return panel_schedule(c, it, per);
 }
 
 /* median CUDA-event time of the product kernel over `trials` products (after
@@ -812,7 +822,27 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 		if (cudaMalloc(&flush, bytes) != cudaSuccess) flush = NULL;
 	}
 	cudaGetLastError();
-	const jn_status s = autotune(c, trials, tune_engine, out, flush, bytes);
+	/* the panel schedule is tuned at both precisions (the FP64 kernel is
+	   bound by the FP64 pipe, the 32-bit one by instruction issue: they
+	   favour different task lengths); jn_set_precision installs the other
+	   one.  `out` reports the context's own precision. */
+	const int prec0 = c->precision, f32_0 = prec0 == 32;
+	c->tuned_iter[0] = c->tuned_iter[1] = 0;
+	jn_status s = autotune(c, trials, tune_engine, out, flush, bytes);
+	if (!s && out->engine == 4) {
+		c->tuned_iter[f32_0] = out->rows_per_lane;
+		c->tuned_per[f32_0] = out->ctas_per_sm;
+		jn_tuning other;
+		const int prec1 = f32_0 ? 64 : 32;
+		if (jn_panels_fit(c, !f32_0) && jn_set_precision(c, prec1) == JN_OK) {
+			if (autotune(c, trials, 0, &other, flush, bytes) == JN_OK && other.engine == 4) {
+				c->tuned_iter[!f32_0] = other.rows_per_lane;
+				c->tuned_per[!f32_0] = other.ctas_per_sm;
+			}
+			c->precision = prec0;
+			s = panel_schedule(c, out->rows_per_lane, out->ctas_per_sm);
+		}
+	}
 	if (flush) {
 		cudaStreamSynchronize(c->stream);
 		cudaFree(flush);
