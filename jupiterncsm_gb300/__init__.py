@@ -357,7 +357,9 @@ class Hamiltonian:
         _check(gpu_lib().jn_lanczos_save_eigenvectors(self._h, directory.encode(), int(count)))
 
     def autotune(self, trials=5, tune_engine=False):
-        """Time candidate product schedules on this problem and install the fastest (jn_autotune)."""
+        """Time candidate product schedules on this problem, L2 flushed before each, at both
+        precisions; install the fastest for the current one (set_precision installs the
+        other's) and report it (jn_autotune)."""
         t = Tuning()
         _check(gpu_lib().jn_autotune(self._h, int(trials), int(tune_engine), ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in Tuning._fields_}

@@ -224,14 +224,22 @@ def test_panel_schedules_do_not_change_a_bit(problem, bits):
     the autotuner installs one of them without changing the product."""
     d, Z, N, *_ = problem("he4_n6_3b")
     H = jn.Hamiltonian.from_dir(d, Z, N)
-    H.set_precision(bits)
+    other = 64 if bits == 32 else 32
     x = np.random.default_rng(25).standard_normal(H.dimension)
+    H.set_precision(other)
+    want_other = H.matvec(x)
+    H.set_precision(bits)
     want = H.matvec(x)
     for rows, per in ((8, 1), (64, 2), (128, 3)):
         H.set_panel_schedule(rows, per)
         assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
     t = H.autotune(trials=3)
     assert t["engine"] == 4 and t["candidates"] >= 5 and t["ms"] > 0
+    assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
+    # the other precision was tuned too: switching installs its schedule, and back
+    H.set_precision(other)
+    assert np.array_equal(H.matvec(x).view(np.uint64), want_other.view(np.uint64))
+    H.set_precision(bits)
     assert np.array_equal(H.matvec(x).view(np.uint64), want.view(np.uint64))
     with pytest.raises(jn.JnError):
         H.set_panel_schedule(0, 1)
