@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(PANEL_THREADS) jn_panel_kernel_fp64(const uint
 /* One cluster of PREP_CTAS CTAs: max|x| into ctrl[0] (with the FP32 round-up
  * margin of the other engines' scale), then the panel kernels' copies of x:
  * the 32-bit fixed-point x in the [p][n] layout (xn, when not NULL) and the
- * copy with every block transposed to [n][p] (xt); FP64 copies x itself.
+ * copy with every block transposed to [n][p] (xt, when not NULL); FP64
+ * copies x itself.
  * Each thread holds its PREP_PER states in registers across the cluster-wide
  * max (partial maxima meet in distributed shared memory), so x is read once;
  * elem[i] is the basis block of state i.  The work is integer: max|x| is the
@@ -355,13 +356,15 @@ __global__ void __cluster_dims__(PREP_CTAS, 1, 1) __launch_bounds__(PREP_THREADS
 	for (int u = 0; u < PREP_PER; u++) {
 		const int64_t i = ((int64_t)u * PREP_CTAS + rank) * PREP_THREADS + threadIdx.x;
 		if (i < dim) {
-			const uint4 bk = __ldg(blocks + __ldg(elem + i));
-			const uint32_t e = (uint32_t)(i - bk.x), Nn = bk.w, Np = bk.z;
 			T t;
 			if (sizeof(T) == 4) t = (T)fixed32_bits(v[u], Sx);
 			else t = (T)v[u];
 			if (xn) xn[i] = t;
-			xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+			if (xt) {
+				const uint4 bk = __ldg(blocks + __ldg(elem + i));
+				const uint32_t e = (uint32_t)(i - bk.x), Nn = bk.w, Np = bk.z;
+				xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+			}
 		}
 	}
 	/* no CTA leaves while another may still read its partial maximum */
@@ -613,7 +616,9 @@ static void panel_launch(const panel_sig_t *g, int has_tasks, int capturing)
 	unsigned int *ctrl = (unsigned int *)g->ctrl;
 	if (g->start) cudaEventRecordWithFlags((cudaEvent_t)g->start, st, evflags);
 	if (g->f32)
-		jn_panel_prep_kernel<int><<<PREP_CTAS, PREP_THREADS, 0, st>>>((const double *)g->x, (int *)g->xi, (int *)g->xt, blocks,
+		/* the kernel that stages x in shared memory reads only the [p][n] copy */
+		jn_panel_prep_kernel<int><<<PREP_CTAS, PREP_THREADS, 0, st>>>((const double *)g->x, (int *)g->xi,
+									 g->xs && has_tasks ? NULL : (int *)g->xt, blocks,
 									 (const uint16_t *)g->elem, g->dim, ctrl);
 	else
 		jn_panel_prep_kernel<double><<<PREP_CTAS, PREP_THREADS, 0, st>>>((const double *)g->x, NULL, (double *)g->xt, blocks,
