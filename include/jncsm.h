@@ -143,20 +143,43 @@ jn_status jn_matvec_profile(jn_ctx *ctx, const double *d_x, double *d_y, int acc
  * FP32 copy, which is the reference's skip (matrix_vector_multiplication.c:52-53). */
 jn_status jn_set_precision(jn_ctx *ctx, int precision);
 
-/* Product engine: 4 (default when the dimension is at most 28 672) — panels:
+/* Product engine: 4 (default when the dimension is at most 26 624) — panels:
  * every instruction's referenced matrix elements, signs applied, stored
- * densely and streamed once, with the whole of y accumulated in shared
- * memory as exact 64-bit fixed-point integers; 3 (default above that) —
- * shared-memory block tiles with exact 64-bit fixed-point sums; both give
- * bit-identical results whatever the execution order; 2 — one warp per
- * 32-element piece, FP64 sums in fixed term order. */
+ * densely and streamed once, with the blocks of y a CTA touches accumulated
+ * in shared memory as exact 64-bit fixed-point integers; 5 (default above
+ * that) — walks: each instruction's longer list walked by destination in
+ * lane chunks, the other list's rows grouped by connection index, each row
+ * summed in registers over a chunk and rounded once into a warp-private
+ * shared-memory accumulator (the walk plan is built on the first product);
+ * 3 — shared-memory block tiles with exact 64-bit fixed-point sums; 2 —
+ * one warp per 32-element piece, FP64 sums in fixed term order.  Engines 3,
+ * 4 and 5 give bit-identical results whatever the execution order. */
 jn_status jn_set_engine(jn_ctx *ctx, int engine);
+
+/* Arithmetic of the walk engine's precision-64 products: 0 (default) —
+ * exact integers: matrix elements and x as 52-bit fixed-point integers
+ * (scaled to max|M| and max|x|) split into 28 + 24 bits, three 32 x 32 ->
+ * 64-bit integer multiply-adds per contribution, every sum exact and each
+ * row's sum rounded once to the nearest output unit; 1 — FP64 fused
+ * multiply-adds (bound by GB300's narrow FP64 pipe).  Both are within
+ * 1e-13 of FP64 products relative to max|y|.  This extends the solver seam
+ * (no reference counterpart: the reference computes in FP64 only). */
+jn_status jn_set_walk_arithmetic(jn_ctx *ctx, int fp64_fma);
+
+/* The walk engine's plan (built here if it was not yet):
+ * out[0] warp tasks, out[1] pieces, out[2] row groups, out[3] multiply-adds
+ * including chunk padding, out[4] including idle lanes, out[5] length of the
+ * walk element array (the matrix elements plus the transposed copies of the
+ * blocks that proton walks read), out[6] persistent CTAs at the current
+ * arithmetic.  No reference counterpart (plan statistics). */
+jn_status jn_walk_stats(jn_ctx *ctx, double out[7]);
 
 /*
  * Autotuner.  Times candidate schedules of the product on the context's own
  * problem and precision: for the panel engine, rows per lane per warp task
- * (8 ... 128) x persistent CTAs per SM; with tune_engine also the
- * block-tile engine.  The fastest (median of `trials` CUDA-event timings of
+ * (8 ... 128) x persistent CTAs per SM; the walk and block-tile engines
+ * are one candidate each (with tune_engine, every engine is timed; without,
+ * only the context's own).  The fastest (median of `trials` CUDA-event timings of
  * the product kernel, each after a write of twice the L2 size, so that the
  * product's data streams from HBM) is installed.  The panel schedule is
  * tuned at both precisions (when the FP64 kernel fits): `tuning` reports the
@@ -169,7 +192,7 @@ jn_status jn_set_engine(jn_ctx *ctx, int engine);
  * (src/Mars/programs/mars.c:92-170).
  */
 typedef struct {
-	int engine;             /* 4 panels, 3 block tiles */
+	int engine;             /* 4 panels, 5 walks, 3 block tiles */
 	int rows_per_lane;      /* panel tasks: rows a lane walks */
 	int ctas_per_sm;        /* panel kernels: persistent CTAs per SM */
 	float ms;               /* product-kernel time of the choice */

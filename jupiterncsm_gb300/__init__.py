@@ -174,6 +174,10 @@ def gpu_lib():
     L.jn_set_panel_schedule.restype = ci
     L.jn_active_engine.argtypes = [vp]
     L.jn_active_engine.restype = ci
+    L.jn_set_walk_arithmetic.argtypes = [vp, ci]
+    L.jn_set_walk_arithmetic.restype = ci
+    L.jn_walk_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.jn_walk_stats.restype = ci
     fp = ctypes.POINTER(ctypes.c_float)
     L.jn_mlp_create.argtypes = [ci, ci, ci, ctypes.c_uint64, ctypes.POINTER(vp)]
     L.jn_mlp_destroy.argtypes = [vp]
@@ -384,12 +388,25 @@ class Hamiltonian:
                                         norm_matrix_path.encode() if norm_matrix_path else None,
                                         subspace_operator_path.encode() if subspace_operator_path else None))
 
+    def set_walk_arithmetic(self, fp64_fma):
+        """Precision-64 products of the walk engine: exact integers (False, the default) or FP64 FMAs (True)."""
+        _check(gpu_lib().jn_set_walk_arithmetic(self._h, 1 if fp64_fma else 0))
+
+    def walk_stats(self):
+        """The walk engine's plan: tasks, pieces, row groups, multiply-adds with padding (and with idle lanes), the
+        walk element array's length, and the persistent grid."""
+        out = (ctypes.c_double * 7)()
+        _check(gpu_lib().jn_walk_stats(self._h, out))
+        return dict(zip(("tasks", "pieces", "groups", "padded_multiply_adds", "lane_slots", "walk_elements", "grid"),
+                        list(out)))
+
     def active_engine(self):
         """The engine the next product runs (4 panels, 3 block tiles, 2 warp pieces)."""
         return gpu_lib().jn_active_engine(self._h)
 
     def set_engine(self, engine):
-        """4: panels (default where the accumulator fits in shared memory); 3: block tiles; 2: warp pieces."""
+        """4: panels (default where the accumulator fits in shared memory); 5: walks (default above that);
+        3: block tiles; 2: warp pieces."""
         _check(gpu_lib().jn_set_engine(self._h, int(engine)))
 
     def matvec_files(self, out_dir, in_dir):

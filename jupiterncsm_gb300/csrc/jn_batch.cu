@@ -717,6 +717,7 @@ extern "C" jn_status jn_set_matrix_elements(jn_ctx *c, const double *me)
 	p->abs_bound = jn_plan_abs_bound(p, p->me);
 	CUDA_TRY(cudaMemcpy(c->d_me, p->me, (size_t)p->n_me * sizeof(double), cudaMemcpyHostToDevice));
 	jn_panels_invalidate(c);
+	jn_walk_invalidate(c);
 	if (c->d_me32) {
 		float *h = (float *)malloc((p->n_me ? p->n_me : 1) * sizeof(float));
 		if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory");

@@ -41,7 +41,7 @@ struct jn_ctx {
 	int precision;          /* 64: FP64 products; 32: FP32 matrix elements and x, compensated sums */
 	float *d_me32;          /* FP32 copy of the matrix elements (built on first FP32 use) */
 	float *d_x32;
-	int engine;             /* 3: block tiles with exact fixed-point sums (default); 2: warp pieces */
+	int engine;             /* 4: panels (default up to JN_PANEL_MAX_DIM states); 5: walks (default above); 3: block tiles; 2: warp pieces */
 	jn_btile_t *d_btiles;
 	jn_piece_t *d_pieces;
 	jn_tterm_t *d_tterms;
@@ -71,6 +71,15 @@ struct jn_ctx {
 	struct jn_product_graph *graphs;
 	int ngraphs, graph_next;
 	cudaEvent_t prof_ev[4];         /* start, before and after the product kernel, end: recorded inside product graphs */
+	/* walk engine (engine 5, jn_walk.cu) */
+	int walk_ready;                 /* the walk plan is on the device */
+	int walk_per_sm[3];             /* CTAs per SM of the FP32, FP64 and integer walk kernels */
+	int walk_fp64;                  /* precision 64: 0 exact integers (default), 1 FP64 fused multiply-adds */
+	int walk_sc;                    /* coefficient exponent of the integer path */
+	uint4 *d_wtasks, *d_wpieces;
+	uint32_t *d_wlanes, *d_wwalks, *d_wrows, *d_wrdst, *d_wgroups;
+	void *d_welem[3];               /* walk element arrays: FP32, FP64, split integers (built on first use) */
+	int2 *d_wx;                     /* x converted for the product (FP32 or split 52-bit integers) */
 };
 
 /* drop the cached product graphs (before any product buffer is freed) */
@@ -136,6 +145,14 @@ jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const u
 				    const double *src, int64_t src_ld, const int *d_sel, int64_t sel_ld, double *y,
 				    int64_t y_ld, int *xbuf, unsigned long long *gacc, unsigned int *ctrl,
 				    const int *d_active, const jn_panel_partition *pp, cudaStream_t st);
+
+/* walk engine (jn_walk.cu): plan upload (built on first use), coefficient
+ * reset after new matrix elements, release, and the product */
+jn_status jn_walk_setup(jn_ctx *c);
+void jn_walk_invalidate(jn_ctx *c);
+void jn_walk_release(jn_ctx *c);
+jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
+			  cudaEvent_t mid);
 
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);

@@ -526,6 +526,7 @@ extern "C" void jn_close(jn_ctx *c)
 	for (int i = 0; i < 4; i++)
 		if (c->prof_ev[i]) cudaEventDestroy(c->prof_ev[i]);
 	jn_panels_release(c);
+	jn_walk_release(c);
 	jn_lanczos_release(c);
 	if (c->stream) cudaStreamDestroy(c->stream);
 	jn_plan_free(&c->plan);
@@ -593,8 +594,9 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 		c->tile_grid = c->num_sms * per_sm;
 		if (c->tile_grid > p->nbtiles) c->tile_grid = p->nbtiles > 0 ? p->nbtiles : 1;
 	}
-	/* the panel engine where the whole accumulator fits in shared memory, else block tiles */
-	c->engine = 3;
+	/* the panel engine where the whole accumulator fits in shared memory, else
+	   the walk engine (its plan is built on the first product) */
+	c->engine = 5;
 	if (p->dim <= JN_PANEL_MAX_DIM) {
 		if (jn_panels_setup(c) == JN_OK) c->engine = 4;
 		else jn_panels_release(c);
@@ -731,7 +733,8 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 	const jn_plan_t *p = &c->plan;
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
 	const int f32 = c->precision == 32;
-	if (f32) {
+	if (c->engine == 5) return jn_enqueue_walk(c, d_x, d_y, accumulate, st, pre, mid);
+	if (f32 && !(c->engine == 4 && jn_panels_fit(c, 1))) {
 		jn_status s = ensure_f32(c);
 		if (s) return s;
 	}
@@ -763,9 +766,13 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 
 extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 {
-	if (!c || engine < 2 || engine > 4) return fail(JN_ERR_INVALID, "engine must be 2, 3 or 4");
+	if (!c || engine < 2 || engine > 5) return fail(JN_ERR_INVALID, "engine must be 2, 3, 4 or 5");
 	if (engine == 4) {
 		jn_status s = jn_panels_setup(c);
+		if (s) return s;
+	}
+	if (engine == 5) {
+		jn_status s = jn_walk_setup(c);
 		if (s) return s;
 	}
 	c->engine = engine;
@@ -788,6 +795,7 @@ extern "C" jn_status jn_set_precision(jn_ctx *c, int precision)
 {
 	if (!c || (precision != 32 && precision != 64)) return fail(JN_ERR_INVALID, "precision must be 32 or 64");
 	if (precision == 32) {
+		/* the block-tile engine's FP32 copy, which the allocation-free product also reads */
 		jn_status s = ensure_f32(c);
 		if (s) return s;
 	}

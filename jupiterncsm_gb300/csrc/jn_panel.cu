@@ -881,13 +881,16 @@ static jn_status autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out
 				if (ms < best) { best = ms; best_engine = 4; best_iter = iters[a]; best_per = per; }
 			}
 	}
-	if (tune_engine || engine0 != 4) {
+	/* the walk and block-tile engines have no schedule to tune: each is one candidate */
+	for (int eng = 5; eng >= 3; eng -= 2) {
+		if (!(tune_engine || engine0 == eng)) continue;
+		if (eng == 5 && jn_walk_setup(c) != JN_OK) continue;
 		float ms;
-		c->engine = 3;
+		c->engine = eng;
 		jn_status s = time_product(c, trials, &ms, flush, flush_bytes);
 		if (s) { c->engine = engine0; return s; }
 		out->candidates++;
-		if (ms < best) { best = ms; best_engine = 3; }
+		if (ms < best) { best = ms; best_engine = eng; }
 	}
 	c->engine = best_engine;
 	if (best_engine == 4) {

@@ -334,6 +334,7 @@ void jn_plan_free(jn_plan_t *p)
 	free(p->btiles); free(p->pieces); free(p->tterms); free(p->walks); free(p->items);
 	free(p->term_dst);
 	jn_panels_free(p);
+	jn_walk_free(p);
 	memset(p, 0, sizeof *p);
 }
 

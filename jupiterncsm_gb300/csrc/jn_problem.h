@@ -186,6 +186,60 @@ typedef struct {
 	int32_t Np_out, Np_in;  /* proton dimensions: strides of the blocks' transposed copy of x */
 } jn_panel_t;
 
+/*
+ * Walk engine (engine 5, jn_walk.c / jn_walk.cu).  Every instruction is
+ * applied as one or two directed instructions: forward (input block ->
+ * output block) and, off-diagonal, transpose (output block -> input block).
+ * The longer list of an n x p instruction is the walk list: its view by
+ * destination is cut into walks (entries with one destination) and each walk
+ * into lane chunks of at most U entries (U = 8, 4 or 2, chosen per directed
+ * instruction).  The other list gives the rows (source row -> destination
+ * row, sign, connection index k).  Rows that share k read one row of the
+ * matrix-element block, so rows are grouped by k and a group's element row
+ * is gathered once per lane entry.  A single-species instruction walks its
+ * list, and its rows are the spectators (identity, sign +, one group).  A
+ * piece is a run of rows with at most JN_WALK_RS distinct destination rows;
+ * a warp task is one piece times 32 lane chunks.  For every row a lane sums
+ * its chunk's contributions in registers and adds the sum into a
+ * warp-private slot (destination row, walk) in shared memory, which the warp
+ * adds into the global accumulator once per task.
+ *
+ * Walk list = neutron list (wp = 0): D(r, w) = dst + r Nn_dst + w,
+ * S(r, w) = src + r Nn_src + w; proton list (wp = 1): D(r, w) = dst + w Nn_dst + r,
+ * S(r, w) = src + w Nn_src + r.
+ *
+ * Coefficients come from the walk element array: the plan's matrix elements
+ * (single-species elements below 1e-12 stored as 0, the reference's skip),
+ * then a transposed copy [k_p][k_n] of every n x p block that a proton-walk
+ * instruction uses.  The coefficient of (group g, entry e) is
+ * s_e A[base_g + k_e]: base_g = block + Nd_walk-stride k_row, so that a
+ * group reads one contiguous row of its block.
+ */
+#define JN_WALK_RS 16           /* distinct destination rows of a piece */
+#define JN_WALK_GROUP_END 0x40000000u   /* row word: the last row of its group */
+#define JN_WALK_PADBIT 0x40000000u      /* lane entry: padding (coefficient 0) */
+
+/* lane record of a chunk set, word-major (32 lanes per word): the walk slot,
+ * U / 2 words of packed 16-bit sources, U words of element offset | pad << 30
+ * | sign << 31 */
+#define JN_WALK_LANE_WORDS(U) (1 + (U) / 2 + (U))
+
+typedef struct {                /* 32 bytes */
+	int32_t src_off, dst_off;       /* offsets of the source and destination blocks in x and y */
+	int32_t Nn_src, Nn_dst;
+	int32_t row0;                   /* first row word in wrows */
+	int32_t rdst0;                  /* destination of each slot row in wrdst */
+	int32_t group0;                 /* element-row base of each group in wgroups */
+	uint32_t meta;                  /* slot rows | walk list is the proton list << 8 | row groups << 9 */
+} jn_wpiece_t;
+
+typedef struct {                /* 16 bytes */
+	uint32_t piece;
+	uint32_t lanes;                 /* first word of the lane records */
+	uint32_t walk0;                 /* walk table: the destination index of each walk slot */
+	uint32_t meta;                  /* walk slots | U << 8 */
+} jn_wtask_t;
+
 typedef struct {
 	/* problem */
 	int Z, N;
@@ -232,6 +286,18 @@ typedef struct {
 	int64_t n_pmeta;   uint32_t *pmeta;    /* each list's entries in panel order (list_order in jn_panel.c) */
 	uint32_t *pperm;                        /* per packed entry: its index in the list's by-out order */
 	int64_t n_coef;                         /* coefficients of all panels */
+	/* walk engine (built by jn_walk_build) */
+	int64_t nwtasks;   jn_wtask_t *wtasks;  /* in instruction order */
+	int64_t nwpieces;  jn_wpiece_t *wpieces;
+	int64_t n_wlanes;  uint32_t *wlanes;
+	int64_t n_wwalks;  uint32_t *wwalks;
+	int64_t n_wrows;   uint32_t *wrows;    /* source row | slot row << 16 | group end | sign << 31 */
+	int64_t n_wrdst;   uint32_t *wrdst;
+	int64_t n_wgroups; uint32_t *wgroups;  /* element-row base of each group */
+	int64_t n_wme;                          /* walk element array: n_me + transposed copies */
+	int64_t *wtpos;                         /* per matrix-element block: offset of its transpose, or -1 */
+	double wvisits;                         /* multiply-adds including padding */
+	double wlane_slots;                     /* lane slots of all tasks x rows: multiply-adds including idle lanes */
 } jn_plan_t;
 
 typedef struct {
@@ -283,6 +349,13 @@ int jn_panels_coefficients_int(const jn_plan_t *plan, const double *me, int32_t 
  * (single-species block, where |M| < 1e-12 counts as zero) << 30; the plan
  * must hold fewer than 2^30 matrix elements */
 void jn_panels_gather_index(const jn_plan_t *plan, uint32_t *gather);
+/* the walk engine's plan (jn_walk.c); the walk element array must hold
+ * fewer than 2^30 values.  jn_walk_free releases it (jn_plan_free does too). */
+int jn_walk_build(jn_plan_t *plan, char *err, size_t errlen);
+void jn_walk_free(jn_plan_t *plan);
+/* the walk element array (plan->n_wme values) from matrix elements in the
+ * plan's layout */
+void jn_walk_elements(const jn_plan_t *plan, const double *me, double *out);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,356 @@
+/*
+ * jn_walk.c — host side of the walk engine (engine 5): directed
+ * instructions, row groups, pieces, lane chunks and the walk element array
+ * (the layout is described in jn_problem.h).
+ *
+ * Semantics are the reference Minerva kernels'
+ * (src/Minerva/matrix_vector_multiplication/matrix_vector_multiplication.c:
+ * n list :20-77, p list :79-132, n x p lists :134-210, off-diagonal
+ * transposes :212-462, |M| < 1e-12 skip of single-species terms :52-53).
+ * The n x p contribution of a proton entry (p_i -> p_o, k_p) and a neutron
+ * entry (n_i -> n_o, k_n) is s_p s_n M[k_n + Nd k_p] x[n_i + Nn_i p_i] into
+ * y[n_o + Nn_o p_o]; here one of the two lists is walked by destination and
+ * the other supplies the rows, and the same contributions are summed in
+ * another order (each row sum is rounded once, at a place this plan fixes,
+ * and the rounded sums are added as integers, so the order never changes a
+ * result between runs).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#include "jn_problem.h"
+
+#define ERR(...) do { snprintf(err, errlen, __VA_ARGS__); goto fail; } while (0)
+#define MASK31 0x7fffffffu
+
+void jn_walk_free(jn_plan_t *p)
+{
+	free(p->wtasks); free(p->wpieces); free(p->wlanes); free(p->wwalks); free(p->wrows); free(p->wrdst);
+	free(p->wgroups); free(p->wtpos);
+	p->wtasks = NULL; p->wpieces = NULL; p->wlanes = NULL; p->wwalks = NULL; p->wrows = NULL; p->wrdst = NULL;
+	p->wgroups = NULL; p->wtpos = NULL;
+	p->nwtasks = p->nwpieces = p->n_wlanes = p->n_wwalks = p->n_wrows = p->n_wrdst = p->n_wgroups = p->n_wme = 0;
+	p->wvisits = p->wlane_slots = 0.0;
+}
+
+void jn_walk_elements(const jn_plan_t *p, const double *me, double *out)
+{
+	for (int b = 0; b < p->nmes; b++) {
+		const jn_me_t *M = &p->mes[b];
+		for (int64_t e = 0; e < M->len; e++) {
+			const double v = me[M->offset + e];
+			/* single-species terms skip |M| < 1e-12 (matrix_vector_multiplication.c:52-53) */
+			out[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0 : v;
+		}
+		if (p->wtpos && p->wtpos[b] >= 0) {
+			/* [k_p][k_n] copy of an n x p block stored [k_n + Nd_n k_p] */
+			const int64_t nn = (int64_t)M->nd_n, npp = (int64_t)M->nd_p;
+			double *t = out + p->wtpos[b];
+			for (int64_t kp = 0; kp < npp; kp++)
+				for (int64_t kn = 0; kn < nn; kn++) t[kp + npp * kn] = me[M->offset + kn + nn * kp];
+		}
+	}
+}
+
+/* growable arrays */
+typedef struct { void *a; int64_t n, cap; size_t sz; } vec_t;
+static int vec_reserve(vec_t *v, int64_t add)
+{
+	if (v->n + add <= v->cap) return 0;
+	int64_t c = v->cap ? v->cap : 1024;
+	while (c < v->n + add) c *= 2;
+	void *b = realloc(v->a, (size_t)c * v->sz);
+	if (!b) return 1;
+	v->a = b;
+	v->cap = c;
+	return 0;
+}
+
+typedef struct { uint32_t src, dst, k, sign; } row_t;
+
+static int cmp_row(const void *a, const void *b)
+{
+	const row_t *x = a, *y = b;
+	if (x->k != y->k) return x->k < y->k ? -1 : 1;
+	if (x->dst != y->dst) return x->dst < y->dst ? -1 : 1;
+	if (x->src != y->src) return x->src < y->src ? -1 : 1;
+	return (int)x->sign - (int)y->sign;
+}
+
+/* lane chunks of width U over the walks [w0, w0 + nw) */
+static int64_t chunks_for(const uint32_t *walks, int64_t w0, int64_t nw, int U)
+{
+	int64_t n = 0;
+	for (int64_t w = 0; w < nw; w++) n += ((walks[2 * (w0 + w) + 1] & 0xffffu) + U - 1) / U;
+	return n;
+}
+
+int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
+{
+	vec_t tasks = { 0, 0, 0, sizeof(jn_wtask_t) }, pieces = { 0, 0, 0, sizeof(jn_wpiece_t) };
+	vec_t lanes = { 0, 0, 0, sizeof(uint32_t) }, walks = { 0, 0, 0, sizeof(uint32_t) };
+	vec_t rows = { 0, 0, 0, sizeof(uint32_t) }, rdst = { 0, 0, 0, sizeof(uint32_t) };
+	vec_t groups = { 0, 0, 0, sizeof(uint32_t) };
+	row_t *R = NULL;
+	int64_t Rcap = 0;
+	uint32_t *chunk = NULL;         /* per chunk: first ent index, count, walk index */
+	int64_t ccap = 0;
+	int32_t *stamp = calloc(65536, sizeof(int32_t));
+	int32_t stamp_clock = 0;
+	double visits = 0.0, slots = 0.0;
+	jn_walk_free(p);
+	p->wtpos = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int64_t));
+	if (!stamp || !p->wtpos) ERR("out of host memory");
+	if (p->dim >= 0x7fffffffll) ERR("dimension %lld: too large for the walk engine's 32-bit offsets", (long long)p->dim);
+	/* transposed copies of the n x p blocks that proton-walk instructions use */
+	for (int b = 0; b < p->nmes; b++) p->wtpos[b] = -1;
+	p->n_wme = p->n_me;
+	for (int q = 0; q < p->ninstr; q++) {
+		const jn_instr_t *x = &p->instr[q];
+		if (x->kind != JN_KIND_NP || p->lists[x->lp].len <= p->lists[x->ln].len || p->wtpos[x->me] >= 0) continue;
+		p->wtpos[x->me] = p->n_wme;
+		p->n_wme += p->mes[x->me].len;
+	}
+	if (p->n_wme >= 0x3fffffffll) ERR("%lld walk matrix elements: too many for the walk engine", (long long)p->n_wme);
+	for (int q = 0; q < p->ninstr; q++) {
+		const jn_instr_t *x = &p->instr[q];
+		const jn_block_t *bi = &p->blocks[x->bin], *bo = &p->blocks[x->bout];
+		const jn_me_t *M = &p->mes[x->me];
+		const jn_list_t *W, *RL = NULL;
+		int wp;
+		int64_t base, stride;           /* element row of k_row: base + stride k_row */
+		if (x->kind == JN_KIND_NP) {
+			const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+			wp = Lp->len > Ln->len;
+			W = wp ? Lp : Ln;
+			RL = wp ? Ln : Lp;
+			base = wp ? p->wtpos[x->me] : M->offset;
+			stride = wp ? (int64_t)M->nd_p : (int64_t)M->nd_n;
+		} else if (x->kind == JN_KIND_N) {
+			W = &p->lists[x->ln];
+			wp = 0;
+			base = M->offset;
+			stride = 0;
+			if (bi->Np != bo->Np) ERR("instruction %d: spectator rows differ", q);
+		} else {
+			W = &p->lists[x->lp];
+			wp = 1;
+			base = M->offset;
+			stride = 0;
+			if (bi->Nn != bo->Nn) ERR("instruction %d: spectator columns differ", q);
+		}
+		const int64_t wlen = RL ? (wp ? (int64_t)M->nd_p : (int64_t)M->nd_n) : M->len;   /* walk-side k range */
+		const int64_t rlen = RL ? (wp ? (int64_t)M->nd_n : (int64_t)M->nd_p) : 1;         /* row-side k range */
+		if (W->len == 0) continue;
+		for (int dir = 0; dir < 2; dir++) {
+			if (dir == 1 && x->bin == x->bout) break;
+			const jn_block_t *bs = dir ? bo : bi, *bd = dir ? bi : bo;
+			/* rows of this direction */
+			const int64_t nr = RL ? RL->len : (wp ? bo->Nn : bo->Np);
+			if (nr > Rcap) {
+				Rcap = nr;
+				row_t *g = realloc(R, (size_t)Rcap * sizeof(row_t));
+				if (!g) ERR("out of host memory");
+				R = g;
+			}
+			if (RL) {
+				for (int64_t e = 0; e < nr; e++) {
+					const int32_t *t = RL->triples + 3 * e;
+					R[e].src = (uint32_t)(dir ? t[1] : t[0]);
+					R[e].dst = (uint32_t)(dir ? t[0] : t[1]);
+					R[e].k = (uint32_t)t[2] & MASK31;
+					R[e].sign = (uint32_t)t[2] >> 31;
+				}
+				qsort(R, (size_t)nr, sizeof(row_t), cmp_row);
+			} else {
+				for (int64_t r = 0; r < nr; r++) R[r] = (row_t){ (uint32_t)r, (uint32_t)r, 0u, 0u };
+			}
+			if (nr == 0) continue;
+			/* row index bounds: sources and destinations inside their blocks, k inside the element block */
+			const int64_t src_rows = wp ? bs->Nn : bs->Np, dst_rows = wp ? bd->Nn : bd->Np;
+			for (int64_t e = 0; e < nr; e++)
+				if (R[e].src >= src_rows || R[e].dst >= dst_rows || R[e].src > 0xffffu || R[e].k >= rlen)
+					ERR("instruction %d: row index out of range", q);
+			/* walk view and its bounds: destinations and sources inside their blocks, k inside the block */
+			const int64_t w0 = dir ? W->walk_in : W->walk_out, nw = dir ? W->nwalk_in : W->nwalk_out;
+			const int64_t src_cols = wp ? bs->Np : bs->Nn, dst_cols = wp ? bd->Np : bd->Nn;
+			for (int64_t w = 0; w < nw; w++) {
+				const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
+				if ((p->walks[2 * (w0 + w) + 1] >> 16) >= dst_cols) ERR("instruction %d: walk destination out of range", q);
+				for (uint32_t e = a; e < a + len; e++)
+					if ((p->ent[2 * e] & 0xffffu) >= src_cols || (p->ent[2 * e + 1] & MASK31) >= wlen)
+						ERR("instruction %d: walk entry out of range", q);
+			}
+			/* the chunk width with the fewest lane slots, counting a row's fixed
+			   cost as about two entries */
+			int U = 8;
+			{
+				double best = 1e300;
+				for (int u = 8; u >= 2; u /= 2) {
+					const int64_t nc = chunks_for(p->walks, w0, nw, u);
+					const double cost = (double)((nc + 31) / 32) * 32 * (u + 2);
+					if (cost < best) { best = cost; U = u; }
+				}
+			}
+			const int LW = JN_WALK_LANE_WORDS(U);
+			const int64_t nchunk = chunks_for(p->walks, w0, nw, U);
+			if (3 * nchunk > ccap) {
+				ccap = 3 * nchunk;
+				uint32_t *g = realloc(chunk, (size_t)ccap * sizeof(uint32_t));
+				if (!g) ERR("out of host memory");
+				chunk = g;
+			}
+			{
+				int64_t c = 0;
+				for (int64_t w = 0; w < nw; w++) {
+					const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
+					for (uint32_t o = 0; o < len; o += (uint32_t)U) {
+						chunk[3 * c] = a + o;
+						chunk[3 * c + 1] = len - o < (uint32_t)U ? len - o : (uint32_t)U;
+						chunk[3 * c + 2] = (uint32_t)w;
+						c++;
+					}
+				}
+			}
+			/* lane records and walk tables: one per 32 chunks, shared by the pieces */
+			const int64_t nsets = (nchunk + 31) / 32;
+			const int64_t lanes0 = lanes.n;
+			if (vec_reserve(&lanes, nsets * 32 * LW) || vec_reserve(&walks, nsets * 32)) ERR("out of host memory");
+			uint32_t *set_walk0 = malloc((size_t)(nsets ? nsets : 1) * 2 * sizeof(uint32_t));
+			if (!set_walk0) ERR("out of host memory");
+			for (int64_t s = 0; s < nsets; s++) {
+				uint32_t *L = (uint32_t *)lanes.a + lanes.n;
+				uint32_t *T = (uint32_t *)walks.a + walks.n;
+				int nwalk = 0;
+				int64_t prev = -1;
+				for (int l = 0; l < 32; l++) {
+					const int64_t c = s * 32 + l;
+					uint32_t slot = 0, src[8], koff[8];
+					for (int u = 0; u < U; u++) { src[u] = 0; koff[u] = JN_WALK_PADBIT; }
+					if (c < nchunk) {
+						const int64_t w = chunk[3 * c + 2];
+						if (w != prev) {
+							T[nwalk++] = p->walks[2 * (w0 + w) + 1] >> 16;
+							prev = w;
+						}
+						slot = (uint32_t)(nwalk - 1);
+						const uint32_t e0 = chunk[3 * c], n = chunk[3 * c + 1];
+						/* padding repeats the chunk's first source with coefficient 0 */
+						for (int u = 0; u < U; u++) {
+							const uint32_t e = e0 + ((uint32_t)u < n ? (uint32_t)u : 0u);
+							src[u] = p->ent[2 * e] & 0xffffu;
+							koff[u] = (uint32_t)u < n ? p->ent[2 * e + 1] : JN_WALK_PADBIT;
+						}
+					}
+					L[l] = slot;
+					for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l] = src[2 * k] | (src[2 * k + 1] << 16);
+					for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l] = koff[u];
+				}
+				set_walk0[2 * s] = (uint32_t)walks.n;
+				set_walk0[2 * s + 1] = (uint32_t)nwalk;
+				lanes.n += 32 * LW;
+				walks.n += nwalk;
+			}
+			/* pieces: runs of whole row groups with at most RS distinct destination rows
+			   (a group with more is split, and its element row read once per part) */
+			int64_t r0 = 0;
+			while (r0 < nr) {
+				stamp_clock++;
+				if (stamp_clock == 0x7fffffff) { memset(stamp, 0, 65536 * sizeof(int32_t)); stamp_clock = 1; }
+				int rs = 0;
+				int64_t r1 = r0;
+				const int64_t rdst0 = rdst.n, row0 = rows.n, group0 = groups.n;
+				if (vec_reserve(&rdst, JN_WALK_RS) || vec_reserve(&rows, nr - r0) || vec_reserve(&groups, nr - r0)) {
+					free(set_walk0);
+					ERR("out of host memory");
+				}
+				while (r1 < nr) {
+					/* the next group [r1, g1) and the destinations it would add */
+					int64_t g1 = r1;
+					while (g1 < nr && R[g1].k == R[r1].k) g1++;
+					int add = 0;
+					for (int64_t e = r1; e < g1; e++)
+						if (stamp[R[e].dst] != stamp_clock && (e == r1 || R[e].dst != R[e - 1].dst)) add++;
+					if (rs > 0 && rs + add > JN_WALK_RS) break;
+					/* take the group, or as much of it as fits */
+					int64_t e = r1;
+					for (; e < g1; e++) {
+						if (stamp[R[e].dst] != stamp_clock) {
+							if (rs == JN_WALK_RS) break;
+							stamp[R[e].dst] = stamp_clock;
+							((uint32_t *)rdst.a)[rdst.n + rs] = R[e].dst;
+							rs++;
+						}
+					}
+					((uint32_t *)groups.a)[groups.n++] = (uint32_t)(base + stride * (int64_t)R[r1].k);
+					r1 = e;
+					if (e < g1) break;      /* a split group ends the piece */
+				}
+				/* row words: slot rows in order of first appearance */
+				for (int64_t e = r0; e < r1; e++) {
+					int slot = 0;
+					while (((uint32_t *)rdst.a)[rdst.n + slot] != R[e].dst) slot++;
+					const int end = e + 1 == r1 || R[e + 1].k != R[e].k;
+					((uint32_t *)rows.a)[rows.n + (e - r0)] = R[e].src | ((uint32_t)slot << 16) |
+										 (end ? JN_WALK_GROUP_END : 0u) | (R[e].sign << 31);
+				}
+				rows.n += r1 - r0;
+				rdst.n += rs;
+				if (vec_reserve(&pieces, 1) || vec_reserve(&tasks, nsets)) { free(set_walk0); ERR("out of host memory"); }
+				const int64_t pi = pieces.n++;
+				jn_wpiece_t *P = (jn_wpiece_t *)pieces.a + pi;
+				P->src_off = (int32_t)bs->offset;
+				P->dst_off = (int32_t)bd->offset;
+				P->Nn_src = (int32_t)bs->Nn;
+				P->Nn_dst = (int32_t)bd->Nn;
+				P->row0 = (int32_t)row0;
+				P->rdst0 = (int32_t)rdst0;
+				P->group0 = (int32_t)group0;
+				if (groups.n - group0 >= (1 << 23)) { free(set_walk0); ERR("instruction %d: too many row groups", q); }
+				P->meta = (uint32_t)rs | ((uint32_t)wp << 8) | ((uint32_t)(groups.n - group0) << 9);
+				for (int64_t s = 0; s < nsets; s++) {
+					jn_wtask_t *T = (jn_wtask_t *)tasks.a + tasks.n++;
+					T->piece = (uint32_t)pi;
+					T->lanes = (uint32_t)(lanes0 + s * 32 * LW);
+					T->walk0 = set_walk0[2 * s];
+					T->meta = set_walk0[2 * s + 1] | ((uint32_t)U << 8);
+					const int64_t used = (s + 1) * 32 <= nchunk ? 32 : nchunk - s * 32;
+					visits += (double)(r1 - r0) * (double)used * U;
+					slots += (double)(r1 - r0) * 32.0 * U;
+				}
+				r0 = r1;
+			}
+			free(set_walk0);
+		}
+	}
+	/* tasks stay in instruction order: warps take them cyclically (warp w of W
+	   runs tasks w, w + W, ...), so warps that run at the same time work on
+	   neighbouring instructions and share their blocks of x and of matrix
+	   elements in cache */
+	/* one spare row word: the kernel reads the word after a group's last row ahead of time */
+	if (vec_reserve(&rows, 1)) ERR("out of host memory");
+	((uint32_t *)rows.a)[rows.n] = 0u;
+	if (tasks.n > 0xffffffffll || lanes.n > 0xffffffffll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
+	    rdst.n > 0x7fffffffll || groups.n > 0x7fffffffll || pieces.n > 0xffffffffll)
+		ERR("the walk plan is too large");
+	p->wtasks = tasks.a; p->nwtasks = tasks.n;
+	p->wpieces = pieces.a; p->nwpieces = pieces.n;
+	p->wlanes = lanes.a; p->n_wlanes = lanes.n;
+	p->wwalks = walks.a; p->n_wwalks = walks.n;
+	p->wrows = rows.a; p->n_wrows = rows.n;         /* plus the spare word */
+	p->wrdst = rdst.a; p->n_wrdst = rdst.n;
+	p->wgroups = groups.a; p->n_wgroups = groups.n;
+	p->wvisits = visits;
+	p->wlane_slots = slots;
+	free(R); free(chunk); free(stamp);
+	return 0;
+fail:
+	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
+	free(R); free(chunk); free(stamp);
+	free(p->wtpos);
+	p->wtpos = NULL;
+	p->n_wme = 0;
+	return 1;
+}

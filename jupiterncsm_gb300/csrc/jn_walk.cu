@@ -1,0 +1,489 @@
+/*
+ * jn_walk.cu — the walk engine (engine 5): the index-list product with the
+ * contributions summed in registers before they reach memory (host plan in
+ * jn_walk.c, layout in jn_problem.h).
+ *
+ * Semantics are the reference Minerva kernels'
+ * (src/Minerva/matrix_vector_multiplication/matrix_vector_multiplication.c:
+ * n list :20-77, p list :79-132, n x p lists :134-210, off-diagonal
+ * transposes :212-462, |M| < 1e-12 skip of single-species terms :52-53).
+ *
+ * GB300 organisation.  A warp task is 32 lane chunks (up to U = 8, 4 or 2
+ * entries of one walk each: one destination column) times the rows of a
+ * piece.  The rows are grouped by their connection index: a group reads one
+ * contiguous row of its matrix-element block (of its transposed copy for
+ * proton walks), so a lane gathers the coefficients of its chunk from that
+ * row once per group, through L1, and reuses them for every row of the
+ * group; instructions that share a block run on neighbouring warps, and L2
+ * serves each element to all of them.  For each row the lane gathers its
+ * chunk's x values, sums the U products in registers, rounds the sum once
+ * to the 64-bit fixed-point unit and adds it into a warp-private slot
+ * (destination row, walk) in shared memory; after the task the warp adds
+ * its slots into the global accumulator.  Shared-memory adds are U times
+ * fewer than contributions, global adds a further factor of the rows per
+ * destination fewer.
+ *
+ * Arithmetic (the template parameter MODE):
+ *   32  FP32 coefficients and x, fused multiply-adds in entry order;
+ *   64  FP64 coefficients and x, fused multiply-adds (GB300's FP64 pipe is
+ *       narrow: this mode is bound by it);
+ *   1   exact integers: coefficients and x as 52-bit fixed-point integers
+ *       split into a signed high part (28 bits) and a low part (24 bits);
+ *       c x = ch xh 2^48 + (ch xl + cl xh) 2^24 + cl xl, summed over the
+ *       chunk in two 64-bit registers with three 32 x 32 -> 64-bit integer
+ *       multiply-adds per contribution (cl xl < 2^48 is dropped), and the
+ *       sum rounded once to the nearest output unit.  This is the FP64-grade
+ *       product: its inputs keep 52 bits against max|c| and max|x|, every
+ *       sum is exact, and it runs on the integer pipe.
+ * Every row sum is rounded once, at a place fixed by the plan, and the
+ * rounded sums are added as integers: the result is bit-identical from run
+ * to run and independent of the grid.
+ */
+#include "jn_internal.h"
+#include "jn_fixed.cuh"
+
+#define WALK_WARPS 8
+#define WALK_THREADS (WALK_WARPS * 32)
+#define WALK_SLOTS (JN_WALK_RS * 32)    /* per warp: lo words, then hi words */
+#define WALK_SMEM ((size_t)WALK_WARPS * 2 * WALK_SLOTS * sizeof(unsigned int))
+
+static_assert(sizeof(jn_wtask_t) == 16 && sizeof(jn_wpiece_t) == 32, "tasks are read as one uint4, pieces as two");
+
+/* exponent of the 52-bit fixed-point x: |x| 2^Sx < 2^52 for the bound max|x| in xmax_bits */
+__device__ __forceinline__ int walk_x_exponent(unsigned int xmax_bits)
+{
+	if (!(xmax_bits & 0x7fffffffu)) return 0;
+	return 52 - ((int)((xmax_bits >> 23) & 0xff) - 126);
+}
+
+/* The output unit 2^-S and, for the integer path, the shift of a row sum
+ * A 2^48 + B 2^24 (in units of 2^-(Sc + Sx)) down to it: S is the usual
+ * fixed-point exponent (|y| 2^S < 2^62), lowered where needed so that the
+ * shift is at least 48 bits. */
+__device__ __forceinline__ void walk_scales(unsigned int xmax_bits, double abs_bound, int Sc, int mode, int *S, int *sh)
+{
+	int s = fixed_exponent(xmax_bits, abs_bound), k = 0;
+	if (mode == 1) {
+		const int Sx = walk_x_exponent(xmax_bits);
+		if (Sc + Sx - s < 48) s = Sc + Sx - 48;
+		k = Sc + Sx - s - 48;
+		if (k > 63) k = 63;
+	}
+	*S = s;
+	*sh = k;
+}
+
+template <int MODE> struct WalkT;
+template <> struct WalkT<32> { typedef float C; typedef float X; };
+template <> struct WalkT<64> { typedef double C; typedef double X; };
+template <> struct WalkT<1> { typedef int2 C; typedef int2 X; };
+
+/* the sum of one row over a lane's chunk, rounded once to a 64-bit integer in output units */
+template <int MODE, int U>
+__device__ __forceinline__ long long walk_row(const typename WalkT<MODE>::C *c, const typename WalkT<MODE>::X *xv, uint32_t row,
+					      int sh, float scalef, double scale)
+{
+	long long v;
+	if constexpr (MODE == 1) {
+		long long A = 0, B = 0;
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			A += (long long)c[u].x * xv[u].x;
+			B += (long long)c[u].x * xv[u].y;
+			B += (long long)c[u].y * xv[u].x;
+		}
+		/* A 2^48 + B 2^24 rounded to the nearest multiple of 2^(48 + sh) */
+		const long long q = A + (B >> 24);
+		v = sh ? (q + (1ll << (sh - 1))) >> sh : q + ((B >> 23) & 1);
+		if (row >> 31) v = -v;
+	} else if constexpr (MODE == 32) {
+		float acc = 0.0f;
+#pragma unroll
+		for (int u = 0; u < U; u++) acc = __fmaf_rn(c[u], xv[u], acc);
+		v = __float2ll_rn(acc * ((row >> 31) ? -scalef : scalef));
+	} else {
+		double acc = 0.0;
+#pragma unroll
+		for (int u = 0; u < U; u++) acc = __fma_rn(c[u], xv[u], acc);
+		v = __double2ll_rn(acc * ((row >> 31) ? -scale : scale));
+	}
+	return v;
+}
+
+/* one warp task with chunks of U entries (see the file comment).  Rows are
+ * taken two at a time, so that two rows' gathers of x are in flight at once;
+ * the word after a group's last row is read ahead (the plan keeps a spare
+ * word at the end) and not used. */
+template <int MODE, int U>
+__device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const uint4 pb, const uint32_t *__restrict__ lanes,
+					  const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
+					  const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
+					  const typename WalkT<MODE>::C *__restrict__ elem,
+					  const typename WalkT<MODE>::X *__restrict__ x, unsigned long long *__restrict__ gacc,
+					  unsigned int *__restrict__ lo, unsigned int *__restrict__ hi, int lane, int sh, float scalef,
+					  double scale)
+{
+	typedef typename WalkT<MODE>::C C;
+	typedef typename WalkT<MODE>::X X;
+	const int src_off = (int)pa.x, dst_off = (int)pa.y, Nn_src = (int)pa.z, Nn_dst = (int)pa.w;
+	const int rs = (int)(pb.w & 0xffu), wp = (int)((pb.w >> 8) & 1u), ngroups = (int)(pb.w >> 9);
+	const uint32_t *__restrict__ L = lanes + ta.y + lane;
+	const int ws = (int)__ldg(L);
+	int off[U];
+#pragma unroll
+	for (int k = 0; k < U / 2; k++) {
+		const uint32_t w = __ldg(L + (1 + k) * 32);
+		off[2 * k] = (int)(w & 0xffffu);
+		off[2 * k + 1] = (int)(w >> 16);
+	}
+	if (wp) {
+#pragma unroll
+		for (int u = 0; u < U; u++) off[u] *= Nn_src;
+	}
+	const X *__restrict__ xs = x + src_off;
+	int j = (int)pb.x;
+	uint32_t row = __ldg(rows + j);
+	for (int g = 0; g < ngroups; g++) {
+		const C *__restrict__ er = elem + __ldg(groups + (int)pb.z + g);
+		C c[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			const uint32_t ko = __ldg(L + (1 + U / 2 + u) * 32);
+			C v = __ldg(er + (ko & 0x3fffffffu));
+			const bool pad = (ko & JN_WALK_PADBIT) != 0, neg = (ko >> 31) != 0;
+			if constexpr (MODE == 1) {
+				if (pad) v = make_int2(0, 0);
+				if (neg) v = make_int2(-v.x, -v.y);
+			} else {
+				if (pad) v = (C)0;
+				if (neg) v = -v;
+			}
+			c[u] = v;
+		}
+		for (;;) {
+			/* this row and the next one of the group (if any) */
+			const uint32_t row2 = __ldg(rows + j + 1);
+			const bool two = !(row & JN_WALK_GROUP_END);
+			const int sr = (int)(row & 0xffffu), sr2 = (int)(row2 & 0xffffu);
+			const X *__restrict__ xb = xs + (wp ? sr : sr * Nn_src);
+			const X *__restrict__ xb2 = xs + (two ? (wp ? sr2 : sr2 * Nn_src) : 0);
+			X xv[U], xv2[U];
+#pragma unroll
+			for (int u = 0; u < U; u++) xv[u] = __ldg(xb + off[u]);
+#pragma unroll
+			for (int u = 0; u < U; u++) xv2[u] = __ldg(xb2 + (two ? off[u] : 0));
+			const uint32_t next = __ldg(rows + j + 2);
+			add_fixed(lo, hi, (int)((row >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv, row, sh, scalef, scale));
+			if (two) add_fixed(lo, hi, (int)((row2 >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv2, row2, sh, scalef, scale));
+			const bool end = !two || (row2 & JN_WALK_GROUP_END);
+			j += two ? 2 : 1;
+			row = two ? next : row2;
+			if (end) break;
+		}
+	}
+	__syncwarp();
+	/* the task's slots into the global accumulator; slots are left zero */
+	const int nw = (int)(ta.w & 0xffu), n = rs * nw;
+	for (int i = lane; i < n; i += 32) {
+		const int r = i / nw, w = i - r * nw, s = r * 32 + w;
+		const unsigned long long v = (unsigned long long)lo[s] | ((unsigned long long)hi[s] << 32);
+		if (v) {
+			lo[s] = 0u;
+			hi[s] = 0u;
+			const int dr = (int)__ldg(rdst + (int)pb.y + r), dw = (int)__ldg(walks + ta.z + w);
+			atomicAdd(gacc + dst_off + (wp ? dw * Nn_dst + dr : dr * Nn_dst + dw), v);
+		}
+	}
+	__syncwarp();
+}
+
+/* FP32: 4 CTAs an SM (64 registers); the 64-bit paths need more registers: 3 */
+template <int MODE>
+__global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
+	jn_walk_kernel(const uint4 *__restrict__ tasks, const uint4 *__restrict__ pieces, const uint32_t *__restrict__ lanes,
+		       const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
+		       const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
+		       const typename WalkT<MODE>::C *__restrict__ elem, const typename WalkT<MODE>::X *__restrict__ x,
+		       unsigned long long *__restrict__ gacc, const unsigned int *__restrict__ ctrl, long long ntasks,
+		       double abs_bound, int Sc, int nsm)
+{
+	extern __shared__ unsigned int wslots[];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	unsigned int *lo = wslots + warp * 2 * WALK_SLOTS, *hi = lo + WALK_SLOTS;
+	for (int i = lane; i < 2 * WALK_SLOTS; i += 32) lo[i] = 0u;
+	__syncwarp();
+	int S, sh;
+	walk_scales(ctrl[0], abs_bound, Sc, MODE, &S, &sh);
+	const float scalef = MODE == 32 ? __int_as_float((127 + (S < -126 ? -126 : (S > 127 ? 127 : S))) << 23) : 0.0f;
+	const double scale = MODE == 64 ? ldexp(1.0, S) : 0.0;
+	/* warps take tasks cyclically; the warps of the CTAs an SM holds (CTA b
+	   runs on SM b mod nsm when the grid is a multiple of the SM count) get
+	   consecutive indices, so an SM works on neighbouring tasks at a time */
+	const long long nwarps = (long long)gridDim.x * WALK_WARPS;
+	const int per = nsm > 0 && gridDim.x % nsm == 0 ? (int)gridDim.x / nsm : 0;
+	const long long w0 = per ? ((long long)(blockIdx.x % nsm) * per + blockIdx.x / nsm) * WALK_WARPS + warp
+				 : (long long)blockIdx.x * WALK_WARPS + warp;
+	for (long long t = w0; t < ntasks; t += nwarps) {
+		const uint4 ta = __ldg(tasks + t);
+		const uint4 pa = __ldg(pieces + 2 * ta.x), pb = __ldg(pieces + 2 * ta.x + 1);
+		const uint32_t U = (ta.w >> 8) & 0xffu;
+		if (U == 8)
+			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+		else if (U == 4)
+			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+		else
+			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+	}
+}
+
+/* x as 52-bit fixed-point integers {high 28 bits (signed), low 24 bits} */
+__global__ void jn_walk_xsplit_kernel(const double *__restrict__ x, int2 *__restrict__ xi, int64_t n,
+				      const unsigned int *__restrict__ ctrl)
+{
+	const double s = ldexp(1.0, walk_x_exponent(ctrl[0]));
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const long long v = __double2ll_rn(x[i] * s);
+		xi[i] = make_int2((int)(v >> 24), (int)(v & 0xffffff));
+	}
+}
+
+/* y (+)= acc 2^-S with the integer path's unit; the accumulator is cleared */
+__global__ void jn_walk_finalize_kernel(unsigned long long *__restrict__ gacc, double *__restrict__ y, int64_t n,
+					const unsigned int *__restrict__ ctrl, double abs_bound, int Sc, int mode,
+					int accumulate)
+{
+	int S, sh;
+	walk_scales(ctrl[0], abs_bound, Sc, mode, &S, &sh);
+	const double unit = ldexp(1.0, -S);
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = (double)(long long)gacc[i] * unit;
+		y[i] = accumulate ? y[i] + v : v;
+		gacc[i] = 0ull;
+	}
+}
+
+/* bits of max |A| over the walk element array (non-negative doubles order as their bits) */
+__global__ void jn_walk_amax_kernel(const double *__restrict__ a, int64_t n, unsigned long long *__restrict__ amax)
+{
+	double m = 0.0;
+	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+		m = fmax(m, fabs(a[e]));
+	for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(amax, (unsigned long long)__double_as_longlong(m));
+}
+
+/* the walk element array in FP32, or as 52-bit fixed-point integers split into {high 28 bits, low 24 bits} */
+template <int MODE>
+__global__ void jn_walk_convert_kernel(const double *__restrict__ a, int64_t n, typename WalkT<MODE>::C *__restrict__ out, int Sc)
+{
+	const double s = ldexp(1.0, Sc);
+	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+		if constexpr (MODE == 32) {
+			out[e] = (float)a[e];
+		} else {
+			const long long q = __double2ll_rn(a[e] * s);
+			out[e] = make_int2((int)(q >> 24), (int)(q & 0xffffff));
+		}
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* host side                                                           */
+/* ------------------------------------------------------------------ */
+template <typename T>
+static jn_status wupload(T **dst, const void *src, size_t n)
+{
+	size_t bytes = (n ? n : 1) * sizeof(T);
+	cudaError_t e = cudaMalloc((void **)dst, bytes);
+	if (e != cudaSuccess) return jn_fail(JN_ERR_NOMEM, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+	if (n && src) {
+		e = cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "cudaMemcpy failed: %s", cudaGetErrorString(e));
+	}
+	return JN_OK;
+}
+
+static int walk_mode(const jn_ctx *c) { return c->precision == 32 ? 32 : (c->walk_fp64 ? 64 : 1); }
+static int walk_slot(int mode) { return mode == 32 ? 0 : (mode == 64 ? 1 : 2); }
+
+void jn_walk_release(jn_ctx *c)
+{
+	cudaFree(c->d_wtasks); cudaFree(c->d_wpieces); cudaFree(c->d_wlanes); cudaFree(c->d_wwalks); cudaFree(c->d_wrows);
+	cudaFree(c->d_wrdst); cudaFree(c->d_wgroups); cudaFree(c->d_wx);
+	for (int i = 0; i < 3; i++) cudaFree(c->d_welem[i]);
+	c->d_wtasks = NULL; c->d_wpieces = NULL; c->d_wlanes = NULL; c->d_wwalks = NULL; c->d_wrows = NULL;
+	c->d_wrdst = NULL; c->d_wgroups = NULL; c->d_wx = NULL;
+	for (int i = 0; i < 3; i++) c->d_welem[i] = NULL;
+	c->walk_ready = 0;
+}
+
+void jn_walk_invalidate(jn_ctx *c)
+{
+	for (int i = 0; i < 3; i++) {
+		cudaFree(c->d_welem[i]);
+		c->d_welem[i] = NULL;
+	}
+}
+
+jn_status jn_walk_setup(jn_ctx *c)
+{
+	if (c->walk_ready) return JN_OK;
+	jn_plan_t *p = &c->plan;
+	char err[512] = { 0 };
+	if (jn_walk_build(p, err, sizeof err)) return jn_fail(JN_ERR_NOMEM, "walk plan: %s", err);
+	jn_status s;
+	if ((s = wupload(&c->d_wtasks, p->wtasks, (size_t)p->nwtasks)) ||
+	    (s = wupload(&c->d_wpieces, p->wpieces, (size_t)p->nwpieces * 2)) ||
+	    (s = wupload(&c->d_wlanes, p->wlanes, (size_t)p->n_wlanes)) ||
+	    (s = wupload(&c->d_wwalks, p->wwalks, (size_t)p->n_wwalks)) ||
+	    (s = wupload(&c->d_wrows, p->wrows, (size_t)p->n_wrows + 1)) ||
+	    (s = wupload(&c->d_wrdst, p->wrdst, (size_t)p->n_wrdst)) ||
+	    (s = wupload(&c->d_wgroups, p->wgroups, (size_t)p->n_wgroups)) ||
+	    (s = wupload(&c->d_wx, (const void *)NULL, (size_t)(p->dim ? p->dim : 1)))) {
+		jn_walk_release(c);
+		return s;
+	}
+	int per[3] = { 0, 0, 0 };
+	cudaError_t e = cudaFuncSetAttribute(jn_walk_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WALK_SMEM);
+	if (e == cudaSuccess) e = cudaFuncSetAttribute(jn_walk_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WALK_SMEM);
+	if (e == cudaSuccess) e = cudaFuncSetAttribute(jn_walk_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WALK_SMEM);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[0], jn_walk_kernel<32>, WALK_THREADS, WALK_SMEM);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[1], jn_walk_kernel<64>, WALK_THREADS, WALK_SMEM);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[2], jn_walk_kernel<1>, WALK_THREADS, WALK_SMEM);
+	if (e != cudaSuccess) {
+		jn_walk_release(c);
+		return jn_fail(JN_ERR_CUDA, "walk kernel set-up: %s", cudaGetErrorString(e));
+	}
+	for (int i = 0; i < 3; i++) {
+		if (per[i] < 1) {
+			jn_walk_release(c);
+			return jn_fail(JN_ERR_CUDA, "the walk kernel does not fit on an SM");
+		}
+		c->walk_per_sm[i] = per[i];
+	}
+	c->walk_ready = 1;
+	return JN_OK;
+}
+
+/* the walk element array of the current matrix elements for one arithmetic
+ * (built on first use and after the matrix elements change): FP64 on the
+ * host (the plan's elements plus the transposed blocks), converted on the
+ * device for FP32 and for the integer path */
+static jn_status walk_elements(jn_ctx *c, int mode)
+{
+	const jn_plan_t *p = &c->plan;
+	const int slot = walk_slot(mode);
+	if (c->d_welem[slot]) return JN_OK;
+	const int64_t n = p->n_wme;
+	if (!c->d_welem[1]) {
+		double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
+		if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
+		jn_walk_elements(p, p->me, h);
+		double *d = NULL;
+		jn_status s = wupload(&d, h, (size_t)n);
+		free(h);
+		if (s) return s;
+		c->d_welem[1] = d;
+	}
+	if (mode == 64) return JN_OK;
+	const double *a = (const double *)c->d_welem[1];
+	cudaError_t e = cudaMalloc(&c->d_welem[slot], (size_t)(n ? n : 1) * (mode == 32 ? sizeof(float) : sizeof(int2)));
+	if (e != cudaSuccess) {
+		c->d_welem[slot] = NULL;
+		return jn_fail(JN_ERR_NOMEM, "cudaMalloc of %lld walk matrix elements: %s", (long long)n, cudaGetErrorString(e));
+	}
+	const int g = (int)(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
+	if (mode == 1) {
+		/* the coefficient exponent Sc from max|A| over the whole array */
+		unsigned long long *d_amax = NULL, h_amax = 0;
+		CUDA_TRY(cudaMalloc(&d_amax, sizeof(unsigned long long)));
+		e = cudaMemsetAsync(d_amax, 0, sizeof(unsigned long long), c->stream);
+		if (e == cudaSuccess && n) {
+			jn_walk_amax_kernel<<<g, 256, 0, c->stream>>>(a, n, d_amax);
+			e = cudaGetLastError();
+		}
+		if (e == cudaSuccess) e = cudaMemcpyAsync(&h_amax, d_amax, sizeof h_amax, cudaMemcpyDeviceToHost, c->stream);
+		if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+		cudaFree(d_amax);
+		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk element maximum: %s", cudaGetErrorString(e));
+		double amax;
+		memcpy(&amax, &h_amax, sizeof amax);
+		int ec = 0;
+		if (amax > 0.0) frexp(amax, &ec);       /* amax < 2^ec */
+		c->walk_sc = amax > 0.0 ? 52 - ec : 0;
+		if (n) jn_walk_convert_kernel<1><<<g, 256, 0, c->stream>>>(a, n, (int2 *)c->d_welem[slot], c->walk_sc);
+	} else if (n) {
+		jn_walk_convert_kernel<32><<<g, 256, 0, c->stream>>>(a, n, (float *)c->d_welem[slot], 0);
+	}
+	e = cudaGetLastError();
+	if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk matrix elements: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+/* y (+)= H x on the walk engine: max|x| (and the converted copy of x), the
+ * walk kernel, the conversion of the accumulator into y */
+jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
+			  cudaEvent_t mid)
+{
+	const jn_plan_t *p = &c->plan;
+	jn_status s = jn_walk_setup(c);
+	const int mode = walk_mode(c);
+	if (!s) s = walk_elements(c, mode);
+	if (s) return s;
+	int g = (int)((p->dim + 255) / 256);
+	if (g > 1024) g = 1024;
+	if (g < 1) g = 1;
+	CUDA_TRY(cudaMemsetAsync(c->d_xmax, 0, 2 * sizeof(unsigned int), st));
+	if (p->dim) {
+		jn_launch_prep(d_x, mode == 32 ? (float *)c->d_wx : NULL, p->dim, c->d_xmax, st);
+		if (mode == 1) jn_walk_xsplit_kernel<<<g, 256, 0, st>>>(d_x, c->d_wx, p->dim, c->d_xmax);
+	}
+	if (pre) cudaEventRecord(pre, st);
+	if (p->nwtasks) {
+		const int grid = c->num_sms * c->walk_per_sm[walk_slot(mode)];
+		const uint4 *T = (const uint4 *)c->d_wtasks, *P = (const uint4 *)c->d_wpieces;
+		if (mode == 32)
+			jn_walk_kernel<32><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const float *)c->d_welem[0],
+				(const float *)c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+		else if (mode == 64)
+			jn_walk_kernel<64><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const double *)c->d_welem[1],
+				d_x, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+		else
+			jn_walk_kernel<1><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const int2 *)c->d_welem[2],
+				c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc, c->num_sms);
+	}
+	if (mid) cudaEventRecord(mid, st);
+	if (p->dim) jn_walk_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, c->d_xmax, p->abs_bound, c->walk_sc, mode,
+								accumulate);
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk product launch: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
+extern "C" jn_status jn_set_walk_arithmetic(jn_ctx *c, int fp64_fma)
+{
+	if (!c) return jn_fail(JN_ERR_INVALID, "null argument");
+	if (fp64_fma != 0 && fp64_fma != 1) return jn_fail(JN_ERR_INVALID, "walk arithmetic %d: must be 0 (exact integers) or 1 (FP64)", fp64_fma);
+	c->walk_fp64 = fp64_fma;
+	return JN_OK;
+}
+
+extern "C" jn_status jn_walk_stats(jn_ctx *c, double *out)
+{
+	if (!c || !out) return jn_fail(JN_ERR_INVALID, "null argument");
+	jn_status s = jn_walk_setup(c);
+	if (s) return s;
+	const jn_plan_t *p = &c->plan;
+	out[0] = (double)p->nwtasks;
+	out[1] = (double)p->nwpieces;
+	out[2] = (double)p->n_wgroups;
+	out[3] = p->wvisits;
+	out[4] = p->wlane_slots;
+	out[5] = (double)p->n_wme;
+	out[6] = (double)(c->num_sms * c->walk_per_sm[walk_slot(walk_mode(c))]);
+	return JN_OK;
+}

@@ -28,6 +28,13 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference tree the recipes under oracle/ compile from: JNCSM_REFERENCE, else the Makefile's default
+REFERENCE = os.environ.get("JNCSM_REFERENCE", "/root/reference")
+
+
+def reference_tree_present():
+    return os.path.isdir(os.path.join(REFERENCE, "src"))
+
 PORT_LIB = os.path.join(HERE, "_build", "libminerva_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_minerva.so")
 REF_MERCURY = os.path.join(HERE, "_ref", "ref_mercury")
@@ -35,7 +42,7 @@ REF_MERCURY3 = os.path.join(HERE, "_ref", "ref_mercury3")
 
 
 def build():
-    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "all", f"REFERENCE={REFERENCE}"], check=True)
 
 
 REF_TOOLS = {name: os.path.join(HERE, "_ref", name) for name in ("aurora", "mars", "vulcan")}

@@ -21,10 +21,8 @@ def _ensure_built():
         jn.build()
     if not os.path.exists(oracle.PORT_LIB):
         subprocess.run(["make", "-s", "-C", oracle.HERE, "port"], check=True)
-    if os.path.isdir("/root/reference/src") and not os.path.exists(oracle.REF_LIB):
-        subprocess.run(["make", "-s", "-C", oracle.HERE, "ref"], check=True)
-    if os.path.isdir("/root/reference/src") and not os.path.exists(oracle.REF_MERCURY):
-        subprocess.run(["make", "-s", "-C", oracle.HERE, "ref"], check=True)
+    if oracle.reference_tree_present() and not (os.path.exists(oracle.REF_LIB) and os.path.exists(oracle.REF_MERCURY)):
+        subprocess.run(["make", "-s", "-C", oracle.HERE, "ref", f"REFERENCE={oracle.REFERENCE}"], check=True)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "tests", "native")], check=True)
 
 
@@ -37,6 +35,8 @@ PROBLEMS = {
     "he4_n4_2b": (2, 2, 4, 2, 0),
     "li6_n2_3b": (3, 3, 2, 3, 2),
     "he4_n6_3b": (2, 2, 6, 3, 0),
+    # 6Li Nmax 6, 2M = 2, two- plus three-body: D = 186 894, 2.26 G multiply-adds per product
+    "li6_n6_3b": (3, 3, 6, 3, 2),
 }
 
 
@@ -90,4 +90,5 @@ def jproblem(problem_root):
 
 
 def reference_tree_present():
-    return os.path.isdir("/root/reference/src")
+    import oracle
+    return oracle.reference_tree_present()

@@ -467,3 +467,191 @@ int emu_panel_wavefronts(void *h, int by_out, double *out)
 	free(meta); free(seen); free(at);
 	return bad;
 }
+
+/* ------------------------------------------------------------------ */
+/* walk engine: CPU model of jn_walk_kernel (jn_walk.cu), task by task,
+ * lane by lane, with every index checked.  mode 32: FP32 coefficients and
+ * x, fused multiply-adds in entry order, the row sum rounded once to the
+ * fixed-point unit; mode 64: the same in FP64; mode 1: the exact integer
+ * path (52-bit fixed-point coefficients and x split into 28 + 24 bits,
+ * three 32 x 32 -> 64-bit products per multiply-add, the row sum rounded
+ * once to the nearest output unit).  Returns 1 when an index leaves its buffer. */
+static int walk_x_exponent52(float xmax)
+{
+	uint32_t b;
+	memcpy(&b, &xmax, 4);
+	if (!(b & 0x7fffffffu)) return 0;
+	return 52 - ((int)((b >> 23) & 0xff) - 126);
+}
+
+int emu_walk_build(void *h)
+{
+	char err[512];
+	jn_plan_t *P = h;
+	if (P->wtasks) return 0;
+	if (jn_walk_build(P, err, sizeof err)) { fprintf(stderr, "walk plan: %s\n", err); return 1; }
+	return 0;
+}
+
+/* {tasks, pieces, groups, multiply-adds with padding, row words, lane slots x rows, walk elements,
+ * multiply-adds of the product} */
+void emu_walk_stats(void *h, double *out)
+{
+	jn_plan_t *P = h;
+	memset(out, 0, 8 * sizeof(double));
+	if (emu_walk_build(h)) return;
+	out[7] = P->visits;
+	out[0] = (double)P->nwtasks; out[1] = (double)P->nwpieces; out[2] = (double)P->n_wgroups; out[3] = P->wvisits;
+	out[4] = (double)P->n_wrows; out[5] = P->wlane_slots; out[6] = (double)P->n_wme;
+}
+
+int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
+{
+	jn_plan_t *P = h;
+	if (emu_walk_build(h)) return 1;
+	const int64_t D = P->dim, nm = P->n_wme;
+	float xmax = 0;
+	for (int64_t i = 0; i < D; i++) {
+		float v = (float)fabs(x[i]) * 1.0000002f;
+		if (v > xmax) xmax = v;
+	}
+	float *x32 = malloc((D ? D : 1) * sizeof(float)), *a32 = malloc((nm ? nm : 1) * sizeof(float));
+	int32_t *xh = malloc((D ? D : 1) * sizeof(int32_t)), *xl = malloc((D ? D : 1) * sizeof(int32_t));
+	double *a64 = malloc((nm ? nm : 1) * sizeof(double));
+	int32_t *ah = malloc((nm ? nm : 1) * sizeof(int32_t)), *al = malloc((nm ? nm : 1) * sizeof(int32_t));
+	int64_t *gacc = calloc(D ? D : 1, sizeof(int64_t));
+	const int Sx = walk_x_exponent52(xmax);
+	for (int64_t i = 0; i < D; i++) {
+		x32[i] = (float)x[i];
+		int64_t v = llrint(ldexp(x[i], Sx));
+		xh[i] = (int32_t)(v >> 24);
+		xl[i] = (int32_t)(v & 0xffffff);
+	}
+	jn_walk_elements(P, P->me, a64);
+	double amax = 0.0;
+	for (int64_t e = 0; e < nm; e++) amax = fmax(amax, fabs(a64[e]));
+	int ec = 0;
+	if (amax > 0.0) frexp(amax, &ec);
+	const int Sc = amax > 0.0 ? 52 - ec : 0;
+	for (int64_t e = 0; e < nm; e++) {
+		a32[e] = (float)a64[e];
+		int64_t v = llrint(ldexp(a64[e], Sc));
+		ah[e] = (int32_t)(v >> 24);
+		al[e] = (int32_t)(v & 0xffffff);
+	}
+	int S = fixed_exponent(xmax, P->abs_bound), sh = 0;
+	if (mode == 1) {
+		if (Sc + Sx - S < 48) S = Sc + Sx - 48;
+		sh = Sc + Sx - S - 48;
+		if (sh > 63) sh = 63;
+	}
+	const float scalef = (float)ldexp(1.0, S);
+	const double scale = ldexp(1.0, S);
+	int bad = 0;
+	int64_t *slot = calloc(JN_WALK_RS * 32, sizeof(int64_t));
+	for (int64_t t = 0; t < P->nwtasks && !bad; t++) {
+		const jn_wtask_t *T = &P->wtasks[t];
+		if (T->piece >= P->nwpieces) { bad = 1; break; }
+		const jn_wpiece_t *pc = &P->wpieces[T->piece];
+		const int U = (int)((T->meta >> 8) & 0xff), nw = (int)(T->meta & 0xff), LW = JN_WALK_LANE_WORDS(U);
+		const int rs = (int)(pc->meta & 0xff), wp = (int)((pc->meta >> 8) & 1), ng = (int)(pc->meta >> 9);
+		if ((U != 8 && U != 4 && U != 2) || (int64_t)T->lanes + 32 * LW > P->n_wlanes ||
+		    (int64_t)T->walk0 + nw > P->n_wwalks || nw < 1 || nw > 32 || rs < 1 || rs > JN_WALK_RS ||
+		    (int64_t)pc->rdst0 + rs > P->n_wrdst || (int64_t)pc->group0 + ng > P->n_wgroups) { bad = 1; break; }
+		memset(slot, 0, JN_WALK_RS * 32 * sizeof(int64_t));
+		for (int lane = 0; lane < 32 && !bad; lane++) {
+			const uint32_t ws = P->wlanes[T->lanes + lane];
+			if (ws >= (uint32_t)nw) { bad = 1; break; }
+			uint32_t src[8], ko[8];
+			for (int k = 0; k < U / 2; k++) {
+				const uint32_t w = P->wlanes[T->lanes + (1 + k) * 32 + lane];
+				src[2 * k] = w & 0xffffu;
+				src[2 * k + 1] = w >> 16;
+			}
+			for (int u = 0; u < U; u++) ko[u] = P->wlanes[T->lanes + (1 + U / 2 + u) * 32 + lane];
+			int64_t j = pc->row0;
+			for (int g = 0; g < ng && !bad; g++) {
+				const int64_t gb = P->wgroups[pc->group0 + g];
+				int64_t ai[8];
+				for (int u = 0; u < U; u++) {
+					ai[u] = gb + (ko[u] & 0x3fffffffu);
+					if (ai[u] >= nm) { bad = 1; break; }
+				}
+				for (;;) {
+					if (bad || j >= P->n_wrows) { bad = 1; break; }
+					const uint32_t row = P->wrows[j++];
+					const uint32_t sr = row & 0xffffu, rslot = (row >> 16) & 31u;
+					if (rslot >= (uint32_t)rs) { bad = 1; break; }
+					int64_t v = 0;
+					int64_t A = 0, B = 0;
+					float accf = 0.0f;
+					double accd = 0.0;
+					for (int u = 0; u < U; u++) {
+						const int64_t xi = pc->src_off + (wp ? (int64_t)src[u] * pc->Nn_src + sr : (int64_t)sr * pc->Nn_src + src[u]);
+						if (xi < 0 || xi >= D) { bad = 1; break; }
+						const int pad = (ko[u] & JN_WALK_PADBIT) != 0, neg = (ko[u] >> 31) != 0;
+						if (mode == 1) {
+							int32_t ch = pad ? 0 : ah[ai[u]], cl = pad ? 0 : al[ai[u]];
+							if (neg) { ch = -ch; cl = -cl; }
+							A += (int64_t)ch * xh[xi];
+							B += (int64_t)ch * xl[xi] + (int64_t)cl * xh[xi];
+						} else if (mode == 32) {
+							float c = pad ? 0.0f : a32[ai[u]];
+							if (neg) c = -c;
+							accf = fmaf(c, x32[xi], accf);
+						} else {
+							double c = pad ? 0.0 : a64[ai[u]];
+							if (neg) c = -c;
+							accd = fma(c, x[xi], accd);
+						}
+					}
+					if (mode == 1) {
+						const int64_t q = A + (B >> 24);
+						v = sh ? (q + ((int64_t)1 << (sh - 1))) >> sh : q + ((B >> 23) & 1);
+						if (row >> 31) v = -v;
+					} else if (mode == 32) {
+						v = llrintf(accf * ((row >> 31) ? -scalef : scalef));
+					} else {
+						v = llrint(accd * ((row >> 31) ? -scale : scale));
+					}
+					slot[rslot * 32 + ws] = (int64_t)((uint64_t)slot[rslot * 32 + ws] + (uint64_t)v);
+					if (row & JN_WALK_GROUP_END) break;
+				}
+			}
+		}
+		for (int r = 0; r < rs && !bad; r++)
+			for (int w = 0; w < nw; w++) {
+				const uint32_t dr = P->wrdst[pc->rdst0 + r], dw = P->wwalks[T->walk0 + w];
+				const int64_t yi = pc->dst_off + (wp ? (int64_t)dw * pc->Nn_dst + dr : (int64_t)dr * pc->Nn_dst + dw);
+				if (yi < 0 || yi >= D) { bad = 1; break; }
+				gacc[yi] = (int64_t)((uint64_t)gacc[yi] + (uint64_t)slot[r * 32 + w]);
+			}
+	}
+	const double unit = ldexp(1.0, -S);
+	for (int64_t i = 0; i < D; i++) y[i] = accumulate ? y[i] + (double)gacc[i] * unit : (double)gacc[i] * unit;
+	free(slot); free(x32); free(a32); free(xh); free(xl); free(a64); free(ah); free(al); free(gacc);
+	return bad;
+}
+
+/* shape of the walk plan by chunk width U = 8, 4, 2: {tasks, rows x tasks,
+ * groups x tasks, padded multiply-adds} for each, then slot flushes x tasks */
+void emu_walk_shape(void *h, double *out)
+{
+	jn_plan_t *P = h;
+	memset(out, 0, 13 * sizeof(double));
+	if (emu_walk_build(h)) return;
+	for (int64_t t = 0; t < P->nwtasks; t++) {
+		const jn_wtask_t *T = &P->wtasks[t];
+		const jn_wpiece_t *pc = &P->wpieces[T->piece];
+		const int U = (int)((T->meta >> 8) & 0xff), k = U == 8 ? 0 : (U == 4 ? 1 : 2);
+		const int ng = (int)(pc->meta >> 9), rs = (int)(pc->meta & 0xff), nw = (int)(T->meta & 0xff);
+		int64_t nrows = 0, j = pc->row0;
+		for (int g = 0; g < ng; g++)
+			for (;;) { nrows++; if (P->wrows[j++] & JN_WALK_GROUP_END) break; }
+		out[4 * k] += 1;
+		out[4 * k + 1] += (double)nrows;
+		out[4 * k + 2] += ng;
+		out[4 * k + 3] += (double)nrows * 32 * U;
+		out[12] += (double)rs * nw;
+	}
+}
