@@ -1,11 +1,16 @@
 """Benchmark: index-list matvec GB/s on one GB300 (and N independent replicas).
 
 A step is one Hamiltonian product y = H x of the JupiterNCSM hot path on the
-workload below, with x, y, the index lists and the matrix elements already
-resident in HBM.  `value` is the algorithmic traffic of one product (index
-lists in the reference's 12-byte format, the matrix elements they reference,
-x read and y written) times the steps of all ranks, divided by the CUDA-event
-time of the slowest rank.  L2 is flushed (256 MiB write) between timed steps.
+workload below (default: 6Li Nmax 6, 2M = 2, two- plus three-body forces,
+D = 186 894, the largest single-GPU configuration), with x, y, the index
+lists and the matrix elements already resident in HBM.  `value` is the
+algorithmic traffic of one product in the reference's FP64 terms (index
+lists in the reference's 12-byte format, the 8-byte matrix elements they
+reference, x read and y written) times the steps of all ranks, divided by
+the CUDA-event time of the slowest rank.  L2 is flushed (256 MiB write)
+between timed steps.  The headline arithmetic is the walk engine's exact
+integer product (`dtype` "i64"); its error against the CPU reference is
+reported beside the FP64-FMA and FP32 paths'.
 
 `e2e` is the same metric through the public C ABI call jn_matvec with host
 buffers in pinned memory: host->device copy of x and y and device->host copy
@@ -14,7 +19,7 @@ of y inside the timed region of every step.
 `--impl reference` times the reference's CPU algorithm (OpenMP task farm over
 the evaluation order with per-thread output replicas) on the host cores: the
 compiled reference where it was built on this machine, else the oracle's
-plain-C restatement of it.
+plain-C restatement of it, with the same byte formula.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -32,7 +37,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # the A=4 configuration the matvec metric is quoted on: Nmax=6, two- plus three-body forces
+    # the largest single-GPU configuration: A=6 Nmax=6 with two- and three-body forces
+    "li6_nmax6_2nf3nf": dict(Z=3, N=3, nmax=6, nbody=3, M2=2,
+                             label="6Li (Z=3,N=3) HO M-scheme Nmax=6, 2M=2, +parity, seeded 2NF N(0,1) + 3NF N(0,0.1) "
+                                   "MeV, hw=20 MeV"),
+    # the A=4 Nmax=6 configuration with two- plus three-body forces
     "he4_nmax6_2nf3nf": dict(Z=2, N=2, nmax=6, nbody=3, M2=0,
                              label="4He (Z=2,N=2) HO M-scheme Nmax=6, 2M=0, +parity, seeded 2NF N(0,1) + 3NF N(0,0.1) MeV, hw=20 MeV"),
     "he4_nmax4_2nf": dict(Z=2, N=2, nmax=4, nbody=2, M2=0,
@@ -40,6 +49,8 @@ WORKLOADS = {
     "li6_nmax6_2nf": dict(Z=3, N=3, nmax=6, nbody=2, M2=2,
                           label="6Li (Z=3,N=3) HO M-scheme Nmax=6, 2M=2, +parity, seeded 2NF N(0,1) MeV, hw=20 MeV"),
 }
+# product arithmetics: precision, FP64 FMAs on the walk engine
+ARITH = {"i64": (64, False), "fp64": (64, True), "f32": (32, False)}
 METRIC = "index-list matvec GB/s vs HBM peak"
 FLUSH_BYTES = 256 << 20
 
@@ -55,19 +66,20 @@ def measured_peaks():
         return None
 
 
-KERNELS = {(4, 32): "jn_panel_kernel_i32", (4, 64): "jn_panel_kernel_fp64",
-           (3, 32): "jn_tile_kernel<float>", (3, 64): "jn_tile_kernel<double>"}
-# kernels launched per product: max|x| (with the panel engine's copies of x), the product, the conversion into y
-LAUNCHES = {4: 3, 3: 3, 2: 3}
+KERNELS = {(4, "f32"): "jn_panel_kernel_i32", (4, "i64"): "jn_panel_kernel_fp64", (4, "fp64"): "jn_panel_kernel_fp64",
+           (3, "f32"): "jn_tile_kernel<float>", (3, "i64"): "jn_tile_kernel<double>", (3, "fp64"): "jn_tile_kernel<double>",
+           (5, "i64"): "jn_walk_kernel<1>", (5, "fp64"): "jn_walk_kernel<64>", (5, "f32"): "jn_walk_kernel<32>"}
+# kernels launched per product: max|x| (and the copies of x), the product, the conversion into y; the walk
+# engine's integer path converts x in a kernel of its own
+LAUNCHES = {(5, "i64"): 4}
 
 
-def profile_traffic(workload, engine, precision):
+def profile_traffic(workload, engine, arith):
     """DRAM bytes (read + write) per launch of the product kernel from the committed ncu summary, if any."""
-    name = "jn_panel_kernel" if engine == 4 else "jn_tile_kernel"
-    key = ("i32" if precision == 32 else "fp64") if engine == 4 else f"fp{precision}"
+    name = {4: "jn_panel_kernel", 3: "jn_tile_kernel", 5: "jn_walk_kernel"}[engine]
     path = os.path.join(ROOT, "profiles", f"{name}_{workload}.md")
     try:
-        m = re.search(rf"dram_bytes_per_launch_{key}:\s*([0-9.eE+]+)", open(path).read())
+        m = re.search(rf"dram_bytes_per_launch_{arith}:\s*([0-9.eE+]+)", open(path).read())
         return float(m.group(1)) if m else None
     except OSError:
         return None
@@ -299,59 +311,34 @@ def transform3_leg(workdir, steps, warmup, flush, peak):
             "l2": "flushed between timed runs (256 MiB write)", "steps": steps, "warmup": warmup}
 
 
-def large_basis_leg(workdir, steps, warmup, flush, peak):
-    """6Li Nmax=6, 2M=2 (D = 186 894): the two-body interaction comes from the
-    GPU J -> M transform (the transform leg's output files) and feeds the
-    product and the Lanczos solves: one FP32-product mixed-precision solve
-    and one plain FP64 solve, 300 iterations at most, 10 lowest eigenvalues."""
-    import torch
+def large_solve_leg(H, kernel_ms, max_iterations=300, check_every=10):
+    """Lanczos on the headline Hamiltonian (6Li Nmax 6, two- plus three-body,
+    D = 186 894), 10 lowest eigenvalues to 1e-6 MeV, 300 iterations at most:
+    plain FP64-grade (exact-integer products) against mixed precision (FP32
+    products, FP64 recurrence, full reorthogonalisation and an FP64-grade
+    Rayleigh-Ritz refinement), both checking convergence every 10 steps.  The
+    time per step beside the product kernel's time shows what the rest of a
+    step costs."""
     import numpy as np
-    import jupiterncsm_gb300 as jn
-    w = TRANSFORM_WORKLOAD
-    d = os.path.join(workdir, "li6_nmax6_jscheme")
-    mes = os.path.join(d, "transformed")
-    H = jn.Hamiltonian(comb=f"{d}/comb.txt", order=f"{d}/evaluation_order.txt", lists=f"{d}/index_lists", mes=mes,
-                       Z=w["Z"], N=w["N"])
-    try:
-        st = H.stats()
-        D = H.dimension
-        dev = torch.device("cuda", torch.cuda.current_device())
-        x = torch.randn(D, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(11))
-        y = torch.zeros(D, dtype=torch.float64, device=dev)
-        paths = {}
-        for prec in (32, 64):
-            H.set_precision(prec)
-            for _ in range(warmup):
-                H.matvec_profile(x.data_ptr(), y.data_ptr())
-            ks = []
-            for _ in range(steps):
-                flush.zero_()
-                torch.cuda.synchronize()
-                ks.append(H.matvec_profile(x.data_ptr(), y.data_ptr())[0])
-            kms = sum(ks) / len(ks)
-            b = 12.0 * st["list_entries"] + (4 if prec == 32 else 8) * st["me_referenced"] + 16.0 * D
-            paths["i32" if prec == 32 else "fp64"] = {
-                "engine": H.active_engine(), "product_kernel_ms": kms, "GB_per_s": b / (kms / 1e3) / 1e9,
-                "hbm_frac": b / (kms / 1e3) / 1e9 / peak, "multiply_adds_per_s": st["multiply_adds"] / (kms / 1e3)}
-        me = H.read_matrix_elements(mes)
+    out = {}
+    for name, prec in (("plain_fp64_grade", 64), ("mixed_fp32_products", 32)):
+        H.set_precision(prec)
+        H.set_walk_arithmetic(False)
         t0 = time.perf_counter()
-        mixed = H.lanczos_batch([me], max_iterations=300, num_eigenvalues=10, tolerance=1e-6, precision=32)[0]
-        t1 = time.perf_counter()
-        H.set_precision(64)
-        plain = H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, allow_unconverged=True)
-        t2 = time.perf_counter()
-    finally:
-        H.close()
-    return {"workload": "6Li (Z=3,N=3) Nmax=6, 2M=2, two-body interaction from the GPU J->M transform of a seeded "
-                        "J-scheme file", "dimension": int(D), "instructions": st["num_instructions"],
-            "list_entries": st["list_entries"], "me_referenced": st["me_referenced"],
-            "multiply_adds": st["multiply_adds"], "paths": paths,
-            "solve": {"mixed_seconds": t1 - t0, "mixed_iterations": mixed["iterations"],
-                      "mixed_converged": mixed["converged"], "plain_fp64_seconds": t2 - t1,
-                      "plain_fp64_iterations": plain["iterations"], "plain_fp64_converged": plain["converged"],
-                      "max_eigenvalue_diff_MeV": float(np.abs(mixed["eigenvalues"] - plain["eigenvalues"]).max()),
-                      "lowest_eigenvalues_MeV": [float(v) for v in plain["eigenvalues"][:3]]},
-            "l2": "flushed between timed products (256 MiB write)"}
+        r = H.lanczos(max_iterations=max_iterations, num_eigenvalues=10, tolerance=1e-6, check_every=check_every,
+                      allow_unconverged=True)
+        sec = time.perf_counter() - t0
+        out[name] = {"seconds": sec, "iterations": r["iterations"], "converged": r["converged"],
+                     "ms_per_step": 1e3 * sec / max(r["iterations"], 1),
+                     "product_kernel_ms": kernel_ms["i64" if prec == 64 else "f32"],
+                     "eigenvalues_MeV": [float(v) for v in r["eigenvalues"]]}
+    a = np.array(out["plain_fp64_grade"]["eigenvalues_MeV"])
+    b = np.array(out["mixed_fp32_products"]["eigenvalues_MeV"])
+    n = min(len(a), len(b))
+    out["max_eigenvalue_diff_MeV"] = float(np.abs(a[:n] - b[:n]).max()) if n else None
+    out["check_every"] = check_every
+    out["workload"] = "the headline Hamiltonian, 10 lowest eigenvalues to 1e-6 MeV"
+    return out
 
 
 SOLVE_FAMILY = [  # (label, Z, N, Nmax, 2M): the bases of the batched-Hamiltonian workload
@@ -363,16 +350,19 @@ SOLVE_COUPLINGS = 4
 def solves_leg(workdir, seed=20261203):
     """Lanczos solves/s: 64 Hamiltonians H(c) = H0 + sum_{i=1..4} c_i H_i, c_i ~ U(-1,1),
     16 on each of four bases, to 1e-6 MeV on the 10 lowest eigenvalues.
-    Plain: one FP64 Lanczos (full reorthogonalisation, FP64 products) after
-    another.  Batched: one call per basis, all its instances together, FP32
-    products, FP64 recurrence and FP64 Rayleigh-Ritz refinement, one captured
-    CUDA graph per step.  Both start from the same vector; the error of every
-    batched eigenvalue is measured against the plain FP64 solve."""
+    Plain: FP64 Lanczos (full reorthogonalisation, FP64 products) one
+    Hamiltonian after another, with the same convergence-check interval (10
+    steps) and the same captured-graph step as the batched solver (a batch of
+    one at precision 64); the plain solver that synchronises with the host
+    every step is timed beside it.  Batched: one call per basis, all its
+    instances together, FP32 products, FP64 recurrence and FP64 Rayleigh-Ritz
+    refinement.  All start from the same vector; the error of every batched
+    eigenvalue is measured against the plain FP64 solve."""
     import numpy as np
     import jupiterncsm_gb300 as jn
     rng = np.random.default_rng(seed)
     per = SOLVE_INSTANCES // len(SOLVE_FAMILY)
-    plain_s = batch_s = 0.0
+    plain_s = sync_s = batch_s = 0.0
     worst = 0.0
     iters_plain, iters_batch = [], []
     details = []
@@ -384,38 +374,48 @@ def solves_leg(workdir, seed=20261203):
         cs = rng.uniform(-1.0, 1.0, size=(per, SOLVE_COUPLINGS))
         mes = [comps[0] + sum(c[i] * comps[i + 1] for i in range(SOLVE_COUPLINGS)) for c in cs]
         start = np.random.default_rng(seed + bi).standard_normal(H.dimension)
-        # plain FP64, sequential
+        # plain FP64, sequential, graph-replayed steps, convergence checked every 10 steps
+        H.lanczos_batch(mes[:1], start_vectors=[start], max_iterations=300, num_eigenvalues=10, tolerance=1e-6,
+                        precision=64, check_every=10, use_graph=True)     # warm-up: graph and buffers
         plain = []
         t0 = time.perf_counter()
         for me in mes:
-            H.set_matrix_elements(me)
-            plain.append(H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, start_vector=start,
-                                   allow_unconverged=True))
+            plain += H.lanczos_batch([me], start_vectors=[start], max_iterations=300, num_eigenvalues=10,
+                                     tolerance=1e-6, precision=64, check_every=10, use_graph=True)
         t1 = time.perf_counter()
+        # plain FP64 solver that checks (and synchronises with the host) every step, for reference
+        for me in mes[:4]:
+            H.set_matrix_elements(me)
+            H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, start_vector=start,
+                      allow_unconverged=True)
+        t2 = time.perf_counter()
         # batched mixed precision
         res = H.lanczos_batch(mes, start_vectors=[start] * per, max_iterations=300, num_eigenvalues=10,
                               tolerance=1e-6, precision=32, check_every=10, use_graph=True)
-        t2 = time.perf_counter()
+        t3 = time.perf_counter()
         H.close()
         plain_s += t1 - t0
-        batch_s += t2 - t1
+        sync_s += (t2 - t1) * per / 4
+        batch_s += t3 - t2
         err = max(float(np.abs(r["eigenvalues"] - p["eigenvalues"]).max()) for r, p in zip(res, plain))
         worst = max(worst, err)
         iters_plain += [p["iterations"] for p in plain]
         iters_batch += [r["iterations"] for r in res]
         details.append({"basis": label, "dimension": int(len(start)), "instances": per,
-                        "plain_s": t1 - t0, "batched_s": t2 - t1, "max_eigenvalue_diff_MeV": err,
+                        "plain_s": t1 - t0, "batched_s": t3 - t2, "max_eigenvalue_diff_MeV": err,
                         "all_converged": all(r["converged"] for r in res) and all(p["converged"] for p in plain)})
     return {"metric": "Lanczos solves/s at 1e-6 MeV (10 lowest) vs plain FP64",
             "workload": f"{SOLVE_INSTANCES} H(c)=H0+sum_{{i=1..{SOLVE_COUPLINGS}}} c_i H_i, c~U(-1,1), "
                         f"{per} on each of " + ", ".join(f[0] for f in SOLVE_FAMILY) + " (two-body, seeded)",
             "batched_solves_per_s": SOLVE_INSTANCES / batch_s, "plain_fp64_solves_per_s": SOLVE_INSTANCES / plain_s,
             "speedup": plain_s / batch_s, "batched_seconds": batch_s, "plain_seconds": plain_s,
+            "plain_fp64_per_step_sync_solves_per_s": SOLVE_INSTANCES / sync_s,
             "max_eigenvalue_diff_vs_plain_fp64_MeV": worst,
             "mean_iterations": {"plain": float(np.mean(iters_plain)), "batched": float(np.mean(iters_batch))},
             "batched": "FP32 products, FP64 recurrence + full reorthogonalisation + Rayleigh-Ritz refinement, "
                        "CUDA graph per step, convergence checked every 10 steps",
-            "plain": "jn_lanczos full mode, FP64 products, convergence checked every step",
+            "plain": "FP64 products and recurrence, one Hamiltonian at a time, CUDA graph per step, convergence "
+                     "checked every 10 steps (a batch of one at precision 64)",
             "per_basis": details}
 
 
@@ -469,10 +469,14 @@ def warm_start_leg(workdir, seed=20261203, check_every=5):
         warm = H.lanczos_batch(test, start_vectors=starts, max_iterations=300, num_eigenvalues=10, tolerance=1e-6,
                                check_every=check_every)
         t5 = time.perf_counter()
+        # plain FP64, one Hamiltonian at a time, with the same check interval and graph replay
+        H.lanczos_batch(test[:1], max_iterations=300, num_eigenvalues=10, tolerance=1e-6, precision=64,
+                        check_every=check_every, use_graph=True)
+        t5 = time.perf_counter()
         plain = []
         for me in test[:WARM_PLAIN]:
-            H.set_matrix_elements(me)
-            plain.append(H.lanczos(max_iterations=300, num_eigenvalues=10, tolerance=1e-6, allow_unconverged=True))
+            plain += H.lanczos_batch([me], max_iterations=300, num_eigenvalues=10, tolerance=1e-6, precision=64,
+                                     check_every=check_every, use_graph=True)
         t6 = time.perf_counter()
         ws.close()
     finally:
@@ -495,12 +499,14 @@ def warm_start_leg(workdir, seed=20261203, check_every=5):
             "max_eigenvalue_diff_vs_plain_fp64_MeV": {"warm": err_w, "cold": err_c},
             "all_converged": all(r["converged"] for r in cold + warm),
             "check_every": check_every,
-            "note": "warm time includes computing the start vectors; plain FP64 timed on "
+            "note": "warm time includes computing the start vectors; plain FP64 (one Hamiltonian at a time, "
+                    f"graph-replayed steps, convergence checked every {check_every} steps) timed on "
                     f"{WARM_PLAIN} of the held-out Hamiltonians"}
 
 
-def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
-    """The reference's CPU algorithm on all host threads over a time-bounded sample."""
+def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3, x=None):
+    """The reference's CPU algorithm on all host threads over a time-bounded
+    sample; with x, also its y = H x (the reference for the GPU paths' errors)."""
     import numpy as np
     import oracle
     threads = os.cpu_count() or 1
@@ -515,11 +521,12 @@ def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
     if impl is None:
         impl = oracle.Port(d)
     D = impl.dimension
-    x = np.random.default_rng(1).standard_normal(D)
+    x = np.random.default_rng(1).standard_normal(D) if x is None else x
     y = np.zeros(D)
     times = []
     t_end = time.perf_counter() + seconds
     while len(times) < min_steps or time.perf_counter() < t_end:
+        y[:] = 0.0
         if kind == "reference":
             impl.matvec(x, y)
             times.append(impl.seconds)
@@ -530,25 +537,25 @@ def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3):
     return {"value": bytes_per_step / per / 1e9, "unit": "GB/s", "cores": threads, "kind": kind,
             "sample": f"{len(times)} full products of the workload ({sum(times):.1f} s of CPU work), "
                       f"OpenMP task farm with per-thread replicas, {threads} threads",
-            "ms_per_step": per * 1e3}
+            "ms_per_step": per * 1e3}, y
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="he4_nmax6_2nf3nf", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="li6_nmax6_2nf3nf", choices=sorted(WORKLOADS))
     ap.add_argument("--workdir", default=os.environ.get("JNCSM_BENCH_DIR", os.path.join(tempfile.gettempdir(), "jncsm_bench")))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--precision", type=int, default=32, choices=[64, 32],
-                    help="32: 32-bit fixed-point matrix elements and x with exact 64-bit sums (the headline); 64: FP64")
-    ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform leg")
-    ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solves/s leg")
+    ap.add_argument("--arith", default="i64", choices=sorted(ARITH),
+                    help="the headline product: i64 exact integers (FP64-grade), fp64 FP64 FMAs, f32 FP32")
+    ap.add_argument("--no-transform", action="store_true", help="skip the J->M transform legs")
+    ap.add_argument("--no-solves", action="store_true", help="skip the Lanczos solve legs")
     ap.add_argument("--schedule", metavar="ROWS,CTAS",
-                    help="fix the panel schedule (rows per lane, CTAs per SM) instead of autotuning it, "
-                         "e.g. to profile the schedule a plain run chose")
+                    help="fix the panel schedule (rows per lane, CTAs per SM) instead of autotuning it "
+                         "(panel-engine workloads)")
     ap.add_argument("--leg", choices=["transform", "transform3"],
                     help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line)")
     args = ap.parse_args()
@@ -573,11 +580,12 @@ def main():
         import jupiterncsm_gb300 as jn
         d = prepare(args.workload, args.workdir)
         stats = algorithmic_stats(d, w)
-        cb = cpu_baseline(d, w, stats["bytes"], seconds=args.cpu_seconds)
+        cb, _ = cpu_baseline(d, w, stats["bytes"], seconds=args.cpu_seconds)
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": w["label"], "dimension": stats["dimension"], "threads": cb["cores"]},
+                "config": {"workload": w["label"], "dimension": stats["dimension"], "threads": cb["cores"],
+                           "bytes_per_step": stats["bytes"]},
                 "cpu_baseline": cb,
                 "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -595,26 +603,35 @@ def main():
         dist = tdist
     wd = os.path.join(args.workdir, f"rank{rank}") if world > 1 else args.workdir
     d = prepare(args.workload, wd)
+    t0 = time.perf_counter()
     H = jn.Hamiltonian.from_dir(d, w["Z"], w["N"])
+    open_s = time.perf_counter() - t0
     st = H.stats()
     D = H.dimension
     dev = torch.device("cuda", local)
     x = torch.randn(D, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
     y = torch.zeros(D, dtype=torch.float64, device=dev)
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    # bytes of one product: lists (12 B/entry), referenced matrix elements (8 or 4 B), x and y (FP64)
-    me_bytes = {64: 8, 32: 4}
+    engine = H.active_engine()
 
-    def bytes_for(prec):
-        return 12.0 * st["list_entries"] + me_bytes[prec] * st["me_referenced"] + 16.0 * D
+    # bytes of one product in the reference's FP64 terms: lists (12 B/entry), referenced matrix elements
+    # (8 B), x and y (FP64); the FP32 path moves 4-byte elements
+    def bytes_for(arith):
+        return 12.0 * st["list_entries"] + (4 if arith == "f32" else 8) * st["me_referenced"] + 16.0 * D
 
-    def timed(prec):
+    def set_arith(arith):
+        prec, fma = ARITH[arith]
+        H.set_precision(prec)
+        if engine == 5:
+            H.set_walk_arithmetic(fma)
+
+    def timed(arith):
         """K products, each preceded by the L2 flush, all enqueued on one stream
         without host synchronisation; each product is bracketed by CUDA events
-        on that stream, so a step is the device time of one product (its three
-        kernels and the gaps between them).  Then K profiled products (events
-        inside the product's graph) give the product kernel's own duration."""
-        H.set_precision(prec)
+        on that stream, so a step is the device time of one product (its
+        kernels and the gaps between them).  Then K profiled products give the
+        product kernel's own duration."""
+        set_arith(arith)
         s = torch.cuda.Stream(device=dev)
 
         def run_steps(k):
@@ -628,6 +645,10 @@ def main():
             return ev
 
         torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run_steps(1)            # builds the arithmetic's element arrays on first use
+        torch.cuda.synchronize()
+        setup_s = time.perf_counter() - t0
         run_steps(args.warmup)
         torch.cuda.synchronize()
         sampler = ClockSampler(local)
@@ -643,7 +664,6 @@ def main():
         wall = time.perf_counter() - wall0
         clocks = sampler.stop()
         total_ms = sum(a.elapsed_time(b) for a, b in ev)
-        # the product kernel alone: events inside the product's graph
         kern_ms, prof_total = 0.0, 0.0
         for _ in range(args.steps):
             flush.zero_()
@@ -657,26 +677,26 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             t_max = float(t.item())
         return {"ms_per_step": t_max / args.steps, "kernel_ms": kern_ms / args.steps, "wall_s": wall,
-                "profiled_ms_per_step": prof_total / args.steps, "clocks": clocks, "y": y.clone()}
+                "profiled_ms_per_step": prof_total / args.steps, "clocks": clocks, "setup_s": setup_s,
+                "y": y.cpu().numpy().copy()}
 
-    # the product's schedule is chosen by the library's autotuner at the headline precision
-    H.set_precision(args.precision)
-    if args.schedule:
-        rows, ctas = (int(v) for v in args.schedule.split(","))
-        H.set_panel_schedule(rows, ctas)
-        tuning = {"engine": 4, "rows_per_lane": rows, "ctas_per_sm": ctas, "ms": None, "candidates": 0, "fixed": True}
-    else:
-        tuning = H.autotune(trials=5)
-    r64 = timed(64)
-    r32 = timed(32)
-    rel32 = float((r32["y"] - r64["y"]).abs().max() / r64["y"].abs().max())
-    prec = args.precision
-    main_r = r64 if prec == 64 else r32
-    bytes_step = bytes_for(prec)
+    tuning = None
+    if engine == 4:
+        set_arith(args.arith)
+        if args.schedule:
+            rows, ctas = (int(v) for v in args.schedule.split(","))
+            H.set_panel_schedule(rows, ctas)
+            tuning = {"engine": 4, "rows_per_lane": rows, "ctas_per_sm": ctas, "fixed": True}
+        else:
+            tuning = H.autotune(trials=5)
+    order = [args.arith] + [a for a in ("i64", "fp64", "f32") if a != args.arith and (engine == 5 or a != "fp64")]
+    runs = {a: timed(a) for a in order}
+    main_r = runs[args.arith]
+    bytes_step = bytes_for("i64")                      # the reference's FP64 bytes, whatever the arithmetic
     value = bytes_step * world / (main_r["ms_per_step"] / 1e3) / 1e9
 
     # end to end through the public host-pointer call, pinned host buffers
-    H.set_precision(prec)
+    set_arith(args.arith)
     hx = torch.randn(D, dtype=torch.float64).pin_memory().numpy()
     hy = torch.zeros(D, dtype=torch.float64).pin_memory().numpy()
     for _ in range(args.warmup):
@@ -693,54 +713,67 @@ def main():
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = bytes_step / (main_r["kernel_ms"] / 1e3) / 1e9
-    engine = H.active_engine()
-    traffic = profile_traffic(args.workload, engine, prec)
+    traffic = profile_traffic(args.workload, engine, args.arith)
+    wstats = H.walk_stats() if engine == 5 else None
 
-    def path_summary(r, p):
-        b = bytes_for(p)
-        return {"ms_per_step": r["ms_per_step"], "GB_per_s": b / (r["ms_per_step"] / 1e3) / 1e9,
-                "bytes_per_step": b, "product_kernel_ms": r["kernel_ms"],
+    def path_summary(r, a):
+        return {"ms_per_step": r["ms_per_step"], "GB_per_s_fp64_bytes": bytes_step / (r["ms_per_step"] / 1e3) / 1e9,
+                "own_bytes_per_step": bytes_for(a), "product_kernel_ms": r["kernel_ms"],
                 "profiled_ms_per_step": r["profiled_ms_per_step"],
-                "hbm_frac": b / (r["kernel_ms"] / 1e3) / 1e9 / peak,
-                "fp64_multiply_adds_per_s" if p == 64 else "multiply_adds_per_s":
-                    st["multiply_adds"] / (r["kernel_ms"] / 1e3)}
+                "hbm_frac_fp64_bytes": bytes_step / (r["kernel_ms"] / 1e3) / 1e9 / peak,
+                "multiply_adds_per_s": st["multiply_adds"] / (r["kernel_ms"] / 1e3),
+                "first_product_setup_s": r["setup_s"]}
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": main_r["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == 64 else "i32",
-            "arithmetic": "FP64 products, exact 64-bit fixed-point sums" if prec == 64 else
-                          "32-bit fixed-point matrix elements and x, exact 64-bit products and sums; FP64 x and y at the interface",
+            "dtype": {"i64": "i64", "fp64": "f64", "f32": "f32"}[args.arith],
+            "arithmetic": {"i64": "exact integers: FP64 matrix elements (each block at its own exponent) and x as "
+                                  "52-bit fixed-point integers split 28+24 bits, three 32x32->64-bit integer "
+                                  "multiply-adds per contribution, exact sums, one rounding per row sum; FP64 x and "
+                                  "y at the interface; error against the CPU reference in paths",
+                           "fp64": "FP64 fused multiply-adds, one rounding per row sum into exact 64-bit sums",
+                           "f32": "FP32 matrix elements and x, FP32 fused multiply-adds, exact 64-bit sums"}[args.arith],
             "data": "synthetic",
             "config": {"workload": w["label"], "dimension": D, "instructions": st["num_instructions"],
                        "list_entries": st["list_entries"], "me_elements": st["me_elements"],
                        "me_elements_referenced": st["me_referenced"],
                        "multiply_adds": st["multiply_adds"], "bytes_per_step": bytes_step,
+                       "bytes_formula": "12 x list entries + 8 x referenced matrix elements + 16 x D (the reference arm's)",
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{world}",
                        "timing": "CUDA events on the product's stream around each product; flush and products "
                                  "enqueued without host synchronisation; the product kernel's duration from a "
-                                 "second pass with events inside the product's graph",
-                       "precision": prec, "schedule": tuning},
-            "paths": {"fp64": path_summary(r64, 64), "i32": path_summary(r32, 32),
-                      "i32_max_rel_diff_vs_fp64": rel32},
+                                 "second pass with events around the kernel",
+                       "engine": engine, "open_seconds": open_s, "schedule": tuning, "walk_plan": wstats},
+            "paths": {a: path_summary(runs[a], a) for a in order},
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * D, "d2h_bytes_per_step": 8 * D},
-            "gpu_launches": LAUNCHES.get(engine, 3) * args.steps,
+            "gpu_launches": LAUNCHES.get((engine, args.arith), 3) * args.steps,
             "engine": engine,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback 6.8 TB/s",
-                         "kernel": KERNELS.get((engine, prec))},
+                         "kernel": KERNELS.get((engine, args.arith))},
             "clocks": main_r["clocks"]}
+    if rank == 0:
+        try:
+            cb, y_ref = cpu_baseline(d, w, bytes_step, seconds=args.cpu_seconds, x=x.cpu().numpy())
+            line["cpu_baseline"] = cb
+            scale = float(np.abs(y_ref).max())
+            for a in order:
+                line["paths"][a]["max_rel_err_vs_cpu_reference"] = float(np.abs(runs[a]["y"] - y_ref).max()) / scale
+        except Exception as e:  # the baseline must never hide the GPU line
+            line["cpu_baseline"] = {"error": str(e)}
+    if rank == 0 and not args.no_solves:
+        try:
+            line["large_solve"] = large_solve_leg(H, {a: runs[a]["kernel_ms"] for a in order})
+        except Exception as e:
+            line["large_solve"] = {"error": str(e)}
+    H.close()
     if rank == 0 and not args.no_transform:
         try:
             line["transform"] = transform_leg(wd, args.steps, args.warmup, flush, peak)
         except Exception as e:  # the transform leg must never hide the matvec line
             line["transform"] = {"error": str(e)}
-        if "error" not in line["transform"]:
-            try:
-                line["large_basis"] = large_basis_leg(wd, min(args.steps, 10), args.warmup, flush, peak)
-            except Exception as e:
-                line["large_basis"] = {"error": str(e)}
         try:
             line["transform3"] = transform3_leg(wd, min(args.steps, 10), args.warmup, flush, peak)
         except Exception as e:
@@ -755,12 +788,7 @@ def main():
         except Exception as e:
             line["warm_start"] = {"error": str(e)}
     if rank == 0:
-        try:
-            line["cpu_baseline"] = cpu_baseline(d, w, bytes_for(64), seconds=args.cpu_seconds)
-        except Exception as e:  # the baseline must never hide the GPU line
-            line["cpu_baseline"] = {"error": str(e)}
         print(json.dumps(line), flush=True)
-    H.close()
     if dist:
         dist.destroy_process_group()
 

@@ -75,7 +75,8 @@ struct jn_ctx {
 	int walk_ready;                 /* the walk plan is on the device */
 	int walk_per_sm[3];             /* CTAs per SM of the FP32, FP64 and integer walk kernels */
 	int walk_fp64;                  /* precision 64: 0 exact integers (default), 1 FP64 fused multiply-adds */
-	int walk_sc;                    /* coefficient exponent of the integer path */
+	int walk_sc;                    /* the integer path's smallest block exponent (the product's unit) */
+	uint8_t *d_wgshift;             /* per row group: its block's exponent minus walk_sc */
 	uint4 *d_wtasks, *d_wpieces;
 	uint32_t *d_wlanes, *d_wwalks, *d_wrows, *d_wrdst, *d_wgroups;
 	void *d_welem[3];               /* walk element arrays: FP32, FP64, split integers (built on first use) */

@@ -294,6 +294,7 @@ typedef struct {
 	int64_t n_wrows;   uint32_t *wrows;    /* source row | slot row << 16 | group end | sign << 31 */
 	int64_t n_wrdst;   uint32_t *wrdst;
 	int64_t n_wgroups; uint32_t *wgroups;  /* element-row base of each group */
+	int32_t *wgblock;                       /* the matrix-element block of each group */
 	int64_t n_wme;                          /* walk element array: n_me + transposed copies */
 	int64_t *wtpos;                         /* per matrix-element block: offset of its transpose, or -1 */
 	double wvisits;                         /* multiply-adds including padding */
@@ -356,6 +357,12 @@ void jn_walk_free(jn_plan_t *plan);
 /* the walk element array (plan->n_wme values) from matrix elements in the
  * plan's layout */
 void jn_walk_elements(const jn_plan_t *plan, const double *me, double *out);
+/* the integer path's elements: each block scaled by its own 2^Sc_b so that
+ * max|A| of the block is below 2^52, rounded, and split into {high 28 bits
+ * (signed), low 24 bits} (two words per element of the walk element array
+ * a); per group the shift Sc_b - Sc_min (capped at 255) into gshift, and
+ * Sc_min (the smallest block exponent) into *sc_min */
+void jn_walk_int_elements(const jn_plan_t *plan, const double *a, int32_t *split, uint8_t *gshift, int *sc_min);
 
 #ifdef __cplusplus
 }

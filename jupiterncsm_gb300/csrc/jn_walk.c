@@ -28,9 +28,9 @@
 void jn_walk_free(jn_plan_t *p)
 {
 	free(p->wtasks); free(p->wpieces); free(p->wlanes); free(p->wwalks); free(p->wrows); free(p->wrdst);
-	free(p->wgroups); free(p->wtpos);
+	free(p->wgroups); free(p->wgblock); free(p->wtpos);
 	p->wtasks = NULL; p->wpieces = NULL; p->wlanes = NULL; p->wwalks = NULL; p->wrows = NULL; p->wrdst = NULL;
-	p->wgroups = NULL; p->wtpos = NULL;
+	p->wgroups = NULL; p->wgblock = NULL; p->wtpos = NULL;
 	p->nwtasks = p->nwpieces = p->n_wlanes = p->n_wwalks = p->n_wrows = p->n_wrdst = p->n_wgroups = p->n_wme = 0;
 	p->wvisits = p->wlane_slots = 0.0;
 }
@@ -52,6 +52,41 @@ void jn_walk_elements(const jn_plan_t *p, const double *me, double *out)
 				for (int64_t kn = 0; kn < nn; kn++) t[kp + npp * kn] = me[M->offset + kn + nn * kp];
 		}
 	}
+}
+
+void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, uint8_t *gshift, int *sc_min)
+{
+	int *sc = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int));
+	int lo = 1 << 30;
+	for (int b = 0; b < p->nmes; b++) {
+		const jn_me_t *M = &p->mes[b];
+		double m = 0.0;
+		for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(a[M->offset + e]));
+		int eb = 0;
+		if (m > 0.0) frexp(m, &eb);     /* m < 2^eb */
+		sc[b] = m > 0.0 ? 52 - eb : (1 << 30);
+		if (sc[b] < lo) lo = sc[b];
+	}
+	if (lo == (1 << 30)) lo = 0;
+	for (int b = 0; b < p->nmes; b++) {
+		if (sc[b] == (1 << 30)) sc[b] = lo;     /* an all-zero block */
+		const jn_me_t *M = &p->mes[b];
+		for (int pass = 0; pass < 2; pass++) {
+			const int64_t o = pass ? (p->wtpos ? p->wtpos[b] : -1) : M->offset;
+			if (o < 0) continue;
+			for (int64_t e = 0; e < M->len; e++) {
+				const int64_t v = llrint(ldexp(a[o + e], sc[b]));
+				split[2 * (o + e)] = (int32_t)(v >> 24);
+				split[2 * (o + e) + 1] = (int32_t)(v & 0xffffff);
+			}
+		}
+	}
+	for (int64_t g = 0; g < p->n_wgroups; g++) {
+		const int d = sc[p->wgblock[g]] - lo;
+		gshift[g] = (uint8_t)(d > 255 ? 255 : d);
+	}
+	*sc_min = lo;
+	free(sc);
 }
 
 /* growable arrays */
@@ -92,7 +127,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	vec_t tasks = { 0, 0, 0, sizeof(jn_wtask_t) }, pieces = { 0, 0, 0, sizeof(jn_wpiece_t) };
 	vec_t lanes = { 0, 0, 0, sizeof(uint32_t) }, walks = { 0, 0, 0, sizeof(uint32_t) };
 	vec_t rows = { 0, 0, 0, sizeof(uint32_t) }, rdst = { 0, 0, 0, sizeof(uint32_t) };
-	vec_t groups = { 0, 0, 0, sizeof(uint32_t) };
+	vec_t groups = { 0, 0, 0, sizeof(uint32_t) }, gblock = { 0, 0, 0, sizeof(int32_t) };
 	row_t *R = NULL;
 	int64_t Rcap = 0;
 	uint32_t *chunk = NULL;         /* per chunk: first ent index, count, walk index */
@@ -262,7 +297,8 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				int rs = 0;
 				int64_t r1 = r0;
 				const int64_t rdst0 = rdst.n, row0 = rows.n, group0 = groups.n;
-				if (vec_reserve(&rdst, JN_WALK_RS) || vec_reserve(&rows, nr - r0) || vec_reserve(&groups, nr - r0)) {
+				if (vec_reserve(&rdst, JN_WALK_RS) || vec_reserve(&rows, nr - r0) || vec_reserve(&groups, nr - r0) ||
+				    vec_reserve(&gblock, nr - r0)) {
 					free(set_walk0);
 					ERR("out of host memory");
 				}
@@ -285,6 +321,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 						}
 					}
 					((uint32_t *)groups.a)[groups.n++] = (uint32_t)(base + stride * (int64_t)R[r1].k);
+					((int32_t *)gblock.a)[gblock.n++] = x->me;
 					r1 = e;
 					if (e < g1) break;      /* a split group ends the piece */
 				}
@@ -342,12 +379,14 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	p->wrows = rows.a; p->n_wrows = rows.n;         /* plus the spare word */
 	p->wrdst = rdst.a; p->n_wrdst = rdst.n;
 	p->wgroups = groups.a; p->n_wgroups = groups.n;
+	p->wgblock = gblock.a;
 	p->wvisits = visits;
 	p->wlane_slots = slots;
 	free(R); free(chunk); free(stamp);
 	return 0;
 fail:
 	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
+	free(gblock.a);
 	free(R); free(chunk); free(stamp);
 	free(p->wtpos);
 	p->wtpos = NULL;

@@ -28,12 +28,14 @@
  *   64  FP64 coefficients and x, fused multiply-adds (GB300's FP64 pipe is
  *       narrow: this mode is bound by it);
  *   1   exact integers: coefficients and x as 52-bit fixed-point integers
+ *       (each matrix-element block scaled to its own max|M|, x to max|x|)
  *       split into a signed high part (28 bits) and a low part (24 bits);
  *       c x = ch xh 2^48 + (ch xl + cl xh) 2^24 + cl xl, summed over the
  *       chunk in two 64-bit registers with three 32 x 32 -> 64-bit integer
  *       multiply-adds per contribution (cl xl < 2^48 is dropped), and the
  *       sum rounded once to the nearest output unit.  This is the FP64-grade
- *       product: its inputs keep 52 bits against max|c| and max|x|, every
+ *       product: its inputs keep 52 bits against their block's max|c| and
+ *       against max|x|, every
  *       sum is exact, and it runs on the integer pipe.
  * Every row sum is rounded once, at a place fixed by the plan, and the
  * rounded sums are added as integers: the result is bit-identical from run
@@ -118,7 +120,7 @@ template <int MODE, int U>
 __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const uint4 pb, const uint32_t *__restrict__ lanes,
 					  const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
 					  const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
-					  const typename WalkT<MODE>::C *__restrict__ elem,
+					  const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
 					  const typename WalkT<MODE>::X *__restrict__ x, unsigned long long *__restrict__ gacc,
 					  unsigned int *__restrict__ lo, unsigned int *__restrict__ hi, int lane, int sh, float scalef,
 					  double scale)
@@ -145,6 +147,12 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 	uint32_t row = __ldg(rows + j);
 	for (int g = 0; g < ngroups; g++) {
 		const C *__restrict__ er = elem + __ldg(groups + (int)pb.z + g);
+		/* the integer path scales each block by its own exponent: its rows shift further */
+		int shg = sh;
+		if constexpr (MODE == 1) {
+			shg += (int)__ldg(gshift + (int)pb.z + g);
+			if (shg > 62) shg = 62;
+		}
 		C c[U];
 #pragma unroll
 		for (int u = 0; u < U; u++) {
@@ -173,8 +181,8 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 #pragma unroll
 			for (int u = 0; u < U; u++) xv2[u] = __ldg(xb2 + (two ? off[u] : 0));
 			const uint32_t next = __ldg(rows + j + 2);
-			add_fixed(lo, hi, (int)((row >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv, row, sh, scalef, scale));
-			if (two) add_fixed(lo, hi, (int)((row2 >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv2, row2, sh, scalef, scale));
+			add_fixed(lo, hi, (int)((row >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv, row, shg, scalef, scale));
+			if (two) add_fixed(lo, hi, (int)((row2 >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv2, row2, shg, scalef, scale));
 			const bool end = !two || (row2 & JN_WALK_GROUP_END);
 			j += two ? 2 : 1;
 			row = two ? next : row2;
@@ -203,7 +211,8 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 	jn_walk_kernel(const uint4 *__restrict__ tasks, const uint4 *__restrict__ pieces, const uint32_t *__restrict__ lanes,
 		       const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
 		       const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
-		       const typename WalkT<MODE>::C *__restrict__ elem, const typename WalkT<MODE>::X *__restrict__ x,
+		       const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
+		       const typename WalkT<MODE>::X *__restrict__ x,
 		       unsigned long long *__restrict__ gacc, const unsigned int *__restrict__ ctrl, long long ntasks,
 		       double abs_bound, int Sc, int nsm)
 {
@@ -228,11 +237,11 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		const uint4 pa = __ldg(pieces + 2 * ta.x), pb = __ldg(pieces + 2 * ta.x + 1);
 		const uint32_t U = (ta.w >> 8) & 0xffu;
 		if (U == 8)
-			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
 		else if (U == 4)
-			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
 		else
-			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
 	}
 }
 
@@ -262,29 +271,11 @@ __global__ void jn_walk_finalize_kernel(unsigned long long *__restrict__ gacc, d
 	}
 }
 
-/* bits of max |A| over the walk element array (non-negative doubles order as their bits) */
-__global__ void jn_walk_amax_kernel(const double *__restrict__ a, int64_t n, unsigned long long *__restrict__ amax)
+/* the walk element array in FP32 */
+__global__ void jn_walk_f32_kernel(const double *__restrict__ a, int64_t n, float *__restrict__ out)
 {
-	double m = 0.0;
 	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-		m = fmax(m, fabs(a[e]));
-	for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-	if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(amax, (unsigned long long)__double_as_longlong(m));
-}
-
-/* the walk element array in FP32, or as 52-bit fixed-point integers split into {high 28 bits, low 24 bits} */
-template <int MODE>
-__global__ void jn_walk_convert_kernel(const double *__restrict__ a, int64_t n, typename WalkT<MODE>::C *__restrict__ out, int Sc)
-{
-	const double s = ldexp(1.0, Sc);
-	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-		if constexpr (MODE == 32) {
-			out[e] = (float)a[e];
-		} else {
-			const long long q = __double2ll_rn(a[e] * s);
-			out[e] = make_int2((int)(q >> 24), (int)(q & 0xffffff));
-		}
-	}
+		out[e] = (float)a[e];
 }
 
 /* ------------------------------------------------------------------ */
@@ -309,10 +300,10 @@ static int walk_slot(int mode) { return mode == 32 ? 0 : (mode == 64 ? 1 : 2); }
 void jn_walk_release(jn_ctx *c)
 {
 	cudaFree(c->d_wtasks); cudaFree(c->d_wpieces); cudaFree(c->d_wlanes); cudaFree(c->d_wwalks); cudaFree(c->d_wrows);
-	cudaFree(c->d_wrdst); cudaFree(c->d_wgroups); cudaFree(c->d_wx);
+	cudaFree(c->d_wrdst); cudaFree(c->d_wgroups); cudaFree(c->d_wgshift); cudaFree(c->d_wx);
 	for (int i = 0; i < 3; i++) cudaFree(c->d_welem[i]);
 	c->d_wtasks = NULL; c->d_wpieces = NULL; c->d_wlanes = NULL; c->d_wwalks = NULL; c->d_wrows = NULL;
-	c->d_wrdst = NULL; c->d_wgroups = NULL; c->d_wx = NULL;
+	c->d_wrdst = NULL; c->d_wgroups = NULL; c->d_wgshift = NULL; c->d_wx = NULL;
 	for (int i = 0; i < 3; i++) c->d_welem[i] = NULL;
 	c->walk_ready = 0;
 }
@@ -386,35 +377,37 @@ static jn_status walk_elements(jn_ctx *c, int mode)
 		c->d_welem[1] = d;
 	}
 	if (mode == 64) return JN_OK;
+	if (mode == 1) {
+		/* per-block exponents: every block keeps 52 bits against its own max|A| */
+		double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
+		int32_t *sp = (int32_t *)malloc((size_t)(n ? n : 1) * 2 * sizeof(int32_t));
+		uint8_t *gs = (uint8_t *)malloc((size_t)(p->n_wgroups ? p->n_wgroups : 1));
+		jn_status s = JN_OK;
+		if (!h || !sp || !gs) {
+			s = jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
+		} else {
+			jn_walk_elements(p, p->me, h);
+			jn_walk_int_elements(p, h, sp, gs, &c->walk_sc);
+			int2 *d = NULL;
+			s = wupload(&d, sp, (size_t)n);
+			if (!s) {
+				c->d_welem[2] = d;
+				cudaFree(c->d_wgshift);
+				c->d_wgshift = NULL;
+				s = wupload(&c->d_wgshift, gs, (size_t)p->n_wgroups);
+			}
+		}
+		free(h); free(sp); free(gs);
+		return s;
+	}
 	const double *a = (const double *)c->d_welem[1];
-	cudaError_t e = cudaMalloc(&c->d_welem[slot], (size_t)(n ? n : 1) * (mode == 32 ? sizeof(float) : sizeof(int2)));
+	cudaError_t e = cudaMalloc(&c->d_welem[0], (size_t)(n ? n : 1) * sizeof(float));
 	if (e != cudaSuccess) {
-		c->d_welem[slot] = NULL;
+		c->d_welem[0] = NULL;
 		return jn_fail(JN_ERR_NOMEM, "cudaMalloc of %lld walk matrix elements: %s", (long long)n, cudaGetErrorString(e));
 	}
 	const int g = (int)(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
-	if (mode == 1) {
-		/* the coefficient exponent Sc from max|A| over the whole array */
-		unsigned long long *d_amax = NULL, h_amax = 0;
-		CUDA_TRY(cudaMalloc(&d_amax, sizeof(unsigned long long)));
-		e = cudaMemsetAsync(d_amax, 0, sizeof(unsigned long long), c->stream);
-		if (e == cudaSuccess && n) {
-			jn_walk_amax_kernel<<<g, 256, 0, c->stream>>>(a, n, d_amax);
-			e = cudaGetLastError();
-		}
-		if (e == cudaSuccess) e = cudaMemcpyAsync(&h_amax, d_amax, sizeof h_amax, cudaMemcpyDeviceToHost, c->stream);
-		if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-		cudaFree(d_amax);
-		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk element maximum: %s", cudaGetErrorString(e));
-		double amax;
-		memcpy(&amax, &h_amax, sizeof amax);
-		int ec = 0;
-		if (amax > 0.0) frexp(amax, &ec);       /* amax < 2^ec */
-		c->walk_sc = amax > 0.0 ? 52 - ec : 0;
-		if (n) jn_walk_convert_kernel<1><<<g, 256, 0, c->stream>>>(a, n, (int2 *)c->d_welem[slot], c->walk_sc);
-	} else if (n) {
-		jn_walk_convert_kernel<32><<<g, 256, 0, c->stream>>>(a, n, (float *)c->d_welem[slot], 0);
-	}
+	if (n) jn_walk_f32_kernel<<<g, 256, 0, c->stream>>>(a, n, (float *)c->d_welem[0]);
 	e = cudaGetLastError();
 	if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
 	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk matrix elements: %s", cudaGetErrorString(e));
@@ -445,15 +438,15 @@ jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumul
 		const uint4 *T = (const uint4 *)c->d_wtasks, *P = (const uint4 *)c->d_wpieces;
 		if (mode == 32)
 			jn_walk_kernel<32><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
-				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const float *)c->d_welem[0],
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const float *)c->d_welem[0],
 				(const float *)c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
 		else if (mode == 64)
 			jn_walk_kernel<64><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
-				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const double *)c->d_welem[1],
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const double *)c->d_welem[1],
 				d_x, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
 		else
 			jn_walk_kernel<1><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
-				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, (const int2 *)c->d_welem[2],
+				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, c->d_wgshift, (const int2 *)c->d_welem[2],
 				c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc, c->num_sms);
 	}
 	if (mid) cudaEventRecord(mid, st);

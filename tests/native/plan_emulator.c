@@ -473,7 +473,8 @@ int emu_panel_wavefronts(void *h, int by_out, double *out)
  * lane by lane, with every index checked.  mode 32: FP32 coefficients and
  * x, fused multiply-adds in entry order, the row sum rounded once to the
  * fixed-point unit; mode 64: the same in FP64; mode 1: the exact integer
- * path (52-bit fixed-point coefficients and x split into 28 + 24 bits,
+ * path (52-bit fixed-point coefficients, each block at its own exponent,
+ * and x, split into 28 + 24 bits,
  * three 32 x 32 -> 64-bit products per multiply-add, the row sum rounded
  * once to the nearest output unit).  Returns 1 when an index leaves its buffer. */
 static int walk_x_exponent52(float xmax)
@@ -528,17 +529,16 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 		xl[i] = (int32_t)(v & 0xffffff);
 	}
 	jn_walk_elements(P, P->me, a64);
-	double amax = 0.0;
-	for (int64_t e = 0; e < nm; e++) amax = fmax(amax, fabs(a64[e]));
-	int ec = 0;
-	if (amax > 0.0) frexp(amax, &ec);
-	const int Sc = amax > 0.0 ? 52 - ec : 0;
+	int32_t *split = malloc((nm ? nm : 1) * 2 * sizeof(int32_t));
+	uint8_t *gshift = malloc(P->n_wgroups ? P->n_wgroups : 1);
+	int Sc = 0;
+	jn_walk_int_elements(P, a64, split, gshift, &Sc);
 	for (int64_t e = 0; e < nm; e++) {
 		a32[e] = (float)a64[e];
-		int64_t v = llrint(ldexp(a64[e], Sc));
-		ah[e] = (int32_t)(v >> 24);
-		al[e] = (int32_t)(v & 0xffffff);
+		ah[e] = split[2 * e];
+		al[e] = split[2 * e + 1];
 	}
+	free(split);
 	int S = fixed_exponent(xmax, P->abs_bound), sh = 0;
 	if (mode == 1) {
 		if (Sc + Sx - S < 48) S = Sc + Sx - 48;
@@ -572,6 +572,8 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 			int64_t j = pc->row0;
 			for (int g = 0; g < ng && !bad; g++) {
 				const int64_t gb = P->wgroups[pc->group0 + g];
+				int shg = sh + gshift[pc->group0 + g];
+				if (shg > 62) shg = 62;
 				int64_t ai[8];
 				for (int u = 0; u < U; u++) {
 					ai[u] = gb + (ko[u] & 0x3fffffffu);
@@ -607,7 +609,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 					}
 					if (mode == 1) {
 						const int64_t q = A + (B >> 24);
-						v = sh ? (q + ((int64_t)1 << (sh - 1))) >> sh : q + ((B >> 23) & 1);
+						v = shg ? (q + ((int64_t)1 << (shg - 1))) >> shg : q + ((B >> 23) & 1);
 						if (row >> 31) v = -v;
 					} else if (mode == 32) {
 						v = llrintf(accf * ((row >> 31) ? -scalef : scalef));
@@ -629,7 +631,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 	}
 	const double unit = ldexp(1.0, -S);
 	for (int64_t i = 0; i < D; i++) y[i] = accumulate ? y[i] + (double)gacc[i] * unit : (double)gacc[i] * unit;
-	free(slot); free(x32); free(a32); free(xh); free(xl); free(a64); free(ah); free(al); free(gacc);
+	free(slot); free(x32); free(a32); free(xh); free(xl); free(a64); free(ah); free(al); free(gacc); free(gshift);
 	return bad;
 }
 
