@@ -287,7 +287,7 @@ typedef struct {
 	uint32_t *pperm;                        /* per packed entry: its index in the list's by-out order */
 	int64_t n_coef;                         /* coefficients of all panels */
 	/* walk engine (built by jn_walk_build) */
-	int64_t nwtasks;   jn_wtask_t *wtasks;  /* in instruction order */
+	int64_t nwtasks;   jn_wtask_t *wtasks;  /* instructions by matrix-element block */
 	int64_t nwpieces;  jn_wpiece_t *wpieces;
 	int64_t n_wlanes;  uint32_t *wlanes;
 	int64_t n_wwalks;  uint32_t *wwalks;

@@ -114,6 +114,16 @@ static int cmp_row(const void *a, const void *b)
 	return (int)x->sign - (int)y->sign;
 }
 
+static const jn_plan_t *g_order_plan;
+static int cmp_instr_block(const void *a, const void *b)
+{
+	const jn_instr_t *x = &g_order_plan->instr[*(const int *)a], *y = &g_order_plan->instr[*(const int *)b];
+	if (x->me != y->me) return x->me < y->me ? -1 : 1;
+	if (x->bout != y->bout) return x->bout < y->bout ? -1 : 1;
+	if (x->bin != y->bin) return x->bin < y->bin ? -1 : 1;
+	return *(const int *)a - *(const int *)b;
+}
+
 /* lane chunks of width U over the walks [w0, w0 + nw) */
 static int64_t chunks_for(const uint32_t *walks, int64_t w0, int64_t nw, int U)
 {
@@ -134,6 +144,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	int64_t ccap = 0;
 	int32_t *stamp = calloc(65536, sizeof(int32_t));
 	int32_t stamp_clock = 0;
+	int *order = NULL;
 	double visits = 0.0, slots = 0.0;
 	jn_walk_free(p);
 	p->wtpos = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int64_t));
@@ -149,7 +160,16 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 		p->n_wme += p->mes[x->me].len;
 	}
 	if (p->n_wme >= 0x3fffffffll) ERR("%lld walk matrix elements: too many for the walk engine", (long long)p->n_wme);
-	for (int q = 0; q < p->ninstr; q++) {
+	/* instructions in matrix-element-block order: the ~10 instructions (and
+	   both directions of each) that read one block run one after another, so
+	   L2 holds the block's rows while all of them gather from it */
+	order = malloc((size_t)(p->ninstr > 0 ? p->ninstr : 1) * sizeof(int));
+	if (!order) ERR("out of host memory");
+	for (int q = 0; q < p->ninstr; q++) order[q] = q;
+	g_order_plan = p;
+	qsort(order, (size_t)p->ninstr, sizeof(int), cmp_instr_block);
+	for (int oq = 0; oq < p->ninstr; oq++) {
+		const int q = order[oq];
 		const jn_instr_t *x = &p->instr[q];
 		const jn_block_t *bi = &p->blocks[x->bin], *bo = &p->blocks[x->bout];
 		const jn_me_t *M = &p->mes[x->me];
@@ -362,10 +382,9 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 			free(set_walk0);
 		}
 	}
-	/* tasks stay in instruction order: warps take them cyclically (warp w of W
-	   runs tasks w, w + W, ...), so warps that run at the same time work on
-	   neighbouring instructions and share their blocks of x and of matrix
-	   elements in cache */
+	/* tasks stay in this order: warps take them cyclically (warp w of W runs
+	   tasks w, w + W, ...), so warps that run at the same time work on
+	   neighbouring instructions and share their matrix elements in L2 */
 	/* one spare row word: the kernel reads the word after a group's last row ahead of time */
 	if (vec_reserve(&rows, 1)) ERR("out of host memory");
 	((uint32_t *)rows.a)[rows.n] = 0u;
@@ -382,12 +401,12 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	p->wgblock = gblock.a;
 	p->wvisits = visits;
 	p->wlane_slots = slots;
-	free(R); free(chunk); free(stamp);
+	free(R); free(chunk); free(stamp); free(order);
 	return 0;
 fail:
 	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
 	free(gblock.a);
-	free(R); free(chunk); free(stamp);
+	free(R); free(chunk); free(stamp); free(order);
 	free(p->wtpos);
 	p->wtpos = NULL;
 	p->n_wme = 0;
