@@ -115,15 +115,21 @@ jn_status jn_matvec_files(jn_ctx *ctx, const char *output_vector_directory, cons
  * for callers that must not allocate device memory: a solver that has sized
  * its Krylov basis to the memory it was granted, an application under a
  * fixed device-memory budget, or a loop that cannot take the synchronisation
- * an allocation may bring.  Same product as jn_matvec_device (block-tile
- * engine, the context's precision); its scratch is a fixed array inside the
- * library that every GPU loading the library holds until exit, so it serves
- * dimensions up to JN_NOALLOC_MAX_DIM and rejects larger ones.  All calls
- * share that array: calls whose kernels overlap on the GPU race, so
- * serialise them.  The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress) and caches it; make that first call
- * before any stream capture.  No counterpart in the reference, which has no
- * device memory.
+ * an allocation may bring.  It always runs the block-tile engine (3) at the
+ * context's precision, whatever jn_set_engine chose: its result equals
+ * jn_matvec_device's bit for bit when engine 3 is the context's engine, and
+ * agrees with the other engines to rounding (about 1e-15 of max|y| at
+ * precision 64, FP32 level at 32).  Precision 32 needs jn_set_precision(ctx,
+ * 32) first (it builds the FP32 matrix elements this entry point reads).
+ * Its scratch is a fixed array inside the library that every GPU loading
+ * the library holds until exit, so it serves dimensions up to
+ * JN_NOALLOC_MAX_DIM and rejects larger ones.  All calls share that array:
+ * calls whose kernels overlap on the GPU race, so serialise them.  The first
+ * call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) and caches it for the life of the process; make
+ * that first call before any stream capture.  The cached address does not
+ * survive cudaDeviceReset: do not call this entry point on a device after
+ * resetting it.  No counterpart in the reference, which has no device memory.
  */
 #define JN_NOALLOC_MAX_DIM 262144
 jn_status jn_matvec_device_noalloc(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, void *stream);
@@ -259,7 +265,19 @@ typedef struct {
 	int check_every;               /* convergence test interval (1 = every step) */
 	const double *start_vector;    /* host, length D; NULL = e_0 as the reference */
 	int verbose;                   /* per-iteration lines on stdout */
+	int criterion;                 /* JN_LANCZOS_REFERENCE: jn_convergence_criterion (lanczos.converge_eigenvectors) */
 } jn_lanczos_options;
+
+/* What JN_LANCZOS_REFERENCE compares between consecutive steps
+ * (Bacchus/lanczos/lanczos.h:11-16, lanczos.c:199-235): the lowest Ritz
+ * value, or the lowest eigenvector of the tridiagonal matrix (sign chosen so
+ * that its first component is not negative; the previous step's vector, one
+ * component shorter, counts as zero there), converged when the change is
+ * below the tolerance (lanczos.c:276-287). */
+typedef enum {
+	JN_CONVERGE_EIGENVALUES = 0,
+	JN_CONVERGE_EIGENVECTORS = 1
+} jn_convergence_criterion;
 
 typedef struct {
 	int iterations;                /* Krylov dimension reached */

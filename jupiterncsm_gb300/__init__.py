@@ -97,7 +97,7 @@ class WarmStartOptions(ctypes.Structure):
 class LanczosOptions(ctypes.Structure):
     _fields_ = [("max_iterations", ctypes.c_int), ("num_eigenvalues", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("mode", ctypes.c_int), ("check_every", ctypes.c_int), ("start_vector", ctypes.c_void_p),
-                ("verbose", ctypes.c_int)]
+                ("verbose", ctypes.c_int), ("criterion", ctypes.c_int)]
 
 
 class LanczosResult(ctypes.Structure):
@@ -285,9 +285,12 @@ class Hamiltonian:
         _check(gpu_lib().jn_set_precision(self._h, int(bits)))
 
     def lanczos(self, max_iterations=200, num_eigenvalues=10, tolerance=1e-6, mode=LANCZOS_FULL, check_every=1,
-                start_vector=None, verbose=False, allow_unconverged=False):
-        """Run Lanczos on the GPU; returns a dict with eigenvalues (refined), Ritz values, residuals."""
-        o = LanczosOptions(max_iterations, num_eigenvalues, tolerance, mode, check_every, None, int(verbose))
+                start_vector=None, verbose=False, allow_unconverged=False, converge_eigenvectors=False):
+        """Run Lanczos on the GPU; returns a dict with eigenvalues (refined), Ritz values, residuals.
+        converge_eigenvectors (reference mode): converge the lowest eigenvector of the tridiagonal matrix
+        instead of the lowest Ritz value, as the run file's lanczos.converge_eigenvectors does."""
+        o = LanczosOptions(max_iterations, num_eigenvalues, tolerance, mode, check_every, None, int(verbose),
+                           int(bool(converge_eigenvectors)))
         sv = None
         if start_vector is not None:
             sv = np.ascontiguousarray(start_vector, dtype=np.float64)

@@ -80,6 +80,7 @@ int main(int argc, char **argv)
 	o.mode = rs.gpu_full_reorthogonalization ? JN_LANCZOS_FULL : JN_LANCZOS_REFERENCE;
 	o.check_every = 1;
 	o.verbose = 0;
+	o.criterion = rs.converge_eigenvectors ? JN_CONVERGE_EIGENVECTORS : JN_CONVERGE_EIGENVALUES;
 	printf("Diagonalzation start:\n");
 	double td = now_us();
 	jn_lanczos_result r;

@@ -37,6 +37,8 @@
 #include <sys/stat.h>
 #include <sys/types.h>
 
+#include <vector>
+
 #include "jn_internal.h"
 #include "jn_tridiag.cuh"
 
@@ -314,6 +316,10 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 
 	double prev = 0.0;
 	int k, converged = 0;
+	/* the eigenvector criterion keeps the previous step's vector (and the current one after it) */
+	const int by_vector = reference_mode && opt->criterion == JN_CONVERGE_EIGENVECTORS;
+	std::vector<double> zbuf(by_vector ? 2 * (size_t)(m + 1) : 0, 0.0);
+	double *zprev = zbuf.data();
 	res->iterations = 0;
 	for (k = 0; k < m; k++) {
 		double *vk = V + (int64_t)k * D, *vk1 = V + (int64_t)(k + 1) * D;
@@ -341,9 +347,22 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 		CUDA_TRY(cudaMemcpyAsync(s->h_alpha, s->d_alpha, n * sizeof(double), cudaMemcpyDeviceToHost, q));
 		CUDA_TRY(cudaMemcpyAsync(s->h_beta, s->d_beta, n * sizeof(double), cudaMemcpyDeviceToHost, q));
 		if (reference_mode) {
-			st = tri_eig(c, n, 1, 0);
+			st = tri_eig(c, n, 1, by_vector);
 			if (st) return st;
-			double diff = fabs(s->h_theta[0] - prev);
+			double diff;
+			if (by_vector) {
+				/* the lowest eigenvector of T_n against the previous step's (lanczos.c:210-215, 276-287) */
+				CUDA_TRY(cudaMemcpy(zprev + (m + 1), s->d_Z, n * sizeof(double), cudaMemcpyDeviceToHost));
+				double *z = zprev + (m + 1);
+				if (z[0] < 0.0)
+					for (int i = 0; i < n; i++) z[i] = -z[i];
+				double d2 = z[n - 1] * z[n - 1];
+				for (int i = 0; i + 1 < n; i++) d2 += (z[i] - zprev[i]) * (z[i] - zprev[i]);
+				diff = sqrt(d2);
+				memcpy(zprev, z, n * sizeof(double));
+			} else {
+				diff = fabs(s->h_theta[0] - prev);
+			}
 			prev = s->h_theta[0];
 			if (opt->verbose)
 				printf("Lanczos iteration %d: lowest Ritz value %.17lg, difference %lg\n", n, s->h_theta[0], diff);

@@ -9,9 +9,10 @@
  * device memory it was granted, an application that runs under a fixed
  * memory budget (the reference's max_memory_load), or a solver loop that
  * cannot afford the device-wide synchronisation a cudaMalloc may bring.
- * jn_matvec_device_noalloc() computes the same product with its scratch in a
- * file-scope device array of fixed size instead.  It never calls cudaMalloc,
- * cudaFree or an allocating library routine.
+ * jn_matvec_device_noalloc() computes the block-tile engine's product (bit
+ * for bit what jn_matvec_device gives when the context runs engine 3) with
+ * its scratch in a file-scope device array of fixed size instead.  It never
+ * calls cudaMalloc, cudaFree or an allocating library routine.
  *
  * The array lives in the library's device image: every GPU that loads the
  * library holds it (JN_NOALLOC_MAX_DIM * 12 + 8 bytes, about 3 MiB) until the
@@ -23,7 +24,9 @@
  * Host code cannot use the array's name as a device address (it names a
  * host-side stand-in), so the first call on each device looks the address up
  * with cudaGetSymbolAddress while that device is current and caches it.  That
- * first call should therefore come before any stream capture.
+ * first call should therefore come before any stream capture.  The cache
+ * lasts as long as the process: after cudaDeviceReset the cached address is
+ * stale, so the entry point must not be called on a device that was reset.
  */
 #include <pthread.h>
 

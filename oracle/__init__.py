@@ -20,6 +20,9 @@ being measured or shipped.
                  present
 * ``reference_transform3``  the reference's own three-body J -> M transform
                  with its ASCII J-scheme reader (_ref/ref_mercury3)
+* ``reference_bacchus``  the reference's own Bacchus eigensolver
+                 (_ref/ref_bacchus): its Lanczos, tridiagonal solver and
+                 eigensystem output on the same files
 """
 import ctypes
 import os
@@ -39,6 +42,7 @@ PORT_LIB = os.path.join(HERE, "_build", "libminerva_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_minerva.so")
 REF_MERCURY = os.path.join(HERE, "_ref", "ref_mercury")
 REF_MERCURY3 = os.path.join(HERE, "_ref", "ref_mercury3")
+REF_BACCHUS = os.path.join(HERE, "_ref", "ref_bacchus")
 
 
 def build():
@@ -229,3 +233,30 @@ def write_zero_vectors(d):
     if not os.path.isdir(z):
         write_vector_dir(z, blocks, np.zeros(sum(a * b for _, a, b in blocks)))
     return z
+
+
+def reference_bacchus_available():
+    return os.path.exists(REF_BACCHUS)
+
+
+def reference_bacchus(d, Z, N, max_iterations=200, tolerance=1e-6, converge_eigenvectors=False, target=0):
+    """Run the reference's Bacchus on the problem in d; returns {"eigenvalues": the final
+    eigensystem block's values, "num_eigenvalues", "eigenvectors": (target + 1, D) array,
+    "steps": the eigensystem blocks printed while iterating}."""
+    import tempfile
+    blocks = read_blocks(d)
+    with tempfile.TemporaryDirectory() as wd:
+        os.makedirs(os.path.join(wd, "krylov"))
+        os.makedirs(os.path.join(wd, "eigen"))
+        r = subprocess.run([REF_BACCHUS, f"{d}/comb.txt", f"{d}/evaluation_order.txt", f"{d}/index_lists",
+                            f"{d}/matrix_elements", str(Z), str(N), os.path.join(wd, "krylov"), str(max_iterations),
+                            repr(float(tolerance)), "1" if converge_eigenvectors else "0", os.path.join(wd, "eigen"),
+                            str(target)], capture_output=True, text=True, check=True, cwd=wd)
+        out = r.stdout
+        blocks_text = out.split("eigensystem:")
+        last = blocks_text[-1]
+        vals = last[last.index("(") + 1:last.index(")")].split(",")
+        ev = np.array([float(v) for v in vals if v.strip()])
+        vecs = np.array([read_vector_dir(os.path.join(wd, "eigen", f"eigenvector_{i + 1}"), blocks)
+                         for i in range(target + 1)])
+    return {"eigenvalues": ev, "num_eigenvalues": len(ev), "eigenvectors": vecs, "steps": len(blocks_text) - 2}

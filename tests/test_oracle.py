@@ -85,3 +85,25 @@ def test_golden_eigenvalues_from_port(tmp_path):
     H = np.column_stack([p.matvec(np.eye(D)[j]) for j in range(D)])
     w = np.linalg.eigvalsh(0.5 * (H + H.T))[:10]
     assert np.abs(w - g["eig"]).max() < 1e-10
+
+
+@pytest.mark.skipif(not reference_tree_present(), reason="reference tree absent")
+@pytest.mark.parametrize("name", ["bacchus_he4_n4_2b", "bacchus_he4_n4_2b_vec", "bacchus_he4_n2_3b",
+                                  "bacchus_li6_n2_3b_vec"])
+def test_reference_bacchus_fixtures_and_dense_eigh(tmp_path, name):
+    """The reference's Bacchus, run again, reproduces its fixture, and its
+    lowest eigenpair is the dense matrix's (within its convergence tolerance)."""
+    if not oracle.reference_bacchus_available():
+        oracle.build()
+    meta = json.load(open(os.path.join(GOLDEN, f"{name}.json")))
+    d = str(tmp_path / "p")
+    jn.generate(d, basis_files=False, **meta["config"])
+    r = oracle.reference_bacchus(d, meta["config"]["Z"], meta["config"]["N"], **meta["lanczos"])
+    assert r["num_eigenvalues"] == meta["num_eigenvalues"]
+    assert np.abs(r["eigenvalues"] - meta["eigenvalues"]).max() <= 1e-10 * np.abs(r["eigenvalues"]).max()
+    p = oracle.Port(d)
+    D = p.dimension
+    Hd = np.column_stack([p.matvec(np.eye(D)[j]) for j in range(D)])
+    w, V = np.linalg.eigh(0.5 * (Hd + Hd.T))
+    assert abs(r["eigenvalues"][0] - w[0]) < 1e-6
+    assert abs(V[:, 0] @ r["eigenvectors"][0]) > 1 - 1e-8
