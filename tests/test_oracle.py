@@ -38,19 +38,22 @@ def test_golden_files_and_port(tmp_path, name):
 
 
 @pytest.mark.skipif(not reference_tree_present(), reason="reference tree absent")
-@pytest.mark.parametrize("name", ["he4_n2_3b", "he4_n4_2b", "li6_n2_3b"])
+@pytest.mark.parametrize("name", ["he4_n2_3b", "he4_n4_2b", "li6_n2_3b", "he4_n6_3b", "li6_n6_3b"])
 def test_port_pinned_to_reference(problem, name):
+    """The port against the compiled reference kernels, up to the largest
+    single-GPU problem (6Li Nmax 6, two- plus three-body, D = 186 894)."""
     d, Z, N, *_ = problem(name)
-    ref = oracle.Reference(d, Z, N, threads=4)
+    threads = os.cpu_count() or 4
+    ref = oracle.Reference(d, Z, N, threads=threads)
     p = oracle.Port(d)
     rng = np.random.default_rng(5)
-    for _ in range(3):
+    for _ in range(1 if name == "li6_n6_3b" else 3):
         x = rng.standard_normal(p.dimension)
         y0 = rng.standard_normal(p.dimension)
         a = ref.matvec(x, y0.copy())
         b = p.matvec(x, y0.copy())
         c = y0.copy()
-        p.matvec_omp(x, c, 4)
+        p.matvec_omp(x, c, threads)
         scale = np.abs(a).max()
         assert np.abs(a - b).max() <= 1e-12 * scale
         assert np.abs(a - c).max() <= 1e-12 * scale
