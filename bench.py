@@ -46,6 +46,10 @@ WORKLOADS = {
                              label="4He (Z=2,N=2) HO M-scheme Nmax=6, 2M=0, +parity, seeded 2NF N(0,1) + 3NF N(0,0.1) MeV, hw=20 MeV"),
     "he4_nmax4_2nf": dict(Z=2, N=2, nmax=4, nbody=2, M2=0,
                           label="4He (Z=2,N=2) HO M-scheme Nmax=4, 2M=0, +parity, seeded 2NF N(0,1) MeV, hw=20 MeV"),
+    # a medium case of the large workload's structure (larger than L2, a few GB on the device): profiling
+    "li6_nmax4_2nf3nf": dict(Z=3, N=3, nmax=4, nbody=3, M2=2,
+                             label="6Li (Z=3,N=3) HO M-scheme Nmax=4, 2M=2, +parity, seeded 2NF N(0,1) + 3NF N(0,0.1) "
+                                   "MeV, hw=20 MeV"),
     "li6_nmax6_2nf": dict(Z=3, N=3, nmax=6, nbody=2, M2=2,
                           label="6Li (Z=3,N=3) HO M-scheme Nmax=6, 2M=2, +parity, seeded 2NF N(0,1) MeV, hw=20 MeV"),
 }
@@ -631,6 +635,38 @@ def cpu_baseline(d, w, bytes_per_step, seconds=10.0, min_steps=3, x=None):
             "ms_per_step": per * 1e3}, y
 
 
+def product_leg(args):
+    """Diagnostic: --steps products y = H x of --workload with the chosen engine
+    and arithmetic, each after the L2 flush, with the product kernel's
+    CUDA-event time (the target of the ncu captures under profiles/)."""
+    import numpy as np
+    import torch
+    import jupiterncsm_gb300 as jn
+    w = WORKLOADS[args.workload]
+    d = prepare(args.workload, args.workdir)
+    H = jn.Hamiltonian.from_dir(d, w["Z"], w["N"])
+    try:
+        if args.engine:
+            H.set_engine(args.engine)
+        prec, fma = ARITH[args.arith]
+        H.set_precision(prec)
+        if H.active_engine() == 5:
+            H.set_walk_arithmetic(fma)
+        D = H.dimension
+        x = torch.from_numpy(np.random.default_rng(3).standard_normal(D)).cuda()
+        y = torch.zeros(D, dtype=torch.float64, device="cuda")
+        flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(H.matvec_profile(x.data_ptr(), y.data_ptr())[0])
+        return {"workload": w["label"], "dimension": D, "engine": H.active_engine(), "arith": args.arith,
+                "kernel_ms": ms}
+    finally:
+        H.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -647,10 +683,15 @@ def main():
     ap.add_argument("--schedule", metavar="ROWS,CTAS",
                     help="fix the panel schedule (rows per lane, CTAs per SM) instead of autotuning it "
                          "(panel-engine workloads)")
-    ap.add_argument("--leg", choices=["transform", "transform3"],
-                    help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line)")
+    ap.add_argument("--leg", choices=["transform", "transform3", "product"],
+                    help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line); "
+                         "product: --steps products of --workload on --engine in --arith, timed with CUDA events")
+    ap.add_argument("--engine", type=int, choices=[2, 3, 4, 5], help="the product engine (--leg product)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.leg == "product":
+        print(json.dumps({"product": product_leg(args)}), flush=True)
+        return
     if args.leg:
         import torch
         flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
