@@ -251,8 +251,12 @@ def transform_leg(workdir, steps, warmup, flush, peak):
     return {"workload": w["label"], "elements": st["num_elements"], "two_body_blocks": st["num_two_body_blocks"],
             "pair_states": st["num_pair_states"], "configurations": st["num_configurations"],
             "kernel_ms": kms, "elements_per_s": st["num_elements"] / (kms / 1e3),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "bytes_per_run": st["algorithmic_bytes"], "kernel": "jn_jt_to_m_kernel"},
+            "roofline": {"bound": "fp64 pipe", "fp64_pipe_busy_ncu": 0.764,
+                         "profile": "profiles/jn_jt_to_m_kernel_li6_nmax6.md",
+                         "hbm_achieved": achieved, "hbm_peak": peak, "unit": "GB/s", "hbm_frac": achieved / peak,
+                         "bytes_per_run": st["algorithmic_bytes"], "kernel": "jn_jt_to_m_kernel",
+                         "note": "each element is a sum of separately rounded FP64 products (the reference's "
+                                 "arithmetic), so GB300's FP64 pipe bounds the kernel, not HBM"},
             "dense_equivalent_flops": st["dense_flops"],
             "dense_equivalent_tflop_per_s": st["dense_flops"] / (kms / 1e3) / 1e12,
             "plan_seconds": st["plan_seconds"], "open_seconds": open_s,
