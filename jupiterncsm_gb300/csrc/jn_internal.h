@@ -81,6 +81,8 @@ struct jn_ctx {
 	uint32_t *d_wlanes, *d_wwalks, *d_wrows, *d_wrdst, *d_wgroups;
 	void *d_welem[3];               /* walk element arrays: FP32, FP64, split integers (built on first use) */
 	int2 *d_wx;                     /* x converted for the product (FP32 or split 52-bit integers) */
+	int2 *d_wxt;                    /* the transposed view of x that proton walks read, in the product's type */
+	int32_t *d_wxperm;              /* position in x of each element of that view */
 };
 
 /* drop the cached product graphs (before any product buffer is freed) */

@@ -205,8 +205,13 @@ typedef struct {
  * adds into the global accumulator once per task.
  *
  * Walk list = neutron list (wp = 0): D(r, w) = dst + r Nn_dst + w,
- * S(r, w) = src + r Nn_src + w; proton list (wp = 1): D(r, w) = dst + w Nn_dst + r,
- * S(r, w) = src + w Nn_src + r.
+ * S(r, w) = src + r Nn_src + w in x; proton list (wp = 1): D(r, w) = dst +
+ * w Nn_dst + r, and the source is read from the transposed view xT of x
+ * (each block [n][p] instead of [p][n]), S(r, w) = src + r Np_src + w, so
+ * that in both cases a row's walk entries index one contiguous row of the
+ * source block.  The entries of a walk are dealt to its lanes in turn
+ * (entry i of a walk spread over l lanes goes to lane i mod l, position
+ * i / l): at every position neighbouring lanes read neighbouring sources.
  *
  * Coefficients come from the walk element array: the plan's matrix elements
  * (single-species elements below 1e-12 stored as 0, the reference's skip),
@@ -226,7 +231,7 @@ typedef struct {
 
 typedef struct {                /* 32 bytes */
 	int32_t src_off, dst_off;       /* offsets of the source and destination blocks in x and y */
-	int32_t Nn_src, Nn_dst;
+	int32_t src_stride, Nn_dst;     /* row stride of the source view (Nn_src in x, Np_src in xT), Nn of the destination */
 	int32_t row0;                   /* first row word in wrows */
 	int32_t rdst0;                  /* destination of each slot row in wrdst */
 	int32_t group0;                 /* element-row base of each group in wgroups */
@@ -292,6 +297,8 @@ typedef struct {
 	int64_t n_wlanes;  uint32_t *wlanes;
 	int64_t n_wwalks;  uint32_t *wwalks;
 	int64_t n_wrows;   uint32_t *wrows;    /* source row | slot row << 16 | group end | sign << 31 */
+	int32_t *wxperm;                        /* position in x of each element of the transposed view xT */
+	int wxt;                                /* proton walks read xT */
 	int64_t n_wrdst;   uint32_t *wrdst;
 	int64_t n_wgroups; uint32_t *wgroups;  /* element-row base of each group */
 	int32_t *wgblock;                       /* the matrix-element block of each group */

@@ -28,9 +28,10 @@
 void jn_walk_free(jn_plan_t *p)
 {
 	free(p->wtasks); free(p->wpieces); free(p->wlanes); free(p->wwalks); free(p->wrows); free(p->wrdst);
-	free(p->wgroups); free(p->wgblock); free(p->wtpos);
+	free(p->wgroups); free(p->wgblock); free(p->wtpos); free(p->wxperm);
 	p->wtasks = NULL; p->wpieces = NULL; p->wlanes = NULL; p->wwalks = NULL; p->wrows = NULL; p->wrdst = NULL;
-	p->wgroups = NULL; p->wgblock = NULL; p->wtpos = NULL;
+	p->wgroups = NULL; p->wgblock = NULL; p->wtpos = NULL; p->wxperm = NULL;
+	p->wxt = 0;
 	p->nwtasks = p->nwpieces = p->n_wlanes = p->n_wwalks = p->n_wrows = p->n_wrdst = p->n_wgroups = p->n_wme = 0;
 	p->wvisits = p->wlane_slots = 0.0;
 }
@@ -279,29 +280,37 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				uint32_t *L = (uint32_t *)lanes.a + lanes.n;
 				uint32_t *T = (uint32_t *)walks.a + walks.n;
 				int nwalk = 0;
-				int64_t prev = -1;
-				for (int l = 0; l < 32; l++) {
-					const int64_t c = s * 32 + l;
-					uint32_t slot = 0, src[8], koff[8];
-					for (int u = 0; u < U; u++) { src[u] = 0; koff[u] = JN_WALK_PADBIT; }
-					if (c < nchunk) {
-						const int64_t w = chunk[3 * c + 2];
-						if (w != prev) {
-							T[nwalk++] = p->walks[2 * (w0 + w) + 1] >> 16;
-							prev = w;
-						}
-						slot = (uint32_t)(nwalk - 1);
-						const uint32_t e0 = chunk[3 * c], n = chunk[3 * c + 1];
-						/* padding repeats the chunk's first source with coefficient 0 */
-						for (int u = 0; u < U; u++) {
-							const uint32_t e = e0 + ((uint32_t)u < n ? (uint32_t)u : 0u);
-							src[u] = p->ent[2 * e] & 0xffffu;
-							koff[u] = (uint32_t)u < n ? p->ent[2 * e + 1] : JN_WALK_PADBIT;
-						}
+				for (int l = 0; l < 32;) {
+					/* the run of this set's lanes [l, l1) that hold chunks of one walk: its
+					   entries (contiguous in the walk view) are dealt to the run's lanes in
+					   turn, entry i to lane l + i mod nl at position i / nl */
+					int l1 = l + 1;
+					const int64_t c0 = s * 32 + l;
+					if (c0 < nchunk)
+						while (l1 < 32 && s * 32 + l1 < nchunk && chunk[3 * (s * 32 + l1) + 2] == chunk[3 * c0 + 2]) l1++;
+					else
+						l1 = 32;
+					const int nl = l1 - l;
+					uint32_t e0 = 0, ne = 0;
+					if (c0 < nchunk) {
+						T[nwalk++] = p->walks[2 * (w0 + chunk[3 * c0 + 2]) + 1] >> 16;
+						e0 = chunk[3 * c0];
+						for (int64_t c = c0; c < s * 32 + l1; c++) ne += chunk[3 * c + 1];
 					}
-					L[l] = slot;
-					for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l] = src[2 * k] | (src[2 * k + 1] << 16);
-					for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l] = koff[u];
+					for (int r = 0; r < nl; r++) {
+						uint32_t src[8], koff[8];
+						for (int u = 0; u < U; u++) {
+							const uint32_t i = (uint32_t)(u * nl + r);
+							/* padding repeats the lane's first source with coefficient 0 */
+							const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
+							src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
+							koff[u] = i < ne ? p->ent[2 * e + 1] : JN_WALK_PADBIT;
+						}
+						L[l + r] = c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u;
+						for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
+						for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
+					}
+					l = l1;
 				}
 				set_walk0[2 * s] = (uint32_t)walks.n;
 				set_walk0[2 * s + 1] = (uint32_t)nwalk;
@@ -360,7 +369,8 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				jn_wpiece_t *P = (jn_wpiece_t *)pieces.a + pi;
 				P->src_off = (int32_t)bs->offset;
 				P->dst_off = (int32_t)bd->offset;
-				P->Nn_src = (int32_t)bs->Nn;
+				P->src_stride = (int32_t)(wp ? bs->Np : bs->Nn);
+				if (wp) p->wxt = 1;
 				P->Nn_dst = (int32_t)bd->Nn;
 				P->row0 = (int32_t)row0;
 				P->rdst0 = (int32_t)rdst0;
@@ -385,6 +395,16 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	/* tasks stay in this order: warps take them cyclically (warp w of W runs
 	   tasks w, w + W, ...), so warps that run at the same time work on
 	   neighbouring instructions and share their matrix elements in L2 */
+	/* the transposed view of x that proton walks read: block [n][p] */
+	if (p->wxt) {
+		p->wxperm = malloc((size_t)(p->dim ? p->dim : 1) * sizeof(int32_t));
+		if (!p->wxperm) ERR("out of host memory");
+		for (int b = 0; b < p->nblocks; b++) {
+			const jn_block_t *B = &p->blocks[b];
+			for (int64_t n = 0; n < B->Nn; n++)
+				for (int64_t q = 0; q < B->Np; q++) p->wxperm[B->offset + n * B->Np + q] = (int32_t)(B->offset + q * B->Nn + n);
+		}
+	}
 	/* one spare row word: the kernel reads the word after a group's last row ahead of time */
 	if (vec_reserve(&rows, 1)) ERR("out of host memory");
 	((uint32_t *)rows.a)[rows.n] = 0u;
@@ -407,8 +427,10 @@ fail:
 	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
 	free(gblock.a);
 	free(R); free(chunk); free(stamp); free(order);
-	free(p->wtpos);
+	free(p->wtpos); free(p->wxperm);
 	p->wtpos = NULL;
+	p->wxperm = NULL;
+	p->wxt = 0;
 	p->n_wme = 0;
 	return 1;
 }

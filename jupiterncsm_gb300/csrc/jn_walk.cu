@@ -121,13 +121,13 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 					  const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
 					  const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
 					  const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
-					  const typename WalkT<MODE>::X *__restrict__ x, unsigned long long *__restrict__ gacc,
-					  unsigned int *__restrict__ lo, unsigned int *__restrict__ hi, int lane, int sh, float scalef,
-					  double scale)
+					  const typename WalkT<MODE>::X *__restrict__ x, const typename WalkT<MODE>::X *__restrict__ xt,
+					  unsigned long long *__restrict__ gacc, unsigned int *__restrict__ lo,
+					  unsigned int *__restrict__ hi, int lane, int sh, float scalef, double scale)
 {
 	typedef typename WalkT<MODE>::C C;
 	typedef typename WalkT<MODE>::X X;
-	const int src_off = (int)pa.x, dst_off = (int)pa.y, Nn_src = (int)pa.z, Nn_dst = (int)pa.w;
+	const int src_off = (int)pa.x, dst_off = (int)pa.y, stride = (int)pa.z, Nn_dst = (int)pa.w;
 	const int rs = (int)(pb.w & 0xffu), wp = (int)((pb.w >> 8) & 1u), ngroups = (int)(pb.w >> 9);
 	const uint32_t *__restrict__ L = lanes + ta.y + lane;
 	const int ws = (int)__ldg(L);
@@ -138,11 +138,8 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 		off[2 * k] = (int)(w & 0xffffu);
 		off[2 * k + 1] = (int)(w >> 16);
 	}
-	if (wp) {
-#pragma unroll
-		for (int u = 0; u < U; u++) off[u] *= Nn_src;
-	}
-	const X *__restrict__ xs = x + src_off;
+	/* proton walks read the transposed view: a row's entries index one row of the source block */
+	const X *__restrict__ xs = (wp ? xt : x) + src_off;
 	int j = (int)pb.x;
 	uint32_t row = __ldg(rows + j);
 	for (int g = 0; g < ngroups; g++) {
@@ -173,8 +170,8 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 			const uint32_t row2 = __ldg(rows + j + 1);
 			const bool two = !(row & JN_WALK_GROUP_END);
 			const int sr = (int)(row & 0xffffu), sr2 = (int)(row2 & 0xffffu);
-			const X *__restrict__ xb = xs + (wp ? sr : sr * Nn_src);
-			const X *__restrict__ xb2 = xs + (two ? (wp ? sr2 : sr2 * Nn_src) : 0);
+			const X *__restrict__ xb = xs + sr * stride;
+			const X *__restrict__ xb2 = xs + (two ? sr2 * stride : 0);
 			X xv[U], xv2[U];
 #pragma unroll
 			for (int u = 0; u < U; u++) xv[u] = __ldg(xb + off[u]);
@@ -212,7 +209,7 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		       const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
 		       const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
 		       const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
-		       const typename WalkT<MODE>::X *__restrict__ x,
+		       const typename WalkT<MODE>::X *__restrict__ x, const typename WalkT<MODE>::X *__restrict__ xt,
 		       unsigned long long *__restrict__ gacc, const unsigned int *__restrict__ ctrl, long long ntasks,
 		       double abs_bound, int Sc, int nsm)
 {
@@ -237,22 +234,41 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		const uint4 pa = __ldg(pieces + 2 * ta.x), pb = __ldg(pieces + 2 * ta.x + 1);
 		const uint32_t U = (ta.w >> 8) & 0xffu;
 		if (U == 8)
-			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+					       scale);
 		else if (U == 4)
-			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+					       scale);
 		else
-			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, gacc, lo, hi, lane, sh, scalef, scale);
+			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+					       scale);
 	}
 }
 
 /* x as 52-bit fixed-point integers {high 28 bits (signed), low 24 bits} */
-__global__ void jn_walk_xsplit_kernel(const double *__restrict__ x, int2 *__restrict__ xi, int64_t n,
-				      const unsigned int *__restrict__ ctrl)
+__device__ __forceinline__ int2 walk_xsplit(double v, double s)
 {
-	const double s = ldexp(1.0, walk_x_exponent(ctrl[0]));
+	const long long q = __double2ll_rn(v * s);
+	return make_int2((int)(q >> 24), (int)(q & 0xffffff));
+}
+
+/* the x views the walk kernel reads in the arithmetic MODE: the integer
+ * path's split copy of x (MODE 1; MODE 32 gets its FP32 copy from the max|x|
+ * pass), and, where proton walks exist (perm != NULL), the transposed view
+ * xT[i] = x[perm[i]] */
+template <int MODE>
+__global__ void jn_walk_xview_kernel(const double *__restrict__ x, const int32_t *__restrict__ perm,
+				     typename WalkT<MODE>::X *__restrict__ xv, typename WalkT<MODE>::X *__restrict__ xt, int64_t n,
+				     const unsigned int *__restrict__ ctrl)
+{
+	const double s = MODE == 1 ? ldexp(1.0, walk_x_exponent(ctrl[0])) : 1.0;
 	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const long long v = __double2ll_rn(x[i] * s);
-		xi[i] = make_int2((int)(v >> 24), (int)(v & 0xffffff));
+		if constexpr (MODE == 1) {
+			xv[i] = walk_xsplit(x[i], s);
+			if (perm) xt[i] = walk_xsplit(__ldg(x + __ldg(perm + i)), s);
+		} else {
+			xt[i] = (typename WalkT<MODE>::X)__ldg(x + __ldg(perm + i));
+		}
 	}
 }
 
@@ -300,10 +316,11 @@ static int walk_slot(int mode) { return mode == 32 ? 0 : (mode == 64 ? 1 : 2); }
 void jn_walk_release(jn_ctx *c)
 {
 	cudaFree(c->d_wtasks); cudaFree(c->d_wpieces); cudaFree(c->d_wlanes); cudaFree(c->d_wwalks); cudaFree(c->d_wrows);
-	cudaFree(c->d_wrdst); cudaFree(c->d_wgroups); cudaFree(c->d_wgshift); cudaFree(c->d_wx);
+	cudaFree(c->d_wrdst); cudaFree(c->d_wgroups); cudaFree(c->d_wgshift); cudaFree(c->d_wx); cudaFree(c->d_wxt);
+	cudaFree(c->d_wxperm);
 	for (int i = 0; i < 3; i++) cudaFree(c->d_welem[i]);
 	c->d_wtasks = NULL; c->d_wpieces = NULL; c->d_wlanes = NULL; c->d_wwalks = NULL; c->d_wrows = NULL;
-	c->d_wrdst = NULL; c->d_wgroups = NULL; c->d_wgshift = NULL; c->d_wx = NULL;
+	c->d_wrdst = NULL; c->d_wgroups = NULL; c->d_wgshift = NULL; c->d_wx = NULL; c->d_wxt = NULL; c->d_wxperm = NULL;
 	for (int i = 0; i < 3; i++) c->d_welem[i] = NULL;
 	c->walk_ready = 0;
 }
@@ -330,7 +347,9 @@ jn_status jn_walk_setup(jn_ctx *c)
 	    (s = wupload(&c->d_wrows, p->wrows, (size_t)p->n_wrows + 1)) ||
 	    (s = wupload(&c->d_wrdst, p->wrdst, (size_t)p->n_wrdst)) ||
 	    (s = wupload(&c->d_wgroups, p->wgroups, (size_t)p->n_wgroups)) ||
-	    (s = wupload(&c->d_wx, (const void *)NULL, (size_t)(p->dim ? p->dim : 1)))) {
+	    (s = wupload(&c->d_wx, (const void *)NULL, (size_t)(p->dim ? p->dim : 1))) ||
+	    (p->wxt && (s = wupload(&c->d_wxt, (const void *)NULL, (size_t)(p->dim ? p->dim : 1)))) ||
+	    (p->wxt && (s = wupload(&c->d_wxperm, p->wxperm, (size_t)p->dim)))) {
 		jn_walk_release(c);
 		return s;
 	}
@@ -430,7 +449,13 @@ jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumul
 	CUDA_TRY(cudaMemsetAsync(c->d_xmax, 0, 2 * sizeof(unsigned int), st));
 	if (p->dim) {
 		jn_launch_prep(d_x, mode == 32 ? (float *)c->d_wx : NULL, p->dim, c->d_xmax, st);
-		if (mode == 1) jn_walk_xsplit_kernel<<<g, 256, 0, st>>>(d_x, c->d_wx, p->dim, c->d_xmax);
+		const int32_t *perm = p->wxt ? c->d_wxperm : NULL;
+		if (mode == 1)
+			jn_walk_xview_kernel<1><<<g, 256, 0, st>>>(d_x, perm, c->d_wx, c->d_wxt, p->dim, c->d_xmax);
+		else if (perm && mode == 32)
+			jn_walk_xview_kernel<32><<<g, 256, 0, st>>>(d_x, perm, NULL, (float *)c->d_wxt, p->dim, c->d_xmax);
+		else if (perm)
+			jn_walk_xview_kernel<64><<<g, 256, 0, st>>>(d_x, perm, NULL, (double *)c->d_wxt, p->dim, c->d_xmax);
 	}
 	if (pre) cudaEventRecord(pre, st);
 	if (p->nwtasks) {
@@ -439,15 +464,15 @@ jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumul
 		if (mode == 32)
 			jn_walk_kernel<32><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const float *)c->d_welem[0],
-				(const float *)c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+				(const float *)c->d_wx, (const float *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
 		else if (mode == 64)
 			jn_walk_kernel<64><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const double *)c->d_welem[1],
-				d_x, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+				d_x, (const double *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
 		else
 			jn_walk_kernel<1><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, c->d_wgshift, (const int2 *)c->d_welem[2],
-				c->d_wx, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc, c->num_sms);
+				c->d_wx, c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc, c->num_sms);
 	}
 	if (mid) cudaEventRecord(mid, st);
 	if (p->dim) jn_walk_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, c->d_xmax, p->abs_bound, c->walk_sc, mode,

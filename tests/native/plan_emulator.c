@@ -528,6 +528,14 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 		xh[i] = (int32_t)(v >> 24);
 		xl[i] = (int32_t)(v & 0xffffff);
 	}
+	/* the transposed view that proton walks read: xT[i] = x[perm[i]] in every type */
+	double *xT = malloc((D ? D : 1) * sizeof(double));
+	float *x32T = malloc((D ? D : 1) * sizeof(float));
+	int32_t *xhT = malloc((D ? D : 1) * sizeof(int32_t)), *xlT = malloc((D ? D : 1) * sizeof(int32_t));
+	for (int64_t i = 0; i < D; i++) {
+		const int64_t q = P->wxt ? P->wxperm[i] : i;
+		xT[i] = x[q]; x32T[i] = x32[q]; xhT[i] = xh[q]; xlT[i] = xl[q];
+	}
 	jn_walk_elements(P, P->me, a64);
 	int32_t *split = malloc((nm ? nm : 1) * 2 * sizeof(int32_t));
 	uint8_t *gshift = malloc(P->n_wgroups ? P->n_wgroups : 1);
@@ -588,23 +596,27 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 					int64_t A = 0, B = 0;
 					float accf = 0.0f;
 					double accd = 0.0;
+					/* proton walks read the transposed view */
+					const double *X64 = wp ? xT : x;
+					const float *X32 = wp ? x32T : x32;
+					const int32_t *XH = wp ? xhT : xh, *XL = wp ? xlT : xl;
 					for (int u = 0; u < U; u++) {
-						const int64_t xi = pc->src_off + (wp ? (int64_t)src[u] * pc->Nn_src + sr : (int64_t)sr * pc->Nn_src + src[u]);
+						const int64_t xi = pc->src_off + (int64_t)sr * pc->src_stride + src[u];
 						if (xi < 0 || xi >= D) { bad = 1; break; }
 						const int pad = (ko[u] & JN_WALK_PADBIT) != 0, neg = (ko[u] >> 31) != 0;
 						if (mode == 1) {
 							int32_t ch = pad ? 0 : ah[ai[u]], cl = pad ? 0 : al[ai[u]];
 							if (neg) { ch = -ch; cl = -cl; }
-							A += (int64_t)ch * xh[xi];
-							B += (int64_t)ch * xl[xi] + (int64_t)cl * xh[xi];
+							A += (int64_t)ch * XH[xi];
+							B += (int64_t)ch * XL[xi] + (int64_t)cl * XH[xi];
 						} else if (mode == 32) {
 							float c = pad ? 0.0f : a32[ai[u]];
 							if (neg) c = -c;
-							accf = fmaf(c, x32[xi], accf);
+							accf = fmaf(c, X32[xi], accf);
 						} else {
 							double c = pad ? 0.0 : a64[ai[u]];
 							if (neg) c = -c;
-							accd = fma(c, x[xi], accd);
+							accd = fma(c, X64[xi], accd);
 						}
 					}
 					if (mode == 1) {
@@ -632,6 +644,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 	const double unit = ldexp(1.0, -S);
 	for (int64_t i = 0; i < D; i++) y[i] = accumulate ? y[i] + (double)gacc[i] * unit : (double)gacc[i] * unit;
 	free(slot); free(x32); free(a32); free(xh); free(xl); free(a64); free(ah); free(al); free(gacc); free(gshift);
+	free(xT); free(x32T); free(xhT); free(xlT);
 	return bad;
 }
 
