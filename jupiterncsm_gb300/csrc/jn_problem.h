@@ -222,11 +222,14 @@ typedef struct {
  */
 #define JN_WALK_RS 16           /* distinct destination rows of a piece */
 #define JN_WALK_GROUP_END 0x40000000u   /* row word: the last row of its group */
-#define JN_WALK_PADBIT 0x40000000u      /* lane entry: padding (coefficient 0) */
+#define JN_WALK_POS 0x40000000u         /* lane entry multiplier +1 (bits 31:30 = 01) */
+#define JN_WALK_NEG 0xC0000000u         /* lane entry multiplier -1 (bits 31:30 = 11); 00 is padding (0) */
 
-/* lane record of a chunk set, word-major (32 lanes per word): the walk slot,
- * U / 2 words of packed 16-bit sources, U words of element offset | pad << 30
- * | sign << 31 */
+/* lane record of a chunk set, word-major (32 lanes per word): the walk slot
+ * | the entries' multipliers << 16 (2 bits for entry u at bit 16 + 2u), U / 2
+ * words of packed 16-bit sources, U words of element offset (30 bits) |
+ * multiplier << 30.  A multiplier is a 2-bit two's complement: +1 (01), -1
+ * (11), or 0 for padding (00). */
 #define JN_WALK_LANE_WORDS(U) (1 + (U) / 2 + (U))
 
 typedef struct {                /* 32 bytes */

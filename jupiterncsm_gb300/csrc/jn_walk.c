@@ -304,9 +304,13 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 							/* padding repeats the lane's first source with coefficient 0 */
 							const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
 							src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
-							koff[u] = i < ne ? p->ent[2 * e + 1] : JN_WALK_PADBIT;
+							koff[u] = i < ne ? (p->ent[2 * e + 1] & 0x3fffffffu) |
+										   ((p->ent[2 * e + 1] >> 31) ? JN_WALK_NEG : JN_WALK_POS)
+									 : 0u;
 						}
-						L[l + r] = c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u;
+						uint32_t mul = 0;
+						for (int u = 0; u < U; u++) mul |= (koff[u] >> 30) << (2 * u);
+						L[l + r] = (c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u) | (mul << 16);
 						for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
 						for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
 					}
@@ -392,9 +396,9 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 			free(set_walk0);
 		}
 	}
-	/* tasks stay in this order: warps take them cyclically (warp w of W runs
-	   tasks w, w + W, ...), so warps that run at the same time work on
-	   neighbouring instructions and share their matrix elements in L2 */
+	/* tasks stay in this order: warps take the next one from a counter, so
+	   warps that run at the same time work on neighbouring instructions and
+	   share their matrix elements in L2 */
 	/* the transposed view of x that proton walks read: block [n][p] */
 	if (p->wxt) {
 		p->wxperm = malloc((size_t)(p->dim ? p->dim : 1) * sizeof(int32_t));
@@ -408,7 +412,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	/* one spare row word: the kernel reads the word after a group's last row ahead of time */
 	if (vec_reserve(&rows, 1)) ERR("out of host memory");
 	((uint32_t *)rows.a)[rows.n] = 0u;
-	if (tasks.n > 0xffffffffll || lanes.n > 0xffffffffll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
+	if (tasks.n > 0xf0000000ll || lanes.n > 0xffffffffll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
 	    rdst.n > 0x7fffffffll || groups.n > 0x7fffffffll || pieces.n > 0xffffffffll)
 		ERR("the walk plan is too large");
 	p->wtasks = tasks.a; p->nwtasks = tasks.n;

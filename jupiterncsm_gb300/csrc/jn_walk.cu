@@ -44,6 +44,8 @@
 #include "jn_internal.h"
 #include "jn_fixed.cuh"
 
+#include <type_traits>
+
 #define WALK_WARPS 8
 #define WALK_THREADS (WALK_WARPS * 32)
 #define WALK_SLOTS (JN_WALK_RS * 32)    /* per warp: lo words, then hi words */
@@ -112,10 +114,27 @@ __device__ __forceinline__ long long walk_row(const typename WalkT<MODE>::C *c, 
 	return v;
 }
 
+/* the coefficient of lane entry u from its raw element and the lane's
+ * multipliers (2 bits per entry, a two's complement: +1, -1, or 0 for
+ * padding) */
+template <int MODE>
+__device__ __forceinline__ typename WalkT<MODE>::C walk_coef(typename WalkT<MODE>::C v, uint32_t mul, int u)
+{
+	const int m = (int)(mul << (30 - 2 * u)) >> 30;
+	if constexpr (MODE == 1) {
+		return make_int2(v.x * m, v.y * m);
+	} else {
+		if (!m) v = 0;
+		return m < 0 ? -v : v;
+	}
+}
+
 /* one warp task with chunks of U entries (see the file comment).  Rows are
  * taken two at a time, so that two rows' gathers of x are in flight at once;
  * the word after a group's last row is read ahead (the plan keeps a spare
- * word at the end) and not used. */
+ * word at the end) and not used.  A group's first row pair issues its
+ * gathers of x before the coefficients (loaded at the top of the group) are
+ * first used, so the two latencies overlap. */
 template <int MODE, int U>
 __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const uint4 pb, const uint32_t *__restrict__ lanes,
 					  const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
@@ -130,7 +149,9 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 	const int src_off = (int)pa.x, dst_off = (int)pa.y, stride = (int)pa.z, Nn_dst = (int)pa.w;
 	const int rs = (int)(pb.w & 0xffu), wp = (int)((pb.w >> 8) & 1u), ngroups = (int)(pb.w >> 9);
 	const uint32_t *__restrict__ L = lanes + ta.y + lane;
-	const int ws = (int)__ldg(L);
+	const uint32_t head = __ldg(L);
+	const int ws = (int)(head & 0xffffu);
+	const uint32_t mul = head >> 16;
 	int off[U];
 #pragma unroll
 	for (int k = 0; k < U / 2; k++) {
@@ -152,32 +173,24 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 		}
 		C c[U];
 #pragma unroll
-		for (int u = 0; u < U; u++) {
-			const uint32_t ko = __ldg(L + (1 + U / 2 + u) * 32);
-			C v = __ldg(er + (ko & 0x3fffffffu));
-			const bool pad = (ko & JN_WALK_PADBIT) != 0, neg = (ko >> 31) != 0;
-			if constexpr (MODE == 1) {
-				if (pad) v = make_int2(0, 0);
-				if (neg) v = make_int2(-v.x, -v.y);
-			} else {
-				if (pad) v = (C)0;
-				if (neg) v = -v;
-			}
-			c[u] = v;
-		}
-		for (;;) {
+		for (int u = 0; u < U; u++) c[u] = __ldg(er + (__ldg(L + (1 + U / 2 + u) * 32) & 0x3fffffffu));
+		for (bool first = true;; first = false) {
 			/* this row and the next one of the group (if any) */
 			const uint32_t row2 = __ldg(rows + j + 1);
 			const bool two = !(row & JN_WALK_GROUP_END);
-			const int sr = (int)(row & 0xffffu), sr2 = (int)(row2 & 0xffffu);
-			const X *__restrict__ xb = xs + sr * stride;
-			const X *__restrict__ xb2 = xs + (two ? sr2 * stride : 0);
+			const X *__restrict__ xb = xs + (int)(row & 0xffffu) * stride;
+			const X *__restrict__ xb2 = xs + (two ? (int)(row2 & 0xffffu) * stride : 0);
 			X xv[U], xv2[U];
 #pragma unroll
 			for (int u = 0; u < U; u++) xv[u] = __ldg(xb + off[u]);
 #pragma unroll
-			for (int u = 0; u < U; u++) xv2[u] = __ldg(xb2 + (two ? off[u] : 0));
+			for (int u = 0; u < U; u++) xv2[u] = __ldg(xb2 + off[u]);
 			const uint32_t next = __ldg(rows + j + 2);
+			/* the coefficients' multipliers, applied after this pair's gathers are issued */
+			if (first) {
+#pragma unroll
+				for (int u = 0; u < U; u++) c[u] = walk_coef<MODE>(c[u], mul, u);
+			}
 			add_fixed(lo, hi, (int)((row >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv, row, shg, scalef, scale));
 			if (two) add_fixed(lo, hi, (int)((row2 >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv2, row2, shg, scalef, scale));
 			const bool end = !two || (row2 & JN_WALK_GROUP_END);
@@ -210,8 +223,8 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		       const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
 		       const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
 		       const typename WalkT<MODE>::X *__restrict__ x, const typename WalkT<MODE>::X *__restrict__ xt,
-		       unsigned long long *__restrict__ gacc, const unsigned int *__restrict__ ctrl, long long ntasks,
-		       double abs_bound, int Sc, int nsm)
+		       unsigned long long *__restrict__ gacc, unsigned int *__restrict__ ctrl, long long ntasks,
+		       double abs_bound, int Sc)
 {
 	extern __shared__ unsigned int wslots[];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -222,14 +235,16 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 	walk_scales(ctrl[0], abs_bound, Sc, MODE, &S, &sh);
 	const float scalef = MODE == 32 ? __int_as_float((127 + (S < -126 ? -126 : (S > 127 ? 127 : S))) << 23) : 0.0f;
 	const double scale = MODE == 64 ? ldexp(1.0, S) : 0.0;
-	/* warps take tasks cyclically; the warps of the CTAs an SM holds (CTA b
-	   runs on SM b mod nsm when the grid is a multiple of the SM count) get
-	   consecutive indices, so an SM works on neighbouring tasks at a time */
-	const long long nwarps = (long long)gridDim.x * WALK_WARPS;
-	const int per = nsm > 0 && gridDim.x % nsm == 0 ? (int)gridDim.x / nsm : 0;
-	const long long w0 = per ? ((long long)(blockIdx.x % nsm) * per + blockIdx.x / nsm) * WALK_WARPS + warp
-				 : (long long)blockIdx.x * WALK_WARPS + warp;
-	for (long long t = w0; t < ntasks; t += nwarps) {
+	/* warps take the next task from a counter (ctrl[1], zero at launch), so
+	   the tasks in flight stay a window of about two tasks per warp: the
+	   instructions that read one matrix-element block run together and L2
+	   serves the block's rows to all of them (a fixed assignment lets warps
+	   drift apart by many tasks, and the window with them) */
+	unsigned int t = 0, tn = 0;
+	if (lane == 0) t = atomicAdd(ctrl + 1, 1u);
+	t = __shfl_sync(0xffffffffu, t, 0);
+	for (; (long long)t < ntasks; t = __shfl_sync(0xffffffffu, tn, 0)) {
+		if (lane == 0) tn = atomicAdd(ctrl + 1, 1u);
 		const uint4 ta = __ldg(tasks + t);
 		const uint4 pa = __ldg(pieces + 2 * ta.x), pb = __ldg(pieces + 2 * ta.x + 1);
 		const uint32_t U = (ta.w >> 8) & 0xffu;
@@ -464,15 +479,15 @@ jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumul
 		if (mode == 32)
 			jn_walk_kernel<32><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const float *)c->d_welem[0],
-				(const float *)c->d_wx, (const float *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+				(const float *)c->d_wx, (const float *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0);
 		else if (mode == 64)
 			jn_walk_kernel<64><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, NULL, (const double *)c->d_welem[1],
-				d_x, (const double *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0, c->num_sms);
+				d_x, (const double *)c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, 0);
 		else
 			jn_walk_kernel<1><<<grid, WALK_THREADS, WALK_SMEM, st>>>(
 				T, P, c->d_wlanes, c->d_wwalks, c->d_wrows, c->d_wrdst, c->d_wgroups, c->d_wgshift, (const int2 *)c->d_welem[2],
-				c->d_wx, c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc, c->num_sms);
+				c->d_wx, c->d_wxt, c->d_gacc, c->d_xmax, p->nwtasks, p->abs_bound, c->walk_sc);
 	}
 	if (mid) cudaEventRecord(mid, st);
 	if (p->dim) jn_walk_finalize_kernel<<<g, 256, 0, st>>>(c->d_gacc, d_y, p->dim, c->d_xmax, p->abs_bound, c->walk_sc, mode,

@@ -568,7 +568,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 		    (int64_t)pc->rdst0 + rs > P->n_wrdst || (int64_t)pc->group0 + ng > P->n_wgroups) { bad = 1; break; }
 		memset(slot, 0, JN_WALK_RS * 32 * sizeof(int64_t));
 		for (int lane = 0; lane < 32 && !bad; lane++) {
-			const uint32_t ws = P->wlanes[T->lanes + lane];
+			const uint32_t head = P->wlanes[T->lanes + lane], ws = head & 0xffffu, mul = head >> 16;
 			if (ws >= (uint32_t)nw) { bad = 1; break; }
 			uint32_t src[8], ko[8];
 			for (int k = 0; k < U / 2; k++) {
@@ -603,7 +603,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 					for (int u = 0; u < U; u++) {
 						const int64_t xi = pc->src_off + (int64_t)sr * pc->src_stride + src[u];
 						if (xi < 0 || xi >= D) { bad = 1; break; }
-						const int pad = (ko[u] & JN_WALK_PADBIT) != 0, neg = (ko[u] >> 31) != 0;
+						const int m = (int)((mul >> (2 * u)) & 3u), pad = m == 0, neg = m == 3;
 						if (mode == 1) {
 							int32_t ch = pad ? 0 : ah[ai[u]], cl = pad ? 0 : al[ai[u]];
 							if (neg) { ch = -ch; cl = -cl; }
