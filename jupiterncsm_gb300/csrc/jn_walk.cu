@@ -9,19 +9,21 @@
  * transposes :212-462, |M| < 1e-12 skip of single-species terms :52-53).
  *
  * GB300 organisation.  A warp task is 32 lane chunks (up to U = 8, 4 or 2
- * entries of one walk each: one destination column) times the rows of a
- * piece.  The rows are grouped by their connection index: a group reads one
- * contiguous row of its matrix-element block (of its transposed copy for
- * proton walks), so a lane gathers the coefficients of its chunk from that
- * row once per group, through L1, and reuses them for every row of the
- * group; instructions that share a block run on neighbouring warps, and L2
- * serves each element to all of them.  For each row the lane gathers its
- * chunk's x values, sums the U products in registers, rounds the sum once
- * to the 64-bit fixed-point unit and adds it into a warp-private slot
- * (destination row, walk) in shared memory; after the task the warp adds
- * its slots into the global accumulator.  Shared-memory adds are U times
- * fewer than contributions, global adds a further factor of the rows per
- * destination fewer.
+ * entries of one walk each: one destination column; a walk's entries are
+ * dealt to its lanes in turn) times the rows of a piece.  The rows are
+ * grouped by their connection index: a group reads one contiguous row of its
+ * matrix-element block (of its transposed copy for proton walks), so a lane
+ * gathers the coefficients of its chunk from that row once per group,
+ * through L1, and reuses them for every row of the group.  Warps take tasks
+ * from a counter, so the tasks in flight are a narrow window of the plan's
+ * order, which keeps the instructions that share a block together: L2 serves
+ * each element to all of them.  For each row the lane gathers its chunk's x
+ * values, sums the U products in registers, rounds the sum once to the
+ * 64-bit fixed-point unit and adds it into its own slot (destination row,
+ * lane) in shared memory: no atomics, no bank conflicts.  After the task a
+ * segmented sum over the lanes of each walk gives one global add per
+ * (destination row, walk).  A CTA is one warp, so the register file alone
+ * sets how many warps an SM holds.
  *
  * Arithmetic (the template parameter MODE):
  *   32  FP32 coefficients and x, fused multiply-adds in entry order;
@@ -46,10 +48,10 @@
 
 #include <type_traits>
 
-#define WALK_WARPS 8
+#define WALK_WARPS 1     /* one warp a CTA: the register file, not CTA granularity, sets the warps an SM holds */
 #define WALK_THREADS (WALK_WARPS * 32)
-#define WALK_SLOTS (JN_WALK_RS * 32)    /* per warp: lo words, then hi words */
-#define WALK_SMEM ((size_t)WALK_WARPS * 2 * WALK_SLOTS * sizeof(unsigned int))
+#define WALK_SLOTS (JN_WALK_RS * 32)    /* per warp: one 64-bit slot per (destination row, lane) */
+#define WALK_SMEM ((size_t)WALK_WARPS * WALK_SLOTS * sizeof(unsigned long long))
 
 static_assert(sizeof(jn_wtask_t) == 16 && sizeof(jn_wpiece_t) == 32, "tasks are read as one uint4, pieces as two");
 
@@ -63,13 +65,13 @@ __device__ __forceinline__ int walk_x_exponent(unsigned int xmax_bits)
 /* The output unit 2^-S and, for the integer path, the shift of a row sum
  * A 2^48 + B 2^24 (in units of 2^-(Sc + Sx)) down to it: S is the usual
  * fixed-point exponent (|y| 2^S < 2^62), lowered where needed so that the
- * shift is at least 48 bits. */
+ * shift is at least 49 bits (48 + sh, sh >= 1). */
 __device__ __forceinline__ void walk_scales(unsigned int xmax_bits, double abs_bound, int Sc, int mode, int *S, int *sh)
 {
 	int s = fixed_exponent(xmax_bits, abs_bound), k = 0;
 	if (mode == 1) {
 		const int Sx = walk_x_exponent(xmax_bits);
-		if (Sc + Sx - s < 48) s = Sc + Sx - 48;
+		if (Sc + Sx - s < 49) s = Sc + Sx - 49;
 		k = Sc + Sx - s - 48;
 		if (k > 63) k = 63;
 	}
@@ -96,10 +98,10 @@ __device__ __forceinline__ long long walk_row(const typename WalkT<MODE>::C *c, 
 			B += (long long)c[u].x * xv[u].y;
 			B += (long long)c[u].y * xv[u].x;
 		}
-		/* A 2^48 + B 2^24 rounded to the nearest multiple of 2^(48 + sh) */
-		const long long q = A + (B >> 24);
-		v = sh ? (q + (1ll << (sh - 1))) >> sh : q + ((B >> 23) & 1);
-		if (row >> 31) v = -v;
+		/* A 2^48 + B 2^24 rounded to the nearest multiple of 2^(48 + sh), sh >= 1
+		   (ties up), then given the row's sign */
+		const long long q = A + (B >> 24), m = (long long)((int)row >> 31);
+		v = (((q + (1ll << (sh - 1))) >> sh) ^ m) - m;
 	} else if constexpr (MODE == 32) {
 		float acc = 0.0f;
 #pragma unroll
@@ -141,8 +143,8 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 					  const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
 					  const uint8_t *__restrict__ gshift, const typename WalkT<MODE>::C *__restrict__ elem,
 					  const typename WalkT<MODE>::X *__restrict__ x, const typename WalkT<MODE>::X *__restrict__ xt,
-					  unsigned long long *__restrict__ gacc, unsigned int *__restrict__ lo,
-					  unsigned int *__restrict__ hi, int lane, int sh, float scalef, double scale)
+					  unsigned long long *__restrict__ gacc, unsigned long long *__restrict__ slots, int lane,
+					  int sh, float scalef, double scale)
 {
 	typedef typename WalkT<MODE>::C C;
 	typedef typename WalkT<MODE>::X X;
@@ -191,8 +193,10 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 #pragma unroll
 				for (int u = 0; u < U; u++) c[u] = walk_coef<MODE>(c[u], mul, u);
 			}
-			add_fixed(lo, hi, (int)((row >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv, row, shg, scalef, scale));
-			if (two) add_fixed(lo, hi, (int)((row2 >> 16) & 31u) * 32 + ws, walk_row<MODE, U>(c, xv2, row2, shg, scalef, scale));
+			slots[(int)((row >> 16) & 31u) * 32 + lane] += (unsigned long long)walk_row<MODE, U>(c, xv, row, shg, scalef, scale);
+			if (two)
+				slots[(int)((row2 >> 16) & 31u) * 32 + lane] +=
+					(unsigned long long)walk_row<MODE, U>(c, xv2, row2, shg, scalef, scale);
 			const bool end = !two || (row2 & JN_WALK_GROUP_END);
 			j += two ? 2 : 1;
 			row = two ? next : row2;
@@ -200,24 +204,35 @@ __device__ __forceinline__ void walk_task(const uint4 ta, const uint4 pa, const 
 		}
 	}
 	__syncwarp();
-	/* the task's slots into the global accumulator; slots are left zero */
-	const int nw = (int)(ta.w & 0xffu), n = rs * nw;
-	for (int i = lane; i < n; i += 32) {
-		const int r = i / nw, w = i - r * nw, s = r * 32 + w;
-		const unsigned long long v = (unsigned long long)lo[s] | ((unsigned long long)hi[s] << 32);
-		if (v) {
-			lo[s] = 0u;
-			hi[s] = 0u;
-			const int dr = (int)__ldg(rdst + (int)pb.y + r), dw = (int)__ldg(walks + ta.z + w);
+	/* the task's slots into the global accumulator; slots are left zero.  The
+	   lanes of one walk are a run of neighbouring lanes: a segmented sum over
+	   each run (shuffles down, log2 of the longest run steps) leaves the
+	   walk's total in the run's first lane, which adds it */
+	const int ws_prev = __shfl_up_sync(0xffffffffu, ws, 1);     /* every lane takes part */
+	const unsigned int starts = __ballot_sync(0xffffffffu, lane == 0 || ws != ws_prev);
+	const unsigned int after = lane == 31 ? 0u : starts >> (lane + 1);
+	const int end = after ? lane + __ffs(after) : 32;
+	const bool first = (starts >> lane) & 1u;
+	const int longest = __reduce_max_sync(0xffffffffu, first ? (unsigned int)(end - lane) : 0u);
+	const int dw = (int)__ldg(walks + ta.z + ws);
+	for (int r = 0; r < rs; r++) {
+		unsigned long long v = slots[r * 32 + lane];
+		slots[r * 32 + lane] = 0ull;
+		for (int d = 1; d < longest; d <<= 1) {
+			const unsigned long long t = __shfl_down_sync(0xffffffffu, v, d);
+			if (lane + d < end) v += t;
+		}
+		if (first && v) {
+			const int dr = (int)__ldg(rdst + (int)pb.y + r);
 			atomicAdd(gacc + dst_off + (wp ? dw * Nn_dst + dr : dr * Nn_dst + dw), v);
 		}
 	}
 	__syncwarp();
 }
 
-/* FP32: 4 CTAs an SM (64 registers); the 64-bit paths need more registers: 3 */
+/* FP32: 32 warps an SM (64 registers); the 64-bit paths need more registers: 28 (72) */
 template <int MODE>
-__global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
+__global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 32 : 28)
 	jn_walk_kernel(const uint4 *__restrict__ tasks, const uint4 *__restrict__ pieces, const uint32_t *__restrict__ lanes,
 		       const uint32_t *__restrict__ walks, const uint32_t *__restrict__ rows,
 		       const uint32_t *__restrict__ rdst, const uint32_t *__restrict__ groups,
@@ -226,10 +241,10 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		       unsigned long long *__restrict__ gacc, unsigned int *__restrict__ ctrl, long long ntasks,
 		       double abs_bound, int Sc)
 {
-	extern __shared__ unsigned int wslots[];
+	extern __shared__ unsigned long long wslots[];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	unsigned int *lo = wslots + warp * 2 * WALK_SLOTS, *hi = lo + WALK_SLOTS;
-	for (int i = lane; i < 2 * WALK_SLOTS; i += 32) lo[i] = 0u;
+	unsigned long long *slots = wslots + warp * WALK_SLOTS;
+	for (int i = lane; i < WALK_SLOTS; i += 32) slots[i] = 0ull;
 	__syncwarp();
 	int S, sh;
 	walk_scales(ctrl[0], abs_bound, Sc, MODE, &S, &sh);
@@ -249,13 +264,13 @@ __global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 4 : 3)
 		const uint4 pa = __ldg(pieces + 2 * ta.x), pb = __ldg(pieces + 2 * ta.x + 1);
 		const uint32_t U = (ta.w >> 8) & 0xffu;
 		if (U == 8)
-			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+			walk_task<MODE, 8>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, slots, lane, sh, scalef,
 					       scale);
 		else if (U == 4)
-			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+			walk_task<MODE, 4>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, slots, lane, sh, scalef,
 					       scale);
 		else
-			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, lo, hi, lane, sh, scalef,
+			walk_task<MODE, 2>(ta, pa, pb, lanes, walks, rows, rdst, groups, gshift, elem, x, xt, gacc, slots, lane, sh, scalef,
 					       scale);
 	}
 }
