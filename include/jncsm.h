@@ -367,6 +367,24 @@ typedef struct {
 
 jn_status jn_lanczos_batch(jn_ctx *ctx, const jn_batch_options *options, jn_batch_result *results);
 
+/*
+ * Batched Lanczos over several bases in one solve: options[b] gives basis
+ * b's instances (num_instances, matrix_elements, start_vectors,
+ * eigenvectors; the solver options must be the same for every basis) and
+ * results[b] receives them.  Every step is one captured graph for all
+ * instances of all bases: one persistent walk-engine launch computes every
+ * instance's product (the instances' walk plans concatenated into one task
+ * list, each instance with its own matrix elements), then one launch per
+ * vector kernel.  Products in FP32 (precision 32) or FP64 multiply-adds
+ * (precision 64), exact fixed-point sums; refinement in FP64.  The contexts
+ * must be on one device; the solve runs on ctxs[0]'s stream.  No counterpart
+ * in the reference: Vulcan (src/Vulcan/programs/vulcan.c:114-141) writes one
+ * H(c) = sum_i c_i H_i to disk, and each H(c) is then a Bacchus run of its
+ * own.
+ */
+jn_status jn_lanczos_batch_bases(jn_ctx *const *ctxs, int num_bases, const jn_batch_options *options,
+				 jn_batch_result *const *results);
+
 /* ------------------------------------------------------------------ */
 /* J-scheme -> M-scheme two-body transform (Mercury)                   */
 /* ------------------------------------------------------------------ */

@@ -148,6 +148,7 @@ def gpu_lib():
     L.jn_read_matrix_elements.argtypes = [vp, cp, vp]
     L.jn_set_matrix_elements.argtypes = [vp, vp]
     L.jn_lanczos_batch.argtypes = [vp, ctypes.POINTER(BatchOptions), vp]
+    L.jn_lanczos_batch_bases.argtypes = [vp, ci, ctypes.POINTER(BatchOptions), vp]
     L.jn_transform_open.argtypes = [cp, cp, ci, ci, ci, ci, cp, ci, ctypes.POINTER(vp)]
     L.jn_transform_run.argtypes = [vp, vp]
     L.jn_transform_profile.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
@@ -216,7 +217,8 @@ def gpu_lib():
                  "jn_lanczos_ritz_values", "jn_lanczos_eigenvector", "jn_lanczos_save_eigenvectors",
                  "jn_transform_open", "jn_transform_run", "jn_transform_profile", "jn_transform_elements",
                  "jn_transform_write", "jn_transform_get_stats", "jn_transform_2nf", "jn_read_matrix_elements",
-                 "jn_set_matrix_elements", "jn_lanczos_batch", "jn_transform3_open", "jn_transform3_run",
+                 "jn_set_matrix_elements", "jn_lanczos_batch", "jn_lanczos_batch_bases", "jn_transform3_open",
+                 "jn_transform3_run",
                  "jn_transform3_profile", "jn_transform3_elements", "jn_transform3_write", "jn_transform3_get_stats",
                  "jn_transform_3nf"):
         getattr(L, name).restype = ci
@@ -340,12 +342,7 @@ class Hamiltonian:
             o.eigenvectors = ctypes.cast(gs_ptrs, ctypes.c_void_p)
         res = (BatchResult * B)()
         _check(gpu_lib().jn_lanczos_batch(self._h, ctypes.byref(o), res))
-        out = []
-        for r in res:
-            n = r.num_eigenvalues
-            out.append({"iterations": r.iterations, "converged": bool(r.converged),
-                        "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
-                        "residual_norms": np.array(r.residual_norms[:n])})
+        out = _batch_results(res)
         return (out, gs) if eigenvectors else out
 
     def ritz_values(self):
@@ -431,6 +428,54 @@ class Hamiltonian:
             _check(L.jn_block_info(self._h, b, ctypes.byref(i), ctypes.byref(o), ctypes.byref(n)))
             out.append((i.value, o.value, n.value))
         return out
+
+
+def _batch_results(res):
+    out = []
+    for r in res:
+        n = r.num_eigenvalues
+        out.append({"iterations": r.iterations, "converged": bool(r.converged),
+                    "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
+                    "residual_norms": np.array(r.residual_norms[:n])})
+    return out
+
+
+def lanczos_batch_bases(bases, max_iterations=200, num_eigenvalues=10, tolerance=1e-6, precision=32, check_every=10,
+                        use_graph=True, refine_extra=4, eigenvectors=0):
+    """Solve the Hamiltonians of several bases together (jn_lanczos_batch_bases): bases is a list of
+    (Hamiltonian, [matrix-element arrays], start vectors or None).  Every Lanczos step is one graph with
+    one product launch for all instances of all bases.  Returns, per basis, a list of dicts (and with
+    eigenvectors=k, per basis, the k lowest refined eigenvectors of each instance as (k, D) arrays)."""
+    nb = len(bases)
+    opts = (BatchOptions * nb)()
+    keep, results, gs_all = [], [], []
+    for b, entry in enumerate(bases):
+        H, mes = entry[0], [np.ascontiguousarray(m, dtype=np.float64) for m in entry[1]]
+        svs = entry[2] if len(entry) > 2 else None
+        B = len(mes)
+        me_ptrs = (ctypes.c_void_p * B)(*[m.ctypes.data for m in mes])
+        o = opts[b]
+        o.num_instances, o.matrix_elements = B, ctypes.cast(me_ptrs, ctypes.c_void_p)
+        o.max_iterations, o.num_eigenvalues, o.tolerance, o.precision = max_iterations, num_eigenvalues, tolerance, precision
+        o.check_every, o.use_graph, o.refine_extra, o.num_eigenvectors = check_every, int(use_graph), refine_extra, int(eigenvectors)
+        keep += [mes, me_ptrs]
+        if svs is not None:
+            svs = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in svs]
+            sv_ptrs = (ctypes.c_void_p * B)(*[None if v is None else v.ctypes.data for v in svs])
+            o.start_vectors = ctypes.cast(sv_ptrs, ctypes.c_void_p)
+            keep += [svs, sv_ptrs]
+        if eigenvectors:
+            gs = [np.zeros((eigenvectors, H.dimension)) for _ in range(B)]
+            gs_ptrs = (ctypes.c_void_p * B)(*[g.ctypes.data for g in gs])
+            o.eigenvectors = ctypes.cast(gs_ptrs, ctypes.c_void_p)
+            keep += [gs_ptrs]
+            gs_all.append(gs)
+        results.append((BatchResult * B)())
+    ctxs = (ctypes.c_void_p * nb)(*[entry[0]._h for entry in bases])
+    res_ptrs = (ctypes.c_void_p * nb)(*[ctypes.addressof(r) for r in results])
+    _check(gpu_lib().jn_lanczos_batch_bases(ctxs, nb, opts, res_ptrs))
+    out = [_batch_results(r) for r in results]
+    return (out, gs_all) if eigenvectors else out
 
 
 def _f32(a, cols):

@@ -30,6 +30,8 @@
 #include "jn_internal.h"
 #include "jn_tridiag.cuh"
 
+#include <functional>
+
 #define BT 256          /* threads of the vector kernels */
 #define BNB 16          /* reduction CTAs per instance */
 
@@ -39,6 +41,8 @@
 #define SKIP_INACTIVE() \
 	const int inst = blockIdx.y; \
 	if (active && !active[inst]) return
+/* the dimension of an instance: D (the vectors' stride) unless each instance has its own */
+#define DIM_OF(inst) (dims ? dims[inst] : D)
 
 __device__ __forceinline__ void slice(int64_t D, int64_t *i0, int64_t *i1)
 {
@@ -50,15 +54,17 @@ __device__ __forceinline__ void slice(int64_t D, int64_t *i0, int64_t *i1)
 /* part[inst][blk] = x . y over this CTA's slice; x = X + inst*x_ld (+ k*D when xk) */
 __global__ void __launch_bounds__(BT) kb_dot(const double *__restrict__ X, int64_t x_ld, int xk,
 					      const double *__restrict__ Y, int64_t y_ld, int yk, const int *__restrict__ d_k,
-					      int64_t D, double *__restrict__ part, const int *__restrict__ active)
+					      int64_t D, const int64_t *__restrict__ dims, double *__restrict__ part,
+					      const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
+	const int64_t n = DIM_OF(inst);
 	__shared__ double sh[BT];
 	const int k = *d_k;
 	const double *x = X + inst * x_ld + (xk ? (int64_t)k * D : 0);
 	const double *y = Y + inst * y_ld + (yk ? (int64_t)k * D : 0);
 	int64_t i0, i1;
-	slice(D, &i0, &i1);
+	slice(n, &i0, &i1);
 	double s = 0.0;
 	for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(x[i], y[i], s);
 	s = jn_block_sum(s, sh);
@@ -79,14 +85,16 @@ __global__ void kb_finish_dot(const double *__restrict__ part, int nblk, double 
 /* w -= alpha_k v_k + beta_{k-1} v_{k-1} */
 __global__ void kb_three_term(double *__restrict__ W, const double *__restrict__ V, int64_t ldV,
 			      const double *__restrict__ alpha, const double *__restrict__ beta, int64_t ldab,
-			      const int *__restrict__ d_k, int64_t D, const int *__restrict__ active)
+			      const int *__restrict__ d_k, int64_t D, const int64_t *__restrict__ dims,
+			      const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
+	const int64_t n = DIM_OF(inst);
 	const int k = *d_k;
 	const double a = alpha[inst * ldab + k], b = k > 0 ? beta[inst * ldab + k - 1] : 0.0;
 	const double *v = V + inst * ldV + (int64_t)k * D, *u = k > 0 ? v - D : v;
 	double *w = W + inst * D;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		double r = w[i] - a * v[i];
 		if (k > 0) r -= b * u[i];
 		w[i] = r;
@@ -97,15 +105,15 @@ __global__ void kb_three_term(double *__restrict__ W, const double *__restrict__
  * vector j and reduces it with shuffles in a fixed order, so no CTA-wide
  * barrier is taken per vector */
 __global__ void __launch_bounds__(BT) kb_gemv_t(const double *__restrict__ V, int64_t ldV, const double *__restrict__ W,
-						 const int *__restrict__ d_k, int64_t D, double *__restrict__ part, int ncol,
-						 const int *__restrict__ active)
+						 const int *__restrict__ d_k, int64_t D, const int64_t *__restrict__ dims,
+						 double *__restrict__ part, int ncol, const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
 	const int nvec = *d_k + 1;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 	const double *w = W + inst * D;
 	int64_t i0, i1;
-	slice(D, &i0, &i1);
+	slice(DIM_OF(inst), &i0, &i1);
 	for (int j = warp; j < nvec; j += nwarps) {
 		const double *v = V + inst * ldV + (int64_t)j * D;
 		double s = 0.0;
@@ -128,13 +136,15 @@ __global__ void kb_finish(const double *__restrict__ part, int nblk, int ncol, c
 
 /* w -= sum_{j<=k} V_j h_j */
 __global__ void kb_gemv_n_sub(const double *__restrict__ V, int64_t ldV, const double *__restrict__ h, int ncol,
-			      const int *__restrict__ d_k, int64_t D, double *__restrict__ W, const int *__restrict__ active)
+			      const int *__restrict__ d_k, int64_t D, const int64_t *__restrict__ dims, double *__restrict__ W,
+			      const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
+	const int64_t n = DIM_OF(inst);
 	const int nvec = *d_k + 1;
 	const double *hh = h + (int64_t)inst * ncol, *v = V + inst * ldV;
 	double *w = W + inst * D;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		double s = 0.0;
 		for (int j = 0; j < nvec; j++) s = fma(v[(int64_t)j * D + i], hh[j], s);
 		w[i] -= s;
@@ -144,26 +154,30 @@ __global__ void kb_gemv_n_sub(const double *__restrict__ V, int64_t ldV, const d
 /* v_{k+1} = w / |w|, beta_k = |w| (|w|^2 in nrm2[inst]) */
 __global__ void kb_normalize(double *__restrict__ V, int64_t ldV, const double *__restrict__ W,
 			     const double *__restrict__ nrm2, double *__restrict__ beta, int64_t ldab,
-			     const int *__restrict__ d_k, int64_t D, const int *__restrict__ active)
+			     const int *__restrict__ d_k, int64_t D, const int64_t *__restrict__ dims,
+			     const int *__restrict__ active)
 {
 	SKIP_INACTIVE();
+	const int64_t n = DIM_OF(inst);
 	const int k = *d_k;
 	const double b = sqrt(nrm2[inst]);
 	if (blockIdx.x == 0 && threadIdx.x == 0) beta[inst * ldab + k] = b;
 	const double inv = b > 0.0 ? 1.0 / b : 0.0;
 	double *v = V + inst * ldV + (int64_t)(k + 1) * D;
 	const double *w = W + inst * D;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
 		v[i] = w[i] * inv;
 }
 
 /* v_0 /= |v_0| (|v_0|^2 in nrm2[inst]) */
-__global__ void kb_scale_start(double *__restrict__ V, int64_t ldV, const double *__restrict__ nrm2, int64_t D)
+__global__ void kb_scale_start(double *__restrict__ V, int64_t ldV, const double *__restrict__ nrm2, int64_t D,
+			       const int64_t *__restrict__ dims)
 {
 	const int inst = blockIdx.y;
+	const int64_t n = DIM_OF(inst);
 	const double inv = 1.0 / sqrt(nrm2[inst]);
 	double *v = V + inst * ldV;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
 		v[i] *= inv;
 }
 
@@ -237,14 +251,16 @@ __global__ void kb_converged(const double *__restrict__ theta, const double *__r
 
 /* X[inst][j] = sum_{l < n} V[inst][l] Z[inst][j][l], j < r */
 __global__ void kb_ritz(const double *__restrict__ V, int64_t ldV, const double *__restrict__ Z, int ldz,
-			const int *__restrict__ n_arr, int r, int64_t D, double *__restrict__ X)
+			const int *__restrict__ n_arr, int r, int64_t D, const int64_t *__restrict__ dims,
+			double *__restrict__ X)
 {
 	const int inst = blockIdx.y;
 	const int n = n_arr[inst];
+	const int64_t dim = DIM_OF(inst);
 	const double *v = V + inst * ldV;
 	const double *z = Z + (int64_t)inst * r * ldz;
 	double *x = X + (int64_t)inst * r * D;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < dim; i += (int64_t)gridDim.x * blockDim.x)
 		for (int j = 0; j < r; j++) {
 			double s = 0.0;
 			if (j < n)
@@ -255,24 +271,26 @@ __global__ void kb_ritz(const double *__restrict__ V, int64_t ldV, const double 
 
 /* G[inst][i][j] = A[inst][i] . Bm[inst][j]; one CTA per (i, j, inst) */
 __global__ void __launch_bounds__(BT) kb_gram(const double *__restrict__ A, const double *__restrict__ Bm, int r,
-					       int64_t D, double *__restrict__ G)
+					       int64_t D, const int64_t *__restrict__ dims, double *__restrict__ G)
 {
 	__shared__ double sh[BT];
 	const int inst = blockIdx.y, i = blockIdx.x / r, j = blockIdx.x % r;
+	const int64_t n = DIM_OF(inst);
 	const double *a = A + ((int64_t)inst * r + i) * D, *b = Bm + ((int64_t)inst * r + j) * D;
 	double s = 0.0;
-	for (int64_t t = threadIdx.x; t < D; t += blockDim.x) s = fma(a[t], b[t], s);
+	for (int64_t t = threadIdx.x; t < n; t += blockDim.x) s = fma(a[t], b[t], s);
 	s = jn_block_sum(s, sh);
 	if (threadIdx.x == 0) G[((int64_t)inst * r + i) * r + j] = s;
 }
 
 /* out[inst][e] = sum_j X[inst][j] C[inst][e][j], e < nv: the refined vectors */
 __global__ void kb_combine(const double *__restrict__ X, const double *__restrict__ C, int r, int nv, int64_t D,
-			   double *__restrict__ out)
+			   const int64_t *__restrict__ dims, double *__restrict__ out)
 {
 	const int inst = blockIdx.y;
+	const int64_t n = DIM_OF(inst);
 	const double *x = X + (int64_t)inst * r * D;
-	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x)
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
 		for (int e = 0; e < nv; e++) {
 			const double *c = C + ((int64_t)inst * r + e) * r;
 			double s = 0.0;
@@ -402,21 +420,32 @@ static int rayleigh_ritz(const double *G1, const double *G2, const double *G3, i
 /* ------------------------------------------------------------------ */
 /* the solver                                                           */
 /* ------------------------------------------------------------------ */
+/* The instances of one batched solve, their layout and their products.
+ * Instance i has dimension dims[i] <= Dp; its vectors are stored Dp apart. */
+struct batch_job {
+	int B;
+	int64_t Dp;
+	const int64_t *dims;
+	/* W_i = H_i v_k for every active instance, in the solve's arithmetic (k read on the device) */
+	std::function<jn_status(const double *V, int64_t ldV, const int *d_k, double *W, const int *d_active, cudaStream_t)>
+		product;
+	/* HX_i = H_i X_i in FP64-grade arithmetic for every instance (X_i = X + i ld); scratch: B x Dp */
+	std::function<jn_status(const double *X, int64_t ld, double *HX, double *scratch, cudaStream_t)> product64;
+	const double *const *start_vectors;     /* B entries, or NULL */
+	double *const *eigenvectors;            /* B entries, or NULL */
+	jn_batch_result **res;                  /* B results */
+};
+
 struct bstate {
-	double *V, *W, *me64, *x64, *alpha, *beta, *part, *h, *scal, *theta, *zlast, *Z, *work, *X, *HX, *G, *C, *GS;
-	float *me32, *x32;
-	unsigned long long *gacc;
-	unsigned int *ctrl;
+	double *V, *W, *alpha, *beta, *part, *h, *scal, *theta, *zlast, *Z, *work, *X, *HX, *G, *C, *GS;
+	int64_t *dims;
 	int *k, *active, *flag, *narr;
-	int *pcoef, *pxbuf;             /* panel engine: 32-bit coefficients and x of every instance */
-	unsigned long long *pcmax;
 };
 
 static void bstate_free(struct bstate *s)
 {
-	void *p[] = { s->V, s->W, s->me64, s->x64, s->alpha, s->beta, s->part, s->h, s->scal, s->theta, s->zlast, s->Z,
-		      s->work, s->X, s->HX, s->G, s->C, s->GS, s->me32, s->x32, s->gacc, s->ctrl, s->k, s->active,
-		      s->flag, s->narr, s->pcoef, s->pxbuf, s->pcmax };
+	void *p[] = { s->V, s->W, s->alpha, s->beta, s->part, s->h, s->scal, s->theta, s->zlast, s->Z, s->work, s->X,
+		      s->HX, s->G, s->C, s->GS, s->dims, s->k, s->active, s->flag, s->narr };
 	for (size_t i = 0; i < sizeof p / sizeof p[0]; i++) cudaFree(p[i]);
 }
 
@@ -426,17 +455,24 @@ static void bstate_free(struct bstate *s)
 			st = jn_fail(JN_ERR_NOMEM, "batched Lanczos: device allocation of %s failed", #ptr);   \
 	} while (0)
 
-extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_batch_result *res)
+/* the shared options of a batched solve */
+static jn_status batch_check_options(const jn_batch_options *o)
 {
-	if (!c || !o || !res || !o->matrix_elements) return jn_fail(JN_ERR_INVALID, "null argument");
-	const jn_plan_t *p = &c->plan;
-	const int B = o->num_instances;
-	const int64_t D = p->dim, nme = p->n_me;
-	if (B < 1 || B > 4096) return jn_fail(JN_ERR_INVALID, "num_instances must be in 1..4096");
-	if (D < 1) return jn_fail(JN_ERR_INVALID, "empty basis");
 	if (o->precision != 32 && o->precision != 64) return jn_fail(JN_ERR_INVALID, "precision must be 32 or 64");
+	if (o->num_eigenvectors < 0 || o->num_eigenvectors > (o->num_eigenvalues > 0 ? o->num_eigenvalues : 10) ||
+	    o->num_eigenvectors > JN_MAX_REPORTED)
+		return jn_fail(JN_ERR_INVALID, "num_eigenvectors must be in 0..num_eigenvalues");
+	return JN_OK;
+}
+
+/* Lanczos with full reorthogonalisation for every instance of the job, one
+ * captured graph per step; then the FP64 Rayleigh-Ritz refinement. */
+static jn_status batch_solve(cudaStream_t q, const jn_batch_options *o, const batch_job &job)
+{
+	const int B = job.B;
+	const int64_t Dp = job.Dp;
 	int m = o->max_iterations > 0 ? o->max_iterations : 200;
-	if (m > D) m = (int)D;
+	if (m > Dp) m = (int)Dp;
 	int nev = o->num_eigenvalues > 0 ? o->num_eigenvalues : 10;
 	if (nev > JN_MAX_REPORTED) nev = JN_MAX_REPORTED;
 	if (nev > m) nev = m;
@@ -444,25 +480,19 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	int r = nev + extra;
 	if (r > m) r = m;
 	const int check_every = o->check_every > 0 ? o->check_every : 10;
-	if (o->num_eigenvectors < 0 || o->num_eigenvectors > nev || (o->num_eigenvectors && !o->eigenvectors))
-		return jn_fail(JN_ERR_INVALID, "num_eigenvectors must be in 0..num_eigenvalues with an output array");
 	const int nvo = o->num_eigenvectors;
-	const int f32 = o->precision == 32;
 	const int want = nev + 1 < m ? nev + 1 : m;
 	const int ldz = m + 1;
 	const int ncol = m + 2;
-	const int64_t ldV = (int64_t)(m + 1) * D, ldab = m + 1;
-	cudaStream_t q = c->stream;
+	const int64_t ldV = (int64_t)(m + 1) * Dp, ldab = m + 1;
+	/* an instance stops at the dimension of its Krylov space */
+	int *lim = (int *)malloc(B * sizeof(int));
+	for (int i = 0; i < B; i++) lim[i] = job.dims[i] < m ? (int)job.dims[i] : m;
 	jn_status st = JN_OK;
 	struct bstate s;
 	memset(&s, 0, sizeof s);
 	BALLOC(s.V, (size_t)B * ldV);
-	BALLOC(s.W, (size_t)B * D);
-	BALLOC(s.me64, (size_t)B * nme);
-	/* 32-bit products on the panel engine where it is this context's engine */
-	const int panels = f32 && c->engine == 4 && jn_panels_setup(c) == JN_OK && jn_panels_fit(c, 1);
-	if (f32 && !panels) { BALLOC(s.me32, (size_t)B * nme); BALLOC(s.x32, (size_t)B * D); }
-	else BALLOC(s.x64, (size_t)B * D);
+	BALLOC(s.W, (size_t)B * Dp);
 	BALLOC(s.alpha, (size_t)B * ldab);
 	BALLOC(s.beta, (size_t)B * ldab);
 	BALLOC(s.part, (size_t)B * BNB * ncol);
@@ -473,62 +503,24 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	const int zrows = r > want ? r : want;  /* vectors per instance: r at the end, want in checks */
 	BALLOC(s.Z, (size_t)B * zrows * ldz);
 	BALLOC(s.work, (size_t)B * zrows * 5 * ldz);
-	BALLOC(s.gacc, (size_t)B * D);
-	BALLOC(s.ctrl, (size_t)2 * B);
+	BALLOC(s.dims, B);
 	BALLOC(s.k, 1);
 	BALLOC(s.active, B);
 	BALLOC(s.flag, B);
 	BALLOC(s.narr, B);
-	if (panels) {
-		BALLOC(s.pcoef, (size_t)B * (p->n_coef ? p->n_coef : 1));
-		BALLOC(s.pxbuf, (size_t)B * 2 * D);
-		BALLOC(s.pcmax, B);
-	}
-	if (st) { bstate_free(&s); return st; }
+	if (st) { bstate_free(&s); free(lim); return st; }
+	if (cudaMemcpy(s.dims, job.dims, B * sizeof(int64_t), cudaMemcpyHostToDevice) != cudaSuccess)
+		st = jn_fail(JN_ERR_CUDA, "upload of the instances' dimensions");
 
-	/* matrix elements: FP64 for refinement, FP32 copies with the reference's
-	   |M| < 1e-12 skip of single-species blocks (matrix_vector_multiplication.c:52-53) */
-	double maxme = 0.0;
-	float *h32 = f32 && !panels ? (float *)malloc(nme * sizeof(float)) : NULL;
+	/* start vectors: given, or one seeded pseudo-random vector of the instance's dimension */
+	double *hv = (double *)malloc(Dp * sizeof(double));
 	for (int i = 0; i < B && !st; i++) {
-		const double *me = o->matrix_elements[i];
-		if (!me) { st = jn_fail(JN_ERR_INVALID, "matrix_elements[%d] is NULL", i); break; }
-		for (int64_t e = 0; e < nme; e++) maxme = fmax(maxme, fabs(me[e]));
-		if (cudaMemcpyAsync(s.me64 + (size_t)i * nme, me, nme * sizeof(double), cudaMemcpyHostToDevice, q) != cudaSuccess)
-			st = jn_fail(JN_ERR_CUDA, "upload of matrix elements");
-		if (h32 && !st) {
-			for (int b = 0; b < p->nmes; b++) {
-				const jn_me_t *M = &p->mes[b];
-				for (int64_t e = 0; e < M->len; e++) {
-					const double v = me[M->offset + e];
-					h32[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0f : (float)v;
-				}
-			}
-			if (cudaMemcpy(s.me32 + (size_t)i * nme, h32, nme * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-				st = jn_fail(JN_ERR_CUDA, "upload of FP32 matrix elements");
-		}
-	}
-	free(h32);
-	/* fixed-point scale bound valid for every instance */
-	const double abs_bound = jn_plan_abs_bound(p, NULL) * maxme;
-	if (!st && panels) st = jn_panels_batched_coefficients(c, B, s.me64, nme, s.pcoef, s.pcmax, q);
-	/* each instance gets about (resident CTAs) / B persistent CTAs */
-	jn_panel_partition part;
-	memset(&part, 0, sizeof part);
-	if (!st && panels) {
-		int g = c->num_sms * c->panel_per_sm[1] / B;
-		st = jn_panels_partition_upload(c, g < 8 ? 8 : g, &part);
-	}
-
-	/* start vectors: given, or one seeded pseudo-random vector for all */
-	double *hv = (double *)malloc(D * sizeof(double));
-	for (int i = 0; i < B && !st; i++) {
-		const double *sv = o->start_vectors ? o->start_vectors[i] : NULL;
+		const double *sv = job.start_vectors ? job.start_vectors[i] : NULL;
 		if (!sv) {
-			jn_default_start_vector(D, hv);
+			jn_default_start_vector(job.dims[i], hv);
 			sv = hv;
 		}
-		if (cudaMemcpy(s.V + (size_t)i * ldV, sv, D * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+		if (cudaMemcpy(s.V + (size_t)i * ldV, sv, job.dims[i] * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
 			st = jn_fail(JN_ERR_CUDA, "upload of start vectors");
 	}
 	free(hv);
@@ -537,38 +529,34 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	cudaGraphExec_t gexec = NULL;
 	cudaGraph_t graph = NULL;
 	int k = 0, nactive = B;
-	const int vg = (int)((D + BT - 1) / BT < 64 ? (D + BT - 1) / BT : 64);
+	const int vg = (int)((Dp + BT - 1) / BT < 64 ? (Dp + BT - 1) / BT : 64);
 	const dim3 gv(vg > 0 ? vg : 1, B), gr(BNB, B), g1(1, B);
+	const int64_t *dims = s.dims;
 	if (!st) {
 		cudaMemsetAsync(s.k, 0, sizeof(int), q);
-		cudaMemsetAsync(s.gacc, 0, (size_t)B * D * sizeof(unsigned long long), q);
 		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
 		/* v_0 normalised */
-		kb_dot<<<gr, BT, 0, q>>>(s.V, ldV, 0, s.V, ldV, 0, s.k, D, s.part, NULL);
+		kb_dot<<<gr, BT, 0, q>>>(s.V, ldV, 0, s.V, ldV, 0, s.k, Dp, dims, s.part, NULL);
 		kb_finish_dot<<<g1, 32, 0, q>>>(s.part, BNB, s.scal, 1, 0, s.k, NULL);
-		kb_scale_start<<<gv, BT, 0, q>>>(s.V, ldV, s.scal, D);
+		kb_scale_start<<<gv, BT, 0, q>>>(s.V, ldV, s.scal, Dp, dims);
 		if (cudaGetLastError() != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "batched Lanczos start");
 	}
 
 	/* one Lanczos step for every active instance, k read on the device */
 	auto step = [&](cudaStream_t qs) -> jn_status {
-		jn_status e = panels ? jn_enqueue_panels_batched(c, B, s.pcoef, s.pcmax, s.V, ldV, s.k, D, s.W, D, s.pxbuf,
-								 s.gacc, s.ctrl, s.active, &part, qs)
-				     : jn_enqueue_batched(c, B, f32, f32 ? (const void *)s.me32 : (const void *)s.me64, nme,
-							  s.V, ldV, s.k, D, s.W, D, s.x64, s.x32, s.gacc, s.ctrl, s.active,
-							  abs_bound, qs);
+		jn_status e = job.product(s.V, ldV, s.k, s.W, s.active, qs);
 		if (e) return e;
-		kb_dot<<<gr, BT, 0, qs>>>(s.V, ldV, 1, s.W, D, 0, s.k, D, s.part, s.active);
+		kb_dot<<<gr, BT, 0, qs>>>(s.V, ldV, 1, s.W, Dp, 0, s.k, Dp, dims, s.part, s.active);
 		kb_finish_dot<<<g1, 32, 0, qs>>>(s.part, BNB, s.alpha, ldab, 1, s.k, s.active);
-		kb_three_term<<<gv, BT, 0, qs>>>(s.W, s.V, ldV, s.alpha, s.beta, ldab, s.k, D, s.active);
+		kb_three_term<<<gv, BT, 0, qs>>>(s.W, s.V, ldV, s.alpha, s.beta, ldab, s.k, Dp, dims, s.active);
 		for (int pass = 0; pass < 2; pass++) {
-			kb_gemv_t<<<gr, BT, 0, qs>>>(s.V, ldV, s.W, s.k, D, s.part, ncol, s.active);
+			kb_gemv_t<<<gr, BT, 0, qs>>>(s.V, ldV, s.W, s.k, Dp, dims, s.part, ncol, s.active);
 			kb_finish<<<dim3((ncol + 127) / 128, B), 128, 0, qs>>>(s.part, BNB, ncol, s.k, s.h, s.active);
-			kb_gemv_n_sub<<<gv, BT, 0, qs>>>(s.V, ldV, s.h, ncol, s.k, D, s.W, s.active);
+			kb_gemv_n_sub<<<gv, BT, 0, qs>>>(s.V, ldV, s.h, ncol, s.k, Dp, dims, s.W, s.active);
 		}
-		kb_dot<<<gr, BT, 0, qs>>>(s.W, D, 0, s.W, D, 0, s.k, D, s.part, s.active);
+		kb_dot<<<gr, BT, 0, qs>>>(s.W, Dp, 0, s.W, Dp, 0, s.k, Dp, dims, s.part, s.active);
 		kb_finish_dot<<<g1, 32, 0, qs>>>(s.part, BNB, s.scal, 1, 0, s.k, s.active);
-		kb_normalize<<<gv, BT, 0, qs>>>(s.V, ldV, s.W, s.scal, s.beta, ldab, s.k, D, s.active);
+		kb_normalize<<<gv, BT, 0, qs>>>(s.V, ldV, s.W, s.scal, s.beta, ldab, s.k, Dp, dims, s.active);
 		kb_advance<<<1, 32, 0, qs>>>(s.k);
 		return cudaGetLastError() == cudaSuccess ? JN_OK : jn_fail(JN_ERR_CUDA, "batched Lanczos step launch");
 	};
@@ -591,7 +579,9 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		}
 		k++;
 		if (st) break;
-		if (k % check_every && k < m) continue;
+		int at_limit = 0;
+		for (int i = 0; i < B; i++) at_limit |= hact[i] && k >= lim[i];
+		if (k % check_every && k < m && !at_limit) continue;
 		/* convergence of every active instance at n = k */
 		for (int i = 0; i < B; i++) hn[i] = hact[i] ? k : hn[i];
 		cudaMemcpyAsync(s.narr, hn, B * sizeof(int), cudaMemcpyHostToDevice, q);
@@ -607,11 +597,11 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 			break;
 		}
 		for (int i = 0; i < B; i++)
-			if (hact[i] && (hflag[i] || k >= m)) {
+			if (hact[i] && (hflag[i] || k >= lim[i])) {
 				hact[i] = 0;
 				hn[i] = k;
-				res[i].converged = hflag[i];
-				res[i].iterations = k;
+				job.res[i]->converged = hflag[i];
+				job.res[i]->iterations = k;
 				nactive--;
 			}
 		cudaMemcpyAsync(s.active, hact, B * sizeof(int), cudaMemcpyHostToDevice, q);
@@ -621,11 +611,11 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 
 	/* Ritz vectors of the final T of each instance, FP64 products, Rayleigh-Ritz */
 	if (!st) {
-		BALLOC(s.X, (size_t)B * r * D);
-		BALLOC(s.HX, (size_t)B * r * D);
+		BALLOC(s.X, (size_t)B * r * Dp);
+		BALLOC(s.HX, (size_t)B * r * Dp);
 		BALLOC(s.G, (size_t)B * 3 * r * r);
 		BALLOC(s.C, (size_t)B * r * r);
-		if (nvo) BALLOC(s.GS, (size_t)B * nvo * D);
+		if (nvo) BALLOC(s.GS, (size_t)B * nvo * Dp);
 	}
 	double *hG = NULL;
 	if (!st) {
@@ -636,16 +626,15 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 		kb_tri_vectors<<<dim3((r + 31) / 32, B), 32, 0, q>>>(s.alpha, s.beta, ldab, s.narr, r, s.theta, r + 1, s.Z, ldz,
 								     s.work, NULL, NULL);
 		kb_tri_mgs<<<g1, BT, 0, q>>>(s.Z, ldz, s.narr, r, NULL);
-		kb_ritz<<<gv, BT, 0, q>>>(s.V, ldV, s.Z, ldz, s.narr, r, D, s.X);
-		/* H X in FP64, one batched product per Ritz index */
+		kb_ritz<<<gv, BT, 0, q>>>(s.V, ldV, s.Z, ldz, s.narr, r, Dp, dims, s.X);
+		/* H X in FP64-grade arithmetic, one batched product per Ritz index */
 		for (int j = 0; j < r && !st; j++)
-			st = jn_enqueue_batched(c, B, 0, s.me64, nme, s.X + (size_t)j * D, (int64_t)r * D, NULL, 0,
-						s.HX + (size_t)j * D, (int64_t)r * D, s.W, NULL, s.gacc, s.ctrl, NULL, abs_bound, q);
+			st = job.product64(s.X + (size_t)j * Dp, (int64_t)r * Dp, s.HX + (size_t)j * Dp, s.W, q);
 	}
 	if (!st) {
-		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.X, r, D, s.G);
-		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.HX, r, D, s.G + (size_t)B * r * r);
-		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.HX, s.HX, r, D, s.G + (size_t)2 * B * r * r);
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.X, r, Dp, dims, s.G);
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.X, s.HX, r, Dp, dims, s.G + (size_t)B * r * r);
+		kb_gram<<<dim3(r * r, B), BT, 0, q>>>(s.HX, s.HX, r, Dp, dims, s.G + (size_t)2 * B * r * r);
 		hG = (double *)malloc(sizeof(double) * 3 * B * r * r);
 		double *hth = (double *)malloc(sizeof(double) * B * (r + 1));
 		if (cudaMemcpyAsync(hG, s.G, sizeof(double) * 3 * B * r * r, cudaMemcpyDeviceToHost, q) != cudaSuccess ||
@@ -667,31 +656,248 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 				}
 			if (rayleigh_ritz(G1, G2, G3, ri, lam, rn, hC + (size_t)i * r * r, r))
 				st = jn_fail(JN_ERR_NOT_CONVERGED, "instance %d: Ritz vectors are not independent", i);
-			res[i].num_eigenvalues = nev < ri ? nev : ri;
-			for (int e = 0; e < res[i].num_eigenvalues; e++) {
-				res[i].eigenvalues[e] = lam[e];
-				res[i].residual_norms[e] = rn[e];
-				res[i].ritz_values[e] = hth[(size_t)i * (r + 1) + e];
+			jn_batch_result *R = job.res[i];
+			R->num_eigenvalues = nev < ri ? nev : ri;
+			for (int e = 0; e < R->num_eigenvalues; e++) {
+				R->eigenvalues[e] = lam[e];
+				R->residual_norms[e] = rn[e];
+				R->ritz_values[e] = hth[(size_t)i * (r + 1) + e];
 			}
 			free(G1); free(G2); free(G3);
 		}
 		if (!st && nvo) {
 			cudaMemcpyAsync(s.C, hC, sizeof(double) * B * r * r, cudaMemcpyHostToDevice, q);
-			kb_combine<<<gv, BT, 0, q>>>(s.X, s.C, r, nvo, D, s.GS);
+			kb_combine<<<gv, BT, 0, q>>>(s.X, s.C, r, nvo, Dp, dims, s.GS);
 			for (int i = 0; i < B && !st; i++)
-				if (o->eigenvectors[i] &&
-				    cudaMemcpyAsync(o->eigenvectors[i], s.GS + (size_t)i * nvo * D, (size_t)nvo * D * sizeof(double),
-						    cudaMemcpyDeviceToHost, q) != cudaSuccess)
-					st = jn_fail(JN_ERR_CUDA, "eigenvector copy");
+				for (int e = 0; e < nvo && !st && job.eigenvectors && job.eigenvectors[i]; e++)
+					if (cudaMemcpyAsync(job.eigenvectors[i] + (size_t)e * job.dims[i], s.GS + ((size_t)i * nvo + e) * Dp,
+							    (size_t)job.dims[i] * sizeof(double), cudaMemcpyDeviceToHost, q) != cudaSuccess)
+						st = jn_fail(JN_ERR_CUDA, "eigenvector copy");
 			if (!st && cudaStreamSynchronize(q) != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "eigenvector copy");
 		}
 		free(hC); free(lam); free(rn); free(hth);
 	}
 	free(hG);
-	free(hact); free(hn); free(hflag);
+	free(hact); free(hn); free(hflag); free(lim);
 	bstate_free(&s);
-	jn_panels_partition_free(&part);
 	if (!st && cudaGetLastError() != cudaSuccess) st = jn_fail(JN_ERR_CUDA, "batched Lanczos");
+	return st;
+}
+
+extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_batch_result *res)
+{
+	if (!c || !o || !res || !o->matrix_elements) return jn_fail(JN_ERR_INVALID, "null argument");
+	const jn_plan_t *p = &c->plan;
+	const int B = o->num_instances;
+	const int64_t D = p->dim, nme = p->n_me;
+	if (B < 1 || B > 4096) return jn_fail(JN_ERR_INVALID, "num_instances must be in 1..4096");
+	if (D < 1) return jn_fail(JN_ERR_INVALID, "empty basis");
+	jn_status st = batch_check_options(o);
+	if (st) return st;
+	if (o->num_eigenvectors && !o->eigenvectors)
+		return jn_fail(JN_ERR_INVALID, "num_eigenvectors must be in 0..num_eigenvalues with an output array");
+	const int f32 = o->precision == 32;
+	cudaStream_t q = c->stream;
+	/* the products' state: matrix elements, converted x, accumulators */
+	double *me64 = NULL, *x64 = NULL;
+	float *me32 = NULL, *x32 = NULL;
+	unsigned long long *gacc = NULL, *pcmax = NULL;
+	unsigned int *ctrl = NULL;
+	int *pcoef = NULL, *pxbuf = NULL;
+	BALLOC(me64, (size_t)B * nme);
+	/* 32-bit products on the panel engine where it is this context's engine */
+	const int panels = f32 && c->engine == 4 && jn_panels_setup(c) == JN_OK && jn_panels_fit(c, 1);
+	if (f32 && !panels) { BALLOC(me32, (size_t)B * nme); BALLOC(x32, (size_t)B * D); }
+	else BALLOC(x64, (size_t)B * D);
+	BALLOC(gacc, (size_t)B * D);
+	BALLOC(ctrl, (size_t)2 * B);
+	if (panels) {
+		BALLOC(pcoef, (size_t)B * (p->n_coef ? p->n_coef : 1));
+		BALLOC(pxbuf, (size_t)B * 2 * D);
+		BALLOC(pcmax, B);
+	}
+	/* matrix elements: FP64 for refinement, FP32 copies with the reference's
+	   |M| < 1e-12 skip of single-species blocks (matrix_vector_multiplication.c:52-53) */
+	double maxme = 0.0;
+	float *h32 = !st && f32 && !panels ? (float *)malloc(nme * sizeof(float)) : NULL;
+	for (int i = 0; i < B && !st; i++) {
+		const double *me = o->matrix_elements[i];
+		if (!me) { st = jn_fail(JN_ERR_INVALID, "matrix_elements[%d] is NULL", i); break; }
+		for (int64_t e = 0; e < nme; e++) maxme = fmax(maxme, fabs(me[e]));
+		if (cudaMemcpyAsync(me64 + (size_t)i * nme, me, nme * sizeof(double), cudaMemcpyHostToDevice, q) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "upload of matrix elements");
+		if (h32 && !st) {
+			for (int b = 0; b < p->nmes; b++) {
+				const jn_me_t *M = &p->mes[b];
+				for (int64_t e = 0; e < M->len; e++) {
+					const double v = me[M->offset + e];
+					h32[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0f : (float)v;
+				}
+			}
+			if (cudaMemcpy(me32 + (size_t)i * nme, h32, nme * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+				st = jn_fail(JN_ERR_CUDA, "upload of FP32 matrix elements");
+		}
+	}
+	free(h32);
+	if (!st) st = cudaMemsetAsync(gacc, 0, (size_t)B * D * sizeof(unsigned long long), q) == cudaSuccess
+			      ? JN_OK : jn_fail(JN_ERR_CUDA, "accumulator clear");
+	/* fixed-point scale bound valid for every instance */
+	const double abs_bound = jn_plan_abs_bound(p, NULL) * maxme;
+	if (!st && panels) st = jn_panels_batched_coefficients(c, B, me64, nme, pcoef, pcmax, q);
+	/* each instance gets about (resident CTAs) / B persistent CTAs */
+	jn_panel_partition part;
+	memset(&part, 0, sizeof part);
+	if (!st && panels) {
+		int g = c->num_sms * c->panel_per_sm[1] / B;
+		st = jn_panels_partition_upload(c, g < 8 ? 8 : g, &part);
+	}
+	int64_t *dims = (int64_t *)malloc(B * sizeof(int64_t));
+	jn_batch_result **rp = (jn_batch_result **)malloc(B * sizeof(jn_batch_result *));
+	for (int i = 0; i < B; i++) { dims[i] = D; rp[i] = res + i; }
+	if (!st) {
+		batch_job job;
+		job.B = B;
+		job.Dp = D;
+		job.dims = dims;
+		job.product = [&](const double *V, int64_t ldV, const int *d_k, double *W, const int *act, cudaStream_t qs) {
+			return panels ? jn_enqueue_panels_batched(c, B, pcoef, pcmax, V, ldV, d_k, D, W, D, pxbuf, gacc, ctrl, act,
+								  &part, qs)
+				      : jn_enqueue_batched(c, B, f32, f32 ? (const void *)me32 : (const void *)me64, nme, V, ldV,
+							   d_k, D, W, D, x64, x32, gacc, ctrl, act, abs_bound, qs);
+		};
+		job.product64 = [&](const double *X, int64_t ld, double *HX, double *scratch, cudaStream_t qs) {
+			return jn_enqueue_batched(c, B, 0, me64, nme, X, ld, NULL, 0, HX, ld, scratch, NULL, gacc, ctrl, NULL,
+						  abs_bound, qs);
+		};
+		job.start_vectors = o->start_vectors;
+		job.eigenvectors = o->eigenvectors;
+		job.res = rp;
+		st = batch_solve(q, o, job);
+	}
+	free(dims); free(rp);
+	void *bufs[] = { me64, x64, me32, x32, gacc, pcmax, ctrl, pcoef, pxbuf };
+	for (size_t i = 0; i < sizeof bufs / sizeof bufs[0]; i++) cudaFree(bufs[i]);
+	jn_panels_partition_free(&part);
+	return st;
+}
+
+extern "C" jn_status jn_lanczos_batch_bases(jn_ctx *const *ctxs, int num_bases, const jn_batch_options *options,
+					    jn_batch_result *const *results)
+{
+	if (!ctxs || !options || !results || num_bases < 1) return jn_fail(JN_ERR_INVALID, "null argument");
+	const jn_batch_options *o = &options[0];
+	jn_status st = batch_check_options(o);
+	if (st) return st;
+	int B = 0;
+	int64_t Dp = 0;
+	for (int b = 0; b < num_bases; b++) {
+		const jn_batch_options *ob = &options[b];
+		if (!ctxs[b] || !results[b] || !ob->matrix_elements) return jn_fail(JN_ERR_INVALID, "null argument for basis %d", b);
+		if (ob->num_instances < 1) return jn_fail(JN_ERR_INVALID, "basis %d: num_instances must be >= 1", b);
+		if (ob->max_iterations != o->max_iterations || ob->num_eigenvalues != o->num_eigenvalues ||
+		    ob->tolerance != o->tolerance || ob->precision != o->precision || ob->check_every != o->check_every ||
+		    ob->use_graph != o->use_graph || ob->refine_extra != o->refine_extra ||
+		    ob->num_eigenvectors != o->num_eigenvectors)
+			return jn_fail(JN_ERR_INVALID, "basis %d: the solver options differ from basis 0's", b);
+		if (ob->num_eigenvectors && !ob->eigenvectors)
+			return jn_fail(JN_ERR_INVALID, "basis %d: num_eigenvectors without an output array", b);
+		if (ctxs[b]->plan.dim < 1) return jn_fail(JN_ERR_INVALID, "basis %d: empty basis", b);
+		for (int j = 0; j < ob->num_instances; j++)
+			if (!ob->matrix_elements[j]) return jn_fail(JN_ERR_INVALID, "basis %d: matrix_elements[%d] is NULL", b, j);
+		B += ob->num_instances;
+		if (ctxs[b]->plan.dim > Dp) Dp = ctxs[b]->plan.dim;
+	}
+	if (B > 4096) return jn_fail(JN_ERR_INVALID, "more than 4096 instances");
+	cudaStream_t q = ctxs[0]->stream;
+	/* the instances, basis by basis */
+	int *ictx = (int *)malloc(B * sizeof(int)), *count = (int *)malloc(num_bases * sizeof(int));
+	int *first = (int *)malloc(num_bases * sizeof(int));
+	int64_t *dims = (int64_t *)malloc(B * sizeof(int64_t));
+	const double **me = (const double **)malloc(B * sizeof(double *));
+	const double **sv = (const double **)malloc(B * sizeof(double *));
+	double **ev = (double **)malloc(B * sizeof(double *));
+	jn_batch_result **rp = (jn_batch_result **)malloc(B * sizeof(jn_batch_result *));
+	for (int b = 0, i = 0; b < num_bases; b++) {
+		count[b] = options[b].num_instances;
+		first[b] = i;
+		for (int j = 0; j < count[b]; j++, i++) {
+			ictx[i] = b;
+			dims[i] = ctxs[b]->plan.dim;
+			me[i] = options[b].matrix_elements[j];
+			sv[i] = options[b].start_vectors ? options[b].start_vectors[j] : NULL;
+			ev[i] = options[b].eigenvectors ? options[b].eigenvectors[j] : NULL;
+			rp[i] = results[b] + j;
+		}
+	}
+	/* per basis: FP64 matrix elements on the device, the refinement's accumulators, the scale bound */
+	double **me64 = (double **)calloc(num_bases, sizeof(double *));
+	unsigned long long **gacc = (unsigned long long **)calloc(num_bases, sizeof(void *));
+	unsigned int **ctrl = (unsigned int **)calloc(num_bases, sizeof(void *));
+	double *bound = (double *)calloc(num_bases, sizeof(double));
+	for (int b = 0; b < num_bases && !st; b++) {
+		const jn_plan_t *p = &ctxs[b]->plan;
+		const int64_t nme = p->n_me;
+		BALLOC(me64[b], (size_t)count[b] * nme);
+		BALLOC(gacc[b], (size_t)count[b] * p->dim);
+		BALLOC(ctrl[b], (size_t)2 * count[b]);
+		double maxme = 0.0;
+		for (int j = 0; j < count[b] && !st; j++) {
+			const double *m = me[first[b] + j];
+			for (int64_t e = 0; e < nme; e++) maxme = fmax(maxme, fabs(m[e]));
+			if (cudaMemcpy(me64[b] + (size_t)j * nme, m, nme * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+				st = jn_fail(JN_ERR_CUDA, "upload of matrix elements");
+		}
+		if (!st && cudaMemset(gacc[b], 0, (size_t)count[b] * p->dim * sizeof(unsigned long long)) != cudaSuccess)
+			st = jn_fail(JN_ERR_CUDA, "accumulator clear");
+		bound[b] = jn_plan_abs_bound(p, NULL) * maxme;
+	}
+	/* the iteration products: one launch for every instance of every basis, on
+	   the panel engine where every basis runs it (32-bit products), else on the
+	   walk engine */
+	struct jn_panel_batch *pb = NULL;
+	struct jn_walk_batch *wb = NULL;
+	if (!st) {
+		if (o->precision == 32 && jn_panel_batch_possible(ctxs, num_bases))
+			st = jn_panel_batch_create(ctxs, num_bases, count, me64, &pb);
+		else
+			st = jn_walk_batch_create(ctxs, ictx, B, me, o->precision == 32, &wb);
+	}
+	if (!st) {
+		const int mode = o->precision == 32 ? 32 : 64;
+		batch_job job;
+		job.B = B;
+		job.Dp = Dp;
+		job.dims = dims;
+		job.product = [&](const double *V, int64_t ldV, const int *d_k, double *W, const int *act, cudaStream_t qs) {
+			return pb ? jn_panel_batch_enqueue(pb, V, ldV, d_k, Dp, W, Dp, act, Dp, qs)
+				  : jn_walk_batch_enqueue(wb, mode, V, ldV, d_k, Dp, W, Dp, act, Dp, qs);
+		};
+		/* refinement, basis by basis, on the block-tile engine in FP64 */
+		job.product64 = [&](const double *X, int64_t ld, double *HX, double *scratch, cudaStream_t qs) {
+			for (int b = 0; b < num_bases; b++) {
+				jn_ctx *c = ctxs[b];
+				const size_t i0 = (size_t)first[b];
+				jn_status e = jn_enqueue_batched(c, count[b], 0, me64[b], c->plan.n_me, X + i0 * ld, ld, NULL, 0,
+								 HX + i0 * ld, ld, scratch + i0 * Dp, NULL, gacc[b], ctrl[b], NULL,
+								 bound[b], qs);
+				if (e) return e;
+			}
+			return JN_OK;
+		};
+		job.start_vectors = sv;
+		job.eigenvectors = ev;
+		job.res = rp;
+		st = batch_solve(q, o, job);
+	}
+	jn_panel_batch_free(pb);
+	jn_walk_batch_free(wb);
+	for (int b = 0; b < num_bases; b++) {
+		cudaFree(me64[b]);
+		cudaFree(gacc[b]);
+		cudaFree(ctrl[b]);
+	}
+	free(me64); free(gacc); free(ctrl); free(bound);
+	free(ictx); free(count); free(first); free(dims); free(me); free(sv); free(ev); free(rp);
 	return st;
 }
 

@@ -157,6 +157,34 @@ void jn_walk_release(jn_ctx *c);
 jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumulate, cudaStream_t st, cudaEvent_t pre,
 			  cudaEvent_t mid);
 
+/* Batched walk products over instances of several bases (all contexts on
+ * one device): instance i runs on ctxs[inst_ctx[i]]'s walk plan with its own
+ * matrix elements me[i] (host, that context's layout).  Per product:
+ * y + i y_ld = H_i x_i with x_i = src + i src_ld + (*d_sel) sel_ld, in FP32
+ * (mode 32; want32 at creation) or FP64 FMAs (mode 64), exact fixed-point
+ * sums; inactive instances (d_active[i] == 0) are skipped.  max_dim bounds
+ * every instance's dimension. */
+struct jn_walk_batch;
+jn_status jn_walk_batch_create(jn_ctx *const *ctxs, const int *inst_ctx, int B, const double *const *me, int want32,
+			       struct jn_walk_batch **out);
+jn_status jn_walk_batch_enqueue(struct jn_walk_batch *wb, int mode, const double *src, int64_t src_ld, const int *d_sel,
+				int64_t sel_ld, double *y, int64_t y_ld, const int *d_active, int64_t max_dim,
+				cudaStream_t st);
+void jn_walk_batch_free(struct jn_walk_batch *wb);
+
+/* Batched 32-bit panel products over instances of several bases: basis b
+ * (ctxs[b], panel engine) has count[b] instances with FP64 matrix elements
+ * d_me64[b] (device, count[b] x n_me).  Per product, as the walk batch;
+ * possible when every context runs the panel engine. */
+struct jn_panel_batch;
+int jn_panel_batch_possible(jn_ctx *const *ctxs, int nbases);
+jn_status jn_panel_batch_create(jn_ctx *const *ctxs, int nbases, const int *count, const double *const *d_me64,
+				struct jn_panel_batch **out);
+jn_status jn_panel_batch_enqueue(struct jn_panel_batch *pb, const double *src, int64_t src_ld, const int *d_sel,
+				 int64_t sel_ld, double *y, int64_t y_ld, const int *d_active, int64_t max_dim,
+				 cudaStream_t st);
+void jn_panel_batch_free(struct jn_panel_batch *pb);
+
 /* release the Lanczos state of a context */
 void jn_lanczos_release(jn_ctx *c);
 

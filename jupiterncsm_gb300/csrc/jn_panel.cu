@@ -1089,3 +1089,232 @@ jn_status jn_enqueue_panels_batched(jn_ctx *c, int B, const int *d_coef, const u
 	CUDA_TRY(cudaGetLastError());
 	return JN_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* batched 32-bit products over instances of several bases              */
+/* ------------------------------------------------------------------ */
+/* One instance of a several-bases panel product: its basis's panels, tasks
+ * and CTA partition (on the basis's context), its coefficients, x buffers,
+ * accumulator and coefficient scale (112 bytes). */
+struct jn_panel_inst {
+	const uint4 *panels, *tasks;
+	const uint32_t *cta, *flush, *flush_ptr;
+	const uint4 *blocks;
+	const uint32_t *meta;
+	const int *coef;
+	int *xi;                        /* x as 32-bit fixed point, [p][n] then [n][p] (2 dim words) */
+	unsigned long long *gacc;
+	const unsigned long long *cmax; /* max|c| bits of the instance's coefficients */
+	int64_t dim;
+	int grid, words, nblocks;
+	int owner;                      /* the first instance of a basis owns the basis's coefficient arrays */
+};
+static_assert(sizeof(jn_panel_inst) == 112, "one descriptor is 112 bytes");
+
+struct jn_panel_batch {
+	int B;
+	jn_panel_inst *h, *d;
+	unsigned int *d_ctrl;           /* max|x| bits of instance i at 2 i */
+	int max_grid, max_blocks;
+	size_t smem;
+	jn_panel_partition *parts;      /* one per basis */
+	int nbases;
+};
+
+/* instance blockIdx.y; CTAs beyond the instance's grid have no work */
+__global__ void __launch_bounds__(PANEL_THREADS, 3)
+	jn_panel_multi_kernel(const jn_panel_inst *__restrict__ I, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const jn_panel_inst d = I[inst];
+	if ((int)blockIdx.x >= d.grid) return;
+	const FixInt32 fix = {};
+	jn_panel_body<int, FixInt32, false>(d.panels, d.tasks, d.cta, d.flush, d.flush_ptr, d.blocks, d.meta, d.coef, d.xi,
+					    d.xi + d.dim, d.gacc, fix, d.words);
+}
+
+__global__ void jn_panel_multi_xmax_kernel(const jn_panel_inst *__restrict__ I, const double *__restrict__ src,
+					   int64_t src_ld, const int *__restrict__ sel, int64_t sel_ld,
+					   unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const int64_t n = I[inst].dim;
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		m = fmaxf(m, (float)fabs(x[i]) * 1.0000002f);
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(ctrl + 2 * inst, __float_as_uint(m));
+}
+
+/* block blockIdx.x of instance blockIdx.y: x_i as 32-bit fixed point, [p][n] and transposed [n][p] */
+__global__ void jn_panel_multi_x_kernel(const jn_panel_inst *__restrict__ I, const double *__restrict__ src,
+					int64_t src_ld, const int *__restrict__ sel, int64_t sel_ld,
+					const unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const jn_panel_inst d = I[inst];
+	if ((int)blockIdx.x >= d.nblocks) return;
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	int *xn = d.xi, *xt = d.xi + d.dim;
+	const uint4 bk = d.blocks[blockIdx.x];
+	const uint32_t Np = bk.z, Nn = bk.w, n = Np * Nn;
+	const double s = ldexp(1.0, x_exponent(ctrl[2 * inst]));
+	for (uint32_t e = threadIdx.x; e < n; e += blockDim.x) {
+		const int t = __double2int_rn(x[bk.x + e] * s);
+		xn[bk.x + e] = t;
+		xt[bk.x + (e % Nn) * Np + e / Nn] = t;
+	}
+}
+
+/* y_i = acc_i 2^(30 - Sc_i - Sx_i) (y + i y_ld); the accumulators are cleared */
+__global__ void jn_panel_multi_finalize_kernel(const jn_panel_inst *__restrict__ I, double *__restrict__ y, int64_t y_ld,
+					       const unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const jn_panel_inst d = I[inst];
+	const double unit = ldexp(1.0, PANEL_INT_SHIFT - coef_exponent(*d.cmax) - x_exponent(ctrl[2 * inst]));
+	double *yy = y + inst * y_ld;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.dim; i += (int64_t)gridDim.x * blockDim.x) {
+		yy[i] = (double)(long long)d.gacc[i] * unit;
+		d.gacc[i] = 0ull;
+	}
+}
+
+void jn_panel_batch_free(jn_panel_batch *pb)
+{
+	if (!pb) return;
+	if (pb->h)
+		for (int i = 0; i < pb->B; i++) {
+			if (pb->h[i].owner) {
+				cudaFree((void *)pb->h[i].coef);
+				cudaFree((void *)pb->h[i].cmax);
+			}
+			cudaFree(pb->h[i].xi);
+			cudaFree(pb->h[i].gacc);
+		}
+	if (pb->parts)
+		for (int b = 0; b < pb->nbases; b++) jn_panels_partition_free(&pb->parts[b]);
+	free(pb->parts);
+	free(pb->h);
+	cudaFree(pb->d);
+	cudaFree(pb->d_ctrl);
+	free(pb);
+}
+
+int jn_panel_batch_possible(jn_ctx *const *ctxs, int nbases)
+{
+	for (int b = 0; b < nbases; b++)
+		if (ctxs[b]->engine != 4 || jn_panels_setup(ctxs[b]) != JN_OK || !jn_panels_fit(ctxs[b], 1)) {
+			cudaGetLastError();
+			return 0;
+		}
+	return 1;
+}
+
+jn_status jn_panel_batch_create(jn_ctx *const *ctxs, int nbases, const int *count, const double *const *d_me64,
+				jn_panel_batch **out)
+{
+	*out = NULL;
+	int B = 0;
+	for (int b = 0; b < nbases; b++) B += count[b];
+	if (B < 1 || B > 65535) return jn_fail(JN_ERR_INVALID, "batch of %d instances", B);
+	jn_panel_batch *pb = (jn_panel_batch *)calloc(1, sizeof *pb);
+	if (!pb) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	pb->B = B;
+	pb->nbases = nbases;
+	pb->h = (jn_panel_inst *)calloc((size_t)B, sizeof(jn_panel_inst));
+	pb->parts = (jn_panel_partition *)calloc((size_t)nbases, sizeof(jn_panel_partition));
+	jn_status s = (!pb->h || !pb->parts) ? jn_fail(JN_ERR_NOMEM, "out of host memory") : JN_OK;
+	/* CTAs: the resident CTAs of the 32-bit kernel shared out by each instance's coefficients */
+	double work = 0.0;
+	for (int b = 0; b < nbases && !s; b++) {
+		if ((s = jn_panels_setup(ctxs[b]))) break;
+		work += (double)count[b] * (double)(ctxs[b]->plan.n_coef ? ctxs[b]->plan.n_coef : 1);
+	}
+	const int resident = !s ? ctxs[0]->num_sms * ctxs[0]->panel_per_sm[1] : 0;
+	for (int b = 0, i0 = 0; b < nbases && !s; i0 += count[b], b++) {
+		jn_ctx *c = ctxs[b];
+		const jn_plan_t *p = &c->plan;
+		int g = (int)(resident * (double)(p->n_coef ? p->n_coef : 1) / work);
+		if (g < 8) g = 8;
+		if ((s = jn_panels_partition_upload(c, g, &pb->parts[b]))) break;
+		const jn_panel_partition *pp = &pb->parts[b];
+		int *coef = NULL;
+		unsigned long long *cmax = NULL;
+		const int64_t nc = p->n_coef ? p->n_coef : 1;
+		if (cudaMalloc((void **)&coef, (size_t)count[b] * nc * sizeof(int)) != cudaSuccess ||
+		    cudaMalloc((void **)&cmax, (size_t)count[b] * sizeof(unsigned long long)) != cudaSuccess) {
+			cudaFree(coef);
+			s = jn_fail(JN_ERR_NOMEM, "cudaMalloc of batched panel coefficients failed");
+			break;
+		}
+		pb->h[i0].owner = 1;
+		s = jn_panels_batched_coefficients(c, count[b], d_me64[b], p->n_me, coef, cmax, c->stream);
+		for (int j = 0; j < count[b]; j++) {
+			jn_panel_inst *d = &pb->h[i0 + j];
+			d->coef = coef + (size_t)j * nc;
+			d->cmax = cmax + j;
+			d->panels = (const uint4 *)c->d_panels;
+			d->tasks = (const uint4 *)c->d_ptasks;
+			d->cta = pp->cta;
+			d->flush = pp->flush;
+			d->flush_ptr = pp->flush_ptr;
+			d->blocks = (const uint4 *)c->d_pblocks;
+			d->meta = c->d_pmeta;
+			d->dim = p->dim;
+			d->grid = pp->grid;
+			d->words = pp->words;
+			d->nblocks = p->nblocks;
+		}
+		if (s) break;
+		for (int j = 0; j < count[b] && !s; j++) {
+			jn_panel_inst *d = &pb->h[i0 + j];
+			if (cudaMalloc((void **)&d->xi, (size_t)2 * (p->dim ? p->dim : 1) * sizeof(int)) != cudaSuccess ||
+			    cudaMalloc((void **)&d->gacc, (size_t)(p->dim ? p->dim : 1) * sizeof(unsigned long long)) != cudaSuccess ||
+			    cudaMemset(d->gacc, 0, (size_t)(p->dim ? p->dim : 1) * sizeof(unsigned long long)) != cudaSuccess)
+				s = jn_fail(JN_ERR_NOMEM, "cudaMalloc of batched panel buffers failed");
+		}
+		const size_t sm = panel_smem_words(p, pp->words, 0);
+		if (sm > pb->smem) pb->smem = sm;
+		if (pp->grid > pb->max_grid) pb->max_grid = pp->grid;
+		if (p->nblocks > pb->max_blocks) pb->max_blocks = p->nblocks;
+	}
+	if (!s && (cudaMalloc((void **)&pb->d, (size_t)B * sizeof(jn_panel_inst)) != cudaSuccess ||
+		   cudaMalloc((void **)&pb->d_ctrl, (size_t)2 * B * sizeof(unsigned int)) != cudaSuccess))
+		s = jn_fail(JN_ERR_NOMEM, "cudaMalloc of the batch descriptors failed");
+	if (!s && cudaMemcpy(pb->d, pb->h, (size_t)B * sizeof(jn_panel_inst), cudaMemcpyHostToDevice) != cudaSuccess)
+		s = jn_fail(JN_ERR_CUDA, "upload of the batch descriptors failed");
+	if (!s) {
+		cudaError_t e = cudaFuncSetAttribute(jn_panel_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pb->smem);
+		if (e == cudaSuccess) e = cudaDeviceSynchronize();
+		if (e != cudaSuccess) s = jn_fail(JN_ERR_CUDA, "batched panel set-up: %s", cudaGetErrorString(e));
+	}
+	if (s) {
+		jn_panel_batch_free(pb);
+		return s;
+	}
+	*out = pb;
+	return JN_OK;
+}
+
+jn_status jn_panel_batch_enqueue(jn_panel_batch *pb, const double *src, int64_t src_ld, const int *d_sel, int64_t sel_ld,
+				 double *y, int64_t y_ld, const int *d_active, int64_t max_dim, cudaStream_t st)
+{
+	const int B = pb->B;
+	int g = (int)((max_dim + 255) / 256);
+	if (g > 256) g = 256;
+	if (g < 1) g = 1;
+	CUDA_TRY(cudaMemsetAsync(pb->d_ctrl, 0, (size_t)2 * B * sizeof(unsigned int), st));
+	jn_panel_multi_xmax_kernel<<<dim3(g, B), 256, 0, st>>>(pb->d, src, src_ld, d_sel, sel_ld, pb->d_ctrl, d_active);
+	jn_panel_multi_x_kernel<<<dim3(pb->max_blocks > 0 ? pb->max_blocks : 1, B), 256, 0, st>>>(pb->d, src, src_ld, d_sel,
+												      sel_ld, pb->d_ctrl, d_active);
+	jn_panel_multi_kernel<<<dim3(pb->max_grid, B), PANEL_THREADS, pb->smem, st>>>(pb->d, d_active);
+	jn_panel_multi_finalize_kernel<<<dim3(g, B), 256, 0, st>>>(pb->d, y, y_ld, pb->d_ctrl, d_active);
+	CUDA_TRY(cudaGetLastError());
+	return JN_OK;
+}

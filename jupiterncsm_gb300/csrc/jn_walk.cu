@@ -512,6 +512,290 @@ jn_status jn_enqueue_walk(jn_ctx *c, const double *d_x, double *d_y, int accumul
 	return JN_OK;
 }
 
+/* ------------------------------------------------------------------ */
+/* batched products over instances of several bases                    */
+/* ------------------------------------------------------------------ */
+/* One instance of a batched walk product: its basis's plan (on the
+ * basis's context), its own walk element arrays, x views, accumulator and
+ * scale bound, and its range of the batch's task list (128 bytes). */
+struct jn_walk_inst {
+	const uint4 *tasks, *pieces;
+	const uint32_t *lanes, *walks, *rows, *rdst, *groups;
+	const double *elem64;
+	const float *elem32;
+	float *x32;                     /* FP32 copy of the instance's x (arithmetic 32) */
+	void *xt;                       /* transposed view of x in the arithmetic's type, NULL without proton walks */
+	const int32_t *perm;            /* position in x of each element of that view */
+	unsigned long long *gacc;
+	int64_t dim;
+	double abs_bound;               /* |H x| <= abs_bound max|x| */
+	uint32_t task0, ntasks;         /* the instance's tasks in the batch's list */
+};
+static_assert(sizeof(jn_walk_inst) == 128, "one descriptor is 128 bytes");
+
+struct jn_walk_batch {
+	int B;
+	jn_walk_inst *h, *d;
+	uint32_t *d_task0;              /* B + 1 task offsets */
+	uint32_t total;
+	unsigned int *d_ctrl;           /* max|x| bits of instance i at 2 i; the task counter at 2 B */
+	int num_sms, per_sm[2];         /* resident one-warp CTAs an SM: arithmetic 32, 64 */
+	int has32;
+};
+
+/* max|x_i| into ctrl[2 i], the FP32 copy of x_i (MODE 32) and the
+ * transposed view; x_i = src + i src_ld + (*sel) sel_ld */
+template <int MODE>
+__global__ void jn_walk_multi_prep_kernel(const jn_walk_inst *__restrict__ I, const double *__restrict__ src,
+					  int64_t src_ld, const int *__restrict__ sel, int64_t sel_ld,
+					  unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const jn_walk_inst d = I[inst];
+	const double *x = src + inst * src_ld + (sel ? (int64_t)(*sel) * sel_ld : 0);
+	typedef typename WalkT<MODE>::X X;
+	X *xt = (X *)d.xt;
+	float m = 0.0f;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.dim; i += (int64_t)gridDim.x * blockDim.x) {
+		const double v = x[i];
+		if (MODE == 32) d.x32[i] = (float)v;
+		if (xt) xt[i] = (X)x[d.perm[i]];
+		m = fmaxf(m, (float)fabs(v) * 1.0000002f);     /* round-up margin of the FP32 conversion */
+	}
+	for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(ctrl + 2 * inst, __float_as_uint(m));
+}
+
+/* All instances' tasks in one persistent launch: a warp takes task t of
+ * the batch's list from the counter, finds its instance (binary search of
+ * the task offsets) and runs it with that instance's plan, elements, x
+ * views and accumulator. */
+template <int MODE>
+__global__ void __launch_bounds__(WALK_THREADS, MODE == 32 ? 32 : 28)
+	jn_walk_multi_kernel(const jn_walk_inst *__restrict__ I, const uint32_t *__restrict__ task0, int B, uint32_t total,
+			     unsigned int *__restrict__ ctrl, const double *__restrict__ src, int64_t src_ld,
+			     const int *__restrict__ sel, int64_t sel_ld, const int *__restrict__ active)
+{
+	extern __shared__ unsigned long long wslots[];
+	const int lane = threadIdx.x & 31;
+	unsigned long long *slots = wslots;
+	for (int i = lane; i < WALK_SLOTS; i += 32) slots[i] = 0ull;
+	__syncwarp();
+	const int64_t k = sel ? (int64_t)(*sel) : 0;
+	unsigned int t = 0, tn = 0;
+	if (lane == 0) t = atomicAdd(ctrl + 2 * B, 1u);
+	t = __shfl_sync(0xffffffffu, t, 0);
+	for (; t < total; t = __shfl_sync(0xffffffffu, tn, 0)) {
+		if (lane == 0) tn = atomicAdd(ctrl + 2 * B, 1u);
+		int lo = 0, hi = B;             /* task0[lo] <= t < task0[hi] */
+		while (hi - lo > 1) {
+			const int mid = (lo + hi) >> 1;
+			if (__ldg(task0 + mid) <= t) lo = mid;
+			else hi = mid;
+		}
+		if (active && !active[lo]) continue;
+		const jn_walk_inst *d = I + lo;
+		int S, sh;
+		walk_scales(ctrl[2 * lo], d->abs_bound, 0, MODE, &S, &sh);
+		const float scalef = MODE == 32 ? __int_as_float((127 + (S < -126 ? -126 : (S > 127 ? 127 : S))) << 23) : 0.0f;
+		const double scale = MODE == 64 ? ldexp(1.0, S) : 0.0;
+		typedef typename WalkT<MODE>::C C;
+		typedef typename WalkT<MODE>::X X;
+		const C *elem;
+		const X *x;
+		if constexpr (MODE == 32) {
+			elem = d->elem32;
+			x = d->x32;
+		} else {
+			elem = d->elem64;
+			x = src + lo * src_ld + k * sel_ld;
+		}
+		const X *xt = (const X *)d->xt;
+		const uint4 ta = __ldg(d->tasks + (t - __ldg(task0 + lo)));
+		const uint4 pa = __ldg(d->pieces + 2 * ta.x), pb = __ldg(d->pieces + 2 * ta.x + 1);
+		const uint32_t U = (ta.w >> 8) & 0xffu;
+		if (U == 8)
+			walk_task<MODE, 8>(ta, pa, pb, d->lanes, d->walks, d->rows, d->rdst, d->groups, NULL, elem, x, xt, d->gacc,
+					   slots, lane, sh, scalef, scale);
+		else if (U == 4)
+			walk_task<MODE, 4>(ta, pa, pb, d->lanes, d->walks, d->rows, d->rdst, d->groups, NULL, elem, x, xt, d->gacc,
+					   slots, lane, sh, scalef, scale);
+		else
+			walk_task<MODE, 2>(ta, pa, pb, d->lanes, d->walks, d->rows, d->rdst, d->groups, NULL, elem, x, xt, d->gacc,
+					   slots, lane, sh, scalef, scale);
+	}
+}
+
+/* y_i = acc_i 2^-S_i (y + i y_ld); the accumulators are cleared */
+template <int MODE>
+__global__ void jn_walk_multi_finalize_kernel(const jn_walk_inst *__restrict__ I, double *__restrict__ y, int64_t y_ld,
+					      const unsigned int *__restrict__ ctrl, const int *__restrict__ active)
+{
+	const int inst = blockIdx.y;
+	if (active && !active[inst]) return;
+	const jn_walk_inst d = I[inst];
+	int S, sh;
+	walk_scales(ctrl[2 * inst], d.abs_bound, 0, MODE, &S, &sh);
+	const double unit = ldexp(1.0, -S);
+	double *yy = y + inst * y_ld;
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.dim; i += (int64_t)gridDim.x * blockDim.x) {
+		yy[i] = (double)(long long)d.gacc[i] * unit;
+		d.gacc[i] = 0ull;
+	}
+}
+
+void jn_walk_batch_free(jn_walk_batch *wb)
+{
+	if (!wb) return;
+	if (wb->h)
+		for (int i = 0; i < wb->B; i++) {
+			cudaFree((void *)wb->h[i].elem64);
+			cudaFree((void *)wb->h[i].elem32);
+			cudaFree(wb->h[i].x32);
+			cudaFree(wb->h[i].xt);
+			cudaFree(wb->h[i].gacc);
+		}
+	free(wb->h);
+	cudaFree(wb->d);
+	cudaFree(wb->d_task0);
+	cudaFree(wb->d_ctrl);
+	free(wb);
+}
+
+jn_status jn_walk_batch_create(jn_ctx *const *ctxs, const int *inst_ctx, int B, const double *const *me, int want32,
+			       jn_walk_batch **out)
+{
+	*out = NULL;
+	if (B < 1 || B > 65535) return jn_fail(JN_ERR_INVALID, "batch of %d instances", B);
+	jn_walk_batch *wb = (jn_walk_batch *)calloc(1, sizeof *wb);
+	if (!wb) return jn_fail(JN_ERR_NOMEM, "out of host memory");
+	wb->B = B;
+	wb->has32 = want32;
+	wb->h = (jn_walk_inst *)calloc((size_t)B, sizeof(jn_walk_inst));
+	uint32_t *task0 = (uint32_t *)malloc((size_t)(B + 1) * sizeof(uint32_t));
+	jn_status s = (!wb->h || !task0) ? jn_fail(JN_ERR_NOMEM, "out of host memory") : JN_OK;
+	double *hbuf = NULL;
+	int64_t hcap = 0;
+	uint64_t total = 0;
+	for (int i = 0; i < B && !s; i++) {
+		jn_ctx *c = ctxs[inst_ctx[i]];
+		if ((s = jn_walk_setup(c))) break;
+		const jn_plan_t *p = &c->plan;
+		jn_walk_inst *d = &wb->h[i];
+		d->tasks = (const uint4 *)c->d_wtasks;
+		d->pieces = (const uint4 *)c->d_wpieces;
+		d->lanes = c->d_wlanes;
+		d->walks = c->d_wwalks;
+		d->rows = c->d_wrows;
+		d->rdst = c->d_wrdst;
+		d->groups = c->d_wgroups;
+		d->perm = p->wxt ? c->d_wxperm : NULL;
+		d->dim = p->dim;
+		d->abs_bound = jn_plan_abs_bound(p, me[i]);
+		d->task0 = (uint32_t)total;
+		d->ntasks = (uint32_t)p->nwtasks;
+		task0[i] = (uint32_t)total;
+		total += (uint64_t)p->nwtasks;
+		if (total > 0xf0000000ull) { s = jn_fail(JN_ERR_INVALID, "the batch has too many walk tasks"); break; }
+		/* the instance's walk element arrays: FP64 built on the host, FP32 converted on the device */
+		const int64_t n = p->n_wme;
+		if (n > hcap) {
+			free(hbuf);
+			hcap = n;
+			hbuf = (double *)malloc((size_t)hcap * sizeof(double));
+			if (!hbuf) { s = jn_fail(JN_ERR_NOMEM, "out of host memory"); break; }
+		}
+		if (n) jn_walk_elements(p, me[i], hbuf);
+		double *e64 = NULL;
+		if ((s = wupload(&e64, hbuf, (size_t)n))) break;
+		d->elem64 = e64;
+		if (want32) {
+			float *e32 = NULL;
+			if ((s = wupload(&e32, (const void *)NULL, (size_t)n))) break;
+			d->elem32 = e32;
+			const int g = (int)(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
+			if (n) jn_walk_f32_kernel<<<g, 256, 0, c->stream>>>(e64, n, e32);
+			float *x32 = NULL;
+			if ((s = wupload(&x32, (const void *)NULL, (size_t)p->dim))) break;
+			d->x32 = x32;
+		}
+		if (p->wxt) {
+			double *xt = NULL;
+			if ((s = wupload(&xt, (const void *)NULL, (size_t)p->dim))) break;
+			d->xt = xt;
+		}
+		unsigned long long *g = NULL;
+		if ((s = wupload(&g, (const void *)NULL, (size_t)p->dim))) break;
+		if (cudaMemset(g, 0, (size_t)(p->dim ? p->dim : 1) * sizeof(unsigned long long)) != cudaSuccess)
+			s = jn_fail(JN_ERR_CUDA, "cudaMemset of a batch accumulator");
+		d->gacc = g;
+		if (!wb->num_sms) {
+			wb->num_sms = c->num_sms;
+			wb->per_sm[0] = c->walk_per_sm[0];
+			wb->per_sm[1] = c->walk_per_sm[1];
+		}
+	}
+	free(hbuf);
+	if (!s) {
+		task0[B] = (uint32_t)total;
+		wb->total = (uint32_t)total;
+		if ((s = wupload(&wb->d, wb->h, (size_t)B)) || (s = wupload(&wb->d_task0, task0, (size_t)B + 1)) ||
+		    (s = wupload(&wb->d_ctrl, (const void *)NULL, (size_t)2 * B + 1)))
+			;
+	}
+	free(task0);
+	if (!s) {
+		cudaError_t e = cudaFuncSetAttribute(jn_walk_multi_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+						     (int)WALK_SMEM);
+		int per = 0;
+		if (e == cudaSuccess) e = cudaFuncSetAttribute(jn_walk_multi_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+							       (int)WALK_SMEM);
+		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, jn_walk_multi_kernel<32>, WALK_THREADS, WALK_SMEM);
+		if (e == cudaSuccess) wb->per_sm[0] = per;
+		if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, jn_walk_multi_kernel<64>, WALK_THREADS, WALK_SMEM);
+		if (e == cudaSuccess) wb->per_sm[1] = per;
+		if (e == cudaSuccess) e = cudaDeviceSynchronize();
+		if (e != cudaSuccess) s = jn_fail(JN_ERR_CUDA, "batched walk set-up: %s", cudaGetErrorString(e));
+		else if (wb->per_sm[0] < 1 || wb->per_sm[1] < 1) s = jn_fail(JN_ERR_CUDA, "the batched walk kernel does not fit on an SM");
+	}
+	if (s) {
+		jn_walk_batch_free(wb);
+		return s;
+	}
+	*out = wb;
+	return JN_OK;
+}
+
+jn_status jn_walk_batch_enqueue(jn_walk_batch *wb, int mode, const double *src, int64_t src_ld, const int *d_sel,
+				int64_t sel_ld, double *y, int64_t y_ld, const int *d_active, int64_t max_dim, cudaStream_t st)
+{
+	if (mode != 32 && mode != 64) return jn_fail(JN_ERR_INVALID, "batched walk arithmetic %d", mode);
+	if (mode == 32 && !wb->has32) return jn_fail(JN_ERR_INVALID, "the batch has no FP32 elements");
+	const int B = wb->B;
+	int g = (int)((max_dim + 255) / 256);
+	if (g > 256) g = 256;
+	if (g < 1) g = 1;
+	CUDA_TRY(cudaMemsetAsync(wb->d_ctrl, 0, (size_t)(2 * B + 1) * sizeof(unsigned int), st));
+	const int grid = wb->num_sms * wb->per_sm[mode == 32 ? 0 : 1];
+	if (mode == 32) {
+		jn_walk_multi_prep_kernel<32><<<dim3(g, B), 256, 0, st>>>(wb->d, src, src_ld, d_sel, sel_ld, wb->d_ctrl, d_active);
+		if (wb->total)
+			jn_walk_multi_kernel<32><<<grid, WALK_THREADS, WALK_SMEM, st>>>(wb->d, wb->d_task0, B, wb->total, wb->d_ctrl,
+											 src, src_ld, d_sel, sel_ld, d_active);
+		jn_walk_multi_finalize_kernel<32><<<dim3(g, B), 256, 0, st>>>(wb->d, y, y_ld, wb->d_ctrl, d_active);
+	} else {
+		jn_walk_multi_prep_kernel<64><<<dim3(g, B), 256, 0, st>>>(wb->d, src, src_ld, d_sel, sel_ld, wb->d_ctrl, d_active);
+		if (wb->total)
+			jn_walk_multi_kernel<64><<<grid, WALK_THREADS, WALK_SMEM, st>>>(wb->d, wb->d_task0, B, wb->total, wb->d_ctrl,
+											 src, src_ld, d_sel, sel_ld, d_active);
+		jn_walk_multi_finalize_kernel<64><<<dim3(g, B), 256, 0, st>>>(wb->d, y, y_ld, wb->d_ctrl, d_active);
+	}
+	cudaError_t e = cudaGetLastError();
+	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "batched walk product launch: %s", cudaGetErrorString(e));
+	return JN_OK;
+}
+
 extern "C" jn_status jn_set_walk_arithmetic(jn_ctx *c, int fp64_fma)
 {
 	if (!c) return jn_fail(JN_ERR_INVALID, "null argument");

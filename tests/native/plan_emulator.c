@@ -549,7 +549,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 	free(split);
 	int S = fixed_exponent(xmax, P->abs_bound), sh = 0;
 	if (mode == 1) {
-		if (Sc + Sx - S < 48) S = Sc + Sx - 48;
+		if (Sc + Sx - S < 49) S = Sc + Sx - 49;
 		sh = Sc + Sx - S - 48;
 		if (sh > 63) sh = 63;
 	}
