@@ -939,6 +939,7 @@ void jn_t3plan_free(jn_t3plan_t *p)
 {
 	if (!p) return;
 	free(p->info); free(p->tb); free(p->tb_info); free(p->ms); free(p->term); free(p->voff); free(p->vld); free(p->V);
+	free(p->vrows); free(p->elem_pair); free(p->pair_seg); free(p->seg);
 	free(p->conn_ket); free(p->conn_bra); free(p->conn_sign); free(p->pc); free(p->nc); free(p->lut);
 	memset(p, 0, sizeof *p);
 }
@@ -1123,7 +1124,8 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 	p->neb = (int)ebv.n;
 	p->voff = (int64_t *)malloc((p->neb ? p->neb : 1) * t.nslots * sizeof(int64_t));
 	p->vld = (int32_t *)malloc((p->neb ? p->neb : 1) * t.nslots * sizeof(int32_t));
-	if (!p->voff || !p->vld) TERR("out of memory");
+	p->vrows = (int32_t *)malloc((p->neb ? p->neb : 1) * t.nslots * sizeof(int32_t));
+	if (!p->voff || !p->vld || !p->vrows) TERR("out of memory");
 	for (int e = 0; e < p->neb; e++) {
 		const basis3_t *K = &((basis3_t *)t.bases.a)[((int *)ebv.a)[2 * e]];
 		const basis3_t *B = &((basis3_t *)t.bases.a)[((int *)ebv.a)[2 * e + 1]];
@@ -1131,9 +1133,11 @@ int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int
 		for (int s = 0; s < t.nslots; s++) {
 			p->voff[e * t.nslots + s] = -1;
 			p->vld[e * t.nslots + s] = 0;
+			p->vrows[e * t.nslots + s] = 0;
 			if (K->parity != B->parity || !K->nskeys[s] || !B->nskeys[s]) continue;
 			p->voff[e * t.nslots + s] = (int64_t)Vv.n;
 			p->vld[e * t.nslots + s] = K->nskeys[s];
+			p->vrows[e * t.nslots + s] = B->nskeys[s];
 			const double *vt = diag ? vdg : vnd;
 			int64_t *cid = (int64_t *)malloc((size_t)K->nskeys[s] * sizeof(int64_t));
 			if (!cid) TERR("out of memory");
@@ -1204,5 +1208,122 @@ fail:
 	jfile_free(&J);
 	kcache_free(&kc);
 	jn_t3plan_free(p);
+	return -1;
+}
+
+/* ket state, bra state and sign of element i of three-body block blk */
+static void t3_element_states(const jn_t3plan_t *p, int blk, int64_t i, int32_t *ket, int32_t *bra)
+{
+	const jn_t3block_t *b = &p->tb[blk];
+	if (b->kind == 0) {
+		*ket = p->conn_ket[b->conn + i];
+		*bra = p->conn_bra[b->conn + i];
+		return;
+	}
+	const int64_t kp = i / b->nn, kn = i - kp * b->nn;
+	const jn_p3conn_t *c = &p->pc[b->conn + kp];
+	const jn_nconn_t *n = &p->nc[b->nconn + kn];
+	int32_t k = p->lut[c->ket_lut + (int64_t)c->p_ann * c->ket_nn + n->n_ann];
+	int32_t r = p->lut[c->bra_lut + (int64_t)c->p_cre * c->bra_nn + n->n_cre];
+	*ket = k < 0 ? -k - 1 : k;
+	*bra = r < 0 ? -r - 1 : r;
+}
+
+static const jn_t3plan_t *g_eb_plan;
+static int cmp_block_eb(const void *a, const void *b)
+{
+	const int x = *(const int *)a, y = *(const int *)b;
+	const int ex = g_eb_plan->tb[x].eb, ey = g_eb_plan->tb[y].eb;
+	if (ex != ey) return ex < ey ? -1 : 1;
+	return x - y;
+}
+
+/* Every element's inner sums sum_r S_ket,r V[v][v_r] depend on its energy
+ * block, its ket state, the slot and the bra's row v only: they are computed
+ * once per (energy block, ket) pair and slot, for every row (the reference
+ * forms the same products as V S_ket, block_transform.c:147-356). */
+int jn_t3plan_shared(jn_t3plan_t *p, char *err, size_t errlen)
+{
+	free(p->elem_pair); free(p->pair_seg); free(p->seg);
+	p->elem_pair = NULL; p->pair_seg = NULL; p->seg = NULL;
+	p->npairs = p->nseg = p->nT = 0;
+	int32_t *stamp = (int32_t *)malloc((p->nms ? p->nms : 1) * sizeof(int32_t));
+	int32_t *pid = (int32_t *)malloc((p->nms ? p->nms : 1) * sizeof(int32_t));
+	int *order = (int *)malloc((p->n3 ? p->n3 : 1) * sizeof(int));
+	int64_t pcap = 1024, npairs = 0;
+	int32_t *pairs = (int32_t *)malloc(pcap * 2 * sizeof(int32_t));
+	p->elem_pair = (int32_t *)malloc((p->nelem ? p->nelem : 1) * sizeof(int32_t));
+	if (!stamp || !pid || !order || !pairs || !p->elem_pair) goto oom;
+	for (int64_t i = 0; i < p->nms; i++) stamp[i] = -1;
+	for (int b = 0; b < p->n3; b++) order[b] = b;
+	g_eb_plan = p;
+	qsort(order, (size_t)p->n3, sizeof(int), cmp_block_eb);
+	/* pairs in order of first use, blocks grouped by energy block */
+	for (int ob = 0; ob < p->n3; ob++) {
+		const int blk = order[ob];
+		const jn_t3block_t *b = &p->tb[blk];
+		for (int64_t i = 0; i < b->count; i++) {
+			int32_t ket, bra;
+			t3_element_states(p, blk, i, &ket, &bra);
+			if (ket < 0 || ket >= p->nms) { snprintf(err, errlen, "element state out of range"); goto fail; }
+			if (stamp[ket] != b->eb) {
+				stamp[ket] = b->eb;
+				if (npairs == pcap) {
+					pcap *= 2;
+					int32_t *q = (int32_t *)realloc(pairs, pcap * 2 * sizeof(int32_t));
+					if (!q) goto oom;
+					pairs = q;
+				}
+				if (npairs >= 0x7fffffff) { snprintf(err, errlen, "too many (energy block, ket) pairs"); goto fail; }
+				pairs[2 * npairs] = b->eb;
+				pairs[2 * npairs + 1] = ket;
+				pid[ket] = (int32_t)npairs++;
+			}
+			p->elem_pair[b->out + i] = pid[ket];
+		}
+	}
+	/* segments: the ket's slots in term order, T laid out pair by pair */
+	p->pair_seg = (int64_t *)malloc((size_t)(npairs + 1) * sizeof(int64_t));
+	int64_t scap = npairs * 4 + 16, nseg = 0, nT = 0;
+	p->seg = (jn_t3seg_t *)malloc((size_t)scap * sizeof(jn_t3seg_t));
+	if (!p->pair_seg || !p->seg) goto oom;
+	for (int64_t k = 0; k < npairs; k++) {
+		const int eb = pairs[2 * k];
+		const jn_m3state_t *K = &p->ms[pairs[2 * k + 1]];
+		p->pair_seg[k] = nseg;
+		for (int r = K->ent; r < K->ent + K->nent;) {
+			const int slot = p->term[r].slot;
+			int r1 = r;
+			while (r1 < K->ent + K->nent && p->term[r1].slot == slot) r1++;
+			if (nseg == scap) {
+				scap *= 2;
+				jn_t3seg_t *q = (jn_t3seg_t *)realloc(p->seg, (size_t)scap * sizeof(jn_t3seg_t));
+				if (!q) goto oom;
+				p->seg = q;
+			}
+			jn_t3seg_t *sg = &p->seg[nseg++];
+			const int64_t off = p->voff[(int64_t)eb * p->nslots + slot];
+			sg->term0 = r;
+			sg->nterm = (int16_t)(r1 - r);
+			sg->slot = (int16_t)slot;
+			sg->eb = eb;
+			sg->rows = off >= 0 ? p->vrows[(int64_t)eb * p->nslots + slot] : 0;
+			sg->toff = off >= 0 ? nT : -1;
+			nT += sg->rows;
+			r = r1;
+		}
+	}
+	p->pair_seg[npairs] = nseg;
+	p->npairs = npairs;
+	p->nseg = nseg;
+	p->nT = nT;
+	free(stamp); free(pid); free(order); free(pairs);
+	return 0;
+oom:
+	snprintf(err, errlen, "out of memory");
+fail:
+	free(stamp); free(pid); free(order); free(pairs);
+	free(p->elem_pair); free(p->pair_seg); free(p->seg);
+	p->elem_pair = NULL; p->pair_seg = NULL; p->seg = NULL;
 	return -1;
 }

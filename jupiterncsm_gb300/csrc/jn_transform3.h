@@ -59,6 +59,16 @@ typedef struct {
 	int32_t pad;
 } jn_t3block_t;
 
+/* one slot of a (energy block, ket) pair (24 bytes): T[toff + v] =
+ * sum_r S_r V(eb, slot)[v][v_r] over the ket's terms r of the slot, v < rows */
+typedef struct {
+	int64_t toff;           /* first T entry; -1 when V(eb, slot) is absent */
+	int32_t term0;          /* the ket's first term of the slot */
+	int16_t nterm, slot;
+	int32_t rows;
+	int32_t eb;
+} jn_t3seg_t;
+
 /* kind 1: a ket (bra) state is lut[ket_lut + p_pos * ket_nn + n_pos] */
 typedef struct {
 	int32_t p_ann, p_cre;
@@ -85,8 +95,17 @@ typedef struct {
 	int neb;
 	int64_t *voff;                  /* neb x nslots */
 	int32_t *vld;                   /* neb x nslots */
+	int32_t *vrows;                 /* neb x nslots: rows (the bra basis' coupled states) */
 	int64_t nv;
 	double *V;
+	/* shared inner sums (jn_t3plan_shared): T = V(eb, slot) s_ket over every row, for each
+	   (energy block, ket state) pair that elements use and each slot of the ket */
+	int64_t npairs;
+	int32_t *elem_pair;             /* per element: its (energy block, ket) pair */
+	int64_t *pair_seg;              /* per pair: its first segment (npairs + 1 entries) */
+	int64_t nseg;
+	jn_t3seg_t *seg;
+	int64_t nT;                     /* T entries */
 	/* connections */
 	int64_t nconn0;
 	int32_t *conn_ket, *conn_bra, *conn_sign;
@@ -105,6 +124,9 @@ typedef struct {
 int jn_t3plan_build(jn_t3plan_t *p, const char *comb, const char *lists_dir, int Z, int N, int emax,
 		    const char *jscheme_dir, char *err, size_t errlen);
 void jn_t3plan_free(jn_t3plan_t *p);
+/* The shared-inner-sum layout of a built plan (elem_pair, pair_seg, seg, nT);
+ * returns 0 or sets *err. */
+int jn_t3plan_shared(jn_t3plan_t *p, char *err, size_t errlen);
 
 #ifdef __cplusplus
 }
