@@ -379,6 +379,8 @@ def large_solve_leg(workdir, steps, warmup, flush, max_iterations=300, check_eve
             sec = time.perf_counter() - t0
             out[name] = {"seconds": sec, "iterations": r["iterations"], "converged": r["converged"],
                          "ms_per_step": 1e3 * sec / max(r["iterations"], 1),
+                         "loop_ms_per_step": 1e3 * r["iteration_seconds"] / max(r["iterations"], 1),
+                         "refinement_seconds": r["refinement_seconds"],
                          "product_kernel_ms": sum(ks) / len(ks),
                          "eigenvalues_MeV": [float(v) for v in r["eigenvalues"]],
                          "residual_norms": [float(v) for v in r["residual_norms"]]}
@@ -702,9 +704,11 @@ def main():
     ap.add_argument("--schedule", metavar="ROWS,CTAS",
                     help="fix the panel schedule (rows per lane, CTAs per SM) instead of autotuning it "
                          "(panel-engine workloads)")
-    ap.add_argument("--leg", choices=["transform", "transform3", "product"],
+    ap.add_argument("--leg", choices=["transform", "transform3", "product", "large_solve"],
                     help="run only this leg and print its JSON (a diagnostic run, e.g. under ncu; not the bench line); "
-                         "product: --steps products of --workload on --engine in --arith, timed with CUDA events")
+                         "product: --steps products of --workload on --engine in --arith, timed with CUDA events; "
+                         "large_solve: the 6Li Nmax 6 2+3NF solves, --max-iterations steps at most")
+    ap.add_argument("--max-iterations", type=int, default=300, help="Lanczos steps at most (--leg large_solve)")
     ap.add_argument("--engine", type=int, choices=[2, 3, 4, 5], help="the product engine (--leg product)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -714,6 +718,10 @@ def main():
     if args.leg:
         import torch
         flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+        if args.leg == "large_solve":
+            print(json.dumps({"large_solve": large_solve_leg(args.workdir, args.steps, args.warmup, flush,
+                                                             max_iterations=args.max_iterations)}), flush=True)
+            return
         peaks = measured_peaks()
         leg = transform_leg if args.leg == "transform" else transform3_leg
         print(json.dumps({args.leg: leg(args.workdir, args.steps, args.warmup, flush,

@@ -287,6 +287,8 @@ typedef struct {
 	double eigenvalues[JN_MAX_REPORTED];    /* Rayleigh quotients of the Ritz vectors (FP64 products) */
 	double ritz_values[JN_MAX_REPORTED];    /* eigenvalues of the tridiagonal matrix */
 	double residual_norms[JN_MAX_REPORTED]; /* |H x - rq x| / |x| */
+	double iteration_seconds;      /* host time of the Lanczos steps and their convergence checks */
+	double refinement_seconds;     /* host time of the Ritz vectors and their FP64-grade products */
 } jn_lanczos_result;
 
 /* Run Lanczos on the context's Hamiltonian.  Replaces new_lanczos_environment

@@ -103,7 +103,8 @@ class LanczosOptions(ctypes.Structure):
 class LanczosResult(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("num_ritz_values", ctypes.c_int),
                 ("num_eigenvalues", ctypes.c_int), ("eigenvalues", ctypes.c_double * MAX_REPORTED),
-                ("ritz_values", ctypes.c_double * MAX_REPORTED), ("residual_norms", ctypes.c_double * MAX_REPORTED)]
+                ("ritz_values", ctypes.c_double * MAX_REPORTED), ("residual_norms", ctypes.c_double * MAX_REPORTED),
+                ("iteration_seconds", ctypes.c_double), ("refinement_seconds", ctypes.c_double)]
 
 
 _gpu = None
@@ -304,7 +305,8 @@ class Hamiltonian:
         n = r.num_eigenvalues
         return {"iterations": r.iterations, "converged": bool(r.converged), "num_ritz_values": r.num_ritz_values,
                 "eigenvalues": np.array(r.eigenvalues[:n]), "ritz_values": np.array(r.ritz_values[:n]),
-                "residual_norms": np.array(r.residual_norms[:n]), "status": st}
+                "residual_norms": np.array(r.residual_norms[:n]), "status": st,
+                "iteration_seconds": r.iteration_seconds, "refinement_seconds": r.refinement_seconds}
 
     def me_count(self):
         return int(gpu_lib().jn_me_count(self._h))

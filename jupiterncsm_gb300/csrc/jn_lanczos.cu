@@ -36,6 +36,7 @@
 #include <string.h>
 #include <sys/stat.h>
 #include <sys/types.h>
+#include <time.h>
 
 #include <vector>
 
@@ -81,32 +82,36 @@ void jn_lanczos_release(jn_ctx *c)
 /* ------------------------------------------------------------------ */
 /* BLAS-1/2 kernels with fixed reduction order                         */
 /* ------------------------------------------------------------------ */
-#define block_sum jn_block_sum
 
-/* part[b*ncol + j] = sum over this block's slice of V[j] . w, j < nvec */
+/* part[b*ncol + j] = sum over this block's slice of V[j] . w, j < nvec:
+ * warp j % (warps) owns vector j and reduces it with shuffles in a fixed
+ * order, so the vectors run side by side with no CTA-wide barrier */
 __global__ void __launch_bounds__(RED_THREADS) k_gemv_t(const double *__restrict__ V, int64_t D, int nvec,
 							 const double *__restrict__ w, double *__restrict__ part, int ncol)
 {
-	__shared__ double sh[RED_THREADS];
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 	const int64_t chunk = (D + gridDim.x - 1) / gridDim.x;
 	const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(D, i0 + chunk);
-	for (int j = 0; j < nvec; j++) {
+	for (int j = warp; j < nvec; j += nwarps) {
 		const double *v = V + (int64_t)j * D;
 		double s = 0.0;
-		for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s = fma(v[i], w[i], s);
-		s = block_sum(s, sh);
-		if (threadIdx.x == 0) part[(int64_t)blockIdx.x * ncol + j] = s;
+		for (int64_t i = i0 + lane; i < i1; i += 32) s = fma(v[i], w[i], s);
+		for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+		if (lane == 0) part[(int64_t)blockIdx.x * ncol + j] = s;
 	}
 }
 
-/* out[j] = sum_b part[b*ncol + j] in block order; optional scale */
+/* out[j] = sum_b part[b*ncol + j], one warp per j: lane l sums blocks
+ * l, l + 32, ... in order, then the lanes' sums are added by a fixed
+ * shuffle tree (the partials' loads are in flight together) */
 __global__ void k_finish(const double *__restrict__ part, int nblk, int ncol, int nvec, double *__restrict__ out)
 {
-	int j = blockIdx.x * blockDim.x + threadIdx.x;
-	if (j >= nvec) return;
+	const int j = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+	if (j >= nvec) return;          /* warp-uniform */
 	double s = 0.0;
-	for (int b = 0; b < nblk; b++) s += part[(int64_t)b * ncol + j];
-	out[j] = s;
+	for (int b = lane; b < nblk; b += 32) s += part[(int64_t)b * ncol + j];
+	for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	if (lane == 0) out[j] = s;
 }
 
 /* w -= sum_j V[j] h[j] (j < nvec) */
@@ -200,6 +205,13 @@ __global__ void k_tri_mgs(double *__restrict__ Z, int ldz, int n, int want)
 /* ------------------------------------------------------------------ */
 /* host driver                                                         */
 /* ------------------------------------------------------------------ */
+static double seconds_now(void)
+{
+	struct timespec t;
+	clock_gettime(CLOCK_MONOTONIC, &t);
+	return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
 static int grid_for(int64_t D) { int64_t g = (D + 255) / 256; return (int)(g < 4096 ? (g > 0 ? g : 1) : 4096); }
 
 /* res = <x|y> into device scalar */
@@ -217,7 +229,7 @@ static void cgs_pass(jn_ctx *c, int nvec)
 	if (nvec <= 0) return;
 	int ncol = s->mmax + 2;
 	k_gemv_t<<<RED_BLOCKS, RED_THREADS, 0, c->stream>>>(s->d_V, s->D, nvec, s->d_w, s->d_part, ncol);
-	k_finish<<<(nvec + 127) / 128, 128, 0, c->stream>>>(s->d_part, RED_BLOCKS, ncol, nvec, s->d_h);
+	k_finish<<<(nvec + 3) / 4, 128, 0, c->stream>>>(s->d_part, RED_BLOCKS, ncol, nvec, s->d_h);
 	k_gemv_n_sub<<<grid_for(s->D), 256, 0, c->stream>>>(s->d_V, s->D, nvec, s->d_h, s->d_w);
 }
 
@@ -321,6 +333,8 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 	std::vector<double> zbuf(by_vector ? 2 * (size_t)(m + 1) : 0, 0.0);
 	double *zprev = zbuf.data();
 	res->iterations = 0;
+	res->iteration_seconds = res->refinement_seconds = 0.0;
+	const double t_loop = seconds_now();
 	for (k = 0; k < m; k++) {
 		double *vk = V + (int64_t)k * D, *vk1 = V + (int64_t)(k + 1) * D;
 		st = jn_launch_matvec(c, vk, s->d_w, 0, q);
@@ -389,6 +403,8 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 	s->k = k;
 	res->iterations = k;
 	res->converged = converged;
+	const double t_final = seconds_now();      /* the loop ends on a convergence check, which synchronises */
+	res->iteration_seconds = t_final - t_loop;
 	/* final decomposition of T_k: all Ritz values, vectors of the lowest nev */
 	CUDA_TRY(cudaMemcpyAsync(s->h_alpha, s->d_alpha, k * sizeof(double), cudaMemcpyDeviceToHost, q));
 	CUDA_TRY(cudaMemcpyAsync(s->h_beta, s->d_beta, k * sizeof(double), cudaMemcpyDeviceToHost, q));
@@ -428,6 +444,7 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 	}
 	c->precision = prec0;
 	CUDA_TRY(cudaGetLastError());
+	res->refinement_seconds = seconds_now() - t_final;
 	res->num_eigenvalues = want;
 	for (int i = 0; i < want && i < JN_MAX_REPORTED; i++) {
 		res->eigenvalues[i] = s->h_rq[i];
