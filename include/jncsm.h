@@ -149,17 +149,19 @@ jn_status jn_matvec_profile(jn_ctx *ctx, const double *d_x, double *d_y, int acc
  * FP32 copy, which is the reference's skip (matrix_vector_multiplication.c:52-53). */
 jn_status jn_set_precision(jn_ctx *ctx, int precision);
 
-/* Product engine: 4 (default when the dimension is at most 26 624) — panels:
- * every instruction's referenced matrix elements, signs applied, stored
- * densely and streamed once, with the blocks of y a CTA touches accumulated
- * in shared memory as exact 64-bit fixed-point integers; 5 (default above
- * that) — walks: each instruction's longer list walked by destination in
- * lane chunks, the other list's rows grouped by connection index, each row
- * summed in registers over a chunk and rounded once into a warp-private
- * shared-memory accumulator (the walk plan is built on the first product);
- * 3 — shared-memory block tiles with exact 64-bit fixed-point sums; 2 —
- * one warp per 32-element piece, FP64 sums in fixed term order.  Engines 3,
- * 4 and 5 give bit-identical results whatever the execution order. */
+/* Product engine: 4 — panels: every instruction's referenced matrix
+ * elements, signs applied, stored densely and streamed once, with the
+ * blocks of y a CTA touches accumulated in shared memory as exact 64-bit
+ * fixed-point integers; 5 — walks: each instruction's longer list walked by
+ * destination in lane chunks, the other list's rows grouped by connection
+ * index, each row summed in registers over a chunk and rounded once into
+ * the lane's shared-memory slot (the walk plan is built on the first
+ * product); 3 — shared-memory block tiles with exact 64-bit fixed-point
+ * sums; 2 — one warp per 32-element piece, FP64 sums in fixed term order.
+ * Defaults: engine 5 at precision 64 (its exact-integer arithmetic); at
+ * precision 32, engine 4 when the dimension is at most 26 624, else 5.
+ * jn_set_engine fixes one engine for both precisions.  Engines 3, 4 and 5
+ * give bit-identical results whatever the execution order. */
 jn_status jn_set_engine(jn_ctx *ctx, int engine);
 
 /* Arithmetic of the walk engine's precision-64 products: 0 (default) —

@@ -706,7 +706,7 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	int *pcoef = NULL, *pxbuf = NULL;
 	BALLOC(me64, (size_t)B * nme);
 	/* 32-bit products on the panel engine where it is this context's engine */
-	const int panels = f32 && c->engine == 4 && jn_panels_setup(c) == JN_OK && jn_panels_fit(c, 1);
+	const int panels = f32 && c->engine_of[1] == 4 && jn_panels_setup(c) == JN_OK && jn_panels_fit(c, 1);
 	if (f32 && !panels) { BALLOC(me32, (size_t)B * nme); BALLOC(x32, (size_t)B * D); }
 	else BALLOC(x64, (size_t)B * D);
 	BALLOC(gacc, (size_t)B * D);

@@ -41,7 +41,9 @@ struct jn_ctx {
 	int precision;          /* 64: FP64 products; 32: FP32 matrix elements and x, compensated sums */
 	float *d_me32;          /* FP32 copy of the matrix elements (built on first FP32 use) */
 	float *d_x32;
-	int engine;             /* 4: panels (default up to JN_PANEL_MAX_DIM states); 5: walks (default above); 3: block tiles; 2: warp pieces */
+	int engine;             /* the engine at the current precision: 4 panels, 5 walks, 3 block tiles, 2 warp pieces */
+	int engine_of[2];       /* the engine at precision 64 [0] (default 5) and 32 [1] (default 4 up to
+	                           JN_PANEL_MAX_DIM states, 5 above) */
 	jn_btile_t *d_btiles;
 	jn_piece_t *d_pieces;
 	jn_tterm_t *d_tterms;

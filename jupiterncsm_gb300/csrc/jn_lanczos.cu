@@ -420,12 +420,13 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 		k_gemv_n<<<g, 256, 0, q>>>(V, D, k, s->d_Z + (size_t)i * ldz, s->d_ritz + (size_t)i * D);
 	s->have_ritz = 1;
 	/* the refinement's products are FP64-grade whatever the iteration's precision */
-	const int prec0 = c->precision;
+	const int prec0 = c->precision, engine0 = c->engine;
 	c->precision = 64;
+	c->engine = c->engine_of[0];
 	for (int i = 0; i < want; i++) {
 		double *xi = s->d_ritz + (size_t)i * D;
 		st = jn_launch_matvec(c, xi, s->d_w, 0, q);
-		if (st) { c->precision = prec0; return st; }
+		if (st) { c->precision = prec0; c->engine = engine0; return st; }
 		dot_dev(c, xi, s->d_w, s->d_scalar + 0);
 		dot_dev(c, xi, xi, s->d_scalar + 1);
 		double h2[2];
@@ -443,6 +444,7 @@ extern "C" jn_status jn_lanczos(jn_ctx *c, const jn_lanczos_options *opt, jn_lan
 		s->h_res[i] = sqrt(r2 / h2[1]);
 	}
 	c->precision = prec0;
+	c->engine = engine0;
 	CUDA_TRY(cudaGetLastError());
 	res->refinement_seconds = seconds_now() - t_final;
 	res->num_eigenvalues = want;

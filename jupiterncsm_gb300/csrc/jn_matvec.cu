@@ -594,13 +594,15 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 		c->tile_grid = c->num_sms * per_sm;
 		if (c->tile_grid > p->nbtiles) c->tile_grid = p->nbtiles > 0 ? p->nbtiles : 1;
 	}
-	/* the panel engine where the whole accumulator fits in shared memory, else
-	   the walk engine (its plan is built on the first product) */
-	c->engine = 5;
+	/* 32-bit products: the panel engine where the whole accumulator fits in
+	   shared memory, else the walk engine; FP64-grade products: the walk
+	   engine's exact integers (its plan is built on the first product) */
+	c->engine_of[0] = c->engine_of[1] = 5;
 	if (p->dim <= JN_PANEL_MAX_DIM) {
-		if (jn_panels_setup(c) == JN_OK) c->engine = 4;
+		if (jn_panels_setup(c) == JN_OK) c->engine_of[1] = 4;
 		else jn_panels_release(c);
 	}
+	c->engine = c->engine_of[c->precision == 32];
 	cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
 	if (e != cudaSuccess) { jn_close(c); return fail(JN_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
 	e = cudaMallocHost((void **)&c->h_pinned, (p->dim ? p->dim : 1) * sizeof(double));
@@ -775,7 +777,7 @@ extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 		jn_status s = jn_walk_setup(c);
 		if (s) return s;
 	}
-	c->engine = engine;
+	c->engine = c->engine_of[0] = c->engine_of[1] = engine;
 	return JN_OK;
 }
 
@@ -800,6 +802,7 @@ extern "C" jn_status jn_set_precision(jn_ctx *c, int precision)
 		if (s) return s;
 	}
 	c->precision = precision;
+	c->engine = c->engine_of[precision == 32];
 	return jn_panels_apply_tuned(c);
 }
 

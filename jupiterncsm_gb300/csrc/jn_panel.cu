@@ -834,6 +834,7 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 	const int prec0 = c->precision, f32_0 = prec0 == 32;
 	c->tuned_iter[0] = c->tuned_iter[1] = 0;
 	jn_status s = autotune(c, trials, tune_engine, out, flush, bytes);
+	if (!s) c->engine_of[f32_0] = c->engine;      /* the choice holds for this precision */
 	if (!s && out->engine == 4) {
 		c->tuned_iter[f32_0] = out->rows_per_lane;
 		c->tuned_per[f32_0] = out->ctas_per_sm;
@@ -845,6 +846,7 @@ extern "C" jn_status jn_autotune(jn_ctx *c, int trials, int tune_engine, jn_tuni
 				c->tuned_per[!f32_0] = other.ctas_per_sm;
 			}
 			c->precision = prec0;
+			c->engine = c->engine_of[f32_0];
 			s = panel_schedule(c, out->rows_per_lane, out->ctas_per_sm);
 		}
 	}
@@ -1209,7 +1211,7 @@ void jn_panel_batch_free(jn_panel_batch *pb)
 int jn_panel_batch_possible(jn_ctx *const *ctxs, int nbases)
 {
 	for (int b = 0; b < nbases; b++)
-		if (ctxs[b]->engine != 4 || jn_panels_setup(ctxs[b]) != JN_OK || !jn_panels_fit(ctxs[b], 1)) {
+		if (ctxs[b]->engine_of[1] != 4 || jn_panels_setup(ctxs[b]) != JN_OK || !jn_panels_fit(ctxs[b], 1)) {
 			cudaGetLastError();
 			return 0;
 		}
