@@ -28,6 +28,7 @@
  * that the manager's shells lack, indices past the file's states, basis
  * files whose states are not ascending, and blocks that change total M.
  */
+#define _GNU_SOURCE        /* qsort_r */
 #include "jn_transform3.h"
 #include "jn_jt.h"
 
@@ -1229,11 +1230,11 @@ static void t3_element_states(const jn_t3plan_t *p, int blk, int64_t i, int32_t 
 	*bra = r < 0 ? -r - 1 : r;
 }
 
-static const jn_t3plan_t *g_eb_plan;
-static int cmp_block_eb(const void *a, const void *b)
+static int cmp_block_eb(const void *a, const void *b, void *plan)
 {
+	const jn_t3plan_t *p = (const jn_t3plan_t *)plan;
 	const int x = *(const int *)a, y = *(const int *)b;
-	const int ex = g_eb_plan->tb[x].eb, ey = g_eb_plan->tb[y].eb;
+	const int ex = p->tb[x].eb, ey = p->tb[y].eb;
 	if (ex != ey) return ex < ey ? -1 : 1;
 	return x - y;
 }
@@ -1256,8 +1257,7 @@ int jn_t3plan_shared(jn_t3plan_t *p, char *err, size_t errlen)
 	if (!stamp || !pid || !order || !pairs || !p->elem_pair) goto oom;
 	for (int64_t i = 0; i < p->nms; i++) stamp[i] = -1;
 	for (int b = 0; b < p->n3; b++) order[b] = b;
-	g_eb_plan = p;
-	qsort(order, (size_t)p->n3, sizeof(int), cmp_block_eb);
+	qsort_r(order, (size_t)p->n3, sizeof(int), cmp_block_eb, p);
 	/* pairs in order of first use, blocks grouped by energy block */
 	for (int ob = 0; ob < p->n3; ob++) {
 		const int blk = order[ob];

@@ -15,6 +15,7 @@
  * and the rounded sums are added as integers, so the order never changes a
  * result between runs).
  */
+#define _GNU_SOURCE        /* qsort_r */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -115,10 +116,10 @@ static int cmp_row(const void *a, const void *b)
 	return (int)x->sign - (int)y->sign;
 }
 
-static const jn_plan_t *g_order_plan;
-static int cmp_instr_block(const void *a, const void *b)
+static int cmp_instr_block(const void *a, const void *b, void *plan)
 {
-	const jn_instr_t *x = &g_order_plan->instr[*(const int *)a], *y = &g_order_plan->instr[*(const int *)b];
+	const jn_plan_t *P = (const jn_plan_t *)plan;
+	const jn_instr_t *x = &P->instr[*(const int *)a], *y = &P->instr[*(const int *)b];
 	if (x->me != y->me) return x->me < y->me ? -1 : 1;
 	if (x->bout != y->bout) return x->bout < y->bout ? -1 : 1;
 	if (x->bin != y->bin) return x->bin < y->bin ? -1 : 1;
@@ -167,8 +168,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	order = malloc((size_t)(p->ninstr > 0 ? p->ninstr : 1) * sizeof(int));
 	if (!order) ERR("out of host memory");
 	for (int q = 0; q < p->ninstr; q++) order[q] = q;
-	g_order_plan = p;
-	qsort(order, (size_t)p->ninstr, sizeof(int), cmp_instr_block);
+	qsort_r(order, (size_t)p->ninstr, sizeof(int), cmp_instr_block, p);
 	for (int oq = 0; oq < p->ninstr; oq++) {
 		const int q = order[oq];
 		const jn_instr_t *x = &p->instr[q];
@@ -227,7 +227,8 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 			/* row index bounds: sources and destinations inside their blocks, k inside the element block */
 			const int64_t src_rows = wp ? bs->Nn : bs->Np, dst_rows = wp ? bd->Nn : bd->Np;
 			for (int64_t e = 0; e < nr; e++)
-				if (R[e].src >= src_rows || R[e].dst >= dst_rows || R[e].src > 0xffffu || R[e].k >= rlen)
+				if (R[e].src >= src_rows || R[e].dst >= dst_rows || R[e].src > 0xffffu || R[e].dst > 0xffffu ||
+				    R[e].k >= rlen)
 					ERR("instruction %d: row index out of range", q);
 			/* walk view and its bounds: destinations and sources inside their blocks, k inside the block */
 			const int64_t w0 = dir ? W->walk_in : W->walk_out, nw = dir ? W->nwalk_in : W->nwalk_out;
