@@ -46,6 +46,8 @@ class Emu3:
             L.t3emu_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             L.t3emu_close.argtypes = [ctypes.c_void_p]
             L.t3emu_error.restype = ctypes.c_char_p
+            L.t3emu_check_shared.restype = ctypes.c_int64
+            L.t3emu_check_shared.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
             Emu3.lib = L
         jdir = jdir or os.path.join(d, "jjj")
         self.h = Emu3.lib.t3emu_open(os.path.join(d, "comb.txt").encode(), os.path.join(d, "anicr").encode(), Z, N, e,
@@ -70,6 +72,12 @@ class Emu3:
         Emu3.lib.t3emu_stats(self.h, v.ctypes.data)
         return dict(zip(["elements", "states", "terms", "coupled", "file_states", "file_elements", "v_entries",
                          "energy_blocks"], v.tolist()))
+
+    def check_shared(self):
+        """(elements that differ, {pairs, segments, inner sums}) of the shared-inner-sum arithmetic."""
+        v = np.zeros(3, dtype=np.int64)
+        bad = Emu3.lib.t3emu_check_shared(self.h, v.ctypes.data)
+        return int(bad), dict(zip(["pairs", "segments", "inner_sums"], v.tolist()))
 
     def close(self):
         Emu3.lib.t3emu_close(self.h)
@@ -151,6 +159,22 @@ def test_model_matches_golden(j3problem, name):
         assert worst <= ME_TOL
         st = emu.stats()
         assert st["elements"] == meta["num_elements"]
+    finally:
+        emu.close()
+
+
+@pytest.mark.parametrize("Z,N,nmax,M2", [(2, 2, 4, 0), (3, 4, 2, 1), (1, 2, 2, 1)])
+def test_shared_inner_sums_are_bit_identical(Z, N, nmax, M2, tmp_path):
+    """The GPU's two launches (inner sums V s_ket once per (energy block, ket)
+    pair and slot, then each element from them) give every element bit for bit
+    as summing each inner sum on the spot: He4 Nmax 4, Li7 Nmax 2, H3 Nmax 2."""
+    d = str(tmp_path / "p")
+    e, _ = make_case(d, Z, N, nmax, M2)
+    emu = Emu3(d, Z, N, e)
+    try:
+        bad, st = emu.check_shared()
+        assert bad == 0
+        assert st["pairs"] > 0 and st["segments"] >= st["pairs"] and st["inner_sums"] > 0
     finally:
         emu.close()
 
