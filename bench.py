@@ -78,6 +78,21 @@ KERNELS = {(4, "f32"): "jn_panel_kernel_i32", (4, "i64"): "jn_panel_kernel_fp64"
 LAUNCHES = {(5, "i64"): 4}
 
 
+def max_over_ranks(v, dist, device):
+    """The largest of every rank's v (a job takes as long as its slowest rank); v itself on one rank."""
+    if not dist:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gbs(bytes_per_step, world, seconds_per_step):
+    """Whole-job GB/s: every rank's products (replicas of the same workload) over the slowest rank's time."""
+    return bytes_per_step * world / seconds_per_step / 1e9
+
+
 def profile_traffic(workload, engine, arith):
     """DRAM bytes (read + write) per launch of the product kernel from the committed ncu summary, if any."""
     name = {4: "jn_panel_kernel", 3: "jn_tile_kernel", 5: "jn_walk_kernel"}[engine]
@@ -830,11 +845,7 @@ def main():
             k, r = H.matvec_profile(x.data_ptr(), y.data_ptr(), accumulate=False)
             kern_ms += k
             prof_total += k + r
-        t_max = total_ms
-        if dist:
-            t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            t_max = float(t.item())
+        t_max = max_over_ranks(total_ms, dist, dev)
         return {"ms_per_step": t_max / args.steps, "kernel_ms": kern_ms / args.steps, "wall_s": wall,
                 "profiled_ms_per_step": prof_total / args.steps, "clocks": clocks, "setup_s": setup_s,
                 "y": y.cpu().numpy().copy()}
@@ -852,7 +863,7 @@ def main():
     runs = {a: timed(a) for a in order}
     main_r = runs[args.arith]
     bytes_step = bytes_for("i64")                      # the reference's FP64 bytes, whatever the arithmetic
-    value = bytes_step * world / (main_r["ms_per_step"] / 1e3) / 1e9
+    value = job_gbs(bytes_step, world, main_r["ms_per_step"] / 1e3)
 
     # end to end through the public host-pointer call, pinned host buffers
     set_arith(args.arith)
@@ -867,7 +878,7 @@ def main():
         t0 = time.perf_counter()
         H.matvec(hx, hy)
         e2e_s += time.perf_counter() - t0
-    e2e_value = bytes_step * args.steps * world / e2e_s / 1e9
+    e2e_value = job_gbs(bytes_step, world, max_over_ranks(e2e_s, dist, dev) / args.steps)
 
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
