@@ -222,6 +222,7 @@ typedef struct {
  */
 #define JN_WALK_RS 16           /* distinct destination rows of a piece */
 #define JN_WALK_GROUP_END 0x40000000u   /* row word: the last row of its group */
+#define JN_WALK_ROW_SPARE 2             /* zero row words after the last: the kernel reads up to two ahead */
 #define JN_WALK_POS 0x40000000u         /* lane entry multiplier +1 (bits 31:30 = 01) */
 #define JN_WALK_NEG 0xC0000000u         /* lane entry multiplier -1 (bits 31:30 = 11); 00 is padding (0) */
 
@@ -299,7 +300,7 @@ typedef struct {
 	int64_t nwpieces;  jn_wpiece_t *wpieces;
 	int64_t n_wlanes;  uint32_t *wlanes;
 	int64_t n_wwalks;  uint32_t *wwalks;
-	int64_t n_wrows;   uint32_t *wrows;    /* source row | slot row << 16 | group end | sign << 31 */
+	int64_t n_wrows;   uint32_t *wrows;    /* source row | slot row << 16 | group end | sign << 31; JN_WALK_ROW_SPARE more */
 	int32_t *wxperm;                        /* position in x of each element of the transposed view xT */
 	int wxt;                                /* proton walks read xT */
 	int64_t n_wrdst;   uint32_t *wrdst;

@@ -410,9 +410,9 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				for (int64_t q = 0; q < B->Np; q++) p->wxperm[B->offset + n * B->Np + q] = (int32_t)(B->offset + q * B->Nn + n);
 		}
 	}
-	/* one spare row word: the kernel reads the word after a group's last row ahead of time */
-	if (vec_reserve(&rows, 1)) ERR("out of host memory");
-	((uint32_t *)rows.a)[rows.n] = 0u;
+	/* spare row words: the kernel reads up to two words past a task's last row ahead of time */
+	if (vec_reserve(&rows, JN_WALK_ROW_SPARE)) ERR("out of host memory");
+	for (int k = 0; k < JN_WALK_ROW_SPARE; k++) ((uint32_t *)rows.a)[rows.n + k] = 0u;
 	if (tasks.n > 0xf0000000ll || lanes.n > 0xffffffffll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
 	    rdst.n > 0x7fffffffll || groups.n > 0x7fffffffll || pieces.n > 0xffffffffll)
 		ERR("the walk plan is too large");
@@ -420,7 +420,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	p->wpieces = pieces.a; p->nwpieces = pieces.n;
 	p->wlanes = lanes.a; p->n_wlanes = lanes.n;
 	p->wwalks = walks.a; p->n_wwalks = walks.n;
-	p->wrows = rows.a; p->n_wrows = rows.n;         /* plus the spare word */
+	p->wrows = rows.a; p->n_wrows = rows.n;         /* plus the spare words */
 	p->wrdst = rdst.a; p->n_wrdst = rdst.n;
 	p->wgroups = groups.a; p->n_wgroups = groups.n;
 	p->wgblock = gblock.a;

@@ -133,8 +133,8 @@ __device__ __forceinline__ typename WalkT<MODE>::C walk_coef(typename WalkT<MODE
 
 /* one warp task with chunks of U entries (see the file comment).  Rows are
  * taken two at a time, so that two rows' gathers of x are in flight at once;
- * the word after a group's last row is read ahead (the plan keeps a spare
- * word at the end) and not used.  A group's first row pair issues its
+ * up to two words after a group's last row are read ahead (the plan keeps
+ * JN_WALK_ROW_SPARE zero words after the last row) and not used.  A group's first row pair issues its
  * gathers of x before the coefficients (loaded at the top of the group) are
  * first used, so the two latencies overlap. */
 template <int MODE, int U>
@@ -374,7 +374,7 @@ jn_status jn_walk_setup(jn_ctx *c)
 	    (s = wupload(&c->d_wpieces, p->wpieces, (size_t)p->nwpieces * 2)) ||
 	    (s = wupload(&c->d_wlanes, p->wlanes, (size_t)p->n_wlanes)) ||
 	    (s = wupload(&c->d_wwalks, p->wwalks, (size_t)p->n_wwalks)) ||
-	    (s = wupload(&c->d_wrows, p->wrows, (size_t)p->n_wrows + 1)) ||
+	    (s = wupload(&c->d_wrows, p->wrows, (size_t)p->n_wrows + JN_WALK_ROW_SPARE)) ||
 	    (s = wupload(&c->d_wrdst, p->wrdst, (size_t)p->n_wrdst)) ||
 	    (s = wupload(&c->d_wgroups, p->wgroups, (size_t)p->n_wgroups)) ||
 	    (s = wupload(&c->d_wx, (const void *)NULL, (size_t)(p->dim ? p->dim : 1))) ||
