@@ -200,9 +200,10 @@ typedef struct {
  * list, and its rows are the spectators (identity, sign +, one group).  A
  * piece is a run of rows with at most JN_WALK_RS distinct destination rows;
  * a warp task is one piece times 32 lane chunks.  For every row a lane sums
- * its chunk's contributions in registers and adds the sum into a
- * warp-private slot (destination row, walk) in shared memory, which the warp
- * adds into the global accumulator once per task.
+ * its chunk's contributions in registers and adds the sum into its own
+ * shared-memory slot (destination row, lane); at the end of the task the
+ * warp sums each walk's lanes and adds one value per (destination row, walk)
+ * into the global accumulator.
  *
  * Walk list = neutron list (wp = 0): D(r, w) = dst + r Nn_dst + w,
  * S(r, w) = src + r Nn_src + w in x; proton list (wp = 1): D(r, w) = dst +
