@@ -20,6 +20,8 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <pthread.h>
+#include <unistd.h>
 
 #include "jn_problem.h"
 
@@ -37,50 +39,196 @@ void jn_walk_free(jn_plan_t *p)
 	p->wvisits = p->wlane_slots = 0.0;
 }
 
+/* ------------------------------------------------------------------ */
+/* element arrays on the host, built by all cores: work items are chunks  */
+/* of one block (its elements, or the k_p rows of its transposed copy),   */
+/* each independent of the others, so the result does not depend on the  */
+/* number of threads                                                       */
+/* ------------------------------------------------------------------ */
+#define WALK_CHUNK (1 << 20)
+
+typedef struct { int b, kind; int64_t e0, e1; } witem_t;     /* kind 0: elements [e0, e1); 1: transposed rows [e0, e1) */
+
+typedef struct {
+	int64_t n, next;
+	void (*fn)(int64_t, void *);
+	void *arg;
+} par_t;
+
+static void *par_worker(void *v)
+{
+	par_t *p = (par_t *)v;
+	for (;;) {
+		const int64_t i = __atomic_fetch_add(&p->next, 1, __ATOMIC_RELAXED);
+		if (i >= p->n) break;
+		p->fn(i, p->arg);
+	}
+	return NULL;
+}
+
+/* fn(i, arg) for every i < n, on up to 32 threads */
+static void par_for(int64_t n, void (*fn)(int64_t, void *), void *arg)
+{
+	long nt = sysconf(_SC_NPROCESSORS_ONLN);
+	if (nt > 32) nt = 32;
+	if (nt < 1 || n < 2) nt = 1;
+	par_t p = { n, 0, fn, arg };
+	pthread_t th[32];
+	int started = 0;
+	for (long t = 1; t < nt; t++)
+		if (pthread_create(&th[started], NULL, par_worker, &p) == 0) started++;
+	par_worker(&p);
+	for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+/* the work items of every block: its elements and, where proton walks read it, its transposed copy */
+static witem_t *walk_items(const jn_plan_t *p, int64_t *count)
+{
+	int64_t n = 0, cap = 1024;
+	witem_t *it = (witem_t *)malloc((size_t)cap * sizeof(witem_t));
+	for (int b = 0; b < p->nmes && it; b++) {
+		const jn_me_t *M = &p->mes[b];
+		for (int kind = 0; kind < 2; kind++) {
+			if (kind && !(p->wtpos && p->wtpos[b] >= 0)) continue;
+			const int64_t len = kind ? (int64_t)M->nd_p : M->len;
+			const int64_t per = kind ? (M->nd_n ? (WALK_CHUNK + (int64_t)M->nd_n - 1) / (int64_t)M->nd_n : len) : WALK_CHUNK;
+			for (int64_t e0 = 0; e0 < len; e0 += per) {
+				if (n == cap) {
+					cap *= 2;
+					witem_t *g = (witem_t *)realloc(it, (size_t)cap * sizeof(witem_t));
+					if (!g) { free(it); it = NULL; break; }
+					it = g;
+				}
+				it[n++] = (witem_t){ b, kind, e0, e0 + per < len ? e0 + per : len };
+			}
+			if (!it) break;
+		}
+	}
+	*count = n;
+	return it;
+}
+
+typedef struct { const jn_plan_t *p; const witem_t *it; const double *me; double *out; } elem_job_t;
+
+static void elem_item(int64_t i, void *v)
+{
+	const elem_job_t *j = (const elem_job_t *)v;
+	const jn_plan_t *p = j->p;
+	const witem_t *w = &j->it[i];
+	const jn_me_t *M = &p->mes[w->b];
+	if (w->kind == 0) {
+		for (int64_t e = w->e0; e < w->e1; e++) {
+			const double v = j->me[M->offset + e];
+			/* single-species terms skip |M| < 1e-12 (matrix_vector_multiplication.c:52-53) */
+			j->out[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0 : v;
+		}
+	} else {
+		/* [k_p][k_n] copy of an n x p block stored [k_n + Nd_n k_p] */
+		const int64_t nn = (int64_t)M->nd_n, npp = (int64_t)M->nd_p;
+		double *t = j->out + p->wtpos[w->b];
+		for (int64_t kp = w->e0; kp < w->e1; kp++)
+			for (int64_t kn = 0; kn < nn; kn++) t[kp + npp * kn] = j->me[M->offset + kn + nn * kp];
+	}
+}
+
 void jn_walk_elements(const jn_plan_t *p, const double *me, double *out)
 {
-	for (int b = 0; b < p->nmes; b++) {
-		const jn_me_t *M = &p->mes[b];
-		for (int64_t e = 0; e < M->len; e++) {
-			const double v = me[M->offset + e];
-			/* single-species terms skip |M| < 1e-12 (matrix_vector_multiplication.c:52-53) */
-			out[M->offset + e] = (M->single && fabs(v) < 1e-12) ? 0.0 : v;
+	int64_t n = 0;
+	witem_t *it = walk_items(p, &n);
+	if (!it) {              /* out of memory for the item list: one block after another */
+		for (int b = 0; b < p->nmes; b++) {
+			witem_t one[2] = { { b, 0, 0, p->mes[b].len }, { b, 1, 0, (int64_t)p->mes[b].nd_p } };
+			elem_job_t j = { p, one, me, out };
+			elem_item(0, &j);
+			if (p->wtpos && p->wtpos[b] >= 0) elem_item(1, &j);
 		}
-		if (p->wtpos && p->wtpos[b] >= 0) {
-			/* [k_p][k_n] copy of an n x p block stored [k_n + Nd_n k_p] */
-			const int64_t nn = (int64_t)M->nd_n, npp = (int64_t)M->nd_p;
-			double *t = out + p->wtpos[b];
-			for (int64_t kp = 0; kp < npp; kp++)
-				for (int64_t kn = 0; kn < nn; kn++) t[kp + npp * kn] = me[M->offset + kn + nn * kp];
-		}
+		return;
+	}
+	elem_job_t j = { p, it, me, out };
+	par_for(n, elem_item, &j);
+	free(it);
+}
+
+typedef struct { const jn_plan_t *p; const witem_t *it; const double *a; double *imax; const int *sc; int32_t *split; } int_job_t;
+
+/* max |a| over a chunk of a block's own elements */
+static void int_max_item(int64_t i, void *v)
+{
+	const int_job_t *j = (const int_job_t *)v;
+	const witem_t *w = &j->it[i];
+	double m = 0.0;
+	if (w->kind == 0) {
+		const int64_t o = j->p->mes[w->b].offset;
+		for (int64_t e = w->e0; e < w->e1; e++) m = fmax(m, fabs(j->a[o + e]));
+	}
+	j->imax[i] = m;
+}
+
+/* the 52-bit fixed-point split of a chunk (its elements, or its transposed rows) */
+static void int_split_item(int64_t i, void *v)
+{
+	const int_job_t *j = (const int_job_t *)v;
+	const jn_plan_t *p = j->p;
+	const witem_t *w = &j->it[i];
+	const jn_me_t *M = &p->mes[w->b];
+	const int s = j->sc[w->b];
+	int64_t o, e0, e1;
+	if (w->kind == 0) {
+		o = M->offset;
+		e0 = w->e0;
+		e1 = w->e1;
+	} else {            /* transposed rows [e0, e1) hold elements kp + Nd_p kn: convert kp-major runs */
+		o = p->wtpos[w->b];
+		const int64_t npp = (int64_t)M->nd_p, nn = (int64_t)M->nd_n;
+		for (int64_t kn = 0; kn < nn; kn++)
+			for (int64_t kp = w->e0; kp < w->e1; kp++) {
+				const int64_t q = o + kp + npp * kn, v = llrint(ldexp(j->a[q], s));
+				j->split[2 * q] = (int32_t)(v >> 24);
+				j->split[2 * q + 1] = (int32_t)(v & 0xffffff);
+			}
+		return;
+	}
+	for (int64_t e = e0; e < e1; e++) {
+		const int64_t v = llrint(ldexp(j->a[o + e], s));
+		j->split[2 * (o + e)] = (int32_t)(v >> 24);
+		j->split[2 * (o + e) + 1] = (int32_t)(v & 0xffffff);
 	}
 }
 
 void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, uint8_t *gshift, int *sc_min)
 {
 	int *sc = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int));
+	double *bmax = calloc((size_t)(p->nmes ? p->nmes : 1), sizeof(double));
+	int64_t n = 0;
+	witem_t *it = walk_items(p, &n);
+	double *imax = malloc((size_t)(n ? n : 1) * sizeof(double));
+	int_job_t j = { p, it, a, imax, sc, split };
+	if (it && imax) {
+		par_for(n, int_max_item, &j);
+		for (int64_t i = 0; i < n; i++) bmax[it[i].b] = fmax(bmax[it[i].b], imax[i]);
+	} else {
+		for (int b = 0; b < p->nmes; b++)
+			for (int64_t e = 0; e < p->mes[b].len; e++) bmax[b] = fmax(bmax[b], fabs(a[p->mes[b].offset + e]));
+	}
+	/* each block keeps 52 bits against its own max|M|: |v| 2^sc < 2^52 */
 	int lo = 1 << 30;
 	for (int b = 0; b < p->nmes; b++) {
-		const jn_me_t *M = &p->mes[b];
-		double m = 0.0;
-		for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(a[M->offset + e]));
 		int eb = 0;
-		if (m > 0.0) frexp(m, &eb);     /* m < 2^eb */
-		sc[b] = m > 0.0 ? 52 - eb : (1 << 30);
+		if (bmax[b] > 0.0) frexp(bmax[b], &eb);     /* m < 2^eb */
+		sc[b] = bmax[b] > 0.0 ? 52 - eb : (1 << 30);
 		if (sc[b] < lo) lo = sc[b];
 	}
 	if (lo == (1 << 30)) lo = 0;
-	for (int b = 0; b < p->nmes; b++) {
+	for (int b = 0; b < p->nmes; b++)
 		if (sc[b] == (1 << 30)) sc[b] = lo;     /* an all-zero block */
-		const jn_me_t *M = &p->mes[b];
-		for (int pass = 0; pass < 2; pass++) {
-			const int64_t o = pass ? (p->wtpos ? p->wtpos[b] : -1) : M->offset;
-			if (o < 0) continue;
-			for (int64_t e = 0; e < M->len; e++) {
-				const int64_t v = llrint(ldexp(a[o + e], sc[b]));
-				split[2 * (o + e)] = (int32_t)(v >> 24);
-				split[2 * (o + e) + 1] = (int32_t)(v & 0xffffff);
-			}
+	if (it && imax) {
+		par_for(n, int_split_item, &j);
+	} else {
+		for (int b = 0; b < p->nmes; b++) {
+			witem_t one[2] = { { b, 0, 0, p->mes[b].len }, { b, 1, 0, (int64_t)p->mes[b].nd_p } };
+			int_job_t jb = { p, one, a, NULL, sc, split };
+			int_split_item(0, &jb);
+			if (p->wtpos && p->wtpos[b] >= 0) int_split_item(1, &jb);
 		}
 	}
 	for (int64_t g = 0; g < p->n_wgroups; g++) {
@@ -88,7 +236,7 @@ void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, u
 		gshift[g] = (uint8_t)(d > 255 ? 255 : d);
 	}
 	*sc_min = lo;
-	free(sc);
+	free(sc); free(bmax); free(it); free(imax);
 }
 
 /* growable arrays */

@@ -406,36 +406,55 @@ jn_status jn_walk_setup(jn_ctx *c)
 }
 
 /* the walk element array of the current matrix elements for one arithmetic
- * (built on first use and after the matrix elements change): FP64 on the
- * host (the plan's elements plus the transposed blocks), converted on the
- * device for FP32 and for the integer path */
+ * (built on first use and after the matrix elements change), each from the
+ * FP64 array built on the host: FP64 (arithmetic 64); FP32, converted on the
+ * device from the FP64 copy when that exists, else on the host; the
+ * integer path's split 52-bit values with their per-group shifts (only
+ * these reach the device for it) */
 static jn_status walk_elements(jn_ctx *c, int mode)
 {
 	const jn_plan_t *p = &c->plan;
 	const int slot = walk_slot(mode);
 	if (c->d_welem[slot]) return JN_OK;
 	const int64_t n = p->n_wme;
-	if (!c->d_welem[1]) {
-		double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
-		if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
-		jn_walk_elements(p, p->me, h);
-		double *d = NULL;
-		jn_status s = wupload(&d, h, (size_t)n);
-		free(h);
-		if (s) return s;
-		c->d_welem[1] = d;
+	if (mode == 32 && c->d_welem[1]) {
+		const double *a = (const double *)c->d_welem[1];
+		cudaError_t e = cudaMalloc(&c->d_welem[0], (size_t)(n ? n : 1) * sizeof(float));
+		if (e != cudaSuccess) {
+			c->d_welem[0] = NULL;
+			return jn_fail(JN_ERR_NOMEM, "cudaMalloc of %lld walk matrix elements: %s", (long long)n, cudaGetErrorString(e));
+		}
+		const int g = (int)(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
+		if (n) jn_walk_f32_kernel<<<g, 256, 0, c->stream>>>(a, n, (float *)c->d_welem[0]);
+		e = cudaGetLastError();
+		if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk matrix elements: %s", cudaGetErrorString(e));
+		return JN_OK;
 	}
-	if (mode == 64) return JN_OK;
-	if (mode == 1) {
-		/* per-block exponents: every block keeps 52 bits against its own max|A| */
-		double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
-		int32_t *sp = (int32_t *)malloc((size_t)(n ? n : 1) * 2 * sizeof(int32_t));
-		uint8_t *gs = (uint8_t *)malloc((size_t)(p->n_wgroups ? p->n_wgroups : 1));
-		jn_status s = JN_OK;
-		if (!h || !sp || !gs) {
+	double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
+	if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
+	jn_walk_elements(p, p->me, h);
+	jn_status s = JN_OK;
+	if (mode == 64) {
+		double *d = NULL;
+		if (!(s = wupload(&d, h, (size_t)n))) c->d_welem[1] = d;
+	} else if (mode == 32) {
+		float *f = (float *)malloc((size_t)(n ? n : 1) * sizeof(float));
+		if (!f) {
 			s = jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
 		} else {
-			jn_walk_elements(p, p->me, h);
+			for (int64_t e = 0; e < n; e++) f[e] = (float)h[e];
+			float *d = NULL;
+			if (!(s = wupload(&d, f, (size_t)n))) c->d_welem[0] = d;
+			free(f);
+		}
+	} else {
+		/* per-block exponents: every block keeps 52 bits against its own max|A| */
+		int32_t *sp = (int32_t *)malloc((size_t)(n ? n : 1) * 2 * sizeof(int32_t));
+		uint8_t *gs = (uint8_t *)malloc((size_t)(p->n_wgroups ? p->n_wgroups : 1));
+		if (!sp || !gs) {
+			s = jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
+		} else {
 			jn_walk_int_elements(p, h, sp, gs, &c->walk_sc);
 			int2 *d = NULL;
 			s = wupload(&d, sp, (size_t)n);
@@ -446,21 +465,10 @@ static jn_status walk_elements(jn_ctx *c, int mode)
 				s = wupload(&c->d_wgshift, gs, (size_t)p->n_wgroups);
 			}
 		}
-		free(h); free(sp); free(gs);
-		return s;
+		free(sp); free(gs);
 	}
-	const double *a = (const double *)c->d_welem[1];
-	cudaError_t e = cudaMalloc(&c->d_welem[0], (size_t)(n ? n : 1) * sizeof(float));
-	if (e != cudaSuccess) {
-		c->d_welem[0] = NULL;
-		return jn_fail(JN_ERR_NOMEM, "cudaMalloc of %lld walk matrix elements: %s", (long long)n, cudaGetErrorString(e));
-	}
-	const int g = (int)(n / 256 + 1 < 4096 ? n / 256 + 1 : 4096);
-	if (n) jn_walk_f32_kernel<<<g, 256, 0, c->stream>>>(a, n, (float *)c->d_welem[0]);
-	e = cudaGetLastError();
-	if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-	if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk matrix elements: %s", cudaGetErrorString(e));
-	return JN_OK;
+	free(h);
+	return s;
 }
 
 /* y (+)= H x on the walk engine: max|x| (and the converted copy of x), the
