@@ -152,7 +152,7 @@ def emu4(d, Z, N, x, f32):
 @pytest.mark.parametrize("name", ["he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
 @pytest.mark.parametrize("bits", [64, 32])
 def test_panel_engine_is_exact_model(problem, name, bits):
-    """The panel engine (the default at these sizes) gives bit for bit what its CPU model gives."""
+    """The panel engine (the 32-bit default at these sizes) gives bit for bit what its CPU model gives."""
     d, Z, N, *_ = problem(name)
     H = jn.Hamiltonian.from_dir(d, Z, N)
     H.set_engine(4)
