@@ -670,3 +670,75 @@ void emu_walk_shape(void *h, double *out)
 		out[12] += (double)rs * nw;
 	}
 }
+
+/* Structural checks of the walk plan, every index the walk kernel reads
+ * against its array: returns the number of violations (0 for a sound plan).
+ * Per task: U in {2, 4, 8}, its piece, lane record, walk table, rows,
+ * destination rows and groups inside their arrays; per lane: a walk slot
+ * below the task's walks and multipliers +1 (01) or -1 (11) for its entries
+ * and 0 for padding, padding only after them, an element offset inside the
+ * walk element array from every group base; per row: a slot row below the
+ * piece's; each group ends with a group-end row; JN_WALK_ROW_SPARE zero
+ * words after the last row (the kernel reads two words ahead). */
+int64_t emu_walk_validate(void *h)
+{
+	jn_plan_t *P = h;
+	if (emu_walk_build(h)) return -1;
+	int64_t bad = 0;
+	for (int k = 0; k < JN_WALK_ROW_SPARE; k++) bad += P->wrows[P->n_wrows + k] != 0u;
+	for (int64_t t = 0; t < P->nwtasks; t++) {
+		const jn_wtask_t *T = &P->wtasks[t];
+		if (T->piece >= P->nwpieces) { bad++; continue; }
+		const jn_wpiece_t *pc = &P->wpieces[T->piece];
+		const int U = (int)((T->meta >> 8) & 0xff), nw = (int)(T->meta & 0xff), LW = JN_WALK_LANE_WORDS(U);
+		const int rs = (int)(pc->meta & 0xff), ng = (int)(pc->meta >> 9);
+		if ((U != 8 && U != 4 && U != 2) || nw < 1 || nw > 32 || rs < 1 || rs > JN_WALK_RS || ng < 1 ||
+		    (int64_t)T->lanes + 32 * LW > P->n_wlanes || (int64_t)T->walk0 + nw > P->n_wwalks ||
+		    (int64_t)pc->rdst0 + rs > P->n_wrdst || (int64_t)pc->group0 + ng > P->n_wgroups || pc->row0 < 0) {
+			bad++;
+			continue;
+		}
+		for (int lane = 0; lane < 32; lane++) {
+			const uint32_t head = P->wlanes[T->lanes + lane], ws = head & 0xffffu, mul = head >> 16;
+			if (ws >= (uint32_t)nw) bad++;
+			int seen_pad = 0;
+			for (int u = 0; u < U; u++) {
+				const uint32_t m = (mul >> (2 * u)) & 3u, ko = P->wlanes[T->lanes + (1 + U / 2 + u) * 32 + lane];
+				if (m == 2) bad++;                              /* not a multiplier */
+				if (m == 0) seen_pad = 1;
+				else if (seen_pad) bad++;                       /* an entry after padding */
+				if (m != (ko >> 30)) bad++;                     /* the head and the entry word disagree */
+				for (int g = 0; g < ng; g++)
+					if ((int64_t)P->wgroups[pc->group0 + g] + (ko & 0x3fffffffu) >= P->n_wme) bad++;
+			}
+			if (mul >> (2 * U)) bad++;                              /* bits beyond the lane's entries */
+		}
+		int64_t j = pc->row0;
+		for (int g = 0; g < ng; g++) {
+			for (;;) {
+				if (j >= P->n_wrows) { bad++; break; }
+				const uint32_t row = P->wrows[j++];
+				if ((int)((row >> 16) & 31u) >= rs) bad++;
+				if (row & JN_WALK_GROUP_END) break;
+			}
+		}
+		if (j + 1 > P->n_wrows + JN_WALK_ROW_SPARE) bad++;        /* the kernel's read-ahead stays inside */
+	}
+	return bad;
+}
+
+/* Plants one defect in the CPU model's walk plan (test infrastructure: the
+ * validator's own test): 0 a nonzero spare row word, 1 the invalid
+ * multiplier code 2 in a lane head, 2 a row slot beyond its piece's.
+ * Returns 0, or -1 when the plan has nothing to corrupt. */
+int emu_walk_corrupt(void *h, int kind)
+{
+	jn_plan_t *P = h;
+	if (emu_walk_build(h) || P->nwtasks < 1) return -1;
+	const jn_wtask_t *T = &P->wtasks[0];
+	const jn_wpiece_t *pc = &P->wpieces[T->piece];
+	if (kind == 0) P->wrows[P->n_wrows] = 1u;
+	else if (kind == 1) P->wlanes[T->lanes] = (P->wlanes[T->lanes] & 0xffffu) | (2u << 16);
+	else P->wrows[pc->row0] = (P->wrows[pc->row0] & ~(31u << 16)) | (31u << 16);
+	return 0;
+}

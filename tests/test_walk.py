@@ -17,6 +17,9 @@ def walk_lib():
     L.emu_matvec5.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
     L.emu_walk_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     L.emu_walk_shape.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.emu_walk_validate.argtypes = [ctypes.c_void_p]
+    L.emu_walk_validate.restype = ctypes.c_int64
+    L.emu_walk_corrupt.argtypes = [ctypes.c_void_p, ctypes.c_int]
     return L
 
 
@@ -58,4 +61,32 @@ def test_walk_plan_shape(problem):
     assert real <= padded <= slots            # padding and idle lanes only add
     assert padded <= 1.6 * real               # chunk widths keep the padding small
     assert st[6] >= st[2] > 0                 # walk elements, row groups
+    L.emu_close(h)
+
+
+@pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
+def test_walk_plan_is_sound(problem, name):
+    """Every index the walk kernel reads stays inside its array, the entries'
+    sign multipliers and padding are well formed, every group ends, and the
+    kernel's read-ahead past the last row lands on the plan's zero spare words."""
+    d, Z, N, *_ = problem(name)
+    _, h, err = open_plan(d, Z, N)
+    assert h, err
+    L = walk_lib()
+    assert L.emu_walk_validate(h) == 0
+    L.emu_close(h)
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_walk_plan_validator_finds_planted_defects(problem, kind):
+    """The validator is not vacuous: a nonzero spare row word, an invalid
+    multiplier code and a row slot beyond its piece's, each planted in the CPU
+    model's copy of the plan, are reported."""
+    d, Z, N, *_ = problem("he4_n4_2b")
+    _, h, err = open_plan(d, Z, N)
+    assert h, err
+    L = walk_lib()
+    assert L.emu_walk_validate(h) == 0
+    assert L.emu_walk_corrupt(h, kind) == 0
+    assert L.emu_walk_validate(h) > 0
     L.emu_close(h)
