@@ -338,17 +338,32 @@ void jn_plan_free(jn_plan_t *p)
 	memset(p, 0, sizeof *p);
 }
 
+/* max |M| of every matrix-element block (1 for each when me is NULL) */
+static double *block_max(const jn_plan_t *p, const double *me)
+{
+	double *m = calloc(p->nmes ? p->nmes : 1, sizeof(double));
+	if (!m) return NULL;
+	for (int b = 0; b < p->nmes; b++) {
+		const jn_me_t *M = &p->mes[b];
+		double v = me ? 0.0 : 1.0;
+		if (me)
+			for (int64_t e = 0; e < M->len; e++) v = fmax(v, fabs(me[M->offset + e]));
+		m[b] = v;
+	}
+	return m;
+}
+
 double jn_plan_abs_bound(const jn_plan_t *p, const double *me)
 {
 	const uint32_t *rp = p->rowptr;
 	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
-	for (int t = 0; t < p->nterms; t++) {
-		const jn_me_t *M = &p->mes[p->instr[p->terms[t].instr].me];
-		double m = me ? 0.0 : 1.0;
-		if (me)
-			for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(me[M->offset + e]));
-		tmax[t] = m;
+	double *mmax = block_max(p, me);            /* once per block, not once per term */
+	if (!tmax || !mmax) {
+		free(tmax); free(mmax);
+		return INFINITY;
 	}
+	for (int t = 0; t < p->nterms; t++) tmax[t] = mmax[p->instr[p->terms[t].instr].me];
+	free(mmax);
 	/* terms grouped by destination block */
 	int *cnt = calloc((size_t)p->nblocks + 1, sizeof(int));
 	int *byb = malloc((p->nterms > 0 ? (size_t)p->nterms : 1) * sizeof(int));
@@ -466,12 +481,14 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 {
 	const uint32_t *rp = p->rowptr;
 	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
-	for (int t = 0; t < p->nterms; t++) {
-		const jn_me_t *M = &p->mes[p->instr[p->terms[t].instr].me];
-		double m = 0;
-		for (int64_t e = 0; e < M->len; e++) m = fmax(m, fabs(p->me[M->offset + e]));
-		tmax[t] = m;
+	double *mmax = block_max(p, p->me);         /* once per block, not once per term */
+	if (!tmax || !mmax) {
+		free(tmax); free(mmax);
+		if (err) snprintf(err, errlen, "out of host memory");
+		return 1;
 	}
+	for (int t = 0; t < p->nterms; t++) tmax[t] = mmax[p->instr[p->terms[t].instr].me];
+	free(mmax);
 	int *cnt = calloc(p->nblocks + 1, sizeof(int));
 	for (int t = 0; t < p->nterms; t++) cnt[term_dst[t] + 1]++;
 	for (int b = 0; b < p->nblocks; b++) cnt[b + 1] += cnt[b];
