@@ -18,11 +18,14 @@
 
 #include <ctype.h>
 #include <errno.h>
+#include <fcntl.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <pthread.h>
+#include <unistd.h>
 
 #define ERR(...) do { if (err) snprintf(err, errlen, __VA_ARGS__); goto fail; } while (0)
 
@@ -252,33 +255,129 @@ fail:
 	return NULL;
 }
 
-static double *read_me_file(const char *dir, long id, uint64_t *nd_n, uint64_t *nd_p, int64_t *len, char *err,
-			    size_t errlen)
+/* fn(i, arg) for every i < n, on up to 32 host threads taking items from a
+ * shared counter */
+typedef struct {
+	int64_t n, next;
+	void (*fn)(int64_t, void *);
+	void *arg;
+} par_t;
+
+static void *par_worker(void *v)
+{
+	par_t *p = (par_t *)v;
+	for (;;) {
+		const int64_t i = __atomic_fetch_add(&p->next, 1, __ATOMIC_RELAXED);
+		if (i >= p->n) break;
+		p->fn(i, p->arg);
+	}
+	return NULL;
+}
+
+void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg)
+{
+	long nt = sysconf(_SC_NPROCESSORS_ONLN);
+	if (nt > 32) nt = 32;
+	if (nt < 1 || n < 2) nt = 1;
+	par_t p = { n, 0, fn, arg };
+	pthread_t th[32];
+	int started = 0;
+	for (long t = 1; t < nt; t++)
+		if (pthread_create(&th[started], NULL, par_worker, &p) == 0) started++;
+	par_worker(&p);
+	for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+}
+
+/* The header of one matrix-element file (two uint64 dimensions, the
+ * reference's matrix_block.c:22-62 layout) and its element count, checked
+ * against the file's size. */
+static int me_file_header(const char *dir, long id, uint64_t *nd_n, uint64_t *nd_p, int64_t *len, char *err,
+			  size_t errlen)
 {
 	char path[8192];
 	snprintf(path, sizeof path, "%s/%ld_matrix_elements", dir, id);
 	FILE *f = fopen(path, "rb");
-	double *d = NULL;
 	uint64_t hdr[2];
 	if (!f) ERR("Could not open block file %s. %s", path, strerror(errno));
 	if (fread(hdr, sizeof(uint64_t), 2, f) != 2) ERR("Could not read dimensions from matrix file %ld", id);
 	*nd_n = hdr[0]; *nd_p = hdr[1];
 	uint64_t n = hdr[0] == 0 ? hdr[1] : hdr[1] == 0 ? hdr[0] : hdr[0] * hdr[1];
 	if (hdr[0] && hdr[1] && n / hdr[0] != hdr[1]) ERR("matrix file %ld: dimension overflow", id);
-	fseek(f, 0, SEEK_END);
-	long fsz = ftell(f);
-	if ((uint64_t)fsz < 16 + 8 * n) ERR("Could not read matrix elements form matrix file %ld", id);
-	fseek(f, 16, SEEK_SET);
-	*len = (int64_t)n;
-	d = malloc(n ? n * sizeof(double) : 8);
-	if (!d) ERR("out of host memory reading %s", path);
-	if (fread(d, sizeof(double), n, f) != n) ERR("Could not read matrix elements form matrix file %ld", id);
+	if (n > ((uint64_t)1 << 56)) ERR("matrix file %ld: dimension overflow", id);
+	if (fseeko(f, 0, SEEK_END) != 0) ERR("Could not read matrix elements form matrix file %ld", id);
+	off_t fsz = ftello(f);
+	if (fsz < 0 || (uint64_t)fsz < 16 + 8 * n) ERR("Could not read matrix elements form matrix file %ld", id);
 	fclose(f);
-	return d;
+	*len = (int64_t)n;
+	return 0;
 fail:
 	if (f) fclose(f);
-	free(d);
-	return NULL;
+	return 1;
+}
+
+/* Every block's elements, read by all host cores straight into out + offset:
+ * work items are pieces of at most ME_READ_CHUNK elements of one file. */
+#define ME_READ_CHUNK ((int64_t)1 << 22)
+
+typedef struct { int b; int64_t e0, e1; } me_piece_t;
+
+typedef struct {
+	const jn_plan_t *p;
+	const char *dir;
+	double *out;
+	const me_piece_t *pc;
+	uint8_t *bad;
+} me_read_t;
+
+static void me_read_piece(int64_t i, void *v)
+{
+	me_read_t *r = (me_read_t *)v;
+	const me_piece_t *pc = &r->pc[i];
+	const jn_me_t *M = &r->p->mes[pc->b];
+	char path[8192];
+	snprintf(path, sizeof path, "%s/%d_matrix_elements", r->dir, M->id);
+	int fd = open(path, O_RDONLY);
+	if (fd < 0) { r->bad[i] = 1; return; }
+	char *dst = (char *)(r->out + M->offset + pc->e0);
+	size_t want = (size_t)(pc->e1 - pc->e0) * sizeof(double);
+	off_t at = 16 + (off_t)pc->e0 * (off_t)sizeof(double);
+	while (want > 0) {
+		ssize_t got = pread(fd, dst, want, at);
+		if (got < 0 && errno == EINTR) continue;
+		if (got <= 0) { r->bad[i] = 1; break; }
+		dst += got; at += got; want -= (size_t)got;
+	}
+	close(fd);
+}
+
+static int me_read_all(const jn_plan_t *p, const char *dir, double *out, char *err, size_t errlen)
+{
+	int64_t n = 0;
+	for (int b = 0; b < p->nmes; b++) n += (p->mes[b].len + ME_READ_CHUNK - 1) / ME_READ_CHUNK;
+	me_piece_t *pc = malloc((n ? n : 1) * sizeof *pc);
+	uint8_t *bad = calloc(n ? n : 1, 1);
+	if (!pc || !bad) {
+		free(pc); free(bad);
+		if (err) snprintf(err, errlen, "out of host memory reading %s", dir);
+		return 1;
+	}
+	n = 0;
+	for (int b = 0; b < p->nmes; b++)
+		for (int64_t e = 0; e < p->mes[b].len; e += ME_READ_CHUNK) {
+			pc[n].b = b; pc[n].e0 = e;
+			pc[n].e1 = e + ME_READ_CHUNK < p->mes[b].len ? e + ME_READ_CHUNK : p->mes[b].len;
+			n++;
+		}
+	me_read_t r = { p, dir, out, pc, bad };
+	jn_par_for(n, me_read_piece, &r);
+	int rc = 0;
+	for (int64_t i = 0; i < n && !rc; i++)
+		if (bad[i]) {
+			if (err) snprintf(err, errlen, "Could not read matrix elements form matrix file %d", p->mes[pc[i].b].id);
+			rc = 1;
+		}
+	free(pc); free(bad);
+	return rc;
 }
 
 int jn_plan_read_me(const jn_plan_t *p, const char *dir, double *out, char *err, size_t errlen)
@@ -287,19 +386,15 @@ int jn_plan_read_me(const jn_plan_t *p, const char *dir, double *out, char *err,
 		const jn_me_t *M = &p->mes[b];
 		uint64_t nd_n, nd_p;
 		int64_t len;
-		double *d = read_me_file(dir, M->id, &nd_n, &nd_p, &len, err, errlen);
-		if (!d) return 1;
+		if (me_file_header(dir, M->id, &nd_n, &nd_p, &len, err, errlen)) return 1;
 		if (nd_n != M->nd_n || nd_p != M->nd_p || len != M->len) {
-			free(d);
 			if (err) snprintf(err, errlen, "matrix file %d in %s has dimensions (%llu, %llu), the plan (%llu, %llu)", M->id,
 					  dir, (unsigned long long)nd_n, (unsigned long long)nd_p, (unsigned long long)M->nd_n,
 					  (unsigned long long)M->nd_p);
 			return 1;
 		}
-		memcpy(out + M->offset, d, (size_t)len * sizeof(double));
-		free(d);
 	}
-	return 0;
+	return me_read_all(p, dir, out, err, errlen);
 }
 
 static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
@@ -477,6 +572,18 @@ static int cmp_task_cost(const void *a, const void *b)
  * abs_bound, the largest sum of |M| over the contributions to one element,
  * which bounds |y| by abs_bound * max|x| for the fixed-point scale.
  */
+/* the first walk in [lo, hi) whose destination row is at least `row`; a
+ * view's walks are stored in ascending destination-row order */
+static int64_t first_walk_from(const uint32_t *W, int64_t lo, int64_t hi, uint32_t row)
+{
+	while (lo < hi) {
+		const int64_t m = lo + (hi - lo) / 2;
+		if ((W[2 * m + 1] >> 16) < row) lo = m + 1;
+		else hi = m;
+	}
+	return lo;
+}
+
 static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units, char *err, size_t errlen)
 {
 	const uint32_t *rp = p->rowptr;
@@ -559,9 +666,8 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 				/* P-walks with destination rows in [r0, r1) */
 				int64_t pa = T->pw0, pb = T->pw0;
 				if (T->kind != JN_KIND_N) {
-					while (pa < T->pw1 && (W[2 * pa + 1] >> 16) < (uint32_t)r0) pa++;
-					pb = pa;
-					while (pb < T->pw1 && (W[2 * pb + 1] >> 16) < (uint32_t)r1) pb++;
+					pa = first_walk_from(W, T->pw0, T->pw1, (uint32_t)r0);
+					pb = first_walk_from(W, pa, T->pw1, (uint32_t)r1);
 				}
 				const int64_t nR = pb - pa, nC = T->nw1 - T->nw0;
 				int lanes_on_n;
@@ -733,6 +839,90 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	return 0;
 }
 
+/* The matrix elements some product reads (the compulsory traffic): the
+ * entries' matrix indices for single-species instructions, every (k_n, k_p)
+ * pair of the two lists for NP ones.  One work item per matrix block, so no
+ * two threads mark the same bytes. */
+typedef struct {
+	const jn_plan_t *p;
+	const int *iptr, *ilist;        /* instructions of each block */
+	uint8_t *mark;
+	int64_t *count;
+	uint8_t *bad;
+} census_t;
+
+static void census_block(int64_t b, void *v)
+{
+	census_t *cs = (census_t *)v;
+	const jn_plan_t *p = cs->p;
+	const jn_me_t *M = &p->mes[b];
+	uint8_t *mk = cs->mark + M->offset;
+	for (int q = cs->iptr[b]; q < cs->iptr[b + 1]; q++) {
+		const jn_instr_t *x = &p->instr[cs->ilist[q]];
+		if (x->kind != JN_KIND_NP) {
+			const jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
+			for (int64_t e = 0; e < L->len; e++) mk[(uint32_t)L->triples[3 * e + 2] & 0x7fffffffu] = 1;
+			continue;
+		}
+		/* every (k_n, k_p) pair of the two lists is visited: mark the product of the distinct sets */
+		const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+		if (!Ln->len || !Lp->len) continue;     /* no pairs; the indices were not range-checked */
+		int64_t *kn = malloc((Ln->len ? Ln->len : 1) * sizeof(int64_t));
+		int64_t *kp = malloc((Lp->len ? Lp->len : 1) * sizeof(int64_t));
+		uint8_t *seen_n = calloc(M->nd_n + 1, 1), *seen_p = calloc(M->nd_p + 1, 1);
+		if (!kn || !kp || !seen_n || !seen_p) {
+			free(kn); free(kp); free(seen_n); free(seen_p);
+			cs->bad[b] = 1;
+			return;
+		}
+		size_t nn = 0, np_ = 0;
+		for (int64_t e = 0; e < Ln->len; e++) {
+			uint32_t k = (uint32_t)Ln->triples[3 * e + 2] & 0x7fffffffu;
+			if (!seen_n[k]) { seen_n[k] = 1; kn[nn++] = k; }
+		}
+		for (int64_t e = 0; e < Lp->len; e++) {
+			uint32_t k = (uint32_t)Lp->triples[3 * e + 2] & 0x7fffffffu;
+			if (!seen_p[k]) { seen_p[k] = 1; kp[np_++] = k; }
+		}
+		for (size_t a = 0; a < np_; a++)
+			for (size_t c = 0; c < nn; c++) mk[kn[c] + (int64_t)M->nd_n * kp[a]] = 1;
+		free(kn); free(kp); free(seen_n); free(seen_p);
+	}
+	int64_t n = 0;
+	for (int64_t e = 0; e < M->len; e++) n += mk[e];
+	cs->count[b] = n;
+}
+
+static int me_census(jn_plan_t *p)
+{
+	const int nb = p->nmes;
+	uint8_t *mark = calloc(p->n_me ? p->n_me : 1, 1);
+	int *iptr = calloc((size_t)nb + 1, sizeof(int));
+	int *ilist = malloc((p->ninstr ? p->ninstr : 1) * sizeof(int));
+	int64_t *count = calloc(nb ? nb : 1, sizeof(int64_t));
+	uint8_t *bad = calloc(nb ? nb : 1, 1);
+	int rc = 1;
+	if (!mark || !iptr || !ilist || !count || !bad) goto out;
+	for (int i = 0; i < p->ninstr; i++) iptr[p->instr[i].me + 1]++;
+	for (int b = 0; b < nb; b++) iptr[b + 1] += iptr[b];
+	{
+		int *fill = malloc(((size_t)nb + 1) * sizeof(int));
+		if (!fill) goto out;
+		memcpy(fill, iptr, ((size_t)nb + 1) * sizeof(int));
+		for (int i = 0; i < p->ninstr; i++) ilist[fill[p->instr[i].me]++] = i;
+		free(fill);
+	}
+	census_t cs = { p, iptr, ilist, mark, count, bad };
+	jn_par_for(nb, census_block, &cs);
+	rc = 0;
+	for (int b = 0; b < nb; b++) rc |= bad[b];
+	p->me_referenced = 0;
+	for (int b = 0; b < nb; b++) p->me_referenced += count[b];
+out:
+	free(mark); free(iptr); free(ilist); free(count); free(bad);
+	return rc;
+}
+
 int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, const char *lists_dir,
 		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen)
 {
@@ -838,22 +1028,16 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 
 	/* matrix elements */
 	int64_t me_total = 0;
-	double **me_data = calloc(p->nmes, sizeof(double *));
 	for (int i = 0; i < p->nmes; i++) {
 		jn_me_t *M = &p->mes[i];
-		me_data[i] = read_me_file(me_dir, M->id, &M->nd_n, &M->nd_p, &M->len, err, errlen);
-		if (!me_data[i]) { for (int q = 0; q < i; q++) free(me_data[q]); free(me_data); goto fail; }
+		if (me_file_header(me_dir, M->id, &M->nd_n, &M->nd_p, &M->len, err, errlen)) goto fail;
 		M->offset = me_total;
 		me_total += M->len;
 	}
 	p->n_me = me_total;
 	p->me = malloc((me_total ? me_total : 1) * sizeof(double));
 	if (!p->me) ERR("out of host memory for matrix elements");
-	for (int i = 0; i < p->nmes; i++) {
-		memcpy(p->me + p->mes[i].offset, me_data[i], (size_t)p->mes[i].len * sizeof(double));
-		free(me_data[i]);
-	}
-	free(me_data);
+	if (me_read_all(p, me_dir, p->me, err, errlen)) goto fail;
 	p->me_elements = me_total;
 
 	/* validation and list dimensions */
@@ -907,41 +1091,7 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	}
 
 	/* matrix elements some product actually reads: the compulsory traffic */
-	{
-		uint8_t *mark = calloc(p->n_me ? p->n_me : 1, 1);
-		int64_t *kn = NULL, *kp = NULL;
-		size_t capn = 0, capp = 0;
-		if (!mark) ERR("out of host memory");
-		for (int i = 0; i < p->ninstr; i++) {
-			jn_instr_t *x = &p->instr[i];
-			jn_me_t *M = &p->mes[x->me];
-			uint8_t *mk = mark + M->offset;
-			if (x->kind != JN_KIND_NP) {
-				jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
-				for (int64_t e = 0; e < L->len; e++) mk[(uint32_t)L->triples[3 * e + 2] & 0x7fffffffu] = 1;
-				continue;
-			}
-			/* every (k_n, k_p) pair of the two lists is visited: mark the product of the distinct sets */
-			jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
-			size_t nn = 0, np_ = 0;
-			if ((size_t)Ln->len > capn) { capn = Ln->len; kn = realloc(kn, capn * sizeof(int64_t)); }
-			if ((size_t)Lp->len > capp) { capp = Lp->len; kp = realloc(kp, capp * sizeof(int64_t)); }
-			uint8_t *seen_n = calloc(M->nd_n + 1, 1), *seen_p = calloc(M->nd_p + 1, 1);
-			for (int64_t e = 0; e < Ln->len; e++) {
-				uint32_t k = (uint32_t)Ln->triples[3 * e + 2] & 0x7fffffffu;
-				if (!seen_n[k]) { seen_n[k] = 1; kn[nn++] = k; }
-			}
-			for (int64_t e = 0; e < Lp->len; e++) {
-				uint32_t k = (uint32_t)Lp->triples[3 * e + 2] & 0x7fffffffu;
-				if (!seen_p[k]) { seen_p[k] = 1; kp[np_++] = k; }
-			}
-			for (size_t a = 0; a < np_; a++)
-				for (size_t b = 0; b < nn; b++) mk[kn[b] + (int64_t)M->nd_n * kp[a]] = 1;
-			free(seen_n); free(seen_p);
-		}
-		for (int64_t e = 0; e < p->n_me; e++) p->me_referenced += mark[e];
-		free(mark); free(kn); free(kp);
-	}
+	if (me_census(p)) ERR("out of host memory");
 
 	/* CSR views */
 	int64_t nrp = 0, nent = 0;

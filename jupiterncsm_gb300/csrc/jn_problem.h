@@ -328,6 +328,9 @@ typedef struct {
 } jn_runfile_t;
 
 int jn_read_runfile(const char *path, jn_runfile_t *rf, char *err, size_t errlen);
+/* fn(i, arg) for every i < n on all host cores (at most 32 threads); items
+ * are taken from a shared counter, so fn must not depend on their order */
+void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg);
 int jn_plan_build(jn_plan_t *plan, const char *comb, const char *order, const char *lists_dir,
 		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen);
 void jn_plan_free(jn_plan_t *plan);

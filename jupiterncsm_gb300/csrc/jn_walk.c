@@ -49,38 +49,6 @@ void jn_walk_free(jn_plan_t *p)
 
 typedef struct { int b, kind; int64_t e0, e1; } witem_t;     /* kind 0: elements [e0, e1); 1: transposed rows [e0, e1) */
 
-typedef struct {
-	int64_t n, next;
-	void (*fn)(int64_t, void *);
-	void *arg;
-} par_t;
-
-static void *par_worker(void *v)
-{
-	par_t *p = (par_t *)v;
-	for (;;) {
-		const int64_t i = __atomic_fetch_add(&p->next, 1, __ATOMIC_RELAXED);
-		if (i >= p->n) break;
-		p->fn(i, p->arg);
-	}
-	return NULL;
-}
-
-/* fn(i, arg) for every i < n, on up to 32 threads */
-static void par_for(int64_t n, void (*fn)(int64_t, void *), void *arg)
-{
-	long nt = sysconf(_SC_NPROCESSORS_ONLN);
-	if (nt > 32) nt = 32;
-	if (nt < 1 || n < 2) nt = 1;
-	par_t p = { n, 0, fn, arg };
-	pthread_t th[32];
-	int started = 0;
-	for (long t = 1; t < nt; t++)
-		if (pthread_create(&th[started], NULL, par_worker, &p) == 0) started++;
-	par_worker(&p);
-	for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
-}
-
 /* the work items of every block: its elements and, where proton walks read it, its transposed copy */
 static witem_t *walk_items(const jn_plan_t *p, int64_t *count)
 {
@@ -145,7 +113,7 @@ void jn_walk_elements(const jn_plan_t *p, const double *me, double *out)
 		return;
 	}
 	elem_job_t j = { p, it, me, out };
-	par_for(n, elem_item, &j);
+	jn_par_for(n, elem_item, &j);
 	free(it);
 }
 
@@ -204,7 +172,7 @@ void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, u
 	double *imax = malloc((size_t)(n ? n : 1) * sizeof(double));
 	int_job_t j = { p, it, a, imax, sc, split };
 	if (it && imax) {
-		par_for(n, int_max_item, &j);
+		jn_par_for(n, int_max_item, &j);
 		for (int64_t i = 0; i < n; i++) bmax[it[i].b] = fmax(bmax[it[i].b], imax[i]);
 	} else {
 		for (int b = 0; b < p->nmes; b++)
@@ -222,7 +190,7 @@ void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, u
 	for (int b = 0; b < p->nmes; b++)
 		if (sc[b] == (1 << 30)) sc[b] = lo;     /* an all-zero block */
 	if (it && imax) {
-		par_for(n, int_split_item, &j);
+		jn_par_for(n, int_split_item, &j);
 	} else {
 		for (int b = 0; b < p->nmes; b++) {
 			witem_t one[2] = { { b, 0, 0, p->mes[b].len }, { b, 1, 0, (int64_t)p->mes[b].nd_p } };

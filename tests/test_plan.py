@@ -106,6 +106,15 @@ def test_rejects_short_matrix_file(problem, tmp_path):
     assert not h and "matrix" in err
 
 
+def test_missing_matrix_file_reports_path(problem, tmp_path):
+    d, Z, N, *_ = problem("he4_n2_2b")
+    c = corrupt_copy(d, str(tmp_path / "c"))
+    name = sorted(os.listdir(f"{c}/matrix_elements"))[-1]
+    os.remove(f"{c}/matrix_elements/{name}")
+    L, h, err = open_plan(c, Z, N)
+    assert not h and "Could not open block file" in err and name in err
+
+
 def test_missing_file_reports_path(problem, tmp_path):
     d, Z, N, *_ = problem("he4_n2_2b")
     c = corrupt_copy(d, str(tmp_path / "c"))
