@@ -199,8 +199,10 @@ typedef struct {
  * is gathered once per lane entry.  A single-species instruction walks its
  * list, and its rows are the spectators (identity, sign +, one group).  A
  * piece is a run of rows with at most JN_WALK_RS distinct destination rows;
- * a warp task is one piece times 32 lane chunks.  For every row a lane sums
- * its chunk's contributions in registers and adds the sum into its own
+ * a warp task is one piece times 32 lane chunks.  The lane records of a
+ * walk view depend only on its list, the view and U: every directed
+ * instruction that walks the same view points at one copy.  For every row
+ * a lane sums its chunk's contributions in registers and adds the sum into its own
  * shared-memory slot (destination row, lane); at the end of the task the
  * warp sums each walk's lanes and adds one value per (destination row, walk)
  * into the global accumulator.

@@ -250,6 +250,16 @@ static int64_t chunks_for(const uint32_t *walks, int64_t w0, int64_t nw, int U)
 	return n;
 }
 
+/* the lane records of one walk view: they depend on the list, its view and
+ * the chunk width only, so every instruction direction that walks the same
+ * view shares them */
+typedef struct {
+	int64_t lanes0;         /* first lane word; -1 while not built */
+	int64_t nsets, nchunk;
+	int U;
+	uint32_t *set_walk0;    /* per set of 32 chunks: first walk-table entry, walk count */
+} wview_t;
+
 int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 {
 	vec_t tasks = { 0, 0, 0, sizeof(jn_wtask_t) }, pieces = { 0, 0, 0, sizeof(jn_wpiece_t) };
@@ -264,9 +274,11 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	int32_t stamp_clock = 0;
 	int *order = NULL;
 	double visits = 0.0, slots = 0.0;
+	wview_t *views = calloc((size_t)(p->nlists ? p->nlists : 1) * 2, sizeof(wview_t));
 	jn_walk_free(p);
 	p->wtpos = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int64_t));
-	if (!stamp || !p->wtpos) ERR("out of host memory");
+	if (!stamp || !p->wtpos || !views) ERR("out of host memory");
+	for (int v = 0; v < 2 * p->nlists; v++) views[v].lanes0 = -1;
 	if (p->dim >= 0x7fffffffll) ERR("dimension %lld: too large for the walk engine's 32-bit offsets", (long long)p->dim);
 	/* transposed copies of the n x p blocks that proton-walk instructions use */
 	for (int b = 0; b < p->nmes; b++) p->wtpos[b] = -1;
@@ -356,88 +368,100 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 					if ((p->ent[2 * e] & 0xffffu) >= src_cols || (p->ent[2 * e + 1] & MASK31) >= wlen)
 						ERR("instruction %d: walk entry out of range", q);
 			}
-			/* the chunk width with the fewest lane slots, counting a row's fixed
-			   cost as about two entries */
-			int U = 8;
-			{
-				double best = 1e300;
-				for (int u = 8; u >= 2; u /= 2) {
-					const int64_t nc = chunks_for(p->walks, w0, nw, u);
-					const double cost = (double)((nc + 31) / 32) * 32 * (u + 2);
-					if (cost < best) { best = cost; U = u; }
-				}
-			}
-			const int LW = JN_WALK_LANE_WORDS(U);
-			const int64_t nchunk = chunks_for(p->walks, w0, nw, U);
-			if (3 * nchunk > ccap) {
-				ccap = 3 * nchunk;
-				uint32_t *g = realloc(chunk, (size_t)ccap * sizeof(uint32_t));
-				if (!g) ERR("out of host memory");
-				chunk = g;
-			}
-			{
-				int64_t c = 0;
-				for (int64_t w = 0; w < nw; w++) {
-					const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
-					for (uint32_t o = 0; o < len; o += (uint32_t)U) {
-						chunk[3 * c] = a + o;
-						chunk[3 * c + 1] = len - o < (uint32_t)U ? len - o : (uint32_t)U;
-						chunk[3 * c + 2] = (uint32_t)w;
-						c++;
+			wview_t *V = &views[2 * (int64_t)(W - p->lists) + dir];
+			if (V->lanes0 < 0) {
+				/* the chunk width with the fewest lane slots, counting a row's fixed
+				   cost as about two entries */
+				int U = 8;
+				{
+					double best = 1e300;
+					for (int u = 8; u >= 2; u /= 2) {
+						const int64_t nc = chunks_for(p->walks, w0, nw, u);
+						const double cost = (double)((nc + 31) / 32) * 32 * (u + 2);
+						if (cost < best) { best = cost; U = u; }
 					}
 				}
-			}
-			/* lane records and walk tables: one per 32 chunks, shared by the pieces */
-			const int64_t nsets = (nchunk + 31) / 32;
-			const int64_t lanes0 = lanes.n;
-			if (vec_reserve(&lanes, nsets * 32 * LW) || vec_reserve(&walks, nsets * 32)) ERR("out of host memory");
-			uint32_t *set_walk0 = malloc((size_t)(nsets ? nsets : 1) * 2 * sizeof(uint32_t));
-			if (!set_walk0) ERR("out of host memory");
-			for (int64_t s = 0; s < nsets; s++) {
-				uint32_t *L = (uint32_t *)lanes.a + lanes.n;
-				uint32_t *T = (uint32_t *)walks.a + walks.n;
-				int nwalk = 0;
-				for (int l = 0; l < 32;) {
-					/* the run of this set's lanes [l, l1) that hold chunks of one walk: its
-					   entries (contiguous in the walk view) are dealt to the run's lanes in
-					   turn, entry i to lane l + i mod nl at position i / nl */
-					int l1 = l + 1;
-					const int64_t c0 = s * 32 + l;
-					if (c0 < nchunk)
-						while (l1 < 32 && s * 32 + l1 < nchunk && chunk[3 * (s * 32 + l1) + 2] == chunk[3 * c0 + 2]) l1++;
-					else
-						l1 = 32;
-					const int nl = l1 - l;
-					uint32_t e0 = 0, ne = 0;
-					if (c0 < nchunk) {
-						T[nwalk++] = p->walks[2 * (w0 + chunk[3 * c0 + 2]) + 1] >> 16;
-						e0 = chunk[3 * c0];
-						for (int64_t c = c0; c < s * 32 + l1; c++) ne += chunk[3 * c + 1];
-					}
-					for (int r = 0; r < nl; r++) {
-						uint32_t src[8], koff[8];
-						for (int u = 0; u < U; u++) {
-							const uint32_t i = (uint32_t)(u * nl + r);
-							/* padding repeats the lane's first source with coefficient 0 */
-							const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
-							src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
-							koff[u] = i < ne ? (p->ent[2 * e + 1] & 0x3fffffffu) |
-										   ((p->ent[2 * e + 1] >> 31) ? JN_WALK_NEG : JN_WALK_POS)
-									 : 0u;
+				const int LW = JN_WALK_LANE_WORDS(U);
+				const int64_t nchunk = chunks_for(p->walks, w0, nw, U);
+				if (3 * nchunk > ccap) {
+					ccap = 3 * nchunk;
+					uint32_t *g = realloc(chunk, (size_t)ccap * sizeof(uint32_t));
+					if (!g) ERR("out of host memory");
+					chunk = g;
+				}
+				{
+					int64_t c = 0;
+					for (int64_t w = 0; w < nw; w++) {
+						const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
+						for (uint32_t o = 0; o < len; o += (uint32_t)U) {
+							chunk[3 * c] = a + o;
+							chunk[3 * c + 1] = len - o < (uint32_t)U ? len - o : (uint32_t)U;
+							chunk[3 * c + 2] = (uint32_t)w;
+							c++;
 						}
-						uint32_t mul = 0;
-						for (int u = 0; u < U; u++) mul |= (koff[u] >> 30) << (2 * u);
-						L[l + r] = (c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u) | (mul << 16);
-						for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
-						for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
 					}
-					l = l1;
 				}
-				set_walk0[2 * s] = (uint32_t)walks.n;
-				set_walk0[2 * s + 1] = (uint32_t)nwalk;
-				lanes.n += 32 * LW;
-				walks.n += nwalk;
+				/* lane records and walk tables: one per 32 chunks, shared by the pieces
+				   of every directed instruction that walks this view */
+				const int64_t nsets = (nchunk + 31) / 32;
+				const int64_t lanes0 = lanes.n;
+				if (vec_reserve(&lanes, nsets * 32 * LW) || vec_reserve(&walks, nsets * 32)) ERR("out of host memory");
+				uint32_t *set_walk0 = malloc((size_t)(nsets ? nsets : 1) * 2 * sizeof(uint32_t));
+				if (!set_walk0) ERR("out of host memory");
+				V->set_walk0 = set_walk0;
+				for (int64_t s = 0; s < nsets; s++) {
+					uint32_t *L = (uint32_t *)lanes.a + lanes.n;
+					uint32_t *T = (uint32_t *)walks.a + walks.n;
+					int nwalk = 0;
+					for (int l = 0; l < 32;) {
+						/* the run of this set's lanes [l, l1) that hold chunks of one walk: its
+						   entries (contiguous in the walk view) are dealt to the run's lanes in
+						   turn, entry i to lane l + i mod nl at position i / nl */
+						int l1 = l + 1;
+						const int64_t c0 = s * 32 + l;
+						if (c0 < nchunk)
+							while (l1 < 32 && s * 32 + l1 < nchunk && chunk[3 * (s * 32 + l1) + 2] == chunk[3 * c0 + 2]) l1++;
+						else
+							l1 = 32;
+						const int nl = l1 - l;
+						uint32_t e0 = 0, ne = 0;
+						if (c0 < nchunk) {
+							T[nwalk++] = p->walks[2 * (w0 + chunk[3 * c0 + 2]) + 1] >> 16;
+							e0 = chunk[3 * c0];
+							for (int64_t c = c0; c < s * 32 + l1; c++) ne += chunk[3 * c + 1];
+						}
+						for (int r = 0; r < nl; r++) {
+							uint32_t src[8], koff[8];
+							for (int u = 0; u < U; u++) {
+								const uint32_t i = (uint32_t)(u * nl + r);
+								/* padding repeats the lane's first source with coefficient 0 */
+								const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
+								src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
+								koff[u] = i < ne ? (p->ent[2 * e + 1] & 0x3fffffffu) |
+											   ((p->ent[2 * e + 1] >> 31) ? JN_WALK_NEG : JN_WALK_POS)
+										 : 0u;
+							}
+							uint32_t mul = 0;
+							for (int u = 0; u < U; u++) mul |= (koff[u] >> 30) << (2 * u);
+							L[l + r] = (c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u) | (mul << 16);
+							for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
+							for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
+						}
+						l = l1;
+					}
+					set_walk0[2 * s] = (uint32_t)walks.n;
+					set_walk0[2 * s + 1] = (uint32_t)nwalk;
+					lanes.n += 32 * LW;
+					walks.n += nwalk;
+				}
+				V->U = U;
+				V->nsets = nsets;
+				V->nchunk = nchunk;
+				V->lanes0 = lanes0;
 			}
+			const int U = V->U, LW = JN_WALK_LANE_WORDS(U);
+			const int64_t nsets = V->nsets, nchunk = V->nchunk, lanes0 = V->lanes0;
+			const uint32_t *set_walk0 = V->set_walk0;
 			/* pieces: runs of whole row groups with at most RS distinct destination rows
 			   (a group with more is split, and its element row read once per part) */
 			int64_t r0 = 0;
@@ -448,10 +472,8 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				int64_t r1 = r0;
 				const int64_t rdst0 = rdst.n, row0 = rows.n, group0 = groups.n;
 				if (vec_reserve(&rdst, JN_WALK_RS) || vec_reserve(&rows, nr - r0) || vec_reserve(&groups, nr - r0) ||
-				    vec_reserve(&gblock, nr - r0)) {
-					free(set_walk0);
+				    vec_reserve(&gblock, nr - r0))
 					ERR("out of host memory");
-				}
 				while (r1 < nr) {
 					/* the next group [r1, g1) and the destinations it would add */
 					int64_t g1 = r1;
@@ -485,7 +507,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				}
 				rows.n += r1 - r0;
 				rdst.n += rs;
-				if (vec_reserve(&pieces, 1) || vec_reserve(&tasks, nsets)) { free(set_walk0); ERR("out of host memory"); }
+				if (vec_reserve(&pieces, 1) || vec_reserve(&tasks, nsets)) ERR("out of host memory");
 				const int64_t pi = pieces.n++;
 				jn_wpiece_t *P = (jn_wpiece_t *)pieces.a + pi;
 				P->src_off = (int32_t)bs->offset;
@@ -496,7 +518,7 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				P->row0 = (int32_t)row0;
 				P->rdst0 = (int32_t)rdst0;
 				P->group0 = (int32_t)group0;
-				if (groups.n - group0 >= (1 << 23)) { free(set_walk0); ERR("instruction %d: too many row groups", q); }
+				if (groups.n - group0 >= (1 << 23)) ERR("instruction %d: too many row groups", q);
 				P->meta = (uint32_t)rs | ((uint32_t)wp << 8) | ((uint32_t)(groups.n - group0) << 9);
 				for (int64_t s = 0; s < nsets; s++) {
 					jn_wtask_t *T = (jn_wtask_t *)tasks.a + tasks.n++;
@@ -510,7 +532,6 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 				}
 				r0 = r1;
 			}
-			free(set_walk0);
 		}
 	}
 	/* tasks stay in this order: warps take the next one from a counter, so
@@ -543,11 +564,16 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	p->wvisits = visits;
 	p->wlane_slots = slots;
 	free(R); free(chunk); free(stamp); free(order);
+	for (int v = 0; v < 2 * p->nlists; v++) free(views[v].set_walk0);
+	free(views);
 	return 0;
 fail:
 	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
 	free(gblock.a);
 	free(R); free(chunk); free(stamp); free(order);
+	if (views)
+		for (int v = 0; v < 2 * p->nlists; v++) free(views[v].set_walk0);
+	free(views);
 	free(p->wtpos); free(p->wxperm);
 	p->wtpos = NULL;
 	p->wxperm = NULL;

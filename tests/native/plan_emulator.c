@@ -506,6 +506,54 @@ void emu_walk_stats(void *h, double *out)
 	out[4] = (double)P->n_wrows; out[5] = P->wlane_slots; out[6] = (double)P->n_wme;
 }
 
+/* Lane-set sharing: out[0] lane words stored, out[1] lane words of the
+ * distinct sets the tasks reference (equal when no set is orphaned and none
+ * overlaps another), out[2] sets referenced by pieces of more than one
+ * matrix-element block (shared across instructions). */
+typedef struct { uint32_t lanes; int32_t block; int lw; } lane_ref_t;
+
+static int cmp_lane_ref(const void *a, const void *b)
+{
+	const lane_ref_t *x = a, *y = b;
+	if (x->lanes != y->lanes) return x->lanes < y->lanes ? -1 : 1;
+	return x->block < y->block ? -1 : x->block > y->block;
+}
+
+void emu_walk_lane_sharing(void *h, double *out)
+{
+	jn_plan_t *P = h;
+	memset(out, 0, 3 * sizeof(double));
+	if (emu_walk_build(h) || P->nwtasks == 0) return;
+	lane_ref_t *r = malloc((size_t)P->nwtasks * sizeof *r);
+	for (int64_t t = 0; t < P->nwtasks; t++) {
+		const jn_wtask_t *T = &P->wtasks[t];
+		r[t].lanes = T->lanes;
+		r[t].block = P->wgblock[P->wpieces[T->piece].group0];
+		r[t].lw = JN_WALK_LANE_WORDS((int)(T->meta >> 8));
+	}
+	qsort(r, (size_t)P->nwtasks, sizeof *r, cmp_lane_ref);
+	double words = 0, shared = 0;
+	int64_t end = 0;           /* first lane word after the sets seen so far */
+	for (int64_t t = 0; t < P->nwtasks;) {
+		int64_t u = t + 1;
+		int multi = 0;
+		while (u < P->nwtasks && r[u].lanes == r[t].lanes) {
+			if (r[u].block != r[t].block) multi = 1;
+			if (r[u].lw != r[t].lw) { words = -1e300; }      /* one set read with two widths */
+			u++;
+		}
+		if (r[t].lanes < end) words = -1e300;                   /* overlapping sets */
+		end = r[t].lanes + 32 * (int64_t)r[t].lw;
+		words += 32.0 * r[t].lw;
+		shared += multi;
+		t = u;
+	}
+	out[0] = (double)P->n_wlanes;
+	out[1] = words;
+	out[2] = shared;
+	free(r);
+}
+
 int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 {
 	jn_plan_t *P = h;

@@ -64,6 +64,24 @@ def test_walk_plan_shape(problem):
     L.emu_close(h)
 
 
+@pytest.mark.parametrize("name", ["he4_n4_2b", "li6_n2_3b"])
+def test_walk_lane_sets_are_shared(problem, name):
+    """A walk view's lane records are stored once: every stored lane word
+    belongs to exactly one set that tasks read, and sets are read by the
+    instructions of several matrix-element blocks."""
+    d, Z, N, *_ = problem(name)
+    _, h, err = open_plan(d, Z, N)
+    assert h, err
+    L = walk_lib()
+    L.emu_walk_lane_sharing.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    out = np.zeros(3)
+    L.emu_walk_lane_sharing(h, out.ctypes.data)
+    stored, referenced, shared = out
+    assert stored > 0 and referenced == stored
+    assert shared > 0
+    L.emu_close(h)
+
+
 @pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
 def test_walk_plan_is_sound(problem, name):
     """Every index the walk kernel reads stays inside its array, the entries'
