@@ -433,18 +433,34 @@ void jn_plan_free(jn_plan_t *p)
 	memset(p, 0, sizeof *p);
 }
 
-/* max |M| of every matrix-element block (1 for each when me is NULL) */
+/* max |M| of every matrix-element block (1 for each when me is NULL), one
+ * block per work item on all host cores.  A comparison skips NaN as fmax
+ * does, without fmax's library call per element. */
+typedef struct { const jn_plan_t *p; const double *me; double *m; } bmax_t;
+
+static void block_max_item(int64_t b, void *v)
+{
+	const bmax_t *j = (const bmax_t *)v;
+	const jn_me_t *M = &j->p->mes[b];
+	const double *a = j->me + M->offset;
+	double m = 0.0;
+	for (int64_t e = 0; e < M->len; e++) {
+		const double x = fabs(a[e]);
+		if (x > m) m = x;
+	}
+	j->m[b] = m;
+}
+
 static double *block_max(const jn_plan_t *p, const double *me)
 {
 	double *m = calloc(p->nmes ? p->nmes : 1, sizeof(double));
 	if (!m) return NULL;
-	for (int b = 0; b < p->nmes; b++) {
-		const jn_me_t *M = &p->mes[b];
-		double v = me ? 0.0 : 1.0;
-		if (me)
-			for (int64_t e = 0; e < M->len; e++) v = fmax(v, fabs(me[M->offset + e]));
-		m[b] = v;
+	if (!me) {
+		for (int b = 0; b < p->nmes; b++) m[b] = 1.0;
+		return m;
 	}
+	bmax_t j = { p, me, m };
+	jn_par_for(p->nmes, block_max_item, &j);
 	return m;
 }
 
@@ -584,9 +600,152 @@ static int64_t first_walk_from(const uint32_t *W, int64_t lo, int64_t hi, uint32
 	return lo;
 }
 
+/* The first pass of the block-tile plan for one destination block: its
+ * |M| bound, its row ranges and their warp tasks with their costs.  Blocks
+ * are independent, so all host cores build them; the caller concatenates
+ * them in block order. */
+typedef struct { int b; int64_t r0, r1; int64_t t0, t1; double cost; } tile_range_t;
+
+typedef struct {
+	tile_range_t *ranges;
+	int nranges;
+	task_cost_t *tasks;
+	int64_t ntasks;
+	double abs_bound;       /* largest bound of the block's elements */
+	int max_el;             /* largest tile of the block, in shared-memory elements */
+	int status;             /* 1: out of host memory; 2: a row wider than a shared-memory tile */
+} blk_tiles_t;
+
+typedef struct {
+	const jn_plan_t *p;
+	const int *cnt, *byb;
+	const double *tmax;
+	blk_tiles_t *out;
+} tiles_job_t;
+
+static void tiles_block(int64_t bi, void *v)
+{
+	const tiles_job_t *J = (const tiles_job_t *)v;
+	const jn_plan_t *p = J->p;
+	const int b = (int)bi;
+	const jn_block_t *B = &p->blocks[b];
+	blk_tiles_t *o = &J->out[b];
+	const uint32_t *rp = p->rowptr;
+	const int *cnt = J->cnt, *byb = J->byb;
+	const double *tmax = J->tmax;
+	if (B->Np == 0 || B->Nn == 0) return;
+	const int64_t stride = B->Nn | 1;
+	if (stride > TILE_SMEM_ELEMS) { o->status = 2; return; }
+	/* |M| bound per element of this block */
+	const size_t E = (size_t)(B->Np * B->Nn);
+	double *bound = calloc(E ? E : 1, sizeof(double));
+	if (!bound) { o->status = 1; return; }
+	for (int q = cnt[b]; q < cnt[b + 1]; q++) {
+		const jn_term_t *T = &p->terms[byb[q]];
+		for (int64_t r = 0; r < B->Np; r++) {
+			double np = T->kind == JN_KIND_N ? 1.0 : (double)(rp[T->p_ptr + r + 1] - rp[T->p_ptr + r]);
+			if (np == 0) continue;
+			for (int64_t c = 0; c < B->Nn; c++) {
+				double nn = T->kind == JN_KIND_P ? 1.0 : (double)(rp[T->n_ptr + c + 1] - rp[T->n_ptr + c]);
+				bound[r * B->Nn + c] += np * nn * tmax[byb[q]];
+			}
+		}
+	}
+	for (size_t e = 0; e < E; e++) o->abs_bound = fmax(o->abs_bound, bound[e]);
+	free(bound);
+	int64_t tcap = 0;
+	int rcap = 0;
+#define PUSH_TASK(TERM, KIND, COUNT, LANE_BASE, LOOP_BASE, LOOP_LEN, COST)                     \
+	do {                                                                                   \
+		if (o->ntasks == tcap) {                                                       \
+			const int64_t nc_ = tcap ? 2 * tcap : 4096;                            \
+			task_cost_t *g_ = realloc(o->tasks, (size_t)nc_ * sizeof *g_);         \
+			if (!g_) { o->status = 1; return; }                                    \
+			o->tasks = g_;                                                         \
+			tcap = nc_;                                                            \
+		}                                                                              \
+		task_cost_t *q_ = &o->tasks[o->ntasks++];                                      \
+		q_->t.head = (uint32_t)(TERM) | ((uint32_t)(KIND) << 24) | ((uint32_t)((COUNT) - 1) << 27); \
+		q_->t.lane_base = (uint32_t)(LANE_BASE); q_->t.loop_base = (uint32_t)(LOOP_BASE); \
+		q_->t.loop_len = (uint32_t)(LOOP_LEN);                                         \
+		q_->cost = TASK_OVERHEAD + (COST);                                             \
+	} while (0)
+	const int64_t R = TILE_SMEM_ELEMS / stride;
+	for (int64_t r0 = 0; r0 < B->Np; r0 += R) {
+		const int64_t r1 = r0 + R < B->Np ? r0 + R : B->Np;
+		if (o->nranges == rcap) {
+			const int nc = rcap ? 2 * rcap : 16;
+			tile_range_t *g = realloc(o->ranges, (size_t)nc * sizeof *g);
+			if (!g) { o->status = 1; return; }
+			o->ranges = g;
+			rcap = nc;
+		}
+		tile_range_t *rg = &o->ranges[o->nranges++];
+		rg->b = b; rg->r0 = r0; rg->r1 = r1; rg->t0 = o->ntasks;
+		for (int q = cnt[b]; q < cnt[b + 1]; q++) {
+			const int ti = byb[q];
+			const jn_term_t *T = &p->terms[ti];
+			const uint32_t *W = p->walks;
+			/* P-walks with destination rows in [r0, r1) */
+			int64_t pa = T->pw0, pb = T->pw0;
+			if (T->kind != JN_KIND_N) {
+				pa = first_walk_from(W, T->pw0, T->pw1, (uint32_t)r0);
+				pb = first_walk_from(W, pa, T->pw1, (uint32_t)r1);
+			}
+			const int64_t nR = pb - pa, nC = T->nw1 - T->nw0;
+			int lanes_on_n;
+			int64_t lane0, nlane, loop0, nloop;
+			int kind;
+			if (T->kind == JN_KIND_NP) {
+				if (!nR || !nC) continue;
+				lanes_on_n = nC >= nR;
+				kind = lanes_on_n ? JN_TASK_NP_A : JN_TASK_NP_B;
+				lane0 = lanes_on_n ? T->nw0 : pa; nlane = lanes_on_n ? nC : nR;
+				loop0 = lanes_on_n ? pa : T->nw0; nloop = lanes_on_n ? nR : nC;
+			} else if (T->kind == JN_KIND_P) {
+				if (!nR) continue;
+				lanes_on_n = B->Nn >= nR;          /* lanes over columns */
+				kind = lanes_on_n ? JN_TASK_P_A : JN_TASK_P_B;
+				lane0 = lanes_on_n ? 0 : pa; nlane = lanes_on_n ? B->Nn : nR;
+				loop0 = lanes_on_n ? pa : 0; nloop = lanes_on_n ? nR : B->Nn;
+			} else {
+				if (!nC) continue;
+				lanes_on_n = nC >= r1 - r0;         /* lanes over N-walks */
+				kind = lanes_on_n ? JN_TASK_N_A : JN_TASK_N_B;
+				lane0 = lanes_on_n ? T->nw0 : r0; nlane = lanes_on_n ? nC : r1 - r0;
+				loop0 = lanes_on_n ? r0 : T->nw0; nloop = lanes_on_n ? r1 - r0 : nC;
+			}
+			/* walk lengths (1 for a dense column or row) of the two sides */
+#define LANE_LEN(i) ((kind == JN_TASK_P_A || kind == JN_TASK_N_B) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
+#define LOOP_LEN(i) ((kind == JN_TASK_P_B || kind == JN_TASK_N_A) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
+			for (int64_t l0 = 0; l0 < nlane; l0 += 32) {
+				const int64_t cntl = nlane - l0 < 32 ? nlane - l0 : 32;
+				double lane_max = 0;
+				for (int64_t i = 0; i < cntl; i++) lane_max = fmax(lane_max, LANE_LEN(lane0 + l0 + i));
+				/* split the loop so that one task stays short */
+				int64_t s0 = 0;
+				double acc = 0;
+				for (int64_t sI = 0; sI < nloop; sI++) {
+					acc += LOOP_LEN(loop0 + sI) * lane_max + 4.0;
+					if (acc >= LANE_VISITS || sI == nloop - 1) {
+						PUSH_TASK(ti, kind, cntl, lane0 + l0, loop0 + s0, sI + 1 - s0, acc);
+						s0 = sI + 1;
+						acc = 0;
+					}
+				}
+			}
+#undef LANE_LEN
+#undef LOOP_LEN
+		}
+		rg->t1 = o->ntasks;
+		const int64_t el = (r1 - r0) * stride;
+		if (el > o->max_el) o->max_el = (int)el;
+	}
+#undef PUSH_TASK
+}
+
 static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units, char *err, size_t errlen)
 {
-	const uint32_t *rp = p->rowptr;
 	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
 	double *mmax = block_max(p, p->me);         /* once per block, not once per term */
 	if (!tmax || !mmax) {
@@ -603,126 +762,63 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	memcpy(fl, cnt, (p->nblocks + 1) * sizeof(int));
 	for (int t = 0; t < p->nterms; t++) byb[fl[term_dst[t]]++] = t;
 	free(fl);
-	/* pass 1: tasks of every (block, row range), with their costs */
-	typedef struct { int b; int64_t r0, r1; int64_t t0, t1; double cost; } range_t;
-	range_t *ranges = NULL;
-	int nranges = 0, rcap = 0;
-	task_cost_t *tasks = NULL;
-	int64_t ntasks = 0, tcap = 0;
+	/* pass 1: tasks of every (block, row range), with their costs, built per
+	   block on all host cores and concatenated in block order; the running
+	   cost total is summed in that order */
+	blk_tiles_t *bt = calloc(p->nblocks ? p->nblocks : 1, sizeof *bt);
+	if (!bt) {
+		free(tmax); free(cnt); free(byb);
+		if (err) snprintf(err, errlen, "out of host memory");
+		return 1;
+	}
+	tiles_job_t job = { p, cnt, byb, tmax, bt };
+	jn_par_for(p->nblocks, tiles_block, &job);
+	int64_t ntasks = 0;
+	int nranges = 0, status = 0, bad_block = -1;
+	for (int b = 0; b < p->nblocks; b++) {
+		if (bt[b].status && !status) { status = bt[b].status; bad_block = b; }
+		ntasks += bt[b].ntasks;
+		nranges += bt[b].nranges;
+	}
+	tile_range_t *ranges = status ? NULL : malloc((nranges ? nranges : 1) * sizeof *ranges);
+	task_cost_t *tasks = status ? NULL : malloc((ntasks ? ntasks : 1) * sizeof *tasks);
+	if (!status && (!ranges || !tasks)) status = 1;
+	if (status) {
+		for (int b = 0; b < p->nblocks; b++) { free(bt[b].tasks); free(bt[b].ranges); }
+		free(bt); free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
+		if (err && status == 2)
+			snprintf(err, errlen, "basis block %d has %lld neutron states: more than one shared-memory tile row",
+				 p->blocks[bad_block].id, (long long)p->blocks[bad_block].Nn);
+		else if (err)
+			snprintf(err, errlen, "out of host memory");
+		return 1;
+	}
 	double total = 0;
 	p->max_tile_elems = 0;
 	p->abs_bound = 0;
-	double *bound = NULL;
-	size_t bcap = 0;
-#define PUSH_TASK(TERM, KIND, COUNT, LANE_BASE, LOOP_BASE, LOOP_LEN, COST)                     \
-	do {                                                                                   \
-		if (ntasks == tcap) { tcap = tcap ? 2 * tcap : 65536; tasks = realloc(tasks, tcap * sizeof *tasks); } \
-		task_cost_t *q_ = &tasks[ntasks++];                                            \
-		q_->t.head = (uint32_t)(TERM) | ((uint32_t)(KIND) << 24) | ((uint32_t)((COUNT) - 1) << 27); \
-		q_->t.lane_base = (uint32_t)(LANE_BASE); q_->t.loop_base = (uint32_t)(LOOP_BASE); \
-		q_->t.loop_len = (uint32_t)(LOOP_LEN);                                         \
-		q_->cost = TASK_OVERHEAD + (COST);                                             \
-		total += q_->cost;                                                             \
-	} while (0)
-	int bad = 0;
-	if (p->nterms >= (1 << 24)) bad = 2;
+	ntasks = 0;
+	nranges = 0;
 	for (int b = 0; b < p->nblocks; b++) {
-		const jn_block_t *B = &p->blocks[b];
-		if (B->Np == 0 || B->Nn == 0) continue;
-		int64_t stride = B->Nn | 1;
-		if (stride > TILE_SMEM_ELEMS) {
-			free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
-			if (err) snprintf(err, errlen, "basis block %d has %lld neutron states: more than one shared-memory tile row",
-					  B->id, (long long)B->Nn);
-			return 1;
-		}
-		/* |M| bound per element of this block */
-		size_t E = (size_t)(B->Np * B->Nn);
-		if (E > bcap) { bcap = E; bound = realloc(bound, bcap * sizeof(double)); }
-		memset(bound, 0, E * sizeof(double));
-		for (int q = cnt[b]; q < cnt[b + 1]; q++) {
-			const jn_term_t *T = &p->terms[byb[q]];
-			for (int64_t r = 0; r < B->Np; r++) {
-				double np = T->kind == JN_KIND_N ? 1.0 : (double)(rp[T->p_ptr + r + 1] - rp[T->p_ptr + r]);
-				if (np == 0) continue;
-				for (int64_t c = 0; c < B->Nn; c++) {
-					double nn = T->kind == JN_KIND_P ? 1.0 : (double)(rp[T->n_ptr + c + 1] - rp[T->n_ptr + c]);
-					bound[r * B->Nn + c] += np * nn * tmax[byb[q]];
-				}
+		p->abs_bound = fmax(p->abs_bound, bt[b].abs_bound);
+		if (bt[b].max_el > p->max_tile_elems) p->max_tile_elems = bt[b].max_el;
+		for (int k = 0; k < bt[b].nranges; k++) {
+			tile_range_t rg = bt[b].ranges[k];
+			const double before = total;
+			const int64_t t0 = ntasks;
+			for (int64_t i = rg.t0; i < rg.t1; i++) {
+				tasks[ntasks] = bt[b].tasks[i];
+				total += tasks[ntasks++].cost;
 			}
+			rg.t0 = t0;
+			rg.t1 = ntasks;
+			rg.cost = total - before;
+			ranges[nranges++] = rg;
 		}
-		for (size_t e = 0; e < E; e++) p->abs_bound = fmax(p->abs_bound, bound[e]);
-		int64_t R = TILE_SMEM_ELEMS / stride;
-		for (int64_t r0 = 0; r0 < B->Np; r0 += R) {
-			int64_t r1 = r0 + R < B->Np ? r0 + R : B->Np;
-			if (nranges == rcap) { rcap = rcap ? 2 * rcap : 256; ranges = realloc(ranges, rcap * sizeof *ranges); }
-			range_t *rg = &ranges[nranges++];
-			rg->b = b; rg->r0 = r0; rg->r1 = r1; rg->t0 = ntasks;
-			double before = total;
-			for (int q = cnt[b]; q < cnt[b + 1]; q++) {
-				const int ti = byb[q];
-				const jn_term_t *T = &p->terms[ti];
-				const uint32_t *W = p->walks;
-				/* P-walks with destination rows in [r0, r1) */
-				int64_t pa = T->pw0, pb = T->pw0;
-				if (T->kind != JN_KIND_N) {
-					pa = first_walk_from(W, T->pw0, T->pw1, (uint32_t)r0);
-					pb = first_walk_from(W, pa, T->pw1, (uint32_t)r1);
-				}
-				const int64_t nR = pb - pa, nC = T->nw1 - T->nw0;
-				int lanes_on_n;
-				int64_t lane0, nlane, loop0, nloop;
-				int kind;
-				if (T->kind == JN_KIND_NP) {
-					if (!nR || !nC) continue;
-					lanes_on_n = nC >= nR;
-					kind = lanes_on_n ? JN_TASK_NP_A : JN_TASK_NP_B;
-					lane0 = lanes_on_n ? T->nw0 : pa; nlane = lanes_on_n ? nC : nR;
-					loop0 = lanes_on_n ? pa : T->nw0; nloop = lanes_on_n ? nR : nC;
-				} else if (T->kind == JN_KIND_P) {
-					if (!nR) continue;
-					lanes_on_n = B->Nn >= nR;          /* lanes over columns */
-					kind = lanes_on_n ? JN_TASK_P_A : JN_TASK_P_B;
-					lane0 = lanes_on_n ? 0 : pa; nlane = lanes_on_n ? B->Nn : nR;
-					loop0 = lanes_on_n ? pa : 0; nloop = lanes_on_n ? nR : B->Nn;
-				} else {
-					if (!nC) continue;
-					lanes_on_n = nC >= r1 - r0;         /* lanes over N-walks */
-					kind = lanes_on_n ? JN_TASK_N_A : JN_TASK_N_B;
-					lane0 = lanes_on_n ? T->nw0 : r0; nlane = lanes_on_n ? nC : r1 - r0;
-					loop0 = lanes_on_n ? r0 : T->nw0; nloop = lanes_on_n ? r1 - r0 : nC;
-				}
-				/* walk lengths (1 for a dense column or row) of the two sides */
-#define LANE_LEN(i) ((kind == JN_TASK_P_A || kind == JN_TASK_N_B) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
-#define LOOP_LEN(i) ((kind == JN_TASK_P_B || kind == JN_TASK_N_A) ? 1.0 : (double)(W[2 * (i) + 1] & 0xffff))
-				for (int64_t l0 = 0; l0 < nlane; l0 += 32) {
-					const int64_t cntl = nlane - l0 < 32 ? nlane - l0 : 32;
-					double lane_max = 0;
-					for (int64_t i = 0; i < cntl; i++) lane_max = fmax(lane_max, LANE_LEN(lane0 + l0 + i));
-					/* split the loop so that one task stays short */
-					int64_t s0 = 0;
-					double acc = 0;
-					for (int64_t sI = 0; sI < nloop; sI++) {
-						acc += LOOP_LEN(loop0 + sI) * lane_max + 4.0;
-						if (acc >= LANE_VISITS || sI == nloop - 1) {
-							PUSH_TASK(ti, kind, cntl, lane0 + l0, loop0 + s0, sI + 1 - s0, acc);
-							s0 = sI + 1;
-							acc = 0;
-						}
-					}
-				}
-#undef LANE_LEN
-#undef LOOP_LEN
-			}
-			rg->t1 = ntasks;
-			rg->cost = total - before;
-			int64_t el = (r1 - r0) * stride;
-			if (el > p->max_tile_elems) p->max_tile_elems = (int)el;
-		}
+		free(bt[b].tasks); free(bt[b].ranges);
 	}
-#undef PUSH_TASK
-	if (bad) {
-		free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
+	free(bt);
+	if (p->nterms >= (1 << 24)) {
+		free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
 		if (err) snprintf(err, errlen, "too many terms for the packed task format");
 		return 1;
 	}
@@ -731,7 +827,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	for (int t = 0; t < p->nterms; t++) {
 		const jn_term_t *T = &p->terms[t];
 		if (T->src_off > 0x7fffffffll) {
-			free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
+			free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
 			if (err) snprintf(err, errlen, "vector too long for 32-bit block offsets");
 			return 1;
 		}
@@ -757,7 +853,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	typedef struct { uint32_t first, width_n; double cost; } item_t;
 	item_t *items = malloc((ntasks ? ntasks : 1) * sizeof(item_t));
 	for (int ri = 0; ri < nranges; ri++) {
-		const range_t *rg = &ranges[ri];
+		const tile_range_t *rg = &ranges[ri];
 		const jn_block_t *B = &p->blocks[rg->b];
 		int nt = (int)ceil(rg->cost / tile_target);
 		if (nt < 1) nt = 1;
@@ -835,7 +931,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		free(ord);
 	}
 	free(tiles); free(tile_cost); free(items);
-	free(tmax); free(cnt); free(byb); free(bound); free(tasks); free(ranges);
+	free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
 	return 0;
 }
 

@@ -127,7 +127,10 @@ static void int_max_item(int64_t i, void *v)
 	double m = 0.0;
 	if (w->kind == 0) {
 		const int64_t o = j->p->mes[w->b].offset;
-		for (int64_t e = w->e0; e < w->e1; e++) m = fmax(m, fabs(j->a[o + e]));
+		for (int64_t e = w->e0; e < w->e1; e++) {
+			const double x = fabs(j->a[o + e]);
+			if (x > m) m = x;           /* skips NaN as fmax does */
+		}
 	}
 	j->imax[i] = m;
 }
