@@ -397,13 +397,14 @@ int jn_plan_read_me(const jn_plan_t *p, const char *dir, double *out, char *err,
 	return me_read_all(p, dir, out, err, errlen);
 }
 
-static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
+static int build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out, uint32_t *rowptr, uint32_t *ent)
 {
 	/* stable counting sort on the destination index; entries (source | destination << 16, matrix_index) */
 	memset(rowptr, 0, (size_t)(nrows + 1) * sizeof(uint32_t));
 	for (int64_t e = 0; e < len; e++) rowptr[(by_out ? tri[3 * e + 1] : tri[3 * e]) + 1]++;
 	for (int32_t r = 0; r < nrows; r++) rowptr[r + 1] += rowptr[r];
 	uint32_t *fill = malloc((size_t)(nrows + 1) * sizeof(uint32_t));
+	if (!fill) return 1;
 	memcpy(fill, rowptr, (size_t)(nrows + 1) * sizeof(uint32_t));
 	for (int64_t e = 0; e < len; e++) {
 		int32_t dst = by_out ? tri[3 * e + 1] : tri[3 * e];
@@ -414,6 +415,26 @@ static void build_csr(const int32_t *tri, int64_t len, int32_t nrows, int by_out
 		ent[2 * at + 1] = (uint32_t)tri[3 * e + 2];
 	}
 	free(fill);
+	return 0;
+}
+
+/* both CSR views of one list, with absolute entry indices; lists write
+ * disjoint parts of rowptr and ent, so all host cores build them */
+typedef struct { jn_plan_t *p; uint8_t *bad; } csr_job_t;
+
+static void csr_list(int64_t l, void *v)
+{
+	const csr_job_t *j = (const csr_job_t *)v;
+	jn_plan_t *p = j->p;
+	jn_list_t *L = &p->lists[l];
+	if (build_csr(L->triples, L->len, L->nout, 1, p->rowptr + L->csr_out_ptr, p->ent + 2 * L->ent_out) ||
+	    build_csr(L->triples, L->len, L->nin, 0, p->rowptr + L->csr_in_ptr, p->ent + 2 * L->ent_in)) {
+		j->bad[l] = 1;
+		return;
+	}
+	/* the CSR row pointers are list-local: make them absolute entry indices */
+	for (int32_t r = 0; r <= L->nout; r++) p->rowptr[L->csr_out_ptr + r] += (uint32_t)L->ent_out;
+	for (int32_t r = 0; r <= L->nin; r++) p->rowptr[L->csr_in_ptr + r] += (uint32_t)L->ent_in;
 }
 
 void jn_plan_free(jn_plan_t *p)
@@ -744,6 +765,112 @@ static void tiles_block(int64_t bi, void *v)
 #undef PUSH_TASK
 }
 
+/* The second pass for one row range: its tiles of similar work and their
+ * warp items.  Every task becomes one piece at its own task index, so
+ * ranges (disjoint task runs) are built on all host cores; tile item ranges
+ * are local to the range until the caller joins them. */
+typedef struct { uint32_t first, width_n; double cost; } tile_item_t;
+
+typedef struct {
+	jn_btile_t *tiles;
+	double *tile_cost;
+	int ntiles;
+	uint32_t *items;        /* pairs {first piece, width | pieces << 8} */
+	int64_t nitems;
+	int status;             /* 1: out of host memory */
+} range_tiles_t;
+
+typedef struct {
+	jn_plan_t *p;
+	const tile_range_t *ranges;
+	task_cost_t *tasks;
+	double tile_target;
+	range_tiles_t *out;
+} pass2_job_t;
+
+static void tiles_range(int64_t ri, void *v)
+{
+	const pass2_job_t *J = (const pass2_job_t *)v;
+	jn_plan_t *p = J->p;
+	const tile_range_t *rg = &J->ranges[ri];
+	const jn_block_t *B = &p->blocks[rg->b];
+	task_cost_t *tasks = J->tasks;
+	range_tiles_t *o = &J->out[ri];
+	const int64_t nall = rg->t1 - rg->t0;
+	tile_item_t *items = malloc((nall ? nall : 1) * sizeof *items);
+	o->items = malloc((nall ? nall : 1) * 2 * sizeof(uint32_t));
+	if (!items || !o->items) { free(items); o->status = 1; return; }
+	int tcap = 0;
+	int nt = (int)ceil(rg->cost / J->tile_target);
+	if (nt < 1) nt = 1;
+	double per = rg->cost / nt, acc = 0;
+	int64_t begin = rg->t0;
+	for (int64_t k = rg->t0; k < rg->t1; k++) {
+		acc += tasks[k].cost;
+		if (!(acc >= per || k == rg->t1 - 1)) continue;
+		if (o->ntiles == tcap) {
+			const int nc = tcap ? 2 * tcap : 8;
+			jn_btile_t *g = realloc(o->tiles, (size_t)nc * sizeof *g);
+			if (g) o->tiles = g;
+			double *gc = realloc(o->tile_cost, (size_t)nc * sizeof *gc);
+			if (gc) o->tile_cost = gc;
+			if (!g || !gc) { free(items); o->status = 1; return; }
+			tcap = nc;
+		}
+		jn_btile_t *Tl = &o->tiles[o->ntiles];
+		Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)rg->r0;
+		Tl->nrows = (int32_t)(rg->r1 - rg->r0); Tl->stride = (int32_t)(B->Nn | 1);
+		/* group by (kind, width), heaviest first inside a group */
+		int64_t n = k + 1 - begin;
+		for (int64_t q = begin; q <= k; q++) {
+			uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
+			uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32;
+			/* sort key: kind, width, then cost */
+			tasks[q].cost += 1e12 * (double)(JN_TASK_KIND(tasks[q].t.head) * 4 + (w >> 3));
+		}
+		qsort(tasks + begin, n, sizeof *tasks, cmp_task_cost);
+		int64_t nitems = 0;
+		double tcost = 0;
+		for (int64_t q = begin; q <= k;) {
+			const uint32_t kind = JN_TASK_KIND(tasks[q].t.head);
+			const uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
+			const uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32, per_item = 32 / w;
+			tile_item_t *it = &items[nitems++];
+			it->first = (uint32_t)q;
+			it->cost = 0;
+			uint32_t m = 0;
+			while (q <= k && m < per_item && JN_TASK_KIND(tasks[q].t.head) == kind &&
+			       (JN_TASK_COUNT(tasks[q].t.head) <= 8 ? 8u : JN_TASK_COUNT(tasks[q].t.head) <= 16 ? 16u : 32u) == w) {
+				double cst = fmod(tasks[q].cost, 1e12);
+				if (cst > it->cost) it->cost = cst;
+				p->pieces[q] = tasks[q].t;
+				q++;
+				m++;
+			}
+			it->width_n = w | (m << 8);
+			tcost += it->cost;
+		}
+		/* heaviest items first for the warps' dynamic fetch */
+		for (int64_t i = 1; i < nitems; i++) {
+			tile_item_t t = items[i];
+			int64_t j = i - 1;
+			while (j >= 0 && items[j].cost < t.cost) { items[j + 1] = items[j]; j--; }
+			items[j + 1] = t;
+		}
+		Tl->pc0 = o->nitems;
+		for (int64_t i = 0; i < nitems; i++) {
+			o->items[2 * o->nitems] = items[i].first;
+			o->items[2 * o->nitems + 1] = items[i].width_n;
+			o->nitems++;
+		}
+		Tl->pc1 = o->nitems;
+		o->tile_cost[o->ntiles++] = tcost;
+		begin = k + 1;
+		acc = 0;
+	}
+	free(items);
+}
+
 static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units, char *err, size_t errlen)
 {
 	double *tmax = calloc(p->nterms ? p->nterms : 1, sizeof(double));
@@ -846,79 +973,45 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	if (tile_target < 64 * 32) tile_target = 64 * 32;
 	p->pieces = malloc((ntasks ? ntasks : 1) * sizeof(jn_piece_t));
 	p->items = malloc((ntasks ? ntasks : 1) * 2 * sizeof(uint32_t));
-	int tmax_tiles = 1024;
-	jn_btile_t *tiles = malloc(tmax_tiles * sizeof(jn_btile_t));
-	double *tile_cost = malloc(tmax_tiles * sizeof(double));
+	range_tiles_t *rt = calloc(nranges ? nranges : 1, sizeof *rt);
 	int ntl = 0;
-	typedef struct { uint32_t first, width_n; double cost; } item_t;
-	item_t *items = malloc((ntasks ? ntasks : 1) * sizeof(item_t));
-	for (int ri = 0; ri < nranges; ri++) {
-		const tile_range_t *rg = &ranges[ri];
-		const jn_block_t *B = &p->blocks[rg->b];
-		int nt = (int)ceil(rg->cost / tile_target);
-		if (nt < 1) nt = 1;
-		double per = rg->cost / nt, acc = 0;
-		int64_t begin = rg->t0;
-		for (int64_t k = rg->t0; k < rg->t1; k++) {
-			acc += tasks[k].cost;
-			if (!(acc >= per || k == rg->t1 - 1)) continue;
-			if (ntl == tmax_tiles) {
-				tmax_tiles *= 2;
-				tiles = realloc(tiles, tmax_tiles * sizeof(jn_btile_t));
-				tile_cost = realloc(tile_cost, tmax_tiles * sizeof(double));
-			}
-			jn_btile_t *Tl = &tiles[ntl];
-			Tl->dst_off = B->offset; Tl->Nn = (int32_t)B->Nn; Tl->row0 = (int32_t)rg->r0;
-			Tl->nrows = (int32_t)(rg->r1 - rg->r0); Tl->stride = (int32_t)(B->Nn | 1);
-			/* group by (kind, width), heaviest first inside a group */
-			int64_t n = k + 1 - begin;
-			for (int64_t q = begin; q <= k; q++) {
-				uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
-				uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32;
-				/* sort key: kind, width, then cost */
-				tasks[q].cost += 1e12 * (double)(JN_TASK_KIND(tasks[q].t.head) * 4 + (w >> 3));
-			}
-			qsort(tasks + begin, n, sizeof *tasks, cmp_task_cost);
-			int64_t nitems = 0;
-			double tcost = 0;
-			for (int64_t q = begin; q <= k;) {
-				const uint32_t kind = JN_TASK_KIND(tasks[q].t.head);
-				const uint32_t c = JN_TASK_COUNT(tasks[q].t.head);
-				const uint32_t w = c <= 8 ? 8 : c <= 16 ? 16 : 32, per_item = 32 / w;
-				item_t *it = &items[nitems++];
-				it->first = (uint32_t)p->npieces;
-				it->cost = 0;
-				uint32_t m = 0;
-				while (q <= k && m < per_item && JN_TASK_KIND(tasks[q].t.head) == kind &&
-				       (JN_TASK_COUNT(tasks[q].t.head) <= 8 ? 8u : JN_TASK_COUNT(tasks[q].t.head) <= 16 ? 16u : 32u) == w) {
-					double cst = fmod(tasks[q].cost, 1e12);
-					if (cst > it->cost) it->cost = cst;
-					p->pieces[p->npieces++] = tasks[q].t;
-					q++;
-					m++;
-				}
-				it->width_n = w | (m << 8);
-				tcost += it->cost;
-			}
-			/* heaviest items first for the warps' dynamic fetch */
-			for (int64_t i = 1; i < nitems; i++) {
-				item_t v = items[i];
-				int64_t j = i - 1;
-				while (j >= 0 && items[j].cost < v.cost) { items[j + 1] = items[j]; j--; }
-				items[j + 1] = v;
-			}
-			Tl->pc0 = p->nitems;
-			for (int64_t i = 0; i < nitems; i++) {
-				p->items[2 * p->nitems] = items[i].first;
-				p->items[2 * p->nitems + 1] = items[i].width_n;
-				p->nitems++;
-			}
-			Tl->pc1 = p->nitems;
-			tile_cost[ntl++] = tcost;
-			begin = k + 1;
-			acc = 0;
+	status = !p->pieces || !p->items || !rt;
+	if (!status) {
+		pass2_job_t job2 = { p, ranges, tasks, tile_target, rt };
+		jn_par_for(nranges, tiles_range, &job2);
+		for (int ri = 0; ri < nranges; ri++) {
+			status |= rt[ri].status;
+			ntl += rt[ri].ntiles;
 		}
 	}
+	jn_btile_t *tiles = status ? NULL : malloc((ntl ? ntl : 1) * sizeof(jn_btile_t));
+	double *tile_cost = status ? NULL : malloc((ntl ? ntl : 1) * sizeof(double));
+	if (!status && (!tiles || !tile_cost)) status = 1;
+	if (status) {
+		if (rt)
+			for (int ri = 0; ri < nranges; ri++) { free(rt[ri].tiles); free(rt[ri].tile_cost); free(rt[ri].items); }
+		free(rt); free(tiles); free(tile_cost);
+		free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
+		if (err) snprintf(err, errlen, "out of host memory");
+		return 1;
+	}
+	/* every task is one piece, in task order; items and tiles are joined in range order */
+	p->npieces = ntasks;
+	p->nitems = 0;
+	ntl = 0;
+	for (int ri = 0; ri < nranges; ri++) {
+		const range_tiles_t *o = &rt[ri];
+		for (int i = 0; i < o->ntiles; i++) {
+			tiles[ntl] = o->tiles[i];
+			tiles[ntl].pc0 += p->nitems;
+			tiles[ntl].pc1 += p->nitems;
+			tile_cost[ntl++] = o->tile_cost[i];
+		}
+		memcpy(p->items + 2 * p->nitems, o->items, (size_t)o->nitems * 2 * sizeof(uint32_t));
+		p->nitems += o->nitems;
+		free(o->tiles); free(o->tile_cost); free(o->items);
+	}
+	free(rt);
 	/* tiles heaviest first: persistent CTAs fetch them in this order */
 	{
 		int *ord = malloc((ntl ? ntl : 1) * sizeof(int));
@@ -930,7 +1023,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		p->nbtiles = ntl;
 		free(ord);
 	}
-	free(tiles); free(tile_cost); free(items);
+	free(tiles); free(tile_cost);
 	free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
 	return 0;
 }
@@ -1204,13 +1297,15 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	p->rowptr = malloc((nrp ? nrp : 1) * sizeof(uint32_t));
 	p->ent = malloc((nent ? nent : 1) * 2 * sizeof(uint32_t));
 	if (!p->rowptr || !p->ent) ERR("out of host memory for list views");
-	for (int l = 0; l < p->nlists; l++) {
-		jn_list_t *L = &p->lists[l];
-		build_csr(L->triples, L->len, L->nout, 1, p->rowptr + L->csr_out_ptr, p->ent + 2 * L->ent_out);
-		build_csr(L->triples, L->len, L->nin, 0, p->rowptr + L->csr_in_ptr, p->ent + 2 * L->ent_in);
-		/* the CSR row pointers are list-local: make them absolute entry indices */
-		for (int32_t r = 0; r <= L->nout; r++) p->rowptr[L->csr_out_ptr + r] += (uint32_t)L->ent_out;
-		for (int32_t r = 0; r <= L->nin; r++) p->rowptr[L->csr_in_ptr + r] += (uint32_t)L->ent_in;
+	{
+		uint8_t *bad = calloc(p->nlists ? p->nlists : 1, 1);
+		if (!bad) ERR("out of host memory for list views");
+		csr_job_t cj = { p, bad };
+		jn_par_for(p->nlists, csr_list, &cj);
+		int any = 0;
+		for (int l = 0; l < p->nlists; l++) any |= bad[l];
+		free(bad);
+		if (any) ERR("out of host memory for list views");
 	}
 	/* walks: the non-empty destination rows of both views of every list */
 	{
