@@ -135,6 +135,13 @@ static void int_max_item(int64_t i, void *v)
 	j->imax[i] = m;
 }
 
+/* a 2^s: a product with the normal double 2^s is exact (|a 2^s| < 2^52
+ * here) or rounds as ldexp does, so it gives ldexp's bits without its call */
+static inline double scaled(double a, int s, double f)
+{
+	return f != 0.0 ? a * f : ldexp(a, s);
+}
+
 /* the 52-bit fixed-point split of a chunk (its elements, or its transposed rows) */
 static void int_split_item(int64_t i, void *v)
 {
@@ -143,6 +150,7 @@ static void int_split_item(int64_t i, void *v)
 	const witem_t *w = &j->it[i];
 	const jn_me_t *M = &p->mes[w->b];
 	const int s = j->sc[w->b];
+	const double f = s >= -1022 && s <= 1023 ? ldexp(1.0, s) : 0.0;    /* 0: ldexp per element */
 	int64_t o, e0, e1;
 	if (w->kind == 0) {
 		o = M->offset;
@@ -153,14 +161,14 @@ static void int_split_item(int64_t i, void *v)
 		const int64_t npp = (int64_t)M->nd_p, nn = (int64_t)M->nd_n;
 		for (int64_t kn = 0; kn < nn; kn++)
 			for (int64_t kp = w->e0; kp < w->e1; kp++) {
-				const int64_t q = o + kp + npp * kn, v = llrint(ldexp(j->a[q], s));
+				const int64_t q = o + kp + npp * kn, v = llrint(scaled(j->a[q], s, f));
 				j->split[2 * q] = (int32_t)(v >> 24);
 				j->split[2 * q + 1] = (int32_t)(v & 0xffffff);
 			}
 		return;
 	}
 	for (int64_t e = e0; e < e1; e++) {
-		const int64_t v = llrint(ldexp(j->a[o + e], s));
+		const int64_t v = llrint(scaled(j->a[o + e], s, f));
 		j->split[2 * (o + e)] = (int32_t)(v >> 24);
 		j->split[2 * (o + e) + 1] = (int32_t)(v & 0xffffff);
 	}
