@@ -95,7 +95,9 @@ def job_gbs(bytes_per_step, world, seconds_per_step):
 
 def profile_traffic(workload, engine, arith):
     """DRAM bytes (read + write) per launch of the product kernel from the committed ncu summary, if any."""
-    name = {4: "jn_panel_kernel", 3: "jn_tile_kernel", 5: "jn_walk_kernel"}[engine]
+    name = {4: "jn_panel_kernel", 3: "jn_tile_kernel", 5: "jn_walk_kernel"}.get(engine)
+    if name is None:
+        return None
     path = os.path.join(ROOT, "profiles", f"{name}_{workload}.md")
     try:
         m = re.search(rf"dram_bytes_per_launch_{arith}:\s*([0-9.eE+]+)", open(path).read())

@@ -157,7 +157,8 @@ jn_status jn_set_precision(jn_ctx *ctx, int precision);
  * index, each row summed in registers over a chunk and rounded once into
  * the lane's shared-memory slot (the walk plan is built on the first
  * product); 3 — shared-memory block tiles with exact 64-bit fixed-point
- * sums; 2 — one warp per 32-element piece, FP64 sums in fixed term order.
+ * sums; 2 — one warp per 32-element piece, FP64 sums in fixed term order
+ * (its plan is built and uploaded here, the first time it is selected).
  * Defaults: engine 5 at precision 64 (its exact-integer arithmetic); at
  * precision 32, engine 4 when the dimension is at most 26 624, else 5.
  * jn_set_engine fixes one engine for both precisions.  Engines 3, 4 and 5
@@ -223,7 +224,9 @@ jn_status jn_synchronize(jn_ctx *ctx);
  * product: every index list once in the reference's 12-byte record format,
  * every matrix element some list pair indexes (8 bytes), x read and y
  * written (16 bytes per basis state).  multiply_adds counts both directions
- * of off-diagonal instructions. */
+ * of off-diagonal instructions.  num_work_units and num_tiles describe
+ * engine 2's plan, which a context builds when jn_set_engine(ctx, 2) first
+ * selects it: jn_get_plan_stats reports 0 for both before that. */
 typedef struct {
 	size_t dimension;
 	int num_blocks;

@@ -560,10 +560,6 @@ extern "C" jn_status jn_open_files(const char *comb, const char *order, const ch
 	    (s = upload(&c->d_ent, p->ent, p->n_ent)) ||
 	    (s = upload(&c->d_me, p->me, p->n_me)) ||
 	    (s = upload(&c->d_terms, p->terms, p->nterms)) ||
-	    (s = upload(&c->d_tiles, p->tiles, p->ntiles)) ||
-	    (s = upload(&c->d_units, p->units, p->nunits)) ||
-	    (s = upload(&c->d_unit_terms, p->unit_terms, p->n_unit_terms)) ||
-	    (s = upload(&c->d_partial, (const void *)NULL, p->n_partial)) ||
 	    (s = upload(&c->d_x, (const void *)NULL, p->dim)) ||
 	    (s = upload(&c->d_y, (const void *)NULL, p->dim)) ||
 	    (s = upload(&c->d_btiles, p->btiles, p->nbtiles)) ||
@@ -766,9 +762,30 @@ static jn_status enqueue(jn_ctx *c, const double *d_x, double *d_y, int accumula
 	return JN_OK;
 }
 
+/* engine 2's plan and device arrays, built when it is first selected */
+static jn_status units_setup(jn_ctx *c)
+{
+	jn_plan_t *p = &c->plan;
+	if (c->d_units) return JN_OK;
+	char err[1024] = { 0 };
+	if (jn_plan_build_units(p, c->num_sms * 48, err, sizeof err)) return fail(JN_ERR_NOMEM, "%s", err);
+	jn_status s;
+	if ((s = upload(&c->d_tiles, p->tiles, p->ntiles)) || (s = upload(&c->d_unit_terms, p->unit_terms, p->n_unit_terms)) ||
+	    (s = upload(&c->d_partial, (const void *)NULL, p->n_partial)) || (s = upload(&c->d_units, p->units, p->nunits))) {
+		cudaFree(c->d_tiles); cudaFree(c->d_unit_terms); cudaFree(c->d_partial); cudaFree(c->d_units);
+		c->d_tiles = NULL; c->d_unit_terms = NULL; c->d_partial = NULL; c->d_units = NULL;
+		return s;
+	}
+	return JN_OK;
+}
+
 extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 {
 	if (!c || engine < 2 || engine > 5) return fail(JN_ERR_INVALID, "engine must be 2, 3, 4 or 5");
+	if (engine == 2) {
+		jn_status s = units_setup(c);
+		if (s) return s;
+	}
 	if (engine == 4) {
 		jn_status s = jn_panels_setup(c);
 		if (s) return s;
@@ -929,6 +946,10 @@ extern "C" jn_status jn_inspect_files(const char *comb, const char *order, const
 	char err[1024] = { 0 };
 	if (jn_plan_build(&plan, comb, order, lists_dir, me_dir, Z, N, 152 * 8, err, sizeof err))
 		return fail(strstr(err, "open") ? JN_ERR_IO : JN_ERR_FORMAT, "%s", err);
+	if (jn_plan_build_units(&plan, 152 * 8, err, sizeof err)) {
+		jn_plan_free(&plan);
+		return fail(JN_ERR_NOMEM, "%s", err);
+	}
 	fill_stats(&plan, st);
 	jn_plan_free(&plan);
 	return JN_OK;

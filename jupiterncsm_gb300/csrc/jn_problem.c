@@ -1028,6 +1028,128 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	return 0;
 }
 
+/* Engine 2's plan: output tiles of 32 columns, their chunks of terms
+ * (work units) and the chunk partial-sum layout, longest units first.  Built
+ * when engine 2 is selected (jn_set_engine), not at open. */
+int jn_plan_build_units(jn_plan_t *p, int target_units, char *err, size_t errlen)
+{
+	if (p->units) return 0;
+	const int *term_dst = p->term_dst;
+	/* terms grouped per destination block, in evaluation order */
+	int *count = calloc(p->nblocks + 1, sizeof(int));
+	for (int t = 0; t < p->nterms; t++) count[term_dst[t] + 1]++;
+	for (int b = 0; b < p->nblocks; b++) count[b + 1] += count[b];
+	int *byblk = malloc((p->nterms ? p->nterms : 1) * sizeof(int));
+	int *fillp = malloc((p->nblocks + 1) * sizeof(int));
+	memcpy(fillp, count, (p->nblocks + 1) * sizeof(int));
+	for (int t = 0; t < p->nterms; t++) byblk[fillp[term_dst[t]]++] = t;
+	free(fillp);
+	/* pass 1: tiles and their costs */
+	int tcap = 1024;
+	p->tiles = malloc(tcap * sizeof(jn_tile_t));
+	double *tile_cost = malloc(tcap * sizeof(double));
+	double total_cost = 0;
+	for (int b = 0; b < p->nblocks; b++) {
+		jn_block_t *B = &p->blocks[b];
+		if (B->Np == 0 || B->Nn == 0) continue;
+		int64_t cw = B->Nn < PIECE_LANES ? B->Nn : PIECE_LANES;
+		int64_t R = B->Nn >= PIECE_LANES ? 1 : PIECE_LANES / B->Nn;
+		for (int64_t r0 = 0; r0 < B->Np; r0 += R)
+			for (int64_t c0 = 0; c0 < B->Nn; c0 += cw) {
+				if (p->ntiles == tcap) {
+					tcap *= 2;
+					p->tiles = realloc(p->tiles, tcap * sizeof(jn_tile_t));
+					tile_cost = realloc(tile_cost, tcap * sizeof(double));
+				}
+				jn_tile_t *T = &p->tiles[p->ntiles];
+				memset(T, 0, sizeof *T);
+				T->dst_off = B->offset;
+				T->Nn = (int32_t)B->Nn;
+				T->row0 = (int32_t)r0; T->nrows = (int32_t)((r0 + R <= B->Np) ? R : B->Np - r0);
+				T->col0 = (int32_t)c0; T->ncols = (int32_t)((c0 + cw <= B->Nn) ? cw : B->Nn - c0);
+				T->pad = b;     /* destination block while planning */
+				double cost = 0;
+				for (int q = count[b]; q < count[b + 1]; q++)
+					cost += term_cost(p, &p->terms[byblk[q]], T->row0, T->row0 + T->nrows, T->col0, T->col0 + T->ncols);
+				tile_cost[p->ntiles++] = cost;
+				total_cost += cost;
+			}
+	}
+	if (target_units <= 0) target_units = 152 * 48;
+	double target = total_cost / target_units;
+	if (target < 256) target = 256;
+	/* pass 2: chunks */
+	int64_t ucap = 4096, tcap2 = 1 << 16;
+	p->units = malloc(ucap * sizeof(jn_unit_t));
+	p->unit_terms = malloc(tcap2 * sizeof(int32_t));
+	int64_t partial = 0;
+	for (int ti = 0; ti < p->ntiles; ti++) {
+		jn_tile_t *T = &p->tiles[ti];
+		int b = T->pad;
+		T->pad = 0;
+		T->unit0 = p->nunits;
+		int nchunk = (int)ceil(tile_cost[ti] / target);
+		if (nchunk < 1) nchunk = 1;
+		double per = tile_cost[ti] / nchunk, acc = 0;
+		int nb_terms = count[b + 1] - count[b];
+		double *cst = malloc((nb_terms ? nb_terms : 1) * sizeof(double));
+		int lastnz = -1;
+		for (int q = 0; q < nb_terms; q++) {
+			cst[q] = term_cost(p, &p->terms[byblk[count[b] + q]], T->row0, T->row0 + T->nrows, T->col0,
+					   T->col0 + T->ncols);
+			if (cst[q] > 0) lastnz = q;
+		}
+		int64_t begin = p->n_unit_terms;
+		int chunks = 0;
+		for (int q = 0; q <= lastnz; q++) {
+			if (cst[q] == 0) continue;
+			if (p->n_unit_terms == tcap2) { tcap2 *= 2; p->unit_terms = realloc(p->unit_terms, tcap2 * sizeof(int32_t)); }
+			p->unit_terms[p->n_unit_terms++] = byblk[count[b] + q];
+			acc += cst[q];
+			if (acc >= per * (chunks + 1) || q == lastnz) {
+				if (p->nunits == ucap) { ucap *= 2; p->units = realloc(p->units, ucap * sizeof(jn_unit_t)); }
+				jn_unit_t *U = &p->units[p->nunits++];
+				U->tile = ti; U->chunk = chunks++;
+				U->t0 = begin; U->t1 = p->n_unit_terms;
+				begin = p->n_unit_terms;
+			}
+		}
+		free(cst);
+		T->nchunks = chunks;
+		T->partial = partial;
+		partial += (int64_t)chunks * T->nrows * T->ncols;
+	}
+	p->n_partial = partial;
+	/* longest units first: the warps that start first take the heaviest work */
+	{
+		double *uc = malloc((p->nunits ? p->nunits : 1) * sizeof(double));
+		int *ord = malloc((p->nunits ? p->nunits : 1) * sizeof(int));
+		for (int u = 0; u < p->nunits; u++) {
+			const jn_unit_t *U = &p->units[u];
+			const jn_tile_t *T = &p->tiles[U->tile];
+			double cst = 0;
+			for (int64_t q = U->t0; q < U->t1; q++)
+				cst += term_cost(p, &p->terms[p->unit_terms[q]], T->row0, T->row0 + T->nrows, T->col0,
+						 T->col0 + T->ncols);
+			uc[u] = cst;
+			ord[u] = u;
+		}
+		g_unit_cost = uc;
+		qsort(ord, p->nunits, sizeof(int), cmp_unit_cost);
+		jn_unit_t *sorted = malloc((p->nunits ? p->nunits : 1) * sizeof(jn_unit_t));
+		for (int u = 0; u < p->nunits; u++) sorted[u] = p->units[ord[u]];
+		free(p->units);
+		p->units = sorted;
+		free(uc); free(ord);
+	}
+	free(tile_cost); free(byblk); free(count);
+	if (!p->units || !p->tiles || !p->unit_terms) {
+		if (err) snprintf(err, errlen, "out of host memory for the work units");
+		return 1;
+	}
+	return 0;
+}
+
 /* The matrix elements some product reads (the compulsory traffic): the
  * entries' matrix indices for single-species instructions, every (k_n, k_p)
  * pair of the two lists for NP ones.  One work item per matrix block, so no
@@ -1391,117 +1513,6 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 		p->visits += (x->bin == x->bout) ? v : 2 * v;
 	}
 
-	/* tiles and units */
-	{
-		/* terms grouped per destination block, in evaluation order */
-		int *count = calloc(p->nblocks + 1, sizeof(int));
-		for (int t = 0; t < p->nterms; t++) count[term_dst[t] + 1]++;
-		for (int b = 0; b < p->nblocks; b++) count[b + 1] += count[b];
-		int *byblk = malloc((p->nterms ? p->nterms : 1) * sizeof(int));
-		int *fillp = malloc((p->nblocks + 1) * sizeof(int));
-		memcpy(fillp, count, (p->nblocks + 1) * sizeof(int));
-		for (int t = 0; t < p->nterms; t++) byblk[fillp[term_dst[t]]++] = t;
-		free(fillp);
-		/* pass 1: tiles and their costs */
-		int tcap = 1024;
-		p->tiles = malloc(tcap * sizeof(jn_tile_t));
-		double *tile_cost = malloc(tcap * sizeof(double));
-		double total_cost = 0;
-		for (int b = 0; b < p->nblocks; b++) {
-			jn_block_t *B = &p->blocks[b];
-			if (B->Np == 0 || B->Nn == 0) continue;
-			int64_t cw = B->Nn < PIECE_LANES ? B->Nn : PIECE_LANES;
-			int64_t R = B->Nn >= PIECE_LANES ? 1 : PIECE_LANES / B->Nn;
-			for (int64_t r0 = 0; r0 < B->Np; r0 += R)
-				for (int64_t c0 = 0; c0 < B->Nn; c0 += cw) {
-					if (p->ntiles == tcap) {
-						tcap *= 2;
-						p->tiles = realloc(p->tiles, tcap * sizeof(jn_tile_t));
-						tile_cost = realloc(tile_cost, tcap * sizeof(double));
-					}
-					jn_tile_t *T = &p->tiles[p->ntiles];
-					memset(T, 0, sizeof *T);
-					T->dst_off = B->offset;
-					T->Nn = (int32_t)B->Nn;
-					T->row0 = (int32_t)r0; T->nrows = (int32_t)((r0 + R <= B->Np) ? R : B->Np - r0);
-					T->col0 = (int32_t)c0; T->ncols = (int32_t)((c0 + cw <= B->Nn) ? cw : B->Nn - c0);
-					T->pad = b;     /* destination block while planning */
-					double cost = 0;
-					for (int q = count[b]; q < count[b + 1]; q++)
-						cost += term_cost(p, &p->terms[byblk[q]], T->row0, T->row0 + T->nrows, T->col0, T->col0 + T->ncols);
-					tile_cost[p->ntiles++] = cost;
-					total_cost += cost;
-				}
-		}
-		if (target_units <= 0) target_units = 152 * 48;
-		double target = total_cost / target_units;
-		if (target < 256) target = 256;
-		/* pass 2: chunks */
-		int64_t ucap = 4096, tcap2 = 1 << 16;
-		p->units = malloc(ucap * sizeof(jn_unit_t));
-		p->unit_terms = malloc(tcap2 * sizeof(int32_t));
-		int64_t partial = 0;
-		for (int ti = 0; ti < p->ntiles; ti++) {
-			jn_tile_t *T = &p->tiles[ti];
-			int b = T->pad;
-			T->pad = 0;
-			T->unit0 = p->nunits;
-			int nchunk = (int)ceil(tile_cost[ti] / target);
-			if (nchunk < 1) nchunk = 1;
-			double per = tile_cost[ti] / nchunk, acc = 0;
-			int nb_terms = count[b + 1] - count[b];
-			double *cst = malloc((nb_terms ? nb_terms : 1) * sizeof(double));
-			int lastnz = -1;
-			for (int q = 0; q < nb_terms; q++) {
-				cst[q] = term_cost(p, &p->terms[byblk[count[b] + q]], T->row0, T->row0 + T->nrows, T->col0,
-						   T->col0 + T->ncols);
-				if (cst[q] > 0) lastnz = q;
-			}
-			int64_t begin = p->n_unit_terms;
-			int chunks = 0;
-			for (int q = 0; q <= lastnz; q++) {
-				if (cst[q] == 0) continue;
-				if (p->n_unit_terms == tcap2) { tcap2 *= 2; p->unit_terms = realloc(p->unit_terms, tcap2 * sizeof(int32_t)); }
-				p->unit_terms[p->n_unit_terms++] = byblk[count[b] + q];
-				acc += cst[q];
-				if (acc >= per * (chunks + 1) || q == lastnz) {
-					if (p->nunits == ucap) { ucap *= 2; p->units = realloc(p->units, ucap * sizeof(jn_unit_t)); }
-					jn_unit_t *U = &p->units[p->nunits++];
-					U->tile = ti; U->chunk = chunks++;
-					U->t0 = begin; U->t1 = p->n_unit_terms;
-					begin = p->n_unit_terms;
-				}
-			}
-			free(cst);
-			T->nchunks = chunks;
-			T->partial = partial;
-			partial += (int64_t)chunks * T->nrows * T->ncols;
-		}
-		p->n_partial = partial;
-		/* longest units first: the warps that start first take the heaviest work */
-		{
-			double *uc = malloc((p->nunits ? p->nunits : 1) * sizeof(double));
-			int *ord = malloc((p->nunits ? p->nunits : 1) * sizeof(int));
-			for (int u = 0; u < p->nunits; u++) {
-				const jn_unit_t *U = &p->units[u];
-				const jn_tile_t *T = &p->tiles[U->tile];
-				double cst = 0;
-				for (int64_t q = U->t0; q < U->t1; q++)
-					cst += term_cost(p, &p->terms[p->unit_terms[q]], T->row0, T->row0 + T->nrows, T->col0,
-							 T->col0 + T->ncols);
-				uc[u] = cst;
-				ord[u] = u;
-			}
-			g_unit_cost = uc;
-			qsort(ord, p->nunits, sizeof(int), cmp_unit_cost);
-			jn_unit_t *sorted = malloc((p->nunits ? p->nunits : 1) * sizeof(jn_unit_t));
-			for (int u = 0; u < p->nunits; u++) sorted[u] = p->units[ord[u]];
-			free(p->units);
-			p->units = sorted;
-			free(uc); free(ord);
-		}
-		free(tile_cost); free(byblk); free(count);
-	}
 	/* block tiles for exact fixed-point accumulation */
 	if (build_block_tiles(p, term_dst, target_units, err, errlen)) goto fail;
 	free(slot_of_id); free(kind_of_id);

@@ -269,6 +269,7 @@ typedef struct {
 	int64_t n_ent;     uint32_t *ent;      /* pairs: src, matrix_index */
 	int64_t n_me;      double *me;
 	int nterms;        jn_term_t *terms;
+	/* engine 2 (jn_plan_build_units; empty until built) */
 	int ntiles;        jn_tile_t *tiles;
 	int nunits;        jn_unit_t *units;
 	int64_t n_unit_terms; int32_t *unit_terms;
@@ -336,6 +337,9 @@ void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg);
 int jn_plan_build(jn_plan_t *plan, const char *comb, const char *order, const char *lists_dir,
 		  const char *me_dir, int Z, int N, int target_units, char *err, size_t errlen);
 void jn_plan_free(jn_plan_t *plan);
+/* engine 2's tiles and work units (about target_units of them); a no-op
+ * when they exist */
+int jn_plan_build_units(jn_plan_t *plan, int target_units, char *err, size_t errlen);
 /* abs_bound of the plan's lists with another set of matrix elements (same
  * layout as plan->me): the fixed-point scale of a product must use it.  With
  * me == NULL every |M| counts as 1: the largest number of contributions to

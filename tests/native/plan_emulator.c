@@ -53,6 +53,7 @@ void *emu_open(const char *comb, const char *order, const char *lists, const cha
 {
 	jn_plan_t *p = calloc(1, sizeof *p);
 	if (jn_plan_build(p, comb, order, lists, mes, Z, N, units, err, (size_t)errlen)) { free(p); return NULL; }
+	if (jn_plan_build_units(p, units, err, (size_t)errlen)) { jn_plan_free(p); free(p); return NULL; }
 	return p;
 }
 
