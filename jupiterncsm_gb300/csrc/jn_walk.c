@@ -261,35 +261,295 @@ static int64_t chunks_for(const uint32_t *walks, int64_t w0, int64_t nw, int U)
 	return n;
 }
 
-/* the lane records of one walk view: they depend on the list, its view and
- * the chunk width only, so every instruction direction that walks the same
- * view shares them */
+/* The lane records of one walk view.  They depend on the list, its view and
+ * the chunk width only, so every directed instruction that walks the same
+ * view shares them.  Views take their place in the lane array and the walk
+ * table in the order of their first use; their records are built by all
+ * host cores. */
 typedef struct {
-	int64_t lanes0;         /* first lane word; -1 while not built */
-	int64_t nsets, nchunk;
-	int U;
-	uint32_t *set_walk0;    /* per set of 32 chunks: first walk-table entry, walk count */
+	const jn_list_t *W;
+	int dir, U;
+	int64_t w0, nw;         /* the view's walks in jn_plan_t.walks */
+	int64_t nchunk, nsets;
+	int64_t lanes0;         /* first lane word */
+	uint32_t *wtab;         /* walk table of the view's sets (view-local) */
+	int64_t nwtab;
+	int64_t walks0;         /* first entry in the plan's walk table */
+	uint32_t *set_walk0;    /* per set: first wtab entry (view-local), walk count */
+	int status;             /* 1: out of host memory */
 } wview_t;
+
+/* One directed instruction (forward, or the transpose of an off-diagonal
+ * one): its rows cut into pieces, with row, slot and group arrays local to
+ * it until they are joined in instruction order. */
+typedef struct {
+	int q, dir, view;
+	uint32_t *rows, *rdst, *groups;
+	int32_t *gblock;
+	int64_t nrows, nrdst, ngroups;
+	jn_wpiece_t *pieces;    /* row0, rdst0, group0 local */
+	int64_t *prows;         /* rows of each piece */
+	int64_t npieces;
+	int status;             /* 1 memory, 2 row index, 3 walk destination, 4 walk entry, 5 row groups */
+} wdir_t;
+
+typedef struct {
+	jn_plan_t *p;
+	wview_t *views;
+	wdir_t *dirs;
+	uint32_t *lanes;
+} wjob_t;
+
+/* the walk list, the row list and element-row addressing of instruction q */
+typedef struct {
+	const jn_list_t *W, *RL;
+	int wp;
+	int64_t base, stride;   /* element row of k_row: base + stride k_row */
+	int64_t wlen, rlen;     /* walk-side and row-side k ranges */
+} wsides_t;
+
+static wsides_t walk_sides(const jn_plan_t *p, int q)
+{
+	const jn_instr_t *x = &p->instr[q];
+	const jn_me_t *M = &p->mes[x->me];
+	wsides_t w = { NULL, NULL, 0, M->offset, 0, M->len, 1 };
+	if (x->kind == JN_KIND_NP) {
+		const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+		w.wp = Lp->len > Ln->len;
+		w.W = w.wp ? Lp : Ln;
+		w.RL = w.wp ? Ln : Lp;
+		w.base = w.wp ? p->wtpos[x->me] : M->offset;
+		w.stride = w.wp ? (int64_t)M->nd_p : (int64_t)M->nd_n;
+		w.wlen = w.wp ? (int64_t)M->nd_p : (int64_t)M->nd_n;
+		w.rlen = w.wp ? (int64_t)M->nd_n : (int64_t)M->nd_p;
+	} else if (x->kind == JN_KIND_N) {
+		w.W = &p->lists[x->ln];
+	} else {
+		w.W = &p->lists[x->lp];
+		w.wp = 1;
+	}
+	return w;
+}
+
+/* lane records and walk table of one view: one set per 32 chunks */
+static void view_lanes(int64_t vi, void *v)
+{
+	const wjob_t *J = (const wjob_t *)v;
+	const jn_plan_t *p = J->p;
+	wview_t *V = &J->views[vi];
+	const int U = V->U, LW = JN_WALK_LANE_WORDS(U);
+	const int64_t w0 = V->w0, nw = V->nw, nchunk = V->nchunk, nsets = V->nsets;
+	uint32_t *chunk = malloc((size_t)(nchunk ? nchunk : 1) * 3 * sizeof(uint32_t));   /* first ent index, count, walk */
+	V->wtab = malloc((size_t)(nsets ? nsets : 1) * 32 * sizeof(uint32_t));
+	V->set_walk0 = malloc((size_t)(nsets ? nsets : 1) * 2 * sizeof(uint32_t));
+	if (!chunk || !V->wtab || !V->set_walk0) { free(chunk); V->status = 1; return; }
+	{
+		int64_t c = 0;
+		for (int64_t w = 0; w < nw; w++) {
+			const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
+			for (uint32_t o = 0; o < len; o += (uint32_t)U) {
+				chunk[3 * c] = a + o;
+				chunk[3 * c + 1] = len - o < (uint32_t)U ? len - o : (uint32_t)U;
+				chunk[3 * c + 2] = (uint32_t)w;
+				c++;
+			}
+		}
+	}
+	for (int64_t s = 0; s < nsets; s++) {
+		uint32_t *L = J->lanes + V->lanes0 + s * 32 * LW;
+		uint32_t *T = V->wtab + V->nwtab;
+		int nwalk = 0;
+		for (int l = 0; l < 32;) {
+			/* the run of this set's lanes [l, l1) that hold chunks of one walk: its
+			   entries (contiguous in the walk view) are dealt to the run's lanes in
+			   turn, entry i to lane l + i mod nl at position i / nl */
+			int l1 = l + 1;
+			const int64_t c0 = s * 32 + l;
+			if (c0 < nchunk)
+				while (l1 < 32 && s * 32 + l1 < nchunk && chunk[3 * (s * 32 + l1) + 2] == chunk[3 * c0 + 2]) l1++;
+			else
+				l1 = 32;
+			const int nl = l1 - l;
+			uint32_t e0 = 0, ne = 0;
+			if (c0 < nchunk) {
+				T[nwalk++] = p->walks[2 * (w0 + chunk[3 * c0 + 2]) + 1] >> 16;
+				e0 = chunk[3 * c0];
+				for (int64_t c = c0; c < s * 32 + l1; c++) ne += chunk[3 * c + 1];
+			}
+			for (int r = 0; r < nl; r++) {
+				uint32_t src[8], koff[8];
+				for (int u = 0; u < U; u++) {
+					const uint32_t i = (uint32_t)(u * nl + r);
+					/* padding repeats the lane's first source with coefficient 0 */
+					const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
+					src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
+					koff[u] = i < ne ? (p->ent[2 * e + 1] & 0x3fffffffu) |
+								   ((p->ent[2 * e + 1] >> 31) ? JN_WALK_NEG : JN_WALK_POS)
+							 : 0u;
+				}
+				uint32_t mul = 0;
+				for (int u = 0; u < U; u++) mul |= (koff[u] >> 30) << (2 * u);
+				L[l + r] = (c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u) | (mul << 16);
+				for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
+				for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
+			}
+			l = l1;
+		}
+		V->set_walk0[2 * s] = (uint32_t)V->nwtab;
+		V->set_walk0[2 * s + 1] = (uint32_t)nwalk;
+		V->nwtab += nwalk;
+	}
+	free(chunk);
+}
+
+/* rows of one directed instruction, checked and cut into pieces: runs of
+   whole row groups with at most JN_WALK_RS distinct destination rows (a
+   group with more is split, and its element row read once per part) */
+static void dir_pieces(int64_t di, void *v)
+{
+	const wjob_t *J = (const wjob_t *)v;
+	const jn_plan_t *p = J->p;
+	wdir_t *D = &J->dirs[di];
+	const int q = D->q, dir = D->dir;
+	const jn_instr_t *x = &p->instr[q];
+	const jn_block_t *bi = &p->blocks[x->bin], *bo = &p->blocks[x->bout];
+	const jn_block_t *bs = dir ? bo : bi, *bd = dir ? bi : bo;
+	const wsides_t S = walk_sides(p, q);
+	const jn_list_t *RL = S.RL;
+	const int wp = S.wp;
+	const int64_t nr = RL ? RL->len : (wp ? bo->Nn : bo->Np);
+	row_t *R = malloc((size_t)(nr ? nr : 1) * sizeof(row_t));
+	D->rows = malloc((size_t)(nr ? nr : 1) * sizeof(uint32_t));
+	D->groups = malloc((size_t)(nr ? nr : 1) * sizeof(uint32_t));
+	D->gblock = malloc((size_t)(nr ? nr : 1) * sizeof(int32_t));
+	D->rdst = malloc((size_t)(nr ? nr : 1) * sizeof(uint32_t));      /* at most one new slot row per row */
+	D->pieces = malloc((size_t)(nr ? nr : 1) * sizeof(jn_wpiece_t));
+	D->prows = malloc((size_t)(nr ? nr : 1) * sizeof(int64_t));
+	if (!R || !D->rows || !D->groups || !D->gblock || !D->rdst || !D->pieces || !D->prows) {
+		free(R);
+		D->status = 1;
+		return;
+	}
+	if (RL) {
+		for (int64_t e = 0; e < nr; e++) {
+			const int32_t *t = RL->triples + 3 * e;
+			R[e].src = (uint32_t)(dir ? t[1] : t[0]);
+			R[e].dst = (uint32_t)(dir ? t[0] : t[1]);
+			R[e].k = (uint32_t)t[2] & MASK31;
+			R[e].sign = (uint32_t)t[2] >> 31;
+		}
+		qsort(R, (size_t)nr, sizeof(row_t), cmp_row);
+	} else {
+		for (int64_t r = 0; r < nr; r++) R[r] = (row_t){ (uint32_t)r, (uint32_t)r, 0u, 0u };
+	}
+	/* row index bounds: sources and destinations inside their blocks, k inside the element block */
+	const int64_t src_rows = wp ? bs->Nn : bs->Np, dst_rows = wp ? bd->Nn : bd->Np;
+	for (int64_t e = 0; e < nr; e++)
+		if (R[e].src >= src_rows || R[e].dst >= dst_rows || R[e].src > 0xffffu || R[e].dst > 0xffffu || R[e].k >= S.rlen) {
+			free(R);
+			D->status = 2;
+			return;
+		}
+	/* walk view and its bounds: destinations and sources inside their blocks, k inside the block */
+	const wview_t *V = &J->views[D->view];
+	const int64_t src_cols = wp ? bs->Np : bs->Nn, dst_cols = wp ? bd->Np : bd->Nn;
+	for (int64_t w = 0; w < V->nw; w++) {
+		const uint32_t a = p->walks[2 * (V->w0 + w)], len = p->walks[2 * (V->w0 + w) + 1] & 0xffffu;
+		if ((p->walks[2 * (V->w0 + w) + 1] >> 16) >= dst_cols) { free(R); D->status = 3; return; }
+		for (uint32_t e = a; e < a + len; e++)
+			if ((p->ent[2 * e] & 0xffffu) >= src_cols || (p->ent[2 * e + 1] & MASK31) >= S.wlen) {
+				free(R);
+				D->status = 4;
+				return;
+			}
+	}
+	int64_t r0 = 0;
+	while (r0 < nr) {
+		int rs = 0;
+		int64_t r1 = r0;
+		const int64_t rdst0 = D->nrdst, row0 = D->nrows, group0 = D->ngroups;
+		uint32_t *slot = D->rdst + rdst0;       /* the piece's destination rows */
+		while (r1 < nr) {
+			/* the next group [r1, g1) and the destinations it would add */
+			int64_t g1 = r1;
+			while (g1 < nr && R[g1].k == R[r1].k) g1++;
+			int add = 0;
+			for (int64_t e = r1; e < g1; e++) {
+				if (e > r1 && R[e].dst == R[e - 1].dst) continue;
+				int in = 0;
+				for (int i = 0; i < rs; i++) in |= slot[i] == R[e].dst;
+				add += !in;
+			}
+			if (rs > 0 && rs + add > JN_WALK_RS) break;
+			/* take the group, or as much of it as fits */
+			int64_t e = r1;
+			for (; e < g1; e++) {
+				int in = 0;
+				for (int i = 0; i < rs; i++) in |= slot[i] == R[e].dst;
+				if (!in) {
+					if (rs == JN_WALK_RS) break;
+					slot[rs++] = R[e].dst;
+				}
+			}
+			D->groups[D->ngroups] = (uint32_t)(S.base + S.stride * (int64_t)R[r1].k);
+			D->gblock[D->ngroups++] = x->me;
+			r1 = e;
+			if (e < g1) break;      /* a split group ends the piece */
+		}
+		/* row words: slot rows in order of first appearance */
+		for (int64_t e = r0; e < r1; e++) {
+			int sl = 0;
+			while (slot[sl] != R[e].dst) sl++;
+			const int end = e + 1 == r1 || R[e + 1].k != R[e].k;
+			D->rows[D->nrows + (e - r0)] = R[e].src | ((uint32_t)sl << 16) | (end ? JN_WALK_GROUP_END : 0u) | (R[e].sign << 31);
+		}
+		D->nrows += r1 - r0;
+		D->nrdst += rs;
+		if (D->ngroups - group0 >= (1 << 23)) { free(R); D->status = 5; return; }
+		jn_wpiece_t *P = &D->pieces[D->npieces];
+		P->src_off = (int32_t)bs->offset;
+		P->dst_off = (int32_t)bd->offset;
+		P->src_stride = (int32_t)(wp ? bs->Np : bs->Nn);
+		P->Nn_dst = (int32_t)bd->Nn;
+		P->row0 = (int32_t)row0;
+		P->rdst0 = (int32_t)rdst0;
+		P->group0 = (int32_t)group0;
+		P->meta = (uint32_t)rs | ((uint32_t)wp << 8) | ((uint32_t)(D->ngroups - group0) << 9);
+		D->prows[D->npieces++] = r1 - r0;
+		r0 = r1;
+	}
+	free(R);
+}
+
+static void wdir_free(wdir_t *D)
+{
+	free(D->rows); free(D->rdst); free(D->groups); free(D->gblock); free(D->pieces); free(D->prows);
+	D->rows = D->rdst = D->groups = NULL;
+	D->gblock = NULL;
+	D->pieces = NULL;
+	D->prows = NULL;
+}
 
 int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 {
 	vec_t tasks = { 0, 0, 0, sizeof(jn_wtask_t) }, pieces = { 0, 0, 0, sizeof(jn_wpiece_t) };
-	vec_t lanes = { 0, 0, 0, sizeof(uint32_t) }, walks = { 0, 0, 0, sizeof(uint32_t) };
+	vec_t walks = { 0, 0, 0, sizeof(uint32_t) };
 	vec_t rows = { 0, 0, 0, sizeof(uint32_t) }, rdst = { 0, 0, 0, sizeof(uint32_t) };
 	vec_t groups = { 0, 0, 0, sizeof(uint32_t) }, gblock = { 0, 0, 0, sizeof(int32_t) };
-	row_t *R = NULL;
-	int64_t Rcap = 0;
-	uint32_t *chunk = NULL;         /* per chunk: first ent index, count, walk index */
-	int64_t ccap = 0;
-	int32_t *stamp = calloc(65536, sizeof(int32_t));
-	int32_t stamp_clock = 0;
-	int *order = NULL;
+	uint32_t *lanes = NULL;
+	int64_t nlanes = 0;
+	int *order = NULL, *view_of = NULL;
+	wview_t *views = NULL;
+	wdir_t *dirs = NULL;
+	int64_t nviews = 0, ndirs = 0;
 	double visits = 0.0, slots = 0.0;
-	wview_t *views = calloc((size_t)(p->nlists ? p->nlists : 1) * 2, sizeof(wview_t));
 	jn_walk_free(p);
 	p->wtpos = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int64_t));
-	if (!stamp || !p->wtpos || !views) ERR("out of host memory");
-	for (int v = 0; v < 2 * p->nlists; v++) views[v].lanes0 = -1;
+	view_of = malloc((size_t)(p->nlists ? p->nlists : 1) * 2 * sizeof(int));
+	views = calloc((size_t)(p->nlists ? p->nlists : 1) * 2, sizeof(wview_t));
+	dirs = calloc((size_t)(p->ninstr ? p->ninstr : 1) * 2, sizeof(wdir_t));
+	if (!p->wtpos || !view_of || !views || !dirs) ERR("out of host memory");
+	for (int v = 0; v < 2 * p->nlists; v++) view_of[v] = -1;
 	if (p->dim >= 0x7fffffffll) ERR("dimension %lld: too large for the walk engine's 32-bit offsets", (long long)p->dim);
 	/* transposed copies of the n x p blocks that proton-walk instructions use */
 	for (int b = 0; b < p->nmes; b++) p->wtpos[b] = -1;
@@ -308,242 +568,107 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	if (!order) ERR("out of host memory");
 	for (int q = 0; q < p->ninstr; q++) order[q] = q;
 	qsort_r(order, (size_t)p->ninstr, sizeof(int), cmp_instr_block, p);
+	/* the directed instructions in order, and the walk views in order of first use */
 	for (int oq = 0; oq < p->ninstr; oq++) {
 		const int q = order[oq];
 		const jn_instr_t *x = &p->instr[q];
 		const jn_block_t *bi = &p->blocks[x->bin], *bo = &p->blocks[x->bout];
-		const jn_me_t *M = &p->mes[x->me];
-		const jn_list_t *W, *RL = NULL;
-		int wp;
-		int64_t base, stride;           /* element row of k_row: base + stride k_row */
-		if (x->kind == JN_KIND_NP) {
-			const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
-			wp = Lp->len > Ln->len;
-			W = wp ? Lp : Ln;
-			RL = wp ? Ln : Lp;
-			base = wp ? p->wtpos[x->me] : M->offset;
-			stride = wp ? (int64_t)M->nd_p : (int64_t)M->nd_n;
-		} else if (x->kind == JN_KIND_N) {
-			W = &p->lists[x->ln];
-			wp = 0;
-			base = M->offset;
-			stride = 0;
-			if (bi->Np != bo->Np) ERR("instruction %d: spectator rows differ", q);
-		} else {
-			W = &p->lists[x->lp];
-			wp = 1;
-			base = M->offset;
-			stride = 0;
-			if (bi->Nn != bo->Nn) ERR("instruction %d: spectator columns differ", q);
-		}
-		const int64_t wlen = RL ? (wp ? (int64_t)M->nd_p : (int64_t)M->nd_n) : M->len;   /* walk-side k range */
-		const int64_t rlen = RL ? (wp ? (int64_t)M->nd_n : (int64_t)M->nd_p) : 1;         /* row-side k range */
-		if (W->len == 0) continue;
+		if (x->kind == JN_KIND_N && bi->Np != bo->Np) ERR("instruction %d: spectator rows differ", q);
+		if (x->kind == JN_KIND_P && bi->Nn != bo->Nn) ERR("instruction %d: spectator columns differ", q);
+		const wsides_t S = walk_sides(p, q);
+		if (S.W->len == 0) continue;
+		const int64_t nr = S.RL ? S.RL->len : (S.wp ? bo->Nn : bo->Np);
 		for (int dir = 0; dir < 2; dir++) {
 			if (dir == 1 && x->bin == x->bout) break;
-			const jn_block_t *bs = dir ? bo : bi, *bd = dir ? bi : bo;
-			/* rows of this direction */
-			const int64_t nr = RL ? RL->len : (wp ? bo->Nn : bo->Np);
-			if (nr > Rcap) {
-				Rcap = nr;
-				row_t *g = realloc(R, (size_t)Rcap * sizeof(row_t));
-				if (!g) ERR("out of host memory");
-				R = g;
-			}
-			if (RL) {
-				for (int64_t e = 0; e < nr; e++) {
-					const int32_t *t = RL->triples + 3 * e;
-					R[e].src = (uint32_t)(dir ? t[1] : t[0]);
-					R[e].dst = (uint32_t)(dir ? t[0] : t[1]);
-					R[e].k = (uint32_t)t[2] & MASK31;
-					R[e].sign = (uint32_t)t[2] >> 31;
-				}
-				qsort(R, (size_t)nr, sizeof(row_t), cmp_row);
-			} else {
-				for (int64_t r = 0; r < nr; r++) R[r] = (row_t){ (uint32_t)r, (uint32_t)r, 0u, 0u };
-			}
 			if (nr == 0) continue;
-			/* row index bounds: sources and destinations inside their blocks, k inside the element block */
-			const int64_t src_rows = wp ? bs->Nn : bs->Np, dst_rows = wp ? bd->Nn : bd->Np;
-			for (int64_t e = 0; e < nr; e++)
-				if (R[e].src >= src_rows || R[e].dst >= dst_rows || R[e].src > 0xffffu || R[e].dst > 0xffffu ||
-				    R[e].k >= rlen)
-					ERR("instruction %d: row index out of range", q);
-			/* walk view and its bounds: destinations and sources inside their blocks, k inside the block */
-			const int64_t w0 = dir ? W->walk_in : W->walk_out, nw = dir ? W->nwalk_in : W->nwalk_out;
-			const int64_t src_cols = wp ? bs->Np : bs->Nn, dst_cols = wp ? bd->Np : bd->Nn;
-			for (int64_t w = 0; w < nw; w++) {
-				const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
-				if ((p->walks[2 * (w0 + w) + 1] >> 16) >= dst_cols) ERR("instruction %d: walk destination out of range", q);
-				for (uint32_t e = a; e < a + len; e++)
-					if ((p->ent[2 * e] & 0xffffu) >= src_cols || (p->ent[2 * e + 1] & MASK31) >= wlen)
-						ERR("instruction %d: walk entry out of range", q);
-			}
-			wview_t *V = &views[2 * (int64_t)(W - p->lists) + dir];
-			if (V->lanes0 < 0) {
+			const int key = 2 * (int)(S.W - p->lists) + dir;
+			if (view_of[key] < 0) {
+				wview_t *V = &views[nviews];
+				V->W = S.W;
+				V->dir = dir;
+				V->w0 = dir ? S.W->walk_in : S.W->walk_out;
+				V->nw = dir ? S.W->nwalk_in : S.W->nwalk_out;
 				/* the chunk width with the fewest lane slots, counting a row's fixed
 				   cost as about two entries */
 				int U = 8;
-				{
-					double best = 1e300;
-					for (int u = 8; u >= 2; u /= 2) {
-						const int64_t nc = chunks_for(p->walks, w0, nw, u);
-						const double cost = (double)((nc + 31) / 32) * 32 * (u + 2);
-						if (cost < best) { best = cost; U = u; }
-					}
-				}
-				const int LW = JN_WALK_LANE_WORDS(U);
-				const int64_t nchunk = chunks_for(p->walks, w0, nw, U);
-				if (3 * nchunk > ccap) {
-					ccap = 3 * nchunk;
-					uint32_t *g = realloc(chunk, (size_t)ccap * sizeof(uint32_t));
-					if (!g) ERR("out of host memory");
-					chunk = g;
-				}
-				{
-					int64_t c = 0;
-					for (int64_t w = 0; w < nw; w++) {
-						const uint32_t a = p->walks[2 * (w0 + w)], len = p->walks[2 * (w0 + w) + 1] & 0xffffu;
-						for (uint32_t o = 0; o < len; o += (uint32_t)U) {
-							chunk[3 * c] = a + o;
-							chunk[3 * c + 1] = len - o < (uint32_t)U ? len - o : (uint32_t)U;
-							chunk[3 * c + 2] = (uint32_t)w;
-							c++;
-						}
-					}
-				}
-				/* lane records and walk tables: one per 32 chunks, shared by the pieces
-				   of every directed instruction that walks this view */
-				const int64_t nsets = (nchunk + 31) / 32;
-				const int64_t lanes0 = lanes.n;
-				if (vec_reserve(&lanes, nsets * 32 * LW) || vec_reserve(&walks, nsets * 32)) ERR("out of host memory");
-				uint32_t *set_walk0 = malloc((size_t)(nsets ? nsets : 1) * 2 * sizeof(uint32_t));
-				if (!set_walk0) ERR("out of host memory");
-				V->set_walk0 = set_walk0;
-				for (int64_t s = 0; s < nsets; s++) {
-					uint32_t *L = (uint32_t *)lanes.a + lanes.n;
-					uint32_t *T = (uint32_t *)walks.a + walks.n;
-					int nwalk = 0;
-					for (int l = 0; l < 32;) {
-						/* the run of this set's lanes [l, l1) that hold chunks of one walk: its
-						   entries (contiguous in the walk view) are dealt to the run's lanes in
-						   turn, entry i to lane l + i mod nl at position i / nl */
-						int l1 = l + 1;
-						const int64_t c0 = s * 32 + l;
-						if (c0 < nchunk)
-							while (l1 < 32 && s * 32 + l1 < nchunk && chunk[3 * (s * 32 + l1) + 2] == chunk[3 * c0 + 2]) l1++;
-						else
-							l1 = 32;
-						const int nl = l1 - l;
-						uint32_t e0 = 0, ne = 0;
-						if (c0 < nchunk) {
-							T[nwalk++] = p->walks[2 * (w0 + chunk[3 * c0 + 2]) + 1] >> 16;
-							e0 = chunk[3 * c0];
-							for (int64_t c = c0; c < s * 32 + l1; c++) ne += chunk[3 * c + 1];
-						}
-						for (int r = 0; r < nl; r++) {
-							uint32_t src[8], koff[8];
-							for (int u = 0; u < U; u++) {
-								const uint32_t i = (uint32_t)(u * nl + r);
-								/* padding repeats the lane's first source with coefficient 0 */
-								const uint32_t e = e0 + (i < ne ? i : (uint32_t)r);
-								src[u] = c0 < nchunk ? p->ent[2 * e] & 0xffffu : 0u;
-								koff[u] = i < ne ? (p->ent[2 * e + 1] & 0x3fffffffu) |
-											   ((p->ent[2 * e + 1] >> 31) ? JN_WALK_NEG : JN_WALK_POS)
-										 : 0u;
-							}
-							uint32_t mul = 0;
-							for (int u = 0; u < U; u++) mul |= (koff[u] >> 30) << (2 * u);
-							L[l + r] = (c0 < nchunk ? (uint32_t)(nwalk - 1) : 0u) | (mul << 16);
-							for (int k = 0; k < U / 2; k++) L[(1 + k) * 32 + l + r] = src[2 * k] | (src[2 * k + 1] << 16);
-							for (int u = 0; u < U; u++) L[(1 + U / 2 + u) * 32 + l + r] = koff[u];
-						}
-						l = l1;
-					}
-					set_walk0[2 * s] = (uint32_t)walks.n;
-					set_walk0[2 * s + 1] = (uint32_t)nwalk;
-					lanes.n += 32 * LW;
-					walks.n += nwalk;
+				double best = 1e300;
+				for (int u = 8; u >= 2; u /= 2) {
+					const int64_t nc = chunks_for(p->walks, V->w0, V->nw, u);
+					const double cost = (double)((nc + 31) / 32) * 32 * (u + 2);
+					if (cost < best) { best = cost; U = u; }
 				}
 				V->U = U;
-				V->nsets = nsets;
-				V->nchunk = nchunk;
-				V->lanes0 = lanes0;
+				V->nchunk = chunks_for(p->walks, V->w0, V->nw, U);
+				V->nsets = (V->nchunk + 31) / 32;
+				V->lanes0 = nlanes;
+				nlanes += V->nsets * 32 * JN_WALK_LANE_WORDS(U);
+				view_of[key] = (int)nviews++;
 			}
-			const int U = V->U, LW = JN_WALK_LANE_WORDS(U);
-			const int64_t nsets = V->nsets, nchunk = V->nchunk, lanes0 = V->lanes0;
-			const uint32_t *set_walk0 = V->set_walk0;
-			/* pieces: runs of whole row groups with at most RS distinct destination rows
-			   (a group with more is split, and its element row read once per part) */
-			int64_t r0 = 0;
-			while (r0 < nr) {
-				stamp_clock++;
-				if (stamp_clock == 0x7fffffff) { memset(stamp, 0, 65536 * sizeof(int32_t)); stamp_clock = 1; }
-				int rs = 0;
-				int64_t r1 = r0;
-				const int64_t rdst0 = rdst.n, row0 = rows.n, group0 = groups.n;
-				if (vec_reserve(&rdst, JN_WALK_RS) || vec_reserve(&rows, nr - r0) || vec_reserve(&groups, nr - r0) ||
-				    vec_reserve(&gblock, nr - r0))
-					ERR("out of host memory");
-				while (r1 < nr) {
-					/* the next group [r1, g1) and the destinations it would add */
-					int64_t g1 = r1;
-					while (g1 < nr && R[g1].k == R[r1].k) g1++;
-					int add = 0;
-					for (int64_t e = r1; e < g1; e++)
-						if (stamp[R[e].dst] != stamp_clock && (e == r1 || R[e].dst != R[e - 1].dst)) add++;
-					if (rs > 0 && rs + add > JN_WALK_RS) break;
-					/* take the group, or as much of it as fits */
-					int64_t e = r1;
-					for (; e < g1; e++) {
-						if (stamp[R[e].dst] != stamp_clock) {
-							if (rs == JN_WALK_RS) break;
-							stamp[R[e].dst] = stamp_clock;
-							((uint32_t *)rdst.a)[rdst.n + rs] = R[e].dst;
-							rs++;
-						}
-					}
-					((uint32_t *)groups.a)[groups.n++] = (uint32_t)(base + stride * (int64_t)R[r1].k);
-					((int32_t *)gblock.a)[gblock.n++] = x->me;
-					r1 = e;
-					if (e < g1) break;      /* a split group ends the piece */
-				}
-				/* row words: slot rows in order of first appearance */
-				for (int64_t e = r0; e < r1; e++) {
-					int slot = 0;
-					while (((uint32_t *)rdst.a)[rdst.n + slot] != R[e].dst) slot++;
-					const int end = e + 1 == r1 || R[e + 1].k != R[e].k;
-					((uint32_t *)rows.a)[rows.n + (e - r0)] = R[e].src | ((uint32_t)slot << 16) |
-										 (end ? JN_WALK_GROUP_END : 0u) | (R[e].sign << 31);
-				}
-				rows.n += r1 - r0;
-				rdst.n += rs;
-				if (vec_reserve(&pieces, 1) || vec_reserve(&tasks, nsets)) ERR("out of host memory");
-				const int64_t pi = pieces.n++;
-				jn_wpiece_t *P = (jn_wpiece_t *)pieces.a + pi;
-				P->src_off = (int32_t)bs->offset;
-				P->dst_off = (int32_t)bd->offset;
-				P->src_stride = (int32_t)(wp ? bs->Np : bs->Nn);
-				if (wp) p->wxt = 1;
-				P->Nn_dst = (int32_t)bd->Nn;
-				P->row0 = (int32_t)row0;
-				P->rdst0 = (int32_t)rdst0;
-				P->group0 = (int32_t)group0;
-				if (groups.n - group0 >= (1 << 23)) ERR("instruction %d: too many row groups", q);
-				P->meta = (uint32_t)rs | ((uint32_t)wp << 8) | ((uint32_t)(groups.n - group0) << 9);
-				for (int64_t s = 0; s < nsets; s++) {
-					jn_wtask_t *T = (jn_wtask_t *)tasks.a + tasks.n++;
-					T->piece = (uint32_t)pi;
-					T->lanes = (uint32_t)(lanes0 + s * 32 * LW);
-					T->walk0 = set_walk0[2 * s];
-					T->meta = set_walk0[2 * s + 1] | ((uint32_t)U << 8);
-					const int64_t used = (s + 1) * 32 <= nchunk ? 32 : nchunk - s * 32;
-					visits += (double)(r1 - r0) * (double)used * U;
-					slots += (double)(r1 - r0) * 32.0 * U;
-				}
-				r0 = r1;
+			dirs[ndirs].q = q;
+			dirs[ndirs].dir = dir;
+			dirs[ndirs].view = view_of[key];
+			ndirs++;
+		}
+	}
+	if (nlanes > 0xffffffffll) ERR("the walk plan is too large");
+	lanes = malloc((size_t)(nlanes ? nlanes : 1) * sizeof(uint32_t));
+	if (!lanes) ERR("out of host memory");
+	{
+		wjob_t job = { p, views, dirs, lanes };
+		jn_par_for(nviews, view_lanes, &job);
+		jn_par_for(ndirs, dir_pieces, &job);
+	}
+	for (int64_t v = 0; v < nviews; v++)
+		if (views[v].status) ERR("out of host memory");
+	for (int64_t d = 0; d < ndirs; d++) {
+		static const char *const what[] = { "", "out of host memory", "row index out of range",
+						     "walk destination out of range", "walk entry out of range", "too many row groups" };
+		if (dirs[d].status == 1) ERR("out of host memory");
+		if (dirs[d].status) ERR("instruction %d: %s", dirs[d].q, what[dirs[d].status]);
+	}
+	/* join in instruction order: a view's walk table at its first use, then
+	   the instruction's rows and pieces, and per piece one task per set */
+	for (int64_t d = 0; d < ndirs; d++) {
+		wdir_t *D = &dirs[d];
+		wview_t *V = &views[D->view];
+		const int U = V->U, LW = JN_WALK_LANE_WORDS(U);
+		if (V->wtab) {
+			if (vec_reserve(&walks, V->nwtab)) ERR("out of host memory");
+			V->walks0 = walks.n;
+			memcpy((uint32_t *)walks.a + walks.n, V->wtab, (size_t)V->nwtab * sizeof(uint32_t));
+			walks.n += V->nwtab;
+			free(V->wtab);
+			V->wtab = NULL;
+		}
+		const int64_t row_base = rows.n, rdst_base = rdst.n, group_base = groups.n;
+		if (vec_reserve(&rows, D->nrows) || vec_reserve(&rdst, D->nrdst) || vec_reserve(&groups, D->ngroups) ||
+		    vec_reserve(&gblock, D->ngroups) || vec_reserve(&pieces, D->npieces) || vec_reserve(&tasks, D->npieces * V->nsets))
+			ERR("out of host memory");
+		memcpy((uint32_t *)rows.a + rows.n, D->rows, (size_t)D->nrows * sizeof(uint32_t));
+		memcpy((uint32_t *)rdst.a + rdst.n, D->rdst, (size_t)D->nrdst * sizeof(uint32_t));
+		memcpy((uint32_t *)groups.a + groups.n, D->groups, (size_t)D->ngroups * sizeof(uint32_t));
+		memcpy((int32_t *)gblock.a + gblock.n, D->gblock, (size_t)D->ngroups * sizeof(int32_t));
+		rows.n += D->nrows; rdst.n += D->nrdst; groups.n += D->ngroups; gblock.n += D->ngroups;
+		for (int64_t k = 0; k < D->npieces; k++) {
+			jn_wpiece_t P = D->pieces[k];
+			P.row0 += (int32_t)row_base;
+			P.rdst0 += (int32_t)rdst_base;
+			P.group0 += (int32_t)group_base;
+			if ((P.meta >> 8) & 1u) p->wxt = 1;
+			const int64_t pi = pieces.n++;
+			((jn_wpiece_t *)pieces.a)[pi] = P;
+			for (int64_t s = 0; s < V->nsets; s++) {
+				jn_wtask_t *T = (jn_wtask_t *)tasks.a + tasks.n++;
+				T->piece = (uint32_t)pi;
+				T->lanes = (uint32_t)(V->lanes0 + s * 32 * LW);
+				T->walk0 = (uint32_t)(V->walks0 + V->set_walk0[2 * s]);
+				T->meta = V->set_walk0[2 * s + 1] | ((uint32_t)U << 8);
+				const int64_t used = (s + 1) * 32 <= V->nchunk ? 32 : V->nchunk - s * 32;
+				visits += (double)D->prows[k] * (double)used * U;
+				slots += (double)D->prows[k] * 32.0 * U;
 			}
 		}
+		wdir_free(D);
 	}
 	/* tasks stay in this order: warps take the next one from a counter, so
 	   warps that run at the same time work on neighbouring instructions and
@@ -561,12 +686,12 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	/* spare row words: the kernel reads up to two words past a task's last row ahead of time */
 	if (vec_reserve(&rows, JN_WALK_ROW_SPARE)) ERR("out of host memory");
 	for (int k = 0; k < JN_WALK_ROW_SPARE; k++) ((uint32_t *)rows.a)[rows.n + k] = 0u;
-	if (tasks.n > 0xf0000000ll || lanes.n > 0xffffffffll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
+	if (tasks.n > 0xf0000000ll || walks.n > 0xffffffffll || rows.n > 0x7fffffffll ||
 	    rdst.n > 0x7fffffffll || groups.n > 0x7fffffffll || pieces.n > 0xffffffffll)
 		ERR("the walk plan is too large");
 	p->wtasks = tasks.a; p->nwtasks = tasks.n;
 	p->wpieces = pieces.a; p->nwpieces = pieces.n;
-	p->wlanes = lanes.a; p->n_wlanes = lanes.n;
+	p->wlanes = lanes; p->n_wlanes = nlanes;
 	p->wwalks = walks.a; p->n_wwalks = walks.n;
 	p->wrows = rows.a; p->n_wrows = rows.n;         /* plus the spare words */
 	p->wrdst = rdst.a; p->n_wrdst = rdst.n;
@@ -574,17 +699,17 @@ int jn_walk_build(jn_plan_t *p, char *err, size_t errlen)
 	p->wgblock = gblock.a;
 	p->wvisits = visits;
 	p->wlane_slots = slots;
-	free(R); free(chunk); free(stamp); free(order);
-	for (int v = 0; v < 2 * p->nlists; v++) free(views[v].set_walk0);
-	free(views);
+	for (int64_t v = 0; v < nviews; v++) free(views[v].set_walk0);
+	free(views); free(dirs); free(view_of); free(order);
 	return 0;
 fail:
-	free(tasks.a); free(pieces.a); free(lanes.a); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
+	free(tasks.a); free(pieces.a); free(lanes); free(walks.a); free(rows.a); free(rdst.a); free(groups.a);
 	free(gblock.a);
-	free(R); free(chunk); free(stamp); free(order);
 	if (views)
-		for (int v = 0; v < 2 * p->nlists; v++) free(views[v].set_walk0);
-	free(views);
+		for (int64_t v = 0; v < nviews; v++) { free(views[v].set_walk0); free(views[v].wtab); }
+	if (dirs)
+		for (int64_t d = 0; d < ndirs; d++) wdir_free(&dirs[d]);
+	free(views); free(dirs); free(view_of); free(order);
 	free(p->wtpos); free(p->wxperm);
 	p->wtpos = NULL;
 	p->wxperm = NULL;
