@@ -378,12 +378,14 @@ void jn_walk_free(jn_plan_t *plan);
 /* the walk element array (plan->n_wme values) from matrix elements in the
  * plan's layout */
 void jn_walk_elements(const jn_plan_t *plan, const double *me, double *out);
-/* the integer path's elements: each block scaled by its own 2^Sc_b so that
+/* the integer path's elements: each element of the walk element array
+ * (formed from matrix elements me in the plan's layout, as
+ * jn_walk_elements forms it) scaled by its block's own 2^Sc_b so that
  * max|A| of the block is below 2^52, rounded, and split into {high 28 bits
- * (signed), low 24 bits} (two words per element of the walk element array
- * a); per group the shift Sc_b - Sc_min (capped at 255) into gshift, and
- * Sc_min (the smallest block exponent) into *sc_min */
-void jn_walk_int_elements(const jn_plan_t *plan, const double *a, int32_t *split, uint8_t *gshift, int *sc_min);
+ * (signed), low 24 bits} (two words per element); per group the shift
+ * Sc_b - Sc_min (capped at 255) into gshift, and Sc_min (the smallest block
+ * exponent) into *sc_min */
+void jn_walk_int_elements(const jn_plan_t *plan, const double *me, int32_t *split, uint8_t *gshift, int *sc_min);
 
 #ifdef __cplusplus
 }

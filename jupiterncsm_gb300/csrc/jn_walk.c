@@ -117,7 +117,15 @@ void jn_walk_elements(const jn_plan_t *p, const double *me, double *out)
 	free(it);
 }
 
-typedef struct { const jn_plan_t *p; const witem_t *it; const double *a; double *imax; const int *sc; int32_t *split; } int_job_t;
+typedef struct { const jn_plan_t *p; const witem_t *it; const double *me; double *imax; const int *sc; int32_t *split; } int_job_t;
+
+/* a block's own element e as the walk element array holds it: single-species
+   blocks store |M| < 1e-12 as 0 (matrix_vector_multiplication.c:52-53) */
+static inline double own_element(const jn_me_t *M, const double *me, int64_t e)
+{
+	const double v = me[M->offset + e];
+	return (M->single && fabs(v) < 1e-12) ? 0.0 : v;
+}
 
 /* max |a| over a chunk of a block's own elements */
 static void int_max_item(int64_t i, void *v)
@@ -126,9 +134,9 @@ static void int_max_item(int64_t i, void *v)
 	const witem_t *w = &j->it[i];
 	double m = 0.0;
 	if (w->kind == 0) {
-		const int64_t o = j->p->mes[w->b].offset;
+		const jn_me_t *M = &j->p->mes[w->b];
 		for (int64_t e = w->e0; e < w->e1; e++) {
-			const double x = fabs(j->a[o + e]);
+			const double x = fabs(own_element(M, j->me, e));
 			if (x > m) m = x;           /* skips NaN as fmax does */
 		}
 	}
@@ -156,38 +164,38 @@ static void int_split_item(int64_t i, void *v)
 		o = M->offset;
 		e0 = w->e0;
 		e1 = w->e1;
-	} else {            /* transposed rows [e0, e1) hold elements kp + Nd_p kn: convert kp-major runs */
+	} else {            /* transposed rows [e0, e1) hold elements kp + Nd_p kn, copied from kn + Nd_n kp */
 		o = p->wtpos[w->b];
 		const int64_t npp = (int64_t)M->nd_p, nn = (int64_t)M->nd_n;
 		for (int64_t kn = 0; kn < nn; kn++)
 			for (int64_t kp = w->e0; kp < w->e1; kp++) {
-				const int64_t q = o + kp + npp * kn, v = llrint(scaled(j->a[q], s, f));
+				const int64_t q = o + kp + npp * kn, v = llrint(scaled(j->me[M->offset + kn + nn * kp], s, f));
 				j->split[2 * q] = (int32_t)(v >> 24);
 				j->split[2 * q + 1] = (int32_t)(v & 0xffffff);
 			}
 		return;
 	}
 	for (int64_t e = e0; e < e1; e++) {
-		const int64_t v = llrint(scaled(j->a[o + e], s, f));
+		const int64_t v = llrint(scaled(own_element(M, j->me, e), s, f));
 		j->split[2 * (o + e)] = (int32_t)(v >> 24);
 		j->split[2 * (o + e) + 1] = (int32_t)(v & 0xffffff);
 	}
 }
 
-void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, uint8_t *gshift, int *sc_min)
+void jn_walk_int_elements(const jn_plan_t *p, const double *me, int32_t *split, uint8_t *gshift, int *sc_min)
 {
 	int *sc = malloc((size_t)(p->nmes ? p->nmes : 1) * sizeof(int));
 	double *bmax = calloc((size_t)(p->nmes ? p->nmes : 1), sizeof(double));
 	int64_t n = 0;
 	witem_t *it = walk_items(p, &n);
 	double *imax = malloc((size_t)(n ? n : 1) * sizeof(double));
-	int_job_t j = { p, it, a, imax, sc, split };
+	int_job_t j = { p, it, me, imax, sc, split };
 	if (it && imax) {
 		jn_par_for(n, int_max_item, &j);
 		for (int64_t i = 0; i < n; i++) bmax[it[i].b] = fmax(bmax[it[i].b], imax[i]);
 	} else {
 		for (int b = 0; b < p->nmes; b++)
-			for (int64_t e = 0; e < p->mes[b].len; e++) bmax[b] = fmax(bmax[b], fabs(a[p->mes[b].offset + e]));
+			for (int64_t e = 0; e < p->mes[b].len; e++) bmax[b] = fmax(bmax[b], fabs(own_element(&p->mes[b], me, e)));
 	}
 	/* each block keeps 52 bits against its own max|M|: |v| 2^sc < 2^52 */
 	int lo = 1 << 30;
@@ -205,7 +213,7 @@ void jn_walk_int_elements(const jn_plan_t *p, const double *a, int32_t *split, u
 	} else {
 		for (int b = 0; b < p->nmes; b++) {
 			witem_t one[2] = { { b, 0, 0, p->mes[b].len }, { b, 1, 0, (int64_t)p->mes[b].nd_p } };
-			int_job_t jb = { p, one, a, NULL, sc, split };
+			int_job_t jb = { p, one, me, NULL, sc, split };
 			int_split_item(0, &jb);
 			if (p->wtpos && p->wtpos[b] >= 0) int_split_item(1, &jb);
 		}

@@ -406,11 +406,12 @@ jn_status jn_walk_setup(jn_ctx *c)
 }
 
 /* the walk element array of the current matrix elements for one arithmetic
- * (built on first use and after the matrix elements change), each from the
- * FP64 array built on the host: FP64 (arithmetic 64); FP32, converted on the
- * device from the FP64 copy when that exists, else on the host; the
- * integer path's split 52-bit values with their per-group shifts (only
- * these reach the device for it) */
+ * (built on first use and after the matrix elements change): FP64
+ * (arithmetic 64) from the FP64 array built on the host; FP32, converted on
+ * the device from the FP64 copy when that exists, else on the host; the
+ * integer path's split 52-bit values with their per-group shifts, formed on
+ * the host straight from the plan's elements (only these reach the device
+ * for it) */
 static jn_status walk_elements(jn_ctx *c, int mode)
 {
 	const jn_plan_t *p = &c->plan;
@@ -431,9 +432,14 @@ static jn_status walk_elements(jn_ctx *c, int mode)
 		if (e != cudaSuccess) return jn_fail(JN_ERR_CUDA, "walk matrix elements: %s", cudaGetErrorString(e));
 		return JN_OK;
 	}
-	double *h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
-	if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
-	jn_walk_elements(p, p->me, h);
+	/* the exact integer path splits the plan's elements directly; the FP64
+	   and FP32 paths start from the FP64 walk element array */
+	double *h = NULL;
+	if (mode == 64 || mode == 32) {
+		h = (double *)malloc((size_t)(n ? n : 1) * sizeof(double));
+		if (!h) return jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
+		jn_walk_elements(p, p->me, h);
+	}
 	jn_status s = JN_OK;
 	if (mode == 64) {
 		double *d = NULL;
@@ -455,7 +461,7 @@ static jn_status walk_elements(jn_ctx *c, int mode)
 		if (!sp || !gs) {
 			s = jn_fail(JN_ERR_NOMEM, "out of host memory for %lld walk matrix elements", (long long)n);
 		} else {
-			jn_walk_int_elements(p, h, sp, gs, &c->walk_sc);
+			jn_walk_int_elements(p, p->me, sp, gs, &c->walk_sc);
 			int2 *d = NULL;
 			s = wupload(&d, sp, (size_t)n);
 			if (!s) {

@@ -589,7 +589,7 @@ int emu_matvec5(void *h, const double *x, double *y, int accumulate, int mode)
 	int32_t *split = malloc((nm ? nm : 1) * 2 * sizeof(int32_t));
 	uint8_t *gshift = malloc(P->n_wgroups ? P->n_wgroups : 1);
 	int Sc = 0;
-	jn_walk_int_elements(P, a64, split, gshift, &Sc);
+	jn_walk_int_elements(P, P->me, split, gshift, &Sc);
 	for (int64_t e = 0; e < nm; e++) {
 		a32[e] = (float)a64[e];
 		ah[e] = split[2 * e];
