@@ -255,6 +255,17 @@ fail:
 	return NULL;
 }
 
+/* one index list per work item */
+typedef struct { jn_plan_t *p; const char *dir; uint8_t *bad; } list_job_t;
+
+static void list_read_item(int64_t l, void *v)
+{
+	const list_job_t *j = (const list_job_t *)v;
+	jn_list_t *L = &j->p->lists[l];
+	L->triples = read_list_file(j->dir, L->id, &L->len, NULL, 0);
+	if (!L->triples) j->bad[l] = 1;
+}
+
 /* fn(i, arg) for every i < n, on up to 32 host threads taking items from a
  * shared counter */
 typedef struct {
@@ -1308,9 +1319,7 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 				jn_list_t *L = &p->lists[p->nlists];
 				memset(L, 0, sizeof *L);
 				L->id = (int)lids[q]; L->type = c.l[ci].type; L->nin = L->nout = -1;
-				L->triples = read_list_file(lists_dir, lids[q], &L->len, err, errlen);
-				if (!L->triples) goto fail;
-				s = slot_of_id[lids[q]] = p->nlists++;
+				s = slot_of_id[lids[q]] = p->nlists++;          /* read below */
 			}
 			lslot[q] = s;
 			ltype[q] = p->lists[s].type;
@@ -1336,6 +1345,25 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 	}
 	fclose(f); f = NULL;
 	if (!p->ninstr) ERR("evaluation order %s holds no BLOCK rows", order_path);
+
+	/* the index lists, read by all host cores; a failing list is read once
+	   more on its own for its message, the first in order of appearance */
+	{
+		uint8_t *bad = calloc(p->nlists ? p->nlists : 1, 1);
+		if (!bad) ERR("out of host memory");
+		list_job_t lj = { p, lists_dir, bad };
+		jn_par_for(p->nlists, list_read_item, &lj);
+		int first = -1;
+		for (int l = 0; l < p->nlists && first < 0; l++)
+			if (bad[l]) first = l;
+		free(bad);
+		if (first >= 0) {
+			jn_list_t *L = &p->lists[first];
+			L->triples = read_list_file(lists_dir, L->id, &L->len, err, errlen);
+			if (!L->triples) goto fail;
+			ERR("index list %d could not be read", L->id);
+		}
+	}
 
 	/* matrix elements */
 	int64_t me_total = 0;
