@@ -44,6 +44,9 @@ const char *jn_version(void);
  * Open a Hamiltonian described by a Bacchus run file: reads the combination
  * table, evaluation order, every index list and every matrix-element block
  * once, validates all indices, and uploads them to the current CUDA device.
+ * The host plans are built on all cores (at most 32 threads; the
+ * environment variable JN_HOST_THREADS caps them), and the results do not
+ * depend on the number of threads.
  * Replaces parse_settings + new_combination_table + read_evaluation_order +
  * new_generative_matrix (Bacchus/settings/settings.c:27-214,
  * Utilities/combination_table/combination_table.c:83-137,

@@ -288,6 +288,8 @@ static void *par_worker(void *v)
 void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg)
 {
 	long nt = sysconf(_SC_NPROCESSORS_ONLN);
+	const char *cap = getenv("JN_HOST_THREADS");     /* optional cap on the host threads */
+	if (cap && atol(cap) > 0 && atol(cap) < nt) nt = atol(cap);
 	if (nt > 32) nt = 32;
 	if (nt < 1 || n < 2) nt = 1;
 	par_t p = { n, 0, fn, arg };

@@ -331,7 +331,8 @@ typedef struct {
 } jn_runfile_t;
 
 int jn_read_runfile(const char *path, jn_runfile_t *rf, char *err, size_t errlen);
-/* fn(i, arg) for every i < n on all host cores (at most 32 threads); items
+/* fn(i, arg) for every i < n on all host cores (at most 32 threads, or
+ * fewer when the environment variable JN_HOST_THREADS caps them); items
  * are taken from a shared counter, so fn must not depend on their order */
 void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg);
 int jn_plan_build(jn_plan_t *plan, const char *comb, const char *order, const char *lists_dir,

@@ -791,3 +791,52 @@ int emu_walk_corrupt(void *h, int kind)
 	else P->wrows[pc->row0] = (P->wrows[pc->row0] & ~(31u << 16)) | (31u << 16);
 	return 0;
 }
+
+/* FNV-1a digest of every host plan array a product reads (engines 2, 3
+ * and 5, the walk element arrays and the bounds): equal digests, equal plans */
+static uint64_t fnv(uint64_t x, const void *v, size_t n)
+{
+	const unsigned char *c = v;
+	for (size_t i = 0; i < n; i++) { x ^= c[i]; x *= 1099511628211ull; }
+	return x;
+}
+
+uint64_t emu_plan_digest(void *h)
+{
+	jn_plan_t *P = h;
+	uint64_t x = 1469598103934665603ull;
+	x = fnv(x, P->rowptr, (size_t)P->n_rowptr * 4);
+	x = fnv(x, P->ent, (size_t)P->n_ent * 8);
+	x = fnv(x, P->me, (size_t)P->n_me * 8);
+	x = fnv(x, &P->me_referenced, sizeof P->me_referenced);
+	x = fnv(x, P->tiles, (size_t)P->ntiles * sizeof(jn_tile_t));
+	x = fnv(x, P->units, (size_t)P->nunits * sizeof(jn_unit_t));
+	x = fnv(x, P->unit_terms, (size_t)P->n_unit_terms * 4);
+	x = fnv(x, P->btiles, (size_t)P->nbtiles * sizeof(jn_btile_t));
+	x = fnv(x, P->pieces, (size_t)P->npieces * sizeof(jn_piece_t));
+	x = fnv(x, P->items, (size_t)P->nitems * 8);
+	x = fnv(x, &P->abs_bound, sizeof P->abs_bound);
+	if (emu_walk_build(h)) return 0;
+	x = fnv(x, P->wtasks, (size_t)P->nwtasks * sizeof(jn_wtask_t));
+	x = fnv(x, P->wpieces, (size_t)P->nwpieces * sizeof(jn_wpiece_t));
+	x = fnv(x, P->wlanes, (size_t)P->n_wlanes * 4);
+	x = fnv(x, P->wwalks, (size_t)P->n_wwalks * 4);
+	x = fnv(x, P->wrows, (size_t)P->n_wrows * 4);
+	x = fnv(x, P->wrdst, (size_t)P->n_wrdst * 4);
+	x = fnv(x, P->wgroups, (size_t)P->n_wgroups * 4);
+	x = fnv(x, P->wgblock, (size_t)P->n_wgroups * 4);
+	const int64_t nm = P->n_wme;
+	double *a = malloc((nm ? nm : 1) * sizeof(double));
+	int32_t *split = malloc((nm ? nm : 1) * 2 * sizeof(int32_t));
+	uint8_t *gs = malloc(P->n_wgroups ? P->n_wgroups : 1);
+	int sc = 0;
+	if (!a || !split || !gs) { free(a); free(split); free(gs); return 0; }
+	jn_walk_elements(P, P->me, a);
+	jn_walk_int_elements(P, P->me, split, gs, &sc);
+	x = fnv(x, a, (size_t)nm * 8);
+	x = fnv(x, split, (size_t)nm * 8);
+	x = fnv(x, gs, (size_t)P->n_wgroups);
+	x = fnv(x, &sc, sizeof sc);
+	free(a); free(split); free(gs);
+	return x;
+}

@@ -178,3 +178,24 @@ def test_panel_list_order_spreads_atomics(problem, name):
           % (ref[1] / ref[0], got[1] / got[0], ref[3] / max(ref[2], 1), got[3] / max(got[2], 1)))
     assert got[1] + got[3] < 0.8 * (ref[1] + ref[3])
     L.emu_close(h)
+
+
+@pytest.mark.parametrize("name", ["he4_n4_2b", "li6_n2_3b", "he4_n6_3b"])
+def test_plans_do_not_depend_on_the_host_thread_count(problem, name, monkeypatch):
+    """The host builds its plans on all cores; with one thread (JN_HOST_THREADS=1)
+    every array a product reads (engines 2, 3 and 5, the walk element arrays,
+    the bounds) is the same, byte for byte."""
+    d, Z, N, *_ = problem(name)
+    digests = []
+    for threads in ("1", "3", None):
+        if threads:
+            monkeypatch.setenv("JN_HOST_THREADS", threads)
+        else:
+            monkeypatch.delenv("JN_HOST_THREADS", raising=False)
+        L, h, err = open_plan(d, Z, N)
+        assert h, err
+        L.emu_plan_digest.restype = ctypes.c_uint64
+        L.emu_plan_digest.argtypes = [ctypes.c_void_p]
+        digests.append(L.emu_plan_digest(h))
+        L.emu_close(h)
+    assert digests[0] != 0 and digests[0] == digests[1] == digests[2]
