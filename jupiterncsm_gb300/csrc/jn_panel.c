@@ -8,6 +8,7 @@
  * transposes :212-462); the order in which contributions are added does not
  * matter because the device sums them as exact 64-bit integers.
  */
+#define _GNU_SOURCE        /* qsort_r */
 #include <errno.h>
 #include <math.h>
 #include <stdio.h>
@@ -133,18 +134,21 @@ static double task_cost(const jn_plan_t *p, const uint32_t *T)
 	return (double)((T[2] - T[1] + R - 1) / R) * (diag ? 1.0 : 2.0) + 4.0;
 }
 
-static const jn_plan_t *g_sort_plan;
-static int cmp_task_cost(const void *a, const void *b)
+/* qsort_r comparators: the plan comes with the call, so concurrent panel
+ * builds share no state */
+static int cmp_task_cost(const void *a, const void *b, void *plan)
 {
-	const double ca = task_cost(g_sort_plan, a), cb = task_cost(g_sort_plan, b);
+	const jn_plan_t *p = (const jn_plan_t *)plan;
+	const double ca = task_cost(p, a), cb = task_cost(p, b);
 	if (ca != cb) return ca > cb ? -1 : 1;
 	return memcmp(a, b, 4 * sizeof(uint32_t));
 }
 
 /* panels sorted by (output block, input block) so that a CTA's run of tasks touches few blocks */
-static int cmp_panel(const void *a, const void *b)
+static int cmp_panel(const void *a, const void *b, void *plan)
 {
-	const jn_instr_t *x = &g_sort_plan->instr[*(const int *)a], *y = &g_sort_plan->instr[*(const int *)b];
+	const jn_plan_t *p = (const jn_plan_t *)plan;
+	const jn_instr_t *x = &p->instr[*(const int *)a], *y = &p->instr[*(const int *)b];
 	if (x->bout != y->bout) return x->bout < y->bout ? -1 : 1;
 	if (x->bin != y->bin) return x->bin < y->bin ? -1 : 1;
 	return *(const int *)a - *(const int *)b;
@@ -208,8 +212,7 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	/* panels */
 	order = malloc((p->ninstr ? p->ninstr : 1) * sizeof(int));
 	for (int i = 0; i < p->ninstr; i++) order[i] = i;
-	g_sort_plan = p;
-	qsort(order, p->ninstr, sizeof(int), cmp_panel);
+	qsort_r(order, p->ninstr, sizeof(int), cmp_panel, p);
 	p->panels = calloc(p->ninstr ? p->ninstr : 1, sizeof(jn_panel_t));
 	if (!order || !p->panels) ERR("out of host memory");
 	int64_t coef = 0, ntask = 0;
@@ -292,8 +295,7 @@ int jn_panels_build(jn_plan_t *p, int grid, int iter, char *err, size_t errlen)
 	/* within each CTA's run, heaviest tasks first: the warps that finish last
 	   then finish with small tasks (the order never changes a result bit) */
 	for (int b = 0; b < grid; b++) {
-		g_sort_plan = p;
-		qsort(p->ptasks + 4 * (size_t)p->pcta[b], p->pcta[b + 1] - p->pcta[b], 4 * sizeof(uint32_t), cmp_task_cost);
+		qsort_r(p->ptasks + 4 * (size_t)p->pcta[b], p->pcta[b + 1] - p->pcta[b], 4 * sizeof(uint32_t), cmp_task_cost, p);
 	}
 	/* every device index stays inside its buffer: checked once here */
 	for (int q = 0; q < p->npanels; q++) {

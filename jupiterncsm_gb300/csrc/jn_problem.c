@@ -575,10 +575,12 @@ static double term_cost(const jn_plan_t *p, const jn_term_t *t, int r0, int r1, 
 	return 4.0 + npmax * (1.0 + nnmax);
 }
 
-static const double *g_unit_cost;
-static int cmp_unit_cost(const void *a, const void *b)
+/* indices by cost, heaviest first, ties by index (qsort_r: the costs come
+ * with the call, so concurrent plan builds share no state) */
+static int cmp_cost_desc(const void *a, const void *b, void *cost)
 {
-	double x = g_unit_cost[*(const int *)a], y = g_unit_cost[*(const int *)b];
+	const double *c = (const double *)cost;
+	double x = c[*(const int *)a], y = c[*(const int *)b];
 	if (x != y) return x < y ? 1 : -1;
 	return *(const int *)a - *(const int *)b;
 }
@@ -591,14 +593,6 @@ static int cmp_unit_cost(const void *a, const void *b)
 #define TASK_OVERHEAD 6.0
 
 typedef struct { jn_piece_t t; double cost; } task_cost_t;
-
-static const double *g_tile_cost;
-static int cmp_tile_cost(const void *a, const void *b)
-{
-	double x = g_tile_cost[*(const int *)a], y = g_tile_cost[*(const int *)b];
-	if (x != y) return x < y ? 1 : -1;
-	return *(const int *)a - *(const int *)b;
-}
 
 static int cmp_task_cost(const void *a, const void *b)
 {
@@ -1029,8 +1023,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	{
 		int *ord = malloc((ntl ? ntl : 1) * sizeof(int));
 		for (int i = 0; i < ntl; i++) ord[i] = i;
-		g_tile_cost = tile_cost;
-		qsort(ord, ntl, sizeof(int), cmp_tile_cost);
+		qsort_r(ord, ntl, sizeof(int), cmp_cost_desc, tile_cost);
 		p->btiles = malloc((ntl ? ntl : 1) * sizeof(jn_btile_t));
 		for (int i = 0; i < ntl; i++) p->btiles[i] = tiles[ord[i]];
 		p->nbtiles = ntl;
@@ -1147,8 +1140,7 @@ int jn_plan_build_units(jn_plan_t *p, int target_units, char *err, size_t errlen
 			uc[u] = cst;
 			ord[u] = u;
 		}
-		g_unit_cost = uc;
-		qsort(ord, p->nunits, sizeof(int), cmp_unit_cost);
+		qsort_r(ord, p->nunits, sizeof(int), cmp_cost_desc, uc);
 		jn_unit_t *sorted = malloc((p->nunits ? p->nunits : 1) * sizeof(jn_unit_t));
 		for (int u = 0; u < p->nunits; u++) sorted[u] = p->units[ord[u]];
 		free(p->units);
