@@ -199,3 +199,34 @@ def test_plans_do_not_depend_on_the_host_thread_count(problem, name, monkeypatch
         digests.append(L.emu_plan_digest(h))
         L.emu_close(h)
     assert digests[0] != 0 and digests[0] == digests[1] == digests[2]
+
+
+def test_plans_built_concurrently_match(problem):
+    """Plans opened from several threads at once (each build uses all host
+    cores) equal the plans built one after another: the builds share no state."""
+    import threading
+    names = ["he4_n4_2b", "li6_n2_3b", "he4_n2_3b", "he4_n4_2b"]
+    probs = [problem(n) for n in names]
+
+    def digest(d, Z, N):
+        L, h, err = open_plan(d, Z, N)
+        assert h, err
+        L.emu_plan_digest.restype = ctypes.c_uint64
+        L.emu_plan_digest.argtypes = [ctypes.c_void_p]
+        v = L.emu_plan_digest(h)
+        L.emu_close(h)
+        return v
+
+    want = [digest(d, Z, N) for d, Z, N, *_ in probs]
+    got = [None] * len(probs)
+
+    def run(i):
+        d, Z, N, *_ = probs[i]
+        got[i] = digest(d, Z, N)
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(len(probs))]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert got == want and all(want)
