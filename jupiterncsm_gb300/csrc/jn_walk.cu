@@ -48,7 +48,7 @@
 
 #include <type_traits>
 
-#define WALK_WARPS 1     /* one warp a CTA: the register file, not CTA granularity, sets the warps an SM holds */
+#define WALK_WARPS 1     /* one warp a CTA: 32 resident CTAs an SM, the most the integer path's 63 registers allow too */
 #define WALK_THREADS (WALK_WARPS * 32)
 #define WALK_SLOTS (JN_WALK_RS * 32)    /* per warp: one 64-bit slot per (destination row, lane) */
 #define WALK_SMEM ((size_t)WALK_WARPS * WALK_SLOTS * sizeof(unsigned long long))
