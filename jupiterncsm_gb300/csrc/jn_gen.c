@@ -67,12 +67,14 @@
 
 #include <errno.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
 #include <sys/types.h>
+#include <unistd.h>
 
 #define MAXW 8            /* 512 orbitals per species */
 #define SIGN_BIT 0x80000000u
@@ -803,13 +805,17 @@ static size_t list_conns(const kst_t *t, int depth, int dE, int dM, int **pairs)
 	return n;
 }
 
+/* quiet: leave the error text alone (the block writers on several threads) */
 static int write_me_block(const gen_t *g, const meblk_t *b, const char *dir, uint64_t seed,
-			  double sigma, int with_ho)
+			  double sigma, int with_ho, int quiet)
 {
 	char path[4096];
 	snprintf(path, sizeof path, "%s/%d_matrix_elements", dir, b->id);
 	FILE *f = fopen(path, "wb");
-	if (!f) FAIL(JN_GEN_EIO, "cannot open %s: %s", path, strerror(errno));
+	if (!f) {
+		if (quiet) return JN_GEN_EIO;
+		FAIL(JN_GEN_EIO, "cannot open %s: %s", path, strerror(errno));
+	}
 	size_t nd_n = b->kn ? b->nn_conn : 0, nd_p = b->kp ? b->np_conn : 0;
 	fwrite(&nd_n, sizeof(size_t), 1, f);
 	fwrite(&nd_p, sizeof(size_t), 1, f);
@@ -833,11 +839,93 @@ static int write_me_block(const gen_t *g, const meblk_t *b, const char *dir, uin
 			}
 			buf[in] = me_value(g, b->kp, b->kn, ap, bp, an, bn, seed, sigma, with_ho);
 		}
-		if (fwrite(buf, sizeof(double), row, f) != row) { fclose(f); FAIL(JN_GEN_EIO, "short write %s", path); }
+		if (fwrite(buf, sizeof(double), row, f) != row) {
+			fclose(f);
+			free(buf); free(pp); free(pn);
+			if (quiet) return JN_GEN_EIO;
+			FAIL(JN_GEN_EIO, "short write %s", path);
+		}
 	}
 	free(buf); free(pp); free(pn);
-	if (fclose(f) != 0) FAIL(JN_GEN_EIO, "close %s", path);
+	if (fclose(f) != 0) {
+		if (quiet) return JN_GEN_EIO;
+		FAIL(JN_GEN_EIO, "close %s", path);
+	}
 	return 0;
+}
+
+/* The matrix-element blocks, written by all host cores (at most 32 threads,
+ * fewer when JN_HOST_THREADS caps them).  Every element is a counter-based
+ * deviate of its own indices and every block is its own file, so the files
+ * do not depend on the thread count.  A failing block is written once more
+ * on its own for the error text. */
+typedef struct {
+	const gen_t *g;
+	const char *dir;
+	const size_t *blk;      /* the blocks to write, in order */
+	size_t n, next;
+	int *rc;
+} mejob_t;
+
+static uint64_t me_seed(const gen_t *g, const meblk_t *b)
+{
+	return g->cfg.seed * 1000003ull + (uint64_t)(b->kp + b->kn);
+}
+
+static double me_sigma(const gen_t *g, const meblk_t *b)
+{
+	return (b->kp + b->kn == 3) ? g->cfg.sigma3 : g->cfg.sigma2;
+}
+
+static void *me_worker(void *v)
+{
+	mejob_t *j = (mejob_t *)v;
+	const meblk_t *M = j->g->mes.a;
+	for (;;) {
+		const size_t i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+		if (i >= j->n) break;
+		const meblk_t *b = &M[j->blk[i]];
+		j->rc[i] = write_me_block(j->g, b, j->dir, me_seed(j->g, b), me_sigma(j->g, b), j->g->cfg.hbar_omega != 0.0, 1);
+	}
+	return NULL;
+}
+
+static int write_me_blocks(const gen_t *g, const char *dir)
+{
+	const meblk_t *M = g->mes.a;
+	size_t n = 0;
+	size_t *blk = xcalloc(g->mes.n, sizeof(size_t));
+	int *rc = xcalloc(g->mes.n, sizeof(int));
+	if (!blk || !rc) { free(blk); free(rc); FAIL(JN_GEN_ENOMEM, "out of memory"); }
+	for (size_t i = 0; i < g->mes.n; i++) {
+		if (!M[i].id) continue;
+		if (g->cfg.antoine && M[i].kp + M[i].kn == 2) continue;   /* left to the J->M transform */
+		blk[n++] = i;
+	}
+	long nt = sysconf(_SC_NPROCESSORS_ONLN);
+	const char *cap = getenv("JN_HOST_THREADS");
+	if (cap && atol(cap) > 0 && atol(cap) < nt) nt = atol(cap);
+	if (nt > 32) nt = 32;
+	if (nt < 1) nt = 1;
+	mejob_t j = { g, dir, blk, n, 0, rc };
+	pthread_t th[32];
+	int started = 0;
+	for (long t = 1; t < nt; t++)
+		if (pthread_create(&th[started], NULL, me_worker, &j) == 0) started++;
+	me_worker(&j);
+	for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+	int out = 0;
+	for (size_t i = 0; i < n && !out; i++)
+		if (rc[i]) {
+			const meblk_t *b = &M[blk[i]];
+			out = write_me_block(g, b, dir, me_seed(g, b), me_sigma(g, b), g->cfg.hbar_omega != 0.0, 0);
+			if (!out) {
+				out = rc[i];
+				snprintf(g_err, sizeof g_err, "writing matrix-element block %d failed", b->id);
+			}
+		}
+	free(blk); free(rc);
+	return out;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1273,13 +1361,7 @@ int jn_generate(const jn_gen_config *cfg, const char *outdir, jn_gen_summary *su
 		const char *medir = cfg->me_subdir && cfg->me_subdir[0] ? cfg->me_subdir : "matrix_elements";
 		snprintf(path, sizeof path, "%s/%s", outdir, medir);
 		if (mkdir_p(path)) { rc = JN_GEN_EIO; snprintf(g_err, sizeof g_err, "mkdir %s", path); goto done; }
-		for (size_t i = 0; i < g->mes.n; i++) {
-			if (!M[i].id) continue;
-			if (cfg->antoine && M[i].kp + M[i].kn == 2) continue;   /* left to the J->M transform */
-			double sigma = (M[i].kp + M[i].kn == 3) ? cfg->sigma3 : cfg->sigma2;
-			uint64_t seed = cfg->seed * 1000003ull + (M[i].kp + M[i].kn);
-			if ((rc = write_me_block(g, &M[i], path, seed, sigma, cfg->hbar_omega != 0.0))) goto done;
-		}
+		if ((rc = write_me_blocks(g, path))) goto done;
 	}
 	if (cfg->antoine) {
 		snprintf(path, sizeof path, "%s/antoine_2nf.bin", outdir);
