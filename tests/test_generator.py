@@ -30,6 +30,17 @@ def test_two_runs_are_bit_identical(tmp_path):
     assert tree_digest(a) == tree_digest(b)
 
 
+def test_files_do_not_depend_on_the_host_thread_count(tmp_path, monkeypatch):
+    """The matrix-element blocks are written by all host cores; one thread
+    (JN_HOST_THREADS=1) writes the same files."""
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    monkeypatch.setenv("JN_HOST_THREADS", "1")
+    jn.generate(a, nmax=4, nbody=3)
+    monkeypatch.delenv("JN_HOST_THREADS")
+    jn.generate(b, nmax=4, nbody=3)
+    assert tree_digest(a) == tree_digest(b)
+
+
 @pytest.mark.parametrize("name", ["he4_n2_2b", "he4_n2_3b", "li6_n2_3b"])
 def test_index_lists_bit_exact_against_restatement(problem, name):
     d, Z, N, nmax, nbody = problem(name)
