@@ -1,5 +1,6 @@
 """The C-ABI library loads and exports every symbol include/*.h declares.
-No compute call is made here (this suite runs without a GPU)."""
+No device call is made here (this suite runs without a GPU); the host-only
+plan statistics are checked against the files."""
 import ctypes
 import glob
 import os
@@ -39,3 +40,26 @@ def test_null_arguments_are_rejected_without_a_device():
     assert L.jn_open_files(None, None, None, None, 2, 2, ctypes.byref(h)) == 1
     assert L.jn_matvec(None, None, None) == 1
     assert L.jn_get_plan_stats(None, None) == 1
+
+
+def test_host_inspect_matches_the_files(problem):
+    """jn_inspect_files builds the plan on the host (no device): its statistics
+    agree with counts taken from the files and with the oracle's dimension."""
+    import numpy as np
+    import oracle
+    d, Z, N, *_ = problem("li6_n2_3b")
+    st = jn.inspect(d, Z, N)
+    P = oracle.Port(d)
+    assert st["dimension"] == P.dimension
+    P.close()
+    lists = os.listdir(os.path.join(d, "index_lists"))
+    entries = sum(os.path.getsize(os.path.join(d, "index_lists", f)) // 12 for f in lists)
+    mes = os.listdir(os.path.join(d, "matrix_elements"))
+    elements = sum((os.path.getsize(os.path.join(d, "matrix_elements", f)) - 16) // 8 for f in mes)
+    assert st["list_entries"] == entries and st["me_elements"] == elements
+    assert 0 < st["me_referenced"] <= st["me_elements"]
+    assert st["algorithmic_bytes"] == 12.0 * entries + 8.0 * st["me_referenced"] + 16.0 * st["dimension"]
+    assert st["num_work_units"] > 0 and st["num_tiles"] > 0 and st["multiply_adds"] > 0
+    assert st["num_instructions"] == sum(1 for l in open(os.path.join(d, "evaluation_order.txt")) if "BLOCK:" in l
+                                         and "UNLOAD_" not in l)
+    np.testing.assert_equal(jn.inspect(d, Z, N), st)          # deterministic
