@@ -230,3 +230,35 @@ def test_plans_built_concurrently_match(problem):
     for t in ts:
         t.join()
     assert got == want and all(want)
+
+
+def test_empty_lists_match_port(problem, tmp_path):
+    """Index lists with no entries (0-byte files; the reference reads size / 12
+    triples) contribute nothing: every engine's model still matches the oracle
+    and the walk plan stays sound."""
+    d0, Z, N, *_ = problem("he4_n2_3b")
+    d = corrupt_copy(d0, str(tmp_path / "c"))
+    names = sorted(os.listdir(f"{d}/index_lists"), key=lambda s: int(s.split("_")[-1]))
+    for n in names[:3] + names[-2:]:
+        open(f"{d}/index_lists/{n}", "wb").close()
+    L, h, err = open_plan(d, Z, N)
+    assert h, err
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(3).standard_normal(D)
+    want = oracle.Port(d).matvec(x)
+    scale = np.abs(want).max()
+    y = np.zeros(D)
+    L.emu_matvec(h, x.ctypes.data, y.ctypes.data, 0)
+    assert np.abs(y - want).max() <= 1e-12 * scale
+    for fn, modes in (("emu_matvec3", ((0, 1e-12), (1, 2e-6))), ("emu_matvec4", ((0, 1e-12), (1, 2e-6))),
+                      ("emu_matvec5", ((1, 1e-12), (64, 1e-12), (32, 2e-6)))):
+        f = getattr(L, fn)
+        f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+        for mode, tol in modes:
+            y = np.zeros(D)
+            assert f(h, x.ctypes.data, y.ctypes.data, 0, mode) == 0, (fn, mode)
+            assert np.abs(y - want).max() <= tol * scale, (fn, mode)
+    L.emu_walk_validate.restype = ctypes.c_int64
+    L.emu_walk_validate.argtypes = [ctypes.c_void_p]
+    assert L.emu_walk_validate(h) == 0
+    L.emu_close(h)
