@@ -191,6 +191,33 @@ def test_panel_engine_rounds_ties_to_even(problem):
     H.close()
 
 
+def test_empty_lists_on_every_engine(problem, tmp_path):
+    """Index lists with no entries (0-byte files) contribute nothing: every
+    engine at both precisions matches the oracle on the same files."""
+    import shutil
+    d0, Z, N, *_ = problem("he4_n2_3b")
+    d = str(tmp_path / "empty")
+    shutil.copytree(d0, d)
+    names = sorted(os.listdir(f"{d}/index_lists"), key=lambda s: int(s.split("_")[-1]))
+    for n in names[:3] + names[-2:]:
+        open(f"{d}/index_lists/{n}", "wb").close()
+    port = oracle.Port(d)
+    x = np.random.default_rng(5).standard_normal(port.dimension)
+    want = port.matvec(x)
+    port.close()
+    scale = np.abs(want).max()
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    try:
+        for engine in (3, 4, 5):
+            H.set_engine(engine)
+            for bits, tol in ((64, 1e-12), (32, 2e-6)):
+                H.set_precision(bits)
+                got = H.matvec(x)
+                assert np.abs(got - want).max() <= tol * scale, (engine, bits)
+    finally:
+        H.close()
+
+
 def test_engines_agree(problem):
     d, Z, N, *_ = problem("he4_n6_3b")
     H = jn.Hamiltonian.from_dir(d, Z, N)
