@@ -99,11 +99,19 @@ jn_status jn_block_info(const jn_ctx *ctx, int b, int *id, size_t *offset, size_
  * (Minerva/scheduler/scheduler.c:80-145), whose output blocks are also
  * accumulated into (Minerva/vector_block/vector_block.c:49-99).
  * Deterministic: the same inputs give bit-identical y.
+ * Range: every product but engine 2's at precision 64 sums in 64-bit fixed
+ * point, with x bounded in FP32.  It is exact to FP64 level while
+ * max|x| < 2^127 and abs_bound * max|x| lies in [2^-47, 2^121), where
+ * abs_bound bounds |H| row sums (a normalised vector, as in Lanczos, is
+ * always inside).  Outside that range this call returns JN_ERR_INVALID
+ * instead of a wrong result; x = 0 is always accepted.
  */
 jn_status jn_matvec(jn_ctx *ctx, const double *x, double *y);
 
 /* y += H x (accumulate = 1) or y = H x (accumulate = 0) on DEVICE pointers,
- * enqueued on `stream` (a cudaStream_t, NULL for the context's stream). */
+ * enqueued on `stream` (a cudaStream_t, NULL for the context's stream).
+ * The caller keeps x inside jn_matvec's range: it is not checked here,
+ * which would take a synchronisation. */
 jn_status jn_matvec_device(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, void *stream);
 
 /*

@@ -854,9 +854,37 @@ extern "C" jn_status jn_matvec_profile(jn_ctx *c, const double *d_x, double *d_y
 	return JN_OK;
 }
 
+/* The fixed-point products (every engine but engine 2 at precision 64) bound
+ * max|x| as an FP32 number and choose their unit 2^-S from abs_bound *
+ * max|x|, with S kept in [-60, 100].  They are exact to FP64 level while
+ * max|x| < 2^127 and abs_bound * max|x| lies in [2^-47, 2^121) (below 2^-38
+ * the largest element still keeps at least 53 bits); outside that range a
+ * result would be wrong or degraded, so the host-array entry points refuse
+ * it.  x = 0 and all-zero matrix elements give exact zeros. */
+static jn_status check_x_range(const jn_ctx *c, const double *x)
+{
+	if (c->engine == 2 && c->precision == 64) return JN_OK;
+	double m = 0.0;
+	for (int64_t i = 0; i < c->plan.dim; i++) {
+		const double a = fabs(x[i]);
+		if (!(a <= m)) m = a;           /* NaN is kept */
+	}
+	if (m == 0.0 || c->plan.abs_bound == 0.0) return JN_OK;
+	if (!(m < 0x1p127))
+		return fail(JN_ERR_INVALID, "max|x| = %g: the product bounds x in FP32 and needs max|x| < 2^127 "
+			    "(scale x by a power of two, or select engine 2 at precision 64)", m);
+	const double yb = c->plan.abs_bound * m;
+	if (!(yb >= 0x1p-47 && yb < 0x1p121))
+		return fail(JN_ERR_INVALID, "abs_bound * max|x| = %g is outside the fixed-point product's range [2^-47, 2^121) "
+			    "(scale x by a power of two, or select engine 2 at precision 64)", yb);
+	return JN_OK;
+}
+
 extern "C" jn_status jn_matvec(jn_ctx *c, const double *x, double *y)
 {
 	if (!c || !x || !y) return fail(JN_ERR_INVALID, "null argument");
+	jn_status rs = check_x_range(c, x);
+	if (rs) return rs;
 	const size_t bytes = (size_t)c->plan.dim * sizeof(double);
 	CUDA_TRY(cudaMemcpyAsync(c->d_x, x, bytes, cudaMemcpyHostToDevice, c->stream));
 	CUDA_TRY(cudaMemcpyAsync(c->d_y, y, bytes, cudaMemcpyHostToDevice, c->stream));

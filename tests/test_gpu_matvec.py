@@ -218,6 +218,37 @@ def test_empty_lists_on_every_engine(problem, tmp_path):
         H.close()
 
 
+def test_out_of_range_x_is_refused_and_scaling_is_exact(problem):
+    """The fixed-point products refuse an x outside their range instead of
+    returning a wrong result (engine 2 at precision 64, plain FP64 sums,
+    takes it and matches the oracle); x = 0 gives exact zeros; and inside the
+    range, scaling x by 2^60 scales y by 2^60 bit for bit."""
+    d, Z, N, *_ = problem("he4_n2_3b")
+    port = oracle.Port(d)
+    H = jn.Hamiltonian.from_dir(d, Z, N)
+    D = H.dimension
+    huge, tiny = np.full(D, 1e300), np.full(D, 5e-324)
+    x = np.random.default_rng(9).standard_normal(D)
+    try:
+        for engine in (3, 4, 5):
+            H.set_engine(engine)
+            for bits in (64, 32):
+                H.set_precision(bits)
+                assert np.array_equal(H.matvec(np.zeros(D)), np.zeros(D)), (engine, bits)
+                for bad in (huge, tiny):
+                    with pytest.raises(jn.JnError):
+                        H.matvec(bad)
+                a, b = H.matvec(x), H.matvec(x * 2.0 ** 60)
+                assert np.array_equal(b, a * 2.0 ** 60), (engine, bits)
+        H.set_engine(2)
+        H.set_precision(64)
+        want = port.matvec(huge)
+        assert np.abs(H.matvec(huge) - want).max() <= 1e-12 * np.abs(want).max()
+    finally:
+        H.close()
+        port.close()
+
+
 def test_engines_agree(problem):
     d, Z, N, *_ = problem("he4_n6_3b")
     H = jn.Hamiltonian.from_dir(d, Z, N)
