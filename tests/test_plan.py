@@ -262,3 +262,28 @@ def test_empty_lists_match_port(problem, tmp_path):
     L.emu_walk_validate.argtypes = [ctypes.c_void_p]
     assert L.emu_walk_validate(h) == 0
     L.emu_close(h)
+
+
+@pytest.mark.parametrize("name", ["he4_n2_3b", "li6_n2_3b"])
+def test_power_of_two_scaling_is_exact_in_the_models(problem, name):
+    """Inside the fixed-point range, x scaled by 2^60 (or 2^-40) gives y scaled
+    by the same power of two, bit for bit, in every engine's model and
+    arithmetic: the unit exponent moves with max|x| and nothing else rounds
+    differently."""
+    d, Z, N, *_ = problem(name)
+    L, h, err = open_plan(d, Z, N)
+    assert h, err
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(11).standard_normal(D)
+    for fn, modes in (("emu_matvec3", (0, 1)), ("emu_matvec4", (0, 1)), ("emu_matvec5", (1, 64, 32))):
+        f = getattr(L, fn)
+        f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+        for mode in modes:
+            a = np.zeros(D)
+            assert f(h, x.ctypes.data, a.ctypes.data, 0, mode) == 0
+            for k in (60, -40):
+                xs = x * 2.0 ** k
+                b = np.zeros(D)
+                assert f(h, xs.ctypes.data, b.ctypes.data, 0, mode) == 0
+                assert np.array_equal(b, a * 2.0 ** k), (fn, mode, k)
+    L.emu_close(h)
