@@ -310,7 +310,11 @@ typedef struct {
 /* Run Lanczos on the context's Hamiltonian.  Replaces new_lanczos_environment
  * + diagonalize (Bacchus/lanczos/lanczos.c:37-253).  The Krylov basis stays
  * on the device.  Returns JN_ERR_NOT_CONVERGED (results still filled) when
- * JN_LANCZOS_FULL stops at max_iterations. */
+ * JN_LANCZOS_FULL stops at max_iterations.  The Krylov vectors are
+ * normalised (max|x| between D^-1/2 and 1), so the products stay inside
+ * jn_matvec's range whenever the matrix elements' row-sum bound lies in
+ * [2^-47 D^1/2, 2^121): any Hamiltonian in MeV.  The same holds for the
+ * batched solvers. */
 jn_status jn_lanczos(jn_ctx *ctx, const jn_lanczos_options *options, jn_lanczos_result *result);
 
 /* All Ritz values of the last solve in ascending order, as get_eigensystem +
