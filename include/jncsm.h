@@ -140,7 +140,11 @@ jn_status jn_matvec_files(jn_ctx *ctx, const char *output_vector_directory, cons
  * (cudaGetSymbolAddress) and caches it for the life of the process; make
  * that first call before any stream capture.  The cached address does not
  * survive cudaDeviceReset: do not call this entry point on a device after
- * resetting it.  No counterpart in the reference, which has no device memory.
+ * resetting it.  A basis with a sub-basis wider than a block-tile row (more
+ * than 8 191 neutron states in one block) has no block-tile engine: this
+ * entry point, engine 3 and the batched solvers then return JN_ERR_INVALID
+ * with the reason, while jn_open, the walk engine and jn_lanczos work.  No
+ * counterpart in the reference, which has no device memory.
  */
 #define JN_NOALLOC_MAX_DIM 262144
 jn_status jn_matvec_device_noalloc(jn_ctx *ctx, const double *d_x, double *d_y, int accumulate, void *stream);

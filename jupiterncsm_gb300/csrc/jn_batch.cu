@@ -692,6 +692,8 @@ extern "C" jn_status jn_lanczos_batch(jn_ctx *c, const jn_batch_options *o, jn_b
 	const int64_t D = p->dim, nme = p->n_me;
 	if (B < 1 || B > 4096) return jn_fail(JN_ERR_INVALID, "num_instances must be in 1..4096");
 	if (D < 1) return jn_fail(JN_ERR_INVALID, "empty basis");
+	if (p->btiles_off)
+		return jn_fail(JN_ERR_INVALID, "the batched solver's FP64 refinement needs the block-tile engine: %s", p->btiles_why);
 	jn_status st = batch_check_options(o);
 	if (st) return st;
 	if (o->num_eigenvectors && !o->eigenvectors)
@@ -793,6 +795,9 @@ extern "C" jn_status jn_lanczos_batch_bases(jn_ctx *const *ctxs, int num_bases, 
 	for (int b = 0; b < num_bases; b++) {
 		const jn_batch_options *ob = &options[b];
 		if (!ctxs[b] || !results[b] || !ob->matrix_elements) return jn_fail(JN_ERR_INVALID, "null argument for basis %d", b);
+		if (ctxs[b]->plan.btiles_off)
+			return jn_fail(JN_ERR_INVALID, "basis %d: the batched solver's FP64 refinement needs the block-tile engine: %s", b,
+				       ctxs[b]->plan.btiles_why);
 		if (ob->num_instances < 1) return jn_fail(JN_ERR_INVALID, "basis %d: num_instances must be >= 1", b);
 		if (ob->max_iterations != o->max_iterations || ob->num_eigenvalues != o->num_eigenvalues ||
 		    ob->tolerance != o->tolerance || ob->precision != o->precision || ob->check_every != o->check_every ||

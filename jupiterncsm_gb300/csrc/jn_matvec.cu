@@ -659,6 +659,7 @@ jn_status jn_enqueue_tiles(jn_ctx *c, const double *d_x, double *d_y, int accumu
 			   int clear_acc)
 {
 	const jn_plan_t *p = &c->plan;
+	if (p->btiles_off) return fail(JN_ERR_INVALID, "no block-tile engine: %s", p->btiles_why);
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
 	const int f32 = c->precision == 32;
 	if (f32 && !c->d_me32) return fail(JN_ERR_INVALID, "FP32 matrix elements are not set up");
@@ -696,6 +697,7 @@ jn_status jn_enqueue_batched(jn_ctx *c, int B, int f32, const void *me, int64_t 
 {
 	const jn_plan_t *p = &c->plan;
 	if (B < 1 || B > 65535) return fail(JN_ERR_INVALID, "batch of %d instances", B);
+	if (p->btiles_off) return fail(JN_ERR_INVALID, "no block-tile engine: %s", p->btiles_why);
 	DevPlan P = { c->d_rowptr, c->d_ent, c->d_me, c->d_terms, c->d_tiles, c->d_units, c->d_unit_terms };
 	int g = (int)((p->dim + 255) / 256);
 	if (g > 256) g = 256;
@@ -782,6 +784,7 @@ static jn_status units_setup(jn_ctx *c)
 extern "C" jn_status jn_set_engine(jn_ctx *c, int engine)
 {
 	if (!c || engine < 2 || engine > 5) return fail(JN_ERR_INVALID, "engine must be 2, 3, 4 or 5");
+	if (engine == 3 && c->plan.btiles_off) return fail(JN_ERR_INVALID, "no block-tile engine: %s", c->plan.btiles_why);
 	if (engine == 2) {
 		jn_status s = units_setup(c);
 		if (s) return s;

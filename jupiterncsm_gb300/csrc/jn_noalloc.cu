@@ -60,6 +60,7 @@ extern "C" jn_status jn_matvec_device_noalloc(jn_ctx *c, const double *d_x, doub
 {
 	if (!c || !d_x || !d_y) return jn_fail(JN_ERR_INVALID, "null argument");
 	if (d_x == d_y) return jn_fail(JN_ERR_INVALID, "x and y must not alias");
+	if (c->plan.btiles_off) return jn_fail(JN_ERR_INVALID, "no block-tile engine: %s", c->plan.btiles_why);
 	const int64_t D = c->plan.dim;
 	if (D > JN_NOALLOC_MAX_DIM)
 		return jn_fail(JN_ERR_INVALID,

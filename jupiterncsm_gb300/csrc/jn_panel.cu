@@ -887,6 +887,7 @@ static jn_status autotune(jn_ctx *c, int trials, int tune_engine, jn_tuning *out
 	for (int eng = 5; eng >= 3; eng -= 2) {
 		if (!(tune_engine || engine0 == eng)) continue;
 		if (eng == 5 && jn_walk_setup(c) != JN_OK) continue;
+		if (eng == 3 && p->btiles_off) continue;        /* no block tiles for this plan */
 		float ms;
 		c->engine = eng;
 		jn_status s = time_product(c, trials, &ms, flush, flush_bytes);

@@ -663,8 +663,7 @@ static void tiles_block(int64_t bi, void *v)
 	const double *tmax = J->tmax;
 	if (B->Np == 0 || B->Nn == 0) return;
 	const int64_t stride = B->Nn | 1;
-	if (stride > TILE_SMEM_ELEMS) { o->status = 2; return; }
-	/* |M| bound per element of this block */
+	/* |M| bound per element of this block (needed by every engine, tiles or not) */
 	const size_t E = (size_t)(B->Np * B->Nn);
 	double *bound = calloc(E ? E : 1, sizeof(double));
 	if (!bound) { o->status = 1; return; }
@@ -681,6 +680,7 @@ static void tiles_block(int64_t bi, void *v)
 	}
 	for (size_t e = 0; e < E; e++) o->abs_bound = fmax(o->abs_bound, bound[e]);
 	free(bound);
+	if (stride > TILE_SMEM_ELEMS) { o->status = 2; return; }
 	int64_t tcap = 0;
 	int rcap = 0;
 #define PUSH_TASK(TERM, KIND, COUNT, LANE_BASE, LOOP_BASE, LOOP_LEN, COST)                     \
@@ -770,6 +770,29 @@ static void tiles_block(int64_t bi, void *v)
 		if (el > o->max_el) o->max_el = (int)el;
 	}
 #undef PUSH_TASK
+}
+
+/* compact term descriptions read by the tile kernel */
+static int build_tterms(jn_plan_t *p, char *err, size_t errlen)
+{
+	p->tterms = calloc(p->nterms ? p->nterms : 1, sizeof(jn_tterm_t));
+	if (!p->tterms) {
+		if (err) snprintf(err, errlen, "out of host memory");
+		return 1;
+	}
+	for (int t = 0; t < p->nterms; t++) {
+		const jn_term_t *T = &p->terms[t];
+		if (T->src_off > 0x7fffffffll) {
+			if (err) snprintf(err, errlen, "vector too long for 32-bit block offsets");
+			return 1;
+		}
+		p->tterms[t].me_off = T->me_off;
+		p->tterms[t].src_off = (int32_t)T->src_off;
+		p->tterms[t].nd = T->nd;
+		p->tterms[t].Nn_src = T->Nn_src;
+		p->tterms[t].transpose = T->transpose;
+	}
+	return 0;
 }
 
 /* The second pass for one row range: its tiles of similar work and their
@@ -908,11 +931,29 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	tiles_job_t job = { p, cnt, byb, tmax, bt };
 	jn_par_for(p->nblocks, tiles_block, &job);
 	int64_t ntasks = 0;
-	int nranges = 0, status = 0, bad_block = -1;
+	int nranges = 0, status = 0, wide = -1;
 	for (int b = 0; b < p->nblocks; b++) {
-		if (bt[b].status && !status) { status = bt[b].status; bad_block = b; }
+		if (bt[b].status == 1) status = 1;
+		if (bt[b].status == 2 && wide < 0) wide = b;
 		ntasks += bt[b].ntasks;
 		nranges += bt[b].nranges;
+	}
+	if (wide >= 0 && !status) {
+		/* a block row wider than one shared-memory tile: no block tiles, so
+		   engine 3 (and what runs on it) is unavailable for this plan; the
+		   bound and the term descriptions, which other engines use, are built */
+		p->abs_bound = 0;
+		for (int b = 0; b < p->nblocks; b++) {
+			p->abs_bound = fmax(p->abs_bound, bt[b].abs_bound);
+			free(bt[b].tasks); free(bt[b].ranges);
+		}
+		free(bt); free(tmax); free(cnt); free(byb);
+		p->max_tile_elems = 0;
+		p->btiles_off = 1;
+		snprintf(p->btiles_why, sizeof p->btiles_why,
+			 "basis block %d has %lld neutron states: more than one shared-memory row of the block-tile engine (%d)",
+			 p->blocks[wide].id, (long long)p->blocks[wide].Nn, TILE_SMEM_ELEMS - 1);
+		return build_tterms(p, err, errlen);
 	}
 	tile_range_t *ranges = status ? NULL : malloc((nranges ? nranges : 1) * sizeof *ranges);
 	task_cost_t *tasks = status ? NULL : malloc((ntasks ? ntasks : 1) * sizeof *tasks);
@@ -920,11 +961,7 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 	if (status) {
 		for (int b = 0; b < p->nblocks; b++) { free(bt[b].tasks); free(bt[b].ranges); }
 		free(bt); free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
-		if (err && status == 2)
-			snprintf(err, errlen, "basis block %d has %lld neutron states: more than one shared-memory tile row",
-				 p->blocks[bad_block].id, (long long)p->blocks[bad_block].Nn);
-		else if (err)
-			snprintf(err, errlen, "out of host memory");
+		if (err) snprintf(err, errlen, "out of host memory");
 		return 1;
 	}
 	double total = 0;
@@ -956,20 +993,9 @@ static int build_block_tiles(jn_plan_t *p, const int *term_dst, int target_units
 		if (err) snprintf(err, errlen, "too many terms for the packed task format");
 		return 1;
 	}
-	/* compact term descriptions */
-	p->tterms = calloc(p->nterms ? p->nterms : 1, sizeof(jn_tterm_t));
-	for (int t = 0; t < p->nterms; t++) {
-		const jn_term_t *T = &p->terms[t];
-		if (T->src_off > 0x7fffffffll) {
-			free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
-			if (err) snprintf(err, errlen, "vector too long for 32-bit block offsets");
-			return 1;
-		}
-		p->tterms[t].me_off = T->me_off;
-		p->tterms[t].src_off = (int32_t)T->src_off;
-		p->tterms[t].nd = T->nd;
-		p->tterms[t].Nn_src = T->Nn_src;
-		p->tterms[t].transpose = T->transpose;
+	if (build_tterms(p, err, errlen)) {
+		free(tmax); free(cnt); free(byb); free(tasks); free(ranges);
+		return 1;
 	}
 	/* pass 2: tiles of similar work.  Inside a tile, tasks of one kind and
 	 * similar width are packed into warp items (one task per 8, 16 or 32

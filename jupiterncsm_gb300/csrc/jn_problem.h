@@ -275,6 +275,8 @@ typedef struct {
 	int64_t n_unit_terms; int32_t *unit_terms;
 	int64_t n_partial;
 	int nbtiles;       jn_btile_t *btiles;
+	int btiles_off;                 /* no block tiles (engine 3 unavailable): a block row is wider than a tile */
+	char btiles_why[256];
 	int64_t npieces;   jn_piece_t *pieces;
 	jn_tterm_t *tterms;             /* nterms compact term descriptions */
 	int64_t nwalks;    uint32_t *walks;    /* pairs {w0, len | idx << 16} */

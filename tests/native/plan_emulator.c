@@ -58,6 +58,7 @@ void *emu_open(const char *comb, const char *order, const char *lists, const cha
 }
 
 long emu_dimension(void *h) { return (long)((jn_plan_t *)h)->dim; }
+int emu_btiles_off(void *h) { return ((jn_plan_t *)h)->btiles_off; }
 int emu_units(void *h) { return ((jn_plan_t *)h)->nunits; }
 int emu_tiles(void *h) { return ((jn_plan_t *)h)->ntiles; }
 

@@ -120,3 +120,30 @@ def test_large_basis_block_tile_engine(large):
     got = H.matvec(x)
     assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
     H.close()
+
+
+def test_wide_neutron_basis_runs_on_the_walk_engine(tmp_path):
+    """4 neutrons at Nmax 8 (D = 30 626; a sub-basis of 23 868 states, wider
+    than a block-tile row): the context opens, the walk engine's products at
+    both precisions match the oracle, and what needs the block tiles (engine
+    3, the batched solver) is refused with the reason."""
+    d = str(tmp_path / "n4")
+    jn.generate(d, Z=0, N=4, nmax=8, nbody=2, basis_files=False)
+    port = oracle.Port(d)
+    x = np.random.default_rng(4).standard_normal(port.dimension)
+    want = port.matvec(x)
+    port.close()
+    scale = np.abs(want).max()
+    H = jn.Hamiltonian.from_dir(d, 0, 4)
+    try:
+        assert H.active_engine() == 5
+        for bits, tol in ((64, 1e-12), (32, 2e-6)):
+            H.set_precision(bits)
+            assert np.abs(H.matvec(x) - want).max() <= tol * scale, bits
+        with pytest.raises(jn.JnError, match="block-tile"):
+            H.set_engine(3)
+        me = H.read_matrix_elements(os.path.join(d, "matrix_elements"))
+        with pytest.raises(jn.JnError, match="block-tile"):
+            H.lanczos_batch([me], num_eigenvalues=2, max_iterations=20)
+    finally:
+        H.close()

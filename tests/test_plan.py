@@ -287,3 +287,32 @@ def test_power_of_two_scaling_is_exact_in_the_models(problem, name):
                 assert f(h, xs.ctypes.data, b.ctypes.data, 0, mode) == 0
                 assert np.array_equal(b, a * 2.0 ** k), (fn, mode, k)
     L.emu_close(h)
+
+
+def test_wide_neutron_basis_opens_without_block_tiles(tmp_path):
+    """4 neutrons at Nmax 8 (D = 30 626) have a sub-basis of 23 868 states,
+    wider than a block-tile row.  The plan still opens: the block tiles are
+    marked unavailable, and the walk engine's model matches the oracle."""
+    import jupiterncsm_gb300 as jn
+    d = str(tmp_path / "n4")
+    jn.generate(d, Z=0, N=4, nmax=8, nbody=2, basis_files=False)
+    L, h, err = open_plan(d, 0, 4)
+    assert h, err
+    L.emu_btiles_off.argtypes = [ctypes.c_void_p]
+    assert L.emu_btiles_off(h) == 1
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(2).standard_normal(D)
+    port = oracle.Port(d)
+    want = port.matvec(x)
+    port.close()
+    scale = np.abs(want).max()
+    L.emu_matvec5.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+    for mode, tol in ((1, 1e-12), (64, 1e-12), (32, 2e-6)):
+        y = np.zeros(D)
+        assert L.emu_matvec5(h, x.ctypes.data, y.ctypes.data, 0, mode) == 0
+        assert np.abs(y - want).max() <= tol * scale, mode
+    L.emu_walk_validate.restype = ctypes.c_int64
+    L.emu_walk_validate.argtypes = [ctypes.c_void_p]
+    assert L.emu_walk_validate(h) == 0
+    L.emu_close(h)
+    assert jn.inspect(d, 0, 4)["dimension"] == D
