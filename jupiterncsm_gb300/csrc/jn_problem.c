@@ -1181,6 +1181,26 @@ int jn_plan_build_units(jn_plan_t *p, int target_units, char *err, size_t errlen
 	return 0;
 }
 
+/* one list's bound checks: the first entry whose in / out index leaves the
+ * sub-bases (-1 if none), and the largest connection index */
+typedef struct { const jn_plan_t *p; int64_t *bad_e; uint64_t *kmax; } list_check_t;
+
+static void list_check_item(int64_t l, void *v)
+{
+	const list_check_t *j = (const list_check_t *)v;
+	const jn_list_t *L = &j->p->lists[l];
+	int64_t bad = -1;
+	uint64_t km = 0;
+	for (int64_t e = 0; e < L->len; e++) {
+		const int32_t a = L->triples[3 * e], b = L->triples[3 * e + 1];
+		if (bad < 0 && (a < 0 || a >= L->nin || b < 0 || b >= L->nout)) bad = e;
+		const uint64_t k = (uint32_t)L->triples[3 * e + 2] & 0x7fffffffu;
+		if (k > km) km = k;
+	}
+	j->bad_e[l] = bad;
+	j->kmax[l] = km;
+}
+
 /* The matrix elements some product reads (the compulsory traffic): the
  * entries' matrix indices for single-species instructions, every (k_n, k_p)
  * pair of the two lists for NP ones.  One work item per matrix block, so no
@@ -1419,34 +1439,57 @@ int jn_plan_build(jn_plan_t *p, const char *comb_path, const char *order_path, c
 				ERR("index list %d is used between sub-bases of different sizes", L->id);
 		}
 	}
-	for (int l = 0; l < p->nlists; l++) {
-		jn_list_t *L = &p->lists[l];
-		if (L->nin > 65535 || L->nout > 65535)
-			ERR("index list %d maps sub-bases of %d x %d states: more than the 65535 of the packed device format", L->id,
-			    L->nin, L->nout);
-		for (int64_t e = 0; e < L->len; e++) {
-			int32_t a = L->triples[3 * e], b = L->triples[3 * e + 1];
-			if (a < 0 || a >= L->nin || b < 0 || b >= L->nout)
-				ERR("index list %d entry %lld: in %d / out %d outside the %d x %d sub-bases", L->id, (long long)e, a, b,
-				    L->nin, L->nout);
+	{
+		/* per list, on all host cores: the first entry outside the sub-bases
+		   and the largest connection index (lists are shared by many
+		   instructions, so each is scanned once) */
+		int64_t *bad_e = malloc((p->nlists ? p->nlists : 1) * sizeof(int64_t));
+		uint64_t *kmax = malloc((p->nlists ? p->nlists : 1) * sizeof(uint64_t));
+		if (!bad_e || !kmax) { free(bad_e); free(kmax); ERR("out of host memory"); }
+		list_check_t lc = { p, bad_e, kmax };
+		jn_par_for(p->nlists, list_check_item, &lc);
+		char msg[512] = "";
+		int fail_l = -1;
+		for (int l = 0; l < p->nlists && fail_l < 0; l++) {
+			jn_list_t *L = &p->lists[l];
+			if (L->nin > 65535 || L->nout > 65535) {
+				snprintf(msg, sizeof msg,
+					 "index list %d maps sub-bases of %d x %d states: more than the 65535 of the packed device format",
+					 L->id, L->nin, L->nout);
+				fail_l = l;
+			} else if (bad_e[l] >= 0) {
+				const int64_t e = bad_e[l];
+				snprintf(msg, sizeof msg,
+					 "index list %d entry %lld: in %d / out %d outside the %d x %d sub-bases", L->id, (long long)e,
+					 L->triples[3 * e], L->triples[3 * e + 1], L->nin, L->nout);
+				fail_l = l;
+			}
 		}
-	}
-	for (int i = 0; i < p->ninstr; i++) {
-		jn_instr_t *x = &p->instr[i];
-		jn_me_t *M = &p->mes[x->me];
-		if (x->kind == JN_KIND_NP) {
-			uint64_t kmax_n = 0, kmax_p = 0;
-			jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
-			for (int64_t e = 0; e < Ln->len; e++) { uint64_t k = (uint32_t)Ln->triples[3 * e + 2] & 0x7fffffffu; if (k > kmax_n) kmax_n = k; }
-			for (int64_t e = 0; e < Lp->len; e++) { uint64_t k = (uint32_t)Lp->triples[3 * e + 2] & 0x7fffffffu; if (k > kmax_p) kmax_p = k; }
-			if (Ln->len && Lp->len && (kmax_n >= M->nd_n || kmax_n + M->nd_n * kmax_p >= (uint64_t)M->len))
-				ERR("instruction %d: matrix index outside matrix block %d", i, M->id);
-		} else {
-			jn_list_t *L = &p->lists[x->kind == JN_KIND_N ? x->ln : x->lp];
-			for (int64_t e = 0; e < L->len; e++)
-				if ((int64_t)((uint32_t)L->triples[3 * e + 2] & 0x7fffffffu) >= M->len)
-					ERR("index list %d entry %lld: matrix index outside matrix block %d", L->id, (long long)e, M->id);
+		for (int i = 0; i < p->ninstr && fail_l < 0; i++) {
+			const jn_instr_t *x = &p->instr[i];
+			const jn_me_t *M = &p->mes[x->me];
+			if (x->kind == JN_KIND_NP) {
+				const jn_list_t *Ln = &p->lists[x->ln], *Lp = &p->lists[x->lp];
+				const uint64_t kmax_n = kmax[x->ln], kmax_p = kmax[x->lp];
+				if (Ln->len && Lp->len && (kmax_n >= M->nd_n || kmax_n + M->nd_n * kmax_p >= (uint64_t)M->len)) {
+					snprintf(msg, sizeof msg,
+						 "instruction %d: matrix index outside matrix block %d", i, M->id);
+					fail_l = 0;
+				}
+			} else {
+				const int l = x->kind == JN_KIND_N ? x->ln : x->lp;
+				const jn_list_t *L = &p->lists[l];
+				if (L->len && kmax[l] >= (uint64_t)M->len) {
+					int64_t e = 0;
+					while ((int64_t)((uint32_t)L->triples[3 * e + 2] & 0x7fffffffu) < M->len) e++;
+					snprintf(msg, sizeof msg,
+						 "index list %d entry %lld: matrix index outside matrix block %d", L->id, (long long)e, M->id);
+					fail_l = 0;
+				}
+			}
 		}
+		free(bad_e); free(kmax);
+		if (fail_l >= 0) ERR("%s", msg);
 	}
 
 	/* matrix elements some product actually reads: the compulsory traffic */
