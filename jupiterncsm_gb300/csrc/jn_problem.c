@@ -291,7 +291,8 @@ void jn_par_for(int64_t n, void (*fn)(int64_t, void *), void *arg)
 	const char *cap = getenv("JN_HOST_THREADS");     /* optional cap on the host threads */
 	if (cap && atol(cap) > 0 && atol(cap) < nt) nt = atol(cap);
 	if (nt > 32) nt = 32;
-	if (nt < 1 || n < 2) nt = 1;
+	if (nt > n) nt = (long)n;          /* no idle threads for short loops */
+	if (nt < 1) nt = 1;
 	par_t p = { n, 0, fn, arg };
 	pthread_t th[32];
 	int started = 0;
