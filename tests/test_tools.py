@@ -66,6 +66,29 @@ def test_aurora_skips_three_body_lists_and_missing_files(he4, capfd):
     assert "Could not open file" in capfd.readouterr().err
 
 
+def test_aurora_empty_anicre_list(tmp_path):
+    """An Anicre list with no entries becomes an empty index_list_<id>, as with
+    aurora.x (byte for byte, where the reference tool is built)."""
+    import shutil
+    raw = str(tmp_path / "raw")
+    jn.generate(raw, Z=2, N=2, nmax=2, nbody=3, basis_files=False, anicre_lists=1)
+    d0 = f"{raw}/anicr_lists/n_inds_index_lists"
+    open(f"{d0}/{sorted(os.listdir(d0))[0]}", "wb").close()
+    out = str(tmp_path / "ours")
+    n = jn.aurora(f"{raw}/comb.txt", f"{raw}/anicr_lists", out, 2, 2)
+    assert n == len(list_files(f"{raw}/index_lists"))
+    empty = [f for f in list_files(out) if os.path.getsize(f"{out}/{f}") == 0]
+    assert len(empty) == 1
+    if oracle.reference_tool_available("aurora"):
+        ref = str(tmp_path / "ref")
+        os.makedirs(ref)
+        assert oracle.reference_tool("aurora", f"{raw}/comb.txt", f"{raw}/anicr_lists", ref, 2, 2).returncode == 0
+        assert list_files(ref) == list_files(out)
+        for f in list_files(out):
+            assert filecmp.cmp(f"{out}/{f}", f"{ref}/{f}", shallow=False), f
+    shutil.rmtree(raw)
+
+
 @pytest.mark.parametrize("two_body_only", [False, True])
 def test_mars_writes_the_reference_instruction_set(he4, two_body_only):
     root, raw, _ = he4
