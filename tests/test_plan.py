@@ -316,3 +316,42 @@ def test_wide_neutron_basis_opens_without_block_tiles(tmp_path):
     assert L.emu_walk_validate(h) == 0
     L.emu_close(h)
     assert jn.inspect(d, 0, 4)["dimension"] == D
+
+
+def test_duplicate_list_entries_match_port(problem, tmp_path):
+    """Index lists that hold some triples more than once (the reference adds
+    each copy): every engine's model still matches the oracle, and the walk
+    plan stays sound."""
+    d0, Z, N, *_ = problem("he4_n4_2b")
+    d = corrupt_copy(d0, str(tmp_path / "dup"))
+    names = sorted(os.listdir(f"{d}/index_lists"), key=lambda s: int(s.split("_")[-1]))
+    rng = np.random.default_rng(0)
+    for n in names[::7]:
+        f = f"{d}/index_lists/{n}"
+        a = np.fromfile(f, dtype=np.int32).reshape(-1, 3)
+        if len(a):
+            pick = a[rng.integers(0, len(a), size=max(1, len(a) // 3))]
+            np.concatenate([a, pick, a[:1]]).astype(np.int32).tofile(f)
+    L, h, err = open_plan(d, Z, N)
+    assert h, err
+    D = L.emu_dimension(h)
+    x = np.random.default_rng(1).standard_normal(D)
+    port = oracle.Port(d)
+    want = port.matvec(x)
+    port.close()
+    scale = np.abs(want).max()
+    y = np.zeros(D)
+    L.emu_matvec(h, x.ctypes.data, y.ctypes.data, 0)
+    assert np.abs(y - want).max() <= 1e-12 * scale
+    for fn, modes in (("emu_matvec3", ((0, 1e-12), (1, 2e-6))), ("emu_matvec4", ((0, 1e-12), (1, 2e-6))),
+                      ("emu_matvec5", ((1, 1e-12), (64, 1e-12), (32, 2e-6)))):
+        f = getattr(L, fn)
+        f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 2
+        for mode, tol in modes:
+            y = np.zeros(D)
+            assert f(h, x.ctypes.data, y.ctypes.data, 0, mode) == 0, (fn, mode)
+            assert np.abs(y - want).max() <= tol * scale, (fn, mode)
+    L.emu_walk_validate.restype = ctypes.c_int64
+    L.emu_walk_validate.argtypes = [ctypes.c_void_p]
+    assert L.emu_walk_validate(h) == 0
+    L.emu_close(h)
