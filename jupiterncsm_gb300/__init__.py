@@ -263,7 +263,9 @@ class Hamiltonian:
             pass
 
     def matvec(self, x, y=None):
-        """y += H x on host arrays (y = H x when y is None)."""
+        """y += H x on host arrays (y = H x when y is None).  Raises JnError for an x outside
+        the fixed-point products' range (max|x| >= 2^127, or the row-sum bound times max|x|
+        outside [2^-47, 2^121)); engine 2 at precision 64 takes any x."""
         x = np.ascontiguousarray(x, dtype=np.float64)
         if x.shape != (self.dimension,):
             raise ValueError("x has the wrong dimension")
